@@ -1,0 +1,157 @@
+/* C ABI of the GB300 block-AMR hot path (parthenon_gb300).
+ *
+ * One process, one GPU. Device arrays are plain pointers to device memory laid out
+ * per block as [block][component][k][j][i] (cells with ghosts, FP64); coarse buffers
+ * use the same layout with the coarse block size. Every call is stream-ordered on the
+ * stream passed in (a cudaStream_t, or NULL for the legacy default stream) and does no
+ * host synchronisation, so sequences of calls can be captured into a CUDA graph.
+ *
+ * Every function returns an int status: 0 success, < 0 failure (see PGB_ERR_*), and
+ * never throws across the ABI; pgb_last_error() gives the message of the last failure
+ * on the calling thread.
+ *
+ * Each entry point names the reference interface it replaces
+ * (parthenon-hpc-lab/parthenon, file:line).
+ */
+#ifndef PARTHENON_GB300_H_
+#define PARTHENON_GB300_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGB_OK 0
+#define PGB_ERR_INVALID (-1)
+#define PGB_ERR_CUDA (-2)
+#define PGB_ERR_UNSUPPORTED (-3)
+#define PGB_ERR_STATE (-4)
+
+/* exchange flags */
+#define PGB_EXCHANGE_PROLONGATE 1   /* run ProlongateBounds after SetBounds          */
+#define PGB_PROLONG_MINMOD 0        /* ProlongateSharedMinMod (default CC op)        */
+#define PGB_PROLONG_LINEAR 2        /* ProlongateSharedLinear      (flags bits 1-2)  */
+#define PGB_PROLONG_CONSTANT 4      /* ProlongatePiecewiseConstant                   */
+
+typedef struct pgb_mesh pgb_mesh;
+
+/* Root mesh and block shape; every direction periodic (the only boundary the hot
+ * path supports). Mirrors <parthenon/mesh> nx1..3, x?min/x?max, nghost and
+ * <parthenon/meshblock> nx1..3. */
+typedef struct {
+  int32_t nx[3];
+  int32_t block_nx[3];
+  int32_t nghost;
+  double xmin[3];
+  double xmax[3];
+} pgb_mesh_spec;
+
+typedef struct {
+  int32_t nblocks;
+  int32_t multilevel;
+  int32_t root_level;
+  int32_t max_level;
+  int32_t N[3];        /* block array extents with ghosts */
+  int32_t Nc[3];       /* coarse buffer extents with ghosts */
+  int32_t npairs;      /* boundary sender/receiver pairs (index maps) */
+  int64_t buffer_elems;/* packed buffer length per component (reference layout) */
+  int32_t nflux_corr;  /* fine/coarse faces with flux correction */
+} pgb_mesh_info;
+
+/* Stage parameters. physics: 0 advection (constant velocity), 1 Burgers.
+ * recon: advection 0 donor cell / 1 PLM; Burgers 0 WENO5 / 1 MC-linear.
+ * exact: 1 = separately rounded arithmetic in the reference's order (bitwise path),
+ *        0 = FMA-contracted kernels with shared reciprocals (within 1e-12 relative). */
+typedef struct {
+  int32_t physics;
+  int32_t recon;
+  int32_t exact;
+  int32_t pad;
+  double vel[3];
+  double cfl;
+} pgb_stage_params;
+
+const char *pgb_last_error(void);
+int pgb_version(void);
+
+/* Mesh topology from leaf logical locations (level, lx1, lx2, lx3 per leaf; nleaves
+ * == 0 gives the uniform root grid). Host only: builds gids, neighbours, ownership
+ * and every boundary index range.
+ * Replaces Mesh::Mesh/BuildBlockList (src/mesh/mesh.cpp:311-370), Forest::HyperRectangular
+ * (src/mesh/forest/forest.cpp:64-195), SetMeshBlockNeighbors (src/mesh/mesh-gmg.cpp:48-101)
+ * and the BndInfo/ProResInfo construction (src/bvals/comms/bnd_info.cpp:105-448). */
+int pgb_mesh_create(const pgb_mesh_spec *spec, int32_t nleaves, const int64_t *leaves, pgb_mesh **out);
+int pgb_mesh_destroy(pgb_mesh *mesh);
+int pgb_mesh_get_info(const pgb_mesh *mesh, pgb_mesh_info *info);
+/* locs: nblocks x (level, lx1, lx2, lx3); geom: nblocks x (xmin[3], dx[3]) */
+int pgb_mesh_block_info(const pgb_mesh *mesh, int64_t *locs, double *geom);
+/* Buffer index maps, 23 int32 per pair: sender gid, receiver gid, sender-side slot,
+ * send box (is,ie,js,je,ks,ke), send-from-coarse flag, receive box (6), receive-into-
+ * coarse flag, 27-bit receive mask, values per component, 4 reserved.
+ * Replaces the BndInfo index ranges (src/bvals/comms/bnd_info.cpp:273-340). */
+int pgb_mesh_boundaries(const pgb_mesh *mesh, int32_t *out, int32_t capacity);
+
+/* Lower the topology to device tables (needs a GPU); call once per mesh/remesh.
+ * Replaces RebuildBufferCache (src/bvals/comms/bvals_utils.hpp:212-245). */
+int pgb_mesh_upload(pgb_mesh *mesh);
+
+/* Full same-rank ghost exchange of a cell-centred field: send-side restriction,
+ * boundary copies, receive-side restriction, optional prolongation.
+ * buffer == NULL: direct sender->receiver copies; otherwise buffer (>= buffer_elems *
+ * ncomp doubles) is packed and unpacked in the reference layout.
+ * Replaces SendBoundBufs / ReceiveBoundBufs / SetBounds / ProlongateBounds<any>
+ * (src/bvals/comms/boundary_communication.cpp:48-393) and AddBoundaryExchangeTasks
+ * (boundary_communication.cpp:405-445). */
+int pgb_exchange(pgb_mesh *mesh, double *data, double *coarse, int32_t ncomp, int32_t flags, double *buffer,
+                 void *stream);
+
+/* Pack every boundary into `buffer` in the reference's buffer layout (parity checks).
+ * Replaces the pack kernel of SendBoundBufs (boundary_communication.cpp:95-140). */
+int pgb_pack_buffers(pgb_mesh *mesh, const double *data, const double *coarse, int32_t ncomp, double *buffer,
+                     void *stream);
+
+/* Flux correction at fine/coarse faces on flux arrays [block][dir][comp][N3][N2][N1].
+ * Replaces AddFluxCorrectionTasks (boundary_communication.cpp:454-461). */
+int pgb_flux_correct(pgb_mesh *mesh, double *flux, int32_t ncomp, void *stream);
+
+/* One RK stage: fluxes from u_in, flux divergence, u_out = (w_in u_in + w_base u_base)
+ * + beta * dt * dudt on the interior. dt is a device scalar. Uniform meshes use the
+ * fused path (dudt is scratch of the field's size); multilevel meshes store fluxes in
+ * `flux` (3x the field's size), correct them at fine/coarse faces and then update.
+ * Replaces CalculateFluxes (benchmarks/burgers/burgers_package.cpp:202-404,
+ * example/advection/advection_package.cpp:499-647), FluxDivergence
+ * (src/interface/update.cpp:62-85), AverageIndependentData and UpdateIndependentData
+ * (src/interface/update.hpp:121-136). */
+int pgb_stage(pgb_mesh *mesh, const pgb_stage_params *p, const double *u_in, const double *u_base, double *u_out,
+              double *dudt, double *flux, const double *dt, double w_in, double w_base, double beta, int32_t ncomp,
+              void *stream);
+
+/* dt <- SetGlobalTimeStep(cfl * EstimateTimestep(u)) on the device (first != 0: the
+ * initial step). Replaces EstimateTimestep (src/interface/update.hpp:268-278) and
+ * EvolutionDriver::SetGlobalTimeStep (src/driver/driver.cpp:210-232). */
+int pgb_estimate_dt(pgb_mesh *mesh, const pgb_stage_params *p, const double *u, int32_t ncomp, double *dt,
+                    int32_t first, void *stream);
+
+/* ncycles RK2 cycles (two stages with a ghost exchange after each, then the dt update)
+ * on device arrays. base/stage: fields; dudt: scratch of the field's size; flux:
+ * 3x field size (multilevel only, else may be NULL); coarse_*: coarse buffers
+ * (multilevel only). use_graph != 0 captures one cycle in a CUDA graph and replays it.
+ * Replaces MultiStageDriverGeneric::Step (src/driver/multistage.hpp:39-53) with the
+ * advection/Burgers task collections (example/advection/advection_driver.cpp:56-164,
+ * benchmarks/burgers/burgers_driver.cpp:53-148). */
+int pgb_rk2_cycles(pgb_mesh *mesh, const pgb_stage_params *p, double *base, double *stage, double *dudt, double *flux,
+                   double *coarse_base, double *coarse_stage, int32_t ncomp, double *dt, int32_t ncycles,
+                   int32_t use_graph, void *stream);
+
+/* Host-buffer entry point: copies host_in (interior+ghosts, the field layout) to the
+ * device, exchanges ghosts, runs ncycles RK2 cycles and copies the result back.
+ * *dt_inout: in, the current dt (<= 0: estimate the initial dt); out, the next dt. */
+int pgb_run_host(pgb_mesh *mesh, const pgb_stage_params *p, const double *host_in, double *host_out, int32_t ncomp,
+                 int32_t ncycles, double *dt_inout);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARTHENON_GB300_H_ */

@@ -1,0 +1,885 @@
+// Oracle: CPU restatement of Parthenon's block-AMR hot path (test infrastructure).
+//
+// Only tests, the smoke check and the CPU-baseline leg of the benchmark load this
+// library, and only as the checker: the product never links or calls it. Every
+// routine restates the reference algorithm operation for operation (compiled with
+// -ffp-contract=off so that no fused multiply-add changes the rounding), keeping the
+// reference's own data flow (pack into a buffer, unpack from it) rather than the
+// product's direct copies.
+//
+// Reference files followed (paths inside parthenon-hpc-lab/parthenon):
+//   src/bvals/comms/boundary_communication.cpp:48-159   SendBoundBufs (restrict, pack)
+//   src/bvals/comms/boundary_communication.cpp:250-348  SetBounds (unpack, restrict)
+//   src/bvals/comms/boundary_communication.cpp:360-393  ProlongateBounds
+//   src/bvals/comms/bnd_info.cpp:273-448                BndInfo / ProResInfo ranges
+//   src/bvals/comms/bvals_utils.hpp:43-66               Send/Receive keys
+//   src/prolong_restrict/pr_ops.hpp:78-285               RestrictAverage, ProlongateShared*
+//   src/interface/update.hpp:42-136, update.cpp:62-85   FluxDivergence, weighted sums
+//   src/time_integration/low_storage_integrator.cpp:67-86  RK2 weights
+//   src/driver/driver.cpp:210-270                       SetGlobalTimeStep
+//   example/advection/advection_package.cpp:465-647      advection dt and fluxes
+//   src/reconstruct/dc_inline.hpp, plm_inline.hpp        donor cell and PLM
+//   benchmarks/burgers/burgers_package.cpp:170-404      Burgers dt and fluxes
+//   benchmarks/burgers/burgers_package.hpp:32-43        HLL
+//   benchmarks/burgers/recon.hpp:27-99                  WENO5Z, MC-linear
+//   src/amr_criteria/refinement_package.cpp:93-120      first-derivative tagging
+//   src/solvers/mg_solver.hpp, solver_utils.hpp, example/poisson_gmg/poisson_equation.hpp
+#include <omp.h>
+
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+
+#include "mesh.hpp"
+
+namespace oracle {
+
+using std::int64_t;
+
+// ---------------------------------------------------------------- fields
+struct Field {
+  const Mesh *mesh = nullptr;
+  const std::vector<Block> *blocks = nullptr;
+  int ncomp = 1;
+  int N[3], Nc[3];
+  std::vector<double> data, coarse;
+  int64_t bstride() const { return (int64_t)ncomp * N[0] * N[1] * N[2]; }
+  int64_t cstride() const { return (int64_t)ncomp * Nc[0] * Nc[1] * Nc[2]; }
+  double &at(int b, int v, int k, int j, int i) {
+    return data[b * bstride() + (((int64_t)v * N[2] + k) * N[1] + j) * N[0] + i];
+  }
+  double &cat(int b, int v, int k, int j, int i) {
+    return coarse[b * cstride() + (((int64_t)v * Nc[2] + k) * Nc[1] + j) * Nc[0] + i];
+  }
+  double &any(bool c, int b, int v, int k, int j, int i) {
+    return c ? cat(b, v, k, j, i) : at(b, v, k, j, i);
+  }
+  void init(const Mesh *m, const std::vector<Block> *bl, int nc) {
+    mesh = m;
+    blocks = bl;
+    ncomp = nc;
+    const Block &b0 = (*bl)[0];
+    for (int d = 0; d < 3; ++d) {
+      N[d] = b0.nx[d] + 2 * m->p.ng;
+      Nc[d] = std::max(1, b0.nx[d] / 2) + 2 * m->p.ng;
+    }
+    data.assign(bl->size() * bstride(), 0.0);
+    coarse.assign(bl->size() * cstride(), 0.0);
+  }
+};
+
+// ---------------------------------------------------------------- boundary records
+struct BndRec {
+  int sender, receiver, locidx;
+  Box send;
+  bool send_coarse;
+  Box recv;
+  bool recv_coarse;
+};
+
+// ForEachBoundary (loop_utils.hpp:79-168) over receivers, matched to the sender's
+// neighbour entry through the Send/Receive keys (bvals_utils.hpp:43-66).
+enum BType { BAny = 0, BGmgSame = 1 };
+
+inline std::vector<NeighborBlock> *nb_list(Block &b, BType t, int lev) {
+  if (t == BAny) return &b.neighbors;
+  return b.loc.level == lev ? &b.gmg_same : &b.gmg_composite_finer;
+}
+
+inline std::vector<BndRec> build_boundaries(const Mesh &m, std::vector<Block> &bl, BType t,
+                                            int lev) {
+  std::map<int, int> idx_of;
+  for (size_t i = 0; i < bl.size(); ++i) idx_of[bl[i].gid] = (int)i;
+  std::vector<BndRec> out;
+  for (auto &rb : bl) {
+    for (auto &nb : *nb_list(rb, t, lev)) {
+      if (nb.gid == rb.gid && nb.is_cell()) continue;  // same_to_same
+      auto it = idx_of.find(nb.gid);
+      if (it == idx_of.end()) throw std::runtime_error("sender not in block list");
+      Block &sb = bl[it->second];
+      const NeighborBlock *snb = nullptr;
+      for (auto &n2 : *nb_list(sb, t, lev))
+        if (n2.gid == rb.gid && n2.idx() == nb.reverse_idx()) snb = &n2;
+      if (!snb) throw std::runtime_error("no matching send buffer");
+      BndRec r;
+      r.sender = it->second;
+      r.receiver = (int)(&rb - &bl[0]);
+      r.locidx = snb->idx();
+      r.send = calc_indices(*snb, sb.loc, sb.nx, m.p.ng, CC,
+                            snb->is_cell() ? InteriorSend : BoundaryInteriorSend, false, false);
+      r.send_coarse = snb->origin.level < sb.loc.level;
+      r.recv = calc_indices(nb, rb.loc, rb.nx, m.p.ng, CC,
+                            nb.is_cell() ? InteriorRecv : BoundaryExteriorRecv, false, false);
+      r.recv_coarse = nb.origin.level < rb.loc.level;
+      if (r.send.size() != r.recv.size()) throw std::runtime_error("buffer size mismatch");
+      out.push_back(r);
+    }
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------- restrict / prolong
+// pr_ops.hpp:105-164 (CC, 3D). (ck,cj,ci) coarse; fine index = (c - cs)*2 + fs.
+inline void restrict_cell(Field &f, int b, int v, int ck, int cj, int ci, const Coords &fc) {
+  const int ng = f.mesh->p.ng;
+  const int i = (ci - ng) * 2 + ng, j = (cj - ng) * 2 + ng, k = (ck - ng) * 2 + ng;
+  double vol[2][2][2], t[2][2][2];
+  for (int ok = 0; ok < 2; ++ok)
+    for (int oj = 0; oj < 2; ++oj)
+      for (int oi = 0; oi < 2; ++oi) {
+        vol[ok][oj][oi] = fc.vol;
+        t[ok][oj][oi] = vol[ok][oj][oi] * f.at(b, v, k + ok, j + oj, i + oi);
+      }
+  const double tv = ((vol[0][0][0] + vol[0][1][0]) + (vol[0][0][1] + vol[0][1][1])) +
+                    ((vol[1][0][0] + vol[1][1][0]) + (vol[1][0][1] + vol[1][1][1]));
+  f.cat(b, v, ck, cj, ci) =
+      (((t[0][0][0] + t[0][1][0]) + (t[0][0][1] + t[0][1][1])) +
+       ((t[1][0][0] + t[1][1][0]) + (t[1][0][1] + t[1][1][1]))) /
+      tv;
+}
+
+inline double sgn1(double x) { return x < 0.0 ? -1.0 : 1.0; }
+// pr_ops.hpp:97-103
+inline double grad_minmod(double fc, double fm, double fp, double dxm, double dxp, double &gm,
+                          double &gp) {
+  gm = (fc - fm) / dxm;
+  gp = (fp - fc) / dxp;
+  return 0.5 * (sgn1(gm) + sgn1(gp)) * std::min(std::fabs(gm), std::fabs(gp));
+}
+
+enum ProlongOp { PMinMod = 0, PLinear = 1, PConstant = 2 };
+
+// pr_ops.hpp:166-285 (CC, 3D)
+inline void prolong_cell(Field &f, int b, int v, int k, int j, int i, const Coords &fco,
+                         const Coords &cco, int op) {
+  const int ng = f.mesh->p.ng;
+  const int fi = (i - ng) * 2 + ng, fj = (j - ng) * 2 + ng, fk = (k - ng) * 2 + ng;
+  const double fc = f.cat(b, v, k, j, i);
+  double gm[3], gp[3], dfm[3], dfp[3];
+  const int c[3] = {i, j, k};
+  const int fidx[3] = {fi, fj, fk};
+  for (int d = 0; d < 3; ++d) {
+    const double xm = cco.xc(d, c[d] - 1), xc = cco.xc(d, c[d]), xp = cco.xc(d, c[d] + 1);
+    const double dxm = xc - xm, dxp = xp - xc;
+    const double fxm = fco.xc(d, fidx[d]), fxp = fco.xc(d, fidx[d] + 1);
+    dfm[d] = xc - fxm;
+    dfp[d] = fxp - xc;
+    double nm, np;
+    if (d == 0) {
+      nm = f.cat(b, v, k, j, i - 1);
+      np = f.cat(b, v, k, j, i + 1);
+    } else if (d == 1) {
+      nm = f.cat(b, v, k, j - 1, i);
+      np = f.cat(b, v, k, j + 1, i);
+    } else {
+      nm = f.cat(b, v, k - 1, j, i);
+      np = f.cat(b, v, k + 1, j, i);
+    }
+    const double g = grad_minmod(fc, nm, np, dxm, dxp, gm[d], gp[d]);
+    if (op == PMinMod) gm[d] = gp[d] = g;
+    if (op == PConstant) gm[d] = gp[d] = 0.0;
+  }
+  f.at(b, v, fk, fj, fi) = fc - (gm[0] * dfm[0] + gm[1] * dfm[1] + gm[2] * dfm[2]);
+  f.at(b, v, fk, fj, fi + 1) = fc + (gp[0] * dfp[0] - gm[1] * dfm[1] - gm[2] * dfm[2]);
+  f.at(b, v, fk, fj + 1, fi) = fc - (gm[0] * dfm[0] - gp[1] * dfp[1] + gm[2] * dfm[2]);
+  f.at(b, v, fk, fj + 1, fi + 1) = fc + (gp[0] * dfp[0] + gp[1] * dfp[1] - gm[2] * dfm[2]);
+  f.at(b, v, fk + 1, fj, fi) = fc - (gm[0] * dfm[0] + gm[1] * dfm[1] - gp[2] * dfp[2]);
+  f.at(b, v, fk + 1, fj, fi + 1) = fc + (gp[0] * dfp[0] - gm[1] * dfm[1] + gp[2] * dfp[2]);
+  f.at(b, v, fk + 1, fj + 1, fi) = fc - (gm[0] * dfm[0] - gp[1] * dfp[1] - gp[2] * dfp[2]);
+  f.at(b, v, fk + 1, fj + 1, fi + 1) = fc + (gp[0] * dfp[0] + gp[1] * dfp[1] + gp[2] * dfp[2]);
+}
+
+template <class F>
+inline void for_box(const Box &bx, F fn) {
+  for (int k = bx.s[2]; k <= bx.e[2]; ++k)
+    for (int j = bx.s[1]; j <= bx.e[1]; ++j)
+      for (int i = bx.s[0]; i <= bx.e[0]; ++i) fn(k, j, i);
+}
+
+// ---------------------------------------------------------------- exchange
+struct ExchangeStats {
+  int64_t buffered_values = 0;
+  int64_t overlaps = 0;
+};
+
+// One full same-rank exchange: SendBoundBufs -> ReceiveBoundBufs -> SetBounds
+// [-> ProlongateBounds], with an explicit intermediate buffer per boundary.
+inline ExchangeStats exchange(Field &f, std::vector<Block> &bl, BType t, int lev,
+                              const std::vector<BndRec> &recs, bool prolongate, int pop,
+                              bool multilevel, bool check_overlaps = false) {
+  ExchangeStats st;
+  const Mesh &m = *f.mesh;
+  const int ng = m.p.ng;
+  // (1) send-side restriction into coarse buffers (ProResInfo::GetSend)
+  if (multilevel) {
+    for (size_t b = 0; b < bl.size(); ++b) {
+      for (auto &nb : *nb_list(bl[b], t, lev)) {
+        if (!(nb.origin.level < bl[b].loc.level)) continue;
+        Box bx = calc_indices(nb, bl[b].loc, bl[b].nx, ng, CC, BoundaryInteriorSend, true, false);
+        for (int v = 0; v < f.ncomp; ++v)
+          for_box(bx, [&](int k, int j, int i) { restrict_cell(f, (int)b, v, k, j, i, bl[b].coords); });
+      }
+    }
+  }
+  // (2) pack
+  std::vector<std::vector<double>> bufs(recs.size());
+  const int nrec = (int)recs.size();
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int r = 0; r < nrec; ++r) {
+    const BndRec &br = recs[r];
+    auto &buf = bufs[r];
+    buf.reserve(br.send.size() * f.ncomp);
+    for (int v = 0; v < f.ncomp; ++v)
+      for_box(br.send, [&](int k, int j, int i) {
+        buf.push_back(f.any(br.send_coarse, br.sender, v, k, j, i));
+      });
+  }
+  for (auto &b : bufs) st.buffered_values += (int64_t)b.size();
+  // (3) unpack (masked); active writes of different boundaries never overlap, which
+  // the overlap check verifies
+  if (check_overlaps) {
+    std::vector<std::vector<uint8_t>> written(bl.size());
+    for (size_t b = 0; b < bl.size(); ++b) written[b].assign(f.bstride() + f.cstride(), 0);
+    for (int r = 0; r < nrec; ++r) {
+      const BndRec &br = recs[r];
+      size_t m_ = 0;
+      for (int v = 0; v < f.ncomp; ++v)
+        for_box(br.recv, [&](int k, int j, int i) {
+          const double val = bufs[r][m_++];
+          if (br.recv.active(k, j, i)) {
+            double *p = &f.any(br.recv_coarse, br.receiver, v, k, j, i);
+            int64_t off = br.recv_coarse
+                              ? f.bstride() + (p - &f.coarse[br.receiver * f.cstride()])
+                              : (p - &f.data[br.receiver * f.bstride()]);
+            if (written[br.receiver][off]) ++st.overlaps;
+            written[br.receiver][off] = 1;
+            *p = val;
+          }
+        });
+    }
+  } else {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int r = 0; r < nrec; ++r) {
+      const BndRec &br = recs[r];
+      size_t m_ = 0;
+      for (int v = 0; v < f.ncomp; ++v)
+        for_box(br.recv, [&](int k, int j, int i) {
+          const double val = bufs[r][m_++];
+          if (br.recv.active(k, j, i)) f.any(br.recv_coarse, br.receiver, v, k, j, i) = val;
+        });
+    }
+  }
+  // (4) receive-side restriction of fine ghosts into coarse ghosts (ProResInfo::GetSet)
+  if (multilevel) {
+    for (size_t b = 0; b < bl.size(); ++b) {
+      const int my = bl[b].loc.level;
+      bool restricted = false;
+      if (my > 0)
+        for (auto &nb : *nb_list(bl[b], t, lev)) restricted = restricted || (nb.origin.level == my - 1);
+      if (!restricted) continue;
+      for (auto &nb : *nb_list(bl[b], t, lev)) {
+        if (nb.origin.level < my) continue;
+        Box bx = calc_indices(nb, bl[b].loc, bl[b].nx, ng, CC, BoundaryExteriorRecv, true, false);
+        for (int v = 0; v < f.ncomp; ++v)
+          for_box(bx, [&](int k, int j, int i) {
+            if (bx.active(k, j, i)) restrict_cell(f, (int)b, v, k, j, i, bl[b].coords);
+          });
+      }
+    }
+  }
+  // (5) prolongation from coarse buffers (ProlongateShared; ProlongateInternal is a
+  // no-op for cell-centred fields since IsSubmanifold(CC, cel) is false)
+  if (multilevel && prolongate) {
+    for (size_t b = 0; b < bl.size(); ++b) {
+      for (auto &nb : *nb_list(bl[b], t, lev)) {
+        if (!(nb.origin.level < bl[b].loc.level)) continue;
+        Box bx = calc_indices(nb, bl[b].loc, bl[b].nx, ng, CC, BoundaryExteriorRecv, true, false);
+        for (int v = 0; v < f.ncomp; ++v)
+          for_box(bx, [&](int k, int j, int i) {
+            if (bx.active(k, j, i))
+              prolong_cell(f, (int)b, v, k, j, i, bl[b].coords, bl[b].ccoords, pop);
+          });
+      }
+    }
+  }
+  return st;
+}
+
+// ---------------------------------------------------------------- flux correction
+// Flux arrays per block: [3][ncomp][N3][N2][N1] (cell-memory-aligned face fields),
+// coarse flux arrays [3][ncomp][Nc3][Nc2][Nc1].
+struct FluxField {
+  int ncomp = 0;
+  int N[3], Nc[3];
+  std::vector<double> f, fc;
+  int64_t bs() const { return 3ll * ncomp * N[0] * N[1] * N[2]; }
+  int64_t cbs() const { return 3ll * ncomp * Nc[0] * Nc[1] * Nc[2]; }
+  double &at(int b, int dir, int v, int k, int j, int i) {
+    return f[b * bs() + ((((int64_t)dir * ncomp + v) * N[2] + k) * N[1] + j) * N[0] + i];
+  }
+  double &cat(int b, int dir, int v, int k, int j, int i) {
+    return fc[b * cbs() + ((((int64_t)dir * ncomp + v) * Nc[2] + k) * Nc[1] + j) * Nc[0] + i];
+  }
+  void init(const Field &u) {
+    ncomp = u.ncomp;
+    for (int d = 0; d < 3; ++d) {
+      N[d] = u.N[d];
+      Nc[d] = u.Nc[d];
+    }
+    f.assign(u.blocks->size() * bs(), 0.0);
+    fc.assign(u.blocks->size() * cbs(), 0.0);
+  }
+};
+
+// SendBoundBufs<flxcor_send> / SetBounds<flxcor_recv>: restrict F on the fine side of a
+// fine/coarse face (RestrictAverage on the face element, area weights), pack from the
+// coarse flux buffer and overwrite the coarse block's face flux.
+inline void flux_correction(FluxField &F, const Mesh &m, std::vector<Block> &bl) {
+  const int ng = m.p.ng;
+  std::map<int, int> idx_of;
+  for (size_t i = 0; i < bl.size(); ++i) idx_of[bl[i].gid] = (int)i;
+  for (size_t fb = 0; fb < bl.size(); ++fb) {
+    Block &fine = bl[fb];
+    for (auto &nb : fine.neighbors) {
+      if (nb.loc.level != fine.loc.level - 1) continue;
+      int nface = std::abs(nb.off[0]) + std::abs(nb.off[1]) + std::abs(nb.off[2]);
+      if (nface != 1) continue;
+      const int dir = nb.off[0] ? 0 : (nb.off[1] ? 1 : 2);
+      const int el = F1 + dir;
+      // restriction of the face fluxes into the coarse flux buffer
+      Box rb = calc_indices(nb, fine.loc, fine.nx, ng, el, BoundaryInteriorSend, true, true);
+      for (int v = 0; v < F.ncomp; ++v)
+        for_box(rb, [&](int ck, int cj, int ci) {
+          const int i = (ci - ng) * 2 + ng, j = (cj - ng) * 2 + ng, k = (ck - ng) * 2 + ng;
+          const int inc[3] = {dir != 0, dir != 1, dir != 2};
+          double vol[2][2][2] = {}, t[2][2][2] = {};
+          const double a = fine.coords.area[dir];
+          for (int ok = 0; ok < 1 + inc[2]; ++ok)
+            for (int oj = 0; oj < 1 + inc[1]; ++oj)
+              for (int oi = 0; oi < 1 + inc[0]; ++oi) {
+                vol[ok][oj][oi] = a;
+                t[ok][oj][oi] = a * F.at((int)fb, dir, v, k + ok, j + oj, i + oi);
+              }
+          const double tv = ((vol[0][0][0] + vol[0][1][0]) + (vol[0][0][1] + vol[0][1][1])) +
+                            ((vol[1][0][0] + vol[1][1][0]) + (vol[1][0][1] + vol[1][1][1]));
+          F.cat((int)fb, dir, v, ck, cj, ci) =
+              (((t[0][0][0] + t[0][1][0]) + (t[0][0][1] + t[0][1][1])) +
+               ((t[1][0][0] + t[1][1][0]) + (t[1][0][1] + t[1][1][1]))) /
+              tv;
+        });
+      // pack (send box in coarse index space) and set on the coarse block
+      Box sb = calc_indices(nb, fine.loc, fine.nx, ng, el, BoundaryInteriorSend, false, true);
+      std::vector<double> buf;
+      for (int v = 0; v < F.ncomp; ++v)
+        for_box(sb, [&](int k, int j, int i) { buf.push_back(F.cat((int)fb, dir, v, k, j, i)); });
+      const int cb = idx_of.at(nb.gid);
+      Block &coarse = bl[cb];
+      const NeighborBlock *cnb = nullptr;
+      for (auto &n2 : coarse.neighbors)
+        if (n2.gid == fine.gid && n2.idx() == nb.reverse_idx()) cnb = &n2;
+      if (!cnb) throw std::runtime_error("flux correction: no reverse neighbour");
+      Box stb = calc_indices(*cnb, coarse.loc, coarse.nx, ng, el, BoundaryExteriorRecv, false, true);
+      if (stb.size() * F.ncomp != (int64_t)buf.size()) throw std::runtime_error("flux buffer size");
+      size_t mm = 0;
+      for (int v = 0; v < F.ncomp; ++v)
+        for_box(stb, [&](int k, int j, int i) {
+          const double val = buf[mm++];
+          if (stb.active(k, j, i)) F.at(cb, dir, v, k, j, i) = 1.0 * val;
+        });
+    }
+  }
+}
+
+// ---------------------------------------------------------------- update helpers
+// update.hpp:42-56 (ndim = 3)
+inline double flux_div(FluxField &F, const Coords &c, int b, int l, int k, int j, int i) {
+  double du = (c.area[0] * F.at(b, 0, l, k, j, i + 1) - c.area[0] * F.at(b, 0, l, k, j, i));
+  du += (c.area[1] * F.at(b, 1, l, k, j + 1, i) - c.area[1] * F.at(b, 1, l, k, j, i));
+  du += (c.area[2] * F.at(b, 2, l, k + 1, j, i) - c.area[2] * F.at(b, 2, l, k, j, i));
+  return -du / c.vol;
+}
+
+// ---------------------------------------------------------------- WENO5 / HLL
+constexpr double kEps = 10 * DBL_EPSILON;  // robust.hpp:37-40
+
+// recon.hpp:27-33
+inline double mc_lim(double dm, double dp) {
+  const double dc = (dm * dp > 0.0) * 0.5 * (dm + dp);
+  return std::copysign(std::min(std::fabs(dc), 2.0 * std::min(std::fabs(dm), std::fabs(dp))), dc);
+}
+// recon.hpp:35-40
+inline void linear_recon(double qm, double q0, double qp, double &ql, double &qr) {
+  double dq = qp - q0;
+  dq = 0.5 * mc_lim(q0 - qm, dq);
+  ql = q0 + dq;
+  qr = q0 - dq;
+}
+// recon.hpp:42-99
+inline void weno5z(double q0, double q1, double q2, double q3, double q4, double &ql, double &qr) {
+  const double a5[3][3] = {{1.0 / 3.0, -7.0 / 6.0, 11.0 / 6.0},
+                           {-1.0 / 6.0, 5.0 / 6.0, 1.0 / 3.0},
+                           {1.0 / 3.0, 5.0 / 6.0, -1.0 / 6.0}};
+  const double g5[3] = {0.1, 0.6, 0.3};
+  const double tt = 13.0 / 3.0;
+  double a = q0 - 2 * q1 + q2;
+  double b = q0 - 4.0 * q1 + 3.0 * q2;
+  double be0 = tt * a * a + b * b + kEps;
+  a = q1 - 2.0 * q2 + q3;
+  b = q3 - q1;
+  double be1 = tt * a * a + b * b + kEps;
+  a = q2 - 2.0 * q3 + q4;
+  b = q4 - 4.0 * q3 + 3.0 * q2;
+  double be2 = tt * a * a + b * b + kEps;
+  const double tau5 = std::fabs(be2 - be0);
+  be0 = (be0 + tau5) / be0;
+  be1 = (be1 + tau5) / be1;
+  be2 = (be2 + tau5) / be2;
+  double w0 = g5[0] * be0 + kEps;
+  double w1 = g5[1] * be1 + kEps;
+  double w2 = g5[2] * be2 + kEps;
+  double ws = 1.0 / (w0 + w1 + w2);
+  ql = w0 * (a5[0][0] * q0 + a5[0][1] * q1 + a5[0][2] * q2);
+  ql += w1 * (a5[1][0] * q1 + a5[1][1] * q2 + a5[1][2] * q3);
+  ql += w2 * (a5[2][0] * q2 + a5[2][1] * q3 + a5[2][2] * q4);
+  ql *= ws;
+  const double al = 3.0 * ws * w0 * w1 * w2 / (g5[2] * w0 * w1 + g5[1] * w0 * w2 + g5[0] * w1 * w2) + kEps;
+  w0 = g5[0] * be2 + kEps;
+  w1 = g5[1] * be1 + kEps;
+  w2 = g5[2] * be0 + kEps;
+  ws = 1.0 / (w0 + w1 + w2);
+  qr = w0 * (a5[0][0] * q4 + a5[0][1] * q3 + a5[0][2] * q2);
+  qr += w1 * (a5[1][0] * q3 + a5[1][1] * q2 + a5[1][2] * q1);
+  qr += w2 * (a5[2][0] * q2 + a5[2][1] * q1 + a5[2][2] * q0);
+  qr *= ws;
+  const double ar = 3.0 * ws * w0 * w1 * w2 / (g5[2] * w0 * w1 + g5[1] * w0 * w2 + g5[0] * w1 * w2) + kEps;
+  double dq = q3 - q2;
+  dq = 0.5 * mc_lim(q2 - q1, dq);
+  const double alin = 2.0 * al * ar / (al + ar);
+  ql = alin * ql + (1.0 - alin) * (q2 + dq);
+  qr = alin * qr + (1.0 - alin) * (q2 - dq);
+}
+// burgers_package.hpp:32-43
+inline void hll_vel(double uxl, double uxr, double uyl, double uyr, double uzl, double uzr,
+                    double upl, double upr, double &sl, double &sr, double &fx, double &fy,
+                    double &fz) {
+  sl = std::min(std::min(upl, upr), 0.0);
+  sr = std::max(std::max(upl, upr), 0.0);
+  const double is = 1.0 / (sr - sl + (sl * sr == 0.0));
+  fx = 0.5 * (sr * uxl * upl - sl * uxr * upr + sl * sr * (uxr - uxl)) * is;
+  fy = 0.5 * (sr * uyl * upl - sl * uyr * upr + sl * sr * (uyr - uyl)) * is;
+  fz = 0.5 * (sr * uzl * upl - sl * uzr * upr + sl * sr * (uzr - uzl)) * is;
+}
+// burgers_package.cpp:328-333
+inline double hll_scalar(double upl, double upr, double ql, double qr, double sl, double sr) {
+  return (sr * upl * ql - sl * upr * qr + sl * sr * (qr - ql)) / (sr - sl + (sl * sr == 0.0));
+}
+
+// burgers_package.cpp:202-404; recon 0 = WENO5, 1 = linear (MC). Face states are
+// kept per block (the reference stores them in six mesh-wide Derived fields).
+inline void burgers_fluxes(Field &U, FluxField &F, int recon) {
+  const int ng = U.mesh->p.ng;
+  const int nb = (int)U.blocks->size();
+  const int nc = U.ncomp;
+  const int N0 = U.N[0], N1 = U.N[1], N2 = U.N[2];
+  const int is = ng, ie = N0 - ng - 1, js = ng, je = N1 - ng - 1, ks = ng, ke = N2 - ng - 1;
+  const int64_t fs = (int64_t)N0 * N1 * N2;
+#pragma omp parallel
+  {
+    std::vector<double> L[3], R[3];
+    for (int d = 0; d < 3; ++d) {
+      L[d].assign((size_t)nc * fs, 0.0);
+      R[d].assign((size_t)nc * fs, 0.0);
+    }
+    auto id = [&](int v, int k, int j, int i) {
+      return (((int64_t)v * N2 + k) * N1 + j) * N0 + i;
+    };
+#pragma omp for schedule(dynamic, 1)
+    for (int b = 0; b < nb; ++b) {
+      for (int k = ks - 1; k <= ke + 1; ++k)
+        for (int j = js - 1; j <= je + 1; ++j) {
+          const bool xr = (k >= ks && k <= ke) && (j >= js && j <= je);
+          const bool yr = (k >= ks && k <= ke);
+          const bool zr = (j >= js && j <= je);
+          for (int n = 0; n < nc; ++n) {
+            auto q = [&](int kk, int jj, int ii) { return U.at(b, n, kk, jj, ii); };
+            if (xr)
+              for (int i = is - 1; i <= ie + 1; ++i) {
+                double ql, qr;
+                if (recon == 0) weno5z(q(k, j, i - 2), q(k, j, i - 1), q(k, j, i), q(k, j, i + 1), q(k, j, i + 2), ql, qr);
+                else linear_recon(q(k, j, i - 1), q(k, j, i), q(k, j, i + 1), ql, qr);
+                L[0][id(n, k, j, i + 1)] = ql;
+                R[0][id(n, k, j, i)] = qr;
+              }
+            if (yr)
+              for (int i = is; i <= ie; ++i) {
+                double ql, qr;
+                if (recon == 0) weno5z(q(k, j - 2, i), q(k, j - 1, i), q(k, j, i), q(k, j + 1, i), q(k, j + 2, i), ql, qr);
+                else linear_recon(q(k, j - 1, i), q(k, j, i), q(k, j + 1, i), ql, qr);
+                L[1][id(n, k, j + 1, i)] = ql;
+                R[1][id(n, k, j, i)] = qr;
+              }
+            if (zr)
+              for (int i = is; i <= ie; ++i) {
+                double ql, qr;
+                if (recon == 0) weno5z(q(k - 2, j, i), q(k - 1, j, i), q(k, j, i), q(k + 1, j, i), q(k + 2, j, i), ql, qr);
+                else linear_recon(q(k - 1, j, i), q(k, j, i), q(k + 1, j, i), ql, qr);
+                L[2][id(n, k + 1, j, i)] = ql;
+                R[2][id(n, k, j, i)] = qr;
+              }
+          }
+        }
+      for (int k = ks; k <= ke + 1; ++k)
+        for (int j = js; j <= je + 1; ++j) {
+          const bool xf = (k <= ke && j <= je);
+          const bool yf = (k <= ke);
+          const bool zf = (j <= je);
+          for (int d = 0; d < 3; ++d) {
+            if ((d == 0 && !xf) || (d == 1 && !yf) || (d == 2 && !zf)) continue;
+            const int i1 = d == 0 ? ie + 1 : ie;
+            for (int i = is; i <= i1; ++i) {
+              const double uxl = L[d][id(0, k, j, i)], uxr = R[d][id(0, k, j, i)];
+              const double uyl = L[d][id(1, k, j, i)], uyr = R[d][id(1, k, j, i)];
+              const double uzl = L[d][id(2, k, j, i)], uzr = R[d][id(2, k, j, i)];
+              const double upl = L[d][id(d, k, j, i)], upr = R[d][id(d, k, j, i)];
+              double sl, sr, fx, fy, fz;
+              hll_vel(uxl, uxr, uyl, uyr, uzl, uzr, upl, upr, sl, sr, fx, fy, fz);
+              F.at(b, d, 0, k, j, i) = fx;
+              F.at(b, d, 1, k, j, i) = fy;
+              F.at(b, d, 2, k, j, i) = fz;
+              for (int n = 3; n < nc; ++n)
+                F.at(b, d, n, k, j, i) =
+                    hll_scalar(upl, upr, L[d][id(n, k, j, i)], R[d][id(n, k, j, i)], sl, sr);
+            }
+          }
+        }
+    }
+  }
+}
+
+// burgers_package.cpp:170-200 (before the cfl factor)
+inline double burgers_min_dt(Field &U) {
+  const int ng = U.mesh->p.ng;
+  double mn = std::numeric_limits<double>::max();
+  for (size_t b = 0; b < U.blocks->size(); ++b) {
+    const Coords &c = (*U.blocks)[b].coords;
+    for (int k = ng; k < U.N[2] - ng; ++k)
+      for (int j = ng; j < U.N[1] - ng; ++j)
+        for (int i = ng; i < U.N[0] - ng; ++i) {
+          const double r = 1.0 / ((std::fabs(U.at(b, 0, k, j, i))) / c.dx[0] +
+                                  1 * (std::fabs(U.at(b, 1, k, j, i))) / c.dx[1] +
+                                  1 * (std::fabs(U.at(b, 2, k, j, i))) / c.dx[2]);
+          mn = std::min(mn, r);
+        }
+  }
+  return mn;
+}
+
+// advection_package.cpp:499-647 (constant velocity); recon 0 = donor cell, 1 = PLM.
+// PLM follows plm_inline.hpp:40-113 (uniform van Leer branch).
+inline void plm_face_states(const Coords &c, int d, int idx, double qm, double q0, double qp,
+                            double &ql_next, double &qr_here) {
+  const double dql = q0 - qm, dqr = qp - q0;
+  const double dq2 = dql * dqr;
+  double dqm = 2.0 * dq2 / (dql + dqr);
+  if (dq2 <= 0.0) dqm = 0.0;
+  const double xfp = c.xf(d, idx + 1), xcc = c.xc(d, idx), xfm = c.xf(d, idx);
+  ql_next = q0 + ((xfp - xcc) / c.dx[d]) * dqm;
+  qr_here = q0 - ((xcc - xfm) / c.dx[d]) * dqm;
+}
+
+inline void advection_fluxes(Field &U, FluxField &F, int recon, const double vel[3]) {
+  const int ng = U.mesh->p.ng;
+  const int nb = (int)U.blocks->size();
+  const int is = ng, ie = U.N[0] - ng - 1, js = ng, je = U.N[1] - ng - 1, ks = ng, ke = U.N[2] - ng - 1;
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < nb; ++b) {
+    const Coords &c = (*U.blocks)[b].coords;
+    for (int n = 0; n < U.ncomp; ++n) {
+      auto q = [&](int k, int j, int i) { return U.at(b, n, k, j, i); };
+      // x faces: i in [is, ie+1], k in [ks,ke], j in [js,je]
+      for (int k = ks; k <= ke; ++k)
+        for (int j = js; j <= je; ++j)
+          for (int i = is; i <= ie + 1; ++i) {
+            double ql, qr, dummy;
+            if (recon == 0) {
+              ql = q(k, j, i - 1);
+              qr = q(k, j, i);
+            } else {
+              plm_face_states(c, 0, i - 1, q(k, j, i - 2), q(k, j, i - 1), q(k, j, i), ql, dummy);
+              plm_face_states(c, 0, i, q(k, j, i - 1), q(k, j, i), q(k, j, i + 1), dummy, qr);
+            }
+            F.at(b, 0, n, k, j, i) = vel[0] > 0.0 ? ql * vel[0] : qr * vel[0];
+          }
+      for (int k = ks; k <= ke; ++k)
+        for (int j = js; j <= je + 1; ++j)
+          for (int i = is; i <= ie; ++i) {
+            double ql, qr, dummy;
+            if (recon == 0) {
+              ql = q(k, j - 1, i);
+              qr = q(k, j, i);
+            } else {
+              plm_face_states(c, 1, j - 1, q(k, j - 2, i), q(k, j - 1, i), q(k, j, i), ql, dummy);
+              plm_face_states(c, 1, j, q(k, j - 1, i), q(k, j, i), q(k, j + 1, i), dummy, qr);
+            }
+            F.at(b, 1, n, k, j, i) = vel[1] > 0.0 ? ql * vel[1] : qr * vel[1];
+          }
+      for (int k = ks; k <= ke + 1; ++k)
+        for (int j = js; j <= je; ++j)
+          for (int i = is; i <= ie; ++i) {
+            double ql, qr, dummy;
+            if (recon == 0) {
+              ql = q(k - 1, j, i);
+              qr = q(k, j, i);
+            } else {
+              plm_face_states(c, 2, k - 1, q(k - 2, j, i), q(k - 1, j, i), q(k, j, i), ql, dummy);
+              plm_face_states(c, 2, k, q(k - 1, j, i), q(k, j, i), q(k + 1, j, i), dummy, qr);
+            }
+            F.at(b, 2, n, k, j, i) = vel[2] > 0.0 ? ql * vel[2] : qr * vel[2];
+          }
+    }
+  }
+}
+
+// advection_package.cpp:465-494 (before cfl)
+inline double advection_min_dt(Field &U, const double vel[3]) {
+  double mn = std::numeric_limits<double>::max();
+  for (auto &b : *U.blocks)
+    for (int d = 0; d < 3; ++d)
+      if (vel[d] != 0.0) mn = std::min(mn, b.coords.dx[d] / std::fabs(vel[d]));
+  return mn;
+}
+
+// ---------------------------------------------------------------- simulation
+struct Sim {
+  std::unique_ptr<Mesh> mesh;
+  std::vector<BndRec> recs;
+  int physics = 0;  // 0 advection, 1 burgers
+  int recon = 0;
+  double cfl = 0.3;
+  double vel[3] = {1.0, 1.0, 1.0};
+  int ncomp = 1;
+  bool prolong_in_stage = true;
+  Field base, stage, dudt;
+  FluxField flux;
+  double dt = std::numeric_limits<double>::max();
+  double time = 0.0;
+  int ncycle = 0;
+  int64_t zone_cycles = 0;
+};
+
+inline double estimate_dt(Sim &s, Field &U) {
+  if (s.physics == 1) return s.cfl * burgers_min_dt(U);
+  return s.cfl * advection_min_dt(U, s.vel);
+}
+
+// driver.cpp:210-232 (dt_force/dt_init/dt_user/floor/ceil at their defaults)
+inline void set_global_dt(Sim &s, double new_dt) {
+  if (s.dt < 0.1 * std::numeric_limits<double>::max()) s.dt *= 2.0;
+  s.dt = std::min(s.dt, new_dt);
+  s.dt = std::max(std::numeric_limits<double>::min(), std::min(s.dt, std::numeric_limits<double>::max()));
+}
+
+inline void weighted_sum(Field &z, Field &x, Field &y, double w1, double w2) {
+  const size_t n = z.data.size();
+#pragma omp parallel for schedule(static)
+  for (size_t i = 0; i < n; ++i) z.data[i] = w1 * x.data[i] + w2 * y.data[i];
+}
+
+// One RK2 cycle (advection_driver.cpp:56-164, burgers_driver.cpp:53-148 task order)
+inline void cycle(Sim &s) {
+  Mesh &m = *s.mesh;
+  const double betas[2] = {1.0, 0.5};
+  Field *cont[3] = {&s.base, &s.stage, &s.base};  // stage names base, "1", base
+  for (int st = 1; st <= 2; ++st) {
+    Field &mc0 = *cont[st - 1];
+    Field &mc1 = *cont[st];
+    const double beta = betas[st - 1];
+    if (s.physics == 1) burgers_fluxes(mc0, s.flux, s.recon);
+    else advection_fluxes(mc0, s.flux, s.recon, s.vel);
+    if (m.multilevel) flux_correction(s.flux, m, m.blocks);
+    const int ng = m.p.ng;
+    const int nblk = (int)m.blocks.size();
+#pragma omp parallel for schedule(static)
+    for (int b = 0; b < nblk; ++b) {
+      const Coords &c = m.blocks[b].coords;
+      for (int l = 0; l < s.ncomp; ++l)
+        for (int k = ng; k < mc0.N[2] - ng; ++k)
+          for (int j = ng; j < mc0.N[1] - ng; ++j)
+            for (int i = ng; i < mc0.N[0] - ng; ++i)
+              s.dudt.at((int)b, l, k, j, i) = flux_div(s.flux, c, (int)b, l, k, j, i);
+    }
+    weighted_sum(mc0, mc0, s.base, beta, 1.0 - beta);
+    weighted_sum(mc1, mc0, s.dudt, 1.0, beta * s.dt);
+    exchange(mc1, m.blocks, BAny, 0, s.recs, s.prolong_in_stage, PMinMod, m.multilevel);
+  }
+  s.ncycle += 1;
+  s.time += s.dt;
+  s.zone_cycles += (int64_t)m.blocks.size() * m.p.bnx[0] * m.p.bnx[1] * m.p.bnx[2];
+  set_global_dt(s, estimate_dt(s, s.base));
+}
+
+}  // namespace oracle
+
+// ======================================================================== C API
+using namespace oracle;
+
+extern "C" {
+
+// Mesh/Sim creation. leaves: nleaves x (level, l1, l2, l3); nleaves == 0 means uniform.
+void *orc_sim_create(const int *nx, const int *bnx, int ng, const double *xmin,
+                     const double *xmax, int nleaves, const int64_t *leaves, int ncomp,
+                     int physics, int recon, double cfl, const double *vel, int prolong_in_stage) {
+  try {
+    auto s = new Sim();
+    MeshParams p;
+    for (int d = 0; d < 3; ++d) {
+      p.nx[d] = nx[d];
+      p.bnx[d] = bnx[d];
+      p.xmin[d] = xmin[d];
+      p.xmax[d] = xmax[d];
+    }
+    p.ng = ng;
+    p.multilevel = 0;
+    s->mesh.reset(new Mesh(p));
+    for (int n = 0; n < nleaves; ++n) {
+      const int64_t *q = leaves + 4 * n;
+      s->mesh->add_leaf(Loc((int)q[0], q[1], q[2], q[3]));
+    }
+    s->mesh->finalize();
+    s->physics = physics;
+    s->recon = recon;
+    s->cfl = cfl;
+    for (int d = 0; d < 3; ++d) s->vel[d] = vel ? vel[d] : 1.0;
+    s->ncomp = ncomp;
+    s->prolong_in_stage = prolong_in_stage != 0;
+    s->base.init(s->mesh.get(), &s->mesh->blocks, ncomp);
+    s->stage.init(s->mesh.get(), &s->mesh->blocks, ncomp);
+    s->dudt.init(s->mesh.get(), &s->mesh->blocks, ncomp);
+    s->flux.init(s->base);
+    s->recs = build_boundaries(*s->mesh, s->mesh->blocks, BAny, 0);
+    return s;
+  } catch (std::exception &e) {
+    fprintf(stderr, "oracle: %s\n", e.what());
+    return nullptr;
+  }
+}
+
+void orc_sim_destroy(void *h) { delete (Sim *)h; }
+
+int orc_nblocks(void *h) { return (int)((Sim *)h)->mesh->blocks.size(); }
+int orc_multilevel(void *h) { return ((Sim *)h)->mesh->multilevel ? 1 : 0; }
+
+// per block: level, l1, l2, l3 and (xmin[3], dx[3])
+void orc_block_info(void *h, int64_t *locs, double *geom) {
+  Sim *s = (Sim *)h;
+  for (size_t b = 0; b < s->mesh->blocks.size(); ++b) {
+    auto &bl = s->mesh->blocks[b];
+    locs[4 * b + 0] = bl.loc.level;
+    for (int d = 0; d < 3; ++d) locs[4 * b + 1 + d] = bl.loc.l[d];
+    for (int d = 0; d < 3; ++d) {
+      geom[6 * b + d] = bl.bxmin[d];
+      geom[6 * b + 3 + d] = bl.coords.dx[d];
+    }
+  }
+}
+
+double *orc_base(void *h) { return ((Sim *)h)->base.data.data(); }
+double *orc_base_coarse(void *h) { return ((Sim *)h)->base.coarse.data(); }
+int64_t orc_field_size(void *h) { return (int64_t)((Sim *)h)->base.data.size(); }
+int64_t orc_coarse_size(void *h) { return (int64_t)((Sim *)h)->base.coarse.size(); }
+
+// Boundary index maps: per record 23 int32 values
+// [sender_gid, receiver_gid, locidx, send s/e (i,j,k) x6, send_coarse, recv s/e x6,
+//  recv_coarse, recv_mask_bits, nvalues]
+int orc_num_boundaries(void *h) { return (int)((Sim *)h)->recs.size(); }
+void orc_boundaries(void *h, int32_t *out) {
+  Sim *s = (Sim *)h;
+  int r = 0;
+  for (auto &br : s->recs) {
+    int32_t *o = out + 23 * r++;
+    o[0] = s->mesh->blocks[br.sender].gid;
+    o[1] = s->mesh->blocks[br.receiver].gid;
+    o[2] = br.locidx;
+    for (int d = 0; d < 3; ++d) {
+      o[3 + 2 * d] = br.send.s[d];
+      o[4 + 2 * d] = br.send.e[d];
+      o[10 + 2 * d] = br.recv.s[d];
+      o[11 + 2 * d] = br.recv.e[d];
+    }
+    o[9] = br.send_coarse;
+    o[16] = br.recv_coarse;
+    o[17] = (int32_t)br.recv.mask.bits();
+    o[18] = (int32_t)(br.send.size() * s->ncomp);
+    o[19] = o[20] = o[21] = o[22] = 0;
+  }
+}
+
+// Full ghost exchange of the base container (pack -> buffer -> unpack
+// [-> restrict -> prolong]); returns the number of overlapping active writes.
+int64_t orc_exchange(void *h, int prolongate, int op) {
+  Sim *s = (Sim *)h;
+  auto st = exchange(s->base, s->mesh->blocks, BAny, 0, s->recs, prolongate != 0, op,
+                     s->mesh->multilevel, true);
+  return st.overlaps;
+}
+
+// Initialise the time step from the current base state (InitializeBlockTimeSteps +
+// SetGlobalTimeStep at cycle 0).
+double orc_init_dt(void *h) {
+  Sim *s = (Sim *)h;
+  s->dt = std::numeric_limits<double>::max();
+  s->ncycle = 0;
+  s->time = 0.0;
+  s->zone_cycles = 0;
+  set_global_dt(*s, estimate_dt(*s, s->base));
+  return s->dt;
+}
+
+// Run ncycles RK2 cycles; dts (may be null) receives the dt used in each cycle.
+int orc_run(void *h, int ncycles, int nthreads, double *dts) {
+  Sim *s = (Sim *)h;
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  try {
+    for (int c = 0; c < ncycles; ++c) {
+      if (dts) dts[c] = s->dt;
+      cycle(*s);
+    }
+  } catch (std::exception &e) {
+    fprintf(stderr, "oracle: %s\n", e.what());
+    return -1;
+  }
+  return 0;
+}
+
+double orc_dt(void *h) { return ((Sim *)h)->dt; }
+int orc_max_threads() { return omp_get_max_threads(); }
+
+// Known-answer hooks for the reference unit tests (test_logical_location.cpp):
+// ownership of `main` among the given neighbour locations (level,l1,l2,l3 each),
+// returned as the 27-bit mask used by the product.
+uint32_t orc_ownership(const int64_t *main, int n, const int64_t *locs) {
+  Loc m((int)main[0], main[1], main[2], main[3]);
+  std::vector<NbLoc> nbs;
+  for (int i = 0; i < n; ++i) {
+    Loc l((int)locs[4 * i], locs[4 * i + 1], locs[4 * i + 2], locs[4 * i + 3]);
+    nbs.push_back({l, l});
+  }
+  return determine_ownership(m, nbs).bits();
+}
+uint32_t orc_range_mask(int el, uint32_t own_bits, int ox1, int ox2, int ox3) {
+  Own o;
+  for (int c = -1; c <= 1; ++c)
+    for (int b = -1; b <= 1; ++b)
+      for (int a = -1; a <= 1; ++a)
+        o(a, b, c) = (own_bits >> ((a + 1) + 3 * (b + 1) + 9 * (c + 1))) & 1u;
+  return range_mask_from_ownership(el, o, ox1, ox2, ox3).bits();
+}
+void orc_morton(int level, int64_t l1, int64_t l2, int64_t l3, uint64_t *out) {
+  Loc l(level, l1, l2, l3);
+  for (int c = 0; c < 3; ++c) out[c] = l.m[c];
+}
+
+}  // extern "C"

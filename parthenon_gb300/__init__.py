@@ -1,0 +1,12 @@
+"""GB300-native block-structured AMR hot path (Parthenon-compatible semantics).
+
+Native library: libparthenon_gb300.so (C ABI in include/parthenon_gb300.h), built with
+`parthenon_gb300.build.build()`. This package is the host-side mirror of the
+reference's mesh / exchange / driver interface; all compute runs in the library.
+"""
+from .mesh import Mesh  # noqa: F401
+from .driver import RK2Driver, StageConfig  # noqa: F401
+from . import problems  # noqa: F401
+from ._native import NativeError  # noqa: F401
+
+__all__ = ["Mesh", "RK2Driver", "StageConfig", "problems", "NativeError"]

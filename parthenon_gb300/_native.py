@@ -1,0 +1,91 @@
+"""ctypes binding of libparthenon_gb300.so (the C ABI declared in include/parthenon_gb300.h).
+
+There is no fallback: if the native library is missing or cannot be loaded, every
+entry point raises. Build it with `python -m parthenon_gb300.build` (or
+`__graft_entry__.build()`).
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+_lib = None
+
+I32P = ctypes.POINTER(ctypes.c_int32)
+I64P = ctypes.POINTER(ctypes.c_int64)
+DP = ctypes.POINTER(ctypes.c_double)
+VP = ctypes.c_void_p
+
+
+class MeshSpec(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32 * 3), ("block_nx", ctypes.c_int32 * 3), ("nghost", ctypes.c_int32),
+                ("xmin", ctypes.c_double * 3), ("xmax", ctypes.c_double * 3)]
+
+
+class MeshInfo(ctypes.Structure):
+    _fields_ = [("nblocks", ctypes.c_int32), ("multilevel", ctypes.c_int32), ("root_level", ctypes.c_int32),
+                ("max_level", ctypes.c_int32), ("N", ctypes.c_int32 * 3), ("Nc", ctypes.c_int32 * 3),
+                ("npairs", ctypes.c_int32), ("buffer_elems", ctypes.c_int64), ("nflux_corr", ctypes.c_int32)]
+
+
+class StageParams(ctypes.Structure):
+    _fields_ = [("physics", ctypes.c_int32), ("recon", ctypes.c_int32), ("exact", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("vel", ctypes.c_double * 3), ("cfl", ctypes.c_double)]
+
+
+# name -> (argtypes); every function returns int32 status unless noted
+_SIGNATURES = {
+    "pgb_version": [],
+    "pgb_mesh_create": [ctypes.POINTER(MeshSpec), ctypes.c_int32, VP, ctypes.POINTER(VP)],
+    "pgb_mesh_destroy": [VP],
+    "pgb_mesh_get_info": [VP, ctypes.POINTER(MeshInfo)],
+    "pgb_mesh_block_info": [VP, VP, VP],
+    "pgb_mesh_boundaries": [VP, VP, ctypes.c_int32],
+    "pgb_mesh_upload": [VP],
+    "pgb_exchange": [VP, VP, VP, ctypes.c_int32, ctypes.c_int32, VP, VP],
+    "pgb_pack_buffers": [VP, VP, VP, ctypes.c_int32, VP, VP],
+    "pgb_flux_correct": [VP, VP, ctypes.c_int32, VP],
+    "pgb_stage": [VP, ctypes.POINTER(StageParams), VP, VP, VP, VP, VP, VP, ctypes.c_double, ctypes.c_double,
+                  ctypes.c_double, ctypes.c_int32, VP],
+    "pgb_estimate_dt": [VP, ctypes.POINTER(StageParams), VP, ctypes.c_int32, VP, ctypes.c_int32, VP],
+    "pgb_rk2_cycles": [VP, ctypes.POINTER(StageParams), VP, VP, VP, VP, VP, VP, ctypes.c_int32, VP,
+                       ctypes.c_int32, ctypes.c_int32, VP],
+    "pgb_run_host": [VP, ctypes.POINTER(StageParams), VP, VP, ctypes.c_int32, ctypes.c_int32, DP],
+}
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def lib_path():
+    return _build.LIB
+
+
+def lib():
+    """Load the native library (raises if it is absent: no CPU fallback exists)."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise NativeError("libparthenon_gb300.so is not built (%s); run parthenon_gb300.build.build()" % path)
+        L = ctypes.CDLL(path)
+        for name, args in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int32
+        L.pgb_last_error.argtypes = []
+        L.pgb_last_error.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def check(rc, what=""):
+    if rc != 0:
+        msg = lib().pgb_last_error().decode(errors="replace")
+        raise NativeError("%s failed (%d): %s" % (what, rc, msg))
+    return rc
+
+
+def exported_symbols():
+    return sorted(list(_SIGNATURES) + ["pgb_last_error"])

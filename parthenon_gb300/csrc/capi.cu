@@ -1,0 +1,382 @@
+// extern "C" boundary of the library: argument checking, error codes, and the RK2
+// cycle driver that sequences the kernels (one CUDA stream, no host synchronisation
+// inside a cycle, optional CUDA-graph replay).
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <string>
+#include <tuple>
+
+#include "../../include/parthenon_gb300.h"
+#include "common.cuh"
+#include "mesh_state.hpp"
+#include "stencil.cuh"
+
+namespace pgb {
+
+thread_local std::string g_error;
+void set_error(const std::string &m) { g_error = m; }
+int fail(int code, const std::string &m) {
+  set_error(m);
+  return code;
+}
+int check_cuda(cudaError_t e, const char *what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return kErrCuda;
+}
+
+// exchange.cu
+int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate, int prolong_op,
+                  double *buffer, cudaStream_t s);
+int pack_grid(GridTables &t, const double *fine, const double *coarse, int ncomp, double *buffer, cudaStream_t s);
+int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s);
+// reduce.cu
+int estimate_dt(MeshState &m, int physics, const double *u, int ncomp, const double vel[3], double cfl, double *dt,
+                int first, cudaStream_t s);
+// stencil builds
+namespace exact {
+int launch_stage(const StageArgs &a, int ncomp, int physics, bool store_flux, cudaStream_t s);
+int launch_div_update(const StageArgs &a, int ncomp, cudaStream_t s);
+}  // namespace exact
+namespace fast {
+int launch_stage(const StageArgs &a, int ncomp, int physics, bool store_flux, cudaStream_t s);
+int launch_div_update(const StageArgs &a, int ncomp, cudaStream_t s);
+}  // namespace fast
+
+}  // namespace pgb
+
+using namespace pgb;
+
+struct pgb_mesh {
+  MeshState st;
+  // cached cycle graphs keyed by the pointers and parameters they were captured with
+  std::map<std::tuple<const void *, const void *, const void *, const void *, int, int, int, int>, cudaGraphExec_t>
+      graphs;
+  ~pgb_mesh() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+  }
+};
+
+namespace {
+
+int stage_impl(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const double *u_base, double *u_out,
+               double *dudt, double *flux, const double *dt, double w_in, double w_base, double beta, int ncomp,
+               cudaStream_t s) {
+  GridTables &t = m->st.leaf;
+  StageArgs a;
+  a.u_in = u_in;
+  a.u_base = u_base;
+  a.u_out = u_out;
+  a.dudt = dudt;
+  a.flux = flux;
+  a.dt = dt;
+  a.w_in = w_in;
+  a.w_base = w_base;
+  a.beta = beta;
+  a.geom = t.geom;
+  a.d = t.dims;
+  a.nblocks = t.nblocks;
+  a.recon = p->recon;
+  for (int q = 0; q < 3; ++q) a.vel[q] = p->vel[q];
+  const bool ml = t.multilevel;
+  if (ml && !flux) return fail(kErrInvalid, "multilevel stage needs a flux array");
+  if (!ml && !dudt) return fail(kErrInvalid, "stage needs a dudt scratch array");
+  int rc;
+  auto launch = p->exact ? exact::launch_stage : fast::launch_stage;
+  auto divup = p->exact ? exact::launch_div_update : fast::launch_div_update;
+  rc = launch(a, ncomp, p->physics, ml, s);
+  if (rc == kErrUnsupported) return fail(rc, "no stencil kernel for this component count");
+  if (rc != kOk) return check_cuda(cudaGetLastError(), "stencil launch");
+  if (ml) {
+    if ((rc = flux_correct_grid(t, flux, ncomp, s))) return rc;
+    rc = divup(a, ncomp, s);
+    if (rc == kErrUnsupported) return fail(rc, "no update kernel for this component count");
+    if (rc != kOk) return check_cuda(cudaGetLastError(), "update launch");
+  }
+  return kOk;
+}
+
+int check_params(const pgb_mesh *m, const pgb_stage_params *p, int ncomp) {
+  if (!m || !p) return fail(kErrInvalid, "null argument");
+  if (!m->st.uploaded) return fail(kErrState, "mesh tables not uploaded (call pgb_mesh_upload)");
+  if (p->physics != 0 && p->physics != 1) return fail(kErrInvalid, "physics must be 0 or 1");
+  const int ng = m->st.leaf.dims.ng;
+  if (p->physics == 1) {
+    if (ncomp < 4) return fail(kErrInvalid, "Burgers needs 3 velocity components and >= 1 scalar");
+    if (p->recon == 0 && ng < 3) return fail(kErrInvalid, "WENO5 needs nghost >= 3");
+  }
+  if (p->recon == 1 && ng < 2) return fail(kErrInvalid, "this reconstruction needs nghost >= 2");
+  if (m->st.leaf.multilevel && ng < 2) return fail(kErrInvalid, "multilevel meshes need nghost >= 2");
+  return kOk;
+}
+
+int exchange_leaf(pgb_mesh *m, double *data, double *coarse, int ncomp, int flags, double *buffer, cudaStream_t s) {
+  const int prolongate = flags & PGB_EXCHANGE_PROLONGATE;
+  const int op = (flags >> 1) & 3;
+  return exchange_grid(m->st.leaf, data, coarse, ncomp, prolongate, op, buffer, s);
+}
+
+// One RK2 cycle: stage names base, "1", base (low_storage_integrator.cpp:67-86 rk2:
+// beta = {1, 0.5}); Burgers omits the prolongation step of the exchange
+// (burgers_driver.cpp:108-120 wires Send/Receive/Set only).
+int cycle_impl(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage, double *dudt, double *flux,
+               double *cbase, double *cstage, int ncomp, double *dt, cudaStream_t s) {
+  const int xflags = p->physics == 1 ? 0 : PGB_EXCHANGE_PROLONGATE;
+  int rc;
+  if ((rc = stage_impl(m, p, base, base, stage, dudt, flux, dt, 1.0, 0.0, 1.0, ncomp, s))) return rc;
+  if ((rc = exchange_leaf(m, stage, cstage, ncomp, xflags, nullptr, s))) return rc;
+  if ((rc = stage_impl(m, p, stage, base, base, dudt, flux, dt, 0.5, 0.5, 0.5, ncomp, s))) return rc;
+  if ((rc = exchange_leaf(m, base, cbase, ncomp, xflags, nullptr, s))) return rc;
+  return estimate_dt(m->st, p->physics, base, ncomp, p->vel, p->cfl, dt, 0, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *pgb_last_error(void) { return g_error.c_str(); }
+int pgb_version(void) { return 1; }
+
+int pgb_mesh_create(const pgb_mesh_spec *spec, int32_t nleaves, const int64_t *leaves, pgb_mesh **out) {
+  if (!spec || !out || (nleaves > 0 && !leaves)) return fail(kErrInvalid, "null argument");
+  try {
+    MeshSpec ms;
+    for (int d = 0; d < 3; ++d) {
+      ms.nx[d] = spec->nx[d];
+      ms.bnx[d] = spec->block_nx[d];
+      ms.xmin[d] = spec->xmin[d];
+      ms.xmax[d] = spec->xmax[d];
+      if (!(ms.xmax[d] > ms.xmin[d])) return fail(kErrInvalid, "xmax must exceed xmin");
+    }
+    ms.ng = spec->nghost;
+    std::vector<LLoc> lv;
+    for (int n = 0; n < nleaves; ++n)
+      lv.emplace_back((int)leaves[4 * n], leaves[4 * n + 1], leaves[4 * n + 2], leaves[4 * n + 3]);
+    auto *m = new pgb_mesh();
+    m->st.topo.reset(new MeshTopology(ms, lv));
+    *out = m;
+    return kOk;
+  } catch (std::exception &e) {
+    return fail(kErrInvalid, e.what());
+  }
+}
+
+int pgb_mesh_destroy(pgb_mesh *mesh) {
+  delete mesh;
+  return kOk;
+}
+
+int pgb_mesh_get_info(const pgb_mesh *m, pgb_mesh_info *info) {
+  if (!m || !info) return fail(kErrInvalid, "null argument");
+  const auto &t = *m->st.topo;
+  const auto &g = t.leaf();
+  std::memset(info, 0, sizeof(*info));
+  info->nblocks = (int)g.blocks.size();
+  info->multilevel = g.multilevel;
+  info->root_level = t.root_level();
+  info->max_level = t.max_level();
+  const int ng = t.spec().ng;
+  for (int d = 0; d < 3; ++d) {
+    info->N[d] = t.spec().bnx[d] + 2 * ng;
+    info->Nc[d] = std::max(1, t.spec().bnx[d] / 2) + 2 * ng;
+  }
+  info->npairs = (int)g.pairs.size();
+  int64_t be = 0;
+  for (auto &p : g.pairs) be += p.send.count();
+  info->buffer_elems = be;
+  info->nflux_corr = (int)g.flux_corr.size();
+  return kOk;
+}
+
+int pgb_mesh_block_info(const pgb_mesh *m, int64_t *locs, double *geom) {
+  if (!m || !locs || !geom) return fail(kErrInvalid, "null argument");
+  const auto &bl = m->st.topo->leaf().blocks;
+  for (size_t b = 0; b < bl.size(); ++b) {
+    locs[4 * b] = bl[b].loc.level;
+    for (int d = 0; d < 3; ++d) {
+      locs[4 * b + 1 + d] = bl[b].loc.lx[d];
+      geom[6 * b + d] = bl[b].xmin[d];
+      geom[6 * b + 3 + d] = bl[b].dx[d];
+    }
+  }
+  return kOk;
+}
+
+int pgb_mesh_boundaries(const pgb_mesh *m, int32_t *out, int32_t capacity) {
+  if (!m || !out) return fail(kErrInvalid, "null argument");
+  const auto &g = m->st.topo->leaf();
+  if (capacity < (int)g.pairs.size()) return fail(kErrInvalid, "capacity too small");
+  int r = 0;
+  for (auto &p : g.pairs) {
+    int32_t *o = out + 23 * r++;
+    o[0] = g.blocks[p.sender].gid;
+    o[1] = g.blocks[p.receiver].gid;
+    o[2] = p.loc_index;
+    for (int d = 0; d < 3; ++d) {
+      o[3 + 2 * d] = p.send.lo[d];
+      o[4 + 2 * d] = p.send.hi[d];
+      o[10 + 2 * d] = p.recv.lo[d];
+      o[11 + 2 * d] = p.recv.hi[d];
+    }
+    o[9] = p.send_coarse;
+    o[16] = p.recv_coarse;
+    o[17] = (int32_t)p.recv.mask;
+    o[18] = (int32_t)p.send.count();
+    o[19] = o[20] = o[21] = o[22] = 0;
+  }
+  return kOk;
+}
+
+int pgb_mesh_upload(pgb_mesh *m) {
+  if (!m) return fail(kErrInvalid, "null argument");
+  int rc = lower_grid(m->st.topo->leaf(), m->st.topo->spec(), m->st.leaf);
+  if (rc) return rc;
+  if (!m->st.d_minbits) {
+    PGB_CUDA(cudaMalloc(&m->st.d_minbits, sizeof(unsigned long long)));
+    const double big = std::numeric_limits<double>::max();
+    unsigned long long bits;
+    std::memcpy(&bits, &big, sizeof(bits));
+    PGB_CUDA(cudaMemcpy(m->st.d_minbits, &bits, sizeof(bits), cudaMemcpyHostToDevice));
+  }
+  for (auto &kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  m->graphs.clear();
+  m->st.uploaded = true;
+  return kOk;
+}
+
+int pgb_exchange(pgb_mesh *m, double *data, double *coarse, int32_t ncomp, int32_t flags, double *buffer,
+                 void *stream) {
+  if (!m) return fail(kErrInvalid, "null mesh");
+  if (!m->st.uploaded) return fail(kErrState, "mesh tables not uploaded (call pgb_mesh_upload)");
+  return exchange_leaf(m, data, coarse, ncomp, flags, buffer, (cudaStream_t)stream);
+}
+
+int pgb_pack_buffers(pgb_mesh *m, const double *data, const double *coarse, int32_t ncomp, double *buffer,
+                     void *stream) {
+  if (!m) return fail(kErrInvalid, "null mesh");
+  if (!m->st.uploaded) return fail(kErrState, "mesh tables not uploaded (call pgb_mesh_upload)");
+  return pack_grid(m->st.leaf, data, coarse, ncomp, buffer, (cudaStream_t)stream);
+}
+
+int pgb_flux_correct(pgb_mesh *m, double *flux, int32_t ncomp, void *stream) {
+  if (!m || !flux) return fail(kErrInvalid, "null argument");
+  if (!m->st.uploaded) return fail(kErrState, "mesh tables not uploaded (call pgb_mesh_upload)");
+  return flux_correct_grid(m->st.leaf, flux, ncomp, (cudaStream_t)stream);
+}
+
+int pgb_stage(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const double *u_base, double *u_out,
+              double *dudt, double *flux, const double *dt, double w_in, double w_base, double beta, int32_t ncomp,
+              void *stream) {
+  int rc = check_params(m, p, ncomp);
+  if (rc) return rc;
+  if (!u_in || !u_base || !u_out || !dt) return fail(kErrInvalid, "null field pointer");
+  return stage_impl(m, p, u_in, u_base, u_out, dudt, flux, dt, w_in, w_base, beta, ncomp, (cudaStream_t)stream);
+}
+
+int pgb_estimate_dt(pgb_mesh *m, const pgb_stage_params *p, const double *u, int32_t ncomp, double *dt,
+                    int32_t first, void *stream) {
+  int rc = check_params(m, p, ncomp);
+  if (rc) return rc;
+  if (!u || !dt) return fail(kErrInvalid, "null pointer");
+  return estimate_dt(m->st, p->physics, u, ncomp, p->vel, p->cfl, dt, first, (cudaStream_t)stream);
+}
+
+int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage, double *dudt, double *flux,
+                   double *cbase, double *cstage, int32_t ncomp, double *dt, int32_t ncycles, int32_t use_graph,
+                   void *stream) {
+  int rc = check_params(m, p, ncomp);
+  if (rc) return rc;
+  if (!base || !stage || !dt) return fail(kErrInvalid, "null field pointer");
+  if (m->st.leaf.multilevel && (!cbase || !cstage)) return fail(kErrInvalid, "multilevel mesh needs coarse buffers");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!use_graph) {
+    for (int c = 0; c < ncycles; ++c)
+      if ((rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s))) return rc;
+    return kOk;
+  }
+  if (!s) return fail(kErrInvalid, "graph replay needs a non-default stream");
+  auto key = std::make_tuple((const void *)base, (const void *)stage, (const void *)dudt, (const void *)dt,
+                             p->physics * 16 + p->recon * 4 + p->exact, ncomp, (int)(flux != nullptr),
+                             (int)(cbase != nullptr));
+  auto it = m->graphs.find(key);
+  if (it == m->graphs.end()) {
+    cudaGraph_t g;
+    PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s);
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return check_cuda(ce, "cudaStreamEndCapture");
+    cudaGraphExec_t ge;
+    ce = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return check_cuda(ce, "cudaGraphInstantiate");
+    it = m->graphs.emplace(key, ge).first;
+  }
+  for (int c = 0; c < ncycles; ++c) PGB_CUDA(cudaGraphLaunch(it->second, s));
+  return kOk;
+}
+
+int pgb_run_host(pgb_mesh *m, const pgb_stage_params *p, const double *host_in, double *host_out, int32_t ncomp,
+                 int32_t ncycles, double *dt_inout) {
+  int rc = check_params(m, p, ncomp);
+  if (rc) return rc;
+  if (!host_in || !host_out || !dt_inout) return fail(kErrInvalid, "null pointer");
+  const GridTables &t = m->st.leaf;
+  const size_t n = (size_t)t.nblocks * ncomp * t.dims.N[0] * t.dims.N[1] * t.dims.N[2];
+  const size_t nc = (size_t)t.nblocks * ncomp * t.dims.Nc[0] * t.dims.Nc[1] * t.dims.Nc[2];
+  const bool ml = t.multilevel;
+  double *base = nullptr, *stage = nullptr, *dudt = nullptr, *flux = nullptr, *cb = nullptr, *cs = nullptr,
+         *dt = nullptr;
+  cudaStream_t s = nullptr;
+  auto cleanup = [&]() {
+    double *ps[] = {base, stage, dudt, flux, cb, cs, dt};
+    for (double *q : ps)
+      if (q) cudaFree(q);
+    if (s) cudaStreamDestroy(s);
+  };
+  auto guard = [&](cudaError_t e, const char *w) {
+    if (e != cudaSuccess) {
+      int r = check_cuda(e, w);
+      cleanup();
+      return r;
+    }
+    return 0;
+  };
+  if ((rc = guard(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream"))) return rc;
+  if ((rc = guard(cudaMalloc(&base, n * 8), "malloc")) || (rc = guard(cudaMalloc(&stage, n * 8), "malloc")) ||
+      (rc = guard(cudaMalloc(&dt, 8), "malloc")))
+    return rc;
+  if (ml) {
+    if ((rc = guard(cudaMalloc(&flux, 3 * n * 8), "malloc")) || (rc = guard(cudaMalloc(&cb, nc * 8), "malloc")) ||
+        (rc = guard(cudaMalloc(&cs, nc * 8), "malloc")))
+      return rc;
+  } else if ((rc = guard(cudaMalloc(&dudt, n * 8), "malloc"))) {
+    return rc;
+  }
+  if ((rc = guard(cudaMemcpyAsync(base, host_in, n * 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
+  if ((rc = guard(cudaMemcpyAsync(stage, base, n * 8, cudaMemcpyDeviceToDevice, s), "d2d"))) return rc;
+  const int xflags = p->physics == 1 ? 0 : PGB_EXCHANGE_PROLONGATE;
+  if ((rc = exchange_leaf(m, base, cb, ncomp, xflags, nullptr, s))) {
+    cleanup();
+    return rc;
+  }
+  if (*dt_inout > 0) {
+    if ((rc = guard(cudaMemcpyAsync(dt, dt_inout, 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
+  } else if ((rc = estimate_dt(m->st, p->physics, base, ncomp, p->vel, p->cfl, dt, 1, s))) {
+    cleanup();
+    return rc;
+  }
+  for (int c = 0; c < ncycles; ++c)
+    if ((rc = cycle_impl(m, p, base, stage, dudt, flux, cb, cs, ncomp, dt, s))) {
+      cleanup();
+      return rc;
+    }
+  if ((rc = guard(cudaMemcpyAsync(host_out, base, n * 8, cudaMemcpyDeviceToHost, s), "d2h"))) return rc;
+  if ((rc = guard(cudaMemcpyAsync(dt_inout, dt, 8, cudaMemcpyDeviceToHost, s), "d2h"))) return rc;
+  if ((rc = guard(cudaStreamSynchronize(s), "sync"))) return rc;
+  cleanup();
+  return kOk;
+}
+
+}  // extern "C"

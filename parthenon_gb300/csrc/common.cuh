@@ -1,0 +1,57 @@
+// Shared device helpers and the library's error reporting.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "device_tables.hpp"
+
+namespace pgb {
+
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int check_cuda(cudaError_t e, const char *what);
+
+constexpr int kOk = 0;
+constexpr int kErrInvalid = -1;
+constexpr int kErrCuda = -2;
+constexpr int kErrUnsupported = -3;
+constexpr int kErrState = -4;
+
+#define PGB_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t e__ = (call);                            \
+    if (e__ != cudaSuccess) return check_cuda(e__, #call); \
+  } while (0)
+
+// Iterate over the rows (k, j) of a work item, with lanes spread over i. Narrow rows
+// (ghost slabs of depth ng) pack several rows into one warp so every lane has work.
+template <class F>
+__device__ __forceinline__ void for_work_rows(int row0, int nrows, int ni, int nj, F &&f) {
+  const int lpr = ni <= 1 ? 1 : ni <= 2 ? 2 : ni <= 4 ? 4 : ni <= 8 ? 8 : ni <= 16 ? 16 : 32;
+  const int sub = threadIdx.x / lpr;
+  const int li = threadIdx.x - sub * lpr;
+  const int step = blockDim.x / lpr;
+  for (int r = sub; r < nrows; r += step) {
+    const int rr = row0 + r;
+    const int k = rr / nj;
+    const int j = rr - k * nj;
+    for (int i = li; i < ni; i += lpr) f(k, j, i);
+  }
+}
+
+__device__ __forceinline__ int64_t fine_index(const Dims &d, int ncomp, int b, int v, int k, int j, int i) {
+  return (((int64_t)b * ncomp + v) * d.N[2] + k) * (int64_t)(d.N[1] * d.N[0]) + (int64_t)j * d.N[0] + i;
+}
+__device__ __forceinline__ int64_t coarse_index(const Dims &d, int ncomp, int b, int v, int k, int j, int i) {
+  return (((int64_t)b * ncomp + v) * d.Nc[2] + k) * (int64_t)(d.Nc[1] * d.Nc[0]) + (int64_t)j * d.Nc[0] + i;
+}
+
+// std::min / std::max semantics (first argument returned on ties and NaN) so that
+// signed zeros and NaNs propagate exactly as in the reference host code.
+__device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+
+}  // namespace pgb

@@ -1,0 +1,443 @@
+// Same-rank ghost exchange, restriction, prolongation and flux correction.
+//
+// Replaces the reference's SendBoundBufs / ReceiveBoundBufs / SetBounds /
+// ProlongateBounds task chain (src/bvals/comms/boundary_communication.cpp:48-393) for
+// one process on one GPU. The reference packs every boundary into a buffer and
+// unpacks it on the same rank; here the default path copies each sender slab
+// straight into the receiver's ghost cells (one launch over every boundary of every
+// block, driven by the device pair table). A buffered path that writes the
+// reference's buffer layout is kept for index-map parity checks.
+//
+// Operation order per exchange (identical to the reference's):
+//   1. restrict fine data into the coarse buffers that feed coarser neighbours
+//      (ProResInfo::GetSend, bnd_info.cpp:371-387)
+//   2. copy every boundary (pack + unpack, masked by ownership)
+//   3. restrict received fine ghosts into coarse-buffer ghosts (ProResInfo::GetSet)
+//   4. prolongate coarse-buffer ghosts into fine ghosts next to coarser blocks
+//      (ProlongateSharedGeneral, pr_ops.hpp:166-285)
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+#include "mesh_state.hpp"
+
+namespace pgb {
+
+// ------------------------------------------------------------------ lowering
+namespace {
+
+DevBox to_dev(const IBox &b) {
+  DevBox d;
+  for (int q = 0; q < 3; ++q) {
+    d.lo[q] = b.lo[q];
+    d.n[q] = b.hi[q] - b.lo[q] + 1;
+  }
+  return d;
+}
+
+bool mask_is_full(const IBox &b) {
+  // Every element active: either the mask is all ones or every boundary cell of the
+  // box maps to an owned slot.
+  if (b.mask == 0x7FFFFFFu) return true;
+  for (int c = -1; c <= 1; ++c)
+    for (int bb = -1; bb <= 1; ++bb)
+      for (int a = -1; a <= 1; ++a) {
+        // slot reachable only if the box has such positions
+        const int n[3] = {b.hi[0] - b.lo[0] + 1, b.hi[1] - b.lo[1] + 1, b.hi[2] - b.lo[2] + 1};
+        const int s[3] = {a, bb, c};
+        bool reachable = true;
+        for (int d = 0; d < 3; ++d) {
+          if (n[d] == 1 && s[d] != 0) reachable = false;   // single index maps to 0
+          if (n[d] == 2 && s[d] == 0) reachable = false;   // two indices: -1 and +1
+        }
+        if (reachable && !mask_get(b.mask, a, bb, c)) return false;
+      }
+  return true;
+}
+
+// Split `rows` rows of `ni` elements into work items of about `target` elements.
+void add_work(std::vector<DevWork> &w, int item, int rows, int ni, int target = 4096) {
+  const int per = std::max(1, target / std::max(ni, 1));
+  for (int r = 0; r < rows; r += per) w.push_back({item, r, std::min(per, rows - r), 0});
+}
+
+template <class T>
+int upload(T **dptr, const std::vector<T> &h) {
+  if (h.empty()) return kOk;
+  PGB_CUDA(cudaMalloc((void **)dptr, h.size() * sizeof(T)));
+  PGB_CUDA(cudaMemcpy(*dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return kOk;
+}
+
+}  // namespace
+
+void GridTables::release() {
+  void *ptrs[] = {pairs, copy_work, rs, rr, pro, rs_work, rr_work, pro_work, fc, fc_work, geom};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  pairs = nullptr;
+  copy_work = nullptr;
+  rs = rr = pro = nullptr;
+  rs_work = rr_work = pro_work = nullptr;
+  fc = nullptr;
+  fc_work = nullptr;
+  geom = nullptr;
+}
+
+MeshState::~MeshState() {
+  leaf.release();
+  if (d_scalars) cudaFree(d_scalars);
+  if (d_minbits) cudaFree(d_minbits);
+  if (d_status) cudaFree(d_status);
+}
+
+int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out) {
+  out.release();
+  out.nblocks = (int)g.blocks.size();
+  out.multilevel = g.multilevel;
+  if (out.nblocks == 0) return fail(kErrInvalid, "grid has no blocks");
+  const auto &b0 = g.blocks[0];
+  for (int d = 0; d < 3; ++d) {
+    out.dims.nx[d] = b0.nx[d];
+    out.dims.N[d] = b0.nx[d] + 2 * spec.ng;
+    out.dims.Nc[d] = std::max(1, b0.nx[d] / 2) + 2 * spec.ng;
+  }
+  out.dims.ng = spec.ng;
+  for (auto &b : g.blocks)
+    for (int d = 0; d < 3; ++d)
+      if (b.nx[d] != b0.nx[d]) return fail(kErrUnsupported, "blocks of one grid must share a size");
+
+  std::vector<DevPair> pairs;
+  std::vector<DevWork> cw;
+  int64_t off = 0;
+  for (auto &p : g.pairs) {
+    DevPair d;
+    d.src_block = p.sender;
+    d.dst_block = p.receiver;
+    d.src_coarse = p.send_coarse;
+    d.dst_coarse = p.recv_coarse;
+    d.src = to_dev(p.send);
+    d.dst = to_dev(p.recv);
+    d.mask = p.recv.mask;
+    d.full_mask = mask_is_full(p.recv) ? 1 : 0;
+    d.buf_off = off;
+    off += p.send.count();
+    add_work(cw, (int)pairs.size(), d.src.n[1] * d.src.n[2], d.src.n[0]);
+    pairs.push_back(d);
+  }
+  out.buffer_elems = off;
+  out.npairs = (int)pairs.size();
+  out.ncopy_work = (int)cw.size();
+  int rc;
+  if ((rc = upload(&out.pairs, pairs)) || (rc = upload(&out.copy_work, cw))) return rc;
+
+  auto lower_regions = [&](const std::vector<CoarseRegion> &rg, DevRegion **dr, DevWork **dw, int &n,
+                           int &nw) -> int {
+    std::vector<DevRegion> r;
+    std::vector<DevWork> w;
+    for (auto &c : rg) {
+      DevRegion d;
+      d.block = c.block;
+      d.box = to_dev(c.box);
+      d.mask = c.box.mask;
+      d.full_mask = mask_is_full(c.box) ? 1 : 0;
+      add_work(w, (int)r.size(), d.box.n[1] * d.box.n[2], d.box.n[0], 1024);
+      r.push_back(d);
+    }
+    n = (int)r.size();
+    nw = (int)w.size();
+    int rc2;
+    if ((rc2 = upload(dr, r)) || (rc2 = upload(dw, w))) return rc2;
+    return kOk;
+  };
+  if ((rc = lower_regions(g.restrict_send, &out.rs, &out.rs_work, out.nrs, out.nrs_work))) return rc;
+  if ((rc = lower_regions(g.restrict_recv, &out.rr, &out.rr_work, out.nrr, out.nrr_work))) return rc;
+  if ((rc = lower_regions(g.prolong, &out.pro, &out.pro_work, out.npro, out.npro_work))) return rc;
+
+  std::vector<DevFluxCorr> fcs;
+  std::vector<DevWork> fw;
+  for (auto &f : g.flux_corr) {
+    DevFluxCorr d;
+    d.fine_block = f.fine;
+    d.coarse_block = f.coarse;
+    d.dir = f.dir;
+    d.pad = 0;
+    d.fine = to_dev(f.fine_box);
+    d.recv = to_dev(f.recv);
+    d.mask = f.recv.mask;
+    d.full_mask = mask_is_full(f.recv) ? 1 : 0;
+    add_work(fw, (int)fcs.size(), d.fine.n[1] * d.fine.n[2], d.fine.n[0], 1024);
+    fcs.push_back(d);
+  }
+  out.nfc = (int)fcs.size();
+  out.nfc_work = (int)fw.size();
+  if ((rc = upload(&out.fc, fcs)) || (rc = upload(&out.fc_work, fw))) return rc;
+
+  out.geom_h.clear();
+  for (auto &b : g.blocks) {
+    DevBlockGeom gm;
+    for (int d = 0; d < 3; ++d) {
+      gm.dx[d] = b.dx[d];
+      // uniform_cartesian.hpp:29-54: xmin_ is the face at ghost index 0
+      gm.xmin[d] = b.xmin[d] - spec.ng * b.dx[d];
+      gm.cxmin[d] = gm.xmin[d] + spec.ng * b.dx[d] * (1 - 2);
+      gm.cdx[d] = b.dx[d] * 2;
+    }
+    gm.area[0] = gm.dx[1] * gm.dx[2];
+    gm.area[1] = gm.dx[0] * gm.dx[2];
+    gm.area[2] = gm.dx[0] * gm.dx[1];
+    gm.vol = gm.dx[0] * gm.dx[1] * gm.dx[2];
+    out.geom_h.push_back(gm);
+  }
+  if ((rc = upload(&out.geom, out.geom_h))) return rc;
+  return kOk;
+}
+
+// ------------------------------------------------------------------ kernels
+namespace {
+
+__device__ __forceinline__ double *arr(double *fine, double *coarse, int c) { return c ? coarse : fine; }
+
+// Direct copy: sender slab -> receiver ghosts. grid = (work items, components)
+__global__ void __launch_bounds__(128) k_copy(const DevPair *__restrict__ pairs,
+                                              const DevWork *__restrict__ work, Dims d, int ncomp,
+                                              double *__restrict__ fine, double *__restrict__ coarse) {
+  const DevWork w = work[blockIdx.x];
+  const DevPair p = pairs[w.item];
+  const int v = blockIdx.y;
+  const double *src = arr(fine, coarse, p.src_coarse);
+  double *dst = arr(fine, coarse, p.dst_coarse);
+  for_work_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], [&](int k, int j, int i) {
+    const int dk = p.dst.lo[2] + k, dj = p.dst.lo[1] + j, di = p.dst.lo[0] + i;
+    if (!p.full_mask && !mask_active(p.mask, p.dst, dk, dj, di)) return;
+    const int sk = p.src.lo[2] + k, sj = p.src.lo[1] + j, si = p.src.lo[0] + i;
+    const int64_t s = p.src_coarse ? coarse_index(d, ncomp, p.src_block, v, sk, sj, si)
+                                   : fine_index(d, ncomp, p.src_block, v, sk, sj, si);
+    const int64_t t = p.dst_coarse ? coarse_index(d, ncomp, p.dst_block, v, dk, dj, di)
+                                   : fine_index(d, ncomp, p.dst_block, v, dk, dj, di);
+    dst[t] = __ldg(src + s);
+  });
+}
+
+// Buffered path, reference layout: buf[ncomp*buf_off + v*box + (k*nj + j)*ni + i]
+__global__ void __launch_bounds__(128) k_pack(const DevPair *__restrict__ pairs,
+                                              const DevWork *__restrict__ work, Dims d, int ncomp,
+                                              const double *__restrict__ fine,
+                                              const double *__restrict__ coarse,
+                                              double *__restrict__ buf) {
+  const DevWork w = work[blockIdx.x];
+  const DevPair p = pairs[w.item];
+  const int v = blockIdx.y;
+  const int64_t box = (int64_t)p.src.n[0] * p.src.n[1] * p.src.n[2];
+  double *b = buf + p.buf_off * ncomp + v * box;
+  for_work_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], [&](int k, int j, int i) {
+    const int sk = p.src.lo[2] + k, sj = p.src.lo[1] + j, si = p.src.lo[0] + i;
+    const int64_t s = p.src_coarse ? coarse_index(d, ncomp, p.src_block, v, sk, sj, si)
+                                   : fine_index(d, ncomp, p.src_block, v, sk, sj, si);
+    b[((int64_t)k * p.src.n[1] + j) * p.src.n[0] + i] = p.src_coarse ? coarse[s] : fine[s];
+  });
+}
+
+__global__ void __launch_bounds__(128) k_unpack(const DevPair *__restrict__ pairs,
+                                                const DevWork *__restrict__ work, Dims d, int ncomp,
+                                                double *__restrict__ fine, double *__restrict__ coarse,
+                                                const double *__restrict__ buf) {
+  const DevWork w = work[blockIdx.x];
+  const DevPair p = pairs[w.item];
+  const int v = blockIdx.y;
+  const int64_t box = (int64_t)p.src.n[0] * p.src.n[1] * p.src.n[2];
+  const double *b = buf + p.buf_off * ncomp + v * box;
+  // element m of the send box is element m of the receive box
+  for_work_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], [&](int k, int j, int i) {
+    const int64_t m = ((int64_t)k * p.src.n[1] + j) * p.src.n[0] + i;
+    const int ri = (int)(m % p.dst.n[0]);
+    const int64_t q = m / p.dst.n[0];
+    const int rj = (int)(q % p.dst.n[1]);
+    const int rk = (int)(q / p.dst.n[1]);
+    const int dk = p.dst.lo[2] + rk, dj = p.dst.lo[1] + rj, di = p.dst.lo[0] + ri;
+    if (!p.full_mask && !mask_active(p.mask, p.dst, dk, dj, di)) return;
+    const int64_t t = p.dst_coarse ? coarse_index(d, ncomp, p.dst_block, v, dk, dj, di)
+                                   : fine_index(d, ncomp, p.dst_block, v, dk, dj, di);
+    (p.dst_coarse ? coarse : fine)[t] = b[m];
+  });
+}
+
+// RestrictAverage (pr_ops.hpp:105-164): volume-weighted mean of the 2x2x2 fine cells,
+// summed in the reference's pairing order.
+__global__ void __launch_bounds__(128) k_restrict(const DevRegion *__restrict__ regs,
+                                                  const DevWork *__restrict__ work,
+                                                  const DevBlockGeom *__restrict__ geom, Dims d,
+                                                  int ncomp, const double *__restrict__ fine,
+                                                  double *__restrict__ coarse) {
+  const DevWork w = work[blockIdx.x];
+  const DevRegion r = regs[w.item];
+  const int v = blockIdx.y;
+  const double vol = geom[r.block].vol;
+  const int ng = d.ng;
+  for_work_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], [&](int k, int j, int i) {
+    const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
+    if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
+    const int fi = (ci - ng) * 2 + ng, fj = (cj - ng) * 2 + ng, fk = (ck - ng) * 2 + ng;
+    double t[2][2][2];
+#pragma unroll
+    for (int ok = 0; ok < 2; ++ok)
+#pragma unroll
+      for (int oj = 0; oj < 2; ++oj)
+#pragma unroll
+        for (int oi = 0; oi < 2; ++oi)
+          t[ok][oj][oi] = __dmul_rn(vol, fine[fine_index(d, ncomp, r.block, v, fk + ok, fj + oj, fi + oi)]);
+    const double tv = __dadd_rn(__dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)),
+                                __dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)));
+    const double num = __dadd_rn(__dadd_rn(__dadd_rn(t[0][0][0], t[0][1][0]), __dadd_rn(t[0][0][1], t[0][1][1])),
+                                 __dadd_rn(__dadd_rn(t[1][0][0], t[1][1][0]), __dadd_rn(t[1][0][1], t[1][1][1])));
+    coarse[coarse_index(d, ncomp, r.block, v, ck, cj, ci)] = __ddiv_rn(num, tv);
+  });
+}
+
+__device__ __forceinline__ double sign1(double x) { return x < 0.0 ? -1.0 : 1.0; }
+
+// ProlongateSharedGeneral (pr_ops.hpp:166-285): op 0 minmod, 1 linear, 2 constant.
+// Written with explicit round-to-nearest intrinsics so no FMA contraction changes
+// the result relative to the reference's separately rounded host arithmetic.
+__global__ void __launch_bounds__(128) k_prolong(const DevRegion *__restrict__ regs,
+                                                 const DevWork *__restrict__ work,
+                                                 const DevBlockGeom *__restrict__ geom, Dims d,
+                                                 int ncomp, double *__restrict__ fine,
+                                                 const double *__restrict__ coarse, int op) {
+  const DevWork w = work[blockIdx.x];
+  const DevRegion r = regs[w.item];
+  const int v = blockIdx.y;
+  const DevBlockGeom g = geom[r.block];
+  const int ng = d.ng;
+  for_work_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], [&](int k, int j, int i) {
+    const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
+    if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
+    const int c[3] = {ci, cj, ck};
+    const int f[3] = {(ci - ng) * 2 + ng, (cj - ng) * 2 + ng, (ck - ng) * 2 + ng};
+    const double fc = coarse[coarse_index(d, ncomp, r.block, v, ck, cj, ci)];
+    double gm[3], gp[3], dfm[3], dfp[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      auto xcc = [&](int idx) { return __dadd_rn(g.cxmin[q], __dmul_rn(__dadd_rn((double)idx, 0.5), g.cdx[q])); };
+      auto xfc = [&](int idx) { return __dadd_rn(g.xmin[q], __dmul_rn(__dadd_rn((double)idx, 0.5), g.dx[q])); };
+      const double xm = xcc(c[q] - 1), xc = xcc(c[q]), xp = xcc(c[q] + 1);
+      const double dxm = __dsub_rn(xc, xm), dxp = __dsub_rn(xp, xc);
+      dfm[q] = __dsub_rn(xc, xfc(f[q]));
+      dfp[q] = __dsub_rn(xfc(f[q] + 1), xc);
+      const int dk = q == 2, dj = q == 1, di = q == 0;
+      const double nm = coarse[coarse_index(d, ncomp, r.block, v, ck - dk, cj - dj, ci - di)];
+      const double np = coarse[coarse_index(d, ncomp, r.block, v, ck + dk, cj + dj, ci + di)];
+      const double a = __ddiv_rn(__dsub_rn(fc, nm), dxm);
+      const double b = __ddiv_rn(__dsub_rn(np, fc), dxp);
+      const double mm = __dmul_rn(__dmul_rn(0.5, __dadd_rn(sign1(a), sign1(b))), smin(fabs(a), fabs(b)));
+      gm[q] = op == 0 ? mm : (op == 1 ? a : 0.0);
+      gp[q] = op == 0 ? mm : (op == 1 ? b : 0.0);
+    }
+    const double m0 = __dmul_rn(gm[0], dfm[0]), p0 = __dmul_rn(gp[0], dfp[0]);
+    const double m1 = __dmul_rn(gm[1], dfm[1]), p1 = __dmul_rn(gp[1], dfp[1]);
+    const double m2 = __dmul_rn(gm[2], dfm[2]), p2 = __dmul_rn(gp[2], dfp[2]);
+    auto F = [&](int ok, int oj, int oi) -> double & {
+      return fine[fine_index(d, ncomp, r.block, v, f[2] + ok, f[1] + oj, f[0] + oi)];
+    };
+    F(0, 0, 0) = __dsub_rn(fc, __dadd_rn(__dadd_rn(m0, m1), m2));
+    F(0, 0, 1) = __dadd_rn(fc, __dsub_rn(__dsub_rn(p0, m1), m2));
+    F(0, 1, 0) = __dsub_rn(fc, __dadd_rn(__dsub_rn(m0, p1), m2));
+    F(0, 1, 1) = __dadd_rn(fc, __dsub_rn(__dadd_rn(p0, p1), m2));
+    F(1, 0, 0) = __dsub_rn(fc, __dsub_rn(__dadd_rn(m0, m1), p2));
+    F(1, 0, 1) = __dadd_rn(fc, __dadd_rn(__dsub_rn(p0, m1), p2));
+    F(1, 1, 0) = __dsub_rn(fc, __dsub_rn(__dsub_rn(m0, p1), p2));
+    F(1, 1, 1) = __dadd_rn(fc, __dadd_rn(__dadd_rn(p0, p1), p2));
+  });
+}
+
+// Flux correction (SendBoundBufs<flxcor_send> + SetBounds<flxcor_recv>) fused: the
+// area-weighted mean of the 2x2 fine face fluxes is written straight into the coarse
+// block's face flux. Flux arrays: [block][dir][comp][N3][N2][N1].
+__global__ void __launch_bounds__(128) k_flux_correct(const DevFluxCorr *__restrict__ fcs,
+                                                      const DevWork *__restrict__ work,
+                                                      const DevBlockGeom *__restrict__ geom, Dims d,
+                                                      int ncomp, double *__restrict__ flux) {
+  const DevWork w = work[blockIdx.x];
+  const DevFluxCorr c = fcs[w.item];
+  const int v = blockIdx.y;
+  const int ng = d.ng;
+  const double a = geom[c.fine_block].area[c.dir];
+  const int64_t plane = (int64_t)d.N[0] * d.N[1] * d.N[2];
+  auto fidx = [&](int b, int k, int j, int i) {
+    return (((int64_t)b * 3 + c.dir) * ncomp + v) * plane + ((int64_t)k * d.N[1] + j) * d.N[0] + i;
+  };
+  for_work_rows(w.row0, w.nrows, c.fine.n[0], c.fine.n[1], [&](int k, int j, int i) {
+    const int ck = c.fine.lo[2] + k, cj = c.fine.lo[1] + j, ci = c.fine.lo[0] + i;
+    const int fi = (ci - ng) * 2 + ng, fj = (cj - ng) * 2 + ng, fk = (ck - ng) * 2 + ng;
+    // the two tangential directions of the face
+    const int ti = c.dir != 0, tj = c.dir != 1, tk = c.dir != 2;
+    double t[2][2][2] = {{{0.0, 0.0}, {0.0, 0.0}}, {{0.0, 0.0}, {0.0, 0.0}}};
+    double vv[2][2][2] = {{{0.0, 0.0}, {0.0, 0.0}}, {{0.0, 0.0}, {0.0, 0.0}}};
+    for (int ok = 0; ok < 1 + tk; ++ok)
+      for (int oj = 0; oj < 1 + tj; ++oj)
+        for (int oi = 0; oi < 1 + ti; ++oi) {
+          vv[ok][oj][oi] = a;
+          t[ok][oj][oi] = __dmul_rn(a, flux[fidx(c.fine_block, fk + ok, fj + oj, fi + oi)]);
+        }
+    const double tv = __dadd_rn(__dadd_rn(__dadd_rn(vv[0][0][0], vv[0][1][0]), __dadd_rn(vv[0][0][1], vv[0][1][1])),
+                                __dadd_rn(__dadd_rn(vv[1][0][0], vv[1][1][0]), __dadd_rn(vv[1][0][1], vv[1][1][1])));
+    const double num = __dadd_rn(__dadd_rn(__dadd_rn(t[0][0][0], t[0][1][0]), __dadd_rn(t[0][0][1], t[0][1][1])),
+                                 __dadd_rn(__dadd_rn(t[1][0][0], t[1][1][0]), __dadd_rn(t[1][0][1], t[1][1][1])));
+    const double val = __ddiv_rn(num, tv);
+    // element m of the restriction box lands on element m of the receive box
+    const int64_t m = ((int64_t)k * c.fine.n[1] + j) * c.fine.n[0] + i;
+    const int ri = (int)(m % c.recv.n[0]);
+    const int64_t q = m / c.recv.n[0];
+    const int rj = (int)(q % c.recv.n[1]);
+    const int rk = (int)(q / c.recv.n[1]);
+    const int dk = c.recv.lo[2] + rk, dj = c.recv.lo[1] + rj, di = c.recv.lo[0] + ri;
+    if (!c.full_mask && !mask_active(c.mask, c.recv, dk, dj, di)) return;
+    flux[fidx(c.coarse_block, dk, dj, di)] = val;
+  });
+}
+
+}  // namespace
+
+int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate,
+                  int prolong_op, double *buffer, cudaStream_t s) {
+  if (ncomp < 1 || ncomp > 65535) return fail(kErrInvalid, "ncomp out of range");
+  if (!fine) return fail(kErrInvalid, "null field pointer");
+  if (t.multilevel && !coarse) return fail(kErrInvalid, "multilevel mesh needs a coarse buffer");
+  const dim3 blk(128);
+  if (t.multilevel && t.nrs_work)
+    k_restrict<<<dim3(t.nrs_work, ncomp), blk, 0, s>>>(t.rs, t.rs_work, t.geom, t.dims, ncomp, fine, coarse);
+  if (t.ncopy_work) {
+    if (buffer) {
+      k_pack<<<dim3(t.ncopy_work, ncomp), blk, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse, buffer);
+      k_unpack<<<dim3(t.ncopy_work, ncomp), blk, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse, buffer);
+    } else {
+      k_copy<<<dim3(t.ncopy_work, ncomp), blk, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse);
+    }
+  }
+  if (t.multilevel && t.nrr_work)
+    k_restrict<<<dim3(t.nrr_work, ncomp), blk, 0, s>>>(t.rr, t.rr_work, t.geom, t.dims, ncomp, fine, coarse);
+  if (t.multilevel && prolongate && t.npro_work)
+    k_prolong<<<dim3(t.npro_work, ncomp), blk, 0, s>>>(t.pro, t.pro_work, t.geom, t.dims, ncomp, fine, coarse,
+                                                       prolong_op);
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+int pack_grid(GridTables &t, const double *fine, const double *coarse, int ncomp, double *buffer,
+              cudaStream_t s) {
+  if (!buffer || !fine) return fail(kErrInvalid, "null pointer");
+  if (t.ncopy_work)
+    k_pack<<<dim3(t.ncopy_work, ncomp), dim3(128), 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse,
+                                                           buffer);
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s) {
+  if (!t.multilevel || !t.nfc_work) return kOk;
+  k_flux_correct<<<dim3(t.nfc_work, ncomp), dim3(128), 0, s>>>(t.fc, t.fc_work, t.geom, t.dims, ncomp, flux);
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+}  // namespace pgb

@@ -1,0 +1,49 @@
+// The library's mesh object: host topology plus its lowered device tables.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "device_tables.hpp"
+#include "topology.hpp"
+
+namespace pgb {
+
+// Device copy of one grid's tables (the leaf grid, or one multigrid level).
+struct GridTables {
+  int nblocks = 0;
+  Dims dims{};
+  bool multilevel = false;
+  int npairs = 0, ncopy_work = 0;
+  int nrs = 0, nrs_work = 0;    // send-side restriction
+  int nrr = 0, nrr_work = 0;    // receive-side restriction
+  int npro = 0, npro_work = 0;  // prolongation
+  int nfc = 0, nfc_work = 0;    // flux correction
+  int64_t buffer_elems = 0;     // sum of pair box sizes (one component)
+  DevPair *pairs = nullptr;
+  DevWork *copy_work = nullptr;
+  DevRegion *rs = nullptr, *rr = nullptr, *pro = nullptr;
+  DevWork *rs_work = nullptr, *rr_work = nullptr, *pro_work = nullptr;
+  DevFluxCorr *fc = nullptr;
+  DevWork *fc_work = nullptr;
+  DevBlockGeom *geom = nullptr;
+  std::vector<DevBlockGeom> geom_h;
+  void release();
+};
+
+struct MeshState {
+  std::unique_ptr<MeshTopology> topo;
+  GridTables leaf;
+  bool uploaded = false;
+  // device scratch owned by the mesh (reductions, status words)
+  double *d_scalars = nullptr;      // [0] dt, [1] reduction scratch ...
+  unsigned long long *d_minbits = nullptr;
+  int *d_status = nullptr;
+  ~MeshState();
+};
+
+int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out);
+
+}  // namespace pgb

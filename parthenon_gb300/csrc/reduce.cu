@@ -1,0 +1,109 @@
+// Time-step reductions and the device-side SetGlobalTimeStep.
+//
+// EstimateTimestep (src/interface/update.hpp:268-278) followed by
+// EvolutionDriver::SetGlobalTimeStep (src/driver/driver.cpp:210-232) entirely on the
+// device, so a whole RK cycle including its dt update can be replayed from a CUDA graph
+// without a host round trip. The minimum is exact: positive doubles order like their
+// bit patterns, so a warp-shuffle min followed by one 64-bit atomicMin per CTA gives
+// the same value as the reference's Kokkos::Min reduction.
+#include <cfloat>
+
+#include "common.cuh"
+#include "mesh_state.hpp"
+
+namespace pgb {
+
+namespace {
+
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__device__ __forceinline__ void block_min_to(double v, unsigned long long *out) {
+  __shared__ double sm[32];
+  v = warp_min(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (l < (int)(blockDim.x >> 5)) ? sm[l] : DBL_MAX;
+    v = warp_min(v);
+    if (l == 0) atomicMin(out, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// burgers_package.cpp:170-200: min over interior cells of 1/(|u|/dx + |v|/dy + |w|/dz),
+// evaluated with separately rounded operations in the reference's order.
+__global__ void __launch_bounds__(256) k_burgers_min(const double *__restrict__ u, const DevBlockGeom *__restrict__ geom,
+                                                     Dims d, int ncomp, int nblocks, unsigned long long *out) {
+  const int64_t ncell = (int64_t)nblocks * d.nx[0] * d.nx[1] * d.nx[2];
+  double m = DBL_MAX;
+  const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1], cs = N01 * d.N[2];
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % d.nx[0]) + d.ng;
+    int64_t r = c / d.nx[0];
+    const int j = (int)(r % d.nx[1]) + d.ng;
+    r /= d.nx[1];
+    const int k = (int)(r % d.nx[2]) + d.ng;
+    const int b = (int)(r / d.nx[2]);
+    const int64_t e = (int64_t)b * ncomp * cs + (int64_t)k * N01 + (int64_t)j * N0 + i;
+    const DevBlockGeom &g = geom[b];
+    const double s = __dadd_rn(__dadd_rn(__ddiv_rn(fabs(u[e]), g.dx[0]), __ddiv_rn(fabs(u[e + cs]), g.dx[1])),
+                               __ddiv_rn(fabs(u[e + 2 * cs]), g.dx[2]));
+    m = fmin(m, __ddiv_rn(1.0, s));
+  }
+  block_min_to(m, out);
+}
+
+// advection_package.cpp:465-494: min over blocks of dx/|v| per direction with v != 0
+__global__ void k_advection_min(const DevBlockGeom *__restrict__ geom, int nblocks, double vx, double vy, double vz,
+                                unsigned long long *out) {
+  double m = DBL_MAX;
+  const double v[3] = {vx, vy, vz};
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nblocks; b += gridDim.x * blockDim.x)
+    for (int q = 0; q < 3; ++q)
+      if (v[q] != 0.0) m = fmin(m, __ddiv_rn(geom[b].dx[q], fabs(v[q])));
+  block_min_to(m, out);
+}
+
+// driver.cpp:210-232 with the default dt controls; resets the accumulator.
+__global__ void k_set_dt(double *dt, unsigned long long *minbits, double cfl, int first) {
+  const double mn = __longlong_as_double((long long)*minbits);
+  const double newdt = __dmul_rn(cfl, mn);
+  double t = first ? DBL_MAX : *dt;
+  if (t < 0.1 * DBL_MAX) t = __dmul_rn(t, 2.0);
+  t = fmin(t, newdt);
+  t = fmax(DBL_MIN, fmin(t, DBL_MAX));
+  *dt = t;
+  *minbits = (unsigned long long)__double_as_longlong(DBL_MAX);
+}
+
+__global__ void k_reset_min(unsigned long long *minbits) {
+  *minbits = (unsigned long long)__double_as_longlong(DBL_MAX);
+}
+
+}  // namespace
+
+int estimate_dt(MeshState &m, int physics, const double *u, int ncomp, const double vel[3], double cfl,
+                double *dt, int first, cudaStream_t s) {
+  GridTables &t = m.leaf;
+  if (physics == 1) {
+    if (ncomp < 3) return fail(kErrInvalid, "Burgers needs three velocity components");
+    k_burgers_min<<<152 * 8, 256, 0, s>>>(u, t.geom, t.dims, ncomp, t.nblocks, m.d_minbits);
+  } else {
+    k_advection_min<<<1, 256, 0, s>>>(t.geom, t.nblocks, vel[0], vel[1], vel[2], m.d_minbits);
+  }
+  k_set_dt<<<1, 1, 0, s>>>(dt, m.d_minbits, cfl, first);
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+int reset_reduction(MeshState &m, cudaStream_t s) {
+  k_reset_min<<<1, 1, 0, s>>>(m.d_minbits);
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+}  // namespace pgb

@@ -1,0 +1,64 @@
+// Host launchers for one stencil build (included once by stencil_exact.cu and once by
+// stencil_fast.cu after stencil_impl.cuh).
+#pragma once
+
+namespace pgb {
+namespace PGB_NS {
+
+template <int NC, bool BURGERS>
+int launch_stage_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
+  const Dims &d = a.d;
+  auto grid_for = [&](int D) {
+    const int64_t nf = D == 0 ? d.nx[1] : d.nx[0];
+    const int64_t ns = D == 2 ? d.nx[1] : d.nx[2];
+    const int64_t lines = (int64_t)a.nblocks * nf * ns;
+    return dim3((unsigned)((lines + 127) / 128));
+  };
+  if (store_flux) {
+    k_march<NC, 0, kStoreFlux, BURGERS><<<grid_for(0), 128, 0, s>>>(a);
+    k_march<NC, 1, kStoreFlux, BURGERS><<<grid_for(1), 128, 0, s>>>(a);
+    k_march<NC, 2, kStoreFlux, BURGERS><<<grid_for(2), 128, 0, s>>>(a);
+  } else {
+    k_march<NC, 0, kStoreDu, BURGERS><<<grid_for(0), 128, 0, s>>>(a);
+    k_march<NC, 1, kAddDu, BURGERS><<<grid_for(1), 128, 0, s>>>(a);
+    k_march<NC, 2, kFinishUpdate, BURGERS><<<grid_for(2), 128, 0, s>>>(a);
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrCuda;
+}
+
+template <int NC>
+int launch_div_update_nc(const StageArgs &a, cudaStream_t s) {
+  const int64_t cells = (int64_t)a.nblocks * a.d.nx[0] * a.d.nx[1] * a.d.nx[2];
+  k_div_update<NC><<<(unsigned)((cells + 127) / 128), 128, 0, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrCuda;
+}
+
+// physics 0 = advection, 1 = Burgers; store_flux selects the multilevel path.
+int launch_stage(const StageArgs &a, int ncomp, int physics, bool store_flux, cudaStream_t s) {
+  if (physics == 1) {
+    switch (ncomp) {
+      case 4: return launch_stage_nc<4, true>(a, store_flux, s);
+      case 5: return launch_stage_nc<5, true>(a, store_flux, s);
+      case 11: return launch_stage_nc<11, true>(a, store_flux, s);
+      default: return kErrUnsupported;
+    }
+  }
+  switch (ncomp) {
+    case 1: return launch_stage_nc<1, false>(a, store_flux, s);
+    case 5: return launch_stage_nc<5, false>(a, store_flux, s);
+    default: return kErrUnsupported;
+  }
+}
+
+int launch_div_update(const StageArgs &a, int ncomp, cudaStream_t s) {
+  switch (ncomp) {
+    case 1: return launch_div_update_nc<1>(a, s);
+    case 4: return launch_div_update_nc<4>(a, s);
+    case 5: return launch_div_update_nc<5>(a, s);
+    case 11: return launch_div_update_nc<11>(a, s);
+    default: return kErrUnsupported;
+  }
+}
+
+}  // namespace PGB_NS
+}  // namespace pgb

@@ -1,0 +1,96 @@
+"""RK2 evolution driver for the advection and Burgers packages on the GPU.
+
+Mirrors EvolutionDriver::Execute + MultiStageDriverGeneric::Step
+(src/driver/driver.cpp:67-166, src/driver/multistage.hpp:39-53) for the two task
+collections on the hot path (example/advection/advection_driver.cpp:56-164 and
+benchmarks/burgers/burgers_driver.cpp:53-148): per cycle two stages, each
+fluxes -> [flux correction] -> flux divergence -> Average -> Update -> ghost exchange,
+then EstimateTimestep + SetGlobalTimeStep. Every step runs on the device; dt lives in
+device memory, so a cycle is one CUDA-graph launch.
+"""
+import ctypes
+
+from . import _native as nat
+from .mesh import _ptr, _stream
+
+
+class StageConfig:
+    """physics: 'advection' or 'burgers'; recon: 'dc'/'plm' (advection) or
+    'weno5'/'linear' (Burgers); exact: bitwise reference arithmetic instead of the
+    FMA/shared-reciprocal kernels."""
+
+    def __init__(self, physics, recon, cfl, vel=(1.0, 1.0, 1.0), exact=False):
+        self.physics = physics
+        self.recon = recon
+        self.cfl = float(cfl)
+        self.vel = tuple(float(v) for v in vel)
+        self.exact = bool(exact)
+
+    def params(self):
+        p = nat.StageParams()
+        p.physics = {"advection": 0, "burgers": 1}[self.physics]
+        rec = {"advection": {"dc": 0, "plm": 1}, "burgers": {"weno5": 0, "linear": 1}}[self.physics]
+        p.recon = rec[self.recon]
+        p.exact = 1 if self.exact else 0
+        for d in range(3):
+            p.vel[d] = self.vel[d]
+        p.cfl = self.cfl
+        return p
+
+
+class RK2Driver:
+    """Owns the device state of one run: base and stage fields, scratch, coarse
+    buffers (multilevel), and the device dt."""
+
+    def __init__(self, mesh, ncomp, config, stream=None):
+        import torch
+        self.mesh = mesh.upload() if not mesh._uploaded else mesh
+        self.ncomp = int(ncomp)
+        self.cfg = config
+        self.params = config.params()
+        self.stream = stream if stream is not None else torch.cuda.Stream()
+        with torch.cuda.stream(self.stream):
+            self.base = mesh.new_field(ncomp)
+            self.stage = mesh.new_field(ncomp)
+            if mesh.multilevel:
+                self.dudt = None
+                self.flux = torch.zeros((mesh.nblocks, 3) + tuple(self.base.shape[1:]), dtype=torch.float64,
+                                        device="cuda")
+                self.cbase = mesh.new_coarse(ncomp)
+                self.cstage = mesh.new_coarse(ncomp)
+            else:
+                self.dudt = mesh.new_field(ncomp)
+                self.flux = None
+                self.cbase = self.cstage = None
+            self.dt = torch.zeros(1, dtype=torch.float64, device="cuda")
+        self.ncycle = 0
+
+    @property
+    def prolongate(self):
+        # The Burgers task list wires Send/Receive/Set without ProlongateBounds
+        # (burgers_driver.cpp:108-120); the advection list prolongates.
+        return self.cfg.physics != "burgers"
+
+    def set_state(self, host_array):
+        """Load the initial condition (numpy, field layout incl. ghosts), fill ghosts
+        (Mesh::Initialize -> CommunicateBoundaries) and set the first dt."""
+        import torch
+        with torch.cuda.stream(self.stream):
+            self.base.copy_(torch.as_tensor(host_array, dtype=torch.float64), non_blocking=False)
+            self.mesh.exchange(self.base, self.cbase, prolongate=self.prolongate, stream=self.stream)
+            self.stage.copy_(self.base)
+            nat.check(nat.lib().pgb_estimate_dt(self.mesh.handle, ctypes.byref(self.params), _ptr(self.base),
+                                                self.ncomp, _ptr(self.dt), 1, _stream(self.stream)),
+                      "pgb_estimate_dt")
+        self.ncycle = 0
+
+    def run(self, ncycles, graph=True):
+        nat.check(nat.lib().pgb_rk2_cycles(self.mesh.handle, ctypes.byref(self.params), _ptr(self.base),
+                                           _ptr(self.stage), _ptr(self.dudt), _ptr(self.flux), _ptr(self.cbase),
+                                           _ptr(self.cstage), self.ncomp, _ptr(self.dt), int(ncycles),
+                                           1 if graph else 0, _stream(self.stream)), "pgb_rk2_cycles")
+        self.ncycle += ncycles
+
+    def zone_cycles(self, ncycles):
+        nx = self.mesh.block_nx
+        return ncycles * self.mesh.nblocks * nx[0] * nx[1] * nx[2]

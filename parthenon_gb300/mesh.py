@@ -1,0 +1,144 @@
+"""Host-side mesh handle: the Python face of the native block topology.
+
+Mirrors the parts of Parthenon's Mesh / MeshData that the hot path touches:
+block list in gid (Morton) order, per-block geometry, boundary index maps, device
+tables, and the ghost exchange (`AddBoundaryExchangeTasks` semantics). Field storage
+is a torch CUDA tensor of shape (nblocks, ncomp, N3, N2, N1) in FP64 -- PyTorch only
+provides the allocation and the stream; all work runs in the native library.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native as nat
+
+PROLONG_OPS = {"minmod": 0, "linear": 2, "constant": 4}
+
+
+def _ptr(t):
+    """Device pointer of a torch tensor (or None)."""
+    if t is None:
+        return None
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class Mesh:
+    """A single periodic octree of equal-size meshblocks.
+
+    nx, block_nx: root-grid and block cell counts (x1, x2, x3); nghost: ghost width;
+    leaves: optional list of (level, lx1, lx2, lx3) leaf locations (refined regions).
+    """
+
+    def __init__(self, nx, block_nx, nghost, xmin=(0.0, 0.0, 0.0), xmax=(1.0, 1.0, 1.0), leaves=None):
+        L = nat.lib()
+        spec = nat.MeshSpec()
+        for d in range(3):
+            spec.nx[d] = int(nx[d])
+            spec.block_nx[d] = int(block_nx[d])
+            spec.xmin[d] = float(xmin[d])
+            spec.xmax[d] = float(xmax[d])
+        spec.nghost = int(nghost)
+        lv = np.zeros((0, 4), np.int64) if leaves is None else np.ascontiguousarray(leaves, np.int64).reshape(-1, 4)
+        h = ctypes.c_void_p()
+        nat.check(L.pgb_mesh_create(ctypes.byref(spec), int(lv.shape[0]), lv.ctypes.data_as(ctypes.c_void_p),
+                                    ctypes.byref(h)), "pgb_mesh_create")
+        self._h = h
+        self.nghost = int(nghost)
+        self.block_nx = tuple(int(b) for b in block_nx)
+        info = nat.MeshInfo()
+        nat.check(L.pgb_mesh_get_info(self._h, ctypes.byref(info)), "pgb_mesh_get_info")
+        self.nblocks = info.nblocks
+        self.multilevel = bool(info.multilevel)
+        self.root_level = info.root_level
+        self.max_level = info.max_level
+        self.N = tuple(info.N)
+        self.Nc = tuple(info.Nc)
+        self.npairs = info.npairs
+        self.buffer_elems = info.buffer_elems
+        self.nflux_corr = info.nflux_corr
+        self._uploaded = False
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            nat.lib().pgb_mesh_destroy(h)
+            self._h = None
+
+    # ---------------------------------------------------------------- topology
+    def block_info(self):
+        locs = np.zeros((self.nblocks, 4), np.int64)
+        geom = np.zeros((self.nblocks, 6), np.float64)
+        nat.check(nat.lib().pgb_mesh_block_info(self._h, locs.ctypes.data_as(ctypes.c_void_p),
+                                                geom.ctypes.data_as(ctypes.c_void_p)), "pgb_mesh_block_info")
+        return locs, geom
+
+    def boundaries(self):
+        out = np.zeros((self.npairs, 23), np.int32)
+        nat.check(nat.lib().pgb_mesh_boundaries(self._h, out.ctypes.data_as(ctypes.c_void_p), self.npairs),
+                  "pgb_mesh_boundaries")
+        return out
+
+    def cell_centers(self):
+        """Per-block cell-centre coordinates including ghosts: three arrays (nblocks, N)."""
+        _, geom = self.block_info()
+        out = []
+        for d in range(3):
+            idx = np.arange(self.N[d]) - self.nghost
+            out.append(geom[:, d:d + 1] + (idx[None, :] + 0.5) * geom[:, 3 + d:4 + d])
+        return out
+
+    # ---------------------------------------------------------------- device
+    def upload(self):
+        nat.check(nat.lib().pgb_mesh_upload(self._h), "pgb_mesh_upload")
+        self._uploaded = True
+        return self
+
+    def _ensure(self):
+        if not self._uploaded:
+            self.upload()
+
+    def new_field(self, ncomp, fill=0.0):
+        import torch
+        return torch.full((self.nblocks, ncomp, self.N[2], self.N[1], self.N[0]), fill, dtype=torch.float64,
+                          device="cuda")
+
+    def new_coarse(self, ncomp, fill=0.0):
+        import torch
+        return torch.full((self.nblocks, ncomp, self.Nc[2], self.Nc[1], self.Nc[0]), fill, dtype=torch.float64,
+                          device="cuda")
+
+    def exchange(self, field, coarse=None, prolongate=True, op="minmod", buffered=False, stream=None):
+        """SendBoundBufs -> ReceiveBoundBufs -> SetBounds [-> ProlongateBounds] on all blocks."""
+        self._ensure()
+        ncomp = field.shape[1]
+        flags = (1 if prolongate else 0) | PROLONG_OPS[op]
+        buf = None
+        if buffered:
+            import torch
+            buf = torch.empty(max(1, self.buffer_elems * ncomp), dtype=torch.float64, device="cuda")
+        nat.check(nat.lib().pgb_exchange(self._h, _ptr(field), _ptr(coarse), ncomp, flags, _ptr(buf),
+                                         _stream(stream)), "pgb_exchange")
+        return buf
+
+    def pack_buffers(self, field, coarse=None, stream=None):
+        import torch
+        self._ensure()
+        ncomp = field.shape[1]
+        buf = torch.zeros(max(1, self.buffer_elems * ncomp), dtype=torch.float64, device="cuda")
+        nat.check(nat.lib().pgb_pack_buffers(self._h, _ptr(field), _ptr(coarse), ncomp, _ptr(buf), _stream(stream)),
+                  "pgb_pack_buffers")
+        return buf
+
+    def flux_correct(self, flux, ncomp, stream=None):
+        self._ensure()
+        nat.check(nat.lib().pgb_flux_correct(self._h, _ptr(flux), ncomp, _stream(stream)), "pgb_flux_correct")
+
+    @property
+    def handle(self):
+        return self._h

@@ -1,0 +1,80 @@
+"""Seeded initial conditions (problem generators) for the benchmark workloads.
+
+These stand in for the reference's ProblemGenerator functions
+(example/advection/parthenon_app_inputs.cpp:40-124,
+benchmarks/burgers/parthenon_app_inputs.cpp:40-78) with the synthetic fields the
+benchmark configurations ask for. Arrays use the field layout
+(nblocks, ncomp, N3, N2, N1); ghosts are left zero for the first exchange to fill.
+"""
+import numpy as np
+
+
+def _centers(mesh):
+    xs, ys, zs = mesh.cell_centers()
+    return xs, ys, zs
+
+
+def _interior(mesh):
+    g = mesh.nghost
+    n = mesh.block_nx
+    return (slice(g, g + n[2]), slice(g, g + n[1]), slice(g, g + n[0]))
+
+
+def gaussian(mesh, center=(0.5, 0.5, 0.5), sigma=0.1):
+    """exp(-|x - c|^2 / (2 sigma^2)) on cell centres, shape (nblocks, N3, N2, N1)."""
+    xs, ys, zs = _centers(mesh)
+    dx2 = (xs - center[0]) ** 2
+    dy2 = (ys - center[1]) ** 2
+    dz2 = (zs - center[2]) ** 2
+    r2 = dz2[:, :, None, None] + dy2[:, None, :, None] + dx2[:, None, None, :]
+    return np.exp(-r2 / (2.0 * sigma * sigma))
+
+
+def advection_state(mesh, nscalars=0, seed=3):
+    """Advected Gaussian plus `nscalars` U(0,1) scalars (seeded), interior filled."""
+    ncomp = 1 + nscalars
+    out = np.zeros((mesh.nblocks, ncomp) + tuple(mesh.N[::-1]), np.float64)
+    sk, sj, si = _interior(mesh)
+    out[:, 0, sk, sj, si] = gaussian(mesh)[:, sk, sj, si]
+    if nscalars:
+        rng = np.random.default_rng(seed)
+        n = mesh.block_nx
+        out[:, 1:, sk, sj, si] = rng.random((mesh.nblocks, nscalars, n[2], n[1], n[0]))
+    return out
+
+
+def sinusoid_modes(nmodes, kmax, seed):
+    """Per velocity component: wave vectors in {1..kmax}^3, amplitudes U(0,1), phases U(0,2pi)."""
+    rng = np.random.default_rng(seed)
+    modes = []
+    for _ in range(3):
+        k = rng.integers(1, kmax + 1, size=(nmodes, 3))
+        a = rng.random(nmodes)
+        phi = rng.random(nmodes) * 2.0 * np.pi
+        modes.append((k, a, phi))
+    return modes
+
+
+def burgers_state(mesh, nscalars=8, nmodes=8, kmax=4, seed=2):
+    """Burgers velocity as a sum of random-phase sinusoids per component plus
+    `nscalars` U(0,1) passive scalars, all seeded; interior filled."""
+    ncomp = 3 + nscalars
+    out = np.zeros((mesh.nblocks, ncomp) + tuple(mesh.N[::-1]), np.float64)
+    sk, sj, si = _interior(mesh)
+    xs, ys, zs = _centers(mesh)
+    g = mesh.nghost
+    n = mesh.block_nx
+    x = xs[:, g:g + n[0]]
+    y = ys[:, g:g + n[1]]
+    z = zs[:, g:g + n[2]]
+    for c, (k, a, phi) in enumerate(sinusoid_modes(nmodes, kmax, seed)):
+        acc = np.zeros((mesh.nblocks, n[2], n[1], n[0]))
+        for m in range(nmodes):
+            arg = (2.0 * np.pi * (k[m, 2] * z[:, :, None, None] + k[m, 1] * y[:, None, :, None] +
+                                  k[m, 0] * x[:, None, None, :]) + phi[m])
+            acc += a[m] * np.sin(arg)
+        out[:, c, sk, sj, si] = acc
+    if nscalars:
+        rng = np.random.default_rng(seed + 1000)
+        out[:, 3:, sk, sj, si] = rng.random((mesh.nblocks, nscalars, n[2], n[1], n[0]))
+    return out

@@ -1,0 +1,170 @@
+"""ctypes loader for the CPU oracle (test infrastructure).
+
+Only tests, the smoke check and the CPU-baseline leg of bench.py load this module.
+It builds oracle/liboracle.so on first use when the compiled library is missing.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB_PATH = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
+
+_lib = None
+
+I32P = ctypes.POINTER(ctypes.c_int32)
+I64P = ctypes.POINTER(ctypes.c_int64)
+DP = ctypes.POINTER(ctypes.c_double)
+U64P = ctypes.POINTER(ctypes.c_uint64)
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", ORACLE_DIR])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_sim_create.restype = ctypes.c_void_p
+        L.orc_sim_create.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_void_p,
+                                     ctypes.c_int]
+        L.orc_sim_destroy.argtypes = [ctypes.c_void_p]
+        for name in ["orc_nblocks", "orc_multilevel", "orc_num_boundaries"]:
+            getattr(L, name).argtypes = [ctypes.c_void_p]
+            getattr(L, name).restype = ctypes.c_int
+        L.orc_block_info.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        for name in ["orc_base", "orc_base_coarse"]:
+            getattr(L, name).argtypes = [ctypes.c_void_p]
+            getattr(L, name).restype = DP
+        for name in ["orc_field_size", "orc_coarse_size"]:
+            getattr(L, name).argtypes = [ctypes.c_void_p]
+            getattr(L, name).restype = ctypes.c_int64
+        L.orc_boundaries.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_exchange.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.orc_exchange.restype = ctypes.c_int64
+        L.orc_init_dt.argtypes = [ctypes.c_void_p]
+        L.orc_init_dt.restype = ctypes.c_double
+        L.orc_dt.argtypes = [ctypes.c_void_p]
+        L.orc_dt.restype = ctypes.c_double
+        L.orc_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.orc_run.restype = ctypes.c_int
+        L.orc_max_threads.restype = ctypes.c_int
+        L.orc_ownership.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.orc_ownership.restype = ctypes.c_uint32
+        L.orc_range_mask.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int]
+        L.orc_range_mask.restype = ctypes.c_uint32
+        L.orc_morton.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
+                                 ctypes.c_int64, ctypes.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class OracleSim:
+    """A Parthenon-semantics simulation on the CPU (one periodic tree)."""
+
+    def __init__(self, nx, bnx, ng, xmin=(0.0, 0.0, 0.0), xmax=(1.0, 1.0, 1.0),
+                 leaves=None, ncomp=1, physics="advection", recon=0, cfl=0.3,
+                 vel=(1.0, 1.0, 1.0), prolong_in_stage=True):
+        L = lib()
+        nx = np.asarray(nx, np.int32)
+        bnx = np.asarray(bnx, np.int32)
+        xmin = np.asarray(xmin, np.float64)
+        xmax = np.asarray(xmax, np.float64)
+        lv = np.zeros((0, 4), np.int64) if leaves is None else np.asarray(leaves, np.int64)
+        vel = np.asarray(vel, np.float64)
+        self._keep = (nx, bnx, xmin, xmax, lv, vel)
+        phys = {"advection": 0, "burgers": 1}[physics]
+        self.h = L.orc_sim_create(_ptr(nx), _ptr(bnx), int(ng), _ptr(xmin), _ptr(xmax),
+                                  int(lv.shape[0]), _ptr(lv), int(ncomp), phys, int(recon),
+                                  float(cfl), _ptr(vel), int(bool(prolong_in_stage)))
+        if not self.h:
+            raise RuntimeError("oracle mesh construction failed")
+        self.ng = int(ng)
+        self.ncomp = int(ncomp)
+        self.bnx = tuple(int(x) for x in bnx)
+        self.nblocks = L.orc_nblocks(self.h)
+        self.N = tuple(b + 2 * ng for b in self.bnx)
+        self.Nc = tuple(max(1, b // 2) + 2 * ng for b in self.bnx)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_sim_destroy(self.h)
+            self.h = None
+
+    @property
+    def multilevel(self):
+        return bool(lib().orc_multilevel(self.h))
+
+    def block_info(self):
+        locs = np.zeros((self.nblocks, 4), np.int64)
+        geom = np.zeros((self.nblocks, 6), np.float64)
+        lib().orc_block_info(self.h, _ptr(locs), _ptr(geom))
+        return locs, geom
+
+    def base(self):
+        n = lib().orc_field_size(self.h)
+        p = lib().orc_base(self.h)
+        a = np.ctypeslib.as_array(p, shape=(n,))
+        return a.reshape(self.nblocks, self.ncomp, self.N[2], self.N[1], self.N[0])
+
+    def coarse(self):
+        n = lib().orc_coarse_size(self.h)
+        p = lib().orc_base_coarse(self.h)
+        a = np.ctypeslib.as_array(p, shape=(n,))
+        return a.reshape(self.nblocks, self.ncomp, self.Nc[2], self.Nc[1], self.Nc[0])
+
+    def boundaries(self):
+        n = lib().orc_num_boundaries(self.h)
+        out = np.zeros((n, 23), np.int32)
+        lib().orc_boundaries(self.h, _ptr(out))
+        return out
+
+    def exchange(self, prolongate=True, op=0):
+        return lib().orc_exchange(self.h, int(bool(prolongate)), int(op))
+
+    def init_dt(self):
+        return lib().orc_init_dt(self.h)
+
+    def run(self, ncycles, nthreads=0):
+        dts = np.zeros(max(ncycles, 1), np.float64)
+        rc = lib().orc_run(self.h, int(ncycles), int(nthreads), _ptr(dts))
+        if rc != 0:
+            raise RuntimeError("oracle run failed")
+        return dts[:ncycles]
+
+    def dt(self):
+        return lib().orc_dt(self.h)
+
+
+def ownership(main, locs):
+    locs = np.asarray(locs, np.int64).reshape(-1, 4)
+    m = np.asarray(main, np.int64)
+    return lib().orc_ownership(_ptr(m), int(locs.shape[0]), _ptr(locs))
+
+
+def range_mask(el, own_bits, ox1, ox2, ox3):
+    return lib().orc_range_mask(int(el), int(own_bits), int(ox1), int(ox2), int(ox3))
+
+
+def morton(level, l1, l2, l3):
+    out = np.zeros(3, np.uint64)
+    lib().orc_morton(int(level), int(l1), int(l2), int(l3), _ptr(out))
+    return out
+
+
+def bit(a, b, c):
+    return 1 << ((a + 1) + 3 * (b + 1) + 9 * (c + 1))
