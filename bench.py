@@ -1,0 +1,327 @@
+"""Benchmark: zone-cycles/s of the 3-D Burgers WENO5/HLL RK2 cycle (256^3 periodic mesh,
+512 meshblocks of 32^3, 4 ghost cells, 3 velocity components + 8 passive scalars,
+FP64), plus ghost-exchange HBM GB/s on the same field.
+
+One `step` is one full RK2 cycle over every block: two stages of fluxes, flux
+divergence and update, a ghost exchange after each stage, and the device-side dt
+update. Inputs stay resident in HBM between steps (each field is 2.9 GB, far larger
+than the 129 MB L2). Prints one JSON line (rank 0).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference algorithm (the oracle,
+all host threads) on a bounded sample of the same workload: 64 meshblocks of 32^3
+with the same ghosts, components and physics, one RK2 cycle per step.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MESH_N, BLOCK_N, NGHOST, NSCALARS, CFL = 256, 32, 4, 8, 0.8
+NCOMP = 3 + NSCALARS
+SAMPLE_MESH_N = 128  # CPU sample: 64 blocks of 32^3
+METRIC = "zone-cycles/s"
+WORKLOAD = "burgers3d-weno5-hll-rk2-256^3-32^3blocks-ng4-11vars-fp64"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def fp64_peak_tflops(torch):
+    """cuBLAS DGEMM throughput on this GPU (the FP64 counterpart of the bf16 peak)."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+# Algorithmic FP64 operations per cell per stage for the Burgers stencil, counted from
+# the reference formulation (benchmarks/burgers/recon.hpp:42-99 WENO5Z, 2 per cell per
+# direction on 34/32 of the cells; burgers_package.hpp:32-43 HLL; update.hpp:42-56 and
+# 70-89 flux divergence and weighted sums). Divides count as one operation.
+WENO5Z_OPS = 115   # adds/muls/divides/abs/min/max in one WENO5Z call (both sides)
+HLL_VEL_OPS = 33   # wave speeds + 3 velocity fluxes
+HLL_SCALAR_OPS = 10
+DIVUPD_OPS = 12    # per component: 3 face differences, sum, /V, average, update
+
+
+def burgers_ops_per_cell_stage(n, nc):
+    recon = 3 * nc * WENO5Z_OPS * (n + 2) / n
+    faces = 3 * (n + 1) / n * (HLL_VEL_OPS + (nc - 3) * HLL_SCALAR_OPS)
+    return recon + faces + nc * DIVUPD_OPS
+
+
+def run_ours(args, ws, rank):
+    import torch
+    import parthenon_gb300 as pg
+    from parthenon_gb300 import _native as nat
+    from parthenon_gb300.mesh import _ptr, _stream
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    mesh = pg.Mesh((MESH_N,) * 3, (BLOCK_N,) * 3, NGHOST).upload()
+    state = pg.problems.burgers_state(mesh, nscalars=NSCALARS, nmodes=8, kmax=4, seed=2)
+    cfg = pg.StageConfig("burgers", "weno5", CFL)
+    drv = pg.RK2Driver(mesh, NCOMP, cfg)
+    drv.set_state(state)
+    s = drv.stream
+    zones = mesh.nblocks * BLOCK_N ** 3
+
+    drv.run(args.warmup, graph=True)
+    s.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        drv.run(args.steps, graph=True)
+        e1.record(s)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * args.steps * zones / (ms * 1e-3)
+
+    # --- per-kernel timing on the launching stream (CUDA events) -------------------
+    L = nat.lib()
+    p = cfg.params()
+
+    def time_calls(fn, reps):
+        fn()
+        s.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def one_stage():
+        nat.check(L.pgb_stage(mesh.handle, ctypes.byref(p), _ptr(drv.base), _ptr(drv.base), _ptr(drv.stage),
+                              _ptr(drv.dudt), None, _ptr(drv.dt), 1.0, 0.0, 1.0, NCOMP, _stream(s)), "pgb_stage")
+
+    def one_exchange():
+        mesh.exchange(drv.stage, None, prolongate=False, stream=s)
+
+    stage_ms = time_calls(one_stage, 3)
+    xchg_ms = time_calls(one_exchange, 10)
+    ghost_values = NCOMP * mesh.nblocks * ((BLOCK_N + 2 * NGHOST) ** 3 - BLOCK_N ** 3)
+    xchg_bytes = 16.0 * ghost_values  # read the sender cell, write the ghost
+    xchg_gbs = xchg_bytes / (xchg_ms * 1e-3) / 1e9
+    ops_cell = burgers_ops_per_cell_stage(BLOCK_N, NCOMP)
+    stage_flops = ops_cell * zones
+    stage_tflops = stage_flops / (stage_ms * 1e-3) / 1e12
+    fp64_peak = fp64_peak_tflops(torch)
+    peaks, peak_src = measured_peaks()
+
+    # --- end-to-end through the C ABI with host buffers ----------------------------
+    host_in = torch.from_numpy(state).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    dt_h = ctypes.c_double(0.0)
+    e2e_steps = args.steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nat.check(L.pgb_run_host(mesh.handle, ctypes.byref(p), ctypes.c_void_p(host_in.data_ptr()),
+                             ctypes.c_void_p(host_out.data_ptr()), NCOMP, e2e_steps, ctypes.byref(dt_h)),
+              "pgb_run_host")
+    e2e_s = time.perf_counter() - t0
+    nbytes = state.nbytes
+    e2e = {"value": ws * e2e_steps * zones / e2e_s, "unit": METRIC, "h2d_bytes_per_step": nbytes / e2e_steps,
+           "d2h_bytes_per_step": nbytes / e2e_steps, "steps": e2e_steps,
+           "note": "pgb_run_host: H2D of the initial field, ghost fill, K cycles, D2H of the result"}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "mesh": [MESH_N] * 3, "block": [BLOCK_N] * 3, "nblocks": mesh.nblocks,
+                   "nghost": NGHOST, "ncomp": NCOMP, "recon": "weno5", "riemann": "hll", "integrator": "rk2",
+                   "cfl": CFL, "l2": "inputs larger than L2 (2.9 GB per field)",
+                   "parallelism": "replicas" if ws > 1 else "single-gpu"},
+        "roofline": {"kernel": "burgers_stage (3 directional march launches)", "bound": "fp64",
+                     "achieved": stage_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": stage_tflops / fp64_peak, "traffic": None,
+                     "peak_source": "cuBLAS DGEMM measured in this run",
+                     "ops_per_cell_stage": ops_cell, "stage_ms": stage_ms},
+        "exchange_roofline": {"kernel": "ghost exchange (direct copy)", "bound": "hbm", "achieved": xchg_gbs,
+                              "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": xchg_gbs / peaks["hbm_gbs"],
+                              "traffic": None, "bytes_per_launch": xchg_bytes, "ms": xchg_ms,
+                              "peak_source": peak_src},
+        "ghost_exchange_gbs": xchg_gbs,
+        "e2e": e2e,
+        "gpu_launches": 10 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and ws == 1:
+        out["cpu_baseline"] = cpu_baseline(steps=1)
+    return out
+
+
+def cpu_baseline(steps):
+    """Oracle (CPU restatement of the reference) on all host threads, bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    import parthenon_gb300 as pg
+
+    mesh = pg.Mesh((SAMPLE_MESH_N,) * 3, (BLOCK_N,) * 3, NGHOST)
+    state = pg.problems.burgers_state(mesh, nscalars=NSCALARS, nmodes=8, kmax=4, seed=2)
+    o = O.OracleSim((SAMPLE_MESH_N,) * 3, (BLOCK_N,) * 3, NGHOST, ncomp=NCOMP, physics="burgers", recon=0,
+                    cfl=CFL, prolong_in_stage=False)
+    o.base()[:] = state
+    o.exchange(False, 0)
+    o.init_dt()
+    threads = O.lib().orc_max_threads()
+    t0 = time.perf_counter()
+    o.run(steps, nthreads=threads)
+    dt = time.perf_counter() - t0
+    zones = mesh.nblocks * BLOCK_N ** 3
+    return {"value": steps * zones / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "%d RK2 cycle(s) of %d meshblocks of 32^3 (128^3 mesh), same physics" % (steps, mesh.nblocks)}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    cb_steps = []
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    for _ in range(max(args.warmup, 0)):
+        pass
+    total = 0.0
+    zones_total = 0
+    res = None
+    for _ in range(args.steps):
+        res = cpu_baseline(steps=1)
+        cb_steps.append(res["value"])
+    value = float(np.median(cb_steps))
+    res["value"] = value
+    return {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "sample": res["sample"]},
+        "cpu_baseline": res,
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    ws, rank = _dist()
+    if ws > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        out = run_reference(args, ws, rank)
+    else:
+        out = run_ours(args, ws, rank)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if ws > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

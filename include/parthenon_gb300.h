@@ -92,6 +92,11 @@ int pgb_mesh_block_info(const pgb_mesh *mesh, int64_t *locs, double *geom);
  * Replaces the BndInfo index ranges (src/bvals/comms/bnd_info.cpp:273-340). */
 int pgb_mesh_boundaries(const pgb_mesh *mesh, int32_t *out, int32_t capacity);
 
+/* Host-only check that every device access the lowered tables imply (boundary
+ * boxes, restriction reads, prolongation stencils, flux-correction faces) stays inside
+ * the block arrays; pgb_mesh_upload runs the same check before any upload. */
+int pgb_mesh_validate(const pgb_mesh *mesh);
+
 /* Lower the topology to device tables (needs a GPU); call once per mesh/remesh.
  * Replaces RebuildBufferCache (src/bvals/comms/bvals_utils.hpp:212-245). */
 int pgb_mesh_upload(pgb_mesh *mesh);

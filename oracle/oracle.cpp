@@ -855,6 +855,17 @@ int orc_run(void *h, int ncycles, int nthreads, double *dts) {
 }
 
 double orc_dt(void *h) { return ((Sim *)h)->dt; }
+
+// Pack every boundary of the base field into `out` in record order (the reference
+// buffer layout: per boundary, components outermost, then k, j, i of the send box).
+int64_t orc_pack(void *h, double *out) {
+  Sim *s = (Sim *)h;
+  int64_t n = 0;
+  for (auto &br : s->recs)
+    for (int v = 0; v < s->ncomp; ++v)
+      for_box(br.send, [&](int k, int j, int i) { out[n++] = s->base.any(br.send_coarse, br.sender, v, k, j, i); });
+  return n;
+}
 int orc_max_threads() { return omp_get_max_threads(); }
 
 // Known-answer hooks for the reference unit tests (test_logical_location.cpp):

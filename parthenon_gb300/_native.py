@@ -42,6 +42,7 @@ _SIGNATURES = {
     "pgb_mesh_block_info": [VP, VP, VP],
     "pgb_mesh_boundaries": [VP, VP, ctypes.c_int32],
     "pgb_mesh_upload": [VP],
+    "pgb_mesh_validate": [VP],
     "pgb_exchange": [VP, VP, VP, ctypes.c_int32, ctypes.c_int32, VP, VP],
     "pgb_pack_buffers": [VP, VP, VP, ctypes.c_int32, VP, VP],
     "pgb_flux_correct": [VP, VP, ctypes.c_int32, VP],

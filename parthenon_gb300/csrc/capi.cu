@@ -228,6 +228,12 @@ int pgb_mesh_boundaries(const pgb_mesh *m, int32_t *out, int32_t capacity) {
   return kOk;
 }
 
+int pgb_mesh_validate(const pgb_mesh *m) {
+  if (!m) return fail(kErrInvalid, "null argument");
+  GridTables scratch;
+  return lower_grid(m->st.topo->leaf(), m->st.topo->spec(), scratch, true);
+}
+
 int pgb_mesh_upload(pgb_mesh *m) {
   if (!m) return fail(kErrInvalid, "null argument");
   int rc = lower_grid(m->st.topo->leaf(), m->st.topo->spec(), m->st.leaf);

@@ -61,12 +61,41 @@ void add_work(std::vector<DevWork> &w, int item, int rows, int ni, int target = 
   for (int r = 0; r < rows; r += per) w.push_back({item, r, std::min(per, rows - r), 0});
 }
 
+thread_local bool g_dry_run = false;  // validate tables without touching the device
+
 template <class T>
 int upload(T **dptr, const std::vector<T> &h) {
-  if (h.empty()) return kOk;
+  if (h.empty() || g_dry_run) return kOk;
   PGB_CUDA(cudaMalloc((void **)dptr, h.size() * sizeof(T)));
   PGB_CUDA(cudaMemcpy(*dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
   return kOk;
+}
+
+// Host-side bounds proof for every device access a table entry implies; a table that
+// fails is rejected before any kernel can touch memory outside the field arrays.
+bool box_inside(const DevBox &b, const int32_t ext[3]) {
+  for (int q = 0; q < 3; ++q)
+    if (b.n[q] < 1 || b.lo[q] < 0 || b.lo[q] + b.n[q] > ext[q]) return false;
+  return true;
+}
+
+// Fine cells read by restricting coarse box b (2x2x2 per coarse cell).
+bool restrict_reads_inside(const DevBox &b, int ng, const int32_t N[3]) {
+  for (int q = 0; q < 3; ++q) {
+    const int lo = (b.lo[q] - ng) * 2 + ng, hi = (b.lo[q] + b.n[q] - 1 - ng) * 2 + ng + 1;
+    if (lo < 0 || hi >= N[q]) return false;
+  }
+  return true;
+}
+
+// Prolongation of coarse box b reads coarse cells +-1 and writes fine cells 2c, 2c+1.
+bool prolong_inside(const DevBox &b, int ng, const int32_t N[3], const int32_t Nc[3]) {
+  for (int q = 0; q < 3; ++q) {
+    if (b.lo[q] - 1 < 0 || b.lo[q] + b.n[q] + 1 > Nc[q]) return false;
+    const int lo = (b.lo[q] - ng) * 2 + ng, hi = (b.lo[q] + b.n[q] - 1 - ng) * 2 + ng + 1;
+    if (lo < 0 || hi >= N[q]) return false;
+  }
+  return true;
 }
 
 }  // namespace
@@ -91,8 +120,17 @@ MeshState::~MeshState() {
   if (d_status) cudaFree(d_status);
 }
 
-int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out) {
-  out.release();
+int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out);
+
+int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out, bool dry_run) {
+  g_dry_run = dry_run;
+  const int rc = lower_grid_impl(g, spec, out);
+  g_dry_run = false;
+  return rc;
+}
+
+int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out) {
+  if (!g_dry_run) out.release();
   out.nblocks = (int)g.blocks.size();
   out.multilevel = g.multilevel;
   if (out.nblocks == 0) return fail(kErrInvalid, "grid has no blocks");
@@ -122,6 +160,10 @@ int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out) {
     d.full_mask = mask_is_full(p.recv) ? 1 : 0;
     d.buf_off = off;
     off += p.send.count();
+    const int32_t *se = p.send_coarse ? out.dims.Nc : out.dims.N;
+    const int32_t *de = p.recv_coarse ? out.dims.Nc : out.dims.N;
+    if (!box_inside(d.src, se) || !box_inside(d.dst, de))
+      return fail(kErrInvalid, "boundary box outside the block arrays");
     add_work(cw, (int)pairs.size(), d.src.n[1] * d.src.n[2], d.src.n[0]);
     pairs.push_back(d);
   }
@@ -132,7 +174,7 @@ int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out) {
   if ((rc = upload(&out.pairs, pairs)) || (rc = upload(&out.copy_work, cw))) return rc;
 
   auto lower_regions = [&](const std::vector<CoarseRegion> &rg, DevRegion **dr, DevWork **dw, int &n,
-                           int &nw) -> int {
+                           int &nw, bool prolongation) -> int {
     std::vector<DevRegion> r;
     std::vector<DevWork> w;
     for (auto &c : rg) {
@@ -141,6 +183,9 @@ int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out) {
       d.box = to_dev(c.box);
       d.mask = c.box.mask;
       d.full_mask = mask_is_full(c.box) ? 1 : 0;
+      if (!box_inside(d.box, out.dims.Nc) || !restrict_reads_inside(d.box, spec.ng, out.dims.N) ||
+          (prolongation && !prolong_inside(d.box, spec.ng, out.dims.N, out.dims.Nc)))
+        return fail(kErrInvalid, "restriction/prolongation region outside the block arrays");
       add_work(w, (int)r.size(), d.box.n[1] * d.box.n[2], d.box.n[0], 1024);
       r.push_back(d);
     }
@@ -150,9 +195,9 @@ int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out) {
     if ((rc2 = upload(dr, r)) || (rc2 = upload(dw, w))) return rc2;
     return kOk;
   };
-  if ((rc = lower_regions(g.restrict_send, &out.rs, &out.rs_work, out.nrs, out.nrs_work))) return rc;
-  if ((rc = lower_regions(g.restrict_recv, &out.rr, &out.rr_work, out.nrr, out.nrr_work))) return rc;
-  if ((rc = lower_regions(g.prolong, &out.pro, &out.pro_work, out.npro, out.npro_work))) return rc;
+  if ((rc = lower_regions(g.restrict_send, &out.rs, &out.rs_work, out.nrs, out.nrs_work, false))) return rc;
+  if ((rc = lower_regions(g.restrict_recv, &out.rr, &out.rr_work, out.nrr, out.nrr_work, false))) return rc;
+  if ((rc = lower_regions(g.prolong, &out.pro, &out.pro_work, out.npro, out.npro_work, true))) return rc;
 
   std::vector<DevFluxCorr> fcs;
   std::vector<DevWork> fw;
@@ -166,6 +211,8 @@ int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out) {
     d.recv = to_dev(f.recv);
     d.mask = f.recv.mask;
     d.full_mask = mask_is_full(f.recv) ? 1 : 0;
+    if (!box_inside(d.recv, out.dims.N) || !restrict_reads_inside(d.fine, spec.ng, out.dims.N))
+      return fail(kErrInvalid, "flux-correction region outside the flux arrays");
     add_work(fw, (int)fcs.size(), d.fine.n[1] * d.fine.n[2], d.fine.n[0], 1024);
     fcs.push_back(d);
   }

@@ -44,6 +44,6 @@ struct MeshState {
   ~MeshState();
 };
 
-int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out);
+int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out, bool dry_run = false);
 
 }  // namespace pgb

@@ -58,6 +58,8 @@ def lib():
         L.orc_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.orc_run.restype = ctypes.c_int
         L.orc_max_threads.restype = ctypes.c_int
+        L.orc_pack.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_pack.restype = ctypes.c_int64
         L.orc_ownership.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.orc_ownership.restype = ctypes.c_uint32
         L.orc_range_mask.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
@@ -148,6 +150,13 @@ class OracleSim:
 
     def dt(self):
         return lib().orc_dt(self.h)
+
+    def pack(self):
+        total = int(self.boundaries()[:, 18].sum()) * self.ncomp
+        out = np.zeros(max(total, 1), np.float64)
+        n = lib().orc_pack(self.h, _ptr(out))
+        assert n == total
+        return out[:total]
 
 
 def ownership(main, locs):

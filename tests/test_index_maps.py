@@ -28,6 +28,9 @@ def test_index_maps_match_oracle(name, nx, bnx, ng, leaves):
     assert np.array_equal(bo, bp)
     # every pair moves the same number of values on both sides
     assert (bp[:, 18] > 0).all()
+    # every device access implied by the lowered tables stays inside the arrays
+    from parthenon_gb300 import _native
+    _native.check(_native.lib().pgb_mesh_validate(m.handle), "pgb_mesh_validate")
 
 
 def test_c3_block_counts():
