@@ -147,7 +147,7 @@ def run_ours(args, ws, rank):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    mesh = pg.Mesh((MESH_N,) * 3, (BLOCK_N,) * 3, NGHOST).upload()
+    mesh = pg.Mesh((args.mesh,) * 3, (BLOCK_N,) * 3, NGHOST).upload()
     state = pg.problems.burgers_state(mesh, nscalars=NSCALARS, nmodes=8, kmax=4, seed=2)
     cfg = pg.StageConfig("burgers", "weno5", CFL)
     drv = pg.RK2Driver(mesh, NCOMP, cfg)
@@ -177,6 +177,9 @@ def run_ours(args, ws, rank):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * args.steps * zones / (ms * 1e-3)
+    if args.no_extras:
+        return {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "mesh": args.mesh}
 
     # --- per-kernel timing on the launching stream (CUDA events) -------------------
     L = nat.lib()
@@ -231,7 +234,7 @@ def run_ours(args, ws, rank):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "mesh": [MESH_N] * 3, "block": [BLOCK_N] * 3, "nblocks": mesh.nblocks,
+        "config": {"workload": WORKLOAD, "mesh": [args.mesh] * 3, "block": [BLOCK_N] * 3, "nblocks": mesh.nblocks,
                    "nghost": NGHOST, "ncomp": NCOMP, "recon": "weno5", "riemann": "hll", "integrator": "rk2",
                    "cfl": CFL, "l2": "inputs larger than L2 (2.9 GB per field)",
                    "parallelism": "replicas" if ws > 1 else "single-gpu"},
@@ -307,6 +310,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mesh", type=int, default=MESH_N, help="cells per direction (profiling runs use 128)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the per-kernel timing, end-to-end and CPU-baseline legs (profiling runs)")
     args = ap.parse_args()
     ws, rank = _dist()
     if ws > 1:

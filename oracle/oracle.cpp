@@ -812,7 +812,7 @@ void orc_boundaries(void *h, int32_t *out) {
     o[9] = br.send_coarse;
     o[16] = br.recv_coarse;
     o[17] = (int32_t)br.recv.mask.bits();
-    o[18] = (int32_t)(br.send.size() * s->ncomp);
+    o[18] = (int32_t)br.send.size();
     o[19] = o[20] = o[21] = o[22] = 0;
   }
 }
