@@ -1,0 +1,250 @@
+// Burgers WENO5/HLL directional kernel, fast build (included by stencil_fast.cu).
+//
+// A CTA owns 32 lines of cells along direction D (fixed transverse indices) and all NC
+// components: warp v marches component v, lane l marches line l. The warp of the
+// normal velocity component (v == D) goes first: it reconstructs the normal velocity
+// and turns every face into the four HLL coefficients shared by all components
+//   a = sr*upl, b = sl*upr, c = sl*sr, is = 1/(sr - sl + [sl*sr == 0])
+// (burgers_package.hpp:32-43, burgers_package.cpp:328-333), kept in shared memory; the
+// other warps then march their component, form F = (a L - b R + c (R - L)) * is (times
+// 1/2 for velocities) and emit flux differences. Per face the wave speeds and their
+// reciprocal are therefore computed once, not once per component.
+//
+// Along a line consecutive cells share most of the WENO5-Z stencil: the second
+// differences q[j-1] - 2 q[j] + q[j+1] of the smoothness indicators and two of the six
+// candidate polynomials of cell p equal quantities of cell p-1, so each step computes
+// only the new ones. The FP64 pipe bounds this kernel; every saved instruction counts.
+#pragma once
+
+namespace pgb {
+namespace fast {
+
+// One Newton-Raphson step on the hardware reciprocal seed (relative error ~1e-6 ->
+// ~1e-12): enough where the value only sets a nonlinear weight, not a magnitude.
+__device__ __forceinline__ double recip1(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+
+// min of two non-negative, non-NaN doubles through their bit patterns (integer pipe).
+__device__ __forceinline__ double min_nonneg(double a, double b) {
+  return __double_as_longlong(a) < __double_as_longlong(b) ? a : b;
+}
+
+// Incremental WENO5-Z state of one line: window q[p-2..p+2] plus carried terms.
+struct WenoLine {
+  double q0, q1, q2, q3, q4;  // q[p-2] .. q[p+2]
+  double d2a, d2b;            // second differences at p-1 and p
+  double t2a, t2b;            // (13/3) * d2^2 at p-1 and p
+  double p2l_prev, p1l_prev;  // candidate polynomials of cell p-1 reused at cell p
+  double dm;                  // q[p] - q[p-1]
+};
+
+__device__ __forceinline__ void weno_prime(WenoLine &w) {
+  constexpr double tt = 13.0 / 3.0;
+  constexpr double c10 = -1.0 / 6.0, c11 = 5.0 / 6.0, c12 = 1.0 / 3.0;
+  constexpr double c20 = 1.0 / 3.0, c21 = 5.0 / 6.0, c22 = -1.0 / 6.0;
+  // quantities of cell p-1 (window shifted by one to the left: q[p-3]..q[p+1] is not
+  // available, so compute what cell p needs from cell p-1 directly)
+  w.d2a = w.q0 - 2.0 * w.q1 + w.q2;  // at p-1
+  w.d2b = w.q1 - 2.0 * w.q2 + w.q3;  // at p
+  w.t2a = tt * w.d2a * w.d2a;
+  w.t2b = tt * w.d2b * w.d2b;
+  // cell p-1 has window q[p-3..p+1]; its P2L uses q[p-1], q[p], q[p+1] and its P1L uses
+  // q[p-2], q[p-1], q[p]
+  w.p2l_prev = c20 * w.q1 + c21 * w.q2 + c22 * w.q3;
+  w.p1l_prev = c10 * w.q0 + c11 * w.q1 + c12 * w.q2;
+  w.dm = w.q2 - w.q1;
+}
+
+// Reconstruct cell p from the window; then the caller shifts in q[p+3].
+__device__ __forceinline__ void weno_step(WenoLine &w, double &ql, double &qr) {
+  constexpr double c00 = 1.0 / 3.0, c01 = -7.0 / 6.0, c02 = 11.0 / 6.0;
+  constexpr double c10 = -1.0 / 6.0, c11 = 5.0 / 6.0, c12 = 1.0 / 3.0;
+  constexpr double c20 = 1.0 / 3.0, c21 = 5.0 / 6.0, c22 = -1.0 / 6.0;
+  constexpr double g0 = 0.1, g1 = 0.6, g2 = 0.3;
+  constexpr double eps = kWenoEps;
+  constexpr double tt = 13.0 / 3.0;
+  const double q0 = w.q0, q1 = w.q1, q2 = w.q2, q3 = w.q3, q4 = w.q4;
+  // smoothness indicators (second differences carried along the line)
+  const double d2c = q2 - 2.0 * q3 + q4;  // at p+1
+  const double t2c = tt * d2c * d2c;
+  const double b0 = q0 - 4.0 * q1 + 3.0 * q2;
+  const double b1 = q3 - q1;
+  const double b2 = q4 - 4.0 * q3 + 3.0 * q2;
+  const double be0 = fma(b0, b0, w.t2a) + eps;
+  const double be1 = fma(b1, b1, w.t2b) + eps;
+  const double be2 = fma(b2, b2, t2c) + eps;
+  const double tau5 = fabs(be2 - be0);
+  // 1 + tau / be_i with one shared reciprocal
+  const double p01 = be0 * be1;
+  const double rb = recip1(p01 * be2);
+  const double B0 = fma(tau5, (be1 * be2) * rb, 1.0);
+  const double B1 = fma(tau5, (be0 * be2) * rb, 1.0);
+  const double B2 = fma(tau5, p01 * rb, 1.0);
+  const double l0 = fma(g0, B0, eps), l1 = fma(g1, B1, eps), l2 = fma(g2, B2, eps);
+  const double r0 = fma(g0, B2, eps), r2 = fma(g2, B0, eps);  // r1 == l1
+  const double SL = l0 + l1 + l2, SR = r0 + l1 + r2;
+  const double l01 = l0 * l1, r01 = r0 * l1;
+  const double DL = fma(g2, l01, fma(g1, l0 * l2, g0 * (l1 * l2)));
+  const double DR = fma(g2, r01, fma(g1, r0 * r2, g0 * (l1 * r2)));
+  const double SS = SL * SR, DD = DL * DR;
+  const double rr = recip(SS * DD);  // normalisations: full precision
+  const double DDr = DD * rr, SSr = SS * rr;
+  const double wsL = SR * DDr, wsR = SL * DDr;
+  const double iDL = DR * SSr, iDR = DL * SSr;
+  // candidate polynomials; P1R(p) = P2L(p-1) and P2R(p) = P1L(p-1)
+  const double p0l = c00 * q0 + c01 * q1 + c02 * q2;
+  const double p1l = c10 * q1 + c11 * q2 + c12 * q3;
+  const double p2l = c20 * q2 + c21 * q3 + c22 * q4;
+  const double p0r = c00 * q4 + c01 * q3 + c02 * q2;
+  const double xl = (l0 * p0l + l1 * p1l + l2 * p2l) * wsL;
+  const double xr = (r0 * p0r + l1 * w.p2l_prev + r2 * w.p1l_prev) * wsR;
+  const double al = fma(3.0 * wsL * l01 * l2, iDL, eps);
+  const double ar = fma(3.0 * wsR * r01 * r2, iDR, eps);
+  // MC slope: dq = 0.5 mc(dm, dp) = sign(s) min(|s|/4, min(|dm|, |dp|)) when dm dp > 0
+  const double dm = w.dm, dp = q3 - q2;
+  const long long sdm = __double_as_longlong(dm), sdp = __double_as_longlong(dp);
+  const bool same = ((sdm ^ sdp) >= 0) && ((sdm << 1) != 0) && ((sdp << 1) != 0);
+  const double s = dm + dp;
+  const double mag = min_nonneg(0.25 * fabs(s), min_nonneg(fabs(dm), fabs(dp)));
+  const double dq = same ? copysign(mag, s) : 0.0;
+  const double alin = 2.0 * al * ar * recip1(al + ar);
+  const double om = 1.0 - alin;
+  ql = fma(alin, xl, om * (q2 + dq));
+  qr = fma(alin, xr, om * (q2 - dq));
+  // carry to cell p+1
+  w.d2a = w.d2b;
+  w.d2b = d2c;
+  w.t2a = w.t2b;
+  w.t2b = t2c;
+  w.p2l_prev = p2l;
+  w.p1l_prev = p1l;
+  w.dm = dp;
+}
+
+__device__ __forceinline__ void weno_shift(WenoLine &w, double qnew) {
+  w.q0 = w.q1;
+  w.q1 = w.q2;
+  w.q2 = w.q3;
+  w.q3 = w.q4;
+  w.q4 = qnew;
+}
+
+template <int NC, int D, int MODE>
+__global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a) {
+  extern __shared__ double coef[];  // [4][n+1][32]
+  const Dims d = a.d;
+  const int ng = d.ng;
+  const int n = D == 0 ? d.nx[0] : (D == 1 ? d.nx[1] : d.nx[2]);
+  const int n_fast = D == 0 ? d.nx[1] : d.nx[0];
+  const int n_slow = D == 2 ? d.nx[1] : d.nx[2];
+  const int lane = threadIdx.x & 31;
+  const int v = threadIdx.x >> 5;
+  const int64_t line = (int64_t)blockIdx.x * 32 + lane;
+  const int64_t nlines = (int64_t)a.nblocks * n_fast * n_slow;
+  const bool live = line < nlines;
+  const int64_t ln = live ? line : 0;
+  const int t0 = (int)(ln % n_fast);
+  const int64_t r = ln / n_fast;
+  const int t1 = (int)(r % n_slow);
+  const int b = (int)(r / n_slow);
+  int i0, j0, k0;
+  if (D == 0) {
+    i0 = ng; j0 = ng + t0; k0 = ng + t1;
+  } else if (D == 1) {
+    i0 = ng + t0; j0 = ng; k0 = ng + t1;
+  } else {
+    i0 = ng + t0; j0 = ng + t1; k0 = ng;
+  }
+  const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1];
+  const int64_t cs = N01 * d.N[2];
+  const int64_t step = D == 0 ? 1 : (D == 1 ? N0 : N01);
+  const int64_t c0 = (int64_t)b * NC * cs + (int64_t)k0 * N01 + (int64_t)j0 * N0 + i0;
+  const DevBlockGeom &g = a.geom[b];
+  const double area = g.area[D];
+  const int nf = n + 1;
+  double *ca = coef, *cb = coef + nf * 32, *cc = coef + 2 * nf * 32, *ci = coef + 3 * nf * 32;
+
+  auto emit = [&](int64_t e, double du) {
+    if (MODE == kStoreDu) {
+      a.dudt[e] = du;
+    } else if (MODE == kAddDu) {
+      a.dudt[e] = a.dudt[e] + du;
+    } else {
+      if (MODE == kFinishUpdate) du = a.dudt[e] + du;
+      const double dudt = -du / g.vol;
+      const double avg = a.w_in * __ldg(a.u_in + e) + a.w_base * __ldg(a.u_base + e);
+      a.u_out[e] = 1.0 * avg + (a.beta * a.dt[0]) * dudt;
+    }
+  };
+
+  // march component `comp` of this lane's line; `phase1` builds the face coefficients
+  auto march = [&](int comp, bool phase1) {
+    const double *__restrict__ u = a.u_in + c0 + (int64_t)comp * cs;
+    WenoLine w;
+    w.q0 = __ldg(u - 3 * step);
+    w.q1 = __ldg(u - 2 * step);
+    w.q2 = __ldg(u - step);
+    w.q3 = __ldg(u);
+    w.q4 = __ldg(u + step);
+    weno_prime(w);  // window now centred on cell p = -1
+    const double half = comp < 3 ? 0.5 : 1.0;
+    double lprev = 0.0, afprev = 0.0;
+    for (int p = -1; p <= n; ++p) {
+      double ql, qr;
+      weno_step(w, ql, qr);
+      if (p < n) weno_shift(w, __ldg(u + (int64_t)(p + 3) * step));
+      if (p >= 0) {
+        double F;
+        const int fi = p * 32 + lane;
+        if (phase1) {
+          const double upl = lprev, upr = qr;
+          const double sl = fmin(fmin(upl, upr), 0.0);
+          const double sr = fmax(fmax(upl, upr), 0.0);
+          const double flag = (sl * sr == 0.0) ? 1.0 : 0.0;
+          const double is = recip(sr - sl + flag);
+          const double ka = sr * upl, kb = sl * upr, kc = sl * sr;
+          ca[fi] = ka;
+          cb[fi] = kb;
+          cc[fi] = kc;
+          ci[fi] = is;
+          F = (ka * upl - kb * upr + kc * (upr - upl)) * (0.5 * is);
+        } else {
+          F = (ca[fi] * lprev - cb[fi] * qr + cc[fi] * (qr - lprev)) * (half * ci[fi]);
+        }
+        const double af = area * F;
+        if (p >= 1 && live) emit(c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step, af - afprev);
+        afprev = af;
+      }
+      lprev = ql;
+    }
+  };
+
+  if (v == D) march(D, true);
+  __syncthreads();
+  if (v != D) march(v, false);
+}
+
+template <int NC>
+int launch_burgers_nc(const StageArgs &a, cudaStream_t s) {
+  const Dims &d = a.d;
+  auto go = [&](auto kern, int D) {
+    const int n = D == 0 ? d.nx[0] : (D == 1 ? d.nx[1] : d.nx[2]);
+    const int64_t nf = D == 0 ? d.nx[1] : d.nx[0];
+    const int64_t ns = D == 2 ? d.nx[1] : d.nx[2];
+    const int64_t lines = (int64_t)a.nblocks * nf * ns;
+    const size_t smem = 4 * (size_t)(n + 1) * 32 * sizeof(double);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    kern<<<(unsigned)((lines + 31) / 32), 32 * NC, smem, s>>>(a);
+  };
+  go(k_burgers_dir<NC, 0, kStoreDu>, 0);
+  go(k_burgers_dir<NC, 1, kAddDu>, 1);
+  go(k_burgers_dir<NC, 2, kFinishUpdate>, 2);
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrCuda;
+}
+
+}  // namespace fast
+}  // namespace pgb
