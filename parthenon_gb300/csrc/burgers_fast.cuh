@@ -133,74 +133,90 @@ __device__ __forceinline__ void weno_shift(WenoLine &w, double qnew) {
   w.q4 = qnew;
 }
 
+// Named CTA barriers (ids 1..4; 0 is __syncthreads): the producer warp arrives on
+// FULL[buf] once the coefficients of a line group are in shared memory and waits on
+// EMPTY[buf] before overwriting them; consumer warps do the mirror image. Every warp
+// runs the same number of loop trips, so arrivals and waits always pair up.
+__device__ __forceinline__ void bar_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(int id, int count) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// Persistent, warp-specialised launch. Warp 0 (producer) marches the normal velocity
+// of line group g into coefficient buffer g % 2; warps 1..NC-1 (consumers) march the
+// other components of the group in the other buffer's wake, so coefficient building
+// overlaps the flux work of the previous group.
 template <int NC, int D, int MODE>
-__global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a) {
-  extern __shared__ double coef[];  // [4][n+1][32]
+__global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t ngroups) {
+  extern __shared__ double coef_all[];  // [2][4][n+1][32]
   const Dims d = a.d;
   const int ng = d.ng;
   const int n = D == 0 ? d.nx[0] : (D == 1 ? d.nx[1] : d.nx[2]);
   const int n_fast = D == 0 ? d.nx[1] : d.nx[0];
   const int n_slow = D == 2 ? d.nx[1] : d.nx[2];
   const int lane = threadIdx.x & 31;
-  const int v = threadIdx.x >> 5;
-  const int64_t line = (int64_t)blockIdx.x * 32 + lane;
+  const int w = threadIdx.x >> 5;
+  const bool producer = (w == 0);
+  const int comp = producer ? D : (w - 1 + ((w - 1) >= D ? 1 : 0));
   const int64_t nlines = (int64_t)a.nblocks * n_fast * n_slow;
-  const bool live = line < nlines;
-  const int64_t ln = live ? line : 0;
-  const int t0 = (int)(ln % n_fast);
-  const int64_t r = ln / n_fast;
-  const int t1 = (int)(r % n_slow);
-  const int b = (int)(r / n_slow);
-  int i0, j0, k0;
-  if (D == 0) {
-    i0 = ng; j0 = ng + t0; k0 = ng + t1;
-  } else if (D == 1) {
-    i0 = ng + t0; j0 = ng; k0 = ng + t1;
-  } else {
-    i0 = ng + t0; j0 = ng + t1; k0 = ng;
-  }
   const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1];
   const int64_t cs = N01 * d.N[2];
   const int64_t step = D == 0 ? 1 : (D == 1 ? N0 : N01);
-  const int64_t c0 = (int64_t)b * NC * cs + (int64_t)k0 * N01 + (int64_t)j0 * N0 + i0;
-  const DevBlockGeom &g = a.geom[b];
-  const double area = g.area[D];
   const int nf = n + 1;
-  double *ca = coef, *cb = coef + nf * 32, *cc = coef + 2 * nf * 32, *ci = coef + 3 * nf * 32;
+  const int nthreads = 32 * NC;
+  const double half = comp < 3 ? 0.5 : 1.0;
+  const double bdt = a.beta * a.dt[0];
 
-  auto emit = [&](int64_t e, double du) {
-    if (MODE == kStoreDu) {
-      a.dudt[e] = du;
-    } else if (MODE == kAddDu) {
-      a.dudt[e] = a.dudt[e] + du;
+  int it = 0;
+  for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x, ++it) {
+    const int buf = it & 1;
+    double *ca = coef_all + (size_t)buf * 4 * nf * 32;
+    double *cb = ca + nf * 32, *cc = ca + 2 * nf * 32, *ci = ca + 3 * nf * 32;
+    const int64_t line = grp * 32 + lane;
+    const bool live = line < nlines;
+    const int64_t ln = live ? line : 0;
+    const int t0 = (int)(ln % n_fast);
+    const int64_t r = ln / n_fast;
+    const int t1 = (int)(r % n_slow);
+    const int b = (int)(r / n_slow);
+    int i0, j0, k0;
+    if (D == 0) {
+      i0 = ng; j0 = ng + t0; k0 = ng + t1;
+    } else if (D == 1) {
+      i0 = ng + t0; j0 = ng; k0 = ng + t1;
     } else {
-      if (MODE == kFinishUpdate) du = a.dudt[e] + du;
-      const double dudt = -du / g.vol;
-      const double avg = a.w_in * __ldg(a.u_in + e) + a.w_base * __ldg(a.u_base + e);
-      a.u_out[e] = 1.0 * avg + (a.beta * a.dt[0]) * dudt;
+      i0 = ng + t0; j0 = ng + t1; k0 = ng;
     }
-  };
+    const int64_t c0 = (int64_t)b * NC * cs + (int64_t)k0 * N01 + (int64_t)j0 * N0 + i0;
+    const DevBlockGeom &g = a.geom[b];
+    const double area = g.area[D];
+    const double nvol = -1.0 / g.vol;
 
-  // march component `comp` of this lane's line; `phase1` builds the face coefficients
-  auto march = [&](int comp, bool phase1) {
+    if (producer) {
+      if (it >= 2) bar_sync(3 + buf, nthreads);  // consumers released this buffer
+    } else {
+      bar_sync(1 + buf, nthreads);  // coefficients of this group are ready
+    }
+
     const double *__restrict__ u = a.u_in + c0 + (int64_t)comp * cs;
-    WenoLine w;
-    w.q0 = __ldg(u - 3 * step);
-    w.q1 = __ldg(u - 2 * step);
-    w.q2 = __ldg(u - step);
-    w.q3 = __ldg(u);
-    w.q4 = __ldg(u + step);
-    weno_prime(w);  // window now centred on cell p = -1
-    const double half = comp < 3 ? 0.5 : 1.0;
+    WenoLine wl;
+    wl.q0 = __ldg(u - 3 * step);
+    wl.q1 = __ldg(u - 2 * step);
+    wl.q2 = __ldg(u - step);
+    wl.q3 = __ldg(u);
+    wl.q4 = __ldg(u + step);
+    weno_prime(wl);
     double lprev = 0.0, afprev = 0.0;
     for (int p = -1; p <= n; ++p) {
       double ql, qr;
-      weno_step(w, ql, qr);
-      if (p < n) weno_shift(w, __ldg(u + (int64_t)(p + 3) * step));
+      weno_step(wl, ql, qr);
+      if (p < n) weno_shift(wl, __ldg(u + (int64_t)(p + 3) * step));
       if (p >= 0) {
         double F;
         const int fi = p * 32 + lane;
-        if (phase1) {
+        if (producer) {
           const double upl = lprev, upr = qr;
           const double sl = fmin(fmin(upl, upr), 0.0);
           const double sr = fmax(fmax(upl, upr), 0.0);
@@ -216,29 +232,57 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a) {
           F = (ca[fi] * lprev - cb[fi] * qr + cc[fi] * (qr - lprev)) * (half * ci[fi]);
         }
         const double af = area * F;
-        if (p >= 1 && live) emit(c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step, af - afprev);
+        if (p >= 1 && live) {
+          const int64_t e = c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step;
+          double du = af - afprev;
+          if (MODE == kStoreDu) {
+            a.dudt[e] = du;
+          } else if (MODE == kAddDu) {
+            a.dudt[e] = a.dudt[e] + du;
+          } else {
+            if (MODE == kFinishUpdate) du = a.dudt[e] + du;
+            const double avg = a.w_in * __ldg(a.u_in + e) + a.w_base * __ldg(a.u_base + e);
+            a.u_out[e] = avg + bdt * (du * nvol);
+          }
+        }
         afprev = af;
       }
       lprev = ql;
     }
-  };
 
-  if (v == D) march(D, true);
-  __syncthreads();
-  if (v != D) march(v, false);
+    if (producer) {
+      bar_arrive(1 + buf, nthreads);
+    } else {
+      bar_arrive(3 + buf, nthreads);
+    }
+  }
+  // pair the consumers' last releases so no barrier is left with pending arrivals
+  if (producer) {
+    if (it >= 2) bar_sync(3 + (it & 1), nthreads);
+    if (it >= 1) bar_sync(3 + ((it + 1) & 1), nthreads);
+  }
 }
 
 template <int NC>
 int launch_burgers_nc(const StageArgs &a, cudaStream_t s) {
   const Dims &d = a.d;
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 152;
+  }
   auto go = [&](auto kern, int D) {
     const int n = D == 0 ? d.nx[0] : (D == 1 ? d.nx[1] : d.nx[2]);
     const int64_t nf = D == 0 ? d.nx[1] : d.nx[0];
     const int64_t ns = D == 2 ? d.nx[1] : d.nx[2];
     const int64_t lines = (int64_t)a.nblocks * nf * ns;
-    const size_t smem = 4 * (size_t)(n + 1) * 32 * sizeof(double);
+    const int64_t groups = (lines + 31) / 32;
+    const size_t smem = 2 * 4 * (size_t)(n + 1) * 32 * sizeof(double);
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    kern<<<(unsigned)((lines + 31) / 32), 32 * NC, smem, s>>>(a);
+    const int64_t grid = std::min<int64_t>(groups, (int64_t)nsm * 2);
+    kern<<<(unsigned)grid, 32 * NC, smem, s>>>(a, groups);
   };
   go(k_burgers_dir<NC, 0, kStoreDu>, 0);
   go(k_burgers_dir<NC, 1, kAddDu>, 1);
