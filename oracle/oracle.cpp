@@ -33,6 +33,7 @@
 #include <limits>
 #include <memory>
 
+#include "gmg.hpp"
 #include "mesh.hpp"
 
 namespace oracle {
@@ -891,6 +892,37 @@ uint32_t orc_range_mask(int el, uint32_t own_bits, int ox1, int ox2, int ox3) {
 void orc_morton(int level, int64_t l1, int64_t l2, int64_t l3, uint64_t *out) {
   Loc l(level, l1, l2, l3);
   for (int c = 0; c < 3; ++c) out[c] = l.m[c];
+}
+
+// ---------------------------------------------------------------- multigrid
+// n: finest cells per direction; ncoarsen: number of coarser levels; smoother: 1..3
+// SRJ stages, or jacobi != 0 for `stages` sweeps of weighted Jacobi with `weight`.
+void *orc_gmg_create(int n, int ncoarsen, double xmin, double xmax, int stages, int jacobi, double weight,
+                     int coarse_sweeps) {
+  GmgParams p;
+  p.smoother_stages = stages;
+  p.jacobi = jacobi != 0;
+  p.weight = weight;
+  p.coarse_sweeps = coarse_sweeps;
+  return new Gmg(n, ncoarsen, xmin, xmax, p);
+}
+void orc_gmg_destroy(void *h) { delete (Gmg *)h; }
+double *orc_gmg_u(void *h) { return ((Gmg *)h)->lv[0].u.data(); }
+double *orc_gmg_rhs(void *h) { return ((Gmg *)h)->lv[0].rhs.data(); }
+double *orc_gmg_res(void *h) { return ((Gmg *)h)->lv[0].res.data(); }
+// Run `ncycles` V-cycles; rms[c] receives sqrt(sum r^2 / N) after cycle c.
+void orc_gmg_run(void *h, int ncycles, double *rms) {
+  Gmg *g = (Gmg *)h;
+  const double ncell = (double)g->lv[0].size();
+  for (int c = 0; c < ncycles; ++c) {
+    g->vcycle();
+    const double s = g->residual();
+    if (rms) rms[c] = std::sqrt(s / ncell);
+  }
+}
+double orc_gmg_residual(void *h) {
+  Gmg *g = (Gmg *)h;
+  return std::sqrt(g->residual() / (double)g->lv[0].size());
 }
 
 }  // extern "C"

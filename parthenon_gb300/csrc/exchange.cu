@@ -164,6 +164,11 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
     const int32_t *de = p.recv_coarse ? out.dims.Nc : out.dims.N;
     if (!box_inside(d.src, se) || !box_inside(d.dst, de))
       return fail(kErrInvalid, "boundary box outside the block arrays");
+    // element m of the send box maps to element m of the receive box; the direct copy
+    // relies on both boxes having the same extents (always true for cell-centred data
+    // on one tree with the identity logical transformation)
+    for (int q = 0; q < 3; ++q)
+      if (d.src.n[q] != d.dst.n[q]) return fail(kErrUnsupported, "send and receive boxes differ in shape");
     add_work(cw, (int)pairs.size(), d.src.n[1] * d.src.n[2], d.src.n[0]);
     pairs.push_back(d);
   }
@@ -245,25 +250,48 @@ namespace {
 
 __device__ __forceinline__ double *arr(double *fine, double *coarse, int c) { return c ? coarse : fine; }
 
-// Direct copy: sender slab -> receiver ghosts. grid = (work items, components)
+// Direct copy: sender slab -> receiver ghosts. grid = (work items, components).
+// Per thread the row base addresses are formed once per row; rows whose two ends are
+// 16-byte aligned on both sides (every same-level face and edge of an even-sized block)
+// move as double2, the rest element by element.
 __global__ void __launch_bounds__(128) k_copy(const DevPair *__restrict__ pairs,
                                               const DevWork *__restrict__ work, Dims d, int ncomp,
                                               double *__restrict__ fine, double *__restrict__ coarse) {
   const DevWork w = work[blockIdx.x];
   const DevPair p = pairs[w.item];
   const int v = blockIdx.y;
-  const double *src = arr(fine, coarse, p.src_coarse);
-  double *dst = arr(fine, coarse, p.dst_coarse);
-  for_work_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], [&](int k, int j, int i) {
-    const int dk = p.dst.lo[2] + k, dj = p.dst.lo[1] + j, di = p.dst.lo[0] + i;
-    if (!p.full_mask && !mask_active(p.mask, p.dst, dk, dj, di)) return;
-    const int sk = p.src.lo[2] + k, sj = p.src.lo[1] + j, si = p.src.lo[0] + i;
-    const int64_t s = p.src_coarse ? coarse_index(d, ncomp, p.src_block, v, sk, sj, si)
-                                   : fine_index(d, ncomp, p.src_block, v, sk, sj, si);
-    const int64_t t = p.dst_coarse ? coarse_index(d, ncomp, p.dst_block, v, dk, dj, di)
-                                   : fine_index(d, ncomp, p.dst_block, v, dk, dj, di);
-    dst[t] = __ldg(src + s);
-  });
+  const int ni = p.src.n[0], nj = p.src.n[1];
+  const int sN0 = p.src_coarse ? d.Nc[0] : d.N[0], sN1 = p.src_coarse ? d.Nc[1] : d.N[1];
+  const int sN2 = p.src_coarse ? d.Nc[2] : d.N[2];
+  const int dN0 = p.dst_coarse ? d.Nc[0] : d.N[0], dN1 = p.dst_coarse ? d.Nc[1] : d.N[1];
+  const int dN2 = p.dst_coarse ? d.Nc[2] : d.N[2];
+  const double *src = (p.src_coarse ? coarse : fine) +
+                      ((int64_t)p.src_block * ncomp + v) * ((int64_t)sN2 * sN1 * sN0) +
+                      ((int64_t)p.src.lo[2] * sN1 + p.src.lo[1]) * sN0 + p.src.lo[0];
+  double *dst = (p.dst_coarse ? coarse : fine) + ((int64_t)p.dst_block * ncomp + v) * ((int64_t)dN2 * dN1 * dN0) +
+                ((int64_t)p.dst.lo[2] * dN1 + p.dst.lo[1]) * dN0 + p.dst.lo[0];
+  const int sk = sN1 * sN0, dk = dN1 * dN0;
+  const bool vec = p.full_mask && ((ni & 1) == 0) && (((p.src.lo[0] | p.dst.lo[0]) & 1) == 0) &&
+                   ((sN0 & 1) == 0) && ((dN0 & 1) == 0) &&
+                   ((((uintptr_t)src) & 15) == 0) && ((((uintptr_t)dst) & 15) == 0);
+  const int nel = vec ? ni / 2 : ni;  // elements (or pairs) per row
+  const int lpr = nel <= 1 ? 1 : nel <= 2 ? 2 : nel <= 4 ? 4 : nel <= 8 ? 8 : nel <= 16 ? 16 : 32;
+  const int sub = threadIdx.x / lpr, li = threadIdx.x - sub * lpr, stepr = blockDim.x / lpr;
+  for (int r = w.row0 + sub; r < w.row0 + w.nrows; r += stepr) {
+    const int k = r / nj, j = r - k * nj;
+    const double *s = src + k * sk + j * sN0;
+    double *t = dst + k * dk + j * dN0;
+    if (vec) {
+      const double2 *s2 = reinterpret_cast<const double2 *>(s);
+      double2 *t2 = reinterpret_cast<double2 *>(t);
+      for (int i = li; i < nel; i += lpr) t2[i] = __ldg(s2 + i);
+    } else if (p.full_mask) {
+      for (int i = li; i < nel; i += lpr) t[i] = __ldg(s + i);
+    } else {
+      for (int i = li; i < nel; i += lpr)
+        if (mask_active(p.mask, p.dst, p.dst.lo[2] + k, p.dst.lo[1] + j, p.dst.lo[0] + i)) t[i] = __ldg(s + i);
+    }
+  }
 }
 
 // Buffered path, reference layout: buf[ncomp*buf_off + v*box + (k*nj + j)*ni + i]

@@ -177,3 +177,54 @@ def morton(level, l1, l2, l3):
 
 def bit(a, b, c):
     return 1 << ((a + 1) + 3 * (b + 1) + 9 * (c + 1))
+
+
+def _gmg_lib():
+    L = lib()
+    if not getattr(L, "_gmg_ready", False):
+        L.orc_gmg_create.restype = ctypes.c_void_p
+        L.orc_gmg_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.orc_gmg_destroy.argtypes = [ctypes.c_void_p]
+        for name in ["orc_gmg_u", "orc_gmg_rhs", "orc_gmg_res"]:
+            getattr(L, name).argtypes = [ctypes.c_void_p]
+            getattr(L, name).restype = DP
+        L.orc_gmg_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.orc_gmg_residual.argtypes = [ctypes.c_void_p]
+        L.orc_gmg_residual.restype = ctypes.c_double
+        L._gmg_ready = True
+    return L
+
+
+class OracleGmg:
+    """FP64 geometric multigrid (FAS V-cycle) on a uniform periodic grid."""
+
+    def __init__(self, n, ncoarsen, xmin=0.0, xmax=1.0, stages=2, jacobi=False, weight=2.0 / 3.0,
+                 coarse_sweeps=0):
+        L = _gmg_lib()
+        self.n = int(n)
+        self.h = L.orc_gmg_create(self.n, int(ncoarsen), float(xmin), float(xmax), int(stages), int(bool(jacobi)),
+                                  float(weight), int(coarse_sweeps))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _gmg_lib().orc_gmg_destroy(self.h)
+            self.h = None
+
+    def _view(self, fn):
+        p = fn(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.n ** 3,)).reshape(self.n, self.n, self.n)
+
+    def u(self):
+        return self._view(_gmg_lib().orc_gmg_u)
+
+    def rhs(self):
+        return self._view(_gmg_lib().orc_gmg_rhs)
+
+    def run(self, ncycles):
+        rms = np.zeros(max(1, ncycles))
+        _gmg_lib().orc_gmg_run(self.h, int(ncycles), _ptr(rms))
+        return rms[:ncycles]
+
+    def residual(self):
+        return _gmg_lib().orc_gmg_residual(self.h)
