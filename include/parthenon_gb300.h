@@ -111,6 +111,17 @@ int pgb_mesh_upload(pgb_mesh *mesh);
 int pgb_exchange(pgb_mesh *mesh, double *data, double *coarse, int32_t ncomp, int32_t flags, double *buffer,
                  void *stream);
 
+/* Same exchange as pgb_exchange with a packed buffer, but the buffer is a fixed
+ * 32 MiB (4,194,304 doubles) array in static device memory owned by the library, so
+ * the call allocates nothing; for callers that cannot allocate device memory (another
+ * runtime owns the allocator, or the loop must never allocate). No counterpart in the
+ * reference. Requests needing more than buffer_elems * ncomp = 4,194,304 doubles are
+ * rejected (PGB_ERR_INVALID). The first call on each device looks up the array's
+ * device address (make that first call before any stream capture); all calls share
+ * the array, so calls that overlap on the GPU race with each other. */
+int pgb_exchange_static_buffer(pgb_mesh *mesh, double *data, double *coarse, int32_t ncomp, int32_t flags,
+                               void *stream);
+
 /* Pack every boundary into `buffer` in the reference's buffer layout (parity checks).
  * Replaces the pack kernel of SendBoundBufs (boundary_communication.cpp:95-140). */
 int pgb_pack_buffers(pgb_mesh *mesh, const double *data, const double *coarse, int32_t ncomp, double *buffer,

@@ -45,6 +45,7 @@ _SIGNATURES = {
     "pgb_mesh_validate": [VP],
     "pgb_exchange": [VP, VP, VP, ctypes.c_int32, ctypes.c_int32, VP, VP],
     "pgb_pack_buffers": [VP, VP, VP, ctypes.c_int32, VP, VP],
+    "pgb_exchange_static_buffer": [VP, VP, VP, ctypes.c_int32, ctypes.c_int32, VP],
     "pgb_flux_correct": [VP, VP, ctypes.c_int32, VP],
     "pgb_stage": [VP, ctypes.POINTER(StageParams), VP, VP, VP, VP, VP, VP, ctypes.c_double, ctypes.c_double,
                   ctypes.c_double, ctypes.c_int32, VP],

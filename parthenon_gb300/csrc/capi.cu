@@ -58,6 +58,11 @@ struct pgb_mesh {
   }
 };
 
+namespace pgb {
+// Leaf-grid tables of a mesh handle (used by entry points defined in other units).
+GridTables *mesh_leaf_tables(pgb_mesh *m) { return m && m->st.uploaded ? &m->st.leaf : nullptr; }
+}  // namespace pgb
+
 namespace {
 
 int stage_impl(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const double *u_base, double *u_out,
