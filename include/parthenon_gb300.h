@@ -166,6 +166,38 @@ int pgb_rk2_cycles(pgb_mesh *mesh, const pgb_stage_params *p, double *base, doub
 int pgb_run_host(pgb_mesh *mesh, const pgb_stage_params *p, const double *host_in, double *host_out, int32_t ncomp,
                  int32_t ncycles, double *dt_inout);
 
+/* ---------------------------------------------------------------- multigrid
+ * Geometric multigrid for div(grad u) = rhs on a uniform periodic cube of n^3 cells
+ * (n a power of two), arrays of n^3 doubles with x fastest. Levels n, n/2, ...,
+ * n >> ncoarsen. FAS V-cycle with SRJ (Yang-Mittal weights for `stages` 1..3) or
+ * weighted-Jacobi smoothing, volume-average restriction and linear prolongation. */
+typedef struct pgb_gmg pgb_gmg;
+typedef struct {
+  int32_t n;             /* finest cells per direction */
+  int32_t ncoarsen;      /* coarser levels below the finest (max_coarsenings) */
+  int32_t stages;        /* pre- and post-smoothing sweeps */
+  int32_t jacobi;        /* 0: SRJ weights; 1: weighted Jacobi with `weight` */
+  double weight;
+  int32_t coarse_sweeps; /* extra smoother passes at the coarsest level (0 = reference) */
+  int32_t exact;         /* 1: separately rounded reference-order arithmetic */
+  double xmin, xmax;
+} pgb_gmg_params;
+
+/* Allocates every level (FP64 and FP32 hierarchies). Replaces MGSolver construction and
+ * the multigrid block lists (src/solvers/mg_solver.hpp:80-117, src/mesh/mesh-gmg.cpp:103-201). */
+int pgb_gmg_create(const pgb_gmg_params *params, pgb_gmg **out);
+int pgb_gmg_destroy(pgb_gmg *gmg);
+/* ncycles FP64 V-cycles on u (in/out) with right-hand side rhs; rms (host, may be NULL)
+ * receives sqrt(sum r^2 / N) after each cycle. Replaces AddLinearOperatorTasks +
+ * the residual check of MGSolver::AddTasks (mg_solver.hpp:119-186). Synchronises the
+ * stream once per cycle to read the residual. */
+int pgb_gmg_vcycles(pgb_gmg *gmg, double *u, const double *rhs, int32_t ncycles, double *rms, void *stream);
+/* Solve to rms(rhs - A u) / rms(rhs - A u_initial) <= rtol. mixed = 0: FP64 V-cycles;
+ * mixed = 1: FP32 V-cycle on the FP64 residual (iterative refinement, FP64 coarsest
+ * level). Replaces MGSolver::AddTasks (mg_solver.hpp:119-161). */
+int pgb_gmg_solve(pgb_gmg *gmg, double *u, const double *rhs, int32_t mixed, double rtol, int32_t max_cycles,
+                  int32_t *cycles_out, double *relres_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,7 +42,7 @@ struct GmgParams {
   int smoother_stages = 2;       // SRJ stages (1, 2, 3), or Jacobi sweeps when jacobi
   bool jacobi = false;           // weighted Jacobi with `weight` instead of SRJ weights
   double weight = 2.0 / 3.0;
-  int coarse_sweeps = 0;         // extra smoothing at the coarsest level (0 = reference)
+  int coarse_sweeps = 0;         // extra smoother passes at the coarsest level (0 = reference)
   double D = 1.0;                // face coefficient of div(D grad u)
   double alpha = 0.0;            // diagonal shift (poisson/diagonal_alpha)
 };
@@ -201,7 +201,7 @@ struct Gmg {
         Ax(g, g.u, g.temp);
         for (int64_t c = 0; c < g.size(); ++c) g.res[c] = 1.0 * g.rhs[c] + -1.0 * g.temp[c];
       } else {
-        for (int s = 0; s < p.coarse_sweeps; ++s) smooth(g, 1);
+        for (int s = 0; s < p.coarse_sweeps; ++s) smooth(g, pre);
         g.res = g.u;
         if (l > 0)
           for (int64_t c = 0; c < g.size(); ++c) g.res[c] = 1.0 * g.u[c] + -1.0 * g.u0[c];

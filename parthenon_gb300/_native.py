@@ -28,6 +28,12 @@ class MeshInfo(ctypes.Structure):
                 ("npairs", ctypes.c_int32), ("buffer_elems", ctypes.c_int64), ("nflux_corr", ctypes.c_int32)]
 
 
+class GmgParams(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("ncoarsen", ctypes.c_int32), ("stages", ctypes.c_int32),
+                ("jacobi", ctypes.c_int32), ("weight", ctypes.c_double), ("coarse_sweeps", ctypes.c_int32),
+                ("exact", ctypes.c_int32), ("xmin", ctypes.c_double), ("xmax", ctypes.c_double)]
+
+
 class StageParams(ctypes.Structure):
     _fields_ = [("physics", ctypes.c_int32), ("recon", ctypes.c_int32), ("exact", ctypes.c_int32),
                 ("pad", ctypes.c_int32), ("vel", ctypes.c_double * 3), ("cfl", ctypes.c_double)]
@@ -53,6 +59,11 @@ _SIGNATURES = {
     "pgb_rk2_cycles": [VP, ctypes.POINTER(StageParams), VP, VP, VP, VP, VP, VP, ctypes.c_int32, VP,
                        ctypes.c_int32, ctypes.c_int32, VP],
     "pgb_run_host": [VP, ctypes.POINTER(StageParams), VP, VP, ctypes.c_int32, ctypes.c_int32, DP],
+    "pgb_gmg_create": [ctypes.POINTER(GmgParams), ctypes.POINTER(VP)],
+    "pgb_gmg_destroy": [VP],
+    "pgb_gmg_vcycles": [VP, VP, VP, ctypes.c_int32, VP, VP],
+    "pgb_gmg_solve": [VP, VP, VP, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                      DP, VP],
 }
 
 

@@ -21,6 +21,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
 PER_FILE = {
     "stencil_exact.cu": ["-fmad=false"],
+    "gmg_exact.cu": ["-fmad=false"],
 }
 
 

@@ -1,0 +1,358 @@
+// Geometric-multigrid kernels on uniform periodic levels, templated on the working
+// precision (double, or float for the mixed-precision V-cycle).
+//
+// Included once by gmg_exact.cu (-fmad=false, reference expression order: bitwise
+// against the oracle in FP64) and once by gmg_fast.cu (FMA contraction; the constant-
+// coefficient operator written as a 7-point Laplacian with 1/dx^2 precomputed).
+//
+// On a uniform periodic mesh every multigrid level is a uniform periodic grid: the
+// reference's same-level ghost exchange is the periodic image (indices wrap here), the
+// gmg_restrict / gmg_prolongate block transfers act cell by cell, so one array of n^3
+// cells per level (x fastest) carries exactly the reference's values.
+//
+// Reference semantics (parthenon-hpc-lab/parthenon):
+//   example/poisson_gmg/poisson_equation.hpp:59-210   SetDiagonal, fluxes, Ax
+//   src/solvers/mg_solver.hpp:222-297                 Jacobi with robust::ratio
+//   src/solvers/solver_utils.hpp:150-306              copies, weighted sums, dot product
+//   src/prolong_restrict/pr_ops.hpp:105-285           RestrictAverage, ProlongateSharedLinear
+#pragma once
+
+#include <cfloat>
+
+#include "common.cuh"
+
+namespace pgb {
+namespace PGB_GMG_NS {
+
+struct LevelGeom {
+  int n, log2n;
+  double dx, xmin;
+};
+
+__device__ __forceinline__ int wrap(int i, int n) { return i & (n - 1); }  // n is a power of 2
+
+template <class T>
+__device__ __forceinline__ T ax_cell(const T *__restrict__ u, int k, int j, int i, const LevelGeom &g, T D, T alpha) {
+  const int n = g.n;
+  const int64_t nn = (int64_t)n * n;
+  const T dx = (T)g.dx;
+  const T uc = u[(int64_t)k * nn + j * n + i];
+  const T uim = u[(int64_t)k * nn + j * n + wrap(i - 1, n)], uip = u[(int64_t)k * nn + j * n + wrap(i + 1, n)];
+  const T ujm = u[(int64_t)k * nn + wrap(j - 1, n) * n + i], ujp = u[(int64_t)k * nn + wrap(j + 1, n) * n + i];
+  const T ukm = u[(int64_t)wrap(k - 1, n) * nn + j * n + i], ukp = u[(int64_t)wrap(k + 1, n) * nn + j * n + i];
+#ifdef PGB_GMG_EXACT
+  // poisson_equation.hpp:104-210: x1 fluxes D/dx*(u_l - u_r); x2, x3 fluxes D*(u_l - u_r)/dx
+  const T f1l = D / dx * (uim - uc), f1r = D / dx * (uc - uip);
+  const T f2l = D * (ujm - uc) / dx, f2r = D * (uc - ujp) / dx;
+  const T f3l = D * (ukm - uc) / dx, f3r = D * (uc - ukp) / dx;
+  T out = -alpha * uc;
+  out += (f1l - f1r) / dx;
+  out += (f2l - f2r) / dx;
+  out += (f3l - f3r) / dx;
+  return out;
+#else
+  const T idx2 = D / (dx * dx);
+  return ((uim + uip) + (ujm + ujp) + (ukm + ukp) - (T)6 * uc) * idx2 - alpha * uc;
+#endif
+}
+
+template <class T>
+__device__ __forceinline__ T diag_value(const LevelGeom &g, T D, T alpha) {
+  const T dx = (T)g.dx;
+  T d = -(D + D) / (dx * dx) - alpha;
+  d -= (D + D) / (dx * dx);
+  d -= (D + D) / (dx * dx);
+  return d;
+}
+
+__device__ __forceinline__ void cell_of(int64_t c, const LevelGeom &g, int &k, int &j, int &i) {
+  i = (int)(c & (g.n - 1));
+  j = (int)((c >> g.log2n) & (g.n - 1));
+  k = (int)(c >> (2 * g.log2n));
+}
+
+// temp <- Jacobi(u): w * (rhs - (A u - d u)) / d + (1 - w) u   (mg_solver.hpp:277-291)
+template <class T>
+__global__ void __launch_bounds__(256) k_jacobi(const T *__restrict__ u, const T *__restrict__ rhs, T *__restrict__ out,
+                                                LevelGeom g, T D, T alpha, T w) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)g.n * g.n * g.n) return;
+  int k, j, i;
+  cell_of(c, g, k, j, i);
+  const T ax = ax_cell(u, k, j, i, g, D, alpha);
+  const T dg = diag_value(g, D, alpha);
+  const T small = (T)10 * (sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN);
+  const T den = dg + (dg >= (T)0 ? (T)1 : (T)-1) * small;
+  const T off = ax - dg * u[c];
+  const T val = rhs[c] - off;
+  out[c] = w * (val / den) + ((T)1 - w) * u[c];
+}
+
+// res <- 1 rhs + (-1) A u
+template <class T>
+__global__ void __launch_bounds__(256) k_residual(const T *__restrict__ u, const T *__restrict__ rhs, T *__restrict__ res,
+                                                  LevelGeom g, T D, T alpha) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)g.n * g.n * g.n) return;
+  int k, j, i;
+  cell_of(c, g, k, j, i);
+  res[c] = (T)1 * rhs[c] + (T)-1 * ax_cell(u, k, j, i, g, D, alpha);
+}
+
+// FAS coarse problem: u0 <- u; rhs <- 1 A u + 1 res   (mg_solver.hpp:423-431)
+template <class T>
+__global__ void __launch_bounds__(256) k_fas_rhs(const T *__restrict__ u, const T *__restrict__ res, T *__restrict__ rhs,
+                                                 T *__restrict__ u0, LevelGeom g, T D, T alpha) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)g.n * g.n * g.n) return;
+  int k, j, i;
+  cell_of(c, g, k, j, i);
+  u0[c] = u[c];
+  rhs[c] = (T)1 * ax_cell(u, k, j, i, g, D, alpha) + (T)1 * res[c];
+}
+
+// RestrictAverage of two fields (u and res) onto the coarse level (pr_ops.hpp:105-164)
+template <class T>
+__global__ void __launch_bounds__(256) k_restrict2(const T *__restrict__ fu, const T *__restrict__ fr, T *__restrict__ cu,
+                                                   T *__restrict__ cr, LevelGeom fg, LevelGeom cg) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)cg.n * cg.n * cg.n) return;
+  int k, j, i;
+  cell_of(c, cg, k, j, i);
+  const T vol = (T)fg.dx * (T)fg.dx * (T)fg.dx;
+  const int n = fg.n;
+  const int64_t nn = (int64_t)n * n;
+  const T tv = ((vol + vol) + (vol + vol)) + ((vol + vol) + (vol + vol));
+#pragma unroll
+  for (int f = 0; f < 2; ++f) {
+    const T *src = f ? fr : fu;
+    T t[2][2][2];
+#pragma unroll
+    for (int ok = 0; ok < 2; ++ok)
+#pragma unroll
+      for (int oj = 0; oj < 2; ++oj)
+#pragma unroll
+        for (int oi = 0; oi < 2; ++oi)
+          t[ok][oj][oi] = vol * src[(int64_t)(2 * k + ok) * nn + (2 * j + oj) * n + (2 * i + oi)];
+    const T num = ((t[0][0][0] + t[0][1][0]) + (t[0][0][1] + t[0][1][1])) +
+                  ((t[1][0][0] + t[1][1][0]) + (t[1][0][1] + t[1][1][1]));
+    (f ? cr : cu)[c] = num / tv;
+  }
+}
+
+// u_fine <- 1 u_fine + 1 Prolongate(res_coarse) with ProlongateSharedLinear
+// (pr_ops.hpp:166-285, one-sided slopes), fused with AddFieldsAndStore<u, res_err, u>.
+template <class T>
+__global__ void __launch_bounds__(256) k_prolong_add(const T *__restrict__ cres, T *__restrict__ fu, LevelGeom cg,
+                                                     LevelGeom fg) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)cg.n * cg.n * cg.n) return;
+  int k, j, i;
+  cell_of(c, cg, k, j, i);
+  const int n = cg.n;
+  const int64_t nn = (int64_t)n * n;
+  const T fc = cres[c];
+  const int ci[3] = {i, j, k};
+  T gm[3], gp[3], dfm[3], dfp[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const double xc = cg.xmin + (ci[q] + 0.5) * cg.dx;
+    const double xm = cg.xmin + (ci[q] - 1 + 0.5) * cg.dx;
+    const double xp = cg.xmin + (ci[q] + 1 + 0.5) * cg.dx;
+    const double fxm = fg.xmin + (2 * ci[q] + 0.5) * fg.dx;
+    const double fxp = fg.xmin + (2 * ci[q] + 1 + 0.5) * fg.dx;
+    const T dxm = (T)(xc - xm), dxp = (T)(xp - xc);
+    dfm[q] = (T)(xc - fxm);
+    dfp[q] = (T)(fxp - xc);
+    const int64_t om = q == 0 ? ((int64_t)k * nn + j * n + wrap(i - 1, n))
+                              : (q == 1 ? ((int64_t)k * nn + wrap(j - 1, n) * n + i) : ((int64_t)wrap(k - 1, n) * nn + j * n + i));
+    const int64_t op = q == 0 ? ((int64_t)k * nn + j * n + wrap(i + 1, n))
+                              : (q == 1 ? ((int64_t)k * nn + wrap(j + 1, n) * n + i) : ((int64_t)wrap(k + 1, n) * nn + j * n + i));
+    gm[q] = (fc - cres[om]) / dxm;
+    gp[q] = (cres[op] - fc) / dxp;
+  }
+  const T m0 = gm[0] * dfm[0], p0 = gp[0] * dfp[0];
+  const T m1 = gm[1] * dfm[1], p1 = gp[1] * dfp[1];
+  const T m2 = gm[2] * dfm[2], p2 = gp[2] * dfp[2];
+  const int fn = fg.n;
+  const int64_t fnn = (int64_t)fn * fn;
+  const int64_t b0 = (int64_t)(2 * k) * fnn + (2 * j) * fn + 2 * i;
+  const T v[8] = {fc - ((m0 + m1) + m2), fc + ((p0 - m1) - m2), fc - ((m0 - p1) + m2), fc + ((p0 + p1) - m2),
+                  fc - ((m0 + m1) - p2), fc + ((p0 - m1) + p2), fc - ((m0 - p1) - p2), fc + ((p0 + p1) + p2)};
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int oi = q & 1, oj = (q >> 1) & 1, ok = q >> 2;
+    const int64_t e = b0 + ok * fnn + oj * fn + oi;
+    fu[e] = (T)1 * fu[e] + (T)1 * v[q];
+  }
+}
+
+// out <- 1 a + (-1) b
+template <class T>
+__global__ void __launch_bounds__(256) k_sub(const T *__restrict__ a, const T *__restrict__ b, T *__restrict__ out, int64_t n) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) out[c] = (T)1 * a[c] + (T)-1 * b[c];
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_copy_arr(const T *__restrict__ a, T *__restrict__ out, int64_t n) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) out[c] = a[c];
+}
+
+// Per-CTA partial sums of a^2 (FP64 accumulation); a second pass sums them in order.
+template <class T>
+__global__ void __launch_bounds__(256) k_sumsq_partial(const T *__restrict__ a, int64_t n, double *__restrict__ partial) {
+  __shared__ double sm[256];
+  double s = 0.0;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const double v = (double)a[c];
+    s += v * v;
+  }
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sm[0];
+}
+
+}  // namespace PGB_GMG_NS
+}  // namespace pgb
+
+// ---------------------------------------------------------------------------------
+// Host-side V-cycle driver (stream-ordered launches, capturable in a CUDA graph).
+#include "gmg_state.hpp"
+
+namespace pgb {
+namespace PGB_GMG_NS {
+
+inline unsigned nblk(int64_t n) { return (unsigned)((n + 255) / 256); }
+
+template <class T>
+LevelGeom geom_of(const GmgLevelBuf<T> &L) {
+  LevelGeom g;
+  g.n = L.n;
+  g.log2n = L.log2n;
+  g.dx = L.dx;
+  g.xmin = L.xmin;
+  return g;
+}
+
+// Smoother weights: SRJ (mg_solver.hpp:320-326, 3-D rows) or fixed-weight Jacobi.
+inline double smoother_weight(const GmgConfig &c, int s) {
+  static const double m1[3] = {1.0, 0.0, 0.0};
+  static const double m2[3] = {1.7319, 0.5695, 0.0};
+  static const double m3[3] = {2.2473, 0.8571, 0.5296};
+  if (c.jacobi) return c.weight;
+  return c.stages == 1 ? m1[s] : (c.stages == 2 ? m2[s] : m3[s]);
+}
+
+template <class T>
+void smooth(GmgLevelBuf<T> &L, const GmgConfig &c, cudaStream_t s) {
+  if (c.stages == 0) return;
+  const LevelGeom g = geom_of(L);
+  const int64_t n = L.cells();
+  T *a = L.u, *b = L.temp;
+  for (int st = 0; st < c.stages; ++st) {
+    k_jacobi<T><<<nblk(n), 256, 0, s>>>(a, L.rhs, b, g, (T)c.D, (T)c.alpha, (T)smoother_weight(c, st));
+    T *t = a;
+    a = b;
+    b = t;
+  }
+  if (a != L.u) k_copy_arr<T><<<nblk(n), 256, 0, s>>>(a, L.u, n);
+}
+
+template <class Tf, class Tc>
+__global__ void k_convert(const Tf *__restrict__ a, Tc *__restrict__ b, int64_t n) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) b[c] = (Tc)a[c];
+}
+
+// One FAS V-cycle (mg_solver.hpp:375-520) over levels L[0] (finest) .. L[nl-1].
+// When c64 is given, the coarsest level runs in FP64 on c64 (mixed precision).
+template <class T>
+void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *c64, cudaStream_t s) {
+  const T D = (T)c.D, alpha = (T)c.alpha;
+  for (int l = 0; l < nl; ++l) {
+    GmgLevelBuf<T> &g = L[l];
+    const int64_t n = g.cells();
+    const LevelGeom lg = geom_of(g);
+    if (l > 0) {
+      GmgLevelBuf<T> &f = L[l - 1];
+      k_restrict2<T><<<nblk(n), 256, 0, s>>>(f.u, f.res, g.u, g.res, geom_of(f), lg);
+    }
+    const bool coarsest = (l == nl - 1);
+    if (coarsest && c64) {
+      // coarsest level in FP64: convert, solve there, convert the error back
+      GmgLevelBuf<double> &h = *c64;
+      const LevelGeom hg = geom_of(h);
+      k_convert<T, double><<<nblk(n), 256, 0, s>>>(g.u, h.u, n);
+      k_convert<T, double><<<nblk(n), 256, 0, s>>>(g.res, h.res, n);
+      if (l > 0) {
+        k_fas_rhs<double><<<nblk(n), 256, 0, s>>>(h.u, h.res, h.rhs, h.u0, hg, c.D, c.alpha);
+      } else {
+        k_convert<T, double><<<nblk(n), 256, 0, s>>>(g.rhs, h.rhs, n);
+        k_copy_arr<double><<<nblk(n), 256, 0, s>>>(h.u, h.u0, n);
+      }
+      smooth<double>(h, c, s);
+      for (int q = 0; q < c.coarse_sweeps; ++q) smooth<double>(h, c, s);
+      if (l > 0) k_sub<double><<<nblk(n), 256, 0, s>>>(h.u, h.u0, h.res, n);
+      else k_copy_arr<double><<<nblk(n), 256, 0, s>>>(h.u, h.res, n);
+      k_convert<double, T><<<nblk(n), 256, 0, s>>>(h.res, g.res, n);
+      if (l == 0) k_convert<double, T><<<nblk(n), 256, 0, s>>>(h.u, g.u, n);
+      break;
+    }
+    if (l > 0) k_fas_rhs<T><<<nblk(n), 256, 0, s>>>(g.u, g.res, g.rhs, g.u0, lg, D, alpha);
+    else k_copy_arr<T><<<nblk(n), 256, 0, s>>>(g.u, g.u0, n);
+    smooth<T>(g, c, s);
+    if (!coarsest) {
+      k_residual<T><<<nblk(n), 256, 0, s>>>(g.u, g.rhs, g.res, lg, D, alpha);
+    } else {
+      for (int q = 0; q < c.coarse_sweeps; ++q) smooth<T>(g, c, s);
+      if (l > 0) k_sub<T><<<nblk(n), 256, 0, s>>>(g.u, g.u0, g.res, n);
+      else k_copy_arr<T><<<nblk(n), 256, 0, s>>>(g.u, g.res, n);
+    }
+  }
+  for (int l = nl - 2; l >= 0; --l) {
+    GmgLevelBuf<T> &g = L[l], &cl = L[l + 1];
+    const int64_t n = g.cells();
+    k_prolong_add<T><<<nblk(cl.cells()), 256, 0, s>>>(cl.res, g.u, geom_of(cl), geom_of(g));
+    smooth<T>(g, c, s);
+    if (l > 0) k_sub<T><<<nblk(n), 256, 0, s>>>(g.u, g.u0, g.res, n);
+  }
+}
+
+// res = rhs - A u on a level; partial sums of res^2 into `partial` (nparts entries).
+template <class T>
+void residual_sumsq(GmgLevelBuf<T> &L, const GmgConfig &c, double *partial, int nparts, cudaStream_t s) {
+  const int64_t n = L.cells();
+  k_residual<T><<<nblk(n), 256, 0, s>>>(L.u, L.rhs, L.res, geom_of(L), (T)c.D, (T)c.alpha);
+  k_sumsq_partial<T><<<nparts, 256, 0, s>>>(L.res, n, partial);
+}
+
+template <class T>
+void launch_sumsq(const T *a, int64_t n, double *partial, int nparts, cudaStream_t s) {
+  k_sumsq_partial<T><<<nparts, 256, 0, s>>>(a, n, partial);
+}
+
+// x <- x + (double) e  (iterative refinement update)
+template <class T>
+__global__ void k_add_correction(double *__restrict__ x, const T *__restrict__ e, int64_t n) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) x[c] = x[c] + (double)e[c];
+}
+
+inline void launch_mixed_prepare(const double *r64, GmgLevelBuf<float> &L0, cudaStream_t s) {
+  const int64_t n = L0.cells();
+  k_convert<double, float><<<nblk(n), 256, 0, s>>>(r64, L0.rhs, n);
+  cudaMemsetAsync(L0.u, 0, n * sizeof(float), s);
+}
+inline void launch_mixed_update(double *x, const GmgLevelBuf<float> &L0, cudaStream_t s) {
+  const int64_t n = L0.cells();
+  k_add_correction<float><<<nblk(n), 256, 0, s>>>(x, L0.u, n);
+}
+
+}  // namespace PGB_GMG_NS
+}  // namespace pgb

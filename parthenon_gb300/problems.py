@@ -78,3 +78,20 @@ def burgers_state(mesh, nscalars=8, nmodes=8, kmax=4, seed=2):
         rng = np.random.default_rng(seed + 1000)
         out[:, 3:, sk, sj, si] = rng.random((mesh.nblocks, nscalars, n[2], n[1], n[0]))
     return out
+
+
+def poisson_rhs(n, ngauss=32, sigma=0.03, seed=4):
+    """Sum of `ngauss` Gaussians (width sigma, centres U[0,1]^3, amplitudes N(0,1), seeded)
+    with periodic-image distances on the unit cube, minus its mean; array (n, n, n),
+    x fastest."""
+    rng = np.random.default_rng(seed)
+    centres = rng.random((ngauss, 3))
+    amps = rng.standard_normal(ngauss)
+    x = (np.arange(n) + 0.5) / n
+    out = np.zeros((n, n, n))
+    for c, a in zip(centres, amps):
+        d = [x - c[q] for q in range(3)]
+        d = [dd - np.round(dd) for dd in d]
+        r2 = d[2][:, None, None] ** 2 + d[1][None, :, None] ** 2 + d[0][None, None, :] ** 2
+        out += a * np.exp(-r2 / (2.0 * sigma * sigma))
+    return out - out.mean()

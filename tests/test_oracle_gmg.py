@@ -1,0 +1,25 @@
+"""The oracle's multigrid converges (CPU): FAS V-cycles with SRJ2 or weighted Jacobi
+reduce the rms residual every cycle on a periodic Poisson problem."""
+import numpy as np
+
+import oracle_lib as O
+import parthenon_gb300 as pg
+
+
+def test_vcycles_reduce_residual():
+    n = 16
+    o = O.OracleGmg(n, 2)
+    o.rhs()[:] = pg.problems.poisson_rhs(n, ngauss=4, sigma=0.1, seed=1)
+    r0 = o.residual()
+    rms = o.run(6)
+    assert np.all(np.diff(rms) < 0)
+    assert rms[-1] < 1e-3 * r0
+
+
+def test_jacobi_smoother_converges():
+    n = 16
+    o = O.OracleGmg(n, 2, stages=2, jacobi=True, weight=2.0 / 3.0, coarse_sweeps=8)
+    o.rhs()[:] = pg.problems.poisson_rhs(n, ngauss=4, sigma=0.1, seed=1)
+    r0 = o.residual()
+    rms = o.run(8)
+    assert rms[-1] < 1e-3 * r0
