@@ -143,8 +143,10 @@ int pgb_stage(pgb_mesh *mesh, const pgb_stage_params *p, const double *u_in, con
               double *dudt, double *flux, const double *dt, double w_in, double w_base, double beta, int32_t ncomp,
               void *stream);
 
-/* dt <- SetGlobalTimeStep(cfl * EstimateTimestep(u)) on the device (first != 0: the
- * initial step). Replaces EstimateTimestep (src/interface/update.hpp:268-278) and
+/* dt <- SetGlobalTimeStep(cfl * EstimateTimestep(u)) on the device. first = 0: regular
+ * step (growth limited to 2x); 1: the initial step; 2: an extra vote without growth,
+ * dt <- min(dt, cfl * estimate), used after a remesh so that new blocks vote too.
+ * Replaces EstimateTimestep (src/interface/update.hpp:268-278) and
  * EvolutionDriver::SetGlobalTimeStep (src/driver/driver.cpp:210-232). */
 int pgb_estimate_dt(pgb_mesh *mesh, const pgb_stage_params *p, const double *u, int32_t ncomp, double *dt,
                     int32_t first, void *stream);
@@ -197,6 +199,46 @@ int pgb_gmg_vcycles(pgb_gmg *gmg, double *u, const double *rhs, int32_t ncycles,
  * level). Replaces MGSolver::AddTasks (mg_solver.hpp:119-161). */
 int pgb_gmg_solve(pgb_gmg *gmg, double *u, const double *rhs, int32_t mixed, double rtol, int32_t max_cycles,
                   int32_t *cycles_out, double *relres_out, void *stream);
+
+/* ---- adaptive refinement ------------------------------------------------------- */
+
+/* Per-block refinement criterion of component `comp` of u (ghosts must be current),
+ * written to the device array out[nblocks]. method 0: FirstDerivative, max over the
+ * interior of 0.5|q(i+1)-q(i-1)| / (|q| + 1e-20) along each axis; 1: SecondDerivative;
+ * 2: largest central-difference |grad q|. One launch for all blocks. Replaces the
+ * per-block reductions of Refinement::FirstDerivative / SecondDerivative
+ * (src/amr_criteria/refinement_package.cpp:93-150) called from AMRFirstDerivative /
+ * AMRSecondDerivative::operator() (src/amr_criteria/amr_criteria.cpp:87-105). */
+int pgb_amr_block_criterion(pgb_mesh *mesh, const double *u, int32_t ncomp, int32_t comp, int32_t method,
+                            double *out, void *stream);
+
+/* Host: refinement flags (+1, 0, -1 per block in gid order) from the criterion values
+ * crit[nblocks] (host memory): refine above refine_tol, derefine below derefine_tol,
+ * no refinement at or above crit_max_level; then the mesh's per-block derefinement
+ * counters (kept in the handle and carried across pgb_amr_remesh) turn derefine tags
+ * into -1 only after derefine_count consecutive tags and only without a finer
+ * neighbour; no refinement at mesh_max_level. Replaces CheckAllRefinement
+ * (src/amr_criteria/refinement_package.cpp:51-91) + MeshRefinement::SetRefinement
+ * (src/mesh/mesh_refinement.cpp:82-118). */
+int pgb_amr_set_refinement(pgb_mesh *mesh, const double *crit, double refine_tol, double derefine_tol,
+                           int32_t crit_max_level, int32_t mesh_max_level, int32_t derefine_count,
+                           int32_t *flags);
+
+/* Host: the mesh after one adaptive step with the given flags (proper nesting kept, a
+ * parent derefined only when all eight children ask). *out is a new, not yet uploaded
+ * handle, or NULL when the leaf set does not change. Replaces Mesh::UpdateMeshBlockTree
+ * (src/mesh/mesh-amr_loadbalance.cpp:496-629) with Tree::Refine / Tree::Derefine
+ * (src/mesh/forest/tree.cpp:82-137,221-267). */
+int pgb_amr_remesh(pgb_mesh *mesh, const int32_t *flags, pgb_mesh **out);
+
+/* Moves a field from the old mesh to the new one (both uploaded): same-level blocks are
+ * copied, new fine blocks are minmod-prolongated from their parent over the whole
+ * array, new coarse blocks get their children's interiors restricted (ghosts zero; run
+ * an exchange with PGB_EXCHANGE_PROLONGATE afterwards). One launch; synchronises the
+ * stream. Replaces the same-rank data movement of RedistributeAndRefineMeshBlocks
+ * (src/mesh/mesh-amr_loadbalance.cpp:663-1010, amr_loadbalance.cpp:95-135,205-245). */
+int pgb_amr_transfer(pgb_mesh *old_mesh, pgb_mesh *new_mesh, const double *old_data, double *new_data,
+                     int32_t ncomp, void *stream);
 
 #ifdef __cplusplus
 }

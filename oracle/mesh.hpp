@@ -128,6 +128,79 @@ struct Mesh {
     for (auto it = chain.rbegin(); it != chain.rend(); ++it) refine(*it);
   }
 
+  // ---- adaptive step (mesh-amr_loadbalance.cpp:496-629, tree.cpp:82-137, 221-267)
+  Loc wrap_loc(const Loc &n) const {
+    int off[3];
+    tree_offset(n, off);
+    return xform(n, off);
+  }
+  int tree_refine(const Loc &ref) {
+    if (!leaves.count(ref)) return 0;
+    leaves.erase(ref);
+    internal.insert(ref);
+    for (auto &d : ref.daughters()) leaves.insert(d);
+    int nadded = 7;
+    const Loc par = ref.parent();
+    const int64_t o1 = ref.l[0] - (par.l[0] << 1), o2 = ref.l[1] - (par.l[1] << 1), o3 = ref.l[2] - (par.l[2] << 1);
+    for (int k = 0; k < 2; ++k)
+      for (int j = 0; j < 2; ++j)
+        for (int i = 0; i < 2; ++i) {
+          Loc neigh(par.level, par.l[0] + i + o1 - 1, par.l[1] + j + o2 - 1, par.l[2] + k + o3 - 1);
+          nadded += tree_refine(wrap_loc(neigh));
+        }
+    return nadded;
+  }
+  int tree_derefine(const Loc &ref) {
+    auto ds = ref.daughters();
+    for (auto &d : ds) {
+      if (!leaves.count(d)) return 0;
+      for (int k = -1; k <= 1; ++k)
+        for (int j = -1; j <= 1; ++j)
+          for (int i = -1; i <= 1; ++i) {
+            Loc neigh(d.level, d.l[0] + i, d.l[1] + j, d.l[2] + k);
+            if (internal.count(wrap_loc(neigh))) return 0;
+          }
+    }
+    for (auto &d : ds) leaves.erase(d);
+    internal.erase(ref);
+    leaves.insert(ref);
+    return (int)ds.size() - 1;
+  }
+  // flags per leaf block in gid order (+1 refine, -1 derefine, 0 keep); rebuilds
+  // gids, blocks and neighbours. Returns true when the tree changed.
+  bool update_tree(const std::vector<int> &flags) {
+    std::vector<Loc> lref, lderef, cl;
+    for (size_t b = 0; b < blocks.size(); ++b) {
+      if (flags[b] == 1) lref.push_back(blocks[b].loc);
+      if (flags[b] == -1) lderef.push_back(blocks[b].loc);
+    }
+    const int nleaf = 8;
+    const int tnderef = (int)lderef.size();
+    if (lref.empty() && tnderef < nleaf) return false;
+    if (tnderef >= nleaf) {
+      for (int n = 0; n < tnderef; ++n) {
+        if ((lderef[n].l[0] & 1) || (lderef[n].l[1] & 1) || (lderef[n].l[2] & 1)) continue;
+        int r = n, rr = 0;
+        for (int64_t k = 0; k <= 1; ++k)
+          for (int64_t j = 0; j <= 1; ++j)
+            for (int64_t i = 0; i <= 1; ++i)
+              if (r < tnderef) {
+                if (lderef[n].l[0] + i == lderef[r].l[0] && lderef[n].l[1] + j == lderef[r].l[1] &&
+                    lderef[n].l[2] + k == lderef[r].l[2] && lderef[n].level == lderef[r].level)
+                  rr++;
+                r++;
+              }
+        if (rr == nleaf) cl.push_back(lderef[n].parent());
+      }
+    }
+    if (cl.size() > 1)
+      std::stable_sort(cl.begin(), cl.end() - 1, [](const Loc &a, const Loc &b) { return a.level > b.level; });
+    int changed = 0;
+    for (auto &l : lref) changed += tree_refine(l);
+    for (auto &l : cl) changed += tree_derefine(l);
+    return changed != 0;
+  }
+
   // Periodic self-link transform (forest.cpp:170-190: use_offset with the tree offset)
   static void tree_offset(const Loc &n, int off[3]) {
     const int64_t up = 1ll << std::max(n.level, 0);

@@ -653,6 +653,144 @@ inline double advection_min_dt(Field &U, const double vel[3]) {
   return mn;
 }
 
+// ---------------------------------------------------------------- AMR
+// refinement_package.cpp:93-120 (FirstDerivative) on one component of one block.
+inline double first_derivative_max(Field &U, int b, int comp) {
+  const int ng = U.mesh->p.ng;
+  double maxd = 0.0;
+  for (int k = ng; k < U.N[2] - ng; ++k)
+    for (int j = ng; j < U.N[1] - ng; ++j)
+      for (int i = ng; i < U.N[0] - ng; ++i) {
+        const double scale = std::fabs(U.at(b, comp, k, j, i));
+        double d = 0.5 * std::fabs((U.at(b, comp, k, j, i + 1) - U.at(b, comp, k, j, i - 1))) / (scale + 1.0e-20);
+        maxd = (d > maxd ? d : maxd);
+        d = 0.5 * std::fabs((U.at(b, comp, k, j + 1, i) - U.at(b, comp, k, j - 1, i))) / (scale + 1.0e-20);
+        maxd = (d > maxd ? d : maxd);
+        d = 0.5 * std::fabs((U.at(b, comp, k + 1, j, i) - U.at(b, comp, k - 1, j, i))) / (scale + 1.0e-20);
+        maxd = (d > maxd ? d : maxd);
+      }
+  return maxd;
+}
+
+// refinement_package.cpp:122-150 (SecondDerivative) on one component of one block.
+inline double second_derivative_max(Field &U, int b, int comp) {
+  const int ng = U.mesh->p.ng;
+  double maxd = 0.0;
+  for (int k = ng; k < U.N[2] - ng; ++k)
+    for (int j = ng; j < U.N[1] - ng; ++j)
+      for (int i = ng; i < U.N[0] - ng; ++i) {
+        const double q = U.at(b, comp, k, j, i);
+        const double aqt = std::fabs(q) + 1.0e-20;
+        double qavg = 0.5 * (U.at(b, comp, k, j, i + 1) + U.at(b, comp, k, j, i - 1));
+        double d = std::fabs(qavg - q) / (std::fabs(qavg) + aqt);
+        maxd = (d > maxd ? d : maxd);
+        qavg = 0.5 * (U.at(b, comp, k, j + 1, i) + U.at(b, comp, k, j - 1, i));
+        d = std::fabs(qavg - q) / (std::fabs(qavg) + aqt);
+        maxd = (d > maxd ? d : maxd);
+        qavg = 0.5 * (U.at(b, comp, k + 1, j, i) + U.at(b, comp, k - 1, j, i));
+        d = std::fabs(qavg - q) / (std::fabs(qavg) + aqt);
+        maxd = (d > maxd ? d : maxd);
+      }
+  return maxd;
+}
+
+// Largest central-difference gradient magnitude |grad q| of one component of one block
+// (the absolute-gradient criterion; the caller scales its tolerances by the mesh maximum).
+inline double gradient_max(Field &U, const Coords &c, int b, int comp) {
+  const int ng = U.mesh->p.ng;
+  double maxd = 0.0;
+  for (int k = ng; k < U.N[2] - ng; ++k)
+    for (int j = ng; j < U.N[1] - ng; ++j)
+      for (int i = ng; i < U.N[0] - ng; ++i) {
+        const double gx = 0.5 * (U.at(b, comp, k, j, i + 1) - U.at(b, comp, k, j, i - 1)) / c.dx[0];
+        const double gy = 0.5 * (U.at(b, comp, k, j + 1, i) - U.at(b, comp, k, j - 1, i)) / c.dx[1];
+        const double gz = 0.5 * (U.at(b, comp, k + 1, j, i) - U.at(b, comp, k - 1, j, i)) / c.dx[2];
+        const double d = std::sqrt((gx * gx + gy * gy) + gz * gz);
+        maxd = (d > maxd ? d : maxd);
+      }
+  return maxd;
+}
+
+// CheckAllRefinement (refinement_package.cpp:51-91) for one criterion followed by
+// MeshRefinement::SetRefinement (mesh_refinement.cpp:82-118). `crit_max_level` is the
+// criterion's level cap, `mesh_max_level` the mesh's; deref_count is per block state.
+inline int set_refinement(double crit, double rtol, double dtol, int level, int crit_max_level, int root_level,
+                          int mesh_max_level, bool finer_neighbor, int threshold, int &deref_count) {
+  int tag = crit > rtol ? 1 : (crit < dtol ? -1 : 0);
+  if (tag == 1 && level >= crit_max_level) tag = 0;
+  int flag = 0;
+  if (tag >= 0) deref_count = 0;
+  if (tag > 0) {
+    flag = level == mesh_max_level ? 0 : 1;
+  } else if (tag < 0) {
+    if (level == root_level) {
+      flag = 0;
+      deref_count = 0;
+    } else {
+      deref_count++;
+      if (finer_neighbor) flag = 0;
+      else flag = deref_count >= threshold ? -1 : 0;
+    }
+  }
+  return flag;
+}
+
+// RedistributeAndRefineMeshBlocks data movement (mesh-amr_loadbalance.cpp:663-1010):
+// same-level blocks copy their whole array; a new fine block takes the parent's data
+// into its coarse buffer (TryRecvCoarseToFine, :95-135) and prolongates (minmod) over
+// the coarse interior +- ng/2; a new coarse block receives each child's interior
+// restricted into the child's coarse buffer (TryRecvFineToCoarse, :205-245).
+inline void transfer(const Mesh &om, const std::vector<Block> &ob, Field &of, const Mesh &nm,
+                     std::vector<Block> &nb, Field &nf) {
+  const int ng = nm.p.ng;
+  const int n = nm.p.bnx[0], h = n / 2;
+  std::map<std::tuple<int, int64_t, int64_t, int64_t>, int> old_index;
+  for (size_t b = 0; b < ob.size(); ++b)
+    old_index[{ob[b].loc.level, ob[b].loc.l[0], ob[b].loc.l[1], ob[b].loc.l[2]}] = (int)b;
+  auto find = [&](const Loc &l) {
+    auto it = old_index.find({l.level, l.l[0], l.l[1], l.l[2]});
+    return it == old_index.end() ? -1 : it->second;
+  };
+  for (size_t b = 0; b < nb.size(); ++b) {
+    const Loc &L = nb[b].loc;
+    const int same = find(L);
+    if (same >= 0) {
+      for (int v = 0; v < nf.ncomp; ++v)
+        for (int k = 0; k < nf.N[2]; ++k)
+          for (int j = 0; j < nf.N[1]; ++j)
+            for (int i = 0; i < nf.N[0]; ++i) nf.at((int)b, v, k, j, i) = of.at(same, v, k, j, i);
+      continue;
+    }
+    const int par = find(L.parent());
+    if (par >= 0) {
+      const int os[3] = {(int)(L.l[0] & 1) * h, (int)(L.l[1] & 1) * h, (int)(L.l[2] & 1) * h};
+      for (int v = 0; v < nf.ncomp; ++v) {
+        for (int k = 0; k < nf.Nc[2]; ++k)
+          for (int j = 0; j < nf.Nc[1]; ++j)
+            for (int i = 0; i < nf.Nc[0]; ++i) nf.cat((int)b, v, k, j, i) = of.at(par, v, k + os[2], j + os[1], i + os[0]);
+        for (int k = ng - ng / 2; k <= ng + h - 1 + ng / 2; ++k)
+          for (int j = ng - ng / 2; j <= ng + h - 1 + ng / 2; ++j)
+            for (int i = ng - ng / 2; i <= ng + h - 1 + ng / 2; ++i)
+              prolong_cell(nf, (int)b, v, k, j, i, nb[b].coords, nb[b].ccoords, PMinMod);
+      }
+      continue;
+    }
+    // derefined: eight children
+    for (auto &c : L.daughters()) {
+      const int ch = find(c);
+      if (ch < 0) throw std::runtime_error("remesh: block without a source");
+      const int os[3] = {(int)(c.l[0] & 1) * h, (int)(c.l[1] & 1) * h, (int)(c.l[2] & 1) * h};
+      for (int v = 0; v < nf.ncomp; ++v)
+        for (int k = ng; k < ng + h; ++k)
+          for (int j = ng; j < ng + h; ++j)
+            for (int i = ng; i < ng + h; ++i) {
+              restrict_cell(of, ch, v, k, j, i, ob[ch].coords);
+              nf.at((int)b, v, k + os[2], j + os[1], i + os[0]) = of.cat(ch, v, k, j, i);
+            }
+    }
+  }
+}
+
 // ---------------------------------------------------------------- simulation
 struct Sim {
   std::unique_ptr<Mesh> mesh;
@@ -669,6 +807,7 @@ struct Sim {
   double time = 0.0;
   int ncycle = 0;
   int64_t zone_cycles = 0;
+  std::vector<int> deref_count;  // per block, MeshRefinement::deref_count_
 };
 
 inline double estimate_dt(Sim &s, Field &U) {
@@ -868,6 +1007,80 @@ int64_t orc_pack(void *h, double *out) {
   return n;
 }
 int orc_max_threads() { return omp_get_max_threads(); }
+
+// Per-block criterion of component `comp` of the base field: method 0 FirstDerivative,
+// 1 SecondDerivative, 2 largest |grad q|.
+void orc_block_criterion(void *h, int comp, int method, double *out) {
+  Sim *s = (Sim *)h;
+  const int nb = (int)s->mesh->blocks.size();
+#pragma omp parallel for schedule(dynamic)
+  for (int b = 0; b < nb; ++b)
+    out[b] = method == 0   ? first_derivative_max(s->base, b, comp)
+             : method == 1 ? second_derivative_max(s->base, b, comp)
+                           : gradient_max(s->base, s->mesh->blocks[b].coords, b, comp);
+}
+
+// After a remesh every block of the new mesh votes on the current dt (no growth):
+// dt = min(dt, cfl * estimate over the new blocks).
+double orc_limit_dt(void *h) {
+  Sim *s = (Sim *)h;
+  s->dt = std::min(s->dt, estimate_dt(*s, s->base));
+  return s->dt;
+}
+
+// Refinement flags from per-block criterion values (tolerances already scaled).
+void orc_set_refinement(void *h, const double *crit, double rtol, double dtol, int crit_max_level,
+                        int mesh_max_level, int threshold, int *flags) {
+  Sim *s = (Sim *)h;
+  const auto &bl = s->mesh->blocks;
+  s->deref_count.resize(bl.size(), 0);
+  for (size_t b = 0; b < bl.size(); ++b) {
+    bool finer = false;
+    for (auto &n : bl[b].neighbors) finer = finer || n.loc.level > bl[b].loc.level;
+    flags[b] = set_refinement(crit[b], rtol, dtol, bl[b].loc.level, crit_max_level, s->mesh->root_level,
+                              mesh_max_level, finer, threshold, s->deref_count[b]);
+  }
+}
+
+// One adaptive step with per-block flags (+1, 0, -1 in gid order): tree update, new
+// blocks, data movement of the base field. Returns 1 when the mesh changed.
+int orc_remesh(void *h, const int *flags) {
+  Sim *s = (Sim *)h;
+  try {
+    std::vector<int> fl(flags, flags + s->mesh->blocks.size());
+    std::vector<Block> old_blocks = s->mesh->blocks;
+    Field old_base = s->base;
+    std::unique_ptr<Mesh> keep(new Mesh(*s->mesh));
+    old_base.mesh = keep.get();
+    old_base.blocks = &old_blocks;
+    if (!s->mesh->update_tree(fl)) return 0;
+    s->mesh->multilevel = true;
+    s->mesh->finalize();
+    // surviving blocks keep their derefinement counters, new blocks start at zero
+    std::map<std::tuple<int, int64_t, int64_t, int64_t>, int> old_count;
+    s->deref_count.resize(old_blocks.size(), 0);
+    for (size_t b = 0; b < old_blocks.size(); ++b) {
+      const Loc &l = old_blocks[b].loc;
+      old_count[{l.level, l.l[0], l.l[1], l.l[2]}] = s->deref_count[b];
+    }
+    s->deref_count.assign(s->mesh->blocks.size(), 0);
+    for (size_t b = 0; b < s->mesh->blocks.size(); ++b) {
+      const Loc &l = s->mesh->blocks[b].loc;
+      auto it = old_count.find({l.level, l.l[0], l.l[1], l.l[2]});
+      if (it != old_count.end()) s->deref_count[b] = it->second;
+    }
+    s->base.init(s->mesh.get(), &s->mesh->blocks, s->ncomp);
+    transfer(*keep, old_blocks, old_base, *s->mesh, s->mesh->blocks, s->base);
+    s->stage.init(s->mesh.get(), &s->mesh->blocks, s->ncomp);
+    s->dudt.init(s->mesh.get(), &s->mesh->blocks, s->ncomp);
+    s->flux.init(s->base);
+    s->recs = build_boundaries(*s->mesh, s->mesh->blocks, BAny, 0);
+    return 1;
+  } catch (std::exception &e) {
+    fprintf(stderr, "oracle remesh: %s\n", e.what());
+    return -1;
+  }
+}
 
 // Known-answer hooks for the reference unit tests (test_logical_location.cpp):
 // ownership of `main` among the given neighbour locations (level,l1,l2,l3 each),

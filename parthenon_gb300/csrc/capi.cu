@@ -61,6 +61,19 @@ struct pgb_mesh {
 namespace pgb {
 // Leaf-grid tables of a mesh handle (used by entry points defined in other units).
 GridTables *mesh_leaf_tables(pgb_mesh *m) { return m && m->st.uploaded ? &m->st.leaf : nullptr; }
+MeshState *mesh_state(pgb_mesh *m) { return m ? &m->st : nullptr; }
+// New (not uploaded) mesh handle over the given leaves.
+int mesh_from_leaves(const MeshSpec &spec, const std::vector<LLoc> &leaves, pgb_mesh **out) {
+  auto *m = new pgb_mesh();
+  try {
+    m->st.topo.reset(new MeshTopology(spec, leaves));
+  } catch (...) {
+    delete m;
+    throw;
+  }
+  *out = m;
+  return kOk;
+}
 }  // namespace pgb
 
 namespace {
@@ -290,6 +303,7 @@ int pgb_estimate_dt(pgb_mesh *m, const pgb_stage_params *p, const double *u, int
   int rc = check_params(m, p, ncomp);
   if (rc) return rc;
   if (!u || !dt) return fail(kErrInvalid, "null pointer");
+  if (first < 0 || first > 2) return fail(kErrInvalid, "first must be 0, 1 or 2");
   return estimate_dt(m->st, p->physics, u, ncomp, p->vel, p->cfl, dt, first, (cudaStream_t)stream);
 }
 

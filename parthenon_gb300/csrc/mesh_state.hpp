@@ -41,6 +41,7 @@ struct MeshState {
   double *d_scalars = nullptr;      // [0] dt, [1] reduction scratch ...
   unsigned long long *d_minbits = nullptr;
   int *d_status = nullptr;
+  std::vector<int> deref_count;     // per leaf block, MeshRefinement::deref_count_
   ~MeshState();
 };
 

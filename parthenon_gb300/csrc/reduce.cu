@@ -69,11 +69,13 @@ __global__ void k_advection_min(const DevBlockGeom *__restrict__ geom, int nbloc
 }
 
 // driver.cpp:210-232 with the default dt controls; resets the accumulator.
+// first: 0 regular step (growth limited to 2x), 1 first step, 2 extra vote on the
+// current dt without growth (after a remesh).
 __global__ void k_set_dt(double *dt, unsigned long long *minbits, double cfl, int first) {
   const double mn = __longlong_as_double((long long)*minbits);
   const double newdt = __dmul_rn(cfl, mn);
-  double t = first ? DBL_MAX : *dt;
-  if (t < 0.1 * DBL_MAX) t = __dmul_rn(t, 2.0);
+  double t = first == 1 ? DBL_MAX : *dt;
+  if (first != 2 && t < 0.1 * DBL_MAX) t = __dmul_rn(t, 2.0);
   t = fmin(t, newdt);
   t = fmax(DBL_MIN, fmin(t, DBL_MAX));
   *dt = t;

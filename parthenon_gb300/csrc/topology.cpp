@@ -461,6 +461,95 @@ void MeshTopology::build_grid_tables(GridTopology &g, bool composite) {
   }
 }
 
+namespace {
+// Working copy of the tree for one adaptive step (tree.cpp:82-137 Refine with proper
+// nesting, tree.cpp:221-267 Derefine).
+struct TreeEdit {
+  std::set<LLoc> leaves;
+  std::unordered_map<LLoc, int, LLocHash> internal;
+  static LLoc in_tree(const LLoc &n) {
+    // periodic single tree: bring a location back into [0, 2^level)
+    const int64_t w = 1ll << std::max(n.level, 0);
+    std::array<int64_t, 3> l;
+    for (int d = 0; d < 3; ++d) l[d] = ((n.lx[d] % w) + w) % w;
+    return LLoc(n.level, l[0], l[1], l[2]);
+  }
+  int refine(const LLoc &loc) {
+    if (!leaves.count(loc)) return 0;
+    leaves.erase(loc);
+    internal[loc] = 0;
+    for (auto &c : loc.children()) leaves.insert(c);
+    int added = 7;
+    const LLoc par = loc.parent();
+    int ox[3];
+    for (int d = 0; d < 3; ++d) ox[d] = (int)(loc.lx[d] - (par.lx[d] << 1));
+    for (int k = 0; k < 2; ++k)
+      for (int j = 0; j < 2; ++j)
+        for (int i = 0; i < 2; ++i) {
+          const LLoc ng(par.level, par.lx[0] + i + ox[0] - 1, par.lx[1] + j + ox[1] - 1, par.lx[2] + k + ox[2] - 1);
+          added += refine(in_tree(ng));
+        }
+    return added;
+  }
+  int derefine(const LLoc &loc) {
+    const auto kids = loc.children();
+    for (auto &d : kids) {
+      if (!leaves.count(d)) return 0;
+      for (int k = -1; k <= 1; ++k)
+        for (int j = -1; j <= 1; ++j)
+          for (int i = -1; i <= 1; ++i) {
+            const LLoc n = in_tree(LLoc(d.level, d.lx[0] + i, d.lx[1] + j, d.lx[2] + k));
+            if (internal.count(n)) return 0;
+          }
+    }
+    for (auto &d : kids) leaves.erase(d);
+    internal.erase(loc);
+    leaves.insert(loc);
+    return (int)kids.size() - 1;
+  }
+};
+}  // namespace
+
+std::vector<LLoc> MeshTopology::amr_update(const std::vector<int> &flags) const {
+  const auto &bl = leaf_.blocks;
+  if (flags.size() != bl.size()) throw std::invalid_argument("one flag per leaf block is required");
+  TreeEdit t;
+  t.leaves = leaves_;
+  t.internal = internal_;
+  std::vector<LLoc> lref, lderef;
+  for (size_t b = 0; b < bl.size(); ++b) {
+    if (flags[b] == 1) lref.push_back(bl[b].loc);
+    if (flags[b] == -1) lderef.push_back(bl[b].loc);
+  }
+  const int nleaf = 8;
+  std::vector<LLoc> cl;
+  if ((int)lderef.size() >= nleaf) {
+    const int nd = (int)lderef.size();
+    for (int n = 0; n < nd; ++n) {
+      const LLoc &a = lderef[n];
+      if ((a.lx[0] & 1) || (a.lx[1] & 1) || (a.lx[2] & 1)) continue;
+      int r = n, rr = 0;
+      for (int k = 0; k <= 1; ++k)
+        for (int j = 0; j <= 1; ++j)
+          for (int i = 0; i <= 1; ++i) {
+            if (r < nd) {
+              const LLoc &q = lderef[r];
+              if (a.lx[0] + i == q.lx[0] && a.lx[1] + j == q.lx[1] && a.lx[2] + k == q.lx[2] && a.level == q.level)
+                ++rr;
+              ++r;
+            }
+          }
+      if (rr == nleaf) cl.push_back(a.parent());
+    }
+  }
+  // the reference orders all but the last candidate by decreasing level
+  if (cl.size() > 1)
+    std::stable_sort(cl.begin(), cl.end() - 1, [](const LLoc &x, const LLoc &y) { return x.level > y.level; });
+  for (auto &l : lref) t.refine(l);
+  for (auto &l : cl) t.derefine(l);
+  return std::vector<LLoc>(t.leaves.begin(), t.leaves.end());
+}
+
 void MeshTopology::build_multigrid() {
   // Blocks per multigrid logical level: leaves of that level, leaves one level coarser
   // (two-level composite), and internal blocks sharing a Morton key with a leaf.

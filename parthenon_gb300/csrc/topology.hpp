@@ -143,8 +143,12 @@ class MeshTopology {
   int mg_min_level() const { return mg_min_level_; }
   int gid_of(const LLoc &l) const;
   bool is_leaf(const LLoc &l) const { return leaves_.count(l) != 0; }
-  // Transfer lists between multigrid levels: for each block of level `lev` the list of
-  // finer (or leaf-self) blocks of level lev+1 it restricts from / prolongates to.
+  // Leaf set after one adaptive step (Mesh::UpdateMeshBlockTree,
+  // mesh-amr_loadbalance.cpp:496-629): flags per leaf in gid order, +1 refine, -1
+  // derefine (a parent is derefined only when all eight children ask), 0 keep;
+  // refinement keeps neighbouring levels within one of each other.
+  std::vector<LLoc> amr_update(const std::vector<int> &flags) const;
+  const std::set<LLoc> &leaves() const { return leaves_; }
   std::string error;
 
  private:

@@ -44,13 +44,21 @@ class RK2Driver:
 
     def __init__(self, mesh, ncomp, config, stream=None):
         import torch
-        self.mesh = mesh.upload() if not mesh._uploaded else mesh
         self.ncomp = int(ncomp)
         self.cfg = config
         self.params = config.params()
         self.stream = stream if stream is not None else torch.cuda.Stream()
+        self._allocate(mesh)
         with torch.cuda.stream(self.stream):
-            self.base = mesh.new_field(ncomp)
+            self.dt = torch.zeros(1, dtype=torch.float64, device="cuda")
+        self.ncycle = 0
+
+    def _allocate(self, mesh, base=None):
+        import torch
+        self.mesh = mesh.upload() if not mesh._uploaded else mesh
+        ncomp = self.ncomp
+        with torch.cuda.stream(self.stream):
+            self.base = mesh.new_field(ncomp) if base is None else base
             self.stage = mesh.new_field(ncomp)
             if mesh.multilevel:
                 self.dudt = None
@@ -62,8 +70,21 @@ class RK2Driver:
                 self.dudt = mesh.new_field(ncomp)
                 self.flux = None
                 self.cbase = self.cstage = None
-            self.dt = torch.zeros(1, dtype=torch.float64, device="cuda")
-        self.ncycle = 0
+
+    def rebind(self, mesh, base):
+        """Continue on a new mesh (after a remesh) with `base` already on it: fresh
+        scratch and coarse buffers, ghosts filled with prolongation (the post-remesh
+        CommunicateBoundaries of RedistributeAndRefineMeshBlocks), then every block of
+        the new mesh votes on the current dt. The cycle graph is captured again on the
+        next run because the new mesh handle has an empty graph cache."""
+        import torch
+        self._allocate(mesh, base)
+        with torch.cuda.stream(self.stream):
+            self.mesh.exchange(self.base, self.cbase, prolongate=True, stream=self.stream)
+            self.stage.copy_(self.base)
+            nat.check(nat.lib().pgb_estimate_dt(self.mesh.handle, ctypes.byref(self.params), _ptr(self.base),
+                                                self.ncomp, _ptr(self.dt), 2, _stream(self.stream)),
+                      "pgb_estimate_dt")
 
     @property
     def prolongate(self):
@@ -73,11 +94,12 @@ class RK2Driver:
 
     def set_state(self, host_array):
         """Load the initial condition (numpy, field layout incl. ghosts), fill ghosts
-        (Mesh::Initialize -> CommunicateBoundaries) and set the first dt."""
+        (Mesh::Initialize -> Mesh::CommunicateBoundaries, which prolongates on
+        multilevel meshes for every package, mesh.cpp:640-706) and set the first dt."""
         import torch
         with torch.cuda.stream(self.stream):
             self.base.copy_(torch.as_tensor(host_array, dtype=torch.float64), non_blocking=False)
-            self.mesh.exchange(self.base, self.cbase, prolongate=self.prolongate, stream=self.stream)
+            self.mesh.exchange(self.base, self.cbase, prolongate=True, stream=self.stream)
             self.stage.copy_(self.base)
             nat.check(nat.lib().pgb_estimate_dt(self.mesh.handle, ctypes.byref(self.params), _ptr(self.base),
                                                 self.ncomp, _ptr(self.dt), 1, _stream(self.stream)),

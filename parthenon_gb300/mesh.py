@@ -13,6 +13,7 @@ import numpy as np
 from . import _native as nat
 
 PROLONG_OPS = {"minmod": 0, "linear": 2, "constant": 4}
+CRITERIA = {"first": 0, "second": 1, "gradient": 2}
 
 
 def _ptr(t):
@@ -49,6 +50,17 @@ class Mesh:
         nat.check(L.pgb_mesh_create(ctypes.byref(spec), int(lv.shape[0]), lv.ctypes.data_as(ctypes.c_void_p),
                                     ctypes.byref(h)), "pgb_mesh_create")
         self._h = h
+        self._read_info(nghost, block_nx)
+
+    @classmethod
+    def _wrap(cls, handle, nghost, block_nx):
+        m = cls.__new__(cls)
+        m._h = handle
+        m._read_info(nghost, block_nx)
+        return m
+
+    def _read_info(self, nghost, block_nx):
+        L = nat.lib()
         self.nghost = int(nghost)
         self.block_nx = tuple(int(b) for b in block_nx)
         info = nat.MeshInfo()
@@ -138,6 +150,57 @@ class Mesh:
     def flux_correct(self, flux, ncomp, stream=None):
         self._ensure()
         nat.check(nat.lib().pgb_flux_correct(self._h, _ptr(flux), ncomp, _stream(stream)), "pgb_flux_correct")
+
+    # ---------------------------------------------------------------- adaptive refinement
+    def block_criterion(self, field, comp, method="first", stream=None):
+        """Per-block refinement criterion of one component (device tensor, one value per block).
+
+        method: "first" (FirstDerivative), "second" (SecondDerivative) or "gradient"
+        (largest |grad q|). The field's ghosts must be current.
+        """
+        import torch
+        self._ensure()
+        out = torch.empty(self.nblocks, dtype=torch.float64, device="cuda")
+        nat.check(nat.lib().pgb_amr_block_criterion(self._h, _ptr(field), field.shape[1], int(comp),
+                                                    CRITERIA[method], _ptr(out), _stream(stream)),
+                  "pgb_amr_block_criterion")
+        return out
+
+    def set_refinement(self, crit, refine_tol, derefine_tol, crit_max_level, mesh_max_level, derefine_count=10):
+        """Refinement flags (+1/0/-1 per block) from host criterion values; updates the
+        per-block derefinement counters kept with the mesh."""
+        c = np.ascontiguousarray(crit, np.float64)
+        if c.shape != (self.nblocks,):
+            raise ValueError("one criterion value per block is required")
+        flags = np.zeros(self.nblocks, np.int32)
+        nat.check(nat.lib().pgb_amr_set_refinement(self._h, c.ctypes.data_as(ctypes.c_void_p), float(refine_tol),
+                                                   float(derefine_tol), int(crit_max_level), int(mesh_max_level),
+                                                   int(derefine_count), flags.ctypes.data_as(ctypes.c_void_p)),
+                  "pgb_amr_set_refinement")
+        return flags
+
+    def remesh(self, flags):
+        """The mesh after one adaptive step, or None when the leaf set is unchanged."""
+        f = np.ascontiguousarray(flags, np.int32)
+        if f.shape != (self.nblocks,):
+            raise ValueError("one flag per block is required")
+        h = ctypes.c_void_p()
+        nat.check(nat.lib().pgb_amr_remesh(self._h, f.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h)),
+                  "pgb_amr_remesh")
+        if not h:
+            return None
+        return Mesh._wrap(h, self.nghost, self.block_nx)
+
+    def transfer(self, new_mesh, field, stream=None):
+        """New field on new_mesh: same-level copies, prolongated new fine blocks,
+        restricted new coarse blocks (ghosts to be filled by an exchange)."""
+        self._ensure()
+        new_mesh._ensure()
+        ncomp = field.shape[1]
+        out = new_mesh.new_field(ncomp)
+        nat.check(nat.lib().pgb_amr_transfer(self._h, new_mesh._h, _ptr(field), _ptr(out), ncomp, _stream(stream)),
+                  "pgb_amr_transfer")
+        return out
 
     @property
     def handle(self):

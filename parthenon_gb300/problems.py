@@ -80,6 +80,52 @@ def burgers_state(mesh, nscalars=8, nmodes=8, kmax=4, seed=2):
     return out
 
 
+class BlockGeometry:
+    """Cell-centre geometry of a block list given as (nblocks, 6) rows of
+    (xmin1, xmin2, xmin3, dx1, dx2, dx3) -- the layout Mesh.block_info returns -- so the
+    problem generators can run on any block list."""
+
+    def __init__(self, geom, nghost, block_nx):
+        self.geom = np.asarray(geom, np.float64)
+        self.nblocks = self.geom.shape[0]
+        self.nghost = int(nghost)
+        self.block_nx = tuple(int(b) for b in block_nx)
+        self.N = tuple(b + 2 * self.nghost for b in self.block_nx)
+
+    def cell_centers(self):
+        out = []
+        for d in range(3):
+            idx = np.arange(self.N[d]) - self.nghost
+            out.append(self.geom[:, d:d + 1] + (idx[None, :] + 0.5) * self.geom[:, 3 + d:4 + d])
+        return out
+
+
+def burgers_amr_state(mesh, nscalars=2, nmodes=16, kmax=6, seed=5):
+    """Adaptive Burgers initial data, a pure function of position so that it can be
+    evaluated again on every refined mesh (as Mesh::Initialize re-runs the problem
+    generator while the initial refinement settles): velocity = sum of `nmodes`
+    random-phase sinusoids per component with wave vectors in {1..kmax}^3 (seeded);
+    scalar s (s = 0, 1, ...) = 1 + 0.5 sin(2 pi (s+1) x) sin(2 pi y) sin(2 pi z)."""
+    ncomp = 3 + nscalars
+    out = np.zeros((mesh.nblocks, ncomp) + tuple(mesh.N[::-1]), np.float64)
+    sk, sj, si = _interior(mesh)
+    xs, ys, zs = _centers(mesh)
+    g = mesh.nghost
+    n = mesh.block_nx
+    x = xs[:, g:g + n[0]][:, None, None, :]
+    y = ys[:, g:g + n[1]][:, None, :, None]
+    z = zs[:, g:g + n[2]][:, :, None, None]
+    for c, (k, a, phi) in enumerate(sinusoid_modes(nmodes, kmax, seed)):
+        acc = np.zeros((mesh.nblocks, n[2], n[1], n[0]))
+        for m in range(nmodes):
+            acc += a[m] * np.sin(2.0 * np.pi * (k[m, 2] * z + k[m, 1] * y + k[m, 0] * x) + phi[m])
+        out[:, c, sk, sj, si] = acc
+    for s in range(nscalars):
+        out[:, 3 + s, sk, sj, si] = 1.0 + 0.5 * (np.sin(2.0 * np.pi * (s + 1) * x) * np.sin(2.0 * np.pi * y) *
+                                                 np.sin(2.0 * np.pi * z))
+    return out
+
+
 def poisson_rhs(n, ngauss=32, sigma=0.03, seed=4):
     """Sum of `ngauss` Gaussians (width sigma, centres U[0,1]^3, amplitudes N(0,1), seeded)
     with periodic-image distances on the unit cube, minus its mean; array (n, n, n),

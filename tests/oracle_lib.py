@@ -67,6 +67,13 @@ def lib():
         L.orc_range_mask.restype = ctypes.c_uint32
         L.orc_morton.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int64,
                                  ctypes.c_int64, ctypes.c_void_p]
+        L.orc_block_criterion.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.orc_set_refinement.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.orc_remesh.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_remesh.restype = ctypes.c_int
+        L.orc_limit_dt.argtypes = [ctypes.c_void_p]
+        L.orc_limit_dt.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -157,6 +164,31 @@ class OracleSim:
         n = lib().orc_pack(self.h, _ptr(out))
         assert n == total
         return out[:total]
+
+    # adaptive refinement
+    def block_criterion(self, comp, method=0):
+        out = np.zeros(self.nblocks, np.float64)
+        lib().orc_block_criterion(self.h, int(comp), int(method), _ptr(out))
+        return out
+
+    def set_refinement(self, crit, rtol, dtol, crit_max_level, mesh_max_level, threshold=10):
+        c = np.ascontiguousarray(crit, np.float64)
+        flags = np.zeros(self.nblocks, np.int32)
+        lib().orc_set_refinement(self.h, _ptr(c), float(rtol), float(dtol), int(crit_max_level),
+                                 int(mesh_max_level), int(threshold), _ptr(flags))
+        return flags
+
+    def remesh(self, flags):
+        """Tree update + data movement of the base field; True when the mesh changed."""
+        f = np.ascontiguousarray(flags, np.int32)
+        rc = lib().orc_remesh(self.h, _ptr(f))
+        if rc < 0:
+            raise RuntimeError("oracle remesh failed")
+        self.nblocks = lib().orc_nblocks(self.h)
+        return rc == 1
+
+    def limit_dt(self):
+        return lib().orc_limit_dt(self.h)
 
 
 def ownership(main, locs):
