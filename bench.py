@@ -12,6 +12,10 @@ than the 129 MB L2). Prints one JSON line (rank 0).
 --impl reference times the CPU restatement of the reference algorithm (the oracle,
 all host threads) on a bounded sample of the same workload: 64 meshblocks of 32^3
 with the same ghosts, components and physics, one RK2 cycle per step.
+
+Extra legs in the same line: per-kernel rooflines, the end-to-end host-buffer run, the
+multigrid solve (FP64 vs mixed precision, key "gmg") and the adaptive 3-level Burgers
+run (key "amr", --amr-cycles cycles with remeshing inside the timed region).
 """
 import argparse
 import ctypes
@@ -255,6 +259,9 @@ def run_ours(args, ws, rank):
     out["gmg"] = gmg_bench(torch)
     if rank == 0 and ws == 1:
         out["cpu_baseline"] = cpu_baseline(steps=1)
+    del drv, state, host_in, host_out
+    if args.amr_cycles > 0:
+        out["amr"] = amr_bench(torch, args.amr_cycles, with_cpu=(rank == 0 and ws == 1))
     return out
 
 
@@ -292,6 +299,101 @@ def gmg_bench(torch):
     res["config"] = {"n": GMG_N, "levels": GMG_COARSEN + 1, "smoother": "weighted Jacobi 2/3, 2+2",
                      "coarse": "+16 smoother passes, FP64", "rhs": "32 Gaussians sigma 0.03 seed 4, mean removed"}
     return res
+
+
+AMR_ROOT, AMR_BLOCK, AMR_NUMLEVEL, AMR_NSCALARS, AMR_CHECK = 128, 16, 3, 2, 5
+
+
+def _amr_driver(pg, root):
+    crit = pg.RefinementCriterion(comps=(0, 1, 2), method="gradient", refine_tol=0.5, derefine_tol=0.05,
+                                  relative=True)
+    mesh = pg.Mesh((root,) * 3, (AMR_BLOCK,) * 3, NGHOST)
+    return pg.AMRDriver(mesh, 3 + AMR_NSCALARS, pg.StageConfig("burgers", "weno5", CFL), crit,
+                        numlevel=AMR_NUMLEVEL, derefine_count=10, check_interval=AMR_CHECK)
+
+
+def amr_bench(torch, cycles, with_cpu):
+    """Adaptive Burgers: 128^3 root in 16^3 blocks, 3 levels, refine above 0.5 and
+    derefine below 0.05 of the mesh-wide max |grad u| (checked every 5 cycles, 10
+    consecutive derefine tags needed), 16 random-phase sinusoids with wavenumbers 1-6,
+    2 passive scalars, WENO5 + HLL, RK2, CFL 0.8. Zone-cycles/s over `cycles` cycles
+    with every check, remesh, data movement and graph re-capture inside the timed
+    region; the initial refinement (problem generation repeated on each new mesh) is
+    timed separately."""
+    import parthenon_gb300 as pg
+    drv = _amr_driver(pg, AMR_ROOT)
+    adapt_s = []
+    inner = drv.adapt
+
+    def timed_adapt():
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        changed = inner()
+        torch.cuda.synchronize()
+        adapt_s.append((time.perf_counter() - t, changed))
+        return changed
+
+    drv.adapt = timed_adapt
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    drv.initialize(lambda m: pg.problems.burgers_amr_state_device(m, nscalars=AMR_NSCALARS))
+    torch.cuda.synchronize()
+    init_s = time.perf_counter() - t0
+    init_blocks = drv.mesh.nblocks
+    adapt_s.clear()
+    hist0 = len(drv.block_history)
+    drv.run(2)  # warm-up: first graph capture on this mesh
+    torch.cuda.synchronize()
+    zc0 = drv.zone_cycles
+    t0 = time.perf_counter()
+    drv.run(cycles)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    zc = drv.zone_cycles - zc0
+    blocks = drv.block_history[hist0 - 1:]
+    levels = np.bincount(drv.mesh.block_info()[0][:, 0])
+    res = {
+        "value": zc / el, "unit": METRIC, "cycles": cycles, "seconds": el, "ms_per_cycle": 1e3 * el / cycles,
+        "zone_cycles": zc, "init_seconds": init_s, "blocks_after_init": init_blocks,
+        "blocks_min": int(min(blocks)), "blocks_max": int(max(blocks)), "blocks_final": drv.mesh.nblocks,
+        "levels_final": {str(l): int(c) for l, c in enumerate(levels) if c},
+        "checks": len(adapt_s), "remeshes": int(sum(1 for _, c in adapt_s if c)),
+        "check_seconds": float(sum(t for t, _ in adapt_s)),
+        "remesh_seconds_max": float(max([t for t, c in adapt_s if c], default=0.0)),
+        "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9,
+        "config": {"workload": "burgers3d-amr-128^3root-16^3blocks-3levels-ng4-5vars-fp64",
+                   "criterion": "|grad u| relative: refine > 0.5 max, derefine < 0.05 max (10 tags)",
+                   "check_interval": AMR_CHECK, "initial": "16 sinusoids, k in 1..6, seed 5; 2 scalars"},
+    }
+    del drv
+    if with_cpu:
+        res["cpu_baseline"] = amr_cpu_baseline(torch, pg)
+    return res
+
+
+def amr_cpu_baseline(torch, pg):
+    """One RK2 cycle of the oracle (all host threads) on the 64^3-root analogue of the
+    adaptive workload: the same criterion, levels, physics and multilevel machinery
+    (flux correction, coarse buffers) on an eighth of the volume."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    drv = _amr_driver(pg, AMR_ROOT // 2)
+    drv.initialize(lambda m: pg.problems.burgers_amr_state_device(m, nscalars=AMR_NSCALARS))
+    drv.stream.synchronize()
+    locs, _ = drv.mesh.block_info()
+    o = O.OracleSim((AMR_ROOT // 2,) * 3, (AMR_BLOCK,) * 3, NGHOST, leaves=locs, ncomp=3 + AMR_NSCALARS,
+                    physics="burgers", recon=0, cfl=CFL, prolong_in_stage=False)
+    o.base()[:] = drv.base.cpu().numpy()
+    o.exchange(True, 0)
+    o.init_dt()
+    threads = O.lib().orc_max_threads()
+    t0 = time.perf_counter()
+    o.run(1, nthreads=threads)
+    el = time.perf_counter() - t0
+    zones = drv.mesh.nblocks * AMR_BLOCK ** 3
+    return {"value": zones / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "1 RK2 cycle of %d meshblocks of 16^3 (64^3-root analogue, 3 levels), no remesh" %
+                      drv.mesh.nblocks}
 
 
 def cpu_baseline(steps):
@@ -350,6 +452,8 @@ def main():
     ap.add_argument("--mesh", type=int, default=MESH_N, help="cells per direction (profiling runs use 128)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the per-kernel timing, end-to-end and CPU-baseline legs (profiling runs)")
+    ap.add_argument("--amr-cycles", type=int, default=100,
+                    help="cycles of the adaptive Burgers leg (0 skips it)")
     args = ap.parse_args()
     ws, rank = _dist()
     if ws > 1:

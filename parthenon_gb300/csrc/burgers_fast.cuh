@@ -231,6 +231,12 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
         } else {
           F = (ca[fi] * lprev - cb[fi] * qr + cc[fi] * (qr - lprev)) * (half * ci[fi]);
         }
+        if (MODE == kStoreFlux) {
+          // face p of direction D at the index of the cell on its right (multilevel path)
+          if (live) a.flux[c0 + ((int64_t)b * 2 + D) * NC * cs + (int64_t)comp * cs + (int64_t)p * step] = F;
+          lprev = ql;
+          continue;
+        }
         const double af = area * F;
         if (p >= 1 && live) {
           const int64_t e = c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step;
@@ -264,7 +270,7 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
 }
 
 template <int NC>
-int launch_burgers_nc(const StageArgs &a, cudaStream_t s) {
+int launch_burgers_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
   const Dims &d = a.d;
   static int nsm = 0;
   if (!nsm) {
@@ -284,9 +290,15 @@ int launch_burgers_nc(const StageArgs &a, cudaStream_t s) {
     const int64_t grid = std::min<int64_t>(groups, (int64_t)nsm * 2);
     kern<<<(unsigned)grid, 32 * NC, smem, s>>>(a, groups);
   };
-  go(k_burgers_dir<NC, 0, kStoreDu>, 0);
-  go(k_burgers_dir<NC, 1, kAddDu>, 1);
-  go(k_burgers_dir<NC, 2, kFinishUpdate>, 2);
+  if (store_flux) {
+    go(k_burgers_dir<NC, 0, kStoreFlux>, 0);
+    go(k_burgers_dir<NC, 1, kStoreFlux>, 1);
+    go(k_burgers_dir<NC, 2, kStoreFlux>, 2);
+  } else {
+    go(k_burgers_dir<NC, 0, kStoreDu>, 0);
+    go(k_burgers_dir<NC, 1, kAddDu>, 1);
+    go(k_burgers_dir<NC, 2, kFinishUpdate>, 2);
+  }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrCuda;
 }
 

@@ -36,12 +36,12 @@ int launch_div_update_nc(const StageArgs &a, cudaStream_t s) {
 // physics 0 = advection, 1 = Burgers; store_flux selects the multilevel path.
 int launch_stage(const StageArgs &a, int ncomp, int physics, bool store_flux, cudaStream_t s) {
 #ifdef PGB_HAVE_BURGERS_FAST
-  // WENO5 on uniform meshes: per-face HLL coefficients shared by all components
-  if (physics == 1 && !store_flux && a.recon == 0) {
+  // WENO5: per-face HLL coefficients shared by all components (uniform and multilevel)
+  if (physics == 1 && a.recon == 0) {
     switch (ncomp) {
-      case 4: return launch_burgers_nc<4>(a, s);
-      case 5: return launch_burgers_nc<5>(a, s);
-      case 11: return launch_burgers_nc<11>(a, s);
+      case 4: return launch_burgers_nc<4>(a, store_flux, s);
+      case 5: return launch_burgers_nc<5>(a, store_flux, s);
+      case 11: return launch_burgers_nc<11>(a, store_flux, s);
       default: break;
     }
   }

@@ -19,15 +19,16 @@ inline uint64_t interleave3(uint64_t v) {
 }
 }  // namespace
 
-void LLoc::make_key() {
+void LLoc::make_key() const {
   // Shift the location to level 63 and interleave 21-bit chunks, most significant first.
   const int lev = std::max(level, 0);
   const uint64_t x = (uint64_t)lx[0] << (63 - lev), y = (uint64_t)lx[1] << (63 - lev),
                  z = (uint64_t)lx[2] << (63 - lev);
   for (int c = 0; c < 3; ++c) {
     const int sh = (2 - c) * 21;
-    key[c] = (interleave3(z >> sh) << 2) | (interleave3(y >> sh) << 1) | interleave3(x >> sh);
+    key_[c] = (interleave3(z >> sh) << 2) | (interleave3(y >> sh) << 1) | interleave3(x >> sh);
   }
+  keyed_ = true;
 }
 
 LLoc LLoc::parent() const {
@@ -98,7 +99,7 @@ Mask27 ownership_among(const LLoc &main, const std::vector<std::pair<LLoc, LLoc>
   // Morton number (block_ownership.cpp:42-74).
   auto beats = [&](const LLoc &a, const LLoc &b) {  // a < b in ownership order
     if (a.level != b.level) return a.level < b.level;
-    return a.key < b.key;
+    return a.key() < b.key();
   };
   Mask27 m = 0;
   for (int a = -1; a <= 1; ++a)
@@ -253,6 +254,7 @@ MeshTopology::MeshTopology(const MeshSpec &spec, const std::vector<LLoc> &leaves
       for (auto &c : it->children()) leaves_.insert(c);
     }
   }
+  leafset_.insert(leaves_.begin(), leaves_.end());
   // gids: leaves in (Morton, level) order, then internal nodes (forest.cpp:27-60)
   std::vector<LLoc> lv(leaves_.begin(), leaves_.end());
   int g = 0;
@@ -334,7 +336,7 @@ void MeshTopology::neighbors_at(const LLoc &loc, int o1, int o2, int o3, Grid g,
     }
   }
   const LLoc tn = wrap(n), tl = wrap(loc);
-  if (same && leaves_.count(tn)) {
+  if (same && leafset_.count(tn)) {
     out.push_back({tn, unwrap(tn)});
   } else if (internal_.count(tn)) {
     if (fine) {
@@ -343,7 +345,7 @@ void MeshTopology::neighbors_at(const LLoc &loc, int o1, int o2, int o3, Grid g,
     } else if (internal) {
       out.push_back({tn, unwrap(tn)});
     }
-  } else if (coarse && leaves_.count(tn.parent())) {
+  } else if (coarse && leafset_.count(tn.parent())) {
     // a coarser neighbour is listed once, in the slot that points at its centre
     const LLoc np = unwrap(tn.parent());
     const auto so = loc.offsets_to(np);
@@ -361,7 +363,12 @@ std::vector<std::pair<LLoc, LLoc>> MeshTopology::neighbors_of(const LLoc &loc, G
 }
 
 Mask27 MeshTopology::ownership(const LLoc &who, Grid g, int lev) const {
-  return ownership_among(who, neighbors_of(who, g, lev));
+  auto &cache = own_cache_[{(int)g, lev}];
+  auto it = cache.find(who);
+  if (it != cache.end()) return it->second;
+  const Mask27 m = ownership_among(who, neighbors_of(who, g, lev));
+  cache.emplace(who, m);
+  return m;
 }
 
 Neighbor MeshTopology::make_neighbor(const LLoc &me, const LLoc &where, const LLoc &origin,
@@ -566,7 +573,7 @@ void MeshTopology::build_multigrid() {
     lists[b.loc.level].push_back(b.loc);
     if (b.loc.level < max_level_) lists[b.loc.level + 1].push_back(b.loc);
     LLoc p = b.loc.parent();
-    while (p.level >= mg_min_level_ && p.key == b.loc.key) {
+    while (p.level >= mg_min_level_ && p.key() == b.loc.key()) {
       lists[p.level].push_back(p);
       p = p.parent();
     }

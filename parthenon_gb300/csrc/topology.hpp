@@ -22,6 +22,7 @@
 #include <set>
 #include <string>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 namespace pgb {
@@ -29,14 +30,18 @@ namespace pgb {
 struct LLoc {
   int level = 0;
   std::array<int64_t, 3> lx{0, 0, 0};
-  std::array<uint64_t, 3> key{0, 0, 0};  // Morton words, most significant first
-  LLoc() { make_key(); }
-  LLoc(int lev, int64_t a, int64_t b, int64_t c) : level(lev), lx{a, b, c} { make_key(); }
-  void make_key();
+  LLoc() {}
+  LLoc(int lev, int64_t a, int64_t b, int64_t c) : level(lev), lx{a, b, c} {}
+  // Morton words, most significant first; computed on first use (most locations built
+  // during neighbour searches are only hashed and compared for equality)
+  const std::array<uint64_t, 3> &key() const {
+    if (!keyed_) make_key();
+    return key_;
+  }
   bool operator==(const LLoc &o) const { return level == o.level && lx == o.lx; }
   bool operator!=(const LLoc &o) const { return !(*this == o); }
   bool operator<(const LLoc &o) const {
-    if (key != o.key) return key < o.key;
+    if (key() != o.key()) return key() < o.key();
     return level < o.level;
   }
   LLoc parent() const;
@@ -45,11 +50,18 @@ struct LLoc {
   std::array<int, 3> offsets_to(const LLoc &nb) const;
   bool touches(const LLoc &in) const;
   bool touches_element(const LLoc &in, const std::array<int, 3> &te) const;
+
+ private:
+  void make_key() const;
+  mutable std::array<uint64_t, 3> key_{0, 0, 0};
+  mutable bool keyed_ = false;
 };
 
 struct LLocHash {
   size_t operator()(const LLoc &l) const {
-    return (size_t)(l.key[0] * 0x9E3779B97F4A7C15ull ^ l.key[1] ^ (uint64_t)(l.level + 64));
+    uint64_t h = (uint64_t)(l.level + 64) * 0x9E3779B97F4A7C15ull;
+    for (int d = 0; d < 3; ++d) h = (h ^ (uint64_t)l.lx[d]) * 0xBF58476D1CE4E5B9ull;
+    return (size_t)(h ^ (h >> 31));
   }
 };
 
@@ -142,7 +154,7 @@ class MeshTopology {
   const std::map<int, GridTopology> &mg_grids() const { return mg_; }
   int mg_min_level() const { return mg_min_level_; }
   int gid_of(const LLoc &l) const;
-  bool is_leaf(const LLoc &l) const { return leaves_.count(l) != 0; }
+  bool is_leaf(const LLoc &l) const { return leafset_.count(l) != 0; }
   // Leaf set after one adaptive step (Mesh::UpdateMeshBlockTree,
   // mesh-amr_loadbalance.cpp:496-629): flags per leaf in gid order, +1 refine, -1
   // derefine (a parent is derefined only when all eight children ask), 0 keep;
@@ -166,6 +178,10 @@ class MeshTopology {
   MeshSpec spec_;
   int root_level_ = 0, max_level_ = 0, mg_min_level_ = 0;
   std::set<LLoc> leaves_;
+  std::unordered_set<LLoc, LLocHash> leafset_;  // membership queries (same content)
+  // ownership of a location per (grid kind, logical level); it depends only on the
+  // tree, so each block's is computed once instead of once per neighbour
+  mutable std::map<std::pair<int, int>, std::unordered_map<LLoc, Mask27, LLocHash>> own_cache_;
   std::unordered_map<LLoc, int, LLocHash> internal_;  // value unused
   std::unordered_map<LLoc, int, LLocHash> gid_;
   GridTopology leaf_;

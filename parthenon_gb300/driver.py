@@ -97,8 +97,12 @@ class RK2Driver:
         (Mesh::Initialize -> Mesh::CommunicateBoundaries, which prolongates on
         multilevel meshes for every package, mesh.cpp:640-706) and set the first dt."""
         import torch
+        src = torch.as_tensor(host_array, dtype=torch.float64)
+        if src.is_cuda:
+            # produced on the caller's stream: order the copy after it
+            self.stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(self.stream):
-            self.base.copy_(torch.as_tensor(host_array, dtype=torch.float64), non_blocking=False)
+            self.base.copy_(src, non_blocking=False)
             self.mesh.exchange(self.base, self.cbase, prolongate=True, stream=self.stream)
             self.stage.copy_(self.base)
             nat.check(nat.lib().pgb_estimate_dt(self.mesh.handle, ctypes.byref(self.params), _ptr(self.base),

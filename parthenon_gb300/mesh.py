@@ -194,10 +194,13 @@ class Mesh:
     def transfer(self, new_mesh, field, stream=None):
         """New field on new_mesh: same-level copies, prolongated new fine blocks,
         restricted new coarse blocks (ghosts to be filled by an exchange)."""
+        import torch
         self._ensure()
         new_mesh._ensure()
         ncomp = field.shape[1]
-        out = new_mesh.new_field(ncomp)
+        # allocate (and zero) on the stream the transfer runs on
+        with torch.cuda.stream(stream if stream is not None else torch.cuda.current_stream()):
+            out = new_mesh.new_field(ncomp)
         nat.check(nat.lib().pgb_amr_transfer(self._h, new_mesh._h, _ptr(field), _ptr(out), ncomp, _stream(stream)),
                   "pgb_amr_transfer")
         return out

@@ -126,6 +126,34 @@ def burgers_amr_state(mesh, nscalars=2, nmodes=16, kmax=6, seed=5):
     return out
 
 
+def burgers_amr_state_device(mesh, nscalars=2, nmodes=16, kmax=6, seed=5):
+    """burgers_amr_state evaluated on the GPU (torch tensor in the field layout), for
+    meshes of tens of thousands of blocks where the host evaluation would dominate."""
+    import torch
+    _, geom = mesh.block_info()
+    geom = torch.as_tensor(geom, dtype=torch.float64, device="cuda")
+    g = mesh.nghost
+    n = mesh.block_nx
+    ncomp = 3 + nscalars
+    out = torch.zeros((mesh.nblocks, ncomp) + tuple(mesh.N[::-1]), dtype=torch.float64, device="cuda")
+    c = [geom[:, d:d + 1] + (torch.arange(n[d], dtype=torch.float64, device="cuda")[None, :] + 0.5) *
+         geom[:, 3 + d:4 + d] for d in range(3)]
+    x = c[0][:, None, None, :]
+    y = c[1][:, None, :, None]
+    z = c[2][:, :, None, None]
+    two_pi = 2.0 * np.pi
+    for comp, (k, a, phi) in enumerate(sinusoid_modes(nmodes, kmax, seed)):
+        acc = torch.zeros((mesh.nblocks, n[2], n[1], n[0]), dtype=torch.float64, device="cuda")
+        for m in range(nmodes):
+            arg = two_pi * (float(k[m, 2]) * z + float(k[m, 1]) * y + float(k[m, 0]) * x) + float(phi[m])
+            acc += float(a[m]) * torch.sin(arg)
+        out[:, comp, g:g + n[2], g:g + n[1], g:g + n[0]] = acc
+    for s in range(nscalars):
+        out[:, 3 + s, g:g + n[2], g:g + n[1], g:g + n[0]] = 1.0 + 0.5 * (
+            torch.sin(two_pi * (s + 1) * x) * torch.sin(two_pi * y) * torch.sin(two_pi * z))
+    return out
+
+
 def poisson_rhs(n, ngauss=32, sigma=0.03, seed=4):
     """Sum of `ngauss` Gaussians (width sigma, centres U[0,1]^3, amplitudes N(0,1), seeded)
     with periodic-image distances on the unit cube, minus its mean; array (n, n, n),
