@@ -137,6 +137,14 @@ HLL_SCALAR_OPS = 10
 DIVUPD_OPS = 12    # per component: 3 face differences, sum, /V, average, update
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per 32^3 block with 11
+# components, from one ncu capture of the same kernels on the 128^3 mesh (64 blocks):
+# the three directional launches of one stage (414.1 + 664.3 + 670.4 MB) and one direct
+# exchange launch (319.6 MB). Traffic grows in proportion to the blocks processed.
+STAGE_DRAM_BYTES_PER_BLOCK = (414.1e6 + 664.3e6 + 670.4e6) / 64
+EXCHANGE_DRAM_BYTES_PER_BLOCK = 319.6e6 / 64
+
+
 def burgers_ops_per_cell_stage(n, nc):
     recon = 3 * nc * WENO5Z_OPS * (n + 2) / n
     faces = 3 * (n + 1) / n * (HLL_VEL_OPS + (nc - 3) * HLL_SCALAR_OPS)
@@ -244,12 +252,14 @@ def run_ours(args, ws, rank):
                    "parallelism": "replicas" if ws > 1 else "single-gpu"},
         "roofline": {"kernel": "burgers_stage (3 directional march launches)", "bound": "fp64",
                      "achieved": stage_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": stage_tflops / fp64_peak, "traffic": None,
+                     "frac": stage_tflops / fp64_peak, "traffic": STAGE_DRAM_BYTES_PER_BLOCK * mesh.nblocks,
+                     "traffic_unit": "bytes per stage (ncu, scaled by blocks)",
                      "peak_source": "cuBLAS DGEMM measured in this run",
                      "ops_per_cell_stage": ops_cell, "stage_ms": stage_ms},
         "exchange_roofline": {"kernel": "ghost exchange (direct copy)", "bound": "hbm", "achieved": xchg_gbs,
                               "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": xchg_gbs / peaks["hbm_gbs"],
-                              "traffic": None, "bytes_per_launch": xchg_bytes, "ms": xchg_ms,
+                              "traffic": EXCHANGE_DRAM_BYTES_PER_BLOCK * mesh.nblocks,
+                              "bytes_per_launch": xchg_bytes, "ms": xchg_ms,
                               "peak_source": peak_src},
         "ghost_exchange_gbs": xchg_gbs,
         "e2e": e2e,
@@ -261,7 +271,7 @@ def run_ours(args, ws, rank):
         out["cpu_baseline"] = cpu_baseline(steps=1)
     del drv, state, host_in, host_out
     if args.amr_cycles > 0:
-        out["amr"] = amr_bench(torch, args.amr_cycles, with_cpu=(rank == 0 and ws == 1))
+        out["amr"] = amr_bench(torch, args.amr_cycles, with_cpu=(rank == 0 and ws == 1), root=args.amr_root)
     return out
 
 
@@ -312,7 +322,7 @@ def _amr_driver(pg, root):
                         numlevel=AMR_NUMLEVEL, derefine_count=10, check_interval=AMR_CHECK)
 
 
-def amr_bench(torch, cycles, with_cpu):
+def amr_bench(torch, cycles, with_cpu, root=AMR_ROOT):
     """Adaptive Burgers: 128^3 root in 16^3 blocks, 3 levels, refine above 0.5 and
     derefine below 0.05 of the mesh-wide max |grad u| (checked every 5 cycles, 10
     consecutive derefine tags needed), 16 random-phase sinusoids with wavenumbers 1-6,
@@ -321,7 +331,7 @@ def amr_bench(torch, cycles, with_cpu):
     region; the initial refinement (problem generation repeated on each new mesh) is
     timed separately."""
     import parthenon_gb300 as pg
-    drv = _amr_driver(pg, AMR_ROOT)
+    drv = _amr_driver(pg, root)
     adapt_s = []
     inner = drv.adapt
 
@@ -361,7 +371,7 @@ def amr_bench(torch, cycles, with_cpu):
         "check_seconds": float(sum(t for t, _ in adapt_s)),
         "remesh_seconds_max": float(max([t for t, c in adapt_s if c], default=0.0)),
         "peak_mem_gb": torch.cuda.max_memory_allocated() / 1e9,
-        "config": {"workload": "burgers3d-amr-128^3root-16^3blocks-3levels-ng4-5vars-fp64",
+        "config": {"workload": "burgers3d-amr-%d^3root-16^3blocks-3levels-ng4-5vars-fp64" % root,
                    "criterion": "|grad u| relative: refine > 0.5 max, derefine < 0.05 max (10 tags)",
                    "check_interval": AMR_CHECK, "initial": "16 sinusoids, k in 1..6, seed 5; 2 scalars"},
     }
@@ -454,12 +464,19 @@ def main():
                     help="skip the per-kernel timing, end-to-end and CPU-baseline legs (profiling runs)")
     ap.add_argument("--amr-cycles", type=int, default=100,
                     help="cycles of the adaptive Burgers leg (0 skips it)")
+    ap.add_argument("--amr-root", type=int, default=AMR_ROOT, help="root cells per direction of the adaptive leg")
+    ap.add_argument("--amr-only", action="store_true",
+                    help="run only the adaptive leg (profiling runs), no CPU baseline")
     args = ap.parse_args()
     ws, rank = _dist()
     if ws > 1:
         import torch
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
-    if args.impl == "reference":
+    if args.amr_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        out = {"amr": amr_bench(torch, args.amr_cycles, with_cpu=False, root=args.amr_root)}
+    elif args.impl == "reference":
         out = run_reference(args, ws, rank)
     else:
         out = run_ours(args, ws, rank)

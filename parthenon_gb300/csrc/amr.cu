@@ -102,14 +102,13 @@ __global__ void __launch_bounds__(256) k_transfer(const DevRemap *__restrict__ m
     // ProlongateSharedMinMod (pr_ops.hpp:166-285) of the parent's cells, child coords
     const double *par = oldu + ((int64_t)r.src[0] * ncomp + v) * cs;
     const DevBlockGeom g = ngeom[b];
-    for (int64_t e = threadIdx.x; e < cs; e += blockDim.x) {
-      const int f[3] = {(int)(e % N0), (int)((e / N0) % N1), (int)(e / N01)};
-      int c[3], o[3];
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        c[q] = ((f[q] - ng) >> 1) + ng;
-        o[q] = (f[q] - ng) & 1;
-      }
+    // one thread per coarse cell of [ng - ng/2, ng + n/2 - 1 + ng/2]^3 (ng even), which
+    // writes its 2x2x2 fine cells: together they cover the child's whole array
+    const int clo = ng - ng / 2;
+    const int nc0 = d.nx[0] / 2 + ng, nc1 = d.nx[1] / 2 + ng, nc2 = d.nx[2] / 2 + ng;
+    const int64_t ncc = (int64_t)nc0 * nc1 * nc2;
+    for (int64_t e = threadIdx.x; e < ncc; e += blockDim.x) {
+      const int c[3] = {clo + (int)(e % nc0), clo + (int)((e / nc0) % nc1), clo + (int)(e / ((int64_t)nc0 * nc1))};
       auto P = [&](int ck, int cj, int ci) {
         return par[(int64_t)(ck + r.oct[2]) * N01 + (int64_t)(cj + r.oct[1]) * N0 + (ci + r.oct[0])];
       };
@@ -134,19 +133,16 @@ __global__ void __launch_bounds__(256) k_transfer(const DevRemap *__restrict__ m
       const double m0 = __dmul_rn(gm[0], dfm[0]), p0 = __dmul_rn(gp[0], dfp[0]);
       const double m1 = __dmul_rn(gm[1], dfm[1]), p1 = __dmul_rn(gp[1], dfp[1]);
       const double m2 = __dmul_rn(gm[2], dfm[2]), p2 = __dmul_rn(gp[2], dfp[2]);
-      double val;
-      const int sel = o[0] + 2 * o[1] + 4 * o[2];
-      switch (sel) {
-        case 0: val = __dsub_rn(fc, __dadd_rn(__dadd_rn(m0, m1), m2)); break;
-        case 1: val = __dadd_rn(fc, __dsub_rn(__dsub_rn(p0, m1), m2)); break;
-        case 2: val = __dsub_rn(fc, __dadd_rn(__dsub_rn(m0, p1), m2)); break;
-        case 3: val = __dadd_rn(fc, __dsub_rn(__dadd_rn(p0, p1), m2)); break;
-        case 4: val = __dsub_rn(fc, __dsub_rn(__dadd_rn(m0, m1), p2)); break;
-        case 5: val = __dadd_rn(fc, __dadd_rn(__dsub_rn(p0, m1), p2)); break;
-        case 6: val = __dsub_rn(fc, __dsub_rn(__dsub_rn(m0, p1), p2)); break;
-        default: val = __dadd_rn(fc, __dadd_rn(__dadd_rn(p0, p1), p2)); break;
-      }
-      dst[e] = val;
+      const int64_t f = (int64_t)((c[2] - ng) * 2 + ng) * N01 + (int64_t)((c[1] - ng) * 2 + ng) * N0 +
+                        ((c[0] - ng) * 2 + ng);
+      dst[f] = __dsub_rn(fc, __dadd_rn(__dadd_rn(m0, m1), m2));
+      dst[f + 1] = __dadd_rn(fc, __dsub_rn(__dsub_rn(p0, m1), m2));
+      dst[f + N0] = __dsub_rn(fc, __dadd_rn(__dsub_rn(m0, p1), m2));
+      dst[f + N0 + 1] = __dadd_rn(fc, __dsub_rn(__dadd_rn(p0, p1), m2));
+      dst[f + N01] = __dsub_rn(fc, __dsub_rn(__dadd_rn(m0, m1), p2));
+      dst[f + N01 + 1] = __dadd_rn(fc, __dadd_rn(__dsub_rn(p0, m1), p2));
+      dst[f + N01 + N0] = __dsub_rn(fc, __dsub_rn(__dsub_rn(m0, p1), p2));
+      dst[f + N01 + N0 + 1] = __dadd_rn(fc, __dadd_rn(__dadd_rn(p0, p1), p2));
     }
     return;
   }

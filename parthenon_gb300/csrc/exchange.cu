@@ -254,7 +254,7 @@ __device__ __forceinline__ double *arr(double *fine, double *coarse, int c) { re
 // Per thread the row base addresses are formed once per row; rows whose two ends are
 // 16-byte aligned on both sides (every same-level face and edge of an even-sized block)
 // move as double2, the rest element by element.
-__global__ void __launch_bounds__(128) k_copy(const DevPair *__restrict__ pairs,
+__global__ void __launch_bounds__(128, 8) k_copy(const DevPair *__restrict__ pairs,
                                               const DevWork *__restrict__ work, Dims d, int ncomp,
                                               double *__restrict__ fine, double *__restrict__ coarse) {
   const DevWork w = work[blockIdx.x];
@@ -277,19 +277,52 @@ __global__ void __launch_bounds__(128) k_copy(const DevPair *__restrict__ pairs,
   const int nel = vec ? ni / 2 : ni;  // elements (or pairs) per row
   const int lpr = nel <= 1 ? 1 : nel <= 2 ? 2 : nel <= 4 ? 4 : nel <= 8 ? 8 : nel <= 16 ? 16 : 32;
   const int sub = threadIdx.x / lpr, li = threadIdx.x - sub * lpr, stepr = blockDim.x / lpr;
-  for (int r = w.row0 + sub; r < w.row0 + w.nrows; r += stepr) {
-    const int k = r / nj, j = r - k * nj;
-    const double *s = src + k * sk + j * sN0;
-    double *t = dst + k * dk + j * dN0;
-    if (vec) {
-      const double2 *s2 = reinterpret_cast<const double2 *>(s);
-      double2 *t2 = reinterpret_cast<double2 *>(t);
-      for (int i = li; i < nel; i += lpr) t2[i] = __ldg(s2 + i);
-    } else if (p.full_mask) {
-      for (int i = li; i < nel; i += lpr) t[i] = __ldg(s + i);
-    } else {
+  const int end = w.row0 + w.nrows;
+  if (!p.full_mask) {
+    for (int r = w.row0 + sub; r < end; r += stepr) {
+      const int k = r / nj, j = r - k * nj;
+      const double *s = src + k * sk + j * sN0;
+      double *t = dst + k * dk + j * dN0;
       for (int i = li; i < nel; i += lpr)
         if (mask_active(p.mask, p.dst, p.dst.lo[2] + k, p.dst.lo[1] + j, p.dst.lo[0] + i)) t[i] = __ldg(s + i);
+    }
+    return;
+  }
+  // U rows per trip, all loads issued before the stores: enough bytes in flight per
+  // thread to keep HBM busy when rows are short (x faces are 32-byte rows)
+  constexpr int U = 4;
+  for (int rb = w.row0 + sub; rb < end; rb += U * stepr) {
+    int so[U], to[U];  // offsets within one component array (< 2^31 elements)
+    bool ok[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int r = rb + u * stepr;
+      ok[u] = r < end;
+      const int rr = ok[u] ? r : rb;
+      const int k = rr / nj, j = rr - k * nj;
+      so[u] = k * sk + j * sN0;
+      to[u] = k * dk + j * dN0;
+    }
+    if (vec) {
+      for (int i = li; i < nel; i += lpr) {
+        double2 x[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (ok[u]) x[u] = __ldg(reinterpret_cast<const double2 *>(src + so[u]) + i);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (ok[u]) reinterpret_cast<double2 *>(dst + to[u])[i] = x[u];
+      }
+    } else {
+      for (int i = li; i < nel; i += lpr) {
+        double x[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (ok[u]) x[u] = __ldg(src + so[u] + i);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (ok[u]) dst[to[u] + i] = x[u];
+      }
     }
   }
 }
