@@ -132,7 +132,7 @@ int pgb_pack_buffers(pgb_mesh *mesh, const double *data, const double *coarse, i
 int pgb_flux_correct(pgb_mesh *mesh, double *flux, int32_t ncomp, void *stream);
 
 /* One RK stage: fluxes from u_in, flux divergence, u_out = (w_in u_in + w_base u_base)
- * + beta * dt * dudt on the interior. dt is a device scalar. Uniform meshes use the
+ * + beta * dt * dudt on the interior. dt is a device scalar (dt[0]). Uniform meshes use the
  * fused path (dudt is scratch of the field's size); multilevel meshes store fluxes in
  * `flux` (3x the field's size), correct them at fine/coarse faces and then update.
  * Replaces CalculateFluxes (benchmarks/burgers/burgers_package.cpp:202-404,
@@ -143,18 +143,23 @@ int pgb_stage(pgb_mesh *mesh, const pgb_stage_params *p, const double *u_in, con
               double *dudt, double *flux, const double *dt, double w_in, double w_base, double beta, int32_t ncomp,
               void *stream);
 
-/* dt <- SetGlobalTimeStep(cfl * EstimateTimestep(u)) on the device. first = 0: regular
- * step (growth limited to 2x); 1: the initial step; 2: an extra vote without growth,
- * dt <- min(dt, cfl * estimate), used after a remesh so that new blocks vote too.
- * Replaces EstimateTimestep (src/interface/update.hpp:268-278) and
- * EvolutionDriver::SetGlobalTimeStep (src/driver/driver.cpp:210-232). */
+/* dt <- SetGlobalTimeStep(cfl * EstimateTimestep(u)) on the device. dt points to three
+ * device doubles: dt[0] the current step (what the stage kernels read), dt[1] the step
+ * the last update started from, dt[2] the simulation time. first = 0: regular update
+ * after a cycle taken with dt[0] (dt[2] += dt[0]; growth limited to 2x); 1: the initial
+ * step; 2: repeat the last update with votes from u (after a remesh, where every block
+ * of the new list votes again).
+ * Replaces EstimateTimestep (src/interface/update.hpp:268-278),
+ * EvolutionDriver::SetGlobalTimeStep (src/driver/driver.cpp:210-232) and
+ * InitializeBlockTimeSteps after a remesh (driver.cpp:129-131,194-204). */
 int pgb_estimate_dt(pgb_mesh *mesh, const pgb_stage_params *p, const double *u, int32_t ncomp, double *dt,
                     int32_t first, void *stream);
 
 /* ncycles RK2 cycles (two stages with a ghost exchange after each, then the dt update)
  * on device arrays. base/stage: fields; dudt: scratch of the field's size; flux:
  * 3x field size (multilevel only, else may be NULL); coarse_*: coarse buffers
- * (multilevel only). use_graph != 0 captures one cycle in a CUDA graph and replays it.
+ * (multilevel only); dt: three device doubles as for pgb_estimate_dt. use_graph != 0
+ * captures one cycle in a CUDA graph and replays it.
  * Replaces MultiStageDriverGeneric::Step (src/driver/multistage.hpp:39-53) with the
  * advection/Burgers task collections (example/advection/advection_driver.cpp:56-164,
  * benchmarks/burgers/burgers_driver.cpp:53-148). */
@@ -199,6 +204,17 @@ int pgb_gmg_vcycles(pgb_gmg *gmg, double *u, const double *rhs, int32_t ncycles,
  * level). Replaces MGSolver::AddTasks (mg_solver.hpp:119-161). */
 int pgb_gmg_solve(pgb_gmg *gmg, double *u, const double *rhs, int32_t mixed, double rtol, int32_t max_cycles,
                   int32_t *cycles_out, double *relres_out, void *stream);
+
+/* ---- history reductions ----------------------------------------------------------- */
+
+/* out[r] (host) = sum over blocks, components and interior cells whose centre lies in
+ * box r (inclusive bounds) of u * u * vol / (mesh_volume + 1e-20); regions holds
+ * nregions (1..8) boxes as x1min, x1max, x2min, x2max, x3min, x3max. Deterministic
+ * (fixed reduction order); synchronises the stream. Replaces MassHistory
+ * (benchmarks/burgers/burgers_package.cpp:406-439) as registered per octant (:106-135)
+ * for the history output (src/outputs/history.cpp:40-210). */
+int pgb_history_mass(pgb_mesh *mesh, const double *u, int32_t ncomp, const double *regions, int32_t nregions,
+                     double mesh_volume, double *out, void *stream);
 
 /* ---- adaptive refinement ------------------------------------------------------- */
 

@@ -804,6 +804,7 @@ struct Sim {
   Field base, stage, dudt;
   FluxField flux;
   double dt = std::numeric_limits<double>::max();
+  double dt_prev = std::numeric_limits<double>::max();  // dt before the last SetGlobalTimeStep
   double time = 0.0;
   int ncycle = 0;
   int64_t zone_cycles = 0;
@@ -817,6 +818,7 @@ inline double estimate_dt(Sim &s, Field &U) {
 
 // driver.cpp:210-232 (dt_force/dt_init/dt_user/floor/ceil at their defaults)
 inline void set_global_dt(Sim &s, double new_dt) {
+  s.dt_prev = s.dt;
   if (s.dt < 0.1 * std::numeric_limits<double>::max()) s.dt *= 2.0;
   s.dt = std::min(s.dt, new_dt);
   s.dt = std::max(std::numeric_limits<double>::min(), std::min(s.dt, std::numeric_limits<double>::max()));
@@ -995,6 +997,41 @@ int orc_run(void *h, int ncycles, int nthreads, double *dts) {
 }
 
 double orc_dt(void *h) { return ((Sim *)h)->dt; }
+double orc_time(void *h) { return ((Sim *)h)->time; }
+int orc_ncycle(void *h) { return ((Sim *)h)->ncycle; }
+
+// MassHistory (burgers_package.cpp:406-439) for `nreg` boxes (x1min, x1max, x2min,
+// x2max, x3min, x3max each) over all components of the base field. The sum is
+// compensated (Neumaier), so it is the accurate value against which any summation
+// order can be checked.
+void orc_history_mass(void *h, const double *boxes, int nreg, double mesh_volume, double *out) {
+  Sim *s = (Sim *)h;
+  Field &U = s->base;
+  const int ng = s->mesh->p.ng;
+  const double den = mesh_volume + 1e-20;
+  for (int r = 0; r < nreg; ++r) {
+    double sum = 0.0, comp = 0.0;
+    const double *bx = boxes + 6 * r;
+    for (size_t b = 0; b < s->mesh->blocks.size(); ++b) {
+      const Coords &c = s->mesh->blocks[b].coords;
+      const double w = c.vol / den;
+      for (int v = 0; v < U.ncomp; ++v)
+        for (int k = ng; k < U.N[2] - ng; ++k)
+          for (int j = ng; j < U.N[1] - ng; ++j)
+            for (int i = ng; i < U.N[0] - ng; ++i) {
+              const double x1 = c.xc(0, i), x2 = c.xc(1, j), x3 = c.xc(2, k);
+              const double mask = (bx[0] <= x1) && (x1 <= bx[1]) && (bx[2] <= x2) && (x2 <= bx[3]) &&
+                                  (bx[4] <= x3) && (x3 <= bx[5]);
+              const double q = U.at((int)b, v, k, j, i);
+              const double term = mask * q * q * w;
+              const double t = sum + term;
+              comp += std::fabs(sum) >= std::fabs(term) ? (sum - t) + term : (term - t) + sum;
+              sum = t;
+            }
+    }
+    out[r] = sum + comp;
+  }
+}
 
 // Pack every boundary of the base field into `out` in record order (the reference
 // buffer layout: per boundary, components outermost, then k, j, i of the send box).
@@ -1020,11 +1057,13 @@ void orc_block_criterion(void *h, int comp, int method, double *out) {
                            : gradient_max(s->base, s->mesh->blocks[b].coords, b, comp);
 }
 
-// After a remesh every block of the new mesh votes on the current dt (no growth):
-// dt = min(dt, cfl * estimate over the new blocks).
-double orc_limit_dt(void *h) {
+// After a remesh (driver.cpp:129-131): InitializeBlockTimeSteps gives every block of
+// the new list the estimate of the current state, replacing the votes of the last
+// stage, and SetGlobalTimeStep then runs from the previous step again.
+double orc_remesh_dt(void *h) {
   Sim *s = (Sim *)h;
-  s->dt = std::min(s->dt, estimate_dt(*s, s->base));
+  s->dt = s->dt_prev;
+  set_global_dt(*s, estimate_dt(*s, s->base));
   return s->dt;
 }
 

@@ -135,15 +135,23 @@ class AMRDriver:
                                                 self.rk.ncomp, _ptr(self.dt), 1, _stream(self.stream)),
                       "pgb_estimate_dt")
 
-    def run(self, ncycles, graph=True):
-        """ncycles RK2 cycles with a refinement check after every check_interval-th."""
+    def run(self, ncycles, graph=True, history=None):
+        """ncycles RK2 cycles with a refinement check after every check_interval-th.
+        history: written at cycle 0 and checked after each cycle's remesh and dt update
+        (the order of EvolutionDriver::Execute, driver.cpp:109-144)."""
         done = 0
         nx = self.mesh.block_nx
+        if history is not None and self.ncycle == 0:
+            history.maybe_write(self.mesh, self.base, self.dt, 0, self.stream)
         while done < ncycles:
             k = min(ncycles - done, self.check_interval - self.ncycle % self.check_interval)
+            if history is not None:
+                k = 1
             self.rk.run(k, graph=graph)
             self.zone_cycles += k * self.mesh.nblocks * nx[0] * nx[1] * nx[2]
             self.ncycle += k
             done += k
             if self.ncycle % self.check_interval == 0:
                 self.adapt()
+            if history is not None:
+                history.maybe_write(self.mesh, self.base, self.dt, self.ncycle, self.stream)

@@ -370,7 +370,8 @@ int pgb_run_host(pgb_mesh *m, const pgb_stage_params *p, const double *host_in, 
   };
   if ((rc = guard(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream"))) return rc;
   if ((rc = guard(cudaMalloc(&base, n * 8), "malloc")) || (rc = guard(cudaMalloc(&stage, n * 8), "malloc")) ||
-      (rc = guard(cudaMalloc(&dt, 8), "malloc")))
+      (rc = guard(cudaMalloc(&dt, 3 * sizeof(double)), "malloc")) ||
+      (rc = guard(cudaMemsetAsync(dt, 0, 3 * sizeof(double), s), "memset")))
     return rc;
   if (ml) {
     if ((rc = guard(cudaMalloc(&flux, 3 * n * 8), "malloc")) || (rc = guard(cudaMalloc(&cb, nc * 8), "malloc")) ||
@@ -381,8 +382,8 @@ int pgb_run_host(pgb_mesh *m, const pgb_stage_params *p, const double *host_in, 
   }
   if ((rc = guard(cudaMemcpyAsync(base, host_in, n * 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
   if ((rc = guard(cudaMemcpyAsync(stage, base, n * 8, cudaMemcpyDeviceToDevice, s), "d2d"))) return rc;
-  const int xflags = p->physics == 1 ? 0 : PGB_EXCHANGE_PROLONGATE;
-  if ((rc = exchange_leaf(m, base, cb, ncomp, xflags, nullptr, s))) {
+  // initial fill: Mesh::CommunicateBoundaries prolongates for every package
+  if ((rc = exchange_leaf(m, base, cb, ncomp, PGB_EXCHANGE_PROLONGATE, nullptr, s))) {
     cleanup();
     return rc;
   }

@@ -69,16 +69,26 @@ __global__ void k_advection_min(const DevBlockGeom *__restrict__ geom, int nbloc
 }
 
 // driver.cpp:210-232 with the default dt controls; resets the accumulator.
-// first: 0 regular step (growth limited to 2x), 1 first step, 2 extra vote on the
-// current dt without growth (after a remesh).
+// dt[0] is the current step, dt[1] the step the last update started from, dt[2] the
+// simulation time. first: 0 regular step after a cycle taken with dt[0] (time advances
+// by it, driver.cpp:123; growth limited to 2x), 1 first step, 2 repeat the last update
+// with new votes (after a remesh, EvolutionDriver::InitializeBlockTimeSteps replaces
+// every block's vote before SetGlobalTimeStep, driver.cpp:129-131,194-204).
 __global__ void k_set_dt(double *dt, unsigned long long *minbits, double cfl, int first) {
   const double mn = __longlong_as_double((long long)*minbits);
   const double newdt = __dmul_rn(cfl, mn);
-  double t = first == 1 ? DBL_MAX : *dt;
-  if (first != 2 && t < 0.1 * DBL_MAX) t = __dmul_rn(t, 2.0);
+  double t;
+  if (first == 2) {
+    t = dt[1];
+  } else {
+    t = first == 1 ? DBL_MAX : dt[0];
+    if (first == 0) dt[2] = __dadd_rn(dt[2], dt[0]);
+    dt[1] = t;
+  }
+  if (t < 0.1 * DBL_MAX) t = __dmul_rn(t, 2.0);
   t = fmin(t, newdt);
   t = fmax(DBL_MIN, fmin(t, DBL_MAX));
-  *dt = t;
+  dt[0] = t;
   *minbits = (unsigned long long)__double_as_longlong(DBL_MAX);
 }
 

@@ -50,7 +50,8 @@ class RK2Driver:
         self.stream = stream if stream is not None else torch.cuda.Stream()
         self._allocate(mesh)
         with torch.cuda.stream(self.stream):
-            self.dt = torch.zeros(1, dtype=torch.float64, device="cuda")
+            # [current step, step the last update started from, simulation time]
+            self.dt = torch.zeros(3, dtype=torch.float64, device="cuda")
         self.ncycle = 0
 
     def _allocate(self, mesh, base=None):
@@ -75,8 +76,10 @@ class RK2Driver:
         """Continue on a new mesh (after a remesh) with `base` already on it: fresh
         scratch and coarse buffers, ghosts filled with prolongation (the post-remesh
         CommunicateBoundaries of RedistributeAndRefineMeshBlocks), then every block of
-        the new mesh votes on the current dt. The cycle graph is captured again on the
-        next run because the new mesh handle has an empty graph cache."""
+        the new mesh votes again and the last dt update is repeated with those votes
+        (InitializeBlockTimeSteps + SetGlobalTimeStep, driver.cpp:129-131). The cycle
+        graph is captured again on the next run because the new mesh handle has an
+        empty graph cache."""
         import torch
         self._allocate(mesh, base)
         with torch.cuda.stream(self.stream):
@@ -103,6 +106,7 @@ class RK2Driver:
             self.stream.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(self.stream):
             self.base.copy_(src, non_blocking=False)
+            self.dt.zero_()
             self.mesh.exchange(self.base, self.cbase, prolongate=True, stream=self.stream)
             self.stage.copy_(self.base)
             nat.check(nat.lib().pgb_estimate_dt(self.mesh.handle, ctypes.byref(self.params), _ptr(self.base),
@@ -110,7 +114,20 @@ class RK2Driver:
                       "pgb_estimate_dt")
         self.ncycle = 0
 
-    def run(self, ncycles, graph=True):
+    def run(self, ncycles, graph=True, history=None):
+        """ncycles RK2 cycles. history (e.g. history.BurgersHistory): checked at cycle 0
+        and after every cycle, as Outputs::MakeOutputs is in the driver loop; cycles then
+        run one launch sequence at a time because the check reads the time."""
+        if history is None:
+            self._cycles(ncycles, graph)
+            return
+        if self.ncycle == 0:
+            history.maybe_write(self.mesh, self.base, self.dt, 0, self.stream)
+        for _ in range(ncycles):
+            self._cycles(1, graph)
+            history.maybe_write(self.mesh, self.base, self.dt, self.ncycle, self.stream)
+
+    def _cycles(self, ncycles, graph):
         nat.check(nat.lib().pgb_rk2_cycles(self.mesh.handle, ctypes.byref(self.params), _ptr(self.base),
                                            _ptr(self.stage), _ptr(self.dudt), _ptr(self.flux), _ptr(self.cbase),
                                            _ptr(self.cstage), self.ncomp, _ptr(self.dt), int(ncycles),

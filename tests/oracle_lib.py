@@ -72,8 +72,14 @@ def lib():
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.orc_remesh.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L.orc_remesh.restype = ctypes.c_int
-        L.orc_limit_dt.argtypes = [ctypes.c_void_p]
-        L.orc_limit_dt.restype = ctypes.c_double
+        L.orc_remesh_dt.argtypes = [ctypes.c_void_p]
+        L.orc_remesh_dt.restype = ctypes.c_double
+        L.orc_time.argtypes = [ctypes.c_void_p]
+        L.orc_time.restype = ctypes.c_double
+        L.orc_ncycle.argtypes = [ctypes.c_void_p]
+        L.orc_ncycle.restype = ctypes.c_int
+        L.orc_history_mass.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -187,8 +193,21 @@ class OracleSim:
         self.nblocks = lib().orc_nblocks(self.h)
         return rc == 1
 
-    def limit_dt(self):
-        return lib().orc_limit_dt(self.h)
+    def time(self):
+        return lib().orc_time(self.h)
+
+    def ncycle(self):
+        return lib().orc_ncycle(self.h)
+
+    def history_mass(self, regions, mesh_volume):
+        r = np.ascontiguousarray(regions, np.float64).reshape(-1, 6)
+        out = np.zeros(r.shape[0], np.float64)
+        lib().orc_history_mass(self.h, _ptr(r), int(r.shape[0]), float(mesh_volume), _ptr(out))
+        return out
+
+    def remesh_dt(self):
+        """Every block of the new mesh votes again; SetGlobalTimeStep from the previous step."""
+        return lib().orc_remesh_dt(self.h)
 
 
 def ownership(main, locs):

@@ -131,7 +131,7 @@ class _OracleAMR:
         self.history.append((vals.copy(), flags.copy()))
         if self.o.remesh(flags):
             self.o.exchange(True, 0)
-            self.o.limit_dt()
+            self.o.remesh_dt()
             return True
         return False
 
