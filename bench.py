@@ -306,6 +306,22 @@ def gmg_bench(torch):
     b = sols[True] - sols[True].mean()
     res["mixed_vs_fp64_rel_err"] = float((a - b).abs().max() / a.abs().max())
     res["time_ratio_mixed_over_fp64"] = res["mixed"]["seconds"] / res["fp64"]["seconds"]
+    # BiCGSTAB with one V-cycle as preconditioner (bicgstab_solver.hpp), same tolerance
+    for prec in ("fp64", "fp32"):
+        best = None
+        for rep in range(3):
+            u = torch.zeros((GMG_N,) * 3, dtype=torch.float64, device="cuda")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            it, rms = g.bicgstab(u, rhs, precondition=prec, rtol=1e-10, relative=True, max_iters=400, stream=s)
+            s.synchronize()
+            dt = time.perf_counter() - t0
+            if rep > 0 and (best is None or dt < best[0]):
+                best = (dt, it, rms)
+        x = u.cpu().double()
+        x = x - x.mean()
+        res["bicgstab_mg_" + prec] = {"seconds": best[0], "iterations": best[1], "rms_residual": best[2],
+                                      "vs_fp64_vcycle_rel_err": float((x - a).abs().max() / a.abs().max())}
     res["config"] = {"n": GMG_N, "levels": GMG_COARSEN + 1, "smoother": "weighted Jacobi 2/3, 2+2",
                      "coarse": "+16 smoother passes, FP64", "rhs": "32 Gaussians sigma 0.03 seed 4, mean removed"}
     return res

@@ -204,6 +204,15 @@ int pgb_gmg_vcycles(pgb_gmg *gmg, double *u, const double *rhs, int32_t ncycles,
  * level). Replaces MGSolver::AddTasks (mg_solver.hpp:119-161). */
 int pgb_gmg_solve(pgb_gmg *gmg, double *u, const double *rhs, int32_t mixed, double rtol, int32_t max_cycles,
                   int32_t *cycles_out, double *relres_out, void *stream);
+/* Right-preconditioned BiCGSTAB for A u = rhs from u = 0 (the result is written to u):
+ * precondition 0: none; 1: one FP64 V-cycle from zero per application; 2: one FP32
+ * V-cycle (FP64 coarsest level). Stops when sqrt((r,r)/N) < rtol (relative = 0) or
+ * < rtol * sqrt((rhs,rhs)/N) (relative = 1), or after max_iters. One iteration is one
+ * CUDA-graph launch (stream must not be the legacy default stream); the host reads one
+ * double per iteration. Replaces BiCGSTABSolver::AddTasks
+ * (src/solvers/bicgstab_solver.hpp:116-315) with MGSolver as its preconditioner. */
+int pgb_gmg_bicgstab(pgb_gmg *gmg, double *u, const double *rhs, int32_t precondition, double rtol,
+                     int32_t relative, int32_t max_iters, int32_t *iters_out, double *rms_out, void *stream);
 
 /* ---- history reductions ----------------------------------------------------------- */
 

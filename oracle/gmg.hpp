@@ -22,6 +22,7 @@
 // z array), which is what every interior face of the reference computes.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -216,6 +217,73 @@ struct Gmg {
       if (l > 0)
         for (int64_t q = 0; q < g.size(); ++q) g.res[q] = 1.0 * g.u[q] + -1.0 * g.u0[q];
     }
+  }
+
+  // u <- M b: one V-cycle from u = 0 with right-hand side b on the finest level
+  // (MGSolver::AddLinearOperatorTasks, mg_solver.hpp:163-186, as BiCGSTAB uses it)
+  void precondition(const std::vector<double> &b, std::vector<double> &out) {
+    GmgLevel &g = lv[0];
+    g.rhs = b;
+    std::fill(g.u.begin(), g.u.end(), 0.0);
+    vcycle();
+    out = g.u;
+  }
+
+  static double dot(const std::vector<double> &a, const std::vector<double> &b) {
+    double s = 0.0, c = 0.0;  // compensated: the accurate value
+    for (size_t q = 0; q < a.size(); ++q) {
+      const double term = a[q] * b[q], t = s + term;
+      c += std::fabs(s) >= std::fabs(term) ? (s - t) + term : (term - t) + s;
+      s = t;
+    }
+    return s + c;
+  }
+
+  // Right-preconditioned BiCGSTAB (bicgstab_solver.hpp:116-315): x0 = 0, r = p =
+  // rhat0 = rhs; stops when sqrt((r,r)/N) < tol, tol = rtol * sqrt((rhs,rhs)/N) if
+  // relative. Returns the iterations run; x holds the solution.
+  int bicgstab(const std::vector<double> &rhs, std::vector<double> &x, bool precondition_on, double rtol,
+               bool relative, int max_iters, double &rms_out) {
+    GmgLevel &g = lv[0];
+    const size_t n = rhs.size();
+    const double N = (double)n;
+    std::vector<double> r = rhs, p = rhs, rhat0 = rhs, v(n), h(n), s(n), t(n), u(n);
+    x.assign(n, 0.0);
+    double rhat0r = dot(rhat0, r);
+    const double tol = relative ? rtol * std::sqrt(dot(rhs, rhs) / N) : rtol;
+    int it = 0;
+    rms_out = 0.0;
+    for (it = 0; it < max_iters; ++it) {
+      const double rhat0r_old = rhat0r;
+      if (precondition_on) precondition(p, u);
+      else u = p;
+      Ax(g, u, v);
+      const double rhat0v = dot(rhat0, v);
+      const double alpha = rhat0r_old / rhat0v;
+      for (size_t q = 0; q < n; ++q) {
+        h[q] = 1.0 * x[q] + alpha * u[q];
+        s[q] = 1.0 * r[q] + -alpha * v[q];
+      }
+      if (precondition_on) precondition(s, u);
+      else u = s;
+      Ax(g, u, t);
+      const double ts = dot(t, s), tt = dot(t, t);
+      const double omega = ts / tt;
+      for (size_t q = 0; q < n; ++q) {
+        x[q] = 1.0 * h[q] + omega * u[q];
+        r[q] = 1.0 * s[q] + -omega * t[q];
+      }
+      const double res = dot(r, r);
+      rhat0r = dot(rhat0, r);
+      const double beta = rhat0r / rhat0r_old * alpha / omega;
+      for (size_t q = 0; q < n; ++q) {
+        p[q] = 1.0 * p[q] + -omega * v[q];
+        p[q] = 1.0 * r[q] + beta * p[q];
+      }
+      rms_out = std::sqrt(res / N);
+      if (rms_out < tol) return it + 1;
+    }
+    return it;
   }
 
   // residual rhs - A u on the finest level; returns sum of squares (fixed order)

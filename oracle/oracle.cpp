@@ -1176,5 +1176,18 @@ double orc_gmg_residual(void *h) {
   Gmg *g = (Gmg *)h;
   return std::sqrt(g->residual() / (double)g->lv[0].size());
 }
+// BiCGSTAB on rhs (n^3 values) with the V-cycle preconditioner; x receives the
+// solution; returns the iterations run, *rms the final rms residual.
+int orc_bicgstab(void *h, const double *rhs, double *x, int precondition, double rtol, int relative, int max_iters,
+                 double *rms) {
+  Gmg *g = (Gmg *)h;
+  const size_t n = (size_t)g->lv[0].size();
+  std::vector<double> b(rhs, rhs + n), sol;
+  double r = 0.0;
+  const int it = g->bicgstab(b, sol, precondition != 0, rtol, relative != 0, max_iters, r);
+  std::copy(sol.begin(), sol.end(), x);
+  if (rms) *rms = r;
+  return it;
+}
 
 }  // extern "C"

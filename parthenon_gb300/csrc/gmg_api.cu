@@ -21,11 +21,13 @@ namespace pgb {
 namespace gmg_exact {
 void vcycle_d(GmgLevelBuf<double> *L, int nl, const GmgConfig &c, cudaStream_t s);
 void residual_sumsq_d(GmgLevelBuf<double> &L, const GmgConfig &c, double *partial, int np, cudaStream_t s);
+void apply_d(const GmgLevelBuf<double> &L, const GmgConfig &c, const double *u, double *out, cudaStream_t s);
 }  // namespace gmg_exact
 namespace gmg_fast {
 void vcycle_d(GmgLevelBuf<double> *L, int nl, const GmgConfig &c, cudaStream_t s);
 void vcycle_f(GmgLevelBuf<float> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *c64, cudaStream_t s);
 void residual_sumsq_d(GmgLevelBuf<double> &L, const GmgConfig &c, double *partial, int np, cudaStream_t s);
+void apply_d(const GmgLevelBuf<double> &L, const GmgConfig &c, const double *u, double *out, cudaStream_t s);
 void mixed_prepare(const double *r64, GmgLevelBuf<float> &L0, cudaStream_t s);
 void mixed_update(double *x, const GmgLevelBuf<float> &L0, cudaStream_t s);
 }  // namespace gmg_fast
@@ -47,11 +49,21 @@ struct pgb_gmg {
   // cached graphs: [0] fp64 iteration, [1] mixed iteration; keyed by caller pointers
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   const void *graph_key[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  // BiCGSTAB state (allocated on first use): vectors x r rhat0 p v h s t u prhs, device
+  // scalars, dot-product partials, pinned copy of (r, r); one graph per preconditioner
+  double *kv[10] = {};
+  double *ks = nullptr;     // rhat0r, rhat0r_old, rhat0v, ts, tt, res, rhs2
+  double *kpart = nullptr;  // dot partials
+  double *kres_h = nullptr; // pinned host: res, rhs2
+  cudaGraphExec_t kgraph[3] = {nullptr, nullptr, nullptr};
   ~pgb_gmg() {
     for (auto &g : graph)
       if (g) cudaGraphExecDestroy(g);
+    for (auto &g : kgraph)
+      if (g) cudaGraphExecDestroy(g);
     for (void *p : allocs) cudaFree(p);
     if (partial_h) cudaFreeHost(partial_h);
+    if (kres_h) cudaFreeHost(kres_h);
   }
   template <class T>
   int alloc(T **p, int64_t n) {
@@ -135,9 +147,209 @@ int run_iteration(pgb_gmg *g, int which, cudaStream_t s, int use_graph) {
   return kOk;
 }
 
+// ------------------------------------------------------------------ BiCGSTAB
+// bicgstab_solver.hpp:116-315: right-preconditioned BiCGSTAB with one multigrid
+// V-cycle from zero as the preconditioner (AddLinearOperatorTasks). Scalars stay on the
+// device so one iteration is one graph launch; only (r, r) comes back to the host.
+enum KScalar { kRhat0r = 0, kRhat0rOld, kRhat0v, kTs, kTt, kRes, kRhs2, kNumScalars };
+enum KVec { kX = 0, kR, kRhat0, kP, kV, kH, kS, kT, kU, kPrhs };
+constexpr int kDotParts = 512;
+
+__global__ void __launch_bounds__(256) k_dot_partial(const double *__restrict__ a, const double *__restrict__ b,
+                                                     int64_t n, double *__restrict__ partial) {
+  __shared__ double sm[256];
+  double s = 0.0;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+    s += a[c] * b[c];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sm[0];
+}
+
+// out = sum of the partials in a fixed order (one CTA)
+__global__ void __launch_bounds__(256) k_dot_final(const double *__restrict__ partial, int np, double *out) {
+  __shared__ double sm[256];
+  double s = 0.0;
+  for (int q = threadIdx.x; q < np; q += 256) s += partial[q];
+  sm[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sm[0];
+}
+
+// x <- 0, r <- rhs, p <- rhs, rhat0 <- rhs
+__global__ void k_kinit(const double *__restrict__ rhs, double *x, double *r, double *p, double *rh, int64_t n) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double b = rhs[c];
+  x[c] = 0.0;
+  r[c] = b;
+  p[c] = b;
+  rh[c] = b;
+}
+
+__global__ void k_set_old(double *ks) { ks[kRhat0rOld] = ks[kRhat0r]; }
+
+// h <- x + alpha u, s <- r - alpha v with alpha = rhat0r_old / rhat0v
+__global__ void k_hs(const double *__restrict__ x, const double *__restrict__ u, const double *__restrict__ r,
+                     const double *__restrict__ v, double *__restrict__ h, double *__restrict__ s,
+                     const double *__restrict__ ks, int64_t n) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double alpha = ks[kRhat0rOld] / ks[kRhat0v];
+  h[c] = 1.0 * x[c] + alpha * u[c];
+  s[c] = 1.0 * r[c] + -alpha * v[c];
+}
+
+// x <- h + omega u, r <- s - omega t with omega = ts / tt
+__global__ void k_xr(const double *__restrict__ h, const double *__restrict__ u, const double *__restrict__ s,
+                     const double *__restrict__ t, double *__restrict__ x, double *__restrict__ r,
+                     const double *__restrict__ ks, int64_t n) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double omega = ks[kTs] / ks[kTt];
+  x[c] = 1.0 * h[c] + omega * u[c];
+  r[c] = 1.0 * s[c] + -omega * t[c];
+}
+
+// p <- p - omega v; p <- r + beta p with beta = rhat0r / rhat0r_old * alpha / omega
+__global__ void k_pupdate(double *__restrict__ p, const double *__restrict__ v, const double *__restrict__ r,
+                          const double *__restrict__ ks, int64_t n) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double alpha = ks[kRhat0rOld] / ks[kRhat0v];
+  const double omega = ks[kTs] / ks[kTt];
+  const double beta = ks[kRhat0r] / ks[kRhat0rOld] * alpha / omega;
+  const double q = 1.0 * p[c] + -omega * v[c];
+  p[c] = 1.0 * r[c] + beta * q;
+}
+
+int krylov_alloc(pgb_gmg *g) {
+  if (g->ks) return kOk;
+  const int64_t n = g->d[0].cells();
+  int rc;
+  for (auto &v : g->kv)
+    if ((rc = g->alloc(&v, n))) return rc;
+  if ((rc = g->alloc(&g->ks, kNumScalars)) || (rc = g->alloc(&g->kpart, kDotParts))) return rc;
+  if (cudaMallocHost(&g->kres_h, 2 * sizeof(double)) != cudaSuccess) return fail(kErrCuda, "cudaMallocHost failed");
+  return kOk;
+}
+
+void kdot(pgb_gmg *g, const double *a, const double *b, int which, cudaStream_t s) {
+  k_dot_partial<<<kDotParts, 256, 0, s>>>(a, b, g->d[0].cells(), g->kpart);
+  k_dot_final<<<1, 256, 0, s>>>(g->kpart, kDotParts, g->ks + which);
+}
+
+// out <- M in: precond 0 copies, 1 FP64 V-cycle from zero, 2 FP32 V-cycle from zero
+// (FP64 coarsest level)
+int kprecondition(pgb_gmg *g, int precond, const double *in, double *out, cudaStream_t s) {
+  const int64_t n = g->d[0].cells();
+  if (precond == 0) {
+    PGB_CUDA(cudaMemcpyAsync(out, in, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return kOk;
+  }
+  PGB_CUDA(cudaMemsetAsync(out, 0, n * sizeof(double), s));
+  if (precond == 1) {
+    double *prhs = g->kv[kPrhs];
+    PGB_CUDA(cudaMemcpyAsync(prhs, in, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    g->d[0].u = out;
+    g->d[0].rhs = prhs;
+    if (g->exact) gmg_exact::vcycle_d(g->d.data(), g->nl, g->cfg, s);
+    else gmg_fast::vcycle_d(g->d.data(), g->nl, g->cfg, s);
+  } else {
+    gmg_fast::mixed_prepare(in, g->f[0], s);
+    gmg_fast::vcycle_f(g->f.data(), g->nl, g->cfg, &g->c64, s);
+    gmg_fast::mixed_update(out, g->f[0], s);
+  }
+  return kOk;
+}
+
+void kapply(pgb_gmg *g, const double *u, double *out, cudaStream_t s) {
+  if (g->exact) gmg_exact::apply_d(g->d[0], g->cfg, u, out, s);
+  else gmg_fast::apply_d(g->d[0], g->cfg, u, out, s);
+}
+
+// One iteration (steps 1-13 of bicgstab_solver.hpp:174-295) + D2H of (r, r).
+int enqueue_bicg_iteration(pgb_gmg *g, int precond, cudaStream_t s) {
+  const int64_t n = g->d[0].cells();
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  double **v = g->kv;
+  int rc;
+  k_set_old<<<1, 1, 0, s>>>(g->ks);
+  if ((rc = kprecondition(g, precond, v[kP], v[kU], s))) return rc;
+  kapply(g, v[kU], v[kV], s);
+  kdot(g, v[kRhat0], v[kV], kRhat0v, s);
+  k_hs<<<nb, 256, 0, s>>>(v[kX], v[kU], v[kR], v[kV], v[kH], v[kS], g->ks, n);
+  if ((rc = kprecondition(g, precond, v[kS], v[kU], s))) return rc;
+  kapply(g, v[kU], v[kT], s);
+  kdot(g, v[kT], v[kS], kTs, s);
+  kdot(g, v[kT], v[kT], kTt, s);
+  k_xr<<<nb, 256, 0, s>>>(v[kH], v[kU], v[kS], v[kT], v[kX], v[kR], g->ks, n);
+  kdot(g, v[kR], v[kR], kRes, s);
+  kdot(g, v[kRhat0], v[kR], kRhat0r, s);
+  k_pupdate<<<nb, 256, 0, s>>>(v[kP], v[kV], v[kR], g->ks, n);
+  PGB_CUDA(cudaMemcpyAsync(g->kres_h, g->ks + kRes, sizeof(double), cudaMemcpyDeviceToHost, s));
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
 }  // namespace
 
 extern "C" {
+
+int pgb_gmg_bicgstab(pgb_gmg *g, double *u, const double *rhs, int32_t precondition, double rtol,
+                     int32_t relative, int32_t max_iters, int32_t *iters_out, double *rms_out, void *stream) {
+  if (!g || !u || !rhs) return fail(kErrInvalid, "null argument");
+  if (precondition < 0 || precondition > 2) return fail(kErrInvalid, "precondition must be 0, 1 or 2");
+  if (precondition == 2 && g->exact) return fail(kErrInvalid, "the FP32 preconditioner uses the fast kernels");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!s) return fail(kErrInvalid, "BiCGSTAB needs a non-default stream (its iteration is a graph)");
+  int rc = krylov_alloc(g);
+  if (rc) return rc;
+  const int64_t n = g->d[0].cells();
+  const double N = (double)n;
+  double **v = g->kv;
+  k_kinit<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rhs, v[kX], v[kR], v[kP], v[kRhat0], n);
+  kdot(g, v[kRhat0], v[kR], kRhat0r, s);
+  kdot(g, rhs, rhs, kRhs2, s);
+  PGB_CUDA(cudaMemcpyAsync(g->kres_h + 1, g->ks + kRhs2, sizeof(double), cudaMemcpyDeviceToHost, s));
+  PGB_CUDA(cudaStreamSynchronize(s));
+  const double tol = relative ? rtol * std::sqrt(g->kres_h[1] / N) : rtol;
+  if (!g->kgraph[precondition]) {
+    cudaGraph_t gr;
+    PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_bicg_iteration(g, precondition, s);
+    const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return check_cuda(ce, "cudaStreamEndCapture");
+    cudaGraphExec_t ge;
+    const cudaError_t ie = cudaGraphInstantiate(&ge, gr, 0);
+    cudaGraphDestroy(gr);
+    if (ie != cudaSuccess) return check_cuda(ie, "cudaGraphInstantiate");
+    g->kgraph[precondition] = ge;
+  }
+  int it = 0;
+  double rms = 0.0;
+  while (it < max_iters) {
+    PGB_CUDA(cudaGraphLaunch(g->kgraph[precondition], s));
+    PGB_CUDA(cudaStreamSynchronize(s));
+    ++it;
+    rms = std::sqrt(g->kres_h[0] / N);
+    if (rms < tol) break;
+  }
+  PGB_CUDA(cudaMemcpyAsync(u, v[kX], n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  PGB_CUDA(cudaStreamSynchronize(s));
+  if (iters_out) *iters_out = it;
+  if (rms_out) *rms_out = rms;
+  return kOk;
+}
 
 int pgb_gmg_create(const pgb_gmg_params *p, pgb_gmg **out) {
   if (!p || !out) return fail(kErrInvalid, "null argument");

@@ -10,5 +10,8 @@ void vcycle_d(GmgLevelBuf<double> *L, int nl, const GmgConfig &c, cudaStream_t s
 void residual_sumsq_d(GmgLevelBuf<double> &L, const GmgConfig &c, double *partial, int np, cudaStream_t s) {
   residual_sumsq<double>(L, c, partial, np, s);
 }
+void apply_d(const GmgLevelBuf<double> &L, const GmgConfig &c, const double *u, double *out, cudaStream_t s) {
+  apply<double>(L, c, u, out, s);
+}
 }  // namespace gmg_exact
 }  // namespace pgb

@@ -13,6 +13,9 @@ void vcycle_f(GmgLevelBuf<float> *L, int nl, const GmgConfig &c, GmgLevelBuf<dou
 void residual_sumsq_d(GmgLevelBuf<double> &L, const GmgConfig &c, double *partial, int np, cudaStream_t s) {
   residual_sumsq<double>(L, c, partial, np, s);
 }
+void apply_d(const GmgLevelBuf<double> &L, const GmgConfig &c, const double *u, double *out, cudaStream_t s) {
+  apply<double>(L, c, u, out, s);
+}
 void mixed_prepare(const double *r64, GmgLevelBuf<float> &L0, cudaStream_t s) { launch_mixed_prepare(r64, L0, s); }
 void mixed_update(double *x, const GmgLevelBuf<float> &L0, cudaStream_t s) { launch_mixed_update(x, L0, s); }
 }  // namespace gmg_fast

@@ -99,6 +99,17 @@ __global__ void __launch_bounds__(256) k_residual(const T *__restrict__ u, const
   res[c] = (T)1 * rhs[c] + (T)-1 * ax_cell(u, k, j, i, g, D, alpha);
 }
 
+// out <- A u (the Krylov solver's operator application, poisson_equation.hpp Ax)
+template <class T>
+__global__ void __launch_bounds__(256) k_apply(const T *__restrict__ u, T *__restrict__ out, LevelGeom g, T D,
+                                               T alpha) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)g.n * g.n * g.n) return;
+  int k, j, i;
+  cell_of(c, g, k, j, i);
+  out[c] = ax_cell(u, k, j, i, g, D, alpha);
+}
+
 // FAS coarse problem: u0 <- u; rhs <- 1 A u + 1 res   (mg_solver.hpp:423-431)
 template <class T>
 __global__ void __launch_bounds__(256) k_fas_rhs(const T *__restrict__ u, const T *__restrict__ res, T *__restrict__ rhs,
@@ -330,6 +341,11 @@ void residual_sumsq(GmgLevelBuf<T> &L, const GmgConfig &c, double *partial, int 
   const int64_t n = L.cells();
   k_residual<T><<<nblk(n), 256, 0, s>>>(L.u, L.rhs, L.res, geom_of(L), (T)c.D, (T)c.alpha);
   k_sumsq_partial<T><<<nparts, 256, 0, s>>>(L.res, n, partial);
+}
+
+template <class T>
+void apply(const GmgLevelBuf<T> &L, const GmgConfig &c, const T *u, T *out, cudaStream_t s) {
+  k_apply<T><<<nblk(L.cells()), 256, 0, s>>>(u, out, geom_of(L), (T)c.D, (T)c.alpha);
 }
 
 template <class T>

@@ -36,6 +36,22 @@ class GmgSolver:
                   "pgb_gmg_vcycles")
         return rms[:ncycles]
 
+    def bicgstab(self, u, rhs, precondition="fp64", rtol=1e-10, relative=True, max_iters=1000, stream=None):
+        """BiCGSTABSolver (bicgstab_solver.hpp) from u = 0 with a V-cycle preconditioner
+        ("fp64", "fp32" or None); returns (iterations, final rms residual)."""
+        import torch
+        if stream is None:
+            stream = self._stream = getattr(self, "_stream", None) or torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        mode = {None: 0, "none": 0, "fp64": 1, "fp32": 2}[precondition]
+        it = ctypes.c_int32(0)
+        rms = ctypes.c_double(0.0)
+        nat.check(nat.lib().pgb_gmg_bicgstab(self._h, _ptr(u), _ptr(rhs), mode, float(rtol), int(bool(relative)),
+                                             int(max_iters), ctypes.byref(it), ctypes.byref(rms), _stream(stream)),
+                  "pgb_gmg_bicgstab")
+        torch.cuda.current_stream().wait_stream(stream)
+        return it.value, rms.value
+
     def solve(self, u, rhs, mixed=False, rtol=1e-10, max_cycles=200, stream=None):
         cyc = ctypes.c_int32(0)
         rel = ctypes.c_double(0.0)

@@ -243,6 +243,9 @@ def _gmg_lib():
         L.orc_gmg_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.orc_gmg_residual.argtypes = [ctypes.c_void_p]
         L.orc_gmg_residual.restype = ctypes.c_double
+        L.orc_bicgstab.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.orc_bicgstab.restype = ctypes.c_int
         L._gmg_ready = True
     return L
 
@@ -279,3 +282,12 @@ class OracleGmg:
 
     def residual(self):
         return _gmg_lib().orc_gmg_residual(self.h)
+
+    def bicgstab(self, rhs, precondition=True, rtol=1e-10, relative=True, max_iters=1000):
+        """(solution, iterations, final rms residual) of the right-preconditioned BiCGSTAB."""
+        b = np.ascontiguousarray(rhs, np.float64).reshape(-1)
+        x = np.zeros_like(b)
+        rms = np.zeros(1)
+        it = _gmg_lib().orc_bicgstab(self.h, _ptr(b), _ptr(x), int(bool(precondition)), float(rtol),
+                                     int(bool(relative)), int(max_iters), _ptr(rms))
+        return x.reshape(self.n, self.n, self.n), it, float(rms[0])

@@ -72,3 +72,32 @@ def test_solve_to_1e10(mixed):
     got = got - got.mean()
     err = np.abs(got - ref).max() / np.abs(ref).max()
     assert err <= 1e-8, err
+
+
+@pytest.mark.parametrize("precondition", ["fp64", "fp32", None], ids=["mg-fp64", "mg-fp32", "plain"])
+def test_bicgstab_matches_oracle(precondition):
+    import torch
+    n, nc = 32, 2
+    rhs = _rhs(n)
+    g = pg.GmgSolver(n, nc, coarse_sweeps=8)
+    u = torch.zeros((n, n, n), dtype=torch.float64, device="cuda")
+    it, rms = g.bicgstab(u, torch.tensor(rhs, device="cuda"), precondition=precondition, rtol=1e-10,
+                         max_iters=2000)
+    tol = 1e-10 * np.sqrt((rhs ** 2).mean())
+    assert rms < tol
+    o = O.OracleGmg(n, nc, coarse_sweeps=8)
+    ref, it_o, rms_o = o.bicgstab(rhs, precondition=precondition is not None, rtol=1e-10, max_iters=2000)
+    assert rms_o < tol
+    # the iteration count follows the oracle's (rounding differs only in dot-product order
+    # and, for the FP32 preconditioner, in the V-cycle's precision)
+    if precondition == "fp64":
+        assert abs(it - it_o) <= 1
+    elif precondition == "fp32":
+        assert it <= it_o + 2
+    got = u.cpu().numpy()
+    a, b = got - got.mean(), ref - ref.mean()
+    assert np.abs(a - b).max() <= 1e-7 * np.abs(b).max()
+    # independent check of the residual with the operator of the oracle's level
+    o.rhs()[:] = rhs
+    o.u()[:] = got
+    assert o.residual() < 2 * tol
