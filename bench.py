@@ -483,6 +483,7 @@ def main():
     ap.add_argument("--amr-root", type=int, default=AMR_ROOT, help="root cells per direction of the adaptive leg")
     ap.add_argument("--amr-only", action="store_true",
                     help="run only the adaptive leg (profiling runs), no CPU baseline")
+    ap.add_argument("--gmg-only", action="store_true", help="run only the multigrid leg (profiling runs)")
     args = ap.parse_args()
     ws, rank = _dist()
     if ws > 1:
@@ -492,6 +493,10 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         out = {"amr": amr_bench(torch, args.amr_cycles, with_cpu=False, root=args.amr_root)}
+    elif args.gmg_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        out = {"gmg": gmg_bench(torch)}
     elif args.impl == "reference":
         out = run_reference(args, ws, rank)
     else:

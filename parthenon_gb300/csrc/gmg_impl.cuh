@@ -27,6 +27,10 @@ namespace PGB_GMG_NS {
 struct LevelGeom {
   int n, log2n;
   double dx, xmin;
+  // fast build only: D/dx^2, the Jacobi diagonal and 1/diagonal of this level, formed
+  // once on the host instead of three FP64 divides per cell (GB300's FP64 divide rate
+  // is ~1/20 of its FMA rate)
+  double idx2, diag, inv_den;
 };
 
 __device__ __forceinline__ int wrap(int i, int n) { return i & (n - 1); }  // n is a power of 2
@@ -51,8 +55,8 @@ __device__ __forceinline__ T ax_cell(const T *__restrict__ u, int k, int j, int 
   out += (f3l - f3r) / dx;
   return out;
 #else
-  const T idx2 = D / (dx * dx);
-  return ((uim + uip) + (ujm + ujp) + (ukm + ukp) - (T)6 * uc) * idx2 - alpha * uc;
+  (void)dx;
+  return ((uim + uip) + (ujm + ujp) + (ukm + ukp) - (T)6 * uc) * (T)g.idx2 - alpha * uc;
 #endif
 }
 
@@ -80,12 +84,17 @@ __global__ void __launch_bounds__(256) k_jacobi(const T *__restrict__ u, const T
   int k, j, i;
   cell_of(c, g, k, j, i);
   const T ax = ax_cell(u, k, j, i, g, D, alpha);
+#ifdef PGB_GMG_EXACT
   const T dg = diag_value(g, D, alpha);
   const T small = (T)10 * (sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN);
   const T den = dg + (dg >= (T)0 ? (T)1 : (T)-1) * small;
   const T off = ax - dg * u[c];
   const T val = rhs[c] - off;
   out[c] = w * (val / den) + ((T)1 - w) * u[c];
+#else
+  const T off = ax - (T)g.diag * u[c];
+  out[c] = w * ((rhs[c] - off) * (T)g.inv_den) + ((T)1 - w) * u[c];
+#endif
 }
 
 // res <- 1 rhs + (-1) A u
@@ -144,10 +153,19 @@ __global__ void __launch_bounds__(256) k_restrict2(const T *__restrict__ fu, con
       for (int oj = 0; oj < 2; ++oj)
 #pragma unroll
         for (int oi = 0; oi < 2; ++oi)
+#ifdef PGB_GMG_EXACT
           t[ok][oj][oi] = vol * src[(int64_t)(2 * k + ok) * nn + (2 * j + oj) * n + (2 * i + oi)];
+#else
+          t[ok][oj][oi] = src[(int64_t)(2 * k + ok) * nn + (2 * j + oj) * n + (2 * i + oi)];
+#endif
     const T num = ((t[0][0][0] + t[0][1][0]) + (t[0][0][1] + t[0][1][1])) +
                   ((t[1][0][0] + t[1][1][0]) + (t[1][0][1] + t[1][1][1]));
+#ifdef PGB_GMG_EXACT
     (f ? cr : cu)[c] = num / tv;
+#else
+    (f ? cr : cu)[c] = num * (T)0.125;  // equal volumes: the volume-weighted mean is the mean
+    (void)tv;
+#endif
   }
 }
 
@@ -167,6 +185,11 @@ __global__ void __launch_bounds__(256) k_prolong_add(const T *__restrict__ cres,
   T gm[3], gp[3], dfm[3], dfp[3];
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
+    const int64_t om = q == 0 ? ((int64_t)k * nn + j * n + wrap(i - 1, n))
+                              : (q == 1 ? ((int64_t)k * nn + wrap(j - 1, n) * n + i) : ((int64_t)wrap(k - 1, n) * nn + j * n + i));
+    const int64_t op = q == 0 ? ((int64_t)k * nn + j * n + wrap(i + 1, n))
+                              : (q == 1 ? ((int64_t)k * nn + wrap(j + 1, n) * n + i) : ((int64_t)wrap(k + 1, n) * nn + j * n + i));
+#ifdef PGB_GMG_EXACT
     const double xc = cg.xmin + (ci[q] + 0.5) * cg.dx;
     const double xm = cg.xmin + (ci[q] - 1 + 0.5) * cg.dx;
     const double xp = cg.xmin + (ci[q] + 1 + 0.5) * cg.dx;
@@ -175,12 +198,14 @@ __global__ void __launch_bounds__(256) k_prolong_add(const T *__restrict__ cres,
     const T dxm = (T)(xc - xm), dxp = (T)(xp - xc);
     dfm[q] = (T)(xc - fxm);
     dfp[q] = (T)(fxp - xc);
-    const int64_t om = q == 0 ? ((int64_t)k * nn + j * n + wrap(i - 1, n))
-                              : (q == 1 ? ((int64_t)k * nn + wrap(j - 1, n) * n + i) : ((int64_t)wrap(k - 1, n) * nn + j * n + i));
-    const int64_t op = q == 0 ? ((int64_t)k * nn + j * n + wrap(i + 1, n))
-                              : (q == 1 ? ((int64_t)k * nn + wrap(j + 1, n) * n + i) : ((int64_t)wrap(k + 1, n) * nn + j * n + i));
     gm[q] = (fc - cres[om]) / dxm;
     gp[q] = (cres[op] - fc) / dxp;
+#else
+    // uniform level: slope (difference / dx_c) times offset (dx_c / 4)
+    dfm[q] = dfp[q] = (T)0.25;
+    gm[q] = fc - cres[om];
+    gp[q] = cres[op] - fc;
+#endif
   }
   const T m0 = gm[0] * dfm[0], p0 = gp[0] * dfp[0];
   const T m1 = gm[1] * dfm[1], p1 = gp[1] * dfp[1];
@@ -248,6 +273,21 @@ LevelGeom geom_of(const GmgLevelBuf<T> &L) {
   g.log2n = L.log2n;
   g.dx = L.dx;
   g.xmin = L.xmin;
+  g.idx2 = g.diag = g.inv_den = 0.0;
+  return g;
+}
+
+// Level geometry with the operator constants the fast kernels use.
+template <class T>
+LevelGeom geom_with(const GmgLevelBuf<T> &L, const GmgConfig &c) {
+  LevelGeom g = geom_of(L);
+  const double dx2 = L.dx * L.dx;
+  g.idx2 = c.D / dx2;
+  double d = -(c.D + c.D) / dx2 - c.alpha;
+  d -= (c.D + c.D) / dx2;
+  d -= (c.D + c.D) / dx2;
+  g.diag = d;
+  g.inv_den = 1.0 / (d + (d >= 0.0 ? 1.0 : -1.0) * 10.0 * DBL_MIN);
   return g;
 }
 
@@ -263,7 +303,7 @@ inline double smoother_weight(const GmgConfig &c, int s) {
 template <class T>
 void smooth(GmgLevelBuf<T> &L, const GmgConfig &c, cudaStream_t s) {
   if (c.stages == 0) return;
-  const LevelGeom g = geom_of(L);
+  const LevelGeom g = geom_with(L, c);
   const int64_t n = L.cells();
   T *a = L.u, *b = L.temp;
   for (int st = 0; st < c.stages; ++st) {
@@ -289,7 +329,7 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
   for (int l = 0; l < nl; ++l) {
     GmgLevelBuf<T> &g = L[l];
     const int64_t n = g.cells();
-    const LevelGeom lg = geom_of(g);
+    const LevelGeom lg = geom_with(g, c);
     if (l > 0) {
       GmgLevelBuf<T> &f = L[l - 1];
       k_restrict2<T><<<nblk(n), 256, 0, s>>>(f.u, f.res, g.u, g.res, geom_of(f), lg);
@@ -298,7 +338,7 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
     if (coarsest && c64) {
       // coarsest level in FP64: convert, solve there, convert the error back
       GmgLevelBuf<double> &h = *c64;
-      const LevelGeom hg = geom_of(h);
+      const LevelGeom hg = geom_with(h, c);
       k_convert<T, double><<<nblk(n), 256, 0, s>>>(g.u, h.u, n);
       k_convert<T, double><<<nblk(n), 256, 0, s>>>(g.res, h.res, n);
       if (l > 0) {
@@ -339,13 +379,13 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
 template <class T>
 void residual_sumsq(GmgLevelBuf<T> &L, const GmgConfig &c, double *partial, int nparts, cudaStream_t s) {
   const int64_t n = L.cells();
-  k_residual<T><<<nblk(n), 256, 0, s>>>(L.u, L.rhs, L.res, geom_of(L), (T)c.D, (T)c.alpha);
+  k_residual<T><<<nblk(n), 256, 0, s>>>(L.u, L.rhs, L.res, geom_with(L, c), (T)c.D, (T)c.alpha);
   k_sumsq_partial<T><<<nparts, 256, 0, s>>>(L.res, n, partial);
 }
 
 template <class T>
 void apply(const GmgLevelBuf<T> &L, const GmgConfig &c, const T *u, T *out, cudaStream_t s) {
-  k_apply<T><<<nblk(L.cells()), 256, 0, s>>>(u, out, geom_of(L), (T)c.D, (T)c.alpha);
+  k_apply<T><<<nblk(L.cells()), 256, 0, s>>>(u, out, geom_with(L, c), (T)c.D, (T)c.alpha);
 }
 
 template <class T>
