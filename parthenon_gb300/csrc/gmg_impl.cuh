@@ -17,6 +17,7 @@
 //   src/prolong_restrict/pr_ops.hpp:105-285           RestrictAverage, ProlongateSharedLinear
 #pragma once
 
+#include <algorithm>
 #include <cfloat>
 
 #include "common.cuh"
@@ -36,7 +37,7 @@ struct LevelGeom {
 __device__ __forceinline__ int wrap(int i, int n) { return i & (n - 1); }  // n is a power of 2
 
 template <class T>
-__device__ __forceinline__ T ax_cell(const T *__restrict__ u, int k, int j, int i, const LevelGeom &g, T D, T alpha) {
+__device__ __forceinline__ T ax_cell(const T *u, int k, int j, int i, const LevelGeom &g, T D, T alpha) {
   const int n = g.n;
   const int64_t nn = (int64_t)n * n;
   const T dx = (T)g.dx;
@@ -76,15 +77,19 @@ __device__ __forceinline__ void cell_of(int64_t c, const LevelGeom &g, int &k, i
 }
 
 // temp <- Jacobi(u): w * (rhs - (A u - d u)) / d + (1 - w) u   (mg_solver.hpp:277-291)
+// Fast build: for the 7-point operator A u - d u is D/dx^2 times the sum of the six
+// neighbours, so a sweep is out = (w/d) (rhs - idx2 * S) + (1 - w) u with w/d and
+// 1 - w formed on the host: 8 FP64 instructions per cell instead of about 14 plus a
+// divide (the FP64 pipe, not HBM, bounds this kernel on GB300).
 template <class T>
-__global__ void __launch_bounds__(256) k_jacobi(const T *__restrict__ u, const T *__restrict__ rhs, T *__restrict__ out,
-                                                LevelGeom g, T D, T alpha, T w) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= (int64_t)g.n * g.n * g.n) return;
+__device__ __forceinline__ void jacobi_at(int64_t c, const T *u, const T *rhs,
+                                          T *out, const LevelGeom &g, T D, T alpha, T w, T wd, T omw) {
   int k, j, i;
   cell_of(c, g, k, j, i);
-  const T ax = ax_cell(u, k, j, i, g, D, alpha);
 #ifdef PGB_GMG_EXACT
+  (void)wd;
+  (void)omw;
+  const T ax = ax_cell(u, k, j, i, g, D, alpha);
   const T dg = diag_value(g, D, alpha);
   const T small = (T)10 * (sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN);
   const T den = dg + (dg >= (T)0 ? (T)1 : (T)-1) * small;
@@ -92,20 +97,40 @@ __global__ void __launch_bounds__(256) k_jacobi(const T *__restrict__ u, const T
   const T val = rhs[c] - off;
   out[c] = w * (val / den) + ((T)1 - w) * u[c];
 #else
-  const T off = ax - (T)g.diag * u[c];
-  out[c] = w * ((rhs[c] - off) * (T)g.inv_den) + ((T)1 - w) * u[c];
+  (void)D;
+  (void)alpha;
+  (void)w;
+  const int n = g.n;
+  const int64_t nn = (int64_t)n * n;
+  const T uc = u[c];
+  const T s = ((u[(int64_t)k * nn + j * n + wrap(i - 1, n)] + u[(int64_t)k * nn + j * n + wrap(i + 1, n)]) +
+               (u[(int64_t)k * nn + wrap(j - 1, n) * n + i] + u[(int64_t)k * nn + wrap(j + 1, n) * n + i])) +
+              (u[(int64_t)wrap(k - 1, n) * nn + j * n + i] + u[(int64_t)wrap(k + 1, n) * nn + j * n + i]);
+  out[c] = wd * (rhs[c] - (T)g.idx2 * s) + omw * uc;
 #endif
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_jacobi(const T *__restrict__ u, const T *__restrict__ rhs, T *__restrict__ out,
+                                                LevelGeom g, T D, T alpha, T w, T wd, T omw) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < (int64_t)g.n * g.n * g.n) jacobi_at(c, u, rhs, out, g, D, alpha, w, wd, omw);
 }
 
 // res <- 1 rhs + (-1) A u
 template <class T>
-__global__ void __launch_bounds__(256) k_residual(const T *__restrict__ u, const T *__restrict__ rhs, T *__restrict__ res,
-                                                  LevelGeom g, T D, T alpha) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= (int64_t)g.n * g.n * g.n) return;
+__device__ __forceinline__ void residual_at(int64_t c, const T *u, const T *rhs,
+                                            T *res, const LevelGeom &g, T D, T alpha) {
   int k, j, i;
   cell_of(c, g, k, j, i);
   res[c] = (T)1 * rhs[c] + (T)-1 * ax_cell(u, k, j, i, g, D, alpha);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_residual(const T *__restrict__ u, const T *__restrict__ rhs, T *__restrict__ res,
+                                                  LevelGeom g, T D, T alpha) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < (int64_t)g.n * g.n * g.n) residual_at(c, u, rhs, res, g, D, alpha);
 }
 
 // out <- A u (the Krylov solver's operator application, poisson_equation.hpp Ax)
@@ -121,22 +146,26 @@ __global__ void __launch_bounds__(256) k_apply(const T *__restrict__ u, T *__res
 
 // FAS coarse problem: u0 <- u; rhs <- 1 A u + 1 res   (mg_solver.hpp:423-431)
 template <class T>
-__global__ void __launch_bounds__(256) k_fas_rhs(const T *__restrict__ u, const T *__restrict__ res, T *__restrict__ rhs,
-                                                 T *__restrict__ u0, LevelGeom g, T D, T alpha) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= (int64_t)g.n * g.n * g.n) return;
+__device__ __forceinline__ void fas_at(int64_t c, const T *u, const T *res,
+                                       T *rhs, T *u0, const LevelGeom &g, T D, T alpha) {
   int k, j, i;
   cell_of(c, g, k, j, i);
   u0[c] = u[c];
   rhs[c] = (T)1 * ax_cell(u, k, j, i, g, D, alpha) + (T)1 * res[c];
 }
 
+template <class T>
+__global__ void __launch_bounds__(256) k_fas_rhs(const T *__restrict__ u, const T *__restrict__ res, T *__restrict__ rhs,
+                                                 T *__restrict__ u0, LevelGeom g, T D, T alpha) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < (int64_t)g.n * g.n * g.n) fas_at(c, u, res, rhs, u0, g, D, alpha);
+}
+
 // RestrictAverage of two fields (u and res) onto the coarse level (pr_ops.hpp:105-164)
 template <class T>
-__global__ void __launch_bounds__(256) k_restrict2(const T *__restrict__ fu, const T *__restrict__ fr, T *__restrict__ cu,
-                                                   T *__restrict__ cr, LevelGeom fg, LevelGeom cg) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= (int64_t)cg.n * cg.n * cg.n) return;
+__device__ __forceinline__ void restrict2_at(int64_t c, const T *fu, const T *fr,
+                                             T *cu, T *cr, const LevelGeom &fg,
+                                             const LevelGeom &cg) {
   int k, j, i;
   cell_of(c, cg, k, j, i);
   const T vol = (T)fg.dx * (T)fg.dx * (T)fg.dx;
@@ -169,13 +198,18 @@ __global__ void __launch_bounds__(256) k_restrict2(const T *__restrict__ fu, con
   }
 }
 
+template <class T>
+__global__ void __launch_bounds__(256) k_restrict2(const T *__restrict__ fu, const T *__restrict__ fr, T *__restrict__ cu,
+                                                   T *__restrict__ cr, LevelGeom fg, LevelGeom cg) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < (int64_t)cg.n * cg.n * cg.n) restrict2_at(c, fu, fr, cu, cr, fg, cg);
+}
+
 // u_fine <- 1 u_fine + 1 Prolongate(res_coarse) with ProlongateSharedLinear
 // (pr_ops.hpp:166-285, one-sided slopes), fused with AddFieldsAndStore<u, res_err, u>.
 template <class T>
-__global__ void __launch_bounds__(256) k_prolong_add(const T *__restrict__ cres, T *__restrict__ fu, LevelGeom cg,
-                                                     LevelGeom fg) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= (int64_t)cg.n * cg.n * cg.n) return;
+__device__ __forceinline__ void prolong_add_at(int64_t c, const T *cres, T *fu,
+                                               const LevelGeom &cg, const LevelGeom &fg) {
   int k, j, i;
   cell_of(c, cg, k, j, i);
   const int n = cg.n;
@@ -221,6 +255,13 @@ __global__ void __launch_bounds__(256) k_prolong_add(const T *__restrict__ cres,
     const int64_t e = b0 + ok * fnn + oj * fn + oi;
     fu[e] = (T)1 * fu[e] + (T)1 * v[q];
   }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_prolong_add(const T *__restrict__ cres, T *__restrict__ fu, LevelGeom cg,
+                                                     LevelGeom fg) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < (int64_t)cg.n * cg.n * cg.n) prolong_add_at(c, cres, fu, cg, fg);
 }
 
 // out <- 1 a + (-1) b
@@ -307,7 +348,8 @@ void smooth(GmgLevelBuf<T> &L, const GmgConfig &c, cudaStream_t s) {
   const int64_t n = L.cells();
   T *a = L.u, *b = L.temp;
   for (int st = 0; st < c.stages; ++st) {
-    k_jacobi<T><<<nblk(n), 256, 0, s>>>(a, L.rhs, b, g, (T)c.D, (T)c.alpha, (T)smoother_weight(c, st));
+    const double w = smoother_weight(c, st);
+    k_jacobi<T><<<nblk(n), 256, 0, s>>>(a, L.rhs, b, g, (T)c.D, (T)c.alpha, (T)w, (T)(w * g.inv_den), (T)(1.0 - w));
     T *t = a;
     a = b;
     b = t;
@@ -321,12 +363,153 @@ __global__ void k_convert(const Tf *__restrict__ a, Tc *__restrict__ b, int64_t 
   if (c < n) b[c] = (Tc)a[c];
 }
 
+// ------------------------------------------------------------------ coarse tail
+// The levels of at most kTailCells cells (8^3 and below) hold a few hundred cells but
+// carry many of a V-cycle's launches (restriction, FAS right-hand side, smoothing and
+// the extra coarsest-level passes, residuals, prolongation). One CTA of kTailThreads
+// threads runs all of them in one launch, phase after phase separated by
+// __syncthreads(), with the same per-cell operations as the standalone kernels. The
+// bound is low because one SM issues only ~2 FP64 operations per clock: a 16^3 level
+// is faster as ordinary launches over 16 SMs. The per-cell functions take plain
+// pointers: arrays written in one phase are read in the next, so no load may go
+// through the non-coherent read-only path.
+constexpr int kTailMax = 4;
+constexpr int kTailThreads = 512;
+constexpr int64_t kTailCells = 512;
+
+template <class T>
+struct TailLevel {
+  T *u, *rhs, *res, *temp, *u0;
+  LevelGeom g;
+  int64_t n;
+};
+
+template <class T>
+struct TailArgs {
+  TailLevel<T> lv[kTailMax];  // lv[0] is hierarchy level `lt`
+  int nlev, lt;
+  const T *above_u, *above_res;  // level lt - 1 (restriction source) when lt > 0
+  LevelGeom above_g;
+  TailLevel<double> h;  // FP64 coarsest level (mixed precision) when use_c64
+  int use_c64;
+  int stages, coarse_sweeps;
+  double w[3], wd[kTailMax][3], hwd[3];
+  double D, alpha;
+};
+
+template <class F>
+__device__ __forceinline__ void tail_cells(int64_t n, F f) {
+  for (int64_t c = threadIdx.x; c < n; c += blockDim.x) f(c);
+  __syncthreads();
+}
+
+template <class T>
+__device__ void tail_smooth(const TailLevel<T> &L, int stages, const double *w, const double *wd, T D, T alpha) {
+  T *a = L.u, *b = L.temp;
+  for (int st = 0; st < stages; ++st) {
+    const T ww = (T)w[st], wdd = (T)wd[st], omw = (T)(1.0 - w[st]);
+    tail_cells(L.n, [&](int64_t c) { jacobi_at(c, a, L.rhs, b, L.g, D, alpha, ww, wdd, omw); });
+    T *t = a;
+    a = b;
+    b = t;
+  }
+  if (a != L.u) tail_cells(L.n, [&](int64_t c) { L.u[c] = a[c]; });
+}
+
+template <class T>
+__global__ void __launch_bounds__(kTailThreads, 1) k_tail(TailArgs<T> a) {
+  const T D = (T)a.D, alpha = (T)a.alpha;
+  for (int q = 0; q < a.nlev; ++q) {
+    const TailLevel<T> &L = a.lv[q];
+    const int l = a.lt + q;
+    const bool coarsest = q == a.nlev - 1;
+    if (l > 0) {
+      const T *su = q == 0 ? a.above_u : a.lv[q - 1].u;
+      const T *sr = q == 0 ? a.above_res : a.lv[q - 1].res;
+      const LevelGeom sg = q == 0 ? a.above_g : a.lv[q - 1].g;
+      tail_cells(L.n, [&](int64_t c) { restrict2_at(c, su, sr, L.u, L.res, sg, L.g); });
+    }
+    if (coarsest && a.use_c64) {
+      const TailLevel<double> &h = a.h;
+      tail_cells(L.n, [&](int64_t c) {
+        h.u[c] = (double)L.u[c];
+        h.res[c] = (double)L.res[c];
+      });
+      if (l > 0) {
+        tail_cells(L.n, [&](int64_t c) { fas_at<double>(c, h.u, h.res, h.rhs, h.u0, h.g, a.D, a.alpha); });
+      } else {
+        tail_cells(L.n, [&](int64_t c) {
+          h.rhs[c] = (double)L.rhs[c];
+          h.u0[c] = h.u[c];
+        });
+      }
+      for (int pass = 0; pass <= a.coarse_sweeps; ++pass) tail_smooth<double>(h, a.stages, a.w, a.hwd, a.D, a.alpha);
+      if (l > 0) tail_cells(L.n, [&](int64_t c) { h.res[c] = 1.0 * h.u[c] + -1.0 * h.u0[c]; });
+      else tail_cells(L.n, [&](int64_t c) { h.res[c] = h.u[c]; });
+      tail_cells(L.n, [&](int64_t c) {
+        L.res[c] = (T)h.res[c];
+        if (l == 0) L.u[c] = (T)h.u[c];
+      });
+      break;
+    }
+    if (l > 0) tail_cells(L.n, [&](int64_t c) { fas_at(c, L.u, L.res, L.rhs, L.u0, L.g, D, alpha); });
+    else tail_cells(L.n, [&](int64_t c) { L.u0[c] = L.u[c]; });
+    tail_smooth<T>(L, a.stages, a.w, a.wd[q], D, alpha);
+    if (!coarsest) {
+      tail_cells(L.n, [&](int64_t c) { residual_at(c, L.u, L.rhs, L.res, L.g, D, alpha); });
+    } else {
+      for (int pass = 0; pass < a.coarse_sweeps; ++pass) tail_smooth<T>(L, a.stages, a.w, a.wd[q], D, alpha);
+      if (l > 0) tail_cells(L.n, [&](int64_t c) { L.res[c] = (T)1 * L.u[c] + (T)-1 * L.u0[c]; });
+      else tail_cells(L.n, [&](int64_t c) { L.res[c] = L.u[c]; });
+    }
+  }
+  for (int q = a.nlev - 2; q >= 0; --q) {
+    const TailLevel<T> &L = a.lv[q], &C = a.lv[q + 1];
+    tail_cells(C.n, [&](int64_t c) { prolong_add_at(c, C.res, L.u, C.g, L.g); });
+    tail_smooth<T>(L, a.stages, a.w, a.wd[q], D, alpha);
+    if (a.lt + q > 0) tail_cells(L.n, [&](int64_t c) { L.res[c] = (T)1 * L.u[c] + (T)-1 * L.u0[c]; });
+  }
+}
+
 // One FAS V-cycle (mg_solver.hpp:375-520) over levels L[0] (finest) .. L[nl-1].
 // When c64 is given, the coarsest level runs in FP64 on c64 (mixed precision).
 template <class T>
 void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *c64, cudaStream_t s) {
   const T D = (T)c.D, alpha = (T)c.alpha;
+  // levels lt .. nl-1 (at most kTailCells cells each, at most kTailMax of them) run in
+  // one tail launch
+  int lt = nl;
+  while (lt > 0 && L[lt - 1].cells() <= kTailCells && nl - (lt - 1) <= kTailMax) --lt;
+  TailArgs<T> ta{};
+  if (lt < nl) {
+    ta.nlev = nl - lt;
+    ta.lt = lt;
+    ta.stages = c.stages;
+    ta.coarse_sweeps = c.coarse_sweeps;
+    ta.D = c.D;
+    ta.alpha = c.alpha;
+    for (int st = 0; st < 3; ++st) ta.w[st] = st < c.stages ? smoother_weight(c, st) : 0.0;
+    for (int q = 0; q < ta.nlev; ++q) {
+      GmgLevelBuf<T> &g = L[lt + q];
+      ta.lv[q] = TailLevel<T>{g.u, g.rhs, g.res, g.temp, g.u0, geom_with(g, c), g.cells()};
+      for (int st = 0; st < 3; ++st) ta.wd[q][st] = ta.w[st] * ta.lv[q].g.inv_den;
+    }
+    if (lt > 0) {
+      ta.above_u = L[lt - 1].u;
+      ta.above_res = L[lt - 1].res;
+      ta.above_g = geom_of(L[lt - 1]);
+    }
+    if (c64) {
+      ta.use_c64 = 1;
+      ta.h = TailLevel<double>{c64->u, c64->rhs, c64->res, c64->temp, c64->u0, geom_with(*c64, c), c64->cells()};
+      for (int st = 0; st < 3; ++st) ta.hwd[st] = ta.w[st] * ta.h.g.inv_den;
+    }
+  }
   for (int l = 0; l < nl; ++l) {
+    if (l == lt) {
+      k_tail<T><<<1, kTailThreads, 0, s>>>(ta);
+      break;
+    }
     GmgLevelBuf<T> &g = L[l];
     const int64_t n = g.cells();
     const LevelGeom lg = geom_with(g, c);
@@ -366,7 +549,8 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
       else k_copy_arr<T><<<nblk(n), 256, 0, s>>>(g.u, g.res, n);
     }
   }
-  for (int l = nl - 2; l >= 0; --l) {
+  // up-sweep of the levels above the tail (the tail did its own)
+  for (int l = std::min(nl - 2, lt - 1); l >= 0; --l) {
     GmgLevelBuf<T> &g = L[l], &cl = L[l + 1];
     const int64_t n = g.cells();
     k_prolong_add<T><<<nblk(cl.cells()), 256, 0, s>>>(cl.res, g.u, geom_of(cl), geom_of(g));
