@@ -20,13 +20,15 @@
 namespace pgb {
 namespace gmg_exact {
 void vcycle_d(GmgLevelBuf<double> *L, int nl, const GmgConfig &c, cudaStream_t s);
-void residual_sumsq_d(GmgLevelBuf<double> &L, const GmgConfig &c, double *partial, int np, cudaStream_t s);
+void residual_sumsq_d(GmgLevelBuf<double> &L, const GmgConfig &c, double *partial, int np, double *res, float *rhs32,
+                      cudaStream_t s);
 void apply_d(const GmgLevelBuf<double> &L, const GmgConfig &c, const double *u, double *out, cudaStream_t s);
 }  // namespace gmg_exact
 namespace gmg_fast {
 void vcycle_d(GmgLevelBuf<double> *L, int nl, const GmgConfig &c, cudaStream_t s);
 void vcycle_f(GmgLevelBuf<float> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *c64, cudaStream_t s);
-void residual_sumsq_d(GmgLevelBuf<double> &L, const GmgConfig &c, double *partial, int np, cudaStream_t s);
+void residual_sumsq_d(GmgLevelBuf<double> &L, const GmgConfig &c, double *partial, int np, double *res, float *rhs32,
+                      cudaStream_t s);
 void apply_d(const GmgLevelBuf<double> &L, const GmgConfig &c, const double *u, double *out, cudaStream_t s);
 void mixed_prepare(const double *r64, GmgLevelBuf<float> &L0, cudaStream_t s);
 void mixed_update(double *x, const GmgLevelBuf<float> &L0, cudaStream_t s);
@@ -44,7 +46,7 @@ struct pgb_gmg {
   GmgLevelBuf<double> c64;
   double *partial = nullptr;  // device
   double *partial_h = nullptr;  // pinned host
-  int nparts = 256;
+  int nparts = 1024;
   std::vector<void *> allocs;
   // cached graphs: [0] fp64 iteration, [1] mixed iteration; keyed by caller pointers
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -99,10 +101,10 @@ double host_rms(pgb_gmg *g, int64_t ncell) {
 int enqueue_fp64_iteration(pgb_gmg *g, cudaStream_t s) {
   if (g->exact) {
     gmg_exact::vcycle_d(g->d.data(), g->nl, g->cfg, s);
-    gmg_exact::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, s);
+    gmg_exact::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, g->d[0].res, nullptr, s);
   } else {
     gmg_fast::vcycle_d(g->d.data(), g->nl, g->cfg, s);
-    gmg_fast::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, s);
+    gmg_fast::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, nullptr, nullptr, s);
   }
   PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
   PGB_CUDA(cudaGetLastError());
@@ -110,12 +112,13 @@ int enqueue_fp64_iteration(pgb_gmg *g, cudaStream_t s) {
 }
 
 // One mixed iteration: FP32 V-cycle on the current FP64 residual, FP64 update, new
-// FP64 residual + partial sums + D2H. Expects d[0].res to hold b - A x on entry.
+// FP64 residual + partial sums + D2H. Expects f[0].rhs to hold (float)(b - A x) on
+// entry and leaves the next one there.
 int enqueue_mixed_iteration(pgb_gmg *g, cudaStream_t s) {
-  gmg_fast::mixed_prepare(g->d[0].res, g->f[0], s);
+  gmg_fast::mixed_prepare(nullptr, g->f[0], s);
   gmg_fast::vcycle_f(g->f.data(), g->nl, g->cfg, &g->c64, s);
   gmg_fast::mixed_update(g->d[0].u, g->f[0], s);
-  gmg_fast::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, s);
+  gmg_fast::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, nullptr, g->f[0].rhs, s);
   PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
   PGB_CUDA(cudaGetLastError());
   return kOk;
@@ -151,7 +154,7 @@ int run_iteration(pgb_gmg *g, int which, cudaStream_t s, int use_graph) {
 // bicgstab_solver.hpp:116-315: right-preconditioned BiCGSTAB with one multigrid
 // V-cycle from zero as the preconditioner (AddLinearOperatorTasks). Scalars stay on the
 // device so one iteration is one graph launch; only (r, r) comes back to the host.
-enum KScalar { kRhat0r = 0, kRhat0rOld, kRhat0v, kTs, kTt, kRes, kRhs2, kNumScalars };
+enum KScalar { kRhat0r = 0, kRhat0rOld, kRhat0v, kTs, kTt, kRes, kRhs2, kAlpha, kOmega, kBeta, kNumScalars };
 enum KVec { kX = 0, kR, kRhat0, kP, kV, kH, kS, kT, kU, kPrhs };
 constexpr int kDotParts = 512;
 
@@ -197,13 +200,19 @@ __global__ void k_kinit(const double *__restrict__ rhs, double *x, double *r, do
 
 __global__ void k_set_old(double *ks) { ks[kRhat0rOld] = ks[kRhat0r]; }
 
+// The step scalars, formed once per iteration (not once per cell: an FP64 divide costs
+// about twenty FMA slots on GB300).
+__global__ void k_alpha(double *ks) { ks[kAlpha] = ks[kRhat0rOld] / ks[kRhat0v]; }
+__global__ void k_omega(double *ks) { ks[kOmega] = ks[kTs] / ks[kTt]; }
+__global__ void k_beta(double *ks) { ks[kBeta] = ks[kRhat0r] / ks[kRhat0rOld] * ks[kAlpha] / ks[kOmega]; }
+
 // h <- x + alpha u, s <- r - alpha v with alpha = rhat0r_old / rhat0v
 __global__ void k_hs(const double *__restrict__ x, const double *__restrict__ u, const double *__restrict__ r,
                      const double *__restrict__ v, double *__restrict__ h, double *__restrict__ s,
                      const double *__restrict__ ks, int64_t n) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
-  const double alpha = ks[kRhat0rOld] / ks[kRhat0v];
+  const double alpha = ks[kAlpha];
   h[c] = 1.0 * x[c] + alpha * u[c];
   s[c] = 1.0 * r[c] + -alpha * v[c];
 }
@@ -214,7 +223,7 @@ __global__ void k_xr(const double *__restrict__ h, const double *__restrict__ u,
                      const double *__restrict__ ks, int64_t n) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
-  const double omega = ks[kTs] / ks[kTt];
+  const double omega = ks[kOmega];
   x[c] = 1.0 * h[c] + omega * u[c];
   r[c] = 1.0 * s[c] + -omega * t[c];
 }
@@ -224,9 +233,7 @@ __global__ void k_pupdate(double *__restrict__ p, const double *__restrict__ v, 
                           const double *__restrict__ ks, int64_t n) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
-  const double alpha = ks[kRhat0rOld] / ks[kRhat0v];
-  const double omega = ks[kTs] / ks[kTt];
-  const double beta = ks[kRhat0r] / ks[kRhat0rOld] * alpha / omega;
+  const double omega = ks[kOmega], beta = ks[kBeta];
   const double q = 1.0 * p[c] + -omega * v[c];
   p[c] = 1.0 * r[c] + beta * q;
 }
@@ -286,14 +293,17 @@ int enqueue_bicg_iteration(pgb_gmg *g, int precond, cudaStream_t s) {
   if ((rc = kprecondition(g, precond, v[kP], v[kU], s))) return rc;
   kapply(g, v[kU], v[kV], s);
   kdot(g, v[kRhat0], v[kV], kRhat0v, s);
+  k_alpha<<<1, 1, 0, s>>>(g->ks);
   k_hs<<<nb, 256, 0, s>>>(v[kX], v[kU], v[kR], v[kV], v[kH], v[kS], g->ks, n);
   if ((rc = kprecondition(g, precond, v[kS], v[kU], s))) return rc;
   kapply(g, v[kU], v[kT], s);
   kdot(g, v[kT], v[kS], kTs, s);
   kdot(g, v[kT], v[kT], kTt, s);
+  k_omega<<<1, 1, 0, s>>>(g->ks);
   k_xr<<<nb, 256, 0, s>>>(v[kH], v[kU], v[kS], v[kT], v[kX], v[kR], g->ks, n);
   kdot(g, v[kR], v[kR], kRes, s);
   kdot(g, v[kRhat0], v[kR], kRhat0r, s);
+  k_beta<<<1, 1, 0, s>>>(g->ks);
   k_pupdate<<<nb, 256, 0, s>>>(v[kP], v[kV], v[kR], g->ks, n);
   PGB_CUDA(cudaMemcpyAsync(g->kres_h, g->ks + kRes, sizeof(double), cudaMemcpyDeviceToHost, s));
   PGB_CUDA(cudaGetLastError());
@@ -418,8 +428,8 @@ int pgb_gmg_solve(pgb_gmg *g, double *u, const double *rhs, int32_t mixed, doubl
   g->d[0].rhs = const_cast<double *>(rhs);
   const int64_t ncell = g->d[0].cells();
   // initial residual b - A x and its norm
-  if (g->exact) gmg_exact::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, s);
-  else gmg_fast::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, s);
+  if (g->exact) gmg_exact::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, g->d[0].res, nullptr, s);
+  else gmg_fast::residual_sumsq_d(g->d[0], g->cfg, g->partial, g->nparts, nullptr, mixed ? g->f[0].rhs : nullptr, s);
   PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
   PGB_CUDA(cudaStreamSynchronize(s));
   const double r0 = host_rms(g, ncell);

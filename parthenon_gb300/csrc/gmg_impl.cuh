@@ -57,7 +57,8 @@ __device__ __forceinline__ T ax_cell(const T *u, int k, int j, int i, const Leve
   return out;
 #else
   (void)dx;
-  return ((uim + uip) + (ujm + ujp) + (ukm + ukp) - (T)6 * uc) * (T)g.idx2 - alpha * uc;
+  const T lap = ((uim + uip) + (ujm + ujp) + (ukm + ukp) - (T)6 * uc) * (T)g.idx2;
+  return alpha == (T)0 ? lap : lap - alpha * uc;  // uniform branch: Poisson has alpha = 0
 #endif
 }
 
@@ -275,6 +276,33 @@ template <class T>
 __global__ void __launch_bounds__(256) k_copy_arr(const T *__restrict__ a, T *__restrict__ out, int64_t n) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n) out[c] = a[c];
+}
+
+// res <- rhs - A u fused with per-CTA partial sums of res^2 (FP64, fixed order within a
+// CTA; the host adds the CTA partials in index order). res and rhs32 (an FP32 copy of
+// the residual: the next right-hand side of the mixed-precision V-cycle) are optional.
+template <class T>
+__global__ void __launch_bounds__(256) k_residual_sumsq(const T *__restrict__ u, const T *__restrict__ rhs,
+                                                        T *__restrict__ res, float *__restrict__ rhs32, LevelGeom g,
+                                                        T D, T alpha, double *__restrict__ partial) {
+  __shared__ double sm[256];
+  double acc = 0.0;
+  const int64_t n = (int64_t)g.n * g.n * g.n;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    int k, j, i;
+    cell_of(c, g, k, j, i);
+    const T r = (T)1 * rhs[c] + (T)-1 * ax_cell(u, k, j, i, g, D, alpha);
+    if (res) res[c] = r;
+    if (rhs32) rhs32[c] = (float)r;
+    acc += (double)r * (double)r;
+  }
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sm[threadIdx.x] += sm[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sm[0];
 }
 
 // Per-CTA partial sums of a^2 (FP64 accumulation); a second pass sums them in order.
@@ -539,7 +567,9 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
       break;
     }
     if (l > 0) k_fas_rhs<T><<<nblk(n), 256, 0, s>>>(g.u, g.res, g.rhs, g.u0, lg, D, alpha);
-    else k_copy_arr<T><<<nblk(n), 256, 0, s>>>(g.u, g.u0, n);
+#ifdef PGB_GMG_EXACT
+    else k_copy_arr<T><<<nblk(n), 256, 0, s>>>(g.u, g.u0, n);  // the reference copies; the finest u0 is unused
+#endif
     smooth<T>(g, c, s);
     if (!coarsest) {
       k_residual<T><<<nblk(n), 256, 0, s>>>(g.u, g.rhs, g.res, lg, D, alpha);
@@ -559,12 +589,12 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
   }
 }
 
-// res = rhs - A u on a level; partial sums of res^2 into `partial` (nparts entries).
+// res = rhs - A u on a level (res written when `res` is not null; an FP32 copy when
+// `rhs32` is not null); partial sums of res^2 into `partial` (nparts entries).
 template <class T>
-void residual_sumsq(GmgLevelBuf<T> &L, const GmgConfig &c, double *partial, int nparts, cudaStream_t s) {
-  const int64_t n = L.cells();
-  k_residual<T><<<nblk(n), 256, 0, s>>>(L.u, L.rhs, L.res, geom_with(L, c), (T)c.D, (T)c.alpha);
-  k_sumsq_partial<T><<<nparts, 256, 0, s>>>(L.res, n, partial);
+void residual_sumsq(GmgLevelBuf<T> &L, const GmgConfig &c, double *partial, int nparts, T *res, float *rhs32,
+                    cudaStream_t s) {
+  k_residual_sumsq<T><<<nparts, 256, 0, s>>>(L.u, L.rhs, res, rhs32, geom_with(L, c), (T)c.D, (T)c.alpha, partial);
 }
 
 template <class T>
@@ -586,7 +616,7 @@ __global__ void k_add_correction(double *__restrict__ x, const T *__restrict__ e
 
 inline void launch_mixed_prepare(const double *r64, GmgLevelBuf<float> &L0, cudaStream_t s) {
   const int64_t n = L0.cells();
-  k_convert<double, float><<<nblk(n), 256, 0, s>>>(r64, L0.rhs, n);
+  if (r64) k_convert<double, float><<<nblk(n), 256, 0, s>>>(r64, L0.rhs, n);
   cudaMemsetAsync(L0.u, 0, n * sizeof(float), s);
 }
 inline void launch_mixed_update(double *x, const GmgLevelBuf<float> &L0, cudaStream_t s) {
