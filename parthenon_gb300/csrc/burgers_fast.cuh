@@ -3,12 +3,13 @@
 // A CTA owns 32 lines of cells along direction D (fixed transverse indices) and all NC
 // components: warp v marches component v, lane l marches line l. The warp of the
 // normal velocity component (v == D) goes first: it reconstructs the normal velocity
-// and turns every face into the four HLL coefficients shared by all components
-//   a = sr*upl, b = sl*upr, c = sl*sr, is = 1/(sr - sl + [sl*sr == 0])
-// (burgers_package.hpp:32-43, burgers_package.cpp:328-333), kept in shared memory; the
-// other warps then march their component, form F = (a L - b R + c (R - L)) * is (times
-// 1/2 for velocities) and emit flux differences. Per face the wave speeds and their
-// reciprocal are therefore computed once, not once per component.
+// and turns every face into the three HLL coefficients shared by all components
+//   A = sr (upl - sl), B = sl (sr - upr), is = 1/(sr - sl + [sl*sr == 0])
+// (the reference's sr upl L - sl upr R + sl sr (R - L) regrouped as A L + B R;
+// burgers_package.hpp:32-43, burgers_package.cpp:328-333), kept in shared memory; the
+// other warps then march their component, form F = (A L + B R) * is (times 1/2 for
+// velocities) and emit flux differences. Per face the wave speeds and their reciprocal
+// are therefore computed once, not once per component.
 //
 // Along a line consecutive cells share most of the WENO5-Z stencil: the second
 // differences q[j-1] - 2 q[j] + q[j+1] of the smoothness indicators and two of the six
@@ -37,7 +38,7 @@ __device__ __forceinline__ double min_nonneg(double a, double b) {
 struct WenoLine {
   double q0, q1, q2, q3, q4;  // q[p-2] .. q[p+2]
   double d2a, d2b;            // second differences at p-1 and p
-  double t2a, t2b;            // (13/3) * d2^2 at p-1 and p
+  double t2a, t2b;            // (13/3) * d2^2 + eps at p-1 and p
   double p2l_prev, p1l_prev;  // candidate polynomials of cell p-1 reused at cell p
   double dm;                  // q[p] - q[p-1]
 };
@@ -50,8 +51,9 @@ __device__ __forceinline__ void weno_prime(WenoLine &w) {
   // available, so compute what cell p needs from cell p-1 directly)
   w.d2a = w.q0 - 2.0 * w.q1 + w.q2;  // at p-1
   w.d2b = w.q1 - 2.0 * w.q2 + w.q3;  // at p
-  w.t2a = tt * w.d2a * w.d2a;
-  w.t2b = tt * w.d2b * w.d2b;
+  // the carried terms include the smoothness indicators' epsilon
+  w.t2a = fma(tt * w.d2a, w.d2a, kWenoEps);
+  w.t2b = fma(tt * w.d2b, w.d2b, kWenoEps);
   // cell p-1 has window q[p-3..p+1]; its P2L uses q[p-1], q[p], q[p+1] and its P1L uses
   // q[p-2], q[p-1], q[p]
   w.p2l_prev = c20 * w.q1 + c21 * w.q2 + c22 * w.q3;
@@ -70,31 +72,34 @@ __device__ __forceinline__ void weno_step(WenoLine &w, double &ql, double &qr) {
   const double q0 = w.q0, q1 = w.q1, q2 = w.q2, q3 = w.q3, q4 = w.q4;
   // smoothness indicators (second differences carried along the line)
   const double d2c = q2 - 2.0 * q3 + q4;  // at p+1
-  const double t2c = tt * d2c * d2c;
+  const double t2c = fma(tt * d2c, d2c, eps);
   const double b0 = q0 - 4.0 * q1 + 3.0 * q2;
   const double b1 = q3 - q1;
   const double b2 = q4 - 4.0 * q3 + 3.0 * q2;
-  const double be0 = fma(b0, b0, w.t2a) + eps;
-  const double be1 = fma(b1, b1, w.t2b) + eps;
-  const double be2 = fma(b2, b2, t2c) + eps;
+  const double be0 = fma(b0, b0, w.t2a);
+  const double be1 = fma(b1, b1, w.t2b);
+  const double be2 = fma(b2, b2, t2c);
   const double tau5 = fabs(be2 - be0);
   // 1 + tau / be_i with one shared reciprocal
   const double p01 = be0 * be1;
-  const double rb = recip1(p01 * be2);
-  const double B0 = fma(tau5, (be1 * be2) * rb, 1.0);
-  const double B1 = fma(tau5, (be0 * be2) * rb, 1.0);
-  const double B2 = fma(tau5, p01 * rb, 1.0);
+  const double tr = tau5 * recip1(p01 * be2);
+  const double B0 = fma(tr, be1 * be2, 1.0);
+  const double B1 = fma(tr, be0 * be2, 1.0);
+  const double B2 = fma(tr, p01, 1.0);
   const double l0 = fma(g0, B0, eps), l1 = fma(g1, B1, eps), l2 = fma(g2, B2, eps);
   const double r0 = fma(g0, B2, eps), r2 = fma(g2, B0, eps);  // r1 == l1
   const double SL = l0 + l1 + l2, SR = r0 + l1 + r2;
-  const double l01 = l0 * l1, r01 = r0 * l1;
-  const double DL = fma(g2, l01, fma(g1, l0 * l2, g0 * (l1 * l2)));
-  const double DR = fma(g2, r01, fma(g1, r0 * r2, g0 * (l1 * r2)));
+  // D = g2 a0 a1 + g1 a0 a2 + g0 a1 a2 formed as a0 (g2 a1 + g1 a2) + g0 (a1 a2), with
+  // the linear weights divided by 3 so that 1/D below is already 3/D
+  constexpr double h0 = g0 / 3.0, h1 = g1 / 3.0, h2 = g2 / 3.0;
+  const double l12 = l1 * l2, r12 = l1 * r2;
+  const double DL = fma(l0, fma(h2, l1, h1 * l2), h0 * l12);
+  const double DR = fma(r0, fma(h2, l1, h1 * r2), h0 * r12);
   const double SS = SL * SR, DD = DL * DR;
   const double rr = recip(SS * DD);  // normalisations: full precision
   const double DDr = DD * rr, SSr = SS * rr;
-  const double wsL = SR * DDr, wsR = SL * DDr;
-  const double iDL = DR * SSr, iDR = DL * SSr;
+  const double wsL = SR * DDr, wsR = SL * DDr;  // 1/SL, 1/SR
+  const double iDL = DR * SSr, iDR = DL * SSr;  // 3/D_L, 3/D_R
   // candidate polynomials; P1R(p) = P2L(p-1) and P2R(p) = P1L(p-1)
   const double p0l = c00 * q0 + c01 * q1 + c02 * q2;
   const double p1l = c10 * q1 + c11 * q2 + c12 * q3;
@@ -102,8 +107,8 @@ __device__ __forceinline__ void weno_step(WenoLine &w, double &ql, double &qr) {
   const double p0r = c00 * q4 + c01 * q3 + c02 * q2;
   const double xl = (l0 * p0l + l1 * p1l + l2 * p2l) * wsL;
   const double xr = (r0 * p0r + l1 * w.p2l_prev + r2 * w.p1l_prev) * wsR;
-  const double al = fma(3.0 * wsL * l01 * l2, iDL, eps);
-  const double ar = fma(3.0 * wsR * r01 * r2, iDR, eps);
+  const double al = fma(wsL * l0 * l12, iDL, eps);
+  const double ar = fma(wsR * r0 * r12, iDR, eps);
   // MC slope: dq = 0.5 mc(dm, dp) = sign(s) min(|s|/4, min(|dm|, |dp|)) when dm dp > 0
   const double dm = w.dm, dp = q3 - q2;
   const long long sdm = __double_as_longlong(dm), sdp = __double_as_longlong(dp);
@@ -150,7 +155,7 @@ __device__ __forceinline__ void bar_arrive(int id, int count) {
 // overlaps the flux work of the previous group.
 template <int NC, int D, int MODE>
 __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t ngroups) {
-  extern __shared__ double coef_all[];  // [2][4][n+1][32]
+  extern __shared__ double coef_all[];  // [2][3][n+1][32]
   const Dims d = a.d;
   const int ng = d.ng;
   const int n = D == 0 ? d.nx[0] : (D == 1 ? d.nx[1] : d.nx[2]);
@@ -166,14 +171,13 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
   const int64_t step = D == 0 ? 1 : (D == 1 ? N0 : N01);
   const int nf = n + 1;
   const int nthreads = 32 * NC;
-  const double half = comp < 3 ? 0.5 : 1.0;
   const double bdt = a.beta * a.dt[0];
 
   int it = 0;
   for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x, ++it) {
     const int buf = it & 1;
-    double *ca = coef_all + (size_t)buf * 4 * nf * 32;
-    double *cb = ca + nf * 32, *cc = ca + 2 * nf * 32, *ci = ca + 3 * nf * 32;
+    double *ca = coef_all + (size_t)buf * 3 * nf * 32;
+    double *cb = ca + nf * 32, *ci = ca + 2 * nf * 32;
     const int64_t line = grp * 32 + lane;
     const bool live = line < nlines;
     const int64_t ln = live ? line : 0;
@@ -222,14 +226,15 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           const double sr = fmax(fmax(upl, upr), 0.0);
           const double flag = (sl * sr == 0.0) ? 1.0 : 0.0;
           const double is = recip(sr - sl + flag);
-          const double ka = sr * upl, kb = sl * upr, kc = sl * sr;
-          ca[fi] = ka;
-          cb[fi] = kb;
-          cc[fi] = kc;
+          const double A = sr * (upl - sl), B = sl * (sr - upr);
+          ca[fi] = A;
+          cb[fi] = B;
           ci[fi] = is;
-          F = (ka * upl - kb * upr + kc * (upr - upl)) * (0.5 * is);
+          F = fma(A, upl, B * upr) * (0.5 * is);
+        } else if (comp < 3) {
+          F = fma(ca[fi], lprev, cb[fi] * qr) * (0.5 * ci[fi]);
         } else {
-          F = (ca[fi] * lprev - cb[fi] * qr + cc[fi] * (qr - lprev)) * (half * ci[fi]);
+          F = fma(ca[fi], lprev, cb[fi] * qr) * ci[fi];
         }
         if (MODE == kStoreFlux) {
           // face p of direction D at the index of the cell on its right (multilevel path)
@@ -285,7 +290,7 @@ int launch_burgers_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
     const int64_t ns = D == 2 ? d.nx[1] : d.nx[2];
     const int64_t lines = (int64_t)a.nblocks * nf * ns;
     const int64_t groups = (lines + 31) / 32;
-    const size_t smem = 2 * 4 * (size_t)(n + 1) * 32 * sizeof(double);
+    const size_t smem = 2 * 3 * (size_t)(n + 1) * 32 * sizeof(double);
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int64_t grid = std::min<int64_t>(groups, (int64_t)nsm * 2);
     kern<<<(unsigned)grid, 32 * NC, smem, s>>>(a, groups);
