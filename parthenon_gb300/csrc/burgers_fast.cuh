@@ -117,9 +117,10 @@ __device__ __forceinline__ void weno_step(WenoLine &w, double &ql, double &qr) {
   const double mag = min_nonneg(0.25 * fabs(s), min_nonneg(fabs(dm), fabs(dp)));
   const double dq = same ? copysign(mag, s) : 0.0;
   const double alin = 2.0 * al * ar * recip1(al + ar);
-  const double om = 1.0 - alin;
-  ql = fma(alin, xl, om * (q2 + dq));
-  qr = fma(alin, xr, om * (q2 - dq));
+  // alin x + (1 - alin) y written as y + alin (x - y)
+  const double yl = q2 + dq, yr = q2 - dq;
+  ql = fma(alin, xl - yl, yl);
+  qr = fma(alin, xr - yr, yr);
   // carry to cell p+1
   w.d2a = w.d2b;
   w.d2b = d2c;
