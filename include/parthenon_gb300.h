@@ -213,6 +213,17 @@ int pgb_gmg_solve(pgb_gmg *gmg, double *u, const double *rhs, int32_t mixed, dou
  * (src/solvers/bicgstab_solver.hpp:116-315) with MGSolver as its preconditioner. */
 int pgb_gmg_bicgstab(pgb_gmg *gmg, double *u, const double *rhs, int32_t precondition, double rtol,
                      int32_t relative, int32_t max_iters, int32_t *iters_out, double *rms_out, void *stream);
+/* The same solves on fields in the meshblock layout of pgb_exchange ([block][comp][k]
+ * [j][i] with ghosts): component comp_rhs of rhs is the right-hand side, component
+ * comp_u of u the initial guess (V-cycle methods) and the result (interior cells; run
+ * an exchange for its ghosts). The mesh must be uniform, uploaded, with n cells per
+ * direction and the solver's extent. method 0: FP64 V-cycles, 1: mixed V-cycles (rtol
+ * relative to the initial residual); 2: BiCGSTAB + FP64 V-cycle, 3: BiCGSTAB + FP32
+ * V-cycle (rtol relative to rms(rhs)). As MGSolver / BiCGSTABSolver on MeshData
+ * (src/solvers/mg_solver.hpp:119-161, src/solvers/bicgstab_solver.hpp:116-315). */
+int pgb_gmg_solve_blocks(pgb_gmg *gmg, pgb_mesh *mesh, double *u, const double *rhs, int32_t ncomp, int32_t comp_u,
+                         int32_t comp_rhs, int32_t method, double rtol, int32_t max_iters, int32_t *iters_out,
+                         double *relres_out, void *stream);
 
 /* ---- history reductions ----------------------------------------------------------- */
 

@@ -66,6 +66,8 @@ _SIGNATURES = {
                       DP, VP],
     "pgb_gmg_bicgstab": [VP, VP, VP, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
                          ctypes.POINTER(ctypes.c_int32), DP, VP],
+    "pgb_gmg_solve_blocks": [VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                             ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), DP, VP],
     "pgb_history_mass": [VP, VP, ctypes.c_int32, VP, ctypes.c_int32, ctypes.c_double, VP, VP],
     "pgb_amr_block_criterion": [VP, VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, VP, VP],
     "pgb_amr_set_refinement": [VP, VP, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,

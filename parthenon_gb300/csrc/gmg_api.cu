@@ -51,9 +51,10 @@ struct pgb_gmg {
   // cached graphs: [0] fp64 iteration, [1] mixed iteration; keyed by caller pointers
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   const void *graph_key[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
-  // BiCGSTAB state (allocated on first use): vectors x r rhat0 p v h s t u prhs, device
+  // BiCGSTAB state (allocated on first use): vectors x r rhat0 p v h s t u prhs and the
+  // gathered solution / right-hand side of the block-layout solve, device
   // scalars, dot-product partials, pinned copy of (r, r); one graph per preconditioner
-  double *kv[10] = {};
+  double *kv[12] = {};
   double *ks = nullptr;     // rhat0r, rhat0r_old, rhat0v, ts, tt, res, rhs2
   double *kpart = nullptr;  // dot partials
   double *kres_h = nullptr; // pinned host: res, rhs2
@@ -155,7 +156,7 @@ int run_iteration(pgb_gmg *g, int which, cudaStream_t s, int use_graph) {
 // V-cycle from zero as the preconditioner (AddLinearOperatorTasks). Scalars stay on the
 // device so one iteration is one graph launch; only (r, r) comes back to the host.
 enum KScalar { kRhat0r = 0, kRhat0rOld, kRhat0v, kTs, kTt, kRes, kRhs2, kAlpha, kOmega, kBeta, kNumScalars };
-enum KVec { kX = 0, kR, kRhat0, kP, kV, kH, kS, kT, kU, kPrhs };
+enum KVec { kX = 0, kR, kRhat0, kP, kV, kH, kS, kT, kU, kPrhs, kGlobalU, kGlobalRhs };
 constexpr int kDotParts = 512;
 
 __global__ void __launch_bounds__(256) k_dot_partial(const double *__restrict__ a, const double *__restrict__ b,
@@ -448,3 +449,89 @@ int pgb_gmg_solve(pgb_gmg *g, double *u, const double *rhs, int32_t mixed, doubl
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Block-layout entry point: the multigrid solve on fields stored per meshblock
+// ([block][component][k][j][i] with ghosts, the layout of pgb_exchange), as MGSolver
+// works on MeshData. The interiors are gathered into the solver's periodic arrays and
+// the solution is scattered back (uniform meshes whose cell count matches the solver).
+#include "mesh_state.hpp"
+
+namespace pgb {
+GridTables *mesh_leaf_tables(pgb_mesh *m);
+MeshState *mesh_state(pgb_mesh *m);
+}  // namespace pgb
+
+namespace {
+
+// gather = 1: global[cell] <- field interior; gather = 0: field interior <- global[cell]
+__global__ void k_block_global(double *__restrict__ field, double *__restrict__ global, const int *__restrict__ off,
+                               Dims d, int ncomp, int comp, int nblocks, int n, int gather) {
+  const int64_t per = (int64_t)d.nx[0] * d.nx[1] * d.nx[2];
+  const int64_t total = per * nblocks;
+  const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1], cs = N01 * d.N[2];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e / per);
+    const int64_t c = e - (int64_t)b * per;
+    const int i = (int)(c % d.nx[0]), j = (int)((c / d.nx[0]) % d.nx[1]), k = (int)(c / ((int64_t)d.nx[0] * d.nx[1]));
+    const int64_t fe = ((int64_t)b * ncomp + comp) * cs + (int64_t)(k + d.ng) * N01 + (int64_t)(j + d.ng) * N0 +
+                       (i + d.ng);
+    const int64_t ge = ((int64_t)(off[3 * b + 2] + k) * n + (off[3 * b + 1] + j)) * n + (off[3 * b] + i);
+    if (gather) global[ge] = field[fe];
+    else field[fe] = global[ge];
+  }
+}
+
+}  // namespace
+
+extern "C" int pgb_gmg_solve_blocks(pgb_gmg *g, pgb_mesh *mesh, double *u, const double *rhs, int32_t ncomp,
+                                    int32_t comp_u, int32_t comp_rhs, int32_t method, double rtol, int32_t max_iters,
+                                    int32_t *iters_out, double *relres_out, void *stream) {
+  if (!g || !mesh || !u || !rhs) return fail(kErrInvalid, "null argument");
+  GridTables *t = mesh_leaf_tables(mesh);
+  if (!t) return fail(kErrState, "mesh tables not uploaded (call pgb_mesh_upload)");
+  if (t->multilevel) return fail(kErrUnsupported, "the block-layout solve needs a uniform mesh");
+  if (comp_u < 0 || comp_u >= ncomp || comp_rhs < 0 || comp_rhs >= ncomp) return fail(kErrInvalid, "bad component");
+  if (method < 0 || method > 3) return fail(kErrInvalid, "method must be 0..3");
+  const MeshTopology &topo = *mesh_state(mesh)->topo;
+  const MeshSpec &sp = topo.spec();
+  const GmgLevelBuf<double> &L0 = g->d[0];
+  for (int q = 0; q < 3; ++q) {
+    if (sp.nx[q] != g->n) return fail(kErrInvalid, "mesh cells per direction differ from the solver's n");
+    if (sp.xmin[q] != L0.xmin || sp.xmax[q] != L0.xmin + L0.n * L0.dx)
+      return fail(kErrInvalid, "mesh extent differs from the solver's [xmin, xmax]");
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t n3 = L0.cells();
+  if (!g->kv[kU]) {
+    int rc = krylov_alloc(g);
+    if (rc) return rc;
+  }
+  double *gu = g->kv[kGlobalU], *grhs = g->kv[kGlobalRhs];
+  std::vector<int> off;
+  for (auto &b : topo.leaf().blocks)
+    for (int q = 0; q < 3; ++q) off.push_back((int)(b.loc.lx[q] * sp.bnx[q]));
+  int *doff = nullptr;
+  PGB_CUDA(cudaMallocAsync((void **)&doff, off.size() * sizeof(int), s));
+  PGB_CUDA(cudaMemcpyAsync(doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  const int nb = t->nblocks;
+  const unsigned grid = (unsigned)std::min<int64_t>((n3 + 255) / 256, 4096);
+  k_block_global<<<grid, 256, 0, s>>>(const_cast<double *>(rhs), grhs, doff, t->dims, ncomp, comp_rhs, nb, g->n, 1);
+  k_block_global<<<grid, 256, 0, s>>>(u, gu, doff, t->dims, ncomp, comp_u, nb, g->n, 1);
+  PGB_CUDA(cudaGetLastError());
+  int rc, it = 0;
+  double res = 0.0;
+  if (method <= 1) rc = pgb_gmg_solve(g, gu, grhs, method, rtol, max_iters, &it, &res, stream);
+  else rc = pgb_gmg_bicgstab(g, gu, grhs, method - 1, rtol, 1, max_iters, &it, &res, stream);
+  if (!rc) {
+    k_block_global<<<grid, 256, 0, s>>>(u, gu, doff, t->dims, ncomp, comp_u, nb, g->n, 0);
+    const cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) rc = check_cuda(le, "scatter");
+  }
+  cudaFreeAsync(doff, s);
+  if (rc) return rc;
+  PGB_CUDA(cudaStreamSynchronize(s));
+  if (iters_out) *iters_out = it;
+  if (relres_out) *relres_out = res;
+  return kOk;
+}

@@ -52,6 +52,27 @@ class GmgSolver:
         torch.cuda.current_stream().wait_stream(stream)
         return it.value, rms.value
 
+    METHODS = {"fp64": 0, "mixed": 1, "bicgstab-fp64": 2, "bicgstab-fp32": 3}
+
+    def solve_blocks(self, mesh, u, rhs, comp_u=0, comp_rhs=0, method="fp64", rtol=1e-10, max_iters=200,
+                     stream=None):
+        """Solve on meshblock fields (Mesh.new_field layout): the right-hand side is
+        component comp_rhs of rhs, the solution goes to the interior of component comp_u
+        of u. Returns (iterations, relative residual)."""
+        import torch
+        if stream is None:
+            stream = self._stream = getattr(self, "_stream", None) or torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        mesh._ensure()
+        it = ctypes.c_int32(0)
+        rel = ctypes.c_double(0.0)
+        nat.check(nat.lib().pgb_gmg_solve_blocks(self._h, mesh.handle, _ptr(u), _ptr(rhs), u.shape[1], int(comp_u),
+                                                 int(comp_rhs), self.METHODS[method], float(rtol), int(max_iters),
+                                                 ctypes.byref(it), ctypes.byref(rel), _stream(stream)),
+                  "pgb_gmg_solve_blocks")
+        torch.cuda.current_stream().wait_stream(stream)
+        return it.value, rel.value
+
     def solve(self, u, rhs, mixed=False, rtol=1e-10, max_cycles=200, stream=None):
         cyc = ctypes.c_int32(0)
         rel = ctypes.c_double(0.0)

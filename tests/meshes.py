@@ -37,4 +37,9 @@ INDEX_MAP_CASES = [
     ("C3-smr-128", (128, 128, 128), (16, 16, 16), 4, refined_cube(3, 2, 6)),
     ("smr-corner", (64, 64, 64), (8, 8, 8), 2, refined_cube(3, 0, 2)),
     ("three-level", (64, 64, 64), (8, 8, 8), 4, two_level_nested(3, 2, 6, 6, 10)),
+    # smallest meshes: one block that is its own neighbour in all 26 directions, and
+    # 2x2x2 blocks that meet every neighbour across two periodic images
+    ("single-block", (16, 16, 16), (16, 16, 16), 2, None),
+    ("two-per-dim", (32, 32, 32), (16, 16, 16), 4, None),
+    ("two-per-dim-refined", (16, 16, 16), (8, 8, 8), 2, refined_cube(1, 0, 1)),
 ]

@@ -64,6 +64,8 @@ CASES = {
     "burgers-5comp": ((32,) * 3, (16,) * 3, 4, None, "burgers", "weno5", 5, 0.8, _burgers5),
     "smr-advection-plm": ((32,) * 3, (8,) * 3, 4, refined_cube(2, 1, 3), "advection", "plm", 5, 0.3,
                           _advection_smr),
+    # one block that is its own neighbour in every direction
+    "single-block-burgers": ((16,) * 3, (16,) * 3, 4, None, "burgers", "weno5", 5, 0.8, _burgers5),
     # multilevel Burgers: stored face fluxes, flux correction, divergence update
     "smr-burgers-weno5": ((32,) * 3, (8,) * 3, 4, refined_cube(2, 1, 3), "burgers", "weno5", 5, 0.8, _burgers5),
     "smr-burgers-11": ((32,) * 3, (8,) * 3, 4, refined_cube(2, 0, 2), "burgers", "weno5", 11, 0.8, _burgers),
