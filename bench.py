@@ -265,6 +265,7 @@ def run_ours(args, ws, rank):
         "e2e": e2e,
         "gpu_launches": 10 * args.steps,
         "clocks": clk.summary(),
+        "autotune": {k: {"choice": c, "ms": ms} for k, (c, ms) in nat.tune_report().items()},
     }
     out["gmg"] = gmg_bench(torch)
     if rank == 0 and ws == 1:

@@ -225,6 +225,17 @@ int pgb_gmg_solve_blocks(pgb_gmg *gmg, pgb_mesh *mesh, double *u, const double *
                          int32_t comp_rhs, int32_t method, double rtol, int32_t max_iters, int32_t *iters_out,
                          double *relres_out, void *stream);
 
+/* ---- launch-shape autotuner ------------------------------------------------------ */
+
+/* The first pgb_rk2_cycles call on a mesh (before it captures the cycle graph) times a
+ * few launch shapes of the hot kernels on the caller's data -- threads per CTA of the
+ * ghost copy, persistent CTAs per SM of the WENO5/HLL sweep -- and keeps the fastest
+ * per kernel and problem size for the process; PGB_TUNE=0 in the environment keeps the
+ * defaults. Writes "key=choice (ms per candidate) ; ..." (NUL-terminated, truncated to
+ * capacity). No counterpart in the reference (its launch shapes are fixed by Kokkos
+ * policies). */
+int pgb_tune_report(char *buf, int32_t capacity);
+
 /* ---- history reductions ----------------------------------------------------------- */
 
 /* out[r] (host) = sum over blocks, components and interior cells whose centre lies in

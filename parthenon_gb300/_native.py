@@ -69,6 +69,7 @@ _SIGNATURES = {
     "pgb_gmg_solve_blocks": [VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                              ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), DP, VP],
     "pgb_history_mass": [VP, VP, ctypes.c_int32, VP, ctypes.c_int32, ctypes.c_double, VP, VP],
+    "pgb_tune_report": [ctypes.c_char_p, ctypes.c_int32],
     "pgb_amr_block_criterion": [VP, VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, VP, VP],
     "pgb_amr_set_refinement": [VP, VP, ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
                                ctypes.c_int32, VP],
@@ -112,3 +113,17 @@ def check(rc, what=""):
 
 def exported_symbols():
     return sorted(list(_SIGNATURES) + ["pgb_last_error"])
+
+
+def tune_report():
+    """Launch shapes chosen by the autotuner so far: {key: (choice, [ms per candidate])}."""
+    buf = ctypes.create_string_buffer(8192)
+    check(lib().pgb_tune_report(buf, len(buf)), "pgb_tune_report")
+    out = {}
+    for item in buf.value.decode().split(" ; "):
+        if "=" not in item:
+            continue
+        key, rest = item.rsplit("=", 1)
+        choice, ms = rest.split(" (", 1)
+        out[key] = (int(choice), [float(x) for x in ms.rstrip(" ms)").split()])
+    return out

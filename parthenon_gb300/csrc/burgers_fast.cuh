@@ -17,6 +17,8 @@
 // only the new ones. The FP64 pipe bounds this kernel; every saved instruction counts.
 #pragma once
 
+#include "tune.hpp"
+
 namespace pgb {
 namespace fast {
 
@@ -293,7 +295,9 @@ int launch_burgers_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
     const int64_t groups = (lines + 31) / 32;
     const size_t smem = 2 * 3 * (size_t)(n + 1) * 32 * sizeof(double);
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const int64_t grid = std::min<int64_t>(groups, (int64_t)nsm * 2);
+    const int pick = g_tune_force >= 0 ? g_tune_force
+                                       : tuned_choice(burgers_tune_key(NC, n, store_flux, a.nblocks), kBurgersGridDefault);
+    const int64_t grid = std::min<int64_t>(groups, (int64_t)nsm * kBurgersGridMult[pick]);
     kern<<<(unsigned)grid, 32 * NC, smem, s>>>(a, groups);
   };
   if (store_flux) {

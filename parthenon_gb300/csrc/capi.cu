@@ -3,6 +3,7 @@
 // inside a cycle, optional CUDA-graph replay).
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <map>
 #include <string>
@@ -12,6 +13,7 @@
 #include "common.cuh"
 #include "mesh_state.hpp"
 #include "stencil.cuh"
+#include "tune.hpp"
 
 namespace pgb {
 
@@ -147,6 +149,38 @@ int cycle_impl(pgb_mesh *m, const pgb_stage_params *p, double *base, double *sta
   if ((rc = stage_impl(m, p, stage, base, base, dudt, flux, dt, 0.5, 0.5, 0.5, ncomp, s))) return rc;
   if ((rc = exchange_leaf(m, base, cbase, ncomp, xflags, nullptr, s))) return rc;
   return estimate_dt(m->st, p->physics, base, ncomp, p->vel, p->cfl, dt, 0, s);
+}
+
+// Times the candidate launch shapes of this mesh's hot kernels on the caller's data
+// (tune.hpp). Only idempotent work runs: ghost exchanges of `base` (the same ghost
+// values each time) and the first RK stage base -> stage (reads base, overwrites stage,
+// dudt and flux, all of which the cycle rewrites before use).
+int autotune(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage, double *dudt, double *flux,
+             double *cbase, int ncomp, double *dt, cudaStream_t s) {
+  if (!tuning_enabled()) return kOk;
+  GridTables &t = m->st.leaf;
+  const int xflags = p->physics == 1 ? 0 : PGB_EXCHANGE_PROLONGATE;
+  int rc = kOk;
+  auto guarded = [&](int c, const std::function<int()> &f) {
+    g_tune_force = c;
+    const int r = f();
+    g_tune_force = -1;
+    return r;
+  };
+  if (t.ncopy_work) {
+    tune(copy_tune_key(ncomp, t.npairs, t.dims.nx[0]), 3, kCopyThreadsDefault, 3,
+         [&](int c) { return guarded(c, [&] { return exchange_leaf(m, base, cbase, ncomp, xflags, nullptr, s); }); },
+         s);
+  }
+  if (p->physics == 1 && p->recon == 0 && !p->exact && (ncomp == 4 || ncomp == 5 || ncomp == 11)) {
+    tune(burgers_tune_key(ncomp, t.dims.nx[0], t.multilevel, t.nblocks), kBurgersGridCandidates, kBurgersGridDefault, 1,
+         [&](int c) {
+           return guarded(c, [&] { return stage_impl(m, p, base, base, stage, dudt, flux, dt, 1.0, 0.0, 1.0, ncomp, s); });
+         },
+         s);
+  }
+  PGB_CUDA(cudaStreamSynchronize(s));
+  return rc;
 }
 
 }  // namespace
@@ -326,6 +360,8 @@ int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double 
                              (int)(cbase != nullptr));
   auto it = m->graphs.find(key);
   if (it == m->graphs.end()) {
+    // launch shapes are chosen before the cycle is frozen into a graph
+    if ((rc = autotune(m, p, base, stage, dudt, flux, cbase, ncomp, dt, s))) return rc;
     cudaGraph_t g;
     PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s);

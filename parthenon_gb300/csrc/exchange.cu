@@ -20,6 +20,7 @@
 
 #include "common.cuh"
 #include "mesh_state.hpp"
+#include "tune.hpp"
 
 namespace pgb {
 
@@ -254,9 +255,10 @@ __device__ __forceinline__ double *arr(double *fine, double *coarse, int c) { re
 // Per thread the row base addresses are formed once per row; rows whose two ends are
 // 16-byte aligned on both sides (every same-level face and edge of an even-sized block)
 // move as double2, the rest element by element.
-__global__ void __launch_bounds__(128, 8) k_copy(const DevPair *__restrict__ pairs,
-                                              const DevWork *__restrict__ work, Dims d, int ncomp,
-                                              double *__restrict__ fine, double *__restrict__ coarse) {
+template <int TPB>
+__global__ void __launch_bounds__(TPB, 1024 / TPB) k_copy(const DevPair *__restrict__ pairs,
+                                                       const DevWork *__restrict__ work, Dims d, int ncomp,
+                                                       double *__restrict__ fine, double *__restrict__ coarse) {
   const DevWork w = work[blockIdx.x];
   const DevPair p = pairs[w.item];
   const int v = blockIdx.y;
@@ -519,7 +521,16 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
       k_pack<<<dim3(t.ncopy_work, ncomp), blk, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse, buffer);
       k_unpack<<<dim3(t.ncopy_work, ncomp), blk, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse, buffer);
     } else {
-      k_copy<<<dim3(t.ncopy_work, ncomp), blk, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse);
+      // threads per CTA: the tuner's choice for this shape (tune.hpp)
+      const int pick = g_tune_force >= 0 ? g_tune_force
+                                         : tuned_choice(copy_tune_key(ncomp, t.npairs, t.dims.nx[0]),
+                                                        kCopyThreadsDefault);
+      const dim3 grid(t.ncopy_work, ncomp);
+      switch (kCopyThreads[pick]) {
+        case 64: k_copy<64><<<grid, 64, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse); break;
+        case 256: k_copy<256><<<grid, 256, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse); break;
+        default: k_copy<128><<<grid, 128, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse); break;
+      }
     }
   }
   if (t.multilevel && t.nrr_work)
