@@ -3,9 +3,10 @@
 - Per-block criteria (FirstDerivative, SecondDerivative, |grad q|): bit-exact.
 - Remesh data movement (same-level copy, prolongation into new fine blocks,
   restriction into new coarse blocks) and the ghost fill after it: bit-exact.
-- A whole adaptive Burgers run (initial refinement, RK2 cycles, periodic tagging,
-  remeshes with refinement and derefinement) in the exact build, step-locked with the
-  oracle: identical flags and block lists at every check, bit-exact fields and dt.
+- Whole adaptive runs (initial refinement, RK2 cycles, periodic tagging, remeshes with
+  refinement and derefinement) in the exact build, step-locked with the oracle:
+  Burgers (no prolongation inside stages) and advection (prolongation in every stage
+  exchange, flux correction); identical flags and block lists, bit-exact fields and dt.
 """
 import numpy as np
 import pytest
@@ -110,9 +111,12 @@ def test_remesh_transfer_bit_exact(name, nx, bnx, ng, leaves, mode):
 class _OracleAMR:
     """The adaptive loop of AMRDriver restated on the oracle (same cadence)."""
 
-    def __init__(self, nx, bnx, ng, ncomp, cfl, criterion, numlevel, count, interval):
-        self.o = O.OracleSim(nx, bnx, ng, ncomp=ncomp, physics="burgers", recon=0, cfl=cfl, prolong_in_stage=False)
+    def __init__(self, nx, bnx, ng, ncomp, cfl, criterion, numlevel, count, interval, physics="burgers", recon=0,
+                 pgen=None):
+        self.o = O.OracleSim(nx, bnx, ng, ncomp=ncomp, physics=physics, recon=recon, cfl=cfl,
+                             prolong_in_stage=(physics != "burgers"))
         self.ng, self.bnx, self.ncomp = ng, bnx, ncomp
+        self.pgen = pgen if pgen is not None else (lambda src: _state(src, ng, bnx, ncomp))
         self.crit = criterion
         root = int(self.o.block_info()[0][:, 0].min())
         self.mml = numlevel + root - 1
@@ -137,7 +141,7 @@ class _OracleAMR:
 
     def initialize(self):
         for _ in range(16):
-            self.o.base()[:] = _state(self.o, self.ng, self.bnx, self.ncomp)
+            self.o.base()[:] = self.pgen(self.o)
             self.o.exchange(True, 0)
             before = self.o.nblocks
             self.adapt()
@@ -188,5 +192,40 @@ def test_adaptive_burgers_run_matches_oracle():
     # initial refinement, then derefinement steps during the run
     assert drv.nremesh >= 3
     assert min(drv.block_history[2:]) < max(drv.block_history[1:])
+    assert np.array_equal(drv.base.cpu().numpy(), ref.o.base())
+    assert float(drv.dt.cpu()[0]) == ref.o.dt()
+
+
+def _blob(src, ng, bnx):
+    # advected Gaussian (sigma 0.08) off the domain centre, a function of position only
+    _, geom = src.block_info()
+    bg = pg.problems.BlockGeometry(geom, ng, bnx)
+    xs, ys, zs = bg.cell_centers()
+    r2 = ((zs - 0.3) ** 2)[:, :, None, None] + ((ys - 0.4) ** 2)[:, None, :, None] + ((xs - 0.5) ** 2)[:, None, None, :]
+    out = np.zeros((bg.nblocks, 1) + tuple(bg.N[::-1]))
+    out[:, 0, ng:-ng, ng:-ng, ng:-ng] = np.exp(-r2 / (2 * 0.08 ** 2))[:, ng:-ng, ng:-ng, ng:-ng]
+    return out
+
+
+def test_adaptive_advection_run_matches_oracle():
+    # advection prolongates inside every stage exchange and corrects fluxes at
+    # fine/coarse faces; the mesh follows the moving blob
+    nx, bnx, ng, ncomp, cfl = (32, 32, 32), (8, 8, 8), 2, 1, 0.3
+    crit = pg.RefinementCriterion(comps=(0,), method="gradient", refine_tol=0.4, derefine_tol=0.3, relative=True)
+    numlevel, count, interval, ncycles = 2, 1, 4, 48
+    pgen = lambda src: _blob(src, ng, bnx)  # noqa: E731
+    ref = _OracleAMR(nx, bnx, ng, ncomp, cfl, crit, numlevel, count, interval, physics="advection", recon=1,
+                     pgen=pgen)
+    drv = pg.AMRDriver(pg.Mesh(nx, bnx, ng), ncomp, pg.StageConfig("advection", "plm", cfl, exact=True), crit,
+                       numlevel=numlevel, derefine_count=count, check_interval=interval)
+    drv.initialize(pgen)
+    ref.initialize()
+    drv.run(ncycles)
+    ref.run(ncycles)
+    drv.stream.synchronize()
+    np.testing.assert_array_equal(drv.mesh.block_info()[0], ref.o.block_info()[0])
+    # refinement and derefinement both happen while the blob moves
+    assert drv.nremesh >= 5 and drv.mesh.multilevel
+    assert len(set(drv.block_history)) >= 3
     assert np.array_equal(drv.base.cpu().numpy(), ref.o.base())
     assert float(drv.dt.cpu()[0]) == ref.o.dt()
