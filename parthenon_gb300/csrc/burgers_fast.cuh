@@ -36,13 +36,15 @@ __device__ __forceinline__ double min_nonneg(double a, double b) {
   return __double_as_longlong(a) < __double_as_longlong(b) ? a : b;
 }
 
-// Incremental WENO5-Z state of one line: window q[p-2..p+2] plus carried terms.
+// Incremental WENO5-Z state of one line: window q[p-2..p+2] plus carried terms. The
+// smoothness indicators are formed from the window's first differences
+// e0..e2 = q1-q0, q2-q1, q3-q2 (e3 = q4-q3 is the one new difference per cell):
+//   second difference at p+1 = e3 - e2, b0 = 3 e1 - e0, b1 = e2 + e1, b2 = e3 - 3 e2.
 struct WenoLine {
   double q0, q1, q2, q3, q4;  // q[p-2] .. q[p+2]
-  double d2a, d2b;            // second differences at p-1 and p
+  double e0, e1, e2;          // q1-q0, q2-q1, q3-q2
   double t2a, t2b;            // (13/3) * d2^2 + eps at p-1 and p
   double p2l_prev, p1l_prev;  // candidate polynomials of cell p-1 reused at cell p
-  double dm;                  // q[p] - q[p-1]
 };
 
 __device__ __forceinline__ void weno_prime(WenoLine &w) {
@@ -51,33 +53,33 @@ __device__ __forceinline__ void weno_prime(WenoLine &w) {
   constexpr double c20 = 1.0 / 3.0, c21 = 5.0 / 6.0, c22 = -1.0 / 6.0;
   // quantities of cell p-1 (window shifted by one to the left: q[p-3]..q[p+1] is not
   // available, so compute what cell p needs from cell p-1 directly)
-  w.d2a = w.q0 - 2.0 * w.q1 + w.q2;  // at p-1
-  w.d2b = w.q1 - 2.0 * w.q2 + w.q3;  // at p
+  w.e0 = w.q1 - w.q0;
+  w.e1 = w.q2 - w.q1;
+  w.e2 = w.q3 - w.q2;
+  const double d2a = w.e1 - w.e0;  // at p-1
+  const double d2b = w.e2 - w.e1;  // at p
   // the carried terms include the smoothness indicators' epsilon
-  w.t2a = fma(tt * w.d2a, w.d2a, kWenoEps);
-  w.t2b = fma(tt * w.d2b, w.d2b, kWenoEps);
+  w.t2a = fma(tt * d2a, d2a, kWenoEps);
+  w.t2b = fma(tt * d2b, d2b, kWenoEps);
   // cell p-1 has window q[p-3..p+1]; its P2L uses q[p-1], q[p], q[p+1] and its P1L uses
   // q[p-2], q[p-1], q[p]
   w.p2l_prev = c20 * w.q1 + c21 * w.q2 + c22 * w.q3;
   w.p1l_prev = c10 * w.q0 + c11 * w.q1 + c12 * w.q2;
-  w.dm = w.q2 - w.q1;
 }
 
 // Reconstruct cell p from the window; then the caller shifts in q[p+3].
 __device__ __forceinline__ void weno_step(WenoLine &w, double &ql, double &qr) {
-  constexpr double c00 = 1.0 / 3.0, c01 = -7.0 / 6.0, c02 = 11.0 / 6.0;
-  constexpr double c10 = -1.0 / 6.0, c11 = 5.0 / 6.0, c12 = 1.0 / 3.0;
-  constexpr double c20 = 1.0 / 3.0, c21 = 5.0 / 6.0, c22 = -1.0 / 6.0;
   constexpr double g0 = 0.1, g1 = 0.6, g2 = 0.3;
   constexpr double eps = kWenoEps;
   constexpr double tt = 13.0 / 3.0;
-  const double q0 = w.q0, q1 = w.q1, q2 = w.q2, q3 = w.q3, q4 = w.q4;
-  // smoothness indicators (second differences carried along the line)
-  const double d2c = q2 - 2.0 * q3 + q4;  // at p+1
+  const double q2 = w.q2, q3 = w.q3, q4 = w.q4;
+  // smoothness indicators from first differences (second differences carried)
+  const double e0 = w.e0, e1 = w.e1, e2 = w.e2, e3 = q4 - q3;
+  const double d2c = e3 - e2;  // at p+1
   const double t2c = fma(tt * d2c, d2c, eps);
-  const double b0 = q0 - 4.0 * q1 + 3.0 * q2;
-  const double b1 = q3 - q1;
-  const double b2 = q4 - 4.0 * q3 + 3.0 * q2;
+  const double b0 = fma(3.0, e1, -e0);
+  const double b1 = e2 + e1;
+  const double b2 = fma(-3.0, e2, e3);
   const double be0 = fma(b0, b0, w.t2a);
   const double be1 = fma(b1, b1, w.t2b);
   const double be2 = fma(b2, b2, t2c);
@@ -102,17 +104,18 @@ __device__ __forceinline__ void weno_step(WenoLine &w, double &ql, double &qr) {
   const double DDr = DD * rr, SSr = SS * rr;
   const double wsL = SR * DDr, wsR = SL * DDr;  // 1/SL, 1/SR
   const double iDL = DR * SSr, iDR = DL * SSr;  // 3/D_L, 3/D_R
-  // candidate polynomials; P1R(p) = P2L(p-1) and P2R(p) = P1L(p-1)
-  const double p0l = c00 * q0 + c01 * q1 + c02 * q2;
-  const double p1l = c10 * q1 + c11 * q2 + c12 * q3;
-  const double p2l = c20 * q2 + c21 * q3 + c22 * q4;
-  const double p0r = c00 * q4 + c01 * q3 + c02 * q2;
+  // candidate polynomials about q2 in first differences (two FMAs each; the stencil
+  // weights sum to one); P1R(p) = P2L(p-1) and P2R(p) = P1L(p-1)
+  const double p0l = fma(-1.0 / 3.0, e0, fma(5.0 / 6.0, e1, q2));
+  const double p1l = fma(1.0 / 6.0, e1, fma(1.0 / 3.0, e2, q2));
+  const double p2l = fma(2.0 / 3.0, e2, fma(-1.0 / 6.0, e3, q2));
+  const double p0r = fma(1.0 / 3.0, e3, fma(-5.0 / 6.0, e2, q2));
   const double xl = (l0 * p0l + l1 * p1l + l2 * p2l) * wsL;
   const double xr = (r0 * p0r + l1 * w.p2l_prev + r2 * w.p1l_prev) * wsR;
   const double al = fma(wsL * l0 * l12, iDL, eps);
   const double ar = fma(wsR * r0 * r12, iDR, eps);
   // MC slope: dq = 0.5 mc(dm, dp) = sign(s) min(|s|/4, min(|dm|, |dp|)) when dm dp > 0
-  const double dm = w.dm, dp = q3 - q2;
+  const double dm = e1, dp = e2;
   const long long sdm = __double_as_longlong(dm), sdp = __double_as_longlong(dp);
   const bool same = ((sdm ^ sdp) >= 0) && ((sdm << 1) != 0) && ((sdp << 1) != 0);
   const double s = dm + dp;
@@ -124,13 +127,13 @@ __device__ __forceinline__ void weno_step(WenoLine &w, double &ql, double &qr) {
   ql = fma(alin, xl - yl, yl);
   qr = fma(alin, xr - yr, yr);
   // carry to cell p+1
-  w.d2a = w.d2b;
-  w.d2b = d2c;
+  w.e0 = e1;
+  w.e1 = e2;
+  w.e2 = e3;
   w.t2a = w.t2b;
   w.t2b = t2c;
   w.p2l_prev = p2l;
   w.p1l_prev = p1l;
-  w.dm = dp;
 }
 
 __device__ __forceinline__ void weno_shift(WenoLine &w, double qnew) {
@@ -198,8 +201,9 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     }
     const int64_t c0 = (int64_t)b * NC * cs + (int64_t)k0 * N01 + (int64_t)j0 * N0 + i0;
     const DevBlockGeom &g = a.geom[b];
-    const double area = g.area[D];
-    const double nvol = -1.0 / g.vol;
+    // a face flux difference enters the update as area * (F+ - F-) * (-1/V) * beta dt:
+    // the three factors are folded into one per line
+    const double scale = g.area[D] * (-1.0 / g.vol) * bdt;
 
     if (producer) {
       if (it >= 2) bar_sync(3 + buf, nthreads);  // consumers released this buffer
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     wl.q3 = __ldg(u);
     wl.q4 = __ldg(u + step);
     weno_prime(wl);
-    double lprev = 0.0, afprev = 0.0;
+    double lprev = 0.0, fprev = 0.0;
     for (int p = -1; p <= n; ++p) {
       double ql, qr;
       weno_step(wl, ql, qr);
@@ -245,21 +249,24 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           lprev = ql;
           continue;
         }
-        const double af = area * F;
         if (p >= 1 && live) {
+          // dudt holds the scaled update increments of the directions done so far
           const int64_t e = c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step;
-          double du = af - afprev;
+          const double df = F - fprev;
           if (MODE == kStoreDu) {
-            a.dudt[e] = du;
+            a.dudt[e] = scale * df;
           } else if (MODE == kAddDu) {
-            a.dudt[e] = a.dudt[e] + du;
+            a.dudt[e] = fma(scale, df, a.dudt[e]);
           } else {
-            if (MODE == kFinishUpdate) du = a.dudt[e] + du;
-            const double avg = a.w_in * __ldg(a.u_in + e) + a.w_base * __ldg(a.u_base + e);
-            a.u_out[e] = avg + bdt * (du * nvol);
+            const double du = MODE == kFinishUpdate ? fma(scale, df, a.dudt[e]) : scale * df;
+            // stage 1 of RK2 averages with weights (1, 0): the average is u_in itself
+            const double avg = (a.w_in == 1.0 && a.w_base == 0.0)
+                                   ? __ldg(a.u_in + e)
+                                   : a.w_in * __ldg(a.u_in + e) + a.w_base * __ldg(a.u_base + e);
+            a.u_out[e] = avg + du;
           }
         }
-        afprev = af;
+        fprev = F;
       }
       lprev = ql;
     }
