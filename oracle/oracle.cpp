@@ -70,6 +70,32 @@ struct Field {
     data.assign(bl->size() * bstride(), 0.0);
     coarse.assign(bl->size() * cstride(), 0.0);
   }
+  // zero one variable of one block (fine and coarse arrays)
+  void zero(int b, int v) {
+    const int64_t n = (int64_t)N[0] * N[1] * N[2], nc = (int64_t)Nc[0] * Nc[1] * Nc[2];
+    std::fill(data.begin() + b * bstride() + v * n, data.begin() + b * bstride() + (v + 1) * n, 0.0);
+    std::fill(coarse.begin() + b * cstride() + v * nc, coarse.begin() + b * cstride() + (v + 1) * nc, 0.0);
+  }
+};
+
+// ---------------------------------------------------------------- sparse variables
+// Metadata::Sparse fields (one component each): per block an allocation flag and a
+// deallocation counter (Variable::dealloc_count); per variable the allocation and
+// deallocation thresholds and the default value (metadata.hpp:398-407, defaults
+// globals.hpp:33-35). An unallocated variable holds zeros in every container, which
+// is what a fresh allocation gives (variable.cpp:112-127).
+struct Sparse {
+  bool on = false;
+  int ncomp = 0;
+  int dealloc_count = 5;
+  std::vector<double> alloc_thr, dealloc_thr, default_val;
+  std::vector<uint8_t> alloc;  // [block * ncomp + v]
+  std::vector<int> count;      // [block * ncomp + v]
+  bool allocated(int b, int v) const { return !on || alloc[(size_t)b * ncomp + v] != 0; }
+  void resize(size_t nblocks) {
+    alloc.assign(nblocks * ncomp, 0);
+    count.assign(nblocks * ncomp, 0);
+  }
 };
 
 // ---------------------------------------------------------------- boundary records
@@ -208,37 +234,60 @@ struct ExchangeStats {
 
 // One full same-rank exchange: SendBoundBufs -> ReceiveBoundBufs -> SetBounds
 // [-> ProlongateBounds], with an explicit intermediate buffer per boundary.
+// With sparse variables (sp != null and on): a sender whose variable is unallocated,
+// or whose packed values all lie below the allocation threshold, sends a null buffer
+// (boundary_communication.cpp:95-140); a receiver allocates its variable when any
+// buffer for it carries data (:216-232); SetBounds writes allocated receivers only,
+// from the buffer or, for a null buffer, the default value (:267-330); restriction and
+// prolongation run on allocated variables only.
 inline ExchangeStats exchange(Field &f, std::vector<Block> &bl, BType t, int lev,
                               const std::vector<BndRec> &recs, bool prolongate, int pop,
-                              bool multilevel, bool check_overlaps = false) {
+                              bool multilevel, bool check_overlaps = false, Sparse *sp = nullptr) {
   ExchangeStats st;
   const Mesh &m = *f.mesh;
   const int ng = m.p.ng;
+  if (sp && !sp->on) sp = nullptr;
+  auto alloc_ok = [&](int b, int v) { return !sp || sp->allocated(b, v); };
   // (1) send-side restriction into coarse buffers (ProResInfo::GetSend)
   if (multilevel) {
     for (size_t b = 0; b < bl.size(); ++b) {
       for (auto &nb : *nb_list(bl[b], t, lev)) {
         if (!(nb.origin.level < bl[b].loc.level)) continue;
         Box bx = calc_indices(nb, bl[b].loc, bl[b].nx, ng, CC, BoundaryInteriorSend, true, false);
-        for (int v = 0; v < f.ncomp; ++v)
+        for (int v = 0; v < f.ncomp; ++v) {
+          if (!alloc_ok((int)b, v)) continue;
           for_box(bx, [&](int k, int j, int i) { restrict_cell(f, (int)b, v, k, j, i, bl[b].coords); });
+        }
       }
     }
   }
-  // (2) pack
+  // (2) pack, with the non-zero flag of each (boundary, variable) buffer
   std::vector<std::vector<double>> bufs(recs.size());
   const int nrec = (int)recs.size();
+  std::vector<uint8_t> nonnull((size_t)nrec * f.ncomp, 1);
 #pragma omp parallel for schedule(dynamic, 16)
   for (int r = 0; r < nrec; ++r) {
     const BndRec &br = recs[r];
     auto &buf = bufs[r];
     buf.reserve(br.send.size() * f.ncomp);
-    for (int v = 0; v < f.ncomp; ++v)
+    for (int v = 0; v < f.ncomp; ++v) {
+      const bool on = alloc_ok(br.sender, v);
+      bool nz = false;
       for_box(br.send, [&](int k, int j, int i) {
-        buf.push_back(f.any(br.send_coarse, br.sender, v, k, j, i));
+        const double x = on ? f.any(br.send_coarse, br.sender, v, k, j, i) : 0.0;
+        if (sp) nz = nz || (std::fabs(x) >= sp->alloc_thr[v]);
+        buf.push_back(x);
       });
+      if (sp) nonnull[(size_t)r * f.ncomp + v] = on && nz;
+    }
   }
   for (auto &b : bufs) st.buffered_values += (int64_t)b.size();
+  // (2b) ReceiveBoundBufs: allocate receivers that get data
+  if (sp)
+    for (int r = 0; r < nrec; ++r)
+      for (int v = 0; v < f.ncomp; ++v)
+        if (nonnull[(size_t)r * f.ncomp + v]) sp->alloc[(size_t)recs[r].receiver * f.ncomp + v] = 1;
+  auto value = [&](int r, int v, double x) { return nonnull[(size_t)r * f.ncomp + v] ? x : sp->default_val[v]; };
   // (3) unpack (masked); active writes of different boundaries never overlap, which
   // the overlap check verifies
   if (check_overlaps) {
@@ -250,6 +299,7 @@ inline ExchangeStats exchange(Field &f, std::vector<Block> &bl, BType t, int lev
       for (int v = 0; v < f.ncomp; ++v)
         for_box(br.recv, [&](int k, int j, int i) {
           const double val = bufs[r][m_++];
+          if (!alloc_ok(br.receiver, v)) return;
           if (br.recv.active(k, j, i)) {
             double *p = &f.any(br.recv_coarse, br.receiver, v, k, j, i);
             int64_t off = br.recv_coarse
@@ -257,7 +307,7 @@ inline ExchangeStats exchange(Field &f, std::vector<Block> &bl, BType t, int lev
                               : (p - &f.data[br.receiver * f.bstride()]);
             if (written[br.receiver][off]) ++st.overlaps;
             written[br.receiver][off] = 1;
-            *p = val;
+            *p = sp ? value(r, v, val) : val;
           }
         });
     }
@@ -269,7 +319,8 @@ inline ExchangeStats exchange(Field &f, std::vector<Block> &bl, BType t, int lev
       for (int v = 0; v < f.ncomp; ++v)
         for_box(br.recv, [&](int k, int j, int i) {
           const double val = bufs[r][m_++];
-          if (br.recv.active(k, j, i)) f.any(br.recv_coarse, br.receiver, v, k, j, i) = val;
+          if (!alloc_ok(br.receiver, v)) return;
+          if (br.recv.active(k, j, i)) f.any(br.recv_coarse, br.receiver, v, k, j, i) = sp ? value(r, v, val) : val;
         });
     }
   }
@@ -284,10 +335,12 @@ inline ExchangeStats exchange(Field &f, std::vector<Block> &bl, BType t, int lev
       for (auto &nb : *nb_list(bl[b], t, lev)) {
         if (nb.origin.level < my) continue;
         Box bx = calc_indices(nb, bl[b].loc, bl[b].nx, ng, CC, BoundaryExteriorRecv, true, false);
-        for (int v = 0; v < f.ncomp; ++v)
+        for (int v = 0; v < f.ncomp; ++v) {
+          if (!alloc_ok((int)b, v)) continue;
           for_box(bx, [&](int k, int j, int i) {
             if (bx.active(k, j, i)) restrict_cell(f, (int)b, v, k, j, i, bl[b].coords);
           });
+        }
       }
     }
   }
@@ -298,11 +351,13 @@ inline ExchangeStats exchange(Field &f, std::vector<Block> &bl, BType t, int lev
       for (auto &nb : *nb_list(bl[b], t, lev)) {
         if (!(nb.origin.level < bl[b].loc.level)) continue;
         Box bx = calc_indices(nb, bl[b].loc, bl[b].nx, ng, CC, BoundaryExteriorRecv, true, false);
-        for (int v = 0; v < f.ncomp; ++v)
+        for (int v = 0; v < f.ncomp; ++v) {
+          if (!alloc_ok((int)b, v)) continue;
           for_box(bx, [&](int k, int j, int i) {
             if (bx.active(k, j, i))
               prolong_cell(f, (int)b, v, k, j, i, bl[b].coords, bl[b].ccoords, pop);
           });
+        }
       }
     }
   }
@@ -338,8 +393,14 @@ struct FluxField {
 // SendBoundBufs<flxcor_send> / SetBounds<flxcor_recv>: restrict F on the fine side of a
 // fine/coarse face (RestrictAverage on the face element, area weights), pack from the
 // coarse flux buffer and overwrite the coarse block's face flux.
-inline void flux_correction(FluxField &F, const Mesh &m, std::vector<Block> &bl) {
+// With sparse variables a fine block whose variable is allocated always sends
+// (boundary_communication.cpp:121), an unallocated one sends a null buffer that leaves
+// the coarse flux alone, and the coarse block allocates its variable on receipt.
+inline void flux_correction(FluxField &F, const Mesh &m, std::vector<Block> &bl, Sparse *sp = nullptr) {
   const int ng = m.p.ng;
+  if (sp && !sp->on) sp = nullptr;
+  const std::vector<uint8_t> pre = sp ? sp->alloc : std::vector<uint8_t>();
+  auto sends = [&](int b, int v) { return !sp || pre[(size_t)b * F.ncomp + v] != 0; };
   std::map<int, int> idx_of;
   for (size_t i = 0; i < bl.size(); ++i) idx_of[bl[i].gid] = (int)i;
   for (size_t fb = 0; fb < bl.size(); ++fb) {
@@ -352,7 +413,8 @@ inline void flux_correction(FluxField &F, const Mesh &m, std::vector<Block> &bl)
       const int el = F1 + dir;
       // restriction of the face fluxes into the coarse flux buffer
       Box rb = calc_indices(nb, fine.loc, fine.nx, ng, el, BoundaryInteriorSend, true, true);
-      for (int v = 0; v < F.ncomp; ++v)
+      for (int v = 0; v < F.ncomp; ++v) {
+        if (!sends((int)fb, v)) continue;
         for_box(rb, [&](int ck, int cj, int ci) {
           const int i = (ci - ng) * 2 + ng, j = (cj - ng) * 2 + ng, k = (ck - ng) * 2 + ng;
           const int inc[3] = {dir != 0, dir != 1, dir != 2};
@@ -371,6 +433,7 @@ inline void flux_correction(FluxField &F, const Mesh &m, std::vector<Block> &bl)
                ((t[1][0][0] + t[1][1][0]) + (t[1][0][1] + t[1][1][1]))) /
               tv;
         });
+      }
       // pack (send box in coarse index space) and set on the coarse block
       Box sb = calc_indices(nb, fine.loc, fine.nx, ng, el, BoundaryInteriorSend, false, true);
       std::vector<double> buf;
@@ -385,11 +448,14 @@ inline void flux_correction(FluxField &F, const Mesh &m, std::vector<Block> &bl)
       Box stb = calc_indices(*cnb, coarse.loc, coarse.nx, ng, el, BoundaryExteriorRecv, false, true);
       if (stb.size() * F.ncomp != (int64_t)buf.size()) throw std::runtime_error("flux buffer size");
       size_t mm = 0;
-      for (int v = 0; v < F.ncomp; ++v)
+      for (int v = 0; v < F.ncomp; ++v) {
+        const bool on = sends((int)fb, v);
+        if (on && sp) sp->alloc[(size_t)cb * F.ncomp + v] = 1;
         for_box(stb, [&](int k, int j, int i) {
           const double val = buf[mm++];
-          if (stb.active(k, j, i)) F.at(cb, dir, v, k, j, i) = 1.0 * val;
+          if (on && stb.active(k, j, i)) F.at(cb, dir, v, k, j, i) = 1.0 * val;
         });
+      }
     }
   }
 }
@@ -591,7 +657,11 @@ inline void plm_face_states(const Coords &c, int d, int idx, double qm, double q
   qr_here = q0 - ((xcc - xfm) / c.dx[d]) * dqm;
 }
 
-inline void advection_fluxes(Field &U, FluxField &F, int recon, const double vel[3]) {
+// cvel (optional): one velocity per component, 3 values each, as the sparse advection
+// package's vx/vy/vz parameters (example/sparse_advection/sparse_advection_package.cpp:
+// 61-66, 160-244); sp (optional): unallocated sparse variables get no fluxes.
+inline void advection_fluxes(Field &U, FluxField &F, int recon, const double vel0[3],
+                             const std::vector<double> *cvel = nullptr, const Sparse *sp = nullptr) {
   const int ng = U.mesh->p.ng;
   const int nb = (int)U.blocks->size();
   const int is = ng, ie = U.N[0] - ng - 1, js = ng, je = U.N[1] - ng - 1, ks = ng, ke = U.N[2] - ng - 1;
@@ -599,6 +669,8 @@ inline void advection_fluxes(Field &U, FluxField &F, int recon, const double vel
   for (int b = 0; b < nb; ++b) {
     const Coords &c = (*U.blocks)[b].coords;
     for (int n = 0; n < U.ncomp; ++n) {
+      if (sp && !sp->allocated(b, n)) continue;
+      const double *vel = (cvel && !cvel->empty()) ? cvel->data() + 3 * n : vel0;
       auto q = [&](int k, int j, int i) { return U.at(b, n, k, j, i); };
       // x faces: i in [is, ie+1], k in [ks,ke], j in [js,je]
       for (int k = ks; k <= ke; ++k)
@@ -644,12 +716,18 @@ inline void advection_fluxes(Field &U, FluxField &F, int recon, const double vel
   }
 }
 
-// advection_package.cpp:465-494 (before cfl)
-inline double advection_min_dt(Field &U, const double vel[3]) {
+// advection_package.cpp:465-494 (before cfl); with per-component velocities the
+// minimum runs over every component, allocated or not (sparse_advection_package.cpp:
+// 126-156)
+inline double advection_min_dt(Field &U, const double vel[3], const std::vector<double> *cvel = nullptr) {
   double mn = std::numeric_limits<double>::max();
+  const int nv = (cvel && !cvel->empty()) ? (int)cvel->size() / 3 : 1;
   for (auto &b : *U.blocks)
-    for (int d = 0; d < 3; ++d)
-      if (vel[d] != 0.0) mn = std::min(mn, b.coords.dx[d] / std::fabs(vel[d]));
+    for (int n = 0; n < nv; ++n) {
+      const double *v = (cvel && !cvel->empty()) ? cvel->data() + 3 * n : vel;
+      for (int d = 0; d < 3; ++d)
+        if (v[d] != 0.0) mn = std::min(mn, b.coords.dx[d] / std::fabs(v[d]));
+    }
   return mn;
 }
 
@@ -809,11 +887,76 @@ struct Sim {
   int ncycle = 0;
   int64_t zone_cycles = 0;
   std::vector<int> deref_count;  // per block, MeshRefinement::deref_count_
+  Sparse sparse;                 // sparse variables (off unless enabled)
+  std::vector<double> cvel;      // per-component advection velocities (empty: vel)
 };
 
 inline double estimate_dt(Sim &s, Field &U) {
   if (s.physics == 1) return s.cfl * burgers_min_dt(U);
-  return s.cfl * advection_min_dt(U, s.vel);
+  return s.cfl * advection_min_dt(U, s.vel, &s.cvel);
+}
+
+// SparseDealloc (update.cpp:143-216) on the container given (the base container after
+// the last stage's exchange): a variable whose every value, ghosts included, has
+// |q| <= its deallocation threshold counts one more consecutive check, otherwise its
+// counter restarts; past `dealloc_count` checks it is deallocated (DeallocateSparse in
+// every stage container, meshblock.cpp:327-345), which here zeroes it everywhere.
+inline void sparse_dealloc(Sim &s, Field &U) {
+  Sparse &sp = s.sparse;
+  if (!sp.on) return;
+  const int nc = s.ncomp;
+  const int64_t n = (int64_t)U.N[0] * U.N[1] * U.N[2];
+  const int nb = (int)U.blocks->size();
+  for (int b = 0; b < nb; ++b)
+    for (int v = 0; v < nc; ++v) {
+      const size_t id = (size_t)b * nc + v;
+      if (!sp.alloc[id]) continue;
+      const double *q = U.data.data() + b * U.bstride() + v * n;
+      bool all_zero = true;
+      for (int64_t e = 0; e < n; ++e)
+        if (std::fabs(q[e]) > sp.dealloc_thr[v]) {
+          all_zero = false;
+          break;
+        }
+      int &c = sp.count[id];
+      c = all_zero ? c + 1 : 0;
+      if (c > sp.dealloc_count) {
+        c = 0;
+        sp.alloc[id] = 0;
+        s.base.zero(b, v);
+        s.stage.zero(b, v);
+        s.dudt.zero(b, v);
+        const int64_t nf = (int64_t)s.flux.N[0] * s.flux.N[1] * s.flux.N[2];
+        const int64_t nfc = (int64_t)s.flux.Nc[0] * s.flux.Nc[1] * s.flux.Nc[2];
+        for (int d = 0; d < 3; ++d) {
+          auto f0 = s.flux.f.begin() + b * s.flux.bs() + ((int64_t)d * nc + v) * nf;
+          std::fill(f0, f0 + nf, 0.0);
+          auto c0 = s.flux.fc.begin() + b * s.flux.cbs() + ((int64_t)d * nc + v) * nfc;
+          std::fill(c0, c0 + nfc, 0.0);
+        }
+      }
+    }
+}
+
+// The sparse advection package's CheckRefinement (sparse_advection_package.cpp:
+// 94-123): min and max over the allocated variables of a block, ghosts included;
+// refine when max > refine_tol and min < derefine_tol, derefine when max <
+// derefine_tol (a block with nothing allocated keeps the reduction's identities and
+// derefines), otherwise keep.
+inline int sparse_minmax_tag(Sim &s, Field &U, int b, double refine_tol, double derefine_tol) {
+  double mn = std::numeric_limits<double>::max(), mx = std::numeric_limits<double>::lowest();
+  const int64_t n = (int64_t)U.N[0] * U.N[1] * U.N[2];
+  for (int v = 0; v < s.ncomp; ++v) {
+    if (!s.sparse.allocated(b, v)) continue;
+    const double *q = U.data.data() + b * U.bstride() + v * n;
+    for (int64_t e = 0; e < n; ++e) {
+      mn = q[e] < mn ? q[e] : mn;
+      mx = q[e] > mx ? q[e] : mx;
+    }
+  }
+  if (mx > refine_tol && mn < derefine_tol) return 1;
+  if (mx < derefine_tol) return -1;
+  return 0;
 }
 
 // driver.cpp:210-232 (dt_force/dt_init/dt_user/floor/ceil at their defaults)
@@ -824,10 +967,23 @@ inline void set_global_dt(Sim &s, double new_dt) {
   s.dt = std::max(std::numeric_limits<double>::min(), std::min(s.dt, std::numeric_limits<double>::max()));
 }
 
-inline void weighted_sum(Field &z, Field &x, Field &y, double w1, double w2) {
-  const size_t n = z.data.size();
+inline void weighted_sum(Field &z, Field &x, Field &y, double w1, double w2, const Sparse *sp = nullptr) {
+  if (!sp || !sp->on) {
+    const size_t n = z.data.size();
 #pragma omp parallel for schedule(static)
-  for (size_t i = 0; i < n; ++i) z.data[i] = w1 * x.data[i] + w2 * y.data[i];
+    for (size_t i = 0; i < n; ++i) z.data[i] = w1 * x.data[i] + w2 * y.data[i];
+    return;
+  }
+  // WeightedSumData over allocated variables only (update.hpp:70-136)
+  const int64_t n = (int64_t)z.N[0] * z.N[1] * z.N[2];
+  const int nb = (int)z.blocks->size();
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < nb; ++b)
+    for (int v = 0; v < z.ncomp; ++v) {
+      if (!sp->allocated(b, v)) continue;
+      const int64_t o = b * z.bstride() + v * n;
+      for (int64_t e = 0; e < n; ++e) z.data[o + e] = w1 * x.data[o + e] + w2 * y.data[o + e];
+    }
 }
 
 // One RK2 cycle (advection_driver.cpp:56-164, burgers_driver.cpp:53-148 task order)
@@ -839,23 +995,29 @@ inline void cycle(Sim &s) {
     Field &mc0 = *cont[st - 1];
     Field &mc1 = *cont[st];
     const double beta = betas[st - 1];
+    Sparse *sp = s.sparse.on ? &s.sparse : nullptr;
     if (s.physics == 1) burgers_fluxes(mc0, s.flux, s.recon);
-    else advection_fluxes(mc0, s.flux, s.recon, s.vel);
-    if (m.multilevel) flux_correction(s.flux, m, m.blocks);
+    else advection_fluxes(mc0, s.flux, s.recon, s.vel, &s.cvel, sp);
+    if (m.multilevel) flux_correction(s.flux, m, m.blocks, sp);
     const int ng = m.p.ng;
     const int nblk = (int)m.blocks.size();
 #pragma omp parallel for schedule(static)
     for (int b = 0; b < nblk; ++b) {
       const Coords &c = m.blocks[b].coords;
-      for (int l = 0; l < s.ncomp; ++l)
+      for (int l = 0; l < s.ncomp; ++l) {
+        if (sp && !sp->allocated(b, l)) continue;
         for (int k = ng; k < mc0.N[2] - ng; ++k)
           for (int j = ng; j < mc0.N[1] - ng; ++j)
             for (int i = ng; i < mc0.N[0] - ng; ++i)
               s.dudt.at((int)b, l, k, j, i) = flux_div(s.flux, c, (int)b, l, k, j, i);
+      }
     }
-    weighted_sum(mc0, mc0, s.base, beta, 1.0 - beta);
-    weighted_sum(mc1, mc0, s.dudt, 1.0, beta * s.dt);
-    exchange(mc1, m.blocks, BAny, 0, s.recs, s.prolong_in_stage, PMinMod, m.multilevel);
+    weighted_sum(mc0, mc0, s.base, beta, 1.0 - beta, sp);
+    weighted_sum(mc1, mc0, s.dudt, 1.0, beta * s.dt, sp);
+    exchange(mc1, m.blocks, BAny, 0, s.recs, s.prolong_in_stage, PMinMod, m.multilevel, false, sp);
+    // the last stage checks for deallocation after its exchange
+    // (sparse_advection_driver.cpp:120-123)
+    if (st == 2 && sp) sparse_dealloc(s, mc1);
   }
   s.ncycle += 1;
   s.time += s.dt;
@@ -964,8 +1126,55 @@ void orc_boundaries(void *h, int32_t *out) {
 int64_t orc_exchange(void *h, int prolongate, int op) {
   Sim *s = (Sim *)h;
   auto st = exchange(s->base, s->mesh->blocks, BAny, 0, s->recs, prolongate != 0, op,
-                     s->mesh->multilevel, true);
+                     s->mesh->multilevel, true, &s->sparse);
   return st.overlaps;
+}
+
+// ---- sparse variables
+// Enable sparse handling of every component: per-component allocation and
+// deallocation thresholds and default values, and the deallocation count. All
+// variables start unallocated.
+void orc_sparse_enable(void *h, const double *alloc_thr, const double *dealloc_thr, const double *default_val,
+                       int dealloc_count) {
+  Sim *s = (Sim *)h;
+  Sparse &sp = s->sparse;
+  sp.on = true;
+  sp.ncomp = s->ncomp;
+  sp.dealloc_count = dealloc_count;
+  sp.alloc_thr.assign(alloc_thr, alloc_thr + s->ncomp);
+  sp.dealloc_thr.assign(dealloc_thr, dealloc_thr + s->ncomp);
+  sp.default_val.assign(default_val, default_val + s->ncomp);
+  sp.resize(s->mesh->blocks.size());
+}
+// alloc[b * ncomp + v] in {0, 1}; counts may be null (kept)
+void orc_sparse_set(void *h, const uint8_t *alloc, const int *counts) {
+  Sim *s = (Sim *)h;
+  Sparse &sp = s->sparse;
+  const size_t n = s->mesh->blocks.size() * s->ncomp;
+  sp.alloc.assign(alloc, alloc + n);
+  if (counts) sp.count.assign(counts, counts + n);
+}
+void orc_sparse_get(void *h, uint8_t *alloc, int *counts) {
+  Sim *s = (Sim *)h;
+  std::copy(s->sparse.alloc.begin(), s->sparse.alloc.end(), alloc);
+  if (counts) std::copy(s->sparse.count.begin(), s->sparse.count.end(), counts);
+}
+// SparseDealloc on the base container (standalone; the RK2 cycle runs it itself)
+void orc_sparse_dealloc(void *h) {
+  Sim *s = (Sim *)h;
+  sparse_dealloc(*s, s->base);
+}
+// Per-block tag of the sparse advection package's CheckRefinement, as -1, 0 or 1.
+void orc_sparse_tag(void *h, double refine_tol, double derefine_tol, double *out) {
+  Sim *s = (Sim *)h;
+  const int nb = (int)s->mesh->blocks.size();
+  for (int b = 0; b < nb; ++b) out[b] = (double)sparse_minmax_tag(*s, s->base, b, refine_tol, derefine_tol);
+}
+// Per-component advection velocities: ncomp x 3 values (null: the common velocity)
+void orc_set_comp_vel(void *h, const double *v) {
+  Sim *s = (Sim *)h;
+  if (v) s->cvel.assign(v, v + 3 * s->ncomp);
+  else s->cvel.clear();
 }
 
 // Initialise the time step from the current base state (InitializeBlockTimeSteps +
@@ -1110,6 +1319,42 @@ int orc_remesh(void *h, const int *flags) {
     }
     s->base.init(s->mesh.get(), &s->mesh->blocks, s->ncomp);
     transfer(*keep, old_blocks, old_base, *s->mesh, s->mesh->blocks, s->base);
+    if (s->sparse.on) {
+      // allocation follows the data (mesh-amr_loadbalance.cpp:95-145, 187-213): a
+      // surviving block keeps its flags and counters; a new fine block allocates what
+      // its parent had; a new coarse block what any child had; new blocks' counters
+      // start at zero. Unallocated sources are zeros, so the moved data is zero there.
+      Sparse &sp = s->sparse;
+      const int nc = s->ncomp;
+      std::map<std::tuple<int, int64_t, int64_t, int64_t>, int> oi;
+      for (size_t b = 0; b < old_blocks.size(); ++b) {
+        const Loc &l = old_blocks[b].loc;
+        oi[{l.level, l.l[0], l.l[1], l.l[2]}] = (int)b;
+      }
+      auto find = [&](const Loc &l) {
+        auto it = oi.find({l.level, l.l[0], l.l[1], l.l[2]});
+        return it == oi.end() ? -1 : it->second;
+      };
+      const std::vector<uint8_t> oa = sp.alloc;
+      const std::vector<int> oc = sp.count;
+      sp.resize(s->mesh->blocks.size());
+      for (size_t b = 0; b < s->mesh->blocks.size(); ++b) {
+        const Loc &L = s->mesh->blocks[b].loc;
+        const int same = find(L), par = find(L.parent());
+        for (int v = 0; v < nc; ++v) {
+          uint8_t a = 0;
+          if (same >= 0) {
+            a = oa[(size_t)same * nc + v];
+            sp.count[b * nc + v] = oc[(size_t)same * nc + v];
+          } else if (par >= 0) {
+            a = oa[(size_t)par * nc + v];
+          } else {
+            for (auto &c : L.daughters()) a = a | oa[(size_t)find(c) * nc + v];
+          }
+          sp.alloc[b * nc + v] = a;
+        }
+      }
+    }
     s->stage.init(s->mesh.get(), &s->mesh->blocks, s->ncomp);
     s->dudt.init(s->mesh.get(), &s->mesh->blocks, s->ncomp);
     s->flux.init(s->base);

@@ -80,6 +80,13 @@ def lib():
         L.orc_ncycle.restype = ctypes.c_int
         L.orc_history_mass.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_void_p]
+        L.orc_sparse_enable.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_int]
+        L.orc_sparse_set.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_sparse_get.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_sparse_dealloc.argtypes = [ctypes.c_void_p]
+        L.orc_sparse_tag.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]
+        L.orc_set_comp_vel.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -208,6 +215,40 @@ class OracleSim:
     def remesh_dt(self):
         """Every block of the new mesh votes again; SetGlobalTimeStep from the previous step."""
         return lib().orc_remesh_dt(self.h)
+
+    # sparse variables
+    def sparse_enable(self, alloc_threshold, dealloc_threshold, dealloc_count=5, default_value=0.0):
+        """Every component becomes a sparse variable; per-component thresholds (scalars
+        broadcast). All variables start unallocated."""
+        def vec(x):
+            return np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float64), (self.ncomp,)))
+        a, d, v = vec(alloc_threshold), vec(dealloc_threshold), vec(default_value)
+        lib().orc_sparse_enable(self.h, _ptr(a), _ptr(d), _ptr(v), int(dealloc_count))
+
+    def sparse_set(self, alloc, counts=None):
+        a = np.ascontiguousarray(alloc, np.uint8).reshape(self.nblocks, self.ncomp)
+        c = None if counts is None else np.ascontiguousarray(counts, np.int32).reshape(self.nblocks, self.ncomp)
+        lib().orc_sparse_set(self.h, _ptr(a), None if c is None else _ptr(c))
+
+    def sparse_alloc(self):
+        """(alloc [nblocks, ncomp] uint8, dealloc counters [nblocks, ncomp] int32)"""
+        a = np.zeros((self.nblocks, self.ncomp), np.uint8)
+        c = np.zeros((self.nblocks, self.ncomp), np.int32)
+        lib().orc_sparse_get(self.h, _ptr(a), _ptr(c))
+        return a, c
+
+    def sparse_dealloc(self):
+        lib().orc_sparse_dealloc(self.h)
+
+    def sparse_tag(self, refine_tol, derefine_tol):
+        out = np.zeros(self.nblocks, np.float64)
+        lib().orc_sparse_tag(self.h, float(refine_tol), float(derefine_tol), _ptr(out))
+        return out
+
+    def set_component_velocities(self, vel):
+        v = np.ascontiguousarray(vel, np.float64).reshape(self.ncomp, 3)
+        self._cvel = v
+        lib().orc_set_comp_vel(self.h, _ptr(v))
 
 
 def ownership(main, locs):
