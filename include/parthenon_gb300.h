@@ -62,14 +62,20 @@ typedef struct {
 /* Stage parameters. physics: 0 advection (constant velocity), 1 Burgers.
  * recon: advection 0 donor cell / 1 PLM; Burgers 0 WENO5 / 1 MC-linear.
  * exact: 1 = separately rounded arithmetic in the reference's order (bitwise path),
- *        0 = FMA-contracted kernels with shared reciprocals (within 1e-12 relative). */
+ *        0 = FMA-contracted kernels with shared reciprocals (within 1e-12 relative).
+ * Advection velocities: ncomp_vel == 0 moves every component with vel; otherwise
+ * comp_vel (host memory, read at each call) holds ncomp_vel == ncomp rows of three
+ * velocities, one per component (at most PGB_MAX_COMP_VEL), as the sparse advection
+ * package's vx/vy/vz (example/sparse_advection/sparse_advection_package.cpp:61-66). */
+#define PGB_MAX_COMP_VEL 16
 typedef struct {
   int32_t physics;
   int32_t recon;
   int32_t exact;
-  int32_t pad;
+  int32_t ncomp_vel;
   double vel[3];
   double cfl;
+  const double *comp_vel;
 } pgb_stage_params;
 
 const char *pgb_last_error(void);
@@ -286,6 +292,58 @@ int pgb_amr_remesh(pgb_mesh *mesh, const int32_t *flags, pgb_mesh **out);
  * (src/mesh/mesh-amr_loadbalance.cpp:663-1010, amr_loadbalance.cpp:95-135,205-245). */
 int pgb_amr_transfer(pgb_mesh *old_mesh, pgb_mesh *new_mesh, const double *old_data, double *new_data,
                      int32_t ncomp, void *stream);
+
+/* ---- sparse variables ------------------------------------------------------------ */
+
+/* Every component of the fields exchanged and evolved on this mesh becomes a sparse
+ * variable (Metadata::Sparse): per block an allocation flag and a deallocation counter,
+ * per variable an allocation threshold, a deallocation threshold and a default value
+ * (host arrays of ncomp doubles). Afterwards, on this mesh:
+ *  - pgb_exchange sends a null buffer for an unallocated sender or one whose sent
+ *    values are all below the allocation threshold, allocates a receiver's variable when
+ *    any of its buffers carries data, writes allocated receivers only and fills their
+ *    ghosts behind a null buffer with the default value; restriction and prolongation
+ *    skip unallocated variables (SendBoundBufs / ReceiveBoundBufs / SetBounds,
+ *    src/bvals/comms/boundary_communication.cpp:95-140,216-232,267-330);
+ *  - pgb_flux_correct: an allocated fine block always sends and its coarse neighbour
+ *    allocates (boundary_communication.cpp:121);
+ *  - pgb_stage computes, corrects and applies fluxes of allocated variables only
+ *    (advection only);
+ *  - pgb_rk2_cycles runs pgb_sparse_dealloc on base after the last stage's exchange
+ *    (example/sparse_advection/sparse_advection_driver.cpp:120-123);
+ *  - pgb_amr_remesh carries the flags to the new mesh (a new fine block allocates what
+ *    its parent had, a new coarse block what any child had, counters of new blocks start
+ *    at zero; src/mesh/mesh-amr_loadbalance.cpp:95-145,187-213).
+ * An unallocated variable must hold zeros in every container (what a fresh allocation
+ * gives); the library keeps it so. All variables start unallocated. dealloc_count: a
+ * variable is deallocated after more than this many consecutive all-below checks
+ * (Globals::sparse_config, src/globals.hpp:33-35). */
+typedef struct {
+  int32_t ncomp;
+  int32_t dealloc_count;
+  const double *alloc_threshold;
+  const double *dealloc_threshold;
+  const double *default_value;
+} pgb_sparse_params;
+int pgb_sparse_enable(pgb_mesh *mesh, const pgb_sparse_params *p);
+/* Flags alloc[nblocks * ncomp] (0/1, block-major) and, if non-NULL, counters. */
+int pgb_sparse_set_alloc(pgb_mesh *mesh, const uint8_t *alloc, const int32_t *counts);
+/* Reads the flags and counters (either may be NULL) after synchronising the stream. */
+int pgb_sparse_get_alloc(pgb_mesh *mesh, uint8_t *alloc, int32_t *counts, void *stream);
+/* SparseDealloc (src/interface/update.cpp:143-216) on field u: a variable whose values
+ * (ghosts included) all satisfy |q| <= its deallocation threshold counts one more check,
+ * otherwise its counter restarts; past dealloc_count checks it is deallocated and its
+ * slices in `cells` (ncells fields like u), `coarse` (ncoarse coarse buffers) and `flux`
+ * (flux arrays, may be NULL) are zeroed. */
+int pgb_sparse_dealloc(pgb_mesh *mesh, const double *u, double *const *cells, int32_t ncells, double *const *coarse,
+                       int32_t ncoarse, double *flux, void *stream);
+/* Per-block tag (device out[nblocks], as -1.0 / 0.0 / 1.0) of the sparse advection
+ * package's CheckRefinement (example/sparse_advection/sparse_advection_package.cpp:
+ * 94-123): min and max over the allocated variables, ghosts included; refine when
+ * max > refine_tol and min < derefine_tol, derefine when max < derefine_tol. Feed it to
+ * pgb_amr_set_refinement with refine_tol 0.5 and derefine_tol -0.5. */
+int pgb_sparse_tag(pgb_mesh *mesh, const double *u, double refine_tol, double derefine_tol, double *out,
+                   void *stream);
 
 #ifdef __cplusplus
 }

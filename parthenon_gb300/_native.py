@@ -36,7 +36,13 @@ class GmgParams(ctypes.Structure):
 
 class StageParams(ctypes.Structure):
     _fields_ = [("physics", ctypes.c_int32), ("recon", ctypes.c_int32), ("exact", ctypes.c_int32),
-                ("pad", ctypes.c_int32), ("vel", ctypes.c_double * 3), ("cfl", ctypes.c_double)]
+                ("ncomp_vel", ctypes.c_int32), ("vel", ctypes.c_double * 3), ("cfl", ctypes.c_double),
+                ("comp_vel", DP)]
+
+
+class SparseParams(ctypes.Structure):
+    _fields_ = [("ncomp", ctypes.c_int32), ("dealloc_count", ctypes.c_int32), ("alloc_threshold", DP),
+                ("dealloc_threshold", DP), ("default_value", DP)]
 
 
 # name -> (argtypes); every function returns int32 status unless noted
@@ -75,6 +81,11 @@ _SIGNATURES = {
                                ctypes.c_int32, VP],
     "pgb_amr_remesh": [VP, VP, ctypes.POINTER(VP)],
     "pgb_amr_transfer": [VP, VP, VP, VP, ctypes.c_int32, VP],
+    "pgb_sparse_enable": [VP, ctypes.POINTER(SparseParams)],
+    "pgb_sparse_set_alloc": [VP, VP, VP],
+    "pgb_sparse_get_alloc": [VP, VP, VP, VP],
+    "pgb_sparse_dealloc": [VP, VP, VP, ctypes.c_int32, VP, ctypes.c_int32, VP, VP],
+    "pgb_sparse_tag": [VP, VP, ctypes.c_double, ctypes.c_double, VP, VP],
 }
 
 

@@ -49,6 +49,26 @@ class RefinementCriterion:
         return self.refine_tol * g, self.derefine_tol * g
 
 
+class SparseMinMaxCriterion:
+    """The sparse advection package's CheckRefinement
+    (example/sparse_advection/sparse_advection_package.cpp:94-123): over the allocated
+    variables of a block, ghosts included, refine when max > refine_tol and min <
+    derefine_tol, derefine when max < derefine_tol. Needs a mesh with sparse variables."""
+
+    method = "sparse_minmax"
+    comps = ()
+    relative = False
+    max_level = None
+
+    def __init__(self, refine_tol=0.3, derefine_tol=0.03):
+        self.refine_tol = float(refine_tol)
+        self.derefine_tol = float(derefine_tol)
+
+    def tolerances(self, crit):
+        # the per-block values are the tags themselves
+        return 0.5, -0.5
+
+
 class AMRDriver:
     """RK2 evolution with adaptive refinement.
 
@@ -92,6 +112,9 @@ class AMRDriver:
         m = self.mesh
         vals = None
         with torch.cuda.stream(self.stream):
+            if self.criterion.method == "sparse_minmax":
+                vals = m.sparse_tag(self.base, self.criterion.refine_tol, self.criterion.derefine_tol,
+                                    stream=self.stream)
             for c in self.criterion.comps:
                 v = m.block_criterion(self.base, c, self.criterion.method, stream=self.stream)
                 vals = v if vals is None else torch.maximum(vals, v)
@@ -118,9 +141,18 @@ class AMRDriver:
     def initialize(self, pgen, max_iterations=16):
         """Problem generation + initial refinement (Mesh::Initialize with adaptive
         refinement): pgen(mesh_or_geometry) -> host field; repeated on each new mesh
-        until a remesh leaves the block count unchanged; then the first dt."""
+        until a remesh leaves the block count unchanged; then the first dt. With sparse
+        variables pgen(mesh, current field, current allocation) -> (field, allocation):
+        it sees what the previous mesh's data became on the new one."""
         for _ in range(max_iterations):
-            self.rk.set_state(pgen(self.mesh))
+            if self.mesh.sparse:
+                self.stream.synchronize()
+                prev = self.base.cpu().numpy()
+                alloc, _ = self.mesh.sparse_alloc(self.stream)
+                state, alloc = pgen(self.mesh, prev, alloc)
+                self.rk.set_state(state, alloc)
+            else:
+                self.rk.set_state(pgen(self.mesh))
             before = self.mesh.nblocks
             self.adapt()
             if self.mesh.nblocks == before:

@@ -174,6 +174,64 @@ __global__ void __launch_bounds__(256) k_transfer(const DevRemap *__restrict__ m
   }
 }
 
+// Sparse allocation across a remesh (mesh-amr_loadbalance.cpp:95-145, 187-213): a
+// surviving block keeps its flags and counters, a new fine block allocates what its
+// parent had, a new coarse block what any of its children had; counters of new blocks
+// start at zero. The old flags are read back from the device (after a device-wide
+// synchronisation: the kernels that last wrote them may run on any stream).
+int carry_sparse(MeshState &os, MeshState &ns) {
+  const SparseState &o = os.sparse;
+  const int nc = o.ncomp;
+  const auto &ob = os.topo->leaf().blocks;
+  const size_t onbv = ob.size() * (size_t)nc;
+  std::vector<uint8_t> oa(onbv, 0);
+  std::vector<int32_t> oc(onbv, 0);
+  if (os.uploaded && o.dev.alloc && !o.staged) {
+    PGB_CUDA(cudaDeviceSynchronize());
+    PGB_CUDA(cudaMemcpy(oa.data(), o.dev.alloc, onbv, cudaMemcpyDeviceToHost));
+    PGB_CUDA(cudaMemcpy(oc.data(), o.dev.count, onbv * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  } else {
+    if (o.alloc_h.size() == onbv) oa = o.alloc_h;
+    if (o.count_h.size() == onbv) oc = o.count_h;
+  }
+  std::map<LLoc, int> idx;
+  for (size_t b = 0; b < ob.size(); ++b) idx[ob[b].loc] = (int)b;
+  auto find = [&](const LLoc &l) {
+    auto it = idx.find(l);
+    return it == idx.end() ? -1 : it->second;
+  };
+  SparseState &n = ns.sparse;
+  n.release();
+  n.on = true;
+  n.ncomp = nc;
+  n.dealloc_count = o.dealloc_count;
+  n.thr_h = o.thr_h;
+  const auto &nb = ns.topo->leaf().blocks;
+  n.alloc_h.assign(nb.size() * (size_t)nc, 0);
+  n.count_h.assign(nb.size() * (size_t)nc, 0);
+  for (size_t b = 0; b < nb.size(); ++b) {
+    const int same = find(nb[b].loc), par = same >= 0 ? -1 : find(nb[b].loc.parent());
+    for (int v = 0; v < nc; ++v) {
+      uint8_t a = 0;
+      if (same >= 0) {
+        a = oa[(size_t)same * nc + v];
+        n.count_h[b * nc + v] = oc[(size_t)same * nc + v];
+      } else if (par >= 0) {
+        a = oa[(size_t)par * nc + v];
+      } else {
+        for (auto &c : nb[b].loc.children()) {
+          const int ch = find(c);
+          if (ch < 0) return fail(kErrInvalid, "a new block has no source in the old mesh");
+          a |= oa[(size_t)ch * nc + v];
+        }
+      }
+      n.alloc_h[b * nc + v] = a;
+    }
+  }
+  n.staged = true;
+  return kOk;
+}
+
 }  // namespace
 }  // namespace pgb
 
@@ -258,6 +316,7 @@ int pgb_amr_remesh(pgb_mesh *mesh, const int32_t *flags, pgb_mesh **out) {
       auto it = old_count.find(nb[b].loc);
       if (it != old_count.end()) ns->deref_count[b] = it->second;
     }
+    if (st->sparse.on) return carry_sparse(*st, *ns);
     return kOk;
   } catch (std::exception &e) {
     return fail(kErrInvalid, e.what());

@@ -1,6 +1,7 @@
 // extern "C" boundary of the library: argument checking, error codes, and the RK2
 // cycle driver that sequences the kernels (one CUDA stream, no host synchronisation
 // inside a cycle, optional CUDA-graph replay).
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -30,12 +31,15 @@ int check_cuda(cudaError_t e, const char *what) {
 
 // exchange.cu
 int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate, int prolong_op,
-                  double *buffer, cudaStream_t s);
+                  double *buffer, cudaStream_t s, const SparseDev *sp);
 int pack_grid(GridTables &t, const double *fine, const double *coarse, int ncomp, double *buffer, cudaStream_t s);
-int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s);
+int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s, const SparseDev *sp);
 // reduce.cu
 int estimate_dt(MeshState &m, int physics, const double *u, int ncomp, const double vel[3], double cfl, double *dt,
-                int first, cudaStream_t s);
+                int first, cudaStream_t s, int ncvel, const double *cvel);
+// sparse.cu
+int sparse_dealloc(const GridTables &t, const SparseDev &sp, const double *u, int ncomp, const ZeroList &z,
+                   cudaStream_t s);
 // stencil builds
 namespace exact {
 int launch_stage(const StageArgs &a, int ncomp, int physics, bool store_flux, cudaStream_t s);
@@ -52,9 +56,9 @@ using namespace pgb;
 
 struct pgb_mesh {
   MeshState st;
-  // cached cycle graphs keyed by the pointers and parameters they were captured with
-  std::map<std::tuple<const void *, const void *, const void *, const void *, int, int, int, int>, cudaGraphExec_t>
-      graphs;
+  // cached cycle graphs keyed by the bytes of the pointers and parameters they were
+  // captured with
+  std::map<std::string, cudaGraphExec_t> graphs;
   ~pgb_mesh() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
   }
@@ -64,6 +68,11 @@ namespace pgb {
 // Leaf-grid tables of a mesh handle (used by entry points defined in other units).
 GridTables *mesh_leaf_tables(pgb_mesh *m) { return m && m->st.uploaded ? &m->st.leaf : nullptr; }
 MeshState *mesh_state(pgb_mesh *m) { return m ? &m->st : nullptr; }
+// Drop the cached cycle graphs (their launches hold device pointers that changed).
+void mesh_clear_graphs(pgb_mesh *m) {
+  for (auto &kv : m->graphs) cudaGraphExecDestroy(kv.second);
+  m->graphs.clear();
+}
 // New (not uploaded) mesh handle over the given leaves.
 int mesh_from_leaves(const MeshSpec &spec, const std::vector<LLoc> &leaves, pgb_mesh **out) {
   auto *m = new pgb_mesh();
@@ -99,6 +108,11 @@ int stage_impl(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const
   a.nblocks = t.nblocks;
   a.recon = p->recon;
   for (int q = 0; q < 3; ++q) a.vel[q] = p->vel[q];
+  a.ncvel = p->physics == 0 ? p->ncomp_vel : 0;
+  for (int c = 0; c < a.ncvel; ++c)
+    for (int q = 0; q < 3; ++q) a.cvel[c][q] = p->comp_vel[3 * c + q];
+  const SparseDev *sp = m->st.sparse_dev();
+  a.alloc = sp ? sp->alloc : nullptr;
   const bool ml = t.multilevel;
   if (ml && !flux) return fail(kErrInvalid, "multilevel stage needs a flux array");
   if (!ml && !dudt) return fail(kErrInvalid, "stage needs a dudt scratch array");
@@ -109,7 +123,7 @@ int stage_impl(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const
   if (rc == kErrUnsupported) return fail(rc, "no stencil kernel for this component count");
   if (rc != kOk) return check_cuda(cudaGetLastError(), "stencil launch");
   if (ml) {
-    if ((rc = flux_correct_grid(t, flux, ncomp, s))) return rc;
+    if ((rc = flux_correct_grid(t, flux, ncomp, s, sp))) return rc;
     rc = divup(a, ncomp, s);
     if (rc == kErrUnsupported) return fail(rc, "no update kernel for this component count");
     if (rc != kOk) return check_cuda(cudaGetLastError(), "update launch");
@@ -128,13 +142,21 @@ int check_params(const pgb_mesh *m, const pgb_stage_params *p, int ncomp) {
   }
   if (p->recon == 1 && ng < 2) return fail(kErrInvalid, "this reconstruction needs nghost >= 2");
   if (m->st.leaf.multilevel && ng < 2) return fail(kErrInvalid, "multilevel meshes need nghost >= 2");
+  if (p->physics == 0 && p->ncomp_vel != 0) {
+    if (p->ncomp_vel != ncomp || ncomp > PGB_MAX_COMP_VEL || !p->comp_vel)
+      return fail(kErrInvalid, "comp_vel needs ncomp_vel == ncomp <= 16 rows");
+  }
+  if (const SparseDev *sp = m->st.sparse_dev()) {
+    if (p->physics != 0) return fail(kErrUnsupported, "sparse variables are supported for advection only");
+    if (sp->ncomp != ncomp) return fail(kErrInvalid, "field components differ from the mesh's sparse variables");
+  }
   return kOk;
 }
 
 int exchange_leaf(pgb_mesh *m, double *data, double *coarse, int ncomp, int flags, double *buffer, cudaStream_t s) {
   const int prolongate = flags & PGB_EXCHANGE_PROLONGATE;
   const int op = (flags >> 1) & 3;
-  return exchange_grid(m->st.leaf, data, coarse, ncomp, prolongate, op, buffer, s);
+  return exchange_grid(m->st.leaf, data, coarse, ncomp, prolongate, op, buffer, s, m->st.sparse_dev());
 }
 
 // One RK2 cycle: stage names base, "1", base (low_storage_integrator.cpp:67-86 rk2:
@@ -148,7 +170,19 @@ int cycle_impl(pgb_mesh *m, const pgb_stage_params *p, double *base, double *sta
   if ((rc = exchange_leaf(m, stage, cstage, ncomp, xflags, nullptr, s))) return rc;
   if ((rc = stage_impl(m, p, stage, base, base, dudt, flux, dt, 0.5, 0.5, 0.5, ncomp, s))) return rc;
   if ((rc = exchange_leaf(m, base, cbase, ncomp, xflags, nullptr, s))) return rc;
-  return estimate_dt(m->st, p->physics, base, ncomp, p->vel, p->cfl, dt, 0, s);
+  // sparse variables: the last stage checks for deallocation after its exchange
+  // (sparse_advection_driver.cpp:120-123)
+  if (const SparseDev *sp = m->st.sparse_dev()) {
+    ZeroList z{};
+    z.cell[z.ncell++] = base;
+    z.cell[z.ncell++] = stage;
+    if (dudt) z.cell[z.ncell++] = dudt;
+    if (cbase) z.coarse[z.ncoarse++] = cbase;
+    if (cstage) z.coarse[z.ncoarse++] = cstage;
+    z.flux = flux;
+    if ((rc = sparse_dealloc(m->st.leaf, *sp, base, ncomp, z, s))) return rc;
+  }
+  return estimate_dt(m->st, p->physics, base, ncomp, p->vel, p->cfl, dt, 0, s, p->ncomp_vel, p->comp_vel);
 }
 
 // Times the candidate launch shapes of this mesh's hot kernels on the caller's data
@@ -167,7 +201,8 @@ int autotune(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage
     g_tune_force = -1;
     return r;
   };
-  if (t.ncopy_work) {
+  // (the sparse exchange does not use the tuned copy kernel)
+  if (t.ncopy_work && !m->st.sparse_dev()) {
     tune(copy_tune_key(ncomp, t.npairs, t.dims.nx[0]), 3, kCopyThreadsDefault, 3,
          [&](int c) { return guarded(c, [&] { return exchange_leaf(m, base, cbase, ncomp, xflags, nullptr, s); }); },
          s);
@@ -290,6 +325,7 @@ int pgb_mesh_upload(pgb_mesh *m) {
   if (!m) return fail(kErrInvalid, "null argument");
   int rc = lower_grid(m->st.topo->leaf(), m->st.topo->spec(), m->st.leaf);
   if (rc) return rc;
+  if ((rc = sparse_upload(m->st))) return rc;
   if (!m->st.d_minbits) {
     PGB_CUDA(cudaMalloc(&m->st.d_minbits, sizeof(unsigned long long)));
     const double big = std::numeric_limits<double>::max();
@@ -320,7 +356,7 @@ int pgb_pack_buffers(pgb_mesh *m, const double *data, const double *coarse, int3
 int pgb_flux_correct(pgb_mesh *m, double *flux, int32_t ncomp, void *stream) {
   if (!m || !flux) return fail(kErrInvalid, "null argument");
   if (!m->st.uploaded) return fail(kErrState, "mesh tables not uploaded (call pgb_mesh_upload)");
-  return flux_correct_grid(m->st.leaf, flux, ncomp, (cudaStream_t)stream);
+  return flux_correct_grid(m->st.leaf, flux, ncomp, (cudaStream_t)stream, m->st.sparse_dev());
 }
 
 int pgb_stage(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const double *u_base, double *u_out,
@@ -338,7 +374,8 @@ int pgb_estimate_dt(pgb_mesh *m, const pgb_stage_params *p, const double *u, int
   if (rc) return rc;
   if (!u || !dt) return fail(kErrInvalid, "null pointer");
   if (first < 0 || first > 2) return fail(kErrInvalid, "first must be 0, 1 or 2");
-  return estimate_dt(m->st, p->physics, u, ncomp, p->vel, p->cfl, dt, first, (cudaStream_t)stream);
+  return estimate_dt(m->st, p->physics, u, ncomp, p->vel, p->cfl, dt, first, (cudaStream_t)stream, p->ncomp_vel,
+                     p->comp_vel);
 }
 
 int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage, double *dudt, double *flux,
@@ -355,9 +392,16 @@ int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double 
     return kOk;
   }
   if (!s) return fail(kErrInvalid, "graph replay needs a non-default stream");
-  auto key = std::make_tuple((const void *)base, (const void *)stage, (const void *)dudt, (const void *)dt,
-                             p->physics * 16 + p->recon * 4 + p->exact, ncomp, (int)(flux != nullptr),
-                             (int)(cbase != nullptr));
+  // everything the captured launches were built from: pointers, stage parameters (the
+  // velocity table by value) and whether sparse variables are on
+  std::string key;
+  auto put = [&](const void *q, size_t n) { key.append((const char *)q, n); };
+  const void *ptrs[] = {base, stage, dudt, flux, cbase, cstage, dt};
+  put(ptrs, sizeof(ptrs));
+  put(p, offsetof(pgb_stage_params, comp_vel));
+  if (p->physics == 0 && p->ncomp_vel) put(p->comp_vel, 3 * sizeof(double) * p->ncomp_vel);
+  const int extra[2] = {ncomp, m->st.sparse_dev() ? 1 : 0};
+  put(extra, sizeof(extra));
   auto it = m->graphs.find(key);
   if (it == m->graphs.end()) {
     // launch shapes are chosen before the cycle is frozen into a graph
@@ -425,7 +469,7 @@ int pgb_run_host(pgb_mesh *m, const pgb_stage_params *p, const double *host_in, 
   }
   if (*dt_inout > 0) {
     if ((rc = guard(cudaMemcpyAsync(dt, dt_inout, 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
-  } else if ((rc = estimate_dt(m->st, p->physics, base, ncomp, p->vel, p->cfl, dt, 1, s))) {
+  } else if ((rc = estimate_dt(m->st, p->physics, base, ncomp, p->vel, p->cfl, dt, 1, s, p->ncomp_vel, p->comp_vel))) {
     cleanup();
     return rc;
   }

@@ -68,6 +68,26 @@ struct Dims {
   int32_t nx[3];  // interior cells
 };
 
+// Sparse-variable state seen by the kernels (one variable per field component).
+struct SparseDev {
+  uint8_t *alloc;      // [block * ncomp + v]: variable allocated on the block
+  int32_t *count;      // [block * ncomp + v]: consecutive all-below deallocation checks
+  uint8_t *recv;       // [block * ncomp + v]: data received this exchange (allocate)
+  uint8_t *pair_flag;  // [pair * ncomp + v]: the pair's buffer carries data (else null)
+  uint8_t *fc_flag;    // [flux correction * ncomp + v]: the fine side sends
+  const double *thr;   // [3][ncomp]: allocation threshold, deallocation threshold, default
+  int32_t ncomp;
+  int32_t dealloc_count;
+};
+
+// Containers whose (block, variable) slices are zeroed when a variable is deallocated.
+struct ZeroList {
+  double *cell[4];     // [block][ncomp][N3][N2][N1]
+  double *coarse[2];   // [block][ncomp][Nc3][Nc2][Nc1]
+  double *flux;        // [block][3][ncomp][N3][N2][N1]
+  int32_t ncell, ncoarse;
+};
+
 __host__ __device__ inline bool mask_active(uint32_t mask, const DevBox &b, int k, int j, int i) {
   const int ii = (i == b.lo[0] + b.n[0] - 1) - (i == b.lo[0]);
   const int jj = (j == b.lo[1] + b.n[1] - 1) - (j == b.lo[1]);

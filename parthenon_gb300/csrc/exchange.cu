@@ -24,6 +24,11 @@
 
 namespace pgb {
 
+// sparse.cu
+int sparse_exchange_copy(const GridTables &t, const SparseDev &sp, double *fine, double *coarse, int ncomp,
+                         cudaStream_t s);
+int sparse_flux_flags(const GridTables &t, const SparseDev &sp, int ncomp, cudaStream_t s);
+
 // ------------------------------------------------------------------ lowering
 namespace {
 
@@ -116,6 +121,7 @@ void GridTables::release() {
 
 MeshState::~MeshState() {
   leaf.release();
+  sparse.release();
   if (d_scalars) cudaFree(d_scalars);
   if (d_minbits) cudaFree(d_minbits);
   if (d_status) cudaFree(d_status);
@@ -378,10 +384,11 @@ __global__ void __launch_bounds__(128) k_restrict(const DevRegion *__restrict__ 
                                                   const DevWork *__restrict__ work,
                                                   const DevBlockGeom *__restrict__ geom, Dims d,
                                                   int ncomp, const double *__restrict__ fine,
-                                                  double *__restrict__ coarse) {
+                                                  double *__restrict__ coarse, const uint8_t *__restrict__ alloc) {
   const DevWork w = work[blockIdx.x];
   const DevRegion r = regs[w.item];
   const int v = blockIdx.y;
+  if (alloc && !alloc[r.block * ncomp + v]) return;  // unallocated sparse variable
   const double vol = geom[r.block].vol;
   const int ng = d.ng;
   for_work_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], [&](int k, int j, int i) {
@@ -413,10 +420,12 @@ __global__ void __launch_bounds__(128) k_prolong(const DevRegion *__restrict__ r
                                                  const DevWork *__restrict__ work,
                                                  const DevBlockGeom *__restrict__ geom, Dims d,
                                                  int ncomp, double *__restrict__ fine,
-                                                 const double *__restrict__ coarse, int op) {
+                                                 const double *__restrict__ coarse, int op,
+                                                 const uint8_t *__restrict__ alloc) {
   const DevWork w = work[blockIdx.x];
   const DevRegion r = regs[w.item];
   const int v = blockIdx.y;
+  if (alloc && !alloc[r.block * ncomp + v]) return;  // unallocated sparse variable
   const DevBlockGeom g = geom[r.block];
   const int ng = d.ng;
   for_work_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], [&](int k, int j, int i) {
@@ -466,10 +475,12 @@ __global__ void __launch_bounds__(128) k_prolong(const DevRegion *__restrict__ r
 __global__ void __launch_bounds__(128) k_flux_correct(const DevFluxCorr *__restrict__ fcs,
                                                       const DevWork *__restrict__ work,
                                                       const DevBlockGeom *__restrict__ geom, Dims d,
-                                                      int ncomp, double *__restrict__ flux) {
+                                                      int ncomp, double *__restrict__ flux,
+                                                      const uint8_t *__restrict__ send) {
   const DevWork w = work[blockIdx.x];
   const DevFluxCorr c = fcs[w.item];
   const int v = blockIdx.y;
+  if (send && !send[(int64_t)w.item * ncomp + v]) return;  // null buffer: coarse flux kept
   const int ng = d.ng;
   const double a = geom[c.fine_block].area[c.dir];
   const int64_t plane = (int64_t)d.N[0] * d.N[1] * d.N[2];
@@ -509,14 +520,20 @@ __global__ void __launch_bounds__(128) k_flux_correct(const DevFluxCorr *__restr
 }  // namespace
 
 int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate,
-                  int prolong_op, double *buffer, cudaStream_t s) {
+                  int prolong_op, double *buffer, cudaStream_t s, const SparseDev *sp) {
   if (ncomp < 1 || ncomp > 65535) return fail(kErrInvalid, "ncomp out of range");
   if (!fine) return fail(kErrInvalid, "null field pointer");
   if (t.multilevel && !coarse) return fail(kErrInvalid, "multilevel mesh needs a coarse buffer");
+  if (sp && sp->ncomp != ncomp) return fail(kErrInvalid, "field components differ from the mesh's sparse variables");
+  if (sp && buffer) return fail(kErrUnsupported, "the packed-buffer exchange does not take sparse variables");
+  const uint8_t *alloc = sp ? sp->alloc : nullptr;
   const dim3 blk(128);
   if (t.multilevel && t.nrs_work)
-    k_restrict<<<dim3(t.nrs_work, ncomp), blk, 0, s>>>(t.rs, t.rs_work, t.geom, t.dims, ncomp, fine, coarse);
-  if (t.ncopy_work) {
+    k_restrict<<<dim3(t.nrs_work, ncomp), blk, 0, s>>>(t.rs, t.rs_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
+  if (sp) {
+    int rc = sparse_exchange_copy(t, *sp, fine, coarse, ncomp, s);
+    if (rc) return rc;
+  } else if (t.ncopy_work) {
     if (buffer) {
       k_pack<<<dim3(t.ncopy_work, ncomp), blk, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse, buffer);
       k_unpack<<<dim3(t.ncopy_work, ncomp), blk, 0, s>>>(t.pairs, t.copy_work, t.dims, ncomp, fine, coarse, buffer);
@@ -534,10 +551,10 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
     }
   }
   if (t.multilevel && t.nrr_work)
-    k_restrict<<<dim3(t.nrr_work, ncomp), blk, 0, s>>>(t.rr, t.rr_work, t.geom, t.dims, ncomp, fine, coarse);
+    k_restrict<<<dim3(t.nrr_work, ncomp), blk, 0, s>>>(t.rr, t.rr_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
   if (t.multilevel && prolongate && t.npro_work)
     k_prolong<<<dim3(t.npro_work, ncomp), blk, 0, s>>>(t.pro, t.pro_work, t.geom, t.dims, ncomp, fine, coarse,
-                                                       prolong_op);
+                                                       prolong_op, alloc);
   PGB_CUDA(cudaGetLastError());
   return kOk;
 }
@@ -552,9 +569,15 @@ int pack_grid(GridTables &t, const double *fine, const double *coarse, int ncomp
   return kOk;
 }
 
-int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s) {
+int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s, const SparseDev *sp) {
   if (!t.multilevel || !t.nfc_work) return kOk;
-  k_flux_correct<<<dim3(t.nfc_work, ncomp), dim3(128), 0, s>>>(t.fc, t.fc_work, t.geom, t.dims, ncomp, flux);
+  if (sp && sp->ncomp != ncomp) return fail(kErrInvalid, "field components differ from the mesh's sparse variables");
+  if (sp) {
+    int rc = sparse_flux_flags(t, *sp, ncomp, s);
+    if (rc) return rc;
+  }
+  k_flux_correct<<<dim3(t.nfc_work, ncomp), dim3(128), 0, s>>>(t.fc, t.fc_work, t.geom, t.dims, ncomp, flux,
+                                                               sp ? sp->fc_flag : nullptr);
   PGB_CUDA(cudaGetLastError());
   return kOk;
 }

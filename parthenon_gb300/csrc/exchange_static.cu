@@ -18,8 +18,9 @@
 namespace pgb {
 
 int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate, int prolong_op,
-                  double *buffer, cudaStream_t s);
+                  double *buffer, cudaStream_t s, const SparseDev *sp);
 GridTables *mesh_leaf_tables(pgb_mesh *m);
+MeshState *mesh_state(pgb_mesh *m);
 
 namespace {
 
@@ -66,5 +67,6 @@ extern "C" int pgb_exchange_static_buffer(pgb_mesh *mesh, double *data, double *
   if (rc) return rc;
   const int prolongate = flags & PGB_EXCHANGE_PROLONGATE;
   const int op = (flags >> 1) & 3;
-  return exchange_grid(*t, data, coarse, ncomp, prolongate, op, buf, (cudaStream_t)stream);
+  return exchange_grid(*t, data, coarse, ncomp, prolongate, op, buf, (cudaStream_t)stream,
+                       mesh_state(mesh)->sparse_dev());
 }

@@ -33,6 +33,22 @@ struct GridTables {
   void release();
 };
 
+// Sparse variables of a mesh (Metadata::Sparse, one field component each): per block
+// an allocation flag and a deallocation counter, per variable the thresholds and the
+// default value. The device arrays exist while the mesh is uploaded; the host copies
+// carry the state from one mesh to the next across a remesh.
+struct SparseState {
+  bool on = false;
+  int ncomp = 0;
+  int dealloc_count = 5;
+  std::vector<double> thr_h;       // [3][ncomp]: allocation, deallocation, default
+  std::vector<uint8_t> alloc_h;    // staged flags [nblocks * ncomp]
+  std::vector<int32_t> count_h;    // staged counters
+  bool staged = false;             // host copies to be uploaded with the mesh tables
+  SparseDev dev{};                 // device arrays (null until uploaded)
+  void release();
+};
+
 struct MeshState {
   std::unique_ptr<MeshTopology> topo;
   GridTables leaf;
@@ -42,8 +58,14 @@ struct MeshState {
   unsigned long long *d_minbits = nullptr;
   int *d_status = nullptr;
   std::vector<int> deref_count;     // per leaf block, MeshRefinement::deref_count_
+  SparseState sparse;
+  // device view for the kernels, or null when the mesh has no sparse variables
+  const SparseDev *sparse_dev() const { return sparse.on && sparse.dev.alloc ? &sparse.dev : nullptr; }
   ~MeshState();
 };
+
+// sparse.cu: (re)create the device arrays of m.sparse for the uploaded tables
+int sparse_upload(MeshState &m);
 
 int lower_grid(const GridTopology &g, const MeshSpec &spec, GridTables &out, bool dry_run = false);
 

@@ -57,14 +57,21 @@ __global__ void __launch_bounds__(256) k_burgers_min(const double *__restrict__ 
   block_min_to(m, out);
 }
 
-// advection_package.cpp:465-494: min over blocks of dx/|v| per direction with v != 0
-__global__ void k_advection_min(const DevBlockGeom *__restrict__ geom, int nblocks, double vx, double vy, double vz,
+struct VelTable {
+  double v[16][3];
+  int n;
+};
+
+// advection_package.cpp:465-494: min over blocks of dx/|v| per direction with v != 0;
+// with one velocity per component, over every component too
+// (sparse_advection_package.cpp:126-156)
+__global__ void k_advection_min(const DevBlockGeom *__restrict__ geom, int nblocks, VelTable vt,
                                 unsigned long long *out) {
   double m = DBL_MAX;
-  const double v[3] = {vx, vy, vz};
   for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nblocks; b += gridDim.x * blockDim.x)
-    for (int q = 0; q < 3; ++q)
-      if (v[q] != 0.0) m = fmin(m, __ddiv_rn(geom[b].dx[q], fabs(v[q])));
+    for (int c = 0; c < vt.n; ++c)
+      for (int q = 0; q < 3; ++q)
+        if (vt.v[c][q] != 0.0) m = fmin(m, __ddiv_rn(geom[b].dx[q], fabs(vt.v[c][q])));
   block_min_to(m, out);
 }
 
@@ -99,13 +106,18 @@ __global__ void k_reset_min(unsigned long long *minbits) {
 }  // namespace
 
 int estimate_dt(MeshState &m, int physics, const double *u, int ncomp, const double vel[3], double cfl,
-                double *dt, int first, cudaStream_t s) {
+                double *dt, int first, cudaStream_t s, int ncvel, const double *cvel) {
   GridTables &t = m.leaf;
   if (physics == 1) {
     if (ncomp < 3) return fail(kErrInvalid, "Burgers needs three velocity components");
     k_burgers_min<<<152 * 8, 256, 0, s>>>(u, t.geom, t.dims, ncomp, t.nblocks, m.d_minbits);
   } else {
-    k_advection_min<<<1, 256, 0, s>>>(t.geom, t.nblocks, vel[0], vel[1], vel[2], m.d_minbits);
+    if (ncvel < 0 || ncvel > 16 || (ncvel && !cvel)) return fail(kErrInvalid, "bad component velocity table");
+    VelTable vt{};
+    vt.n = ncvel ? ncvel : 1;
+    for (int c = 0; c < vt.n; ++c)
+      for (int q = 0; q < 3; ++q) vt.v[c][q] = ncvel ? cvel[3 * c + q] : vel[q];
+    k_advection_min<<<1, 256, 0, s>>>(t.geom, t.nblocks, vt, m.d_minbits);
   }
   k_set_dt<<<1, 1, 0, s>>>(dt, m.d_minbits, cfl, first);
   PGB_CUDA(cudaGetLastError());

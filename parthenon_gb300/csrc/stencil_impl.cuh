@@ -100,6 +100,10 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
   const DevBlockGeom g = a.geom[b];
   const double area = g.area[D];
   const double *__restrict__ u = a.u_in;
+  // sparse variables: unallocated components are neither read nor written
+  bool on[NC];
+#pragma unroll
+  for (int v = 0; v < NC; ++v) on[v] = BURGERS || !a.alloc || a.alloc[b * NC + v];
 
   double Lprev[NC], AFprev[NC];
   // march from cell p = -1 (first ghost) to p = n (last ghost); face p lies between
@@ -129,6 +133,10 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
 #pragma unroll
       for (int v = 0; v < NC; ++v) {
         const int64_t e = cp + v * cs;
+        if (!on[v]) {
+          Lc[v] = Rc[v] = 0.0;
+          continue;
+        }
         const double q0 = ld<D>(u, e);
         if (a.recon == 0) {
           Lc[v] = q0;
@@ -148,9 +156,11 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
       if (BURGERS) {
         burgers_face_flux<NC>(Lprev, Rc, D, F);
       } else {
-        const double vd = a.vel[D];
 #pragma unroll
-        for (int v = 0; v < NC; ++v) F[v] = vd > 0.0 ? Lprev[v] * vd : Rc[v] * vd;
+        for (int v = 0; v < NC; ++v) {
+          const double vd = a.ncvel ? a.cvel[v][D] : a.vel[D];
+          F[v] = vd > 0.0 ? Lprev[v] * vd : Rc[v] * vd;
+        }
       }
       if (MODE == kStoreFlux) {
         // face p of direction D, stored at the cell index of the cell on its right
@@ -158,7 +168,7 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
 #pragma unroll
         for (int v = 0; v < NC; ++v) {
           const int64_t e = cp - (int64_t)b * NC * cs + v * cs;
-          a.flux[fbase + e] = F[v];
+          if (on[v]) a.flux[fbase + e] = F[v];
         }
       } else {
         double AF[NC];
@@ -168,6 +178,7 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
           const int64_t cc = cp - step;  // cell p-1
 #pragma unroll
           for (int v = 0; v < NC; ++v) {
+            if (!on[v]) continue;
             const int64_t e = cc + v * cs;
             double du = AF[v] - AFprev[v];
             if (MODE == kStoreDu) {
@@ -211,6 +222,7 @@ __global__ void __launch_bounds__(128) k_div_update(StageArgs a) {
   const double bdt = a.beta * a.dt[0];
 #pragma unroll
   for (int v = 0; v < NC; ++v) {
+    if (a.alloc && !a.alloc[b * NC + v]) continue;  // unallocated sparse variable
     const int64_t e = (int64_t)b * NC * cs + v * cs + (int64_t)k * N01 + (int64_t)j * N0 + i;
     const double *F0 = a.flux + ((int64_t)b * 3 + 0) * NC * cs + v * cs;
     const double *F1 = a.flux + ((int64_t)b * 3 + 1) * NC * cs + v * cs;

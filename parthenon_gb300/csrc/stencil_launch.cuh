@@ -56,6 +56,7 @@ int launch_stage(const StageArgs &a, int ncomp, int physics, bool store_flux, cu
   }
   switch (ncomp) {
     case 1: return launch_stage_nc<1, false>(a, store_flux, s);
+    case 4: return launch_stage_nc<4, false>(a, store_flux, s);
     case 5: return launch_stage_nc<5, false>(a, store_flux, s);
     default: return kErrUnsupported;
   }

@@ -10,6 +10,8 @@ device memory, so a cycle is one CUDA-graph launch.
 """
 import ctypes
 
+import numpy as np
+
 from . import _native as nat
 from .mesh import _ptr, _stream
 
@@ -17,14 +19,16 @@ from .mesh import _ptr, _stream
 class StageConfig:
     """physics: 'advection' or 'burgers'; recon: 'dc'/'plm' (advection) or
     'weno5'/'linear' (Burgers); exact: bitwise reference arithmetic instead of the
-    FMA/shared-reciprocal kernels."""
+    FMA/shared-reciprocal kernels. comp_vel (advection): one (vx, vy, vz) per
+    component instead of the common `vel` (the sparse advection package's velocities)."""
 
-    def __init__(self, physics, recon, cfl, vel=(1.0, 1.0, 1.0), exact=False):
+    def __init__(self, physics, recon, cfl, vel=(1.0, 1.0, 1.0), exact=False, comp_vel=None):
         self.physics = physics
         self.recon = recon
         self.cfl = float(cfl)
         self.vel = tuple(float(v) for v in vel)
         self.exact = bool(exact)
+        self.comp_vel = None if comp_vel is None else np.ascontiguousarray(comp_vel, np.float64).reshape(-1, 3)
 
     def params(self):
         p = nat.StageParams()
@@ -35,6 +39,9 @@ class StageConfig:
         for d in range(3):
             p.vel[d] = self.vel[d]
         p.cfl = self.cfl
+        if self.comp_vel is not None:
+            p.ncomp_vel = self.comp_vel.shape[0]
+            p.comp_vel = self.comp_vel.ctypes.data_as(nat.DP)  # kept alive by self.comp_vel
         return p
 
 
@@ -95,11 +102,17 @@ class RK2Driver:
         # (burgers_driver.cpp:108-120); the advection list prolongates.
         return self.cfg.physics != "burgers"
 
-    def set_state(self, host_array):
+    def set_state(self, host_array, alloc=None):
         """Load the initial condition (numpy, field layout incl. ghosts), fill ghosts
         (Mesh::Initialize -> Mesh::CommunicateBoundaries, which prolongates on
-        multilevel meshes for every package, mesh.cpp:640-706) and set the first dt."""
+        multilevel meshes for every package, mesh.cpp:640-706) and set the first dt.
+        alloc (meshes with sparse variables): allocation flags (nblocks, ncomp); the
+        values of unallocated variables are dropped (they hold zeros)."""
         import torch
+        if alloc is not None:
+            a = np.asarray(alloc, np.uint8).reshape(self.mesh.nblocks, self.ncomp)
+            self.mesh.set_sparse_alloc(a)
+            host_array = np.where(a[:, :, None, None, None] != 0, np.asarray(host_array, np.float64), 0.0)
         src = torch.as_tensor(host_array, dtype=torch.float64)
         if src.is_cuda:
             # produced on the caller's stream: order the copy after it

@@ -189,7 +189,11 @@ class Mesh:
                   "pgb_amr_remesh")
         if not h:
             return None
-        return Mesh._wrap(h, self.nghost, self.block_nx)
+        m = Mesh._wrap(h, self.nghost, self.block_nx)
+        if self.sparse:
+            # the native remesh carried the allocation flags to the new handle
+            m.sparse_ncomp = self.sparse_ncomp
+        return m
 
     def transfer(self, new_mesh, field, stream=None):
         """New field on new_mesh: same-level copies, prolongated new fine blocks,
@@ -203,6 +207,69 @@ class Mesh:
             out = new_mesh.new_field(ncomp)
         nat.check(nat.lib().pgb_amr_transfer(self._h, new_mesh._h, _ptr(field), _ptr(out), ncomp, _stream(stream)),
                   "pgb_amr_transfer")
+        return out
+
+    # ---------------------------------------------------------------- sparse variables
+    def enable_sparse(self, ncomp, alloc_threshold=1e-12, dealloc_threshold=1e-14, dealloc_count=5,
+                      default_value=0.0):
+        """Every component of the fields on this mesh becomes a sparse variable
+        (Metadata::Sparse) with these thresholds (scalars or one value per component);
+        all start unallocated. Defaults: Globals::sparse_config (src/globals.hpp:33-35).
+        Exchanges, stages, RK2 cycles and remeshes on this mesh then follow the
+        reference's allocation rules."""
+        def vec(x):
+            return np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float64), (int(ncomp),)))
+        self._sparse_keep = (vec(alloc_threshold), vec(dealloc_threshold), vec(default_value))
+        p = nat.SparseParams()
+        p.ncomp = int(ncomp)
+        p.dealloc_count = int(dealloc_count)
+        p.alloc_threshold, p.dealloc_threshold, p.default_value = (
+            a.ctypes.data_as(nat.DP) for a in self._sparse_keep)
+        nat.check(nat.lib().pgb_sparse_enable(self._h, ctypes.byref(p)), "pgb_sparse_enable")
+        self.sparse_ncomp = int(ncomp)
+        return self
+
+    @property
+    def sparse(self):
+        return getattr(self, "sparse_ncomp", 0) > 0
+
+    def set_sparse_alloc(self, alloc, counts=None):
+        """Allocation flags (nblocks, ncomp) in {0, 1} and optional deallocation counters."""
+        a = np.ascontiguousarray(alloc, np.uint8).reshape(self.nblocks, self.sparse_ncomp)
+        c = None if counts is None else np.ascontiguousarray(counts, np.int32).reshape(a.shape)
+        nat.check(nat.lib().pgb_sparse_set_alloc(self._h, a.ctypes.data_as(ctypes.c_void_p),
+                                                 None if c is None else c.ctypes.data_as(ctypes.c_void_p)),
+                  "pgb_sparse_set_alloc")
+
+    def sparse_alloc(self, stream=None):
+        """(allocation flags uint8 (nblocks, ncomp), deallocation counters int32) after
+        synchronising the stream."""
+        a = np.zeros((self.nblocks, self.sparse_ncomp), np.uint8)
+        c = np.zeros((self.nblocks, self.sparse_ncomp), np.int32)
+        nat.check(nat.lib().pgb_sparse_get_alloc(self._h, a.ctypes.data_as(ctypes.c_void_p),
+                                                 c.ctypes.data_as(ctypes.c_void_p), _stream(stream)),
+                  "pgb_sparse_get_alloc")
+        return a, c
+
+    def sparse_dealloc(self, field, cells=(), coarse=(), flux=None, stream=None):
+        """SparseDealloc on `field`; deallocated variables are zeroed in `field`, the
+        fields in `cells`, the coarse buffers in `coarse` and `flux`."""
+        self._ensure()
+        cl = [field] + [c for c in cells if c is not None and c is not field]
+        cc = [c for c in coarse if c is not None]
+        ca = (ctypes.c_void_p * max(1, len(cl)))(*[t.data_ptr() for t in cl])
+        co = (ctypes.c_void_p * max(1, len(cc)))(*[t.data_ptr() for t in cc])
+        nat.check(nat.lib().pgb_sparse_dealloc(self._h, _ptr(field), ca, len(cl), co, len(cc), _ptr(flux),
+                                               _stream(stream)), "pgb_sparse_dealloc")
+
+    def sparse_tag(self, field, refine_tol, derefine_tol, stream=None):
+        """Per-block tag (-1/0/1, device tensor) of the sparse advection package's
+        min/max CheckRefinement over allocated variables."""
+        import torch
+        self._ensure()
+        out = torch.empty(self.nblocks, dtype=torch.float64, device="cuda")
+        nat.check(nat.lib().pgb_sparse_tag(self._h, _ptr(field), float(refine_tol), float(derefine_tol), _ptr(out),
+                                           _stream(stream)), "pgb_sparse_tag")
         return out
 
     @property

@@ -100,6 +100,48 @@ class BlockGeometry:
         return out
 
 
+# The sparse advection example's fields (example/sparse_advection/
+# sparse_advection_package.cpp:58-66): starting centres in the x-y plane, each field
+# moving diagonally away from its corner. The example is two-dimensional; here the
+# mesh is three-dimensional and the fields are spheres around z = 0 with vz = 0.
+SPARSE_X0 = (0.8, -0.8, -0.8, 0.8)
+SPARSE_Y0 = (0.8, 0.8, -0.8, -0.8)
+
+
+def sparse_advection_velocities(speed=1.5):
+    """(4, 3) velocities: field 0 moves along (-1,-1), 1 along (1,-1), 2 along (1,1),
+    3 along (-1,1), each at `speed` (sparse_advection_package.cpp:61-66)."""
+    s = speed / np.sqrt(2.0)
+    return np.array([[-s, -s, 0.0], [s, -s, 0.0], [s, s, 0.0], [-s, s, 0.0]])
+
+
+def sparse_advection_state(mesh, prev=None, prev_alloc=None, init_size=0.1, nfields=4):
+    """ProblemGenerator of the sparse advection example
+    (example/sparse_advection/parthenon_app_inputs.cpp:42-103) on the current block
+    list: field f is allocated on every block where some interior cell centre lies
+    within init_size of its centre, and there set to 1 inside and 0 outside; on other
+    blocks the field keeps `prev` and its allocation `prev_alloc` (the previous mesh's
+    data during the initial refinement). Returns (state, alloc)."""
+    shape = (mesh.nblocks, nfields) + tuple(mesh.N[::-1])
+    out = np.zeros(shape) if prev is None else np.array(prev, np.float64)
+    alloc = np.zeros((mesh.nblocks, nfields), np.uint8) if prev_alloc is None else np.array(prev_alloc, np.uint8)
+    xs, ys, zs = mesh.cell_centers()
+    sk, sj, si = _interior(mesh)
+    size = init_size * init_size
+    for f in range(nfields):
+        x = xs[:, si] - SPARSE_X0[f % 4]
+        y = ys[:, sj] - SPARSE_Y0[f % 4]
+        z = zs[:, sk]
+        # x*x + y*y + z*z in the example's order
+        r2 = (x[:, None, None, :] * x[:, None, None, :] + y[:, None, :, None] * y[:, None, :, None]) + \
+            z[:, :, None, None] * z[:, :, None, None]
+        inside = r2 < size
+        hit = inside.reshape(mesh.nblocks, -1).any(axis=1)
+        alloc[hit, f] = 1
+        out[hit, f, sk, sj, si] = inside[hit].astype(np.float64)
+    return out, alloc
+
+
 def burgers_amr_state(mesh, nscalars=2, nmodes=16, kmax=6, seed=5):
     """Adaptive Burgers initial data, a pure function of position so that it can be
     evaluated again on every refined mesh (as Mesh::Initialize re-runs the problem
