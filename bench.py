@@ -273,6 +273,8 @@ def run_ours(args, ws, rank):
     del drv, state, host_in, host_out
     if args.amr_cycles > 0:
         out["amr"] = amr_bench(torch, args.amr_cycles, with_cpu=(rank == 0 and ws == 1), root=args.amr_root)
+    if args.sparse_cycles > 0:
+        out["sparse"] = sparse_bench(torch, args.sparse_cycles, with_cpu=(rank == 0 and ws == 1))
     return out
 
 
@@ -423,6 +425,100 @@ def amr_cpu_baseline(torch, pg):
                       drv.mesh.nblocks}
 
 
+# Sparse advection (example/sparse_advection/parthinput.sparse_advection) in three
+# dimensions: [-1,1]^3, 64^3 root in 8^3 blocks, 2 ghosts, 3 levels, four sparse fields
+# (spheres of radius 0.1 moving diagonally at 1.5), donor cell, RK2, CFL 0.45;
+# allocation threshold 1e-5, deallocation threshold 1e-6 after 5 checks; tagging every
+# cycle (refine where max > 0.3 and min < 0.03, derefine where max < 0.03, 10 tags).
+SPARSE_ROOT, SPARSE_BLOCK, SPARSE_NG, SPARSE_NUMLEVEL, SPARSE_NFIELDS = 64, 8, 2, 3, 4
+
+
+def _sparse_driver(pg, root):
+    mesh = pg.Mesh((root,) * 3, (SPARSE_BLOCK,) * 3, SPARSE_NG, xmin=(-1.0,) * 3, xmax=(1.0,) * 3)
+    mesh.enable_sparse(SPARSE_NFIELDS, 1e-5, 1e-6, dealloc_count=5)
+    cfg = pg.StageConfig("advection", "dc", 0.45, comp_vel=pg.problems.sparse_advection_velocities(1.5))
+    return pg.AMRDriver(mesh, SPARSE_NFIELDS, cfg, pg.SparseMinMaxCriterion(0.3, 0.03), numlevel=SPARSE_NUMLEVEL,
+                        derefine_count=10, check_interval=1)
+
+
+def _sparse_pgen(pg):
+    return lambda m, prev, a: pg.problems.sparse_advection_state(m, prev, a, init_size=0.1)
+
+
+def sparse_bench(torch, cycles, with_cpu, root=SPARSE_ROOT):
+    """Adaptive sparse advection: zone-cycles/s over `cycles` cycles with the tagging
+    of every cycle, the remeshes (allocation carried over), the allocation on receipt
+    and the deallocation checks inside the timed region."""
+    import parthenon_gb300 as pg
+    drv = _sparse_driver(pg, root)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    drv.initialize(_sparse_pgen(pg))
+    torch.cuda.synchronize()
+    init_s = time.perf_counter() - t0
+    init_blocks = drv.mesh.nblocks
+    a0, _ = drv.mesh.sparse_alloc(drv.stream)
+    drv.run(2)  # warm-up: first graph capture on this mesh
+    torch.cuda.synchronize()
+    zc0, nr0, hist0 = drv.zone_cycles, drv.nremesh, len(drv.block_history)
+    t0 = time.perf_counter()
+    drv.run(cycles)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    zc = drv.zone_cycles - zc0
+    a, _ = drv.mesh.sparse_alloc(drv.stream)
+    blocks = drv.block_history[hist0 - 1:]
+    res = {
+        "value": zc / el, "unit": METRIC, "cycles": cycles, "seconds": el, "ms_per_cycle": 1e3 * el / cycles,
+        "zone_cycles": zc, "init_seconds": init_s, "blocks_after_init": init_blocks,
+        "blocks_min": int(min(blocks)), "blocks_max": int(max(blocks)), "blocks_final": drv.mesh.nblocks,
+        "remeshes": drv.nremesh - nr0, "allocated_fraction_init": float(a0.mean()),
+        "allocated_fraction_final": float(a.mean()),
+        "config": {"workload": "sparse-advection3d-%d^3root-8^3blocks-3levels-ng2-4sparse-fp64" % root,
+                   "sparse": "alloc 1e-5, dealloc 1e-6 after 5 checks, default 0",
+                   "criterion": "min/max over allocated fields: refine max>0.3 & min<0.03, derefine max<0.03",
+                   "check_interval": 1, "initial": "4 spheres r=0.1 at (+-0.8,+-0.8,0), speed 1.5 diagonal"},
+    }
+    if with_cpu:
+        res["cpu_baseline"] = sparse_cpu_baseline(torch, pg, drv)
+    del drv
+    return res
+
+
+def sparse_cpu_baseline(torch, pg, drv, cycles=8):
+    """The oracle (all host threads) continuing the GPU run's mesh, fields and
+    allocation for a few cycles, with the tagging and remesh of every cycle."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    drv.stream.synchronize()
+    locs, _ = drv.mesh.block_info()
+    o = O.OracleSim((SPARSE_ROOT,) * 3, (SPARSE_BLOCK,) * 3, SPARSE_NG, xmin=(-1.0,) * 3, xmax=(1.0,) * 3, leaves=locs,
+                    ncomp=SPARSE_NFIELDS, physics="advection", recon=0, cfl=0.45)
+    o.set_component_velocities(pg.problems.sparse_advection_velocities(1.5))
+    o.sparse_enable(1e-5, 1e-6, dealloc_count=5)
+    a, c = drv.mesh.sparse_alloc(drv.stream)
+    o.sparse_set(a, c)
+    o.base()[:] = drv.base.cpu().numpy()
+    o.exchange(True, 0)
+    o.init_dt()
+    mml = SPARSE_NUMLEVEL + drv.mesh.root_level - 1
+    threads = O.lib().orc_max_threads()
+    zones = 0
+    t0 = time.perf_counter()
+    for _ in range(cycles):
+        o.run(1, nthreads=threads)
+        zones += o.nblocks * SPARSE_BLOCK ** 3
+        t = o.sparse_tag(0.3, 0.03)
+        flags = o.set_refinement(t, 0.5, -0.5, mml, mml, 10)
+        if o.remesh(flags):
+            o.exchange(True, 0)
+            o.remesh_dt()
+    el = time.perf_counter() - t0
+    return {"value": zones / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "%d cycles (tag + remesh each) from the GPU run's final mesh of %d meshblocks of 8^3" %
+                      (cycles, len(locs))}
+
+
 def cpu_baseline(steps):
     """Oracle (CPU restatement of the reference) on all host threads, bounded sample."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -485,6 +581,10 @@ def main():
     ap.add_argument("--amr-only", action="store_true",
                     help="run only the adaptive leg (profiling runs), no CPU baseline")
     ap.add_argument("--gmg-only", action="store_true", help="run only the multigrid leg (profiling runs)")
+    ap.add_argument("--sparse-cycles", type=int, default=100,
+                    help="cycles of the adaptive sparse-advection leg (0 skips it)")
+    ap.add_argument("--sparse-only", action="store_true",
+                    help="run only the sparse-advection leg (with its CPU baseline)")
     args = ap.parse_args()
     ws, rank = _dist()
     if ws > 1:
@@ -498,6 +598,10 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         out = {"gmg": gmg_bench(torch)}
+    elif args.sparse_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        out = {"sparse": sparse_bench(torch, args.sparse_cycles, with_cpu=(rank == 0))}
     elif args.impl == "reference":
         out = run_reference(args, ws, rank)
     else:

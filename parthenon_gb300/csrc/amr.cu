@@ -294,8 +294,12 @@ int pgb_amr_remesh(pgb_mesh *mesh, const int32_t *flags, pgb_mesh **out) {
     const MeshTopology &topo = *st->topo;
     const auto &bl = topo.leaf().blocks;
     std::vector<int> fl(flags, flags + bl.size());
-    for (int f : fl)
+    bool any = false;
+    for (int f : fl) {
       if (f < -1 || f > 1) return fail(kErrInvalid, "flags must be -1, 0 or 1");
+      any = any || f != 0;
+    }
+    if (!any) return kOk;  // nothing tagged: the tree stays as it is
     std::vector<LLoc> nl = topo.amr_update(fl);
     bool same = nl.size() == topo.leaves().size();
     if (same) {

@@ -26,14 +26,15 @@ constexpr int kErrState = -4;
     if (e__ != cudaSuccess) return check_cuda(e__, #call); \
   } while (0)
 
-// Iterate over the rows (k, j) of a work item, with lanes spread over i. Narrow rows
-// (ghost slabs of depth ng) pack several rows into one warp so every lane has work.
+// Iterate over the rows (k, j) of a work item with `nt` threads (this one is number
+// `lt`), lanes spread over i. Narrow rows (ghost slabs of depth ng) pack several rows
+// into one warp so every lane has work. nt is a multiple of 32.
 template <class F>
-__device__ __forceinline__ void for_work_rows(int row0, int nrows, int ni, int nj, F &&f) {
+__device__ __forceinline__ void for_item_rows(int row0, int nrows, int ni, int nj, int lt, int nt, F &&f) {
   const int lpr = ni <= 1 ? 1 : ni <= 2 ? 2 : ni <= 4 ? 4 : ni <= 8 ? 8 : ni <= 16 ? 16 : 32;
-  const int sub = threadIdx.x / lpr;
-  const int li = threadIdx.x - sub * lpr;
-  const int step = blockDim.x / lpr;
+  const int sub = lt / lpr;
+  const int li = lt - sub * lpr;
+  const int step = nt / lpr;
   for (int r = sub; r < nrows; r += step) {
     const int rr = row0 + r;
     const int k = rr / nj;
@@ -41,6 +42,20 @@ __device__ __forceinline__ void for_work_rows(int row0, int nrows, int ni, int n
     for (int i = li; i < ni; i += lpr) f(k, j, i);
   }
 }
+
+// The same with the whole CTA on one work item.
+template <class F>
+__device__ __forceinline__ void for_work_rows(int row0, int nrows, int ni, int nj, F &&f) {
+  for_item_rows(row0, nrows, ni, nj, (int)threadIdx.x, (int)blockDim.x, f);
+}
+
+// Warp-per-item launches: the boxes of small blocks hold a few dozen to a few hundred
+// cells, so a CTA per box leaves most of its threads idle and the launch is bound by
+// CTA scheduling; here each warp takes one (item, component) and a CTA of kItemWarps
+// warps takes consecutive ones.
+constexpr int kItemWarps = 8;
+__device__ __forceinline__ int warp_item() { return (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); }
+inline unsigned warp_item_grid(int64_t items) { return (unsigned)((items + kItemWarps - 1) / kItemWarps); }
 
 __device__ __forceinline__ int64_t fine_index(const Dims &d, int ncomp, int b, int v, int k, int j, int i) {
   return (((int64_t)b * ncomp + v) * d.N[2] + k) * (int64_t)(d.N[1] * d.N[0]) + (int64_t)j * d.N[0] + i;

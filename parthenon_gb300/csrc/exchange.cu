@@ -380,18 +380,21 @@ __global__ void __launch_bounds__(128) k_unpack(const DevPair *__restrict__ pair
 
 // RestrictAverage (pr_ops.hpp:105-164): volume-weighted mean of the 2x2x2 fine cells,
 // summed in the reference's pairing order.
-__global__ void __launch_bounds__(128) k_restrict(const DevRegion *__restrict__ regs,
-                                                  const DevWork *__restrict__ work,
+// One warp per (work item, component).
+__global__ void __launch_bounds__(256) k_restrict(const DevRegion *__restrict__ regs,
+                                                  const DevWork *__restrict__ work, int nwork,
                                                   const DevBlockGeom *__restrict__ geom, Dims d,
                                                   int ncomp, const double *__restrict__ fine,
                                                   double *__restrict__ coarse, const uint8_t *__restrict__ alloc) {
-  const DevWork w = work[blockIdx.x];
+  const int q = warp_item();
+  if (q >= nwork * ncomp) return;
+  const int wi = q / ncomp, v = q - wi * ncomp;
+  const DevWork w = work[wi];
   const DevRegion r = regs[w.item];
-  const int v = blockIdx.y;
   if (alloc && !alloc[r.block * ncomp + v]) return;  // unallocated sparse variable
   const double vol = geom[r.block].vol;
   const int ng = d.ng;
-  for_work_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], [&](int k, int j, int i) {
+  for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
     const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
     if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
     const int fi = (ci - ng) * 2 + ng, fj = (cj - ng) * 2 + ng, fk = (ck - ng) * 2 + ng;
@@ -416,19 +419,22 @@ __device__ __forceinline__ double sign1(double x) { return x < 0.0 ? -1.0 : 1.0;
 // ProlongateSharedGeneral (pr_ops.hpp:166-285): op 0 minmod, 1 linear, 2 constant.
 // Written with explicit round-to-nearest intrinsics so no FMA contraction changes
 // the result relative to the reference's separately rounded host arithmetic.
-__global__ void __launch_bounds__(128) k_prolong(const DevRegion *__restrict__ regs,
-                                                 const DevWork *__restrict__ work,
+// One warp per (work item, component).
+__global__ void __launch_bounds__(256) k_prolong(const DevRegion *__restrict__ regs,
+                                                 const DevWork *__restrict__ work, int nwork,
                                                  const DevBlockGeom *__restrict__ geom, Dims d,
                                                  int ncomp, double *__restrict__ fine,
                                                  const double *__restrict__ coarse, int op,
                                                  const uint8_t *__restrict__ alloc) {
-  const DevWork w = work[blockIdx.x];
+  const int q = warp_item();
+  if (q >= nwork * ncomp) return;
+  const int wi = q / ncomp, v = q - wi * ncomp;
+  const DevWork w = work[wi];
   const DevRegion r = regs[w.item];
-  const int v = blockIdx.y;
   if (alloc && !alloc[r.block * ncomp + v]) return;  // unallocated sparse variable
   const DevBlockGeom g = geom[r.block];
   const int ng = d.ng;
-  for_work_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], [&](int k, int j, int i) {
+  for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
     const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
     if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
     const int c[3] = {ci, cj, ck};
@@ -472,14 +478,16 @@ __global__ void __launch_bounds__(128) k_prolong(const DevRegion *__restrict__ r
 // Flux correction (SendBoundBufs<flxcor_send> + SetBounds<flxcor_recv>) fused: the
 // area-weighted mean of the 2x2 fine face fluxes is written straight into the coarse
 // block's face flux. Flux arrays: [block][dir][comp][N3][N2][N1].
-__global__ void __launch_bounds__(128) k_flux_correct(const DevFluxCorr *__restrict__ fcs,
-                                                      const DevWork *__restrict__ work,
+__global__ void __launch_bounds__(256) k_flux_correct(const DevFluxCorr *__restrict__ fcs,
+                                                      const DevWork *__restrict__ work, int nwork,
                                                       const DevBlockGeom *__restrict__ geom, Dims d,
                                                       int ncomp, double *__restrict__ flux,
                                                       const uint8_t *__restrict__ send) {
-  const DevWork w = work[blockIdx.x];
+  const int q = warp_item();  // one warp per (work item, component)
+  if (q >= nwork * ncomp) return;
+  const int wi = q / ncomp, v = q - wi * ncomp;
+  const DevWork w = work[wi];
   const DevFluxCorr c = fcs[w.item];
-  const int v = blockIdx.y;
   if (send && !send[(int64_t)w.item * ncomp + v]) return;  // null buffer: coarse flux kept
   const int ng = d.ng;
   const double a = geom[c.fine_block].area[c.dir];
@@ -487,7 +495,7 @@ __global__ void __launch_bounds__(128) k_flux_correct(const DevFluxCorr *__restr
   auto fidx = [&](int b, int k, int j, int i) {
     return (((int64_t)b * 3 + c.dir) * ncomp + v) * plane + ((int64_t)k * d.N[1] + j) * d.N[0] + i;
   };
-  for_work_rows(w.row0, w.nrows, c.fine.n[0], c.fine.n[1], [&](int k, int j, int i) {
+  for_item_rows(w.row0, w.nrows, c.fine.n[0], c.fine.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
     const int ck = c.fine.lo[2] + k, cj = c.fine.lo[1] + j, ci = c.fine.lo[0] + i;
     const int fi = (ci - ng) * 2 + ng, fj = (cj - ng) * 2 + ng, fk = (ck - ng) * 2 + ng;
     // the two tangential directions of the face
@@ -529,7 +537,8 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
   const uint8_t *alloc = sp ? sp->alloc : nullptr;
   const dim3 blk(128);
   if (t.multilevel && t.nrs_work)
-    k_restrict<<<dim3(t.nrs_work, ncomp), blk, 0, s>>>(t.rs, t.rs_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
+    k_restrict<<<warp_item_grid((int64_t)t.nrs_work * ncomp), 32 * kItemWarps, 0, s>>>(
+        t.rs, t.rs_work, t.nrs_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
   if (sp) {
     int rc = sparse_exchange_copy(t, *sp, fine, coarse, ncomp, s);
     if (rc) return rc;
@@ -551,10 +560,11 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
     }
   }
   if (t.multilevel && t.nrr_work)
-    k_restrict<<<dim3(t.nrr_work, ncomp), blk, 0, s>>>(t.rr, t.rr_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
+    k_restrict<<<warp_item_grid((int64_t)t.nrr_work * ncomp), 32 * kItemWarps, 0, s>>>(
+        t.rr, t.rr_work, t.nrr_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
   if (t.multilevel && prolongate && t.npro_work)
-    k_prolong<<<dim3(t.npro_work, ncomp), blk, 0, s>>>(t.pro, t.pro_work, t.geom, t.dims, ncomp, fine, coarse,
-                                                       prolong_op, alloc);
+    k_prolong<<<warp_item_grid((int64_t)t.npro_work * ncomp), 32 * kItemWarps, 0, s>>>(
+        t.pro, t.pro_work, t.npro_work, t.geom, t.dims, ncomp, fine, coarse, prolong_op, alloc);
   PGB_CUDA(cudaGetLastError());
   return kOk;
 }
@@ -576,8 +586,8 @@ int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s, co
     int rc = sparse_flux_flags(t, *sp, ncomp, s);
     if (rc) return rc;
   }
-  k_flux_correct<<<dim3(t.nfc_work, ncomp), dim3(128), 0, s>>>(t.fc, t.fc_work, t.geom, t.dims, ncomp, flux,
-                                                               sp ? sp->fc_flag : nullptr);
+  k_flux_correct<<<warp_item_grid((int64_t)t.nfc_work * ncomp), 32 * kItemWarps, 0, s>>>(
+      t.fc, t.fc_work, t.nfc_work, t.geom, t.dims, ncomp, flux, sp ? sp->fc_flag : nullptr);
   PGB_CUDA(cudaGetLastError());
   return kOk;
 }

@@ -117,7 +117,8 @@ int estimate_dt(MeshState &m, int physics, const double *u, int ncomp, const dou
     vt.n = ncvel ? ncvel : 1;
     for (int c = 0; c < vt.n; ++c)
       for (int q = 0; q < 3; ++q) vt.v[c][q] = ncvel ? cvel[3 * c + q] : vel[q];
-    k_advection_min<<<1, 256, 0, s>>>(t.geom, t.nblocks, vt, m.d_minbits);
+    // one thread per block
+    k_advection_min<<<(t.nblocks + 255) / 256, 256, 0, s>>>(t.geom, t.nblocks, vt, m.d_minbits);
   }
   k_set_dt<<<1, 1, 0, s>>>(dt, m.d_minbits, cfl, first);
   PGB_CUDA(cudaGetLastError());

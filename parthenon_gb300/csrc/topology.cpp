@@ -2,11 +2,49 @@
 #include "topology.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <exception>
+#include <mutex>
 #include <stdexcept>
+#include <thread>
 
 namespace pgb {
 
 namespace {
+// Runs f(i) for i in [0, n) on the host's cores (work is handed out in chunks). The
+// first exception thrown by any f is rethrown on the calling thread.
+template <class F>
+void parallel_for(int n, F &&f) {
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::min({hw, 32, n / 64});
+  if (nt <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::exception_ptr err;
+  std::mutex mu;
+  auto work = [&] {
+    try {
+      for (;;) {
+        const int s = next.fetch_add(16);
+        if (s >= n) break;
+        const int e = std::min(n, s + 16);
+        for (int i = s; i < e; ++i) f(i);
+      }
+    } catch (...) {
+      std::lock_guard<std::mutex> lk(mu);
+      if (!err) err = std::current_exception();
+      next.store(n);
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(work);
+  work();
+  for (auto &t : th) t.join();
+  if (err) std::rethrow_exception(err);
+}
+
 // Interleave the low 21 bits of v with two zero bits between each.
 inline uint64_t interleave3(uint64_t v) {
   v &= 0x1FFFFFull;
@@ -124,7 +162,25 @@ static inline int topo_offset(int el, int d) {
   return 0;
 }
 
+namespace {
+Mask27 element_mask_uncached(int el, Mask27 owner, int ox1, int ox2, int ox3);
+}
+
 Mask27 element_mask_from_ownership(int el, Mask27 owner, int ox1, int ox2, int ox3) {
+  // a pure function of a few small integers that the table builder evaluates hundreds
+  // of thousands of times on a few distinct arguments: memoised per thread
+  thread_local std::unordered_map<uint64_t, Mask27> memo;
+  const uint64_t key = (uint64_t)el | ((uint64_t)owner << 3) |
+                       ((uint64_t)((ox1 + 1) + 3 * (ox2 + 1) + 9 * (ox3 + 1)) << 30);
+  auto it = memo.find(key);
+  if (it != memo.end()) return it->second;
+  const Mask27 m = element_mask_uncached(el, owner, ox1, ox2, ox3);
+  if (memo.size() < (1u << 16)) memo.emplace(key, m);
+  return m;
+}
+
+namespace {
+Mask27 element_mask_uncached(int el, Mask27 owner, int ox1, int ox2, int ox3) {
   // block_ownership.cpp:89-142: map block ownership onto the element's index range,
   // then treat the interior-facing edges of the sent region as owned.
   Mask27 e = 0;
@@ -150,6 +206,7 @@ Mask27 element_mask_from_ownership(int el, Mask27 owner, int ox1, int ox2, int o
       for (int b = -1; b <= 1; ++b) copy_from(a, b, -ox3, a, b, 0);
   return e;
 }
+}  // namespace
 
 // ------------------------------------------------------------------ index boxes
 IBox boundary_box(const Neighbor &nb, const LLoc &me, const std::array<int, 3> &bnx, int ng,
@@ -267,11 +324,33 @@ MeshTopology::MeshTopology(const MeshSpec &spec, const std::vector<LLoc> &leaves
   for (auto &l : lv) max_level_ = std::max(max_level_, l.level);
   leaf_.logical_level = max_level_;
   leaf_.multilevel = max_level_ > root_level_;
-  for (auto &l : lv) {
+  // Every block's neighbours, their ownership and then the boundary tables are
+  // independent per block: built in parallel on the host's cores. Ownership of every
+  // leaf first (the neighbour lists read it), into the cache the serial paths use.
+  for (auto &l : lv) l.key();  // Morton keys are computed lazily; fix them before sharing
+  std::vector<Mask27> own(lv.size());
+  parallel_for((int)lv.size(), [&](int i) { own[i] = ownership_among(lv[i], neighbors_of(lv[i], kLeaf, 0)); });
+  auto &cache = own_cache_[{(int)kLeaf, 0}];
+  cache.reserve(lv.size());
+  for (size_t i = 0; i < lv.size(); ++i) cache.emplace(lv[i], own[i]);
+  const auto &owns = cache;
+  leaf_.blocks.resize(lv.size());
+  parallel_for((int)lv.size(), [&](int i) {
+    const LLoc &l = lv[i];
     BlockInfo b = make_block(l);
-    for (auto &n : neighbors_of(l, kLeaf, 0)) b.nbrs.push_back(make_neighbor(l, n.first, n.second, kLeaf, 0));
-    leaf_.blocks.push_back(std::move(b));
-  }
+    for (auto &n : neighbors_of(l, kLeaf, 0)) {
+      Neighbor nb;
+      nb.gid = gid_of(n.first);
+      nb.where = n.first;
+      nb.origin = n.second;
+      nb.off = l.offsets_to(n.second);
+      auto it = owns.find(n.first);
+      nb.owns = it != owns.end() ? it->second : ownership_among(n.first, neighbors_of(n.first, kLeaf, 0));
+      block_nx(n.first, nb.nx);
+      b.nbrs.push_back(nb);
+    }
+    leaf_.blocks[i] = std::move(b);
+  });
   build_grid_tables(leaf_, false);
 }
 
@@ -395,8 +474,12 @@ void MeshTopology::build_grid_tables(GridTopology &g, bool composite) {
   g.restrict_recv.clear();
   g.prolong.clear();
   g.flux_corr.clear();
-  for (size_t r = 0; r < g.blocks.size(); ++r) {
+  // per-block lists built in parallel, then joined in block order
+  const int nblk = (int)g.blocks.size();
+  std::vector<std::vector<CopyPair>> pairs_of(nblk);
+  parallel_for(nblk, [&](int r) {
     BlockInfo &rb = g.blocks[r];
+    pairs_of[r].reserve(list(rb).size());
     for (auto &nb : list(rb)) {
       if (nb.gid == rb.gid && nb.self_offset()) continue;
       auto it = index.find(nb.gid);
@@ -419,24 +502,31 @@ void MeshTopology::build_grid_tables(GridTopology &g, bool composite) {
                             false, false);
       p.recv_coarse = nb.origin.level < rb.loc.level;
       if (p.send.count() != p.recv.count()) throw std::runtime_error("boundary box size mismatch");
-      g.pairs.push_back(p);
+      pairs_of[r].push_back(p);
     }
-  }
+  });
+  size_t npairs = 0;
+  for (auto &v : pairs_of) npairs += v.size();
+  g.pairs.reserve(npairs);
+  for (auto &v : pairs_of) g.pairs.insert(g.pairs.end(), v.begin(), v.end());
   if (!g.multilevel) return;
-  for (size_t b = 0; b < g.blocks.size(); ++b) {
+  struct PerBlock {
+    std::vector<CoarseRegion> rs, rr, pro;
+    std::vector<FluxCorrection> fc;
+  };
+  std::vector<PerBlock> per(nblk);
+  parallel_for(nblk, [&](int b) {
     BlockInfo &bl = g.blocks[b];
+    PerBlock &out = per[b];
     const int my = bl.loc.level;
     bool has_coarser = false;
     for (auto &nb : list(bl)) has_coarser = has_coarser || nb.origin.level == my - 1;
     for (auto &nb : list(bl)) {
       if (nb.origin.level < my) {
-        g.restrict_send.push_back(
-            {(int)b, boundary_box(nb, bl.loc, bl.nx, ng, 0, RangeKind::BoundaryInteriorSend, true, false)});
-        g.prolong.push_back(
-            {(int)b, boundary_box(nb, bl.loc, bl.nx, ng, 0, RangeKind::BoundaryExteriorRecv, true, false)});
+        out.rs.push_back({b, boundary_box(nb, bl.loc, bl.nx, ng, 0, RangeKind::BoundaryInteriorSend, true, false)});
+        out.pro.push_back({b, boundary_box(nb, bl.loc, bl.nx, ng, 0, RangeKind::BoundaryExteriorRecv, true, false)});
       } else if (has_coarser && my > 0) {
-        g.restrict_recv.push_back(
-            {(int)b, boundary_box(nb, bl.loc, bl.nx, ng, 0, RangeKind::BoundaryExteriorRecv, true, false)});
+        out.rr.push_back({b, boundary_box(nb, bl.loc, bl.nx, ng, 0, RangeKind::BoundaryExteriorRecv, true, false)});
       }
     }
     // flux correction: this block is the fine side of a face with a coarser block
@@ -446,7 +536,7 @@ void MeshTopology::build_grid_tables(GridTopology &g, bool composite) {
         if (std::abs(nb.off[0]) + std::abs(nb.off[1]) + std::abs(nb.off[2]) != 1) continue;
         const int dir = nb.off[0] ? 0 : (nb.off[1] ? 1 : 2);
         FluxCorrection fc;
-        fc.fine = (int)b;
+        fc.fine = b;
         fc.dir = dir;
         fc.fine_box = boundary_box(nb, bl.loc, bl.nx, ng, 3 + dir, RangeKind::BoundaryInteriorSend, true, true);
         fc.coarse = index.at(nb.gid);
@@ -462,9 +552,15 @@ void MeshTopology::build_grid_tables(GridTopology &g, bool composite) {
         for (int d = 0; d < 3; ++d)
           if (sendb.lo[d] != fc.fine_box.lo[d] || sendb.hi[d] != fc.fine_box.hi[d])
             throw std::runtime_error("flux-correction send box differs from its restriction box");
-        g.flux_corr.push_back(fc);
+        out.fc.push_back(fc);
       }
     }
+  });
+  for (auto &pb : per) {
+    g.restrict_send.insert(g.restrict_send.end(), pb.rs.begin(), pb.rs.end());
+    g.restrict_recv.insert(g.restrict_recv.end(), pb.rr.begin(), pb.rr.end());
+    g.prolong.insert(g.prolong.end(), pb.pro.begin(), pb.pro.end());
+    g.flux_corr.insert(g.flux_corr.end(), pb.fc.begin(), pb.fc.end());
   }
 }
 
