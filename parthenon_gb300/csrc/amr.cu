@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) k_block_criterion(const double *__restric
     } else {
       double g[3];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) g[a] = __ddiv_rn(__dmul_rn(0.5, __dsub_rn(q[e + st[a]], q[e - st[a]])), geom[b].dx[a]);
+      for (int a = 0; a < 3; ++a) g[a] = div_rn(__dmul_rn(0.5, __dsub_rn(q[e + st[a]], q[e - st[a]])), geom[b].dx[a]);
       m = ordered_max(m, __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(g[0], g[0]), __dmul_rn(g[1], g[1])), __dmul_rn(g[2], g[2]))));
     }
   }
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(256) k_transfer(const DevRemap *__restrict__ m
         dfp[q] = __dsub_rn(xfc(fi0 + 1), xc);
         const int dk = q == 2, dj = q == 1, di = q == 0;
         const double nm = P(c[2] - dk, c[1] - dj, c[0] - di), np = P(c[2] + dk, c[1] + dj, c[0] + di);
-        const double a = __ddiv_rn(__dsub_rn(fc, nm), dxm), bb = __ddiv_rn(__dsub_rn(np, fc), dxp);
+        const double a = div_rn(__dsub_rn(fc, nm), dxm), bb = div_rn(__dsub_rn(np, fc), dxp);
         const double mm = __dmul_rn(__dmul_rn(0.5, __dadd_rn(sgn1(a), sgn1(bb))), smin(fabs(a), fabs(bb)));
         gm[q] = mm;
         gp[q] = mm;
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(256) k_transfer(const DevRemap *__restrict__ m
     const double tv = __dadd_rn(__dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)), __dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)));
     const double num = __dadd_rn(__dadd_rn(__dadd_rn(t[0][0][0], t[0][1][0]), __dadd_rn(t[0][0][1], t[0][1][1])),
                                  __dadd_rn(__dadd_rn(t[1][0][0], t[1][1][0]), __dadd_rn(t[1][0][1], t[1][1][1])));
-    dst[e] = __ddiv_rn(num, tv);
+    dst[e] = div_rn(num, tv);
   }
 }
 

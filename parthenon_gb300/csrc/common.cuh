@@ -64,6 +64,20 @@ __device__ __forceinline__ int64_t coarse_index(const Dims &d, int ncomp, int b,
   return (((int64_t)b * ncomp + v) * d.Nc[2] + k) * (int64_t)(d.Nc[1] * d.Nc[0]) + (int64_t)j * d.Nc[0] + i;
 }
 
+// x / d with IEEE round-to-nearest. When d is a power of two whose reciprocal is a
+// normal number, x * (1/d) is the same exact real quotient rounded once, so the result
+// is identical and the FP64 divide (about 20 FMA issue slots on GB300) becomes one
+// multiply. Block spacings of power-of-two meshes on power-of-two extents hit this.
+__device__ __forceinline__ double div_rn(double x, double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
+  if ((b & 0xFFFFFFFFFFFFFull) == 0 && e >= 1 && e <= 2045) {
+    const unsigned long long rb = (b & 0x8000000000000000ull) | ((unsigned long long)(2046 - e) << 52);
+    return __dmul_rn(x, __longlong_as_double((long long)rb));
+  }
+  return __ddiv_rn(x, d);
+}
+
 // std::min / std::max semantics (first argument returned on ties and NaN) so that
 // signed zeros and NaNs propagate exactly as in the reference host code.
 __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }

@@ -380,38 +380,39 @@ __global__ void __launch_bounds__(128) k_unpack(const DevPair *__restrict__ pair
 
 // RestrictAverage (pr_ops.hpp:105-164): volume-weighted mean of the 2x2x2 fine cells,
 // summed in the reference's pairing order.
-// One warp per (work item, component).
+// One warp per work item, components in turn.
 __global__ void __launch_bounds__(256) k_restrict(const DevRegion *__restrict__ regs,
                                                   const DevWork *__restrict__ work, int nwork,
                                                   const DevBlockGeom *__restrict__ geom, Dims d,
                                                   int ncomp, const double *__restrict__ fine,
                                                   double *__restrict__ coarse, const uint8_t *__restrict__ alloc) {
-  const int q = warp_item();
-  if (q >= nwork * ncomp) return;
-  const int wi = q / ncomp, v = q - wi * ncomp;
+  const int wi = warp_item();
+  if (wi >= nwork) return;
   const DevWork w = work[wi];
   const DevRegion r = regs[w.item];
-  if (alloc && !alloc[r.block * ncomp + v]) return;  // unallocated sparse variable
   const double vol = geom[r.block].vol;
   const int ng = d.ng;
-  for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
-    const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
-    if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
-    const int fi = (ci - ng) * 2 + ng, fj = (cj - ng) * 2 + ng, fk = (ck - ng) * 2 + ng;
-    double t[2][2][2];
-#pragma unroll
-    for (int ok = 0; ok < 2; ++ok)
-#pragma unroll
-      for (int oj = 0; oj < 2; ++oj)
-#pragma unroll
-        for (int oi = 0; oi < 2; ++oi)
-          t[ok][oj][oi] = __dmul_rn(vol, fine[fine_index(d, ncomp, r.block, v, fk + ok, fj + oj, fi + oi)]);
-    const double tv = __dadd_rn(__dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)),
-                                __dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)));
-    const double num = __dadd_rn(__dadd_rn(__dadd_rn(t[0][0][0], t[0][1][0]), __dadd_rn(t[0][0][1], t[0][1][1])),
-                                 __dadd_rn(__dadd_rn(t[1][0][0], t[1][1][0]), __dadd_rn(t[1][0][1], t[1][1][1])));
-    coarse[coarse_index(d, ncomp, r.block, v, ck, cj, ci)] = __ddiv_rn(num, tv);
-  });
+  for (int v = 0; v < ncomp; ++v) {
+    if (alloc && !alloc[r.block * ncomp + v]) continue;  // unallocated sparse variable
+    for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
+      const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
+      if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
+      const int fi = (ci - ng) * 2 + ng, fj = (cj - ng) * 2 + ng, fk = (ck - ng) * 2 + ng;
+      double t[2][2][2];
+  #pragma unroll
+      for (int ok = 0; ok < 2; ++ok)
+  #pragma unroll
+        for (int oj = 0; oj < 2; ++oj)
+  #pragma unroll
+          for (int oi = 0; oi < 2; ++oi)
+            t[ok][oj][oi] = __dmul_rn(vol, fine[fine_index(d, ncomp, r.block, v, fk + ok, fj + oj, fi + oi)]);
+      const double tv = __dadd_rn(__dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)),
+                                  __dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)));
+      const double num = __dadd_rn(__dadd_rn(__dadd_rn(t[0][0][0], t[0][1][0]), __dadd_rn(t[0][0][1], t[0][1][1])),
+                                   __dadd_rn(__dadd_rn(t[1][0][0], t[1][1][0]), __dadd_rn(t[1][0][1], t[1][1][1])));
+      coarse[coarse_index(d, ncomp, r.block, v, ck, cj, ci)] = div_rn(num, tv);
+    });
+  }
 }
 
 __device__ __forceinline__ double sign1(double x) { return x < 0.0 ? -1.0 : 1.0; }
@@ -419,60 +420,65 @@ __device__ __forceinline__ double sign1(double x) { return x < 0.0 ? -1.0 : 1.0;
 // ProlongateSharedGeneral (pr_ops.hpp:166-285): op 0 minmod, 1 linear, 2 constant.
 // Written with explicit round-to-nearest intrinsics so no FMA contraction changes
 // the result relative to the reference's separately rounded host arithmetic.
-// One warp per (work item, component).
-__global__ void __launch_bounds__(256) k_prolong(const DevRegion *__restrict__ regs,
+// One warp per work item, components in turn.
+__global__ void __launch_bounds__(256, 2) k_prolong(const DevRegion *__restrict__ regs,
                                                  const DevWork *__restrict__ work, int nwork,
                                                  const DevBlockGeom *__restrict__ geom, Dims d,
                                                  int ncomp, double *__restrict__ fine,
                                                  const double *__restrict__ coarse, int op,
                                                  const uint8_t *__restrict__ alloc) {
-  const int q = warp_item();
-  if (q >= nwork * ncomp) return;
-  const int wi = q / ncomp, v = q - wi * ncomp;
+  const int wi = warp_item();
+  if (wi >= nwork) return;
   const DevWork w = work[wi];
   const DevRegion r = regs[w.item];
-  if (alloc && !alloc[r.block * ncomp + v]) return;  // unallocated sparse variable
-  const DevBlockGeom g = geom[r.block];
-  const int ng = d.ng;
-  for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
-    const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
-    if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
-    const int c[3] = {ci, cj, ck};
-    const int f[3] = {(ci - ng) * 2 + ng, (cj - ng) * 2 + ng, (ck - ng) * 2 + ng};
-    const double fc = coarse[coarse_index(d, ncomp, r.block, v, ck, cj, ci)];
-    double gm[3], gp[3], dfm[3], dfp[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      auto xcc = [&](int idx) { return __dadd_rn(g.cxmin[q], __dmul_rn(__dadd_rn((double)idx, 0.5), g.cdx[q])); };
-      auto xfc = [&](int idx) { return __dadd_rn(g.xmin[q], __dmul_rn(__dadd_rn((double)idx, 0.5), g.dx[q])); };
-      const double xm = xcc(c[q] - 1), xc = xcc(c[q]), xp = xcc(c[q] + 1);
-      const double dxm = __dsub_rn(xc, xm), dxp = __dsub_rn(xp, xc);
-      dfm[q] = __dsub_rn(xc, xfc(f[q]));
-      dfp[q] = __dsub_rn(xfc(f[q] + 1), xc);
-      const int dk = q == 2, dj = q == 1, di = q == 0;
-      const double nm = coarse[coarse_index(d, ncomp, r.block, v, ck - dk, cj - dj, ci - di)];
-      const double np = coarse[coarse_index(d, ncomp, r.block, v, ck + dk, cj + dj, ci + di)];
-      const double a = __ddiv_rn(__dsub_rn(fc, nm), dxm);
-      const double b = __ddiv_rn(__dsub_rn(np, fc), dxp);
-      const double mm = __dmul_rn(__dmul_rn(0.5, __dadd_rn(sign1(a), sign1(b))), smin(fabs(a), fabs(b)));
-      gm[q] = op == 0 ? mm : (op == 1 ? a : 0.0);
-      gp[q] = op == 0 ? mm : (op == 1 ? b : 0.0);
-    }
-    const double m0 = __dmul_rn(gm[0], dfm[0]), p0 = __dmul_rn(gp[0], dfp[0]);
-    const double m1 = __dmul_rn(gm[1], dfm[1]), p1 = __dmul_rn(gp[1], dfp[1]);
-    const double m2 = __dmul_rn(gm[2], dfm[2]), p2 = __dmul_rn(gp[2], dfp[2]);
-    auto F = [&](int ok, int oj, int oi) -> double & {
-      return fine[fine_index(d, ncomp, r.block, v, f[2] + ok, f[1] + oj, f[0] + oi)];
-    };
-    F(0, 0, 0) = __dsub_rn(fc, __dadd_rn(__dadd_rn(m0, m1), m2));
-    F(0, 0, 1) = __dadd_rn(fc, __dsub_rn(__dsub_rn(p0, m1), m2));
-    F(0, 1, 0) = __dsub_rn(fc, __dadd_rn(__dsub_rn(m0, p1), m2));
-    F(0, 1, 1) = __dadd_rn(fc, __dsub_rn(__dadd_rn(p0, p1), m2));
-    F(1, 0, 0) = __dsub_rn(fc, __dsub_rn(__dadd_rn(m0, m1), p2));
-    F(1, 0, 1) = __dadd_rn(fc, __dadd_rn(__dsub_rn(p0, m1), p2));
-    F(1, 1, 0) = __dsub_rn(fc, __dsub_rn(__dsub_rn(m0, p1), p2));
-    F(1, 1, 1) = __dadd_rn(fc, __dadd_rn(__dadd_rn(p0, p1), p2));
-  });
+  for (int v = 0; v < ncomp; ++v) {
+    if (alloc && !alloc[r.block * ncomp + v]) continue;  // unallocated sparse variable
+    // geometry read through the pointer, and each direction's two slope products formed
+    // as soon as they exist: keeps the kernel near 64 registers (4 CTAs of 8 warps)
+    const DevBlockGeom *__restrict__ g = geom + r.block;
+    const int ng = d.ng;
+    const double *__restrict__ cb = coarse + coarse_index(d, ncomp, r.block, v, 0, 0, 0);
+    const int64_t cs1 = d.Nc[0], cs2 = (int64_t)d.Nc[0] * d.Nc[1];
+    for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
+      const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
+      if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
+      const int c[3] = {ci, cj, ck};
+      const int f[3] = {(ci - ng) * 2 + ng, (cj - ng) * 2 + ng, (ck - ng) * 2 + ng};
+      const int64_t ce = ck * cs2 + cj * cs1 + ci;
+      const double fc = cb[ce];
+      double mq[3], pq[3];
+  #pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const double cx0 = g->cxmin[q], cdx = g->cdx[q], x0 = g->xmin[q], dx = g->dx[q];
+        auto xcc = [&](int idx) { return __dadd_rn(cx0, __dmul_rn(__dadd_rn((double)idx, 0.5), cdx)); };
+        auto xfc = [&](int idx) { return __dadd_rn(x0, __dmul_rn(__dadd_rn((double)idx, 0.5), dx)); };
+        const double xm = xcc(c[q] - 1), xc = xcc(c[q]), xp = xcc(c[q] + 1);
+        const double dxm = __dsub_rn(xc, xm), dxp = __dsub_rn(xp, xc);
+        const double dfm = __dsub_rn(xc, xfc(f[q]));
+        const double dfp = __dsub_rn(xfc(f[q] + 1), xc);
+        const int64_t st = q == 0 ? 1 : (q == 1 ? cs1 : cs2);
+        const double nm = cb[ce - st], np = cb[ce + st];
+        const double a = div_rn(__dsub_rn(fc, nm), dxm);
+        const double b = div_rn(__dsub_rn(np, fc), dxp);
+        const double mm = __dmul_rn(__dmul_rn(0.5, __dadd_rn(sign1(a), sign1(b))), smin(fabs(a), fabs(b)));
+        const double gm = op == 0 ? mm : (op == 1 ? a : 0.0);
+        const double gp = op == 0 ? mm : (op == 1 ? b : 0.0);
+        mq[q] = __dmul_rn(gm, dfm);
+        pq[q] = __dmul_rn(gp, dfp);
+      }
+      const double m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
+      double *F = fine + fine_index(d, ncomp, r.block, v, f[2], f[1], f[0]);
+      const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1];
+      F[0] = __dsub_rn(fc, __dadd_rn(__dadd_rn(m0, m1), m2));
+      F[1] = __dadd_rn(fc, __dsub_rn(__dsub_rn(p0, m1), m2));
+      F[N0] = __dsub_rn(fc, __dadd_rn(__dsub_rn(m0, p1), m2));
+      F[N0 + 1] = __dadd_rn(fc, __dsub_rn(__dadd_rn(p0, p1), m2));
+      F[N01] = __dsub_rn(fc, __dsub_rn(__dadd_rn(m0, m1), p2));
+      F[N01 + 1] = __dadd_rn(fc, __dadd_rn(__dsub_rn(p0, m1), p2));
+      F[N01 + N0] = __dsub_rn(fc, __dsub_rn(__dsub_rn(m0, p1), p2));
+      F[N01 + N0 + 1] = __dadd_rn(fc, __dadd_rn(__dadd_rn(p0, p1), p2));
+    });
+  }
 }
 
 // Flux correction (SendBoundBufs<flxcor_send> + SetBounds<flxcor_recv>) fused: the
@@ -512,7 +518,7 @@ __global__ void __launch_bounds__(256) k_flux_correct(const DevFluxCorr *__restr
                                 __dadd_rn(__dadd_rn(vv[1][0][0], vv[1][1][0]), __dadd_rn(vv[1][0][1], vv[1][1][1])));
     const double num = __dadd_rn(__dadd_rn(__dadd_rn(t[0][0][0], t[0][1][0]), __dadd_rn(t[0][0][1], t[0][1][1])),
                                  __dadd_rn(__dadd_rn(t[1][0][0], t[1][1][0]), __dadd_rn(t[1][0][1], t[1][1][1])));
-    const double val = __ddiv_rn(num, tv);
+    const double val = div_rn(num, tv);
     // element m of the restriction box lands on element m of the receive box
     const int64_t m = ((int64_t)k * c.fine.n[1] + j) * c.fine.n[0] + i;
     const int ri = (int)(m % c.recv.n[0]);
@@ -537,7 +543,7 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
   const uint8_t *alloc = sp ? sp->alloc : nullptr;
   const dim3 blk(128);
   if (t.multilevel && t.nrs_work)
-    k_restrict<<<warp_item_grid((int64_t)t.nrs_work * ncomp), 32 * kItemWarps, 0, s>>>(
+    k_restrict<<<warp_item_grid(t.nrs_work), 32 * kItemWarps, 0, s>>>(
         t.rs, t.rs_work, t.nrs_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
   if (sp) {
     int rc = sparse_exchange_copy(t, *sp, fine, coarse, ncomp, s);
@@ -560,10 +566,10 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
     }
   }
   if (t.multilevel && t.nrr_work)
-    k_restrict<<<warp_item_grid((int64_t)t.nrr_work * ncomp), 32 * kItemWarps, 0, s>>>(
+    k_restrict<<<warp_item_grid(t.nrr_work), 32 * kItemWarps, 0, s>>>(
         t.rr, t.rr_work, t.nrr_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
   if (t.multilevel && prolongate && t.npro_work)
-    k_prolong<<<warp_item_grid((int64_t)t.npro_work * ncomp), 32 * kItemWarps, 0, s>>>(
+    k_prolong<<<warp_item_grid(t.npro_work), 32 * kItemWarps, 0, s>>>(
         t.pro, t.pro_work, t.npro_work, t.geom, t.dims, ncomp, fine, coarse, prolong_op, alloc);
   PGB_CUDA(cudaGetLastError());
   return kOk;

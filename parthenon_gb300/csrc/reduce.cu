@@ -50,8 +50,8 @@ __global__ void __launch_bounds__(256) k_burgers_min(const double *__restrict__ 
     const int b = (int)(r / d.nx[2]);
     const int64_t e = (int64_t)b * ncomp * cs + (int64_t)k * N01 + (int64_t)j * N0 + i;
     const DevBlockGeom &g = geom[b];
-    const double s = __dadd_rn(__dadd_rn(__ddiv_rn(fabs(u[e]), g.dx[0]), __ddiv_rn(fabs(u[e + cs]), g.dx[1])),
-                               __ddiv_rn(fabs(u[e + 2 * cs]), g.dx[2]));
+    const double s = __dadd_rn(__dadd_rn(div_rn(fabs(u[e]), g.dx[0]), div_rn(fabs(u[e + cs]), g.dx[1])),
+                               div_rn(fabs(u[e + 2 * cs]), g.dx[2]));
     m = fmin(m, __ddiv_rn(1.0, s));
   }
   block_min_to(m, out);

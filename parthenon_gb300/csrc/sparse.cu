@@ -43,41 +43,44 @@ int dev_alloc(T **p, size_t n) {
   return kOk;
 }
 
-// One warp per (pair, variable): the non-zero flag of the pair's buffer
-// (boundary_communication.cpp:95-140: |buf| >= allocation threshold, and only for an
-// allocated sender). The warp stops reading at the first value above the threshold.
+// One warp per pair, variables in turn: the non-zero flag of each (pair, variable)
+// buffer (boundary_communication.cpp:95-140: |buf| >= allocation threshold, and only
+// for an allocated sender). The warp stops reading at the first value above the
+// threshold.
 __global__ void __launch_bounds__(256) k_pair_flags(const DevPair *__restrict__ pairs, int npairs, Dims d, int ncomp,
                                                     const double *__restrict__ fine,
                                                     const double *__restrict__ coarse, SparseDev sp) {
-  const int q = warp_item();
-  if (q >= npairs * ncomp) return;
-  const int pi = q / ncomp, v = q - pi * ncomp;
+  const int pi = warp_item();
+  if (pi >= npairs) return;
   const int lane = threadIdx.x & 31;
   const DevPair p = pairs[pi];
-  if (!sp.alloc[p.src_block * ncomp + v]) {
-    if (lane == 0) sp.pair_flag[q] = 0;
-    return;
-  }
-  const double thr = sp.thr[v];
   const int n0 = p.src.n[0], n1 = p.src.n[1];
   const int cnt = n0 * n1 * p.src.n[2];
-  const double *src = p.src_coarse ? coarse + coarse_index(d, ncomp, p.src_block, v, 0, 0, 0)
-                                   : fine + fine_index(d, ncomp, p.src_block, v, 0, 0, 0);
   const int S0 = p.src_coarse ? d.Nc[0] : d.N[0];
   const int S01 = S0 * (p.src_coarse ? d.Nc[1] : d.N[1]);
-  int any = 0;
-  for (int e0 = 0; e0 < cnt && !any; e0 += 32) {
-    const int e = e0 + lane;
-    int nz = 0;
-    if (e < cnt) {
-      const int i = e % n0, j = (e / n0) % n1, k = e / (n0 * n1);
-      nz = fabs(src[(p.src.lo[2] + k) * S01 + (p.src.lo[1] + j) * S0 + p.src.lo[0] + i]) >= thr;
+  for (int v = 0; v < ncomp; ++v) {
+    const int64_t q = (int64_t)pi * ncomp + v;
+    if (!sp.alloc[p.src_block * ncomp + v]) {
+      if (lane == 0) sp.pair_flag[q] = 0;
+      continue;
     }
-    any = __any_sync(0xffffffffu, nz);
-  }
-  if (lane == 0) {
-    sp.pair_flag[q] = (uint8_t)(any != 0);
-    if (any && !sp.alloc[p.dst_block * ncomp + v]) sp.recv[p.dst_block * ncomp + v] = 1;
+    const double thr = sp.thr[v];
+    const double *src = p.src_coarse ? coarse + coarse_index(d, ncomp, p.src_block, v, 0, 0, 0)
+                                     : fine + fine_index(d, ncomp, p.src_block, v, 0, 0, 0);
+    int any = 0;
+    for (int e0 = 0; e0 < cnt && !any; e0 += 32) {
+      const int e = e0 + lane;
+      int nz = 0;
+      if (e < cnt) {
+        const int i = e % n0, j = (e / n0) % n1, k = e / (n0 * n1);
+        nz = fabs(src[(p.src.lo[2] + k) * S01 + (p.src.lo[1] + j) * S0 + p.src.lo[0] + i]) >= thr;
+      }
+      any = __any_sync(0xffffffffu, nz);
+    }
+    if (lane == 0) {
+      sp.pair_flag[q] = (uint8_t)(any != 0);
+      if (any && !sp.alloc[p.dst_block * ncomp + v]) sp.recv[p.dst_block * ncomp + v] = 1;
+    }
   }
 }
 
@@ -91,31 +94,34 @@ __global__ void k_commit(SparseDev sp, int n) {
 }
 
 // SetBounds into allocated receivers: the sender's values, or the default value behind
-// a null buffer (boundary_communication.cpp:267-330). One warp per (work item, variable).
+// a null buffer (boundary_communication.cpp:267-330). One warp per work item, variables
+// in turn (most (item, variable) pairs of a sparse mesh have nothing to do, and a warp
+// each would make the launch bound by CTA scheduling).
 __global__ void __launch_bounds__(256) k_set(const DevPair *__restrict__ pairs, const DevWork *__restrict__ work,
                                              int nwork, Dims d, int ncomp, double *__restrict__ fine,
                                              double *__restrict__ coarse, SparseDev sp) {
-  const int q = warp_item();
-  if (q >= nwork * ncomp) return;
-  const int wi = q / ncomp, v = q - wi * ncomp;
+  const int wi = warp_item();
+  if (wi >= nwork) return;
   const DevWork w = work[wi];
   const DevPair p = pairs[w.item];
-  if (!sp.alloc[p.dst_block * ncomp + v]) return;
-  const bool data = sp.pair_flag[(int64_t)w.item * ncomp + v] != 0;
-  const double dflt = sp.thr[2 * ncomp + v];
-  for_item_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
-    const int dk = p.dst.lo[2] + k, dj = p.dst.lo[1] + j, di = p.dst.lo[0] + i;
-    if (!p.full_mask && !mask_active(p.mask, p.dst, dk, dj, di)) return;
-    double x = dflt;
-    if (data) {
-      const int sk = p.src.lo[2] + k, sj = p.src.lo[1] + j, si = p.src.lo[0] + i;
-      x = p.src_coarse ? coarse[coarse_index(d, ncomp, p.src_block, v, sk, sj, si)]
-                       : fine[fine_index(d, ncomp, p.src_block, v, sk, sj, si)];
-    }
-    const int64_t t = p.dst_coarse ? coarse_index(d, ncomp, p.dst_block, v, dk, dj, di)
-                                   : fine_index(d, ncomp, p.dst_block, v, dk, dj, di);
-    (p.dst_coarse ? coarse : fine)[t] = x;
-  });
+  for (int v = 0; v < ncomp; ++v) {
+    if (!sp.alloc[p.dst_block * ncomp + v]) continue;
+    const bool data = sp.pair_flag[(int64_t)w.item * ncomp + v] != 0;
+    const double dflt = sp.thr[2 * ncomp + v];
+    for_item_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
+      const int dk = p.dst.lo[2] + k, dj = p.dst.lo[1] + j, di = p.dst.lo[0] + i;
+      if (!p.full_mask && !mask_active(p.mask, p.dst, dk, dj, di)) return;
+      double x = dflt;
+      if (data) {
+        const int sk = p.src.lo[2] + k, sj = p.src.lo[1] + j, si = p.src.lo[0] + i;
+        x = p.src_coarse ? coarse[coarse_index(d, ncomp, p.src_block, v, sk, sj, si)]
+                         : fine[fine_index(d, ncomp, p.src_block, v, sk, sj, si)];
+      }
+      const int64_t t = p.dst_coarse ? coarse_index(d, ncomp, p.dst_block, v, dk, dj, di)
+                                     : fine_index(d, ncomp, p.dst_block, v, dk, dj, di);
+      (p.dst_coarse ? coarse : fine)[t] = x;
+    });
+  }
 }
 
 // Flux correction: the fine side of every fine/coarse face sends when its variable is
@@ -252,12 +258,12 @@ int sparse_upload(MeshState &m) {
 int sparse_exchange_copy(const GridTables &t, const SparseDev &sp, double *fine, double *coarse, int ncomp,
                          cudaStream_t s) {
   if (!t.npairs) return kOk;
-  k_pair_flags<<<warp_item_grid((int64_t)t.npairs * ncomp), 32 * kItemWarps, 0, s>>>(t.pairs, t.npairs, t.dims,
-                                                                                      ncomp, fine, coarse, sp);
+  k_pair_flags<<<warp_item_grid(t.npairs), 32 * kItemWarps, 0, s>>>(t.pairs, t.npairs, t.dims, ncomp, fine, coarse,
+                                                                     sp);
   const int nbv = t.nblocks * ncomp;
   k_commit<<<(nbv + 255) / 256, 256, 0, s>>>(sp, nbv);
-  k_set<<<warp_item_grid((int64_t)t.ncopy_work * ncomp), 32 * kItemWarps, 0, s>>>(t.pairs, t.copy_work, t.ncopy_work,
-                                                                                   t.dims, ncomp, fine, coarse, sp);
+  k_set<<<warp_item_grid(t.ncopy_work), 32 * kItemWarps, 0, s>>>(t.pairs, t.copy_work, t.ncopy_work, t.dims, ncomp,
+                                                                 fine, coarse, sp);
   PGB_CUDA(cudaGetLastError());
   return kOk;
 }

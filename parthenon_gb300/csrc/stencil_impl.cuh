@@ -67,43 +67,54 @@ __device__ __forceinline__ double ld(const double *__restrict__ u, int64_t idx) 
   return __ldg(u + idx);
 }
 
-// One directional launch. Threads map to (block, t1, t0) lines where t0 is the
-// fastest transverse index (j for D = 0, i for D = 1, 2).
-template <int NC, int D, int MODE, bool BURGERS>
-__global__ void __launch_bounds__(128) k_march(StageArgs a) {
+// Shared line geometry of a directional launch: thread -> (block, t1, t0) line, where t0
+// is the fastest transverse index (j for D = 0, i for D = 1, 2).
+struct MarchLine {
+  int b, i0, j0, k0, n;
+  int64_t N0, N01, cs, step;
+};
+template <int D>
+__device__ __forceinline__ bool march_line(const StageArgs &a, MarchLine &m) {
   const Dims d = a.d;
   const int nx0 = d.nx[0], nx1 = d.nx[1], nx2 = d.nx[2];
   const int ng = d.ng;
-  // transverse extents
   const int n_fast = D == 0 ? nx1 : nx0;
   const int n_slow = D == 2 ? nx1 : nx2;
   const int64_t line = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nlines = (int64_t)a.nblocks * n_fast * n_slow;
-  if (line >= nlines) return;
+  if (line >= nlines) return false;
   const int t0 = (int)(line % n_fast);
   const int64_t r = line / n_fast;
   const int t1 = (int)(r % n_slow);
-  const int b = (int)(r / n_slow);
-  int i0, j0, k0;  // cell of march position 0 (interior start along D)
+  m.b = (int)(r / n_slow);
   if (D == 0) {
-    i0 = ng; j0 = ng + t0; k0 = ng + t1;
+    m.i0 = ng; m.j0 = ng + t0; m.k0 = ng + t1;
   } else if (D == 1) {
-    i0 = ng + t0; j0 = ng; k0 = ng + t1;
+    m.i0 = ng + t0; m.j0 = ng; m.k0 = ng + t1;
   } else {
-    i0 = ng + t0; j0 = ng + t1; k0 = ng;
+    m.i0 = ng + t0; m.j0 = ng + t1; m.k0 = ng;
   }
-  const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1];
-  const int64_t cs = N01 * d.N[2];                 // component stride
-  const int64_t step = D == 0 ? 1 : (D == 1 ? N0 : N01);
-  const int64_t c0 = (int64_t)b * NC * cs + (int64_t)k0 * N01 + (int64_t)j0 * N0 + i0;
-  const int n = D == 0 ? nx0 : (D == 1 ? nx1 : nx2);
+  m.N0 = d.N[0];
+  m.N01 = (int64_t)d.N[0] * d.N[1];
+  m.cs = m.N01 * d.N[2];  // component stride
+  m.step = D == 0 ? 1 : (D == 1 ? m.N0 : m.N01);
+  m.n = D == 0 ? nx0 : (D == 1 ? nx1 : nx2);
+  return true;
+}
+
+// One directional Burgers launch (all NC components per thread: the HLL flux couples
+// them through the normal velocity's face states).
+template <int NC, int D, int MODE>
+__global__ void __launch_bounds__(128) k_march(StageArgs a) {
+  MarchLine m;
+  if (!march_line<D>(a, m)) return;
+  const int b = m.b;
+  const int64_t cs = m.cs, step = m.step;
+  const int64_t c0 = (int64_t)b * NC * cs + (int64_t)m.k0 * m.N01 + (int64_t)m.j0 * m.N0 + m.i0;
+  const int n = m.n;
   const DevBlockGeom g = a.geom[b];
   const double area = g.area[D];
   const double *__restrict__ u = a.u_in;
-  // sparse variables: unallocated components are neither read nor written
-  bool on[NC];
-#pragma unroll
-  for (int v = 0; v < NC; ++v) on[v] = BURGERS || !a.alloc || a.alloc[b * NC + v];
 
   double Lprev[NC], AFprev[NC];
   // march from cell p = -1 (first ghost) to p = n (last ghost); face p lies between
@@ -111,64 +122,26 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
   for (int p = -1; p <= n; ++p) {
     double Lc[NC], Rc[NC];
     const int64_t cp = c0 + (int64_t)p * step;
-    if (BURGERS) {
 #pragma unroll
-      for (int v = 0; v < NC; ++v) {
-        const int64_t e = cp + v * cs;
-        if (a.recon == 0) {
-          weno5z(ld<D>(u, e - 2 * step), ld<D>(u, e - step), ld<D>(u, e), ld<D>(u, e + step),
-                 ld<D>(u, e + 2 * step), Lc[v], Rc[v]);
-        } else {
-          linear_mc(ld<D>(u, e - step), ld<D>(u, e), ld<D>(u, e + step), Lc[v], Rc[v]);
-        }
-      }
-    } else {
-      // advection: donor cell or PLM (plm_inline.hpp, uniform van Leer)
-      const int pos = (D == 0 ? i0 : (D == 1 ? j0 : k0)) + p;
-      const double xc = g.xmin[D] + (pos + 0.5) * g.dx[D];
-      const double xfp = g.xmin[D] + (pos + 1) * g.dx[D];
-      const double xfm = g.xmin[D] + pos * g.dx[D];
-      const double cp_ = (xfp - xc) / g.dx[D];
-      const double cm_ = (xc - xfm) / g.dx[D];
-#pragma unroll
-      for (int v = 0; v < NC; ++v) {
-        const int64_t e = cp + v * cs;
-        if (!on[v]) {
-          Lc[v] = Rc[v] = 0.0;
-          continue;
-        }
-        const double q0 = ld<D>(u, e);
-        if (a.recon == 0) {
-          Lc[v] = q0;
-          Rc[v] = q0;
-        } else {
-          const double dql = q0 - ld<D>(u, e - step), dqr = ld<D>(u, e + step) - q0;
-          const double dq2 = dql * dqr;
-          double dqm = 2.0 * dq2 / (dql + dqr);
-          if (dq2 <= 0.0) dqm = 0.0;
-          Lc[v] = q0 + cp_ * dqm;
-          Rc[v] = q0 - cm_ * dqm;
-        }
+    for (int v = 0; v < NC; ++v) {
+      const int64_t e = cp + v * cs;
+      if (a.recon == 0) {
+        weno5z(ld<D>(u, e - 2 * step), ld<D>(u, e - step), ld<D>(u, e), ld<D>(u, e + step),
+               ld<D>(u, e + 2 * step), Lc[v], Rc[v]);
+      } else {
+        linear_mc(ld<D>(u, e - step), ld<D>(u, e), ld<D>(u, e + step), Lc[v], Rc[v]);
       }
     }
     if (p >= 0) {
       double F[NC];
-      if (BURGERS) {
-        burgers_face_flux<NC>(Lprev, Rc, D, F);
-      } else {
-#pragma unroll
-        for (int v = 0; v < NC; ++v) {
-          const double vd = a.ncvel ? a.cvel[v][D] : a.vel[D];
-          F[v] = vd > 0.0 ? Lprev[v] * vd : Rc[v] * vd;
-        }
-      }
+      burgers_face_flux<NC>(Lprev, Rc, D, F);
       if (MODE == kStoreFlux) {
         // face p of direction D, stored at the cell index of the cell on its right
         const int64_t fbase = ((int64_t)b * 3 + D) * NC * cs;
 #pragma unroll
         for (int v = 0; v < NC; ++v) {
           const int64_t e = cp - (int64_t)b * NC * cs + v * cs;
-          if (on[v]) a.flux[fbase + e] = F[v];
+          a.flux[fbase + e] = F[v];
         }
       } else {
         double AF[NC];
@@ -178,7 +151,6 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
           const int64_t cc = cp - step;  // cell p-1
 #pragma unroll
           for (int v = 0; v < NC; ++v) {
-            if (!on[v]) continue;
             const int64_t e = cc + v * cs;
             double du = AF[v] - AFprev[v];
             if (MODE == kStoreDu) {
@@ -200,6 +172,76 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
     }
 #pragma unroll
     for (int v = 0; v < NC; ++v) Lprev[v] = Lc[v];
+  }
+}
+
+// One directional advection launch: components are independent, so each thread marches
+// one line of one component (grid.y = component). Small blocks get NC times the
+// threads a thread-per-line launch would have, and an unallocated sparse variable
+// costs its threads one flag load.
+template <int NC, int D, int MODE>
+__global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
+  MarchLine m;
+  if (!march_line<D>(a, m)) return;
+  const int b = m.b, v = blockIdx.y;
+  if (a.alloc && !a.alloc[b * NC + v]) return;  // unallocated sparse variable
+  const int64_t cs = m.cs, step = m.step;
+  const int64_t c0 = ((int64_t)b * NC + v) * cs + (int64_t)m.k0 * m.N01 + (int64_t)m.j0 * m.N0 + m.i0;
+  const int n = m.n;
+  const DevBlockGeom g = a.geom[b];
+  const double area = g.area[D];
+  const double *__restrict__ u = a.u_in;
+  const double vd = a.ncvel ? a.cvel[v][D] : a.vel[D];
+  const int pos0 = D == 0 ? m.i0 : (D == 1 ? m.j0 : m.k0);
+  double Lprev = 0.0, AFprev = 0.0;
+  for (int p = -1; p <= n; ++p) {
+    const int64_t e = c0 + (int64_t)p * step;
+    // donor cell or PLM (plm_inline.hpp, uniform van Leer)
+    const double q0 = ld<D>(u, e);
+    double Lc, Rc;
+    if (a.recon == 0) {
+      Lc = q0;
+      Rc = q0;
+    } else {
+      const int pos = pos0 + p;
+      const double xc = g.xmin[D] + (pos + 0.5) * g.dx[D];
+      const double xfp = g.xmin[D] + (pos + 1) * g.dx[D];
+      const double xfm = g.xmin[D] + pos * g.dx[D];
+      const double cp_ = (xfp - xc) / g.dx[D];
+      const double cm_ = (xc - xfm) / g.dx[D];
+      const double dql = q0 - ld<D>(u, e - step), dqr = ld<D>(u, e + step) - q0;
+      const double dq2 = dql * dqr;
+      double dqm = 2.0 * dq2 / (dql + dqr);
+      if (dq2 <= 0.0) dqm = 0.0;
+      Lc = q0 + cp_ * dqm;
+      Rc = q0 - cm_ * dqm;
+    }
+    if (p >= 0) {
+      const double F = vd > 0.0 ? Lprev * vd : Rc * vd;
+      if (MODE == kStoreFlux) {
+        // face p of direction D, stored at the cell index of the cell on its right
+        a.flux[(((int64_t)b * 3 + D) * NC + v) * cs + (e - ((int64_t)b * NC + v) * cs)] = F;
+      } else {
+        const double AF = area * F;
+        if (p >= 1) {
+          const int64_t ec = e - step;  // cell p-1
+          double du = AF - AFprev;
+          if (MODE == kStoreDu) {
+            a.dudt[ec] = du;
+          } else if (MODE == kAddDu) {
+            a.dudt[ec] = a.dudt[ec] + du;
+          } else {
+            if (MODE == kFinishUpdate) du = a.dudt[ec] + du;
+            const double dudt = -du / g.vol;
+            const double avg = a.w_in * __ldg(a.u_in + ec) + a.w_base * __ldg(a.u_base + ec);
+            const double bdt = a.beta * a.dt[0];
+            a.u_out[ec] = 1.0 * avg + bdt * dudt;
+          }
+        }
+        AFprev = AF;
+      }
+    }
+    Lprev = Lc;
   }
 }
 

@@ -14,14 +14,28 @@ int launch_stage_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
     const int64_t lines = (int64_t)a.nblocks * nf * ns;
     return dim3((unsigned)((lines + 127) / 128));
   };
-  if (store_flux) {
-    k_march<NC, 0, kStoreFlux, BURGERS><<<grid_for(0), 128, 0, s>>>(a);
-    k_march<NC, 1, kStoreFlux, BURGERS><<<grid_for(1), 128, 0, s>>>(a);
-    k_march<NC, 2, kStoreFlux, BURGERS><<<grid_for(2), 128, 0, s>>>(a);
+  if (BURGERS) {
+    if (store_flux) {
+      k_march<NC, 0, kStoreFlux><<<grid_for(0), 128, 0, s>>>(a);
+      k_march<NC, 1, kStoreFlux><<<grid_for(1), 128, 0, s>>>(a);
+      k_march<NC, 2, kStoreFlux><<<grid_for(2), 128, 0, s>>>(a);
+    } else {
+      k_march<NC, 0, kStoreDu><<<grid_for(0), 128, 0, s>>>(a);
+      k_march<NC, 1, kAddDu><<<grid_for(1), 128, 0, s>>>(a);
+      k_march<NC, 2, kFinishUpdate><<<grid_for(2), 128, 0, s>>>(a);
+    }
   } else {
-    k_march<NC, 0, kStoreDu, BURGERS><<<grid_for(0), 128, 0, s>>>(a);
-    k_march<NC, 1, kAddDu, BURGERS><<<grid_for(1), 128, 0, s>>>(a);
-    k_march<NC, 2, kFinishUpdate, BURGERS><<<grid_for(2), 128, 0, s>>>(a);
+    // advection: one component per thread, grid.y = component
+    auto g = [&](int D) { return dim3(grid_for(D).x, NC); };
+    if (store_flux) {
+      k_march_adv<NC, 0, kStoreFlux><<<g(0), 128, 0, s>>>(a);
+      k_march_adv<NC, 1, kStoreFlux><<<g(1), 128, 0, s>>>(a);
+      k_march_adv<NC, 2, kStoreFlux><<<g(2), 128, 0, s>>>(a);
+    } else {
+      k_march_adv<NC, 0, kStoreDu><<<g(0), 128, 0, s>>>(a);
+      k_march_adv<NC, 1, kAddDu><<<g(1), 128, 0, s>>>(a);
+      k_march_adv<NC, 2, kFinishUpdate><<<g(2), 128, 0, s>>>(a);
+    }
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrCuda;
 }
