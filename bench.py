@@ -445,7 +445,7 @@ def _sparse_pgen(pg):
     return lambda m, prev, a: pg.problems.sparse_advection_state(m, prev, a, init_size=0.1)
 
 
-def sparse_bench(torch, cycles, with_cpu, root=SPARSE_ROOT):
+def sparse_bench(torch, cycles, with_cpu, root=SPARSE_ROOT, profile_range=False):
     """Adaptive sparse advection: zone-cycles/s over `cycles` cycles with the tagging
     of every cycle, the remeshes (allocation carried over), the allocation on receipt
     and the deallocation checks inside the timed region."""
@@ -461,10 +461,14 @@ def sparse_bench(torch, cycles, with_cpu, root=SPARSE_ROOT):
     drv.run(2)  # warm-up: first graph capture on this mesh
     torch.cuda.synchronize()
     zc0, nr0, hist0 = drv.zone_cycles, drv.nremesh, len(drv.block_history)
+    if profile_range:  # launch lists of the timed cycles only (ncu --profile-from-start off)
+        torch.cuda.profiler.start()
     t0 = time.perf_counter()
     drv.run(cycles)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
+    if profile_range:
+        torch.cuda.profiler.stop()
     zc = drv.zone_cycles - zc0
     a, _ = drv.mesh.sparse_alloc(drv.stream)
     blocks = drv.block_history[hist0 - 1:]
@@ -585,6 +589,8 @@ def main():
                     help="cycles of the adaptive sparse-advection leg (0 skips it)")
     ap.add_argument("--sparse-only", action="store_true",
                     help="run only the sparse-advection leg (with its CPU baseline)")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket the sparse leg's timed cycles with cudaProfilerStart/Stop")
     args = ap.parse_args()
     ws, rank = _dist()
     if ws > 1:
@@ -601,7 +607,8 @@ def main():
     elif args.sparse_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        out = {"sparse": sparse_bench(torch, args.sparse_cycles, with_cpu=(rank == 0))}
+        out = {"sparse": sparse_bench(torch, args.sparse_cycles, with_cpu=(rank == 0),
+                                      profile_range=args.profile_range)}
     elif args.impl == "reference":
         out = run_reference(args, ws, rank)
     else:
