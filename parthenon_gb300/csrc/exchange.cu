@@ -17,6 +17,7 @@
 //      (ProlongateSharedGeneral, pr_ops.hpp:166-285)
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "common.cuh"
 #include "mesh_state.hpp"
@@ -69,13 +70,30 @@ void add_work(std::vector<DevWork> &w, int item, int rows, int ni, int target = 
 
 thread_local bool g_dry_run = false;  // validate tables without touching the device
 
-template <class T>
-int upload(T **dptr, const std::vector<T> &h) {
-  if (h.empty() || g_dry_run) return kOk;
-  PGB_CUDA(cudaMalloc((void **)dptr, h.size() * sizeof(T)));
-  PGB_CUDA(cudaMemcpy(*dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
-  return kOk;
-}
+// Every table of one grid is staged in one host buffer and moved to the device with
+// one allocation and one copy (a remesh of a few thousand blocks otherwise spends more
+// time in a dozen cudaMalloc/cudaMemcpy pairs than in its kernels).
+struct TableStage {
+  std::vector<char> bytes;
+  std::vector<std::pair<void **, size_t>> slots;  // table pointer, offset in the arena
+  template <class T>
+  void add(T **dptr, const std::vector<T> &h) {
+    *dptr = nullptr;
+    if (h.empty()) return;
+    const size_t off = (bytes.size() + 255) & ~size_t(255);
+    bytes.resize(off + h.size() * sizeof(T));
+    std::memcpy(bytes.data() + off, h.data(), h.size() * sizeof(T));
+    slots.push_back({(void **)dptr, off});
+  }
+  int commit(void **arena) {
+    *arena = nullptr;
+    if (g_dry_run || bytes.empty()) return kOk;
+    PGB_CUDA(cudaMalloc(arena, bytes.size()));
+    PGB_CUDA(cudaMemcpy(*arena, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
+    for (auto &sl : slots) *sl.first = static_cast<char *>(*arena) + sl.second;
+    return kOk;
+  }
+};
 
 // Host-side bounds proof for every device access a table entry implies; a table that
 // fails is rejected before any kernel can touch memory outside the field arrays.
@@ -107,9 +125,8 @@ bool prolong_inside(const DevBox &b, int ng, const int32_t N[3], const int32_t N
 }  // namespace
 
 void GridTables::release() {
-  void *ptrs[] = {pairs, copy_work, rs, rr, pro, rs_work, rr_work, pro_work, fc, fc_work, geom};
-  for (void *p : ptrs)
-    if (p) cudaFree(p);
+  if (arena) cudaFree(arena);  // every table lives in it
+  arena = nullptr;
   pairs = nullptr;
   copy_work = nullptr;
   rs = rr = pro = nullptr;
@@ -183,7 +200,9 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
   out.npairs = (int)pairs.size();
   out.ncopy_work = (int)cw.size();
   int rc;
-  if ((rc = upload(&out.pairs, pairs)) || (rc = upload(&out.copy_work, cw))) return rc;
+  TableStage stage;
+  stage.add(&out.pairs, pairs);
+  stage.add(&out.copy_work, cw);
 
   auto lower_regions = [&](const std::vector<CoarseRegion> &rg, DevRegion **dr, DevWork **dw, int &n,
                            int &nw, bool prolongation) -> int {
@@ -203,8 +222,8 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
     }
     n = (int)r.size();
     nw = (int)w.size();
-    int rc2;
-    if ((rc2 = upload(dr, r)) || (rc2 = upload(dw, w))) return rc2;
+    stage.add(dr, r);
+    stage.add(dw, w);
     return kOk;
   };
   if ((rc = lower_regions(g.restrict_send, &out.rs, &out.rs_work, out.nrs, out.nrs_work, false))) return rc;
@@ -230,7 +249,8 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
   }
   out.nfc = (int)fcs.size();
   out.nfc_work = (int)fw.size();
-  if ((rc = upload(&out.fc, fcs)) || (rc = upload(&out.fc_work, fw))) return rc;
+  stage.add(&out.fc, fcs);
+  stage.add(&out.fc_work, fw);
 
   out.geom_h.clear();
   for (auto &b : g.blocks) {
@@ -248,8 +268,8 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
     gm.vol = gm.dx[0] * gm.dx[1] * gm.dx[2];
     out.geom_h.push_back(gm);
   }
-  if ((rc = upload(&out.geom, out.geom_h))) return rc;
-  return kOk;
+  stage.add(&out.geom, out.geom_h);
+  return stage.commit(&out.arena);
 }
 
 // ------------------------------------------------------------------ kernels

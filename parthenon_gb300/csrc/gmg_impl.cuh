@@ -17,6 +17,10 @@
 //   src/prolong_restrict/pr_ops.hpp:105-285           RestrictAverage, ProlongateSharedLinear
 #pragma once
 
+#include <cooperative_groups.h>
+
+#include <type_traits>
+
 #include <algorithm>
 #include <cfloat>
 
@@ -499,6 +503,103 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_tail(TailArgs<T> a) {
   }
 }
 
+// The coarsest level alone (8^3 below a 16^3 level: the usual case) spread over a
+// cluster of kClusterCtas CTAs on as many SMs. Its ~34 Jacobi sweeps are bound by the
+// FP64 issue rate of whatever runs them; one SM spends ~1 us per 8^3 sweep, eight SMs an
+// eighth of that plus a cluster barrier. Every CTA keeps the whole level in its shared
+// memory: the arrays read at neighbouring cells (u and the sweep's other buffer) are
+// replicated -- each CTA computes its slab of cells and stores every new value into all
+// eight copies through distributed shared memory -- while the arrays only read at the
+// cell being written (rhs, res, u0) stay local. Phases end with a cluster barrier
+// (release/acquire at cluster scope, so the remote stores are visible). The per-cell
+// operations are the ones of k_tail, so the results are identical.
+constexpr int kClusterCtas = 8;
+constexpr int kClusterThreads = 64;
+
+template <class T>
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
+    k_tail_cluster(TailArgs<T> a) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  extern __shared__ double tail_sm[];
+  const TailLevel<T> &G = a.lv[0];  // device arrays of the coarsest level
+  const int64_t n = G.n;
+  T *lu = reinterpret_cast<T *>(tail_sm);
+  T *ltmp = lu + n, *lrhs = ltmp + n, *lres = lrhs + n, *lu0 = lres + n;
+  double *hu = tail_sm + ((5 * n * (int64_t)sizeof(T) + 7) / 8);
+  double *htmp = hu + n, *hrhs = htmp + n, *hres = hrhs + n, *hu0 = hres + n;
+  const TailLevel<T> L{lu, lrhs, lres, ltmp, lu0, G.g, n};
+  const TailLevel<double> H{hu, hrhs, hres, htmp, hu0, a.h.g, n};
+  const int64_t per = n / kClusterCtas, c0 = rank * per, c1 = c0 + per;
+  auto cells = [&](auto f) {
+    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) f(c);
+    cl.sync();
+  };
+  auto share = [&](auto *arr, int64_t c) {  // copy this CTA's new value to the other CTAs
+    const auto v = arr[c];
+    for (int r = 1; r < kClusterCtas; ++r) cl.map_shared_rank(arr, (rank + r) % kClusterCtas)[c] = v;
+  };
+  auto smooth = [&](auto &X, const double *wd) {
+    using U = typename std::remove_pointer<decltype(X.u)>::type;
+    U *x = X.u, *y = X.temp;
+    for (int st = 0; st < a.stages; ++st) {
+      const U ww = (U)a.w[st], wdd = (U)wd[st], omw = (U)(1.0 - a.w[st]);
+      cells([&](int64_t c) {
+        jacobi_at(c, x, X.rhs, y, X.g, (U)a.D, (U)a.alpha, ww, wdd, omw);
+        share(y, c);
+      });
+      U *t = x;
+      x = y;
+      y = t;
+    }
+    if (x != X.u) cells([&](int64_t c) {
+        X.u[c] = x[c];
+        share(X.u, c);
+      });
+  };
+  // restriction from the level above (l > 0 always on this path)
+  cells([&](int64_t c) {
+    restrict2_at(c, a.above_u, a.above_res, L.u, L.res, a.above_g, L.g);
+    share(L.u, c);
+  });
+  if (a.use_c64) {
+    cells([&](int64_t c) {
+      H.u[c] = (double)L.u[c];
+      H.res[c] = (double)L.res[c];
+      share(H.u, c);
+    });
+    cells([&](int64_t c) { fas_at<double>(c, H.u, H.res, H.rhs, H.u0, H.g, a.D, a.alpha); });
+    for (int pass = 0; pass <= a.coarse_sweeps; ++pass) smooth(H, a.hwd);
+    cells([&](int64_t c) {
+      H.res[c] = 1.0 * H.u[c] + -1.0 * H.u0[c];
+      L.res[c] = (T)H.res[c];
+    });
+    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {  // device copies
+      a.h.u[c] = H.u[c];
+      a.h.res[c] = H.res[c];
+      a.h.rhs[c] = H.rhs[c];
+      a.h.u0[c] = H.u0[c];
+      a.h.temp[c] = H.temp[c];
+      G.u[c] = L.u[c];
+      G.res[c] = L.res[c];
+    }
+    return;
+  }
+  const T D = (T)a.D, alpha = (T)a.alpha;
+  cells([&](int64_t c) { fas_at(c, L.u, L.res, L.rhs, L.u0, L.g, D, alpha); });
+  smooth(L, a.wd[0]);
+  for (int pass = 0; pass < a.coarse_sweeps; ++pass) smooth(L, a.wd[0]);
+  cells([&](int64_t c) { L.res[c] = (T)1 * L.u[c] + (T)-1 * L.u0[c]; });
+  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {  // device copies
+    G.u[c] = L.u[c];
+    G.res[c] = L.res[c];
+    G.rhs[c] = L.rhs[c];
+    G.u0[c] = L.u0[c];
+    G.temp[c] = L.temp[c];
+  }
+}
+
 // One FAS V-cycle (mg_solver.hpp:375-520) over levels L[0] (finest) .. L[nl-1].
 // When c64 is given, the coarsest level runs in FP64 on c64 (mixed precision).
 template <class T>
@@ -535,7 +636,13 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
   }
   for (int l = 0; l < nl; ++l) {
     if (l == lt) {
-      k_tail<T><<<1, kTailThreads, 0, s>>>(ta);
+      const int64_t nc = ta.lv[0].n;
+      if (ta.nlev == 1 && lt > 0 && nc % (kClusterCtas * 32) == 0 && nc / kClusterCtas <= kClusterThreads) {
+        const size_t smem = (size_t)((5 * nc * (int64_t)sizeof(T) + 7) / 8 + 5 * nc) * sizeof(double);
+        k_tail_cluster<T><<<kClusterCtas, kClusterThreads, smem, s>>>(ta);
+      } else {
+        k_tail<T><<<1, kTailThreads, 0, s>>>(ta);
+      }
       break;
     }
     GmgLevelBuf<T> &g = L[l];

@@ -29,6 +29,7 @@ struct GridTables {
   DevFluxCorr *fc = nullptr;
   DevWork *fc_work = nullptr;
   DevBlockGeom *geom = nullptr;
+  void *arena = nullptr;        // one device allocation holding every table above
   std::vector<DevBlockGeom> geom_h;
   void release();
 };
@@ -46,6 +47,7 @@ struct SparseState {
   std::vector<int32_t> count_h;    // staged counters
   bool staged = false;             // host copies to be uploaded with the mesh tables
   SparseDev dev{};                 // device arrays (null until uploaded)
+  void *arena = nullptr;           // the one allocation holding them
   void release();
 };
 

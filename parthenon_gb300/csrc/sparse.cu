@@ -33,16 +33,6 @@ void mesh_clear_graphs(pgb_mesh *m);
 
 namespace {
 
-template <class T>
-int dev_alloc(T **p, size_t n) {
-  if (*p) cudaFree(*p);
-  *p = nullptr;
-  if (n == 0) n = 1;
-  PGB_CUDA(cudaMalloc((void **)p, n * sizeof(T)));
-  PGB_CUDA(cudaMemset(*p, 0, n * sizeof(T)));
-  return kOk;
-}
-
 // One warp per pair, variables in turn: the non-zero flag of each (pair, variable)
 // buffer (boundary_communication.cpp:95-140: |buf| >= allocation threshold, and only
 // for an allocated sender). The warp stops reading at the first value above the
@@ -208,9 +198,8 @@ __global__ void __launch_bounds__(256) k_minmax_tag(const double *__restrict__ u
 }  // namespace
 
 void SparseState::release() {
-  void *ptrs[] = {dev.alloc, dev.count, dev.recv, dev.pair_flag, dev.fc_flag, (void *)dev.thr};
-  for (void *p : ptrs)
-    if (p) cudaFree(p);
+  if (arena) cudaFree(arena);  // every device array lives in it
+  arena = nullptr;
   const int nc = dev.ncomp, dc = dev.dealloc_count;
   dev = SparseDev{};
   dev.ncomp = nc;
@@ -222,7 +211,6 @@ int sparse_upload(MeshState &m) {
   if (!s.on) return kOk;
   const GridTables &t = m.leaf;
   const size_t nbv = (size_t)t.nblocks * s.ncomp;
-  int rc;
   // keep the device flags when the block list did not change (a re-upload)
   std::vector<uint8_t> keep_a;
   std::vector<int32_t> keep_c;
@@ -232,17 +220,25 @@ int sparse_upload(MeshState &m) {
     PGB_CUDA(cudaMemcpy(keep_a.data(), s.dev.alloc, nbv, cudaMemcpyDeviceToHost));
     PGB_CUDA(cudaMemcpy(keep_c.data(), s.dev.count, nbv * sizeof(int32_t), cudaMemcpyDeviceToHost));
   }
-  if ((rc = dev_alloc(&s.dev.alloc, nbv)) || (rc = dev_alloc(&s.dev.count, nbv)) ||
-      (rc = dev_alloc(&s.dev.recv, nbv)) || (rc = dev_alloc(&s.dev.pair_flag, (size_t)t.npairs * s.ncomp)) ||
-      (rc = dev_alloc(&s.dev.fc_flag, (size_t)t.nfc * s.ncomp)))
-    return rc;
-  double *thr = nullptr;
-  if ((rc = dev_alloc(&thr, 3 * (size_t)s.ncomp))) return rc;
-  PGB_CUDA(cudaMemcpy(thr, s.thr_h.data(), s.thr_h.size() * sizeof(double), cudaMemcpyHostToDevice));
-  if (s.dev.thr) cudaFree((void *)s.dev.thr);
-  s.dev.thr = thr;
+  s.release();
+  // one zeroed allocation: thresholds, counters, flags, receipt marks, pair flags
+  const size_t nthr = 3 * (size_t)s.ncomp, npf = std::max<size_t>(1, (size_t)t.npairs * s.ncomp),
+               nff = std::max<size_t>(1, (size_t)t.nfc * s.ncomp);
+  auto up = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t o_thr = 0, o_cnt = up(o_thr + nthr * sizeof(double)), o_alloc = up(o_cnt + nbv * sizeof(int32_t)),
+               o_recv = up(o_alloc + nbv), o_pf = up(o_recv + nbv), o_ff = up(o_pf + npf), total = up(o_ff + nff);
+  PGB_CUDA(cudaMalloc(&s.arena, total));
+  PGB_CUDA(cudaMemset(s.arena, 0, total));
+  char *base = static_cast<char *>(s.arena);
+  s.dev.thr = reinterpret_cast<const double *>(base + o_thr);
+  s.dev.count = reinterpret_cast<int32_t *>(base + o_cnt);
+  s.dev.alloc = reinterpret_cast<uint8_t *>(base + o_alloc);
+  s.dev.recv = reinterpret_cast<uint8_t *>(base + o_recv);
+  s.dev.pair_flag = reinterpret_cast<uint8_t *>(base + o_pf);
+  s.dev.fc_flag = reinterpret_cast<uint8_t *>(base + o_ff);
   s.dev.ncomp = s.ncomp;
   s.dev.dealloc_count = s.dealloc_count;
+  PGB_CUDA(cudaMemcpy(base + o_thr, s.thr_h.data(), nthr * sizeof(double), cudaMemcpyHostToDevice));
   const std::vector<uint8_t> &a = s.staged ? s.alloc_h : keep_a;
   const std::vector<int32_t> &c = s.staged ? s.count_h : keep_c;
   if (a.size() == nbv) PGB_CUDA(cudaMemcpy(s.dev.alloc, a.data(), nbv, cudaMemcpyHostToDevice));
