@@ -107,6 +107,7 @@ int stage_impl(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const
   a.d = t.dims;
   a.nblocks = t.nblocks;
   a.recon = p->recon;
+  a.ncomp = ncomp;
   for (int q = 0; q < 3; ++q) a.vel[q] = p->vel[q];
   a.ncvel = p->physics == 0 ? p->ncomp_vel : 0;
   for (int c = 0; c < a.ncvel; ++c)

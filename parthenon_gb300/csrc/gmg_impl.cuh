@@ -60,9 +60,11 @@ __device__ __forceinline__ T ax_cell(const T *u, int k, int j, int i, const Leve
   out += (f3l - f3r) / dx;
   return out;
 #else
+  // the fast build serves the Poisson operator, alpha = 0 (the only operator
+  // pgb_gmg_create builds): no alpha term, 7 FP64 instructions per cell
   (void)dx;
-  const T lap = ((uim + uip) + (ujm + ujp) + (ukm + ukp) - (T)6 * uc) * (T)g.idx2;
-  return alpha == (T)0 ? lap : lap - alpha * uc;  // uniform branch: Poisson has alpha = 0
+  (void)alpha;
+  return ((uim + uip) + (ujm + ujp) + (ukm + ukp) - (T)6 * uc) * (T)g.idx2;
 #endif
 }
 
@@ -128,7 +130,11 @@ __device__ __forceinline__ void residual_at(int64_t c, const T *u, const T *rhs,
                                             T *res, const LevelGeom &g, T D, T alpha) {
   int k, j, i;
   cell_of(c, g, k, j, i);
+#ifdef PGB_GMG_EXACT
   res[c] = (T)1 * rhs[c] + (T)-1 * ax_cell(u, k, j, i, g, D, alpha);
+#else
+  res[c] = rhs[c] - ax_cell(u, k, j, i, g, D, alpha);  // 1 a + (-1) b is exactly a - b
+#endif
 }
 
 template <class T>
@@ -156,7 +162,11 @@ __device__ __forceinline__ void fas_at(int64_t c, const T *u, const T *res,
   int k, j, i;
   cell_of(c, g, k, j, i);
   u0[c] = u[c];
+#ifdef PGB_GMG_EXACT
   rhs[c] = (T)1 * ax_cell(u, k, j, i, g, D, alpha) + (T)1 * res[c];
+#else
+  rhs[c] = ax_cell(u, k, j, i, g, D, alpha) + res[c];
+#endif
 }
 
 template <class T>
@@ -295,7 +305,11 @@ __global__ void __launch_bounds__(256) k_residual_sumsq(const T *__restrict__ u,
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
     int k, j, i;
     cell_of(c, g, k, j, i);
+#ifdef PGB_GMG_EXACT
     const T r = (T)1 * rhs[c] + (T)-1 * ax_cell(u, k, j, i, g, D, alpha);
+#else
+    const T r = rhs[c] - ax_cell(u, k, j, i, g, D, alpha);
+#endif
     if (res) res[c] = r;
     if (rhs32) rhs32[c] = (float)r;
     acc += (double)r * (double)r;

@@ -52,6 +52,7 @@ struct StageArgs {
   int nblocks;
   int recon;             // Burgers: 0 WENO5, 1 linear; advection: 0 donor cell, 1 PLM
   double vel[3];         // advection velocity
+  int ncomp;             // components of the fields
   int ncvel;             // advection: 0, or one velocity per component in cvel
   double cvel[16][3];
   const uint8_t *alloc;  // sparse variables: [block * ncomp + v] allocated (null: dense)

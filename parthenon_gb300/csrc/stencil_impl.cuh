@@ -179,11 +179,11 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
 // one line of one component (grid.y = component). Small blocks get NC times the
 // threads a thread-per-line launch would have, and an unallocated sparse variable
 // costs its threads one flag load.
-template <int NC, int D, int MODE>
+template <int D, int MODE>
 __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
   MarchLine m;
   if (!march_line<D>(a, m)) return;
-  const int b = m.b, v = blockIdx.y;
+  const int b = m.b, v = blockIdx.y, NC = a.ncomp;
   if (a.alloc && !a.alloc[b * NC + v]) return;  // unallocated sparse variable
   const int64_t cs = m.cs, step = m.step;
   const int64_t c0 = ((int64_t)b * NC + v) * cs + (int64_t)m.k0 * m.N01 + (int64_t)m.j0 * m.N0 + m.i0;
@@ -245,9 +245,11 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
   }
 }
 
-// Flux divergence + RK update from stored flux arrays (multilevel path).
-template <int NC>
+// Flux divergence + RK update from stored flux arrays (multilevel path). NC = 0: the
+// component count is read from the arguments.
+template <int NC_>
 __global__ void __launch_bounds__(128) k_div_update(StageArgs a) {
+  const int NC = NC_ > 0 ? NC_ : a.ncomp;
   const Dims d = a.d;
   const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t ncell = (int64_t)a.nblocks * d.nx[0] * d.nx[1] * d.nx[2];

@@ -24,18 +24,27 @@ int launch_stage_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
       k_march<NC, 1, kAddDu><<<grid_for(1), 128, 0, s>>>(a);
       k_march<NC, 2, kFinishUpdate><<<grid_for(2), 128, 0, s>>>(a);
     }
+  }
+  return cudaGetLastError() == cudaSuccess ? kOk : kErrCuda;
+}
+
+// Advection: one component per thread (grid.y = component), any component count.
+int launch_advection(const StageArgs &a, bool store_flux, cudaStream_t s) {
+  const Dims &d = a.d;
+  auto g = [&](int D) {
+    const int64_t nf = D == 0 ? d.nx[1] : d.nx[0];
+    const int64_t ns = D == 2 ? d.nx[1] : d.nx[2];
+    const int64_t lines = (int64_t)a.nblocks * nf * ns;
+    return dim3((unsigned)((lines + 127) / 128), (unsigned)a.ncomp);
+  };
+  if (store_flux) {
+    k_march_adv<0, kStoreFlux><<<g(0), 128, 0, s>>>(a);
+    k_march_adv<1, kStoreFlux><<<g(1), 128, 0, s>>>(a);
+    k_march_adv<2, kStoreFlux><<<g(2), 128, 0, s>>>(a);
   } else {
-    // advection: one component per thread, grid.y = component
-    auto g = [&](int D) { return dim3(grid_for(D).x, NC); };
-    if (store_flux) {
-      k_march_adv<NC, 0, kStoreFlux><<<g(0), 128, 0, s>>>(a);
-      k_march_adv<NC, 1, kStoreFlux><<<g(1), 128, 0, s>>>(a);
-      k_march_adv<NC, 2, kStoreFlux><<<g(2), 128, 0, s>>>(a);
-    } else {
-      k_march_adv<NC, 0, kStoreDu><<<g(0), 128, 0, s>>>(a);
-      k_march_adv<NC, 1, kAddDu><<<g(1), 128, 0, s>>>(a);
-      k_march_adv<NC, 2, kFinishUpdate><<<g(2), 128, 0, s>>>(a);
-    }
+    k_march_adv<0, kStoreDu><<<g(0), 128, 0, s>>>(a);
+    k_march_adv<1, kAddDu><<<g(1), 128, 0, s>>>(a);
+    k_march_adv<2, kFinishUpdate><<<g(2), 128, 0, s>>>(a);
   }
   return cudaGetLastError() == cudaSuccess ? kOk : kErrCuda;
 }
@@ -68,12 +77,8 @@ int launch_stage(const StageArgs &a, int ncomp, int physics, bool store_flux, cu
       default: return kErrUnsupported;
     }
   }
-  switch (ncomp) {
-    case 1: return launch_stage_nc<1, false>(a, store_flux, s);
-    case 4: return launch_stage_nc<4, false>(a, store_flux, s);
-    case 5: return launch_stage_nc<5, false>(a, store_flux, s);
-    default: return kErrUnsupported;
-  }
+  if (ncomp < 1 || ncomp > 65535) return kErrUnsupported;
+  return launch_advection(a, store_flux, s);
 }
 
 int launch_div_update(const StageArgs &a, int ncomp, cudaStream_t s) {
@@ -82,7 +87,7 @@ int launch_div_update(const StageArgs &a, int ncomp, cudaStream_t s) {
     case 4: return launch_div_update_nc<4>(a, s);
     case 5: return launch_div_update_nc<5>(a, s);
     case 11: return launch_div_update_nc<11>(a, s);
-    default: return kErrUnsupported;
+    default: return ncomp >= 1 ? launch_div_update_nc<0>(a, s) : kErrUnsupported;
   }
 }
 

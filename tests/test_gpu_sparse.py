@@ -231,3 +231,94 @@ def test_sparse_advection_amr_run_matches_oracle():
     assert 0 < a.mean() < 0.75  # the fields stay sparse
     assert np.array_equal(drv.base.cpu().numpy(), np.array(ref.o.base()))
     assert float(drv.dt.cpu()[0]) == ref.o.dt()
+
+
+def test_sparse_api_errors():
+    torch = _torch()
+    m = pg.Mesh((32, 32, 32), (16, 16, 16), 2).upload()
+    m.enable_sparse(2, ALLOC, DEALLOC)
+    f = m.new_field(3)
+    # field components must match the mesh's sparse variables
+    with pytest.raises(pg.NativeError, match="sparse"):
+        m.exchange(f)
+    # the packed-buffer exchange does not take sparse variables
+    with pytest.raises(pg.NativeError, match="sparse"):
+        m.exchange(m.new_field(2), buffered=True)
+    # flags must be 0 or 1
+    with pytest.raises(pg.NativeError):
+        m.set_sparse_alloc(np.full((m.nblocks, 2), 2, np.uint8))
+    # Burgers declares no sparse variables
+    mb = pg.Mesh((32, 32, 32), (16, 16, 16), 4).upload().enable_sparse(5, ALLOC, DEALLOC)
+    with pytest.raises(pg.NativeError, match="advection only"):
+        pg.RK2Driver(mb, 5, pg.StageConfig("burgers", "weno5", 0.8)).run(1, graph=False)
+    del torch
+
+
+def test_sparse_fast_build_within_tolerance():
+    """The FMA-contracted kernels on the sparse advection problem (PLM) stay within 1e-12
+    of the oracle; the allocation flags, which depend on thresholds, match exactly."""
+    nx, bnx, ng, nc, cfl = (32, 32, 32), (16, 16, 16), 4, 4, 0.45
+    vel = pg.problems.sparse_advection_velocities()
+    lo, hi = (-1.0,) * 3, (1.0,) * 3
+    leaves = refined_cube(1, 0, 1)
+    m = pg.Mesh(nx, bnx, ng, xmin=lo, xmax=hi, leaves=leaves)
+    m.enable_sparse(nc, ALLOC, DEALLOC, dealloc_count=2)
+    state, alloc = pg.problems.sparse_advection_state(m, init_size=0.3)
+    drv = pg.RK2Driver(m, nc, pg.StageConfig("advection", "plm", cfl, comp_vel=vel))
+    drv.set_state(state, alloc)
+    o = O.OracleSim(nx, bnx, ng, xmin=lo, xmax=hi, leaves=leaves, ncomp=nc, physics="advection", recon=1, cfl=cfl)
+    o.set_component_velocities(vel)
+    o.sparse_enable(ALLOC, DEALLOC, dealloc_count=2)
+    o.sparse_set(alloc)
+    o.base()[:] = np.where(alloc[:, :, None, None, None] != 0, state, 0.0)
+    o.exchange(True, 0)
+    o.init_dt()
+    drv.run(6, graph=True)
+    o.run(6)
+    drv.stream.synchronize()
+    a, cnt = m.sparse_alloc(drv.stream)
+    ra, rc = o.sparse_alloc()
+    assert np.array_equal(a, ra) and np.array_equal(cnt, rc)
+    g = drv.base.cpu().numpy()[:, :, ng:-ng, ng:-ng, ng:-ng]
+    r = np.array(o.base())[:, :, ng:-ng, ng:-ng, ng:-ng]
+    scale = np.abs(r).max(axis=(0, 2, 3, 4))
+    err = np.abs(g - r).max(axis=(0, 2, 3, 4)) / np.where(scale > 0, scale, 1.0)
+    assert err.max() <= 1e-12, err
+
+
+def test_sparse_three_level_exchange_and_flux_allocation():
+    """Three-level mesh, 16^3-class boxes: one dense-like variable and one that lives only
+    on the finest blocks, so the coarse face neighbours of the fine region allocate
+    through flux correction in the first stage."""
+    torch = _torch()
+    nx, bnx, ng, nc = (64, 64, 64), (8, 8, 8), 4, 2
+    leaves = two_level_nested(3, 2, 6, 6, 10)
+    o = O.OracleSim(nx, bnx, ng, leaves=leaves, ncomp=nc, physics="advection", recon=0, cfl=0.3)
+    m = pg.Mesh(nx, bnx, ng, leaves=leaves)
+    locs, _ = m.block_info()
+    finest = locs[:, 0] == locs[:, 0].max()
+    alloc = np.zeros((m.nblocks, nc), np.uint8)
+    alloc[:, 0] = 1
+    alloc[finest, 1] = 1
+    rng = np.random.default_rng(4)
+    u = np.zeros((m.nblocks, nc) + tuple(m.N[::-1]))
+    u[:, 0, ng:-ng, ng:-ng, ng:-ng] = rng.random((m.nblocks,) + (8, 8, 8))
+    u[finest, 1, ng:-ng, ng:-ng, ng:-ng] = 1e-7  # below the allocation threshold
+    vel = [[1.0, 0.5, -0.25], [-0.5, 1.0, 0.75]]
+    m.enable_sparse(nc, ALLOC, DEALLOC, dealloc_count=3)
+    drv = pg.RK2Driver(m, nc, pg.StageConfig("advection", "dc", 0.3, exact=True, comp_vel=vel))
+    drv.set_state(u, alloc)
+    o.set_component_velocities(vel)
+    o.sparse_enable(ALLOC, DEALLOC, dealloc_count=3)
+    o.sparse_set(alloc)
+    o.base()[:] = u
+    o.exchange(True, 0)
+    o.init_dt()
+    drv.run(2, graph=False)
+    o.run(2)
+    drv.stream.synchronize()
+    a, cnt = m.sparse_alloc(drv.stream)
+    ra, rc = o.sparse_alloc()
+    assert np.array_equal(a, ra) and np.array_equal(cnt, rc)
+    assert a[:, 1].sum() > alloc[:, 1].sum()  # flux correction allocated coarse neighbours
+    assert np.array_equal(drv.base.cpu().numpy(), np.array(o.base()))
