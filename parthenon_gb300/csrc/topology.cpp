@@ -134,24 +134,43 @@ bool LLoc::touches_element(const LLoc &in, const std::array<int, 3> &te) const {
 // ------------------------------------------------------------------ ownership
 Mask27 ownership_among(const LLoc &main, const std::vector<std::pair<LLoc, LLoc>> &allowed) {
   // A block yields an element to the neighbour with the higher level, then the higher
-  // Morton number (block_ownership.cpp:42-74).
+  // Morton number (block_ownership.cpp:42-74). The elements a neighbour touches form a
+  // product of per-axis sets, so its 27-bit mask is built from three 3-bit masks.
   auto beats = [&](const LLoc &a, const LLoc &b) {  // a < b in ownership order
     if (a.level != b.level) return a.level < b.level;
     return a.key() < b.key();
   };
-  Mask27 m = 0;
-  for (int a = -1; a <= 1; ++a)
-    for (int b = -1; b <= 1; ++b)
-      for (int c = -1; c <= 1; ++c) {
-        bool own = true;
-        for (auto &n : allowed)
-          if (beats(main, n.first) && main.touches_element(n.second, {a, b, c})) {
-            own = false;
-            break;
-          }
-        if (own) m |= 1u << mask_bit(a, b, c);
+  Mask27 taken = 0;
+  for (auto &n : allowed) {
+    if (!beats(main, n.first)) continue;
+    const LLoc &in = n.second;
+    const int top = std::max(in.level, main.level);
+    const int64_t wi = 1ll << (top - in.level), wm = 1ll << (top - main.level);
+    unsigned ax[3];
+    for (int d = 0; d < 3; ++d) {
+      const int64_t lo2 = in.lx[d] * wi, hi2 = lo2 + wi - 1;
+      const int64_t blo = main.lx[d] * wm, bhi = blo + wm - 1;
+      ax[d] = 0;
+      for (int t = -1; t <= 1; ++t) {
+        int64_t lo = blo, hi = bhi;  // the element's index range along d (touches_element)
+        if (t < 0) {
+          lo -= 1;
+          hi = lo + 1;
+        } else if (t > 0) {
+          hi += 1;
+          lo = hi - 1;
+        }
+        if (!(hi < lo2 || lo > hi2)) ax[d] |= 1u << (t + 1);
       }
-  return m;
+    }
+    for (int c = 0; c < 3; ++c)
+      if (ax[2] >> c & 1u)
+        for (int b = 0; b < 3; ++b)
+          if (ax[1] >> b & 1u)
+            for (int a = 0; a < 3; ++a)
+              if (ax[0] >> a & 1u) taken |= 1u << (a + 3 * b + 9 * c);
+  }
+  return 0x7FFFFFFu & ~taken;
 }
 
 static inline int topo_offset(int el, int d) {
@@ -329,7 +348,11 @@ MeshTopology::MeshTopology(const MeshSpec &spec, const std::vector<LLoc> &leaves
   // leaf first (the neighbour lists read it), into the cache the serial paths use.
   for (auto &l : lv) l.key();  // Morton keys are computed lazily; fix them before sharing
   std::vector<Mask27> own(lv.size());
-  parallel_for((int)lv.size(), [&](int i) { own[i] = ownership_among(lv[i], neighbors_of(lv[i], kLeaf, 0)); });
+  std::vector<std::vector<std::pair<LLoc, LLoc>>> nlists(lv.size());
+  parallel_for((int)lv.size(), [&](int i) {
+    nlists[i] = neighbors_of(lv[i], kLeaf, 0);
+    own[i] = ownership_among(lv[i], nlists[i]);
+  });
   auto &cache = own_cache_[{(int)kLeaf, 0}];
   cache.reserve(lv.size());
   for (size_t i = 0; i < lv.size(); ++i) cache.emplace(lv[i], own[i]);
@@ -338,7 +361,8 @@ MeshTopology::MeshTopology(const MeshSpec &spec, const std::vector<LLoc> &leaves
   parallel_for((int)lv.size(), [&](int i) {
     const LLoc &l = lv[i];
     BlockInfo b = make_block(l);
-    for (auto &n : neighbors_of(l, kLeaf, 0)) {
+    b.nbrs.reserve(nlists[i].size());
+    for (auto &n : nlists[i]) {
       Neighbor nb;
       nb.gid = gid_of(n.first);
       nb.where = n.first;
