@@ -178,6 +178,11 @@ int pgb_rk2_cycles(pgb_mesh *mesh, const pgb_stage_params *p, double *base, doub
  * *dt_inout: in, the current dt (<= 0: estimate the initial dt); out, the next dt. */
 int pgb_run_host(pgb_mesh *mesh, const pgb_stage_params *p, const double *host_in, double *host_out, int32_t ncomp,
                  int32_t ncycles, double *dt_inout);
+/* The same, and dt_cycles (host, ncycles doubles; may be NULL) receives the dt of the
+ * step after each cycle, read back from the device as that cycle ends (the per-step
+ * scalar result a driver would log). */
+int pgb_run_host_dt(pgb_mesh *mesh, const pgb_stage_params *p, const double *host_in, double *host_out,
+                    int32_t ncomp, int32_t ncycles, double *dt_inout, double *dt_cycles);
 
 /* ---------------------------------------------------------------- multigrid
  * Geometric multigrid for div(grad u) = rhs on a uniform periodic cube of n^3 cells

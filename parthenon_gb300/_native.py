@@ -65,6 +65,7 @@ _SIGNATURES = {
     "pgb_rk2_cycles": [VP, ctypes.POINTER(StageParams), VP, VP, VP, VP, VP, VP, ctypes.c_int32, VP,
                        ctypes.c_int32, ctypes.c_int32, VP],
     "pgb_run_host": [VP, ctypes.POINTER(StageParams), VP, VP, ctypes.c_int32, ctypes.c_int32, DP],
+    "pgb_run_host_dt": [VP, ctypes.POINTER(StageParams), VP, VP, ctypes.c_int32, ctypes.c_int32, DP, DP],
     "pgb_gmg_create": [ctypes.POINTER(GmgParams), ctypes.POINTER(VP)],
     "pgb_gmg_destroy": [VP],
     "pgb_gmg_vcycles": [VP, VP, VP, ctypes.c_int32, VP, VP],

@@ -425,20 +425,27 @@ int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double 
 
 int pgb_run_host(pgb_mesh *m, const pgb_stage_params *p, const double *host_in, double *host_out, int32_t ncomp,
                  int32_t ncycles, double *dt_inout) {
+  return pgb_run_host_dt(m, p, host_in, host_out, ncomp, ncycles, dt_inout, nullptr);
+}
+
+int pgb_run_host_dt(pgb_mesh *m, const pgb_stage_params *p, const double *host_in, double *host_out, int32_t ncomp,
+                    int32_t ncycles, double *dt_inout, double *dt_cycles) {
   int rc = check_params(m, p, ncomp);
   if (rc) return rc;
   if (!host_in || !host_out || !dt_inout) return fail(kErrInvalid, "null pointer");
+  if (ncycles < 0) return fail(kErrInvalid, "ncycles must be >= 0");
   const GridTables &t = m->st.leaf;
   const size_t n = (size_t)t.nblocks * ncomp * t.dims.N[0] * t.dims.N[1] * t.dims.N[2];
   const size_t nc = (size_t)t.nblocks * ncomp * t.dims.Nc[0] * t.dims.Nc[1] * t.dims.Nc[2];
   const bool ml = t.multilevel;
   double *base = nullptr, *stage = nullptr, *dudt = nullptr, *flux = nullptr, *cb = nullptr, *cs = nullptr,
-         *dt = nullptr;
+         *dt = nullptr, *dt_pinned = nullptr;
   cudaStream_t s = nullptr;
   auto cleanup = [&]() {
     double *ps[] = {base, stage, dudt, flux, cb, cs, dt};
     for (double *q : ps)
       if (q) cudaFree(q);
+    if (dt_pinned) cudaFreeHost(dt_pinned);
     if (s) cudaStreamDestroy(s);
   };
   auto guard = [&](cudaError_t e, const char *w) {
@@ -474,14 +481,23 @@ int pgb_run_host(pgb_mesh *m, const pgb_stage_params *p, const double *host_in, 
     cleanup();
     return rc;
   }
-  for (int c = 0; c < ncycles; ++c)
+  // each cycle's dt is read back as the cycle ends (into pinned memory: the copies queue
+  // behind the cycles without stalling the host)
+  if (dt_cycles && ncycles > 0 &&
+      (rc = guard(cudaMallocHost(&dt_pinned, (size_t)ncycles * sizeof(double)), "pinned dt")))
+    return rc;
+  for (int c = 0; c < ncycles; ++c) {
     if ((rc = cycle_impl(m, p, base, stage, dudt, flux, cb, cs, ncomp, dt, s))) {
       cleanup();
       return rc;
     }
+    if (dt_pinned && (rc = guard(cudaMemcpyAsync(dt_pinned + c, dt, 8, cudaMemcpyDeviceToHost, s), "d2h dt")))
+      return rc;
+  }
   if ((rc = guard(cudaMemcpyAsync(host_out, base, n * 8, cudaMemcpyDeviceToHost, s), "d2h"))) return rc;
   if ((rc = guard(cudaMemcpyAsync(dt_inout, dt, 8, cudaMemcpyDeviceToHost, s), "d2h"))) return rc;
   if ((rc = guard(cudaStreamSynchronize(s), "sync"))) return rc;
+  if (dt_pinned) std::memcpy(dt_cycles, dt_pinned, (size_t)ncycles * sizeof(double));
   cleanup();
   return kOk;
 }
