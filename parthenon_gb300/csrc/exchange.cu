@@ -275,8 +275,6 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
 // ------------------------------------------------------------------ kernels
 namespace {
 
-__device__ __forceinline__ double *arr(double *fine, double *coarse, int c) { return c ? coarse : fine; }
-
 // Direct copy: sender slab -> receiver ghosts. grid = (work items, components).
 // Per thread the row base addresses are formed once per row; rows whose two ends are
 // 16-byte aligned on both sides (every same-level face and edge of an even-sized block)

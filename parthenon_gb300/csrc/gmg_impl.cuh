@@ -230,7 +230,9 @@ __device__ __forceinline__ void prolong_add_at(int64_t c, const T *cres, T *fu,
   const int n = cg.n;
   const int64_t nn = (int64_t)n * n;
   const T fc = cres[c];
+#ifdef PGB_GMG_EXACT
   const int ci[3] = {i, j, k};
+#endif
   T gm[3], gp[3], dfm[3], dfp[3];
 #pragma unroll
   for (int q = 0; q < 3; ++q) {

@@ -20,7 +20,6 @@
 #include <algorithm>
 #include <cfloat>
 #include <cstring>
-#include <map>
 
 #include "../../include/parthenon_gb300.h"
 #include "common.cuh"
