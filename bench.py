@@ -151,6 +151,17 @@ def burgers_ops_per_cell_stage(n, nc):
     return recon + faces + nc * DIVUPD_OPS
 
 
+def max_over_ranks(torch, value, ws):
+    """The slowest rank's value (the job's time is its slowest replica's): an all-reduce
+    on the device under NCCL, on the host under gloo."""
+    if ws <= 1:
+        return value
+    dev = "cuda" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args, ws, rank):
     import torch
     import parthenon_gb300 as pg
@@ -183,11 +194,7 @@ def run_ours(args, ws, rank):
         torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(torch, e0.elapsed_time(e1), ws)
     value = ws * args.steps * zones / (ms * 1e-3)
     if args.no_extras:
         return {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
