@@ -16,10 +16,12 @@
 //   4. prolongate coarse-buffer ghosts into fine ghosts next to coarser blocks
 //      (ProlongateSharedGeneral, pr_ops.hpp:166-285)
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
 #include "common.cuh"
+#include "host_parallel.hpp"
 #include "mesh_state.hpp"
 #include "tune.hpp"
 
@@ -44,22 +46,23 @@ DevBox to_dev(const IBox &b) {
 
 bool mask_is_full(const IBox &b) {
   // Every element active: either the mask is all ones or every boundary cell of the
-  // box maps to an owned slot.
+  // box maps to an owned slot. Along an axis a box of one index reaches only slot 0,
+  // one of two indices slots -1 and +1, a longer one all three; the reachable slots of
+  // the box are the product of the per-axis sets.
   if (b.mask == 0x7FFFFFFu) return true;
-  for (int c = -1; c <= 1; ++c)
-    for (int bb = -1; bb <= 1; ++bb)
-      for (int a = -1; a <= 1; ++a) {
-        // slot reachable only if the box has such positions
-        const int n[3] = {b.hi[0] - b.lo[0] + 1, b.hi[1] - b.lo[1] + 1, b.hi[2] - b.lo[2] + 1};
-        const int s[3] = {a, bb, c};
-        bool reachable = true;
-        for (int d = 0; d < 3; ++d) {
-          if (n[d] == 1 && s[d] != 0) reachable = false;   // single index maps to 0
-          if (n[d] == 2 && s[d] == 0) reachable = false;   // two indices: -1 and +1
-        }
-        if (reachable && !mask_get(b.mask, a, bb, c)) return false;
-      }
-  return true;
+  unsigned ax[3];
+  for (int d = 0; d < 3; ++d) {
+    const int n = b.hi[d] - b.lo[d] + 1;
+    ax[d] = n == 1 ? 0b010u : (n == 2 ? 0b101u : 0b111u);
+  }
+  uint32_t reach = 0;
+  for (int c = 0; c < 3; ++c)
+    if (ax[2] >> c & 1u)
+      for (int bb = 0; bb < 3; ++bb)
+        if (ax[1] >> bb & 1u)
+          for (int a = 0; a < 3; ++a)
+            if (ax[0] >> a & 1u) reach |= 1u << (a + 3 * bb + 9 * c);
+  return (b.mask & reach) == reach;
 }
 
 // Split `rows` rows of `ni` elements into work items of about `target` elements.
@@ -67,21 +70,40 @@ void add_work(std::vector<DevWork> &w, int item, int rows, int ni, int target = 
   const int per = std::max(1, target / std::max(ni, 1));
   for (int r = 0; r < rows; r += per) w.push_back({item, r, std::min(per, rows - r), 0});
 }
+// The same split, counted and written in place (parallel lowering).
+int work_count(int rows, int ni, int target = 4096) {
+  const int per = std::max(1, target / std::max(ni, 1));
+  return (rows + per - 1) / per;
+}
+void fill_work(DevWork *w, int item, int rows, int ni, int target = 4096) {
+  const int per = std::max(1, target / std::max(ni, 1));
+  for (int r = 0, k = 0; r < rows; r += per, ++k) w[k] = {item, r, std::min(per, rows - r), 0};
+}
 
 thread_local bool g_dry_run = false;  // validate tables without touching the device
 
 // Every table of one grid is staged in one host buffer and moved to the device with
 // one allocation and one copy (a remesh of a few thousand blocks otherwise spends more
 // time in a dozen cudaMalloc/cudaMemcpy pairs than in its kernels).
+// The host staging buffer lives as long as the thread and keeps its capacity: a remesh
+// then writes into pages that are already mapped (first-touch faults of a fresh
+// multi-megabyte buffer cost more than the copy).
 struct TableStage {
-  std::vector<char> bytes;
+  std::vector<char> &bytes;
   std::vector<std::pair<void **, size_t>> slots;  // table pointer, offset in the arena
+  static std::vector<char> &buffer() {
+    thread_local std::vector<char> b;
+    return b;
+  }
+  TableStage() : bytes(buffer()) { bytes.clear(); }
   template <class T>
   void add(T **dptr, const std::vector<T> &h) {
     *dptr = nullptr;
-    if (h.empty()) return;
+    if (h.empty() || g_dry_run) return;
     const size_t off = (bytes.size() + 255) & ~size_t(255);
-    bytes.resize(off + h.size() * sizeof(T));
+    const size_t end = off + h.size() * sizeof(T);
+    if (end > bytes.capacity()) bytes.reserve(std::max(end, 2 * bytes.capacity()));
+    bytes.resize(end);
     std::memcpy(bytes.data() + off, h.data(), h.size() * sizeof(T));
     slots.push_back({(void **)dptr, off});
   }
@@ -169,11 +191,23 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
     for (int d = 0; d < 3; ++d)
       if (b.nx[d] != b0.nx[d]) return fail(kErrUnsupported, "blocks of one grid must share a size");
 
-  std::vector<DevPair> pairs;
-  std::vector<DevWork> cw;
-  int64_t off = 0;
-  for (auto &p : g.pairs) {
-    DevPair d;
+  // Per-item lowering runs on the host's cores: each pair's device record and its
+  // work-item count in parallel, offsets by a serial prefix sum, work items in parallel.
+  const int np = (int)g.pairs.size();
+  // buffers reused across remeshes (see TableStage); bound to references here because
+  // the worker threads of parallel_for must see this thread's instances
+  thread_local std::vector<DevPair> pairs_tl;
+  thread_local std::vector<int64_t> woff_tl;
+  thread_local std::vector<DevWork> cw_tl;
+  std::vector<DevPair> &pairs = pairs_tl;
+  std::vector<int64_t> &woff = woff_tl;
+  std::vector<DevWork> &cw = cw_tl;
+  pairs.resize(np);
+  woff.assign(np + 1, 0);
+  std::atomic<int> bad{0};
+  parallel_for(np, [&](int i) {
+    const CopyPair &p = g.pairs[i];
+    DevPair &d = pairs[i];
     d.src_block = p.sender;
     d.dst_block = p.receiver;
     d.src_coarse = p.send_coarse;
@@ -182,20 +216,28 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
     d.dst = to_dev(p.recv);
     d.mask = p.recv.mask;
     d.full_mask = mask_is_full(p.recv) ? 1 : 0;
-    d.buf_off = off;
-    off += p.send.count();
     const int32_t *se = p.send_coarse ? out.dims.Nc : out.dims.N;
     const int32_t *de = p.recv_coarse ? out.dims.Nc : out.dims.N;
-    if (!box_inside(d.src, se) || !box_inside(d.dst, de))
-      return fail(kErrInvalid, "boundary box outside the block arrays");
+    if (!box_inside(d.src, se) || !box_inside(d.dst, de)) bad.store(1);
     // element m of the send box maps to element m of the receive box; the direct copy
     // relies on both boxes having the same extents (always true for cell-centred data
     // on one tree with the identity logical transformation)
     for (int q = 0; q < 3; ++q)
-      if (d.src.n[q] != d.dst.n[q]) return fail(kErrUnsupported, "send and receive boxes differ in shape");
-    add_work(cw, (int)pairs.size(), d.src.n[1] * d.src.n[2], d.src.n[0]);
-    pairs.push_back(d);
+      if (d.src.n[q] != d.dst.n[q]) bad.store(2);
+    woff[i + 1] = work_count(d.src.n[1] * d.src.n[2], d.src.n[0]);
+  });
+  if (bad.load() == 1) return fail(kErrInvalid, "boundary box outside the block arrays");
+  if (bad.load() == 2) return fail(kErrUnsupported, "send and receive boxes differ in shape");
+  int64_t off = 0;
+  for (int i = 0; i < np; ++i) {
+    pairs[i].buf_off = off;
+    off += g.pairs[i].send.count();
+    woff[i + 1] += woff[i];
   }
+  cw.resize(woff[np]);
+  parallel_for(np, [&](int i) {
+    fill_work(cw.data() + woff[i], i, pairs[i].src.n[1] * pairs[i].src.n[2], pairs[i].src.n[0]);
+  });
   out.buffer_elems = off;
   out.npairs = (int)pairs.size();
   out.ncopy_work = (int)cw.size();

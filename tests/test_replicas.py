@@ -39,7 +39,7 @@ def _rank_main(rank, world, port, out):
 def test_max_over_ranks_gloo():
     import torch.multiprocessing as mp
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:  # no fork of a threaded process
         out = mgr.dict()
         mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
         assert dict(out) == {0: 15.0, 1: 15.0}
