@@ -85,33 +85,52 @@ thread_local bool g_dry_run = false;  // validate tables without touching the de
 // Every table of one grid is staged in one host buffer and moved to the device with
 // one allocation and one copy (a remesh of a few thousand blocks otherwise spends more
 // time in a dozen cudaMalloc/cudaMemcpy pairs than in its kernels).
-// The host staging buffer lives as long as the thread and keeps its capacity: a remesh
-// then writes into pages that are already mapped (first-touch faults of a fresh
-// multi-megabyte buffer cost more than the copy).
+// The host staging buffer is pinned memory that lives as long as the thread and keeps
+// its capacity: a remesh writes into pages already mapped (first-touch faults of a
+// fresh multi-megabyte buffer cost more than the copy) and the upload is one DMA.
+struct PinnedStage {
+  char *p = nullptr;
+  size_t cap = 0, size = 0;
+  // grow to at least n bytes, keeping the contents
+  int reserve(size_t n) {
+    if (n <= cap) return kOk;
+    const size_t nc = std::max(n, 2 * cap);
+    char *q = nullptr;
+    PGB_CUDA(cudaMallocHost((void **)&q, nc));
+    if (size) std::memcpy(q, p, size);
+    if (p) cudaFreeHost(p);
+    p = q;
+    cap = nc;
+    return kOk;
+  }
+};
+
 struct TableStage {
-  std::vector<char> &bytes;
+  PinnedStage &buf;
   std::vector<std::pair<void **, size_t>> slots;  // table pointer, offset in the arena
-  static std::vector<char> &buffer() {
-    thread_local std::vector<char> b;
+  int rc = kOk;
+  static PinnedStage &buffer() {
+    thread_local PinnedStage b;
     return b;
   }
-  TableStage() : bytes(buffer()) { bytes.clear(); }
+  TableStage() : buf(buffer()) { buf.size = 0; }
   template <class T>
   void add(T **dptr, const std::vector<T> &h) {
     *dptr = nullptr;
-    if (h.empty() || g_dry_run) return;
-    const size_t off = (bytes.size() + 255) & ~size_t(255);
+    if (h.empty() || g_dry_run || rc) return;
+    const size_t off = (buf.size + 255) & ~size_t(255);
     const size_t end = off + h.size() * sizeof(T);
-    if (end > bytes.capacity()) bytes.reserve(std::max(end, 2 * bytes.capacity()));
-    bytes.resize(end);
-    std::memcpy(bytes.data() + off, h.data(), h.size() * sizeof(T));
+    if ((rc = buf.reserve(end))) return;
+    std::memcpy(buf.p + off, h.data(), h.size() * sizeof(T));
+    buf.size = end;
     slots.push_back({(void **)dptr, off});
   }
   int commit(void **arena) {
     *arena = nullptr;
-    if (g_dry_run || bytes.empty()) return kOk;
-    PGB_CUDA(cudaMalloc(arena, bytes.size()));
-    PGB_CUDA(cudaMemcpy(*arena, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
+    if (rc) return rc;
+    if (g_dry_run || buf.size == 0) return kOk;
+    PGB_CUDA(cudaMalloc(arena, buf.size));
+    PGB_CUDA(cudaMemcpy(*arena, buf.p, buf.size, cudaMemcpyHostToDevice));
     for (auto &sl : slots) *sl.first = static_cast<char *>(*arena) + sl.second;
     return kOk;
   }

@@ -604,9 +604,6 @@ struct TreeEdit {
 std::vector<LLoc> MeshTopology::amr_update(const std::vector<int> &flags) const {
   const auto &bl = leaf_.blocks;
   if (flags.size() != bl.size()) throw std::invalid_argument("one flag per leaf block is required");
-  TreeEdit t;
-  t.leaves = leaves_;
-  t.internal = internal_;
   std::vector<LLoc> lref, lderef;
   for (size_t b = 0; b < bl.size(); ++b) {
     if (flags[b] == 1) lref.push_back(bl[b].loc);
@@ -633,9 +630,14 @@ std::vector<LLoc> MeshTopology::amr_update(const std::vector<int> &flags) const 
       if (rr == nleaf) cl.push_back(a.parent());
     }
   }
+  // nothing to refine and no complete sibling group to derefine: the leaves stay
+  if (lref.empty() && cl.empty()) return std::vector<LLoc>(leaves_.begin(), leaves_.end());
   // the reference orders all but the last candidate by decreasing level
   if (cl.size() > 1)
     std::stable_sort(cl.begin(), cl.end() - 1, [](const LLoc &x, const LLoc &y) { return x.level > y.level; });
+  TreeEdit t;
+  t.leaves = leaves_;
+  t.internal = internal_;
   for (auto &l : lref) t.refine(l);
   for (auto &l : cl) t.derefine(l);
   return std::vector<LLoc>(t.leaves.begin(), t.leaves.end());
