@@ -519,18 +519,32 @@ __global__ void __launch_bounds__(kTailThreads, 1) k_tail(TailArgs<T> a) {
   }
 }
 
-// The coarsest level alone (8^3 below a 16^3 level: the usual case) spread over a
-// cluster of kClusterCtas CTAs on as many SMs. Its ~34 Jacobi sweeps are bound by the
-// FP64 issue rate of whatever runs them; one SM spends ~1 us per 8^3 sweep, eight SMs an
-// eighth of that plus a cluster barrier. Every CTA keeps the whole level in its shared
-// memory: the arrays read at neighbouring cells (u and the sweep's other buffer) are
-// replicated -- each CTA computes its slab of cells and stores every new value into all
-// eight copies through distributed shared memory -- while the arrays only read at the
-// cell being written (rhs, res, u0) stay local. Phases end with a cluster barrier
-// (release/acquire at cluster scope, so the remote stores are visible). The per-cell
-// operations are the ones of k_tail, so the results are identical.
+// The coarse end of the hierarchy -- the 16^3 and 8^3 levels, or an 8^3 coarsest level
+// alone -- spread over a cluster of kClusterCtas CTAs on as many SMs, as one launch. A
+// 16^3 level is too small to fill the GPU (its kernels are launch and ramp bound) and
+// the 8^3 level's ~34 Jacobi sweeps are bound by the FP64 issue rate of whatever runs
+// them (one SM spends ~1 us per 8^3 sweep). Every CTA keeps the levels in its shared
+// memory and owns a slab of planes of each (planes 2r, 2r+1 of 16^3 and plane r of 8^3
+// for CTA r, so restriction reads stay in the CTA). Arrays read at neighbouring cells
+// -- the solution and the sweep's other buffer of every level, and the coarsest
+// level's correction that prolongation reads -- get halo planes: each CTA stores the
+// new values of its slab's first and last planes into the neighbouring CTAs' copies
+// through distributed shared memory. The others stay local. Phases end with a cluster barrier (release/acquire at cluster
+// scope, so the remote stores are visible). The per-cell operations are those of
+// k_tail, so the results are identical.
 constexpr int kClusterCtas = 8;
-constexpr int kClusterThreads = 64;
+constexpr int kClusterThreads = 256;
+constexpr int kClusterLevels = 2;
+
+// Shared-memory bytes of a cluster tail over levels of n[0..nlev-1] cells (5 arrays of
+// T each) plus the FP64 coarsest copy (5 arrays) when use_c64.
+template <class T>
+size_t cluster_tail_smem(const int64_t *n, int nlev, bool use_c64) {
+  size_t off = 0;
+  for (int q = 0; q < nlev; ++q) off = ((off + 5 * n[q] * sizeof(T)) + 15) & ~size_t(15);
+  if (use_c64) off += 5 * n[nlev - 1] * sizeof(double);
+  return off;
+}
 
 template <class T>
 __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
@@ -539,80 +553,126 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   extern __shared__ double tail_sm[];
-  const TailLevel<T> &G = a.lv[0];  // device arrays of the coarsest level
-  const int64_t n = G.n;
-  T *lu = reinterpret_cast<T *>(tail_sm);
-  T *ltmp = lu + n, *lrhs = ltmp + n, *lres = lrhs + n, *lu0 = lres + n;
-  double *hu = tail_sm + ((5 * n * (int64_t)sizeof(T) + 7) / 8);
-  double *htmp = hu + n, *hrhs = htmp + n, *hres = hrhs + n, *hu0 = hres + n;
-  const TailLevel<T> L{lu, lrhs, lres, ltmp, lu0, G.g, n};
-  const TailLevel<double> H{hu, hrhs, hres, htmp, hu0, a.h.g, n};
-  const int64_t per = n / kClusterCtas, c0 = rank * per, c1 = c0 + per;
-  auto cells = [&](auto f) {
+  char *base = reinterpret_cast<char *>(tail_sm);
+  TailLevel<T> L[kClusterLevels];
+  size_t off = 0;
+  for (int q = 0; q < a.nlev; ++q) {
+    const int64_t n = a.lv[q].n;
+    T *p = reinterpret_cast<T *>(base + off);
+    L[q] = TailLevel<T>{p, p + 2 * n, p + 3 * n, p + n, p + 4 * n, a.lv[q].g, n};  // u rhs res temp u0
+    off = ((off + 5 * n * sizeof(T)) + 15) & ~size_t(15);
+  }
+  const int64_t nh = a.lv[a.nlev - 1].n;
+  double *hp = reinterpret_cast<double *>(base + off);
+  const TailLevel<double> H{hp, hp + 2 * nh, hp + 3 * nh, hp + nh, hp + 4 * nh, a.h.g, nh};
+  auto cells = [&](int64_t n, auto f) {
+    const int64_t per = n / kClusterCtas, c0 = rank * per, c1 = c0 + per;
     for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) f(c);
     cl.sync();
   };
-  auto share = [&](auto *arr, int64_t c) {  // copy this CTA's new value to the other CTAs
+  // copy this CTA's new value of cell c (level geometry g) to the CTAs that read it: the
+  // operators reach one plane up and down, so the first plane of a slab goes to the CTA
+  // below and the last one to the CTA above (periodic)
+  auto share = [&](auto *arr, int64_t c, const LevelGeom &g) {
     const auto v = arr[c];
-    for (int r = 1; r < kClusterCtas; ++r) cl.map_shared_rank(arr, (rank + r) % kClusterCtas)[c] = v;
+    const int plane = (int)(c >> (2 * g.log2n)), per = g.n / kClusterCtas;
+    const int first = rank * per, last = first + per - 1;
+    if (plane == first) cl.map_shared_rank(arr, (rank + kClusterCtas - 1) % kClusterCtas)[c] = v;
+    if (plane == last) cl.map_shared_rank(arr, (rank + 1) % kClusterCtas)[c] = v;
   };
   auto smooth = [&](auto &X, const double *wd) {
     using U = typename std::remove_pointer<decltype(X.u)>::type;
     U *x = X.u, *y = X.temp;
     for (int st = 0; st < a.stages; ++st) {
       const U ww = (U)a.w[st], wdd = (U)wd[st], omw = (U)(1.0 - a.w[st]);
-      cells([&](int64_t c) {
+      cells(X.n, [&](int64_t c) {
         jacobi_at(c, x, X.rhs, y, X.g, (U)a.D, (U)a.alpha, ww, wdd, omw);
-        share(y, c);
+        share(y, c, X.g);
       });
       U *t = x;
       x = y;
       y = t;
     }
-    if (x != X.u) cells([&](int64_t c) {
+    if (x != X.u) cells(X.n, [&](int64_t c) {
         X.u[c] = x[c];
-        share(X.u, c);
+        share(X.u, c, X.g);
       });
   };
-  // restriction from the level above (l > 0 always on this path)
-  cells([&](int64_t c) {
-    restrict2_at(c, a.above_u, a.above_res, L.u, L.res, a.above_g, L.g);
-    share(L.u, c);
-  });
+  const T D = (T)a.D, alpha = (T)a.alpha;
+  // downward: restriction (l > 0 on this path), FAS right-hand side, smoothing
+  for (int q = 0; q < a.nlev; ++q) {
+    const TailLevel<T> &X = L[q];
+    const bool coarsest = q == a.nlev - 1;
+    const T *su = q == 0 ? a.above_u : L[q - 1].u;
+    const T *sr = q == 0 ? a.above_res : L[q - 1].res;
+    const LevelGeom sg = q == 0 ? a.above_g : L[q - 1].g;
+    cells(X.n, [&](int64_t c) {
+      restrict2_at(c, su, sr, X.u, X.res, sg, X.g);
+      share(X.u, c, X.g);
+    });
+    if (coarsest && a.use_c64) {
+      cells(X.n, [&](int64_t c) {
+        H.u[c] = (double)X.u[c];
+        H.res[c] = (double)X.res[c];
+        share(H.u, c, H.g);
+      });
+      cells(X.n, [&](int64_t c) { fas_at<double>(c, H.u, H.res, H.rhs, H.u0, H.g, a.D, a.alpha); });
+      for (int pass = 0; pass <= a.coarse_sweeps; ++pass) smooth(H, a.hwd);
+      cells(X.n, [&](int64_t c) {
+        H.res[c] = 1.0 * H.u[c] + -1.0 * H.u0[c];
+        X.res[c] = (T)H.res[c];
+        share(X.res, c, X.g);
+      });
+      break;
+    }
+    cells(X.n, [&](int64_t c) { fas_at(c, X.u, X.res, X.rhs, X.u0, X.g, D, alpha); });
+    smooth(X, a.wd[q]);
+    if (!coarsest) {
+      cells(X.n, [&](int64_t c) { residual_at(c, X.u, X.rhs, X.res, X.g, D, alpha); });
+    } else {
+      for (int pass = 0; pass < a.coarse_sweeps; ++pass) smooth(X, a.wd[q]);
+      cells(X.n, [&](int64_t c) {
+        X.res[c] = (T)1 * X.u[c] + (T)-1 * X.u0[c];
+        share(X.res, c, X.g);
+      });
+    }
+  }
+  // upward: prolongate the correction, post-smoothing, correction of this level
+  for (int q = a.nlev - 2; q >= 0; --q) {
+    const TailLevel<T> &X = L[q], &C = L[q + 1];
+    cells(C.n, [&](int64_t c) {
+      prolong_add_at(c, C.res, X.u, C.g, X.g);
+      int k, j, i;
+      cell_of(c, C.g, k, j, i);
+      const int fn = X.g.n;
+      const int64_t fnn = (int64_t)fn * fn;
+      const int64_t b0 = (int64_t)(2 * k) * fnn + (2 * j) * fn + 2 * i;
+      for (int e = 0; e < 8; ++e) share(X.u, b0 + (e >> 2) * fnn + ((e >> 1) & 1) * fn + (e & 1), X.g);
+    });
+    smooth(X, a.wd[q]);
+    cells(X.n, [&](int64_t c) { X.res[c] = (T)1 * X.u[c] + (T)-1 * X.u0[c]; });
+  }
+  // device copies of this CTA's cells
+  for (int q = 0; q < a.nlev; ++q) {
+    const TailLevel<T> &X = L[q], &G = a.lv[q];
+    const int64_t per = X.n / kClusterCtas, c0 = rank * per, c1 = c0 + per;
+    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+      G.u[c] = X.u[c];
+      G.res[c] = X.res[c];
+      G.rhs[c] = X.rhs[c];
+      G.u0[c] = X.u0[c];
+      G.temp[c] = X.temp[c];
+    }
+  }
   if (a.use_c64) {
-    cells([&](int64_t c) {
-      H.u[c] = (double)L.u[c];
-      H.res[c] = (double)L.res[c];
-      share(H.u, c);
-    });
-    cells([&](int64_t c) { fas_at<double>(c, H.u, H.res, H.rhs, H.u0, H.g, a.D, a.alpha); });
-    for (int pass = 0; pass <= a.coarse_sweeps; ++pass) smooth(H, a.hwd);
-    cells([&](int64_t c) {
-      H.res[c] = 1.0 * H.u[c] + -1.0 * H.u0[c];
-      L.res[c] = (T)H.res[c];
-    });
-    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {  // device copies
+    const int64_t per = nh / kClusterCtas, c0 = rank * per, c1 = c0 + per;
+    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
       a.h.u[c] = H.u[c];
       a.h.res[c] = H.res[c];
       a.h.rhs[c] = H.rhs[c];
       a.h.u0[c] = H.u0[c];
       a.h.temp[c] = H.temp[c];
-      G.u[c] = L.u[c];
-      G.res[c] = L.res[c];
     }
-    return;
-  }
-  const T D = (T)a.D, alpha = (T)a.alpha;
-  cells([&](int64_t c) { fas_at(c, L.u, L.res, L.rhs, L.u0, L.g, D, alpha); });
-  smooth(L, a.wd[0]);
-  for (int pass = 0; pass < a.coarse_sweeps; ++pass) smooth(L, a.wd[0]);
-  cells([&](int64_t c) { L.res[c] = (T)1 * L.u[c] + (T)-1 * L.u0[c]; });
-  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {  // device copies
-    G.u[c] = L.u[c];
-    G.res[c] = L.res[c];
-    G.rhs[c] = L.rhs[c];
-    G.u0[c] = L.u0[c];
-    G.temp[c] = L.temp[c];
   }
 }
 
@@ -623,8 +683,13 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
   const T D = (T)c.D, alpha = (T)c.alpha;
   // levels lt .. nl-1 (at most kTailCells cells each, at most kTailMax of them) run in
   // one tail launch
-  int lt = nl;
-  while (lt > 0 && L[lt - 1].cells() <= kTailCells && nl - (lt - 1) <= kTailMax) --lt;
+  // the cluster tail takes a 16^3 + 8^3 or a lone 8^3 coarse end (below another level)
+  int cluster_levels = 0;
+  if (nl >= 3 && L[nl - 1].cells() == 512 && L[nl - 2].cells() == 4096) cluster_levels = 2;
+  else if (nl >= 2 && L[nl - 1].cells() == 512) cluster_levels = 1;
+  int lt = nl - cluster_levels;
+  if (!cluster_levels)
+    while (lt > 0 && L[lt - 1].cells() <= kTailCells && nl - (lt - 1) <= kTailMax) --lt;
   TailArgs<T> ta{};
   if (lt < nl) {
     ta.nlev = nl - lt;
@@ -652,9 +717,11 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
   }
   for (int l = 0; l < nl; ++l) {
     if (l == lt) {
-      const int64_t nc = ta.lv[0].n;
-      if (ta.nlev == 1 && lt > 0 && nc % (kClusterCtas * 32) == 0 && nc / kClusterCtas <= kClusterThreads) {
-        const size_t smem = (size_t)((5 * nc * (int64_t)sizeof(T) + 7) / 8 + 5 * nc) * sizeof(double);
+      if (cluster_levels) {
+        int64_t ns[kClusterLevels];
+        for (int q = 0; q < ta.nlev; ++q) ns[q] = ta.lv[q].n;
+        const size_t smem = cluster_tail_smem<T>(ns, ta.nlev, ta.use_c64 != 0);
+        cudaFuncSetAttribute(k_tail_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_tail_cluster<T><<<kClusterCtas, kClusterThreads, smem, s>>>(ta);
       } else {
         k_tail<T><<<1, kTailThreads, 0, s>>>(ta);
