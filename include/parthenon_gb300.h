@@ -236,6 +236,47 @@ int pgb_gmg_solve_blocks(pgb_gmg *gmg, pgb_mesh *mesh, double *u, const double *
                          int32_t comp_rhs, int32_t method, double rtol, int32_t max_iters, int32_t *iters_out,
                          double *relres_out, void *stream);
 
+/* ---- multigrid on the composite grids of a refined mesh --------------------------
+ * MGSolver<u, rhs, PoissonEquation> on a mesh with refinement: FAS V-cycles over the
+ * two-level composite grids (grid L = every block of level L plus the leaves of level
+ * L-1; the level-L blocks are smoothed, the coarser leaves lend boundary values), with
+ * SRJ or weighted-Jacobi smoothing, volume-average restriction, linear prolongation and
+ * the gmg_same ghost exchange (restriction/prolongation across coarse/fine faces) on
+ * every grid; the outer residual is taken on the leaf grid. The operator is
+ * div(D grad u) - alpha u with constant D (poisson_equation.hpp:41-210, flux correction
+ * off as in the package default). FP64, bitwise the reference's arithmetic.
+ * Replaces MGSolver::AddTasks / AddSetupTasks (src/solvers/mg_solver.hpp:119-520) with
+ * Mesh::BuildGMGBlockLists / SetGMGNeighbors (src/mesh/mesh-gmg.cpp:103-201). */
+typedef struct pgb_mg pgb_mg;
+typedef struct {
+  int32_t stages;          /* SRJ stages 1..3, or weighted-Jacobi sweeps when jacobi */
+  int32_t jacobi;          /* 0: SRJ (Yang-Mittal weights); 1: weighted Jacobi with weight */
+  double weight;
+  int32_t coarse_sweeps;   /* extra smoother passes on the coarsest grid (0 = reference) */
+  int32_t max_coarsenings; /* MGParams::max_coarsenings: grids max .. max(max - this, min) */
+  double D;                /* constant face coefficient (the poisson D field) */
+  double alpha;            /* poisson/diagonal_alpha */
+} pgb_mg_params;
+/* Host only: builds the composite grids of the mesh (which must outlive the solver);
+ * device memory is taken on the first solve. */
+int pgb_mg_create(pgb_mesh *mesh, const pgb_mg_params *params, pgb_mg **out);
+int pgb_mg_destroy(pgb_mg *mg);
+/* out[5]: coarsest and finest logical level, storage slots of full-size blocks, leaf
+ * blocks, grids */
+int pgb_mg_info(const pgb_mg *mg, int32_t *out);
+/* gmg_same boundary index maps of grid `level` in the pgb_mesh_boundaries record
+ * format; *count receives the number of records (out may be NULL to query it). */
+int pgb_mg_boundaries(const pgb_mg *mg, int32_t level, int32_t *out, int32_t capacity, int32_t *count);
+/* u, rhs: device arrays of the leaf blocks, [block][k][j][i] with ghosts (one
+ * component). ncycles V-cycles on u (in/out: interior result, ghosts exchanged);
+ * rms (host, may be NULL) receives sqrt(sum r^2 / N) of the leaf residual after each.
+ * The stream must be a created stream (each iteration is one CUDA-graph launch). */
+int pgb_mg_vcycles(pgb_mg *mg, double *u, const double *rhs, int32_t ncycles, double *rms, void *stream);
+/* V-cycles until rms(rhs - A u) <= tol (relative = 0, the reference's
+ * residual_tolerance) or <= tol * the initial rms (relative = 1), or max_cycles. */
+int pgb_mg_solve(pgb_mg *mg, double *u, const double *rhs, double tol, int32_t relative, int32_t max_cycles,
+                 int32_t *cycles_out, double *rms_out, void *stream);
+
 /* ---- launch-shape autotuner ------------------------------------------------------ */
 
 /* The first pgb_rk2_cycles call on a mesh (before it captures the cycle graph) times a

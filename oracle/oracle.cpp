@@ -47,13 +47,18 @@ struct Field {
   int ncomp = 1;
   int N[3], Nc[3];
   std::vector<double> data, coarse;
+  // Storage slot of block index b of the block list in use (null: slot b). The
+  // multigrid keeps every block of its composite grids in one store, so a leaf that
+  // belongs to two grids is one block, as in the reference (mesh-gmg.cpp:124-132).
+  const std::vector<int> *slot = nullptr;
+  int64_t sl(int b) const { return slot ? (*slot)[b] : b; }
   int64_t bstride() const { return (int64_t)ncomp * N[0] * N[1] * N[2]; }
   int64_t cstride() const { return (int64_t)ncomp * Nc[0] * Nc[1] * Nc[2]; }
   double &at(int b, int v, int k, int j, int i) {
-    return data[b * bstride() + (((int64_t)v * N[2] + k) * N[1] + j) * N[0] + i];
+    return data[sl(b) * bstride() + (((int64_t)v * N[2] + k) * N[1] + j) * N[0] + i];
   }
   double &cat(int b, int v, int k, int j, int i) {
-    return coarse[b * cstride() + (((int64_t)v * Nc[2] + k) * Nc[1] + j) * Nc[0] + i];
+    return coarse[sl(b) * cstride() + (((int64_t)v * Nc[2] + k) * Nc[1] + j) * Nc[0] + i];
   }
   double &any(bool c, int b, int v, int k, int j, int i) {
     return c ? cat(b, v, k, j, i) : at(b, v, k, j, i);
@@ -69,6 +74,18 @@ struct Field {
     }
     data.assign(bl->size() * bstride(), 0.0);
     coarse.assign(bl->size() * cstride(), 0.0);
+  }
+  // `nslots` blocks of nx cells (one component), addressed through `slot`
+  void init_store(const Mesh *m, const int nx[3], int nslots) {
+    mesh = m;
+    blocks = nullptr;
+    ncomp = 1;
+    for (int d = 0; d < 3; ++d) {
+      N[d] = nx[d] + 2 * m->p.ng;
+      Nc[d] = std::max(1, nx[d] / 2) + 2 * m->p.ng;
+    }
+    data.assign((size_t)nslots * bstride(), 0.0);
+    coarse.assign((size_t)nslots * cstride(), 0.0);
   }
   // zero one variable of one block (fine and coarse arrays)
   void zero(int b, int v) {
@@ -1027,6 +1044,9 @@ inline void cycle(Sim &s) {
 
 }  // namespace oracle
 
+// multigrid on composite grids of refined meshes (uses Field, exchange, calc_indices)
+#include "gmg_blocks.hpp"
+
 // ======================================================================== C API
 using namespace oracle;
 
@@ -1421,6 +1441,78 @@ double orc_gmg_residual(void *h) {
   Gmg *g = (Gmg *)h;
   return std::sqrt(g->residual() / (double)g->lv[0].size());
 }
+// ---- multigrid on the composite grids of a (refined) mesh; the Sim must outlive it
+void *orc_mgb_create(void *sim, int stages, int jacobi, double weight, int coarse_sweeps, int max_coarsenings,
+                     double D, double alpha) {
+  try {
+    GmgParams p;
+    p.smoother_stages = stages;
+    p.jacobi = jacobi != 0;
+    p.weight = weight;
+    p.coarse_sweeps = coarse_sweeps;
+    p.D = D;
+    p.alpha = alpha;
+    return new BlockGmg(*((Sim *)sim)->mesh, p, max_coarsenings);
+  } catch (std::exception &e) {
+    fprintf(stderr, "oracle: %s\n", e.what());
+    return nullptr;
+  }
+}
+void orc_mgb_destroy(void *h) { delete (BlockGmg *)h; }
+// out: lmin, lmax, storage slots of the full-size blocks, leaves
+void orc_mgb_info(void *h, int32_t *out) {
+  BlockGmg *g = (BlockGmg *)h;
+  out[0] = g->lmin;
+  out[1] = g->lmax;
+  out[2] = g->nslot0;
+  out[3] = g->nleaf;
+}
+// leaf arrays [nleaf][N3][N2][N1] (the first slots of the full-size store)
+double *orc_mgb_u(void *h) { return ((BlockGmg *)h)->store.at(0).u.data.data(); }
+double *orc_mgb_rhs(void *h) { return ((BlockGmg *)h)->store.at(0).rhs.data.data(); }
+double *orc_mgb_res(void *h) { return ((BlockGmg *)h)->store.at(0).res.data.data(); }
+// ncycles V-cycles; rms[c] = sqrt(sum r^2 / N) of the leaf residual after cycle c
+void orc_mgb_run(void *h, int ncycles, double *rms) {
+  BlockGmg *g = (BlockGmg *)h;
+  for (int c = 0; c < ncycles; ++c) {
+    g->vcycle();
+    const double s = g->residual();
+    if (rms) rms[c] = std::sqrt(s / g->ncells());
+  }
+}
+double orc_mgb_residual(void *h) {
+  BlockGmg *g = (BlockGmg *)h;
+  return std::sqrt(g->residual() / g->ncells());
+}
+// gmg_same boundary records of composite grid `level` (the orc_boundaries format)
+int orc_mgb_num_boundaries(void *h, int level) {
+  BlockGmg *g = (BlockGmg *)h;
+  auto it = g->recs.find(level);
+  return it == g->recs.end() ? -1 : (int)it->second.size();
+}
+void orc_mgb_boundaries(void *h, int level, int32_t *out) {
+  BlockGmg *g = (BlockGmg *)h;
+  const auto &bl = g->m.gmg_levels.at(level);
+  int r = 0;
+  for (auto &br : g->recs.at(level)) {
+    int32_t *o = out + 23 * r++;
+    o[0] = bl[br.sender].gid;
+    o[1] = bl[br.receiver].gid;
+    o[2] = br.locidx;
+    for (int d = 0; d < 3; ++d) {
+      o[3 + 2 * d] = br.send.s[d];
+      o[4 + 2 * d] = br.send.e[d];
+      o[10 + 2 * d] = br.recv.s[d];
+      o[11 + 2 * d] = br.recv.e[d];
+    }
+    o[9] = br.send_coarse;
+    o[16] = br.recv_coarse;
+    o[17] = (int32_t)br.recv.mask.bits();
+    o[18] = (int32_t)br.send.size();
+    o[19] = o[20] = o[21] = o[22] = 0;
+  }
+}
+
 // BiCGSTAB on rhs (n^3 values) with the V-cycle preconditioner; x receives the
 // solution; returns the iterations run, *rms the final rms residual.
 int orc_bicgstab(void *h, const double *rhs, double *x, int precondition, double rtol, int relative, int max_iters,

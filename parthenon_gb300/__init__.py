@@ -6,10 +6,10 @@ reference's mesh / exchange / driver interface; all compute runs in the library.
 """
 from .mesh import Mesh  # noqa: F401
 from .driver import RK2Driver, StageConfig  # noqa: F401
-from .gmg import GmgSolver  # noqa: F401
+from .gmg import CompositeMultigrid, GmgSolver  # noqa: F401
 from .amr import AMRDriver, RefinementCriterion, SparseMinMaxCriterion  # noqa: F401
 from . import history, problems  # noqa: F401
 from ._native import NativeError  # noqa: F401
 
-__all__ = ["Mesh", "RK2Driver", "StageConfig", "GmgSolver", "AMRDriver", "RefinementCriterion",
+__all__ = ["Mesh", "RK2Driver", "StageConfig", "GmgSolver", "CompositeMultigrid", "AMRDriver", "RefinementCriterion",
            "SparseMinMaxCriterion", "history", "problems", "NativeError"]

@@ -34,6 +34,12 @@ class GmgParams(ctypes.Structure):
                 ("exact", ctypes.c_int32), ("xmin", ctypes.c_double), ("xmax", ctypes.c_double)]
 
 
+class MgParams(ctypes.Structure):
+    _fields_ = [("stages", ctypes.c_int32), ("jacobi", ctypes.c_int32), ("weight", ctypes.c_double),
+                ("coarse_sweeps", ctypes.c_int32), ("max_coarsenings", ctypes.c_int32), ("D", ctypes.c_double),
+                ("alpha", ctypes.c_double)]
+
+
 class StageParams(ctypes.Structure):
     _fields_ = [("physics", ctypes.c_int32), ("recon", ctypes.c_int32), ("exact", ctypes.c_int32),
                 ("ncomp_vel", ctypes.c_int32), ("vel", ctypes.c_double * 3), ("cfl", ctypes.c_double),
@@ -75,6 +81,13 @@ _SIGNATURES = {
                          ctypes.POINTER(ctypes.c_int32), DP, VP],
     "pgb_gmg_solve_blocks": [VP, VP, VP, VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                              ctypes.c_double, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), DP, VP],
+    "pgb_mg_create": [VP, ctypes.POINTER(MgParams), ctypes.POINTER(VP)],
+    "pgb_mg_destroy": [VP],
+    "pgb_mg_info": [VP, VP],
+    "pgb_mg_boundaries": [VP, ctypes.c_int32, VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)],
+    "pgb_mg_vcycles": [VP, VP, VP, ctypes.c_int32, VP, VP],
+    "pgb_mg_solve": [VP, VP, VP, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                     DP, VP],
     "pgb_history_mass": [VP, VP, ctypes.c_int32, VP, ctypes.c_int32, ctypes.c_double, VP, VP],
     "pgb_tune_report": [ctypes.c_char_p, ctypes.c_int32],
     "pgb_amr_block_criterion": [VP, VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, VP, VP],

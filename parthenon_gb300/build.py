@@ -22,6 +22,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 PER_FILE = {
     "stencil_exact.cu": ["-fmad=false"],
     "gmg_exact.cu": ["-fmad=false"],
+    "mg_blocks.cu": ["-fmad=false"],
 }
 
 

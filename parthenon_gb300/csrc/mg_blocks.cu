@@ -1,0 +1,806 @@
+// Multigrid on the two-level composite grids of a refined mesh (FP64).
+//
+// MGSolver on a mesh with refinement (src/solvers/mg_solver.hpp:119-520) runs its FAS
+// V-cycle over the grids of src/mesh/mesh-gmg.cpp:103-201: grid L holds every block of
+// level L (leaves and internal blocks) and the leaves of level L-1; the level-L blocks
+// are the active ones (packs of a composite grid hold the finer blocks only,
+// src/interface/sparse_pack.hpp:69-109) and the coarser leaves lend their values across
+// coarse/fine faces through the grid's ghost exchange.
+//
+// Layout. Every block of the full block size (the leaves first, in gid order, then the
+// internal blocks of levels >= 0 by gid) owns one slot of a store of five arrays (u,
+// res_err, rhs, temp, u0) with ghosts, one component, x fastest; the blocks below level
+// 0 are smaller and have a store per level. A leaf in two grids is one slot, as the
+// reference shares the MeshBlock between the two lists, so nothing moves between grids
+// but the restriction and the prolongation. Each grid's gmg_same exchange runs the
+// leaf-grid exchange kernels (exchange.cu) on tables whose block indices are store
+// slots.
+//
+// Fused steps per level: Ax + Jacobi, Ax + residual, Ax + FAS right-hand side; the
+// restriction of u and res_err writes the parent's octant directly (the child's coarse
+// buffer and the message buffer hold the same values); the linear prolongation of
+// res_err is added straight into u over the child's interior. The values the reference
+// also prolongates into the child's ghosts, and the child's res_err after the update,
+// are never read again and are not written. Every read of a ghost cell follows an
+// exchange that writes it. One V-cycle plus the leaf-grid residual is one CUDA graph.
+//
+// The file is compiled with -fmad=false and divides by powers of two as exact
+// multiplications (div_rn), so every value rounds as in the reference's host arithmetic
+// and the interiors are bitwise those of the CPU restatement.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <set>
+#include <stdexcept>
+#include <vector>
+
+#include "../../include/parthenon_gb300.h"
+#include "common.cuh"
+#include "gmg_state.hpp"
+#include "mesh_state.hpp"
+
+namespace pgb {
+MeshState *mesh_state(pgb_mesh *m);
+int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate, int prolong_op,
+                  double *buffer, cudaStream_t s, const SparseDev *sp);
+}  // namespace pgb
+
+using namespace pgb;
+
+namespace {
+
+// One fine block of a grid and its parent in the next coarser grid: `lo` is the first
+// interior cell of the parent's octant that the child covers (parent index space with
+// ghosts), from the InteriorRecv range of bnd_info.cpp:105-252.
+struct MgXfer {
+  int32_t child, parent;
+  int32_t lo[3];
+  int32_t pad;
+};
+
+struct StoreView {
+  double *u, *res, *rhs, *temp, *u0;
+  Dims d;
+};
+
+struct MgOp {
+  double D, alpha;
+};
+
+__device__ __forceinline__ int64_t cell_of(const Dims &d, int slot, int k, int j, int i) {
+  return ((int64_t)slot * d.N[2] + k) * ((int64_t)d.N[1] * d.N[0]) + (int64_t)j * d.N[0] + i;
+}
+
+// Every interior cell of the listed blocks, consecutive threads on consecutive i.
+template <class F>
+__device__ __forceinline__ void for_interior(const int *__restrict__ list, int n, const Dims &d, F &&f) {
+  const int64_t per = (int64_t)d.nx[0] * d.nx[1] * d.nx[2];
+  const int64_t total = per * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(e / per);
+    const int64_t c = e - q * per;
+    const int i = (int)(c % d.nx[0]);
+    const int64_t r = c / d.nx[0];
+    const int j = (int)(r % d.nx[1]);
+    const int k = (int)(r / d.nx[1]);
+    f(list[q], k + d.ng, j + d.ng, i + d.ng);
+  }
+}
+
+// poisson_equation.hpp:104-210: face fluxes D grad u, then their divergence (-alpha u +
+// sum over directions of (F_left - F_right) / dx), in the reference's order
+__device__ __forceinline__ double apply_op(const double *__restrict__ u, int64_t c, int64_t sj, int64_t sk,
+                                           const DevBlockGeom &g, const MgOp &o) {
+  const double D = o.D, dx1 = g.dx[0], dx2 = g.dx[1], dx3 = g.dx[2];
+  const double uc = u[c];
+  const double f1l = div_rn(D, dx1) * (u[c - 1] - uc);
+  const double f1r = div_rn(D, dx1) * (uc - u[c + 1]);
+  const double f2l = div_rn(D * (u[c - sj] - uc), dx2);
+  const double f2r = div_rn(D * (uc - u[c + sj]), dx2);
+  const double f3l = div_rn(D * (u[c - sk] - uc), dx3);
+  const double f3r = div_rn(D * (uc - u[c + sk]), dx3);
+  double out = -o.alpha * uc;
+  out += div_rn(f1l - f1r, dx1);
+  out += div_rn(f2l - f2r, dx2);
+  out += div_rn(f3l - f3r, dx3);
+  return out;
+}
+
+// poisson_equation.hpp:59-102 (SetDiagonal)
+__device__ __forceinline__ double diag_of(const DevBlockGeom &g, const MgOp &o) {
+  const double D = o.D;
+  double d = -div_rn(D + D, g.dx[0] * g.dx[0]) - o.alpha;
+  d -= div_rn(D + D, g.dx[1] * g.dx[1]);
+  d -= div_rn(D + D, g.dx[2] * g.dx[2]);
+  return d;
+}
+
+// Ax + Jacobi (mg_solver.hpp:222-297): temp = w ratio(rhs - (Ax - D u), D) + (1 - w) u
+__global__ void __launch_bounds__(256) k_mg_jacobi(StoreView s, const int *__restrict__ list, int n,
+                                                   const DevBlockGeom *__restrict__ geom, MgOp o, double w) {
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
+  const double small = 10.0 * DBL_MIN;  // robust::ratio (utils/robust.hpp)
+  for_interior(list, n, s.d, [&](int b, int k, int j, int i) {
+    const DevBlockGeom &g = geom[b];
+    const int64_t c = cell_of(s.d, b, k, j, i);
+    const double dg = diag_of(g, o);
+    const double den = dg + (dg >= 0 ? 1.0 : -1.0) * small;
+    const double a = apply_op(s.u, c, sj, sk, g, o);
+    const double off = a - dg * s.u[c];
+    const double val = s.rhs[c] - off;
+    s.temp[c] = w * div_rn(val, den) + (1.0 - w) * s.u[c];
+  });
+}
+
+// Ax + AddFieldsAndStoreInteriorSelect<rhs, temp, res_err>(1, -1): res = rhs - A u
+__global__ void __launch_bounds__(256) k_mg_residual(StoreView s, const int *__restrict__ list, int n,
+                                                     const DevBlockGeom *__restrict__ geom, MgOp o) {
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
+  for_interior(list, n, s.d, [&](int b, int k, int j, int i) {
+    const int64_t c = cell_of(s.d, b, k, j, i);
+    const double t = apply_op(s.u, c, sj, sk, geom[b], o);
+    s.res[c] = s.rhs[c] - t;
+  });
+}
+
+// FAS on internal blocks (mg_solver.hpp:413-430): rhs = A u + res_err
+__global__ void __launch_bounds__(256) k_mg_fas(StoreView s, const int *__restrict__ list, int n,
+                                                const DevBlockGeom *__restrict__ geom, MgOp o) {
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
+  for_interior(list, n, s.d, [&](int b, int k, int j, int i) {
+    const int64_t c = cell_of(s.d, b, k, j, i);
+    const double t = apply_op(s.u, c, sj, sk, geom[b], o);
+    s.rhs[c] = t + s.res[c];
+  });
+}
+
+// CopyData on the interiors of the listed blocks
+__global__ void __launch_bounds__(256) k_mg_copy(double *__restrict__ dst, const double *__restrict__ src,
+                                                 const int *__restrict__ list, int n, Dims d) {
+  for_interior(list, n, d, [&](int b, int k, int j, int i) {
+    const int64_t c = cell_of(d, b, k, j, i);
+    dst[c] = src[c];
+  });
+}
+
+// AddFieldsAndStore<u, u0, res_err>(1, -1): res = u - u0
+__global__ void __launch_bounds__(256) k_mg_error(StoreView s, const int *__restrict__ list, int n) {
+  for_interior(list, n, s.d, [&](int b, int k, int j, int i) {
+    const int64_t c = cell_of(s.d, b, k, j, i);
+    s.res[c] = s.u[c] - s.u0[c];
+  });
+}
+
+// RestrictAverage (pr_ops.hpp:105-164) of the child's interior, u and res_err, into the
+// parent's octant (gmg_restrict_send + gmg_restrict_recv). One thread per parent cell.
+__global__ void __launch_bounds__(256) k_mg_restrict(StoreView cs, StoreView ps, const MgXfer *__restrict__ x,
+                                                     int n, const DevBlockGeom *__restrict__ cgeom) {
+  const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
+  const int64_t per = (int64_t)h0 * h1 * h2, total = per * n;
+  const int ng = cs.d.ng;
+  const int64_t cj = cs.d.N[0], ck = (int64_t)cs.d.N[0] * cs.d.N[1];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(e / per);
+    const int64_t r = e - q * per;
+    const int ci = (int)(r % h0), cjj = (int)((r / h0) % h1), ckk = (int)(r / ((int64_t)h0 * h1));
+    const MgXfer t = x[q];
+    const double vol = cgeom[t.child].vol;
+    const int64_t f = cell_of(cs.d, t.child, 2 * ckk + ng, 2 * cjj + ng, 2 * ci + ng);
+    const int64_t p = cell_of(ps.d, t.parent, t.lo[2] + ckk, t.lo[1] + cjj, t.lo[0] + ci);
+    const double tv = ((vol + vol) + (vol + vol)) + ((vol + vol) + (vol + vol));
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const double *__restrict__ a = v == 0 ? cs.u : cs.res;
+      // t[ok][oj][oi] = vol * fine(k + ok, j + oj, i + oi)
+      const double t000 = vol * a[f], t001 = vol * a[f + 1];
+      const double t010 = vol * a[f + cj], t011 = vol * a[f + cj + 1];
+      const double t100 = vol * a[f + ck], t101 = vol * a[f + ck + 1];
+      const double t110 = vol * a[f + ck + cj], t111 = vol * a[f + ck + cj + 1];
+      const double num = ((t000 + t010) + (t001 + t011)) + ((t100 + t110) + (t101 + t111));
+      (v == 0 ? ps.u : ps.res)[p] = div_rn(num, tv);
+    }
+  }
+}
+
+// ProlongateSharedLinear (pr_ops.hpp:166-285) of the parent's res_err (its octant with
+// ghosts is the child's coarse buffer) and AddFieldsAndStore<u, res_err, u>: one thread
+// per coarse cell of the child's interior, eight fine cells each.
+__global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView cs, StoreView ps, const MgXfer *__restrict__ x,
+                                                        int n, const DevBlockGeom *__restrict__ cgeom) {
+  const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
+  const int64_t per = (int64_t)h0 * h1 * h2, total = per * n;
+  const int ng = cs.d.ng;
+  const int64_t pj = ps.d.N[0], pk = (int64_t)ps.d.N[0] * ps.d.N[1];
+  const int64_t N0 = cs.d.N[0], N01 = (int64_t)cs.d.N[0] * cs.d.N[1];
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(e / per);
+    const int64_t r = e - q * per;
+    const int c0 = (int)(r % h0), c1 = (int)((r / h0) % h1), c2 = (int)(r / ((int64_t)h0 * h1));
+    const MgXfer t = x[q];
+    const DevBlockGeom &g = cgeom[t.child];
+    const int c[3] = {c0 + ng, c1 + ng, c2 + ng};  // coarse-buffer index
+    const int f[3] = {2 * c0 + ng, 2 * c1 + ng, 2 * c2 + ng};
+    const int64_t pe = cell_of(ps.d, t.parent, t.lo[2] + c2, t.lo[1] + c1, t.lo[0] + c0);
+    const double fc = ps.res[pe];
+    double mq[3], pq[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      auto xcc = [&](int idx) { return g.cxmin[d] + ((double)idx + 0.5) * g.cdx[d]; };
+      auto xfc = [&](int idx) { return g.xmin[d] + ((double)idx + 0.5) * g.dx[d]; };
+      const double xm = xcc(c[d] - 1), xc = xcc(c[d]), xp = xcc(c[d] + 1);
+      const double dxm = xc - xm, dxp = xp - xc;
+      const double dfm = xc - xfc(f[d]);
+      const double dfp = xfc(f[d] + 1) - xc;
+      const int64_t st = d == 0 ? 1 : (d == 1 ? pj : pk);
+      const double gm = div_rn(fc - ps.res[pe - st], dxm);
+      const double gp = div_rn(ps.res[pe + st] - fc, dxp);
+      mq[d] = gm * dfm;
+      pq[d] = gp * dfp;
+    }
+    const double m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
+    double *U = cs.u + cell_of(cs.d, t.child, f[2], f[1], f[0]);
+    U[0] = U[0] + (fc - ((m0 + m1) + m2));
+    U[1] = U[1] + (fc + ((p0 - m1) - m2));
+    U[N0] = U[N0] + (fc - ((m0 - p1) + m2));
+    U[N0 + 1] = U[N0 + 1] + (fc + ((p0 + p1) - m2));
+    U[N01] = U[N01] + (fc - ((m0 + m1) - p2));
+    U[N01 + 1] = U[N01 + 1] + (fc + ((p0 - m1) + p2));
+    U[N01 + N0] = U[N01 + N0] + (fc - ((m0 - p1) - p2));
+    U[N01 + N0 + 1] = U[N01 + N0 + 1] + (fc + ((p0 + p1) + p2));
+  }
+}
+
+// Leaf-grid residual of MGSolver::AddTasks (mg_solver.hpp:135-158): res = rhs - A u
+// over every leaf interior and one partial sum of r^2 per CTA (fixed tree order, so
+// the host's fixed-order total is reproducible)
+constexpr int kResThreads = 256;
+__global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView s, int nleaf,
+                                                                  const DevBlockGeom *__restrict__ geom, MgOp o,
+                                                                  double *__restrict__ partial) {
+  __shared__ double sh[kResThreads];
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
+  const int64_t per = (int64_t)s.d.nx[0] * s.d.nx[1] * s.d.nx[2], total = per * nleaf;
+  double acc = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(e / per);
+    const int64_t cc = e - b * per;
+    const int i = (int)(cc % s.d.nx[0]), j = (int)((cc / s.d.nx[0]) % s.d.nx[1]);
+    const int k = (int)(cc / ((int64_t)s.d.nx[0] * s.d.nx[1]));
+    const int64_t c = cell_of(s.d, b, k + s.d.ng, j + s.d.ng, i + s.d.ng);
+    const double r = s.rhs[c] - apply_op(s.u, c, sj, sk, geom[b], o);
+    s.res[c] = r;
+    acc += r * r;
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kResThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+unsigned grid_for(int64_t work) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 16));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------- handle
+struct pgb_mg {
+  pgb_mesh *mesh = nullptr;
+  MeshTopology *topo = nullptr;
+  GmgConfig cfg;
+  int max_coarsenings = 30;
+  int lmin = 0, lmax = 0, nleaf = 0;
+  struct Store {
+    int nslots = 0;
+    std::vector<BlockInfo> blocks;
+    double *u = nullptr, *res = nullptr, *rhs = nullptr, *temp = nullptr, *u0 = nullptr, *coarse = nullptr;
+    Dims dims{};
+    StoreView view() const { return StoreView{u, res, rhs, temp, u0, dims}; }
+  };
+  std::map<int, Store> stores;  // key 0: full-size blocks; key L < 0: the blocks of level L
+  struct Grid {
+    int level = 0, store = 0;
+    GridTopology remap;  // the composite grid's exchange boxes over store slots
+    GridTables tab;
+    std::vector<int> fine_h, internal_h;
+    std::vector<MgXfer> xfer_h;  // fine blocks and their parents (grids above the coarsest)
+    int *fine = nullptr, *internal = nullptr;
+    MgXfer *xfer = nullptr;
+  };
+  std::map<int, Grid> grids;
+  GridTables leaf_tab;
+  void *lists = nullptr;
+  double *partial = nullptr, *partial_h = nullptr;
+  int nparts = 0;
+  bool uploaded = false;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<void *> allocs;
+
+  static int key(int level) { return level >= 0 ? 0 : level; }
+  Store &store_of(int level) { return stores.at(key(level)); }
+
+  ~pgb_mg() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (auto &kv : grids) kv.second.tab.release();
+    leaf_tab.release();
+    for (void *p : allocs) cudaFree(p);
+    if (lists) cudaFree(lists);
+    if (partial_h) cudaFreeHost(partial_h);
+  }
+};
+
+namespace {
+
+// Composite grids, store slots and transfer records (host only).
+int mg_build(pgb_mg *g) {
+  MeshTopology &topo = *g->topo;
+  const MeshSpec &spec = topo.spec();
+  const int ng = spec.ng;
+  topo.build_multigrid();
+  g->lmax = topo.max_level();
+  g->lmin = std::max(g->lmax - g->max_coarsenings, topo.mg_min_level());
+  const auto &leaves = topo.leaf().blocks;
+  g->nleaf = (int)leaves.size();
+  const auto &mg = topo.mg_grids();
+  // store 0: leaves (slot = leaf index = gid), then internal blocks of levels >= 0 by gid
+  std::map<int, int> slot0;
+  pgb_mg::Store &s0 = g->stores[0];
+  for (int b = 0; b < g->nleaf; ++b) {
+    slot0[leaves[b].gid] = b;
+    s0.blocks.push_back(leaves[b]);
+  }
+  std::map<int, const BlockInfo *> internal0;
+  for (int L = std::max(g->lmin, 0); L <= g->lmax; ++L)
+    for (auto &b : mg.at(L).blocks)
+      if (!slot0.count(b.gid)) internal0[b.gid] = &b;
+  for (auto &kv : internal0) {
+    slot0[kv.first] = (int)s0.blocks.size();
+    s0.blocks.push_back(*kv.second);
+  }
+  for (auto &b : s0.blocks) {
+    b.nbrs.clear();
+    b.same_nbrs.clear();
+  }
+  for (int L = g->lmin; L <= g->lmax; ++L) {
+    const GridTopology &src = mg.at(L);
+    if (src.blocks.empty()) return fail(kErrInvalid, "empty multigrid level");
+    for (auto &b : src.blocks)
+      if (b.loc.level != L && (L == g->lmin || b.loc.level != L - 1))
+        return fail(kErrUnsupported, "the coarsest multigrid grid holds leaves of a coarser level "
+                                     "(max_coarsenings must reach the root grid)");
+    pgb_mg::Grid &G = g->grids[L];
+    G.level = L;
+    G.store = pgb_mg::key(L);
+    std::vector<int> slot(src.blocks.size());
+    if (L >= 0) {
+      for (size_t i = 0; i < src.blocks.size(); ++i) slot[i] = slot0.at(src.blocks[i].gid);
+    } else {
+      pgb_mg::Store &sl = g->stores[L];
+      for (size_t i = 0; i < src.blocks.size(); ++i) {
+        slot[i] = (int)i;
+        sl.blocks.push_back(src.blocks[i]);
+        sl.blocks.back().same_nbrs.clear();
+      }
+    }
+    G.remap.logical_level = L;
+    G.remap.multilevel = src.multilevel;
+    G.remap.pairs = src.pairs;
+    for (auto &p : G.remap.pairs) {
+      p.sender = slot[p.sender];
+      p.receiver = slot[p.receiver];
+    }
+    auto remap_regions = [&](const std::vector<CoarseRegion> &in, std::vector<CoarseRegion> &out) {
+      out = in;
+      for (auto &r : out) r.block = slot[r.block];
+    };
+    remap_regions(src.restrict_send, G.remap.restrict_send);
+    remap_regions(src.restrict_recv, G.remap.restrict_recv);
+    remap_regions(src.prolong, G.remap.prolong);
+    for (size_t i = 0; i < src.blocks.size(); ++i) {
+      const BlockInfo &b = src.blocks[i];
+      if (b.loc.level != L) continue;
+      G.fine_h.push_back(slot[i]);
+      if (!topo.is_leaf(b.loc)) G.internal_h.push_back(slot[i]);
+    }
+  }
+  // transfers between grid L and L - 1, per fine block of grid L
+  for (int L = g->lmin + 1; L <= g->lmax; ++L) {
+    pgb_mg::Grid &G = g->grids[L];
+    const GridTopology &src = mg.at(L), &par = mg.at(L - 1);
+    std::map<int, int> pidx;
+    for (size_t i = 0; i < par.blocks.size(); ++i) pidx[par.blocks[i].gid] = (int)i;
+    for (size_t i = 0; i < src.blocks.size(); ++i) {
+      const BlockInfo &c = src.blocks[i];
+      if (c.loc.level != L) continue;
+      if (c.coarser.empty()) return fail(kErrInvalid, "multigrid block without a parent");
+      const Neighbor &up = c.coarser[0];
+      const int pi = pidx.at(up.gid);
+      const BlockInfo &p = par.blocks[pi];
+      const Neighbor *down = nullptr;
+      for (auto &n : p.finer)
+        if (n.gid == c.gid) down = &n;
+      if (!down) return fail(kErrInvalid, "parent does not list its child");
+      // gmg_restrict: child's coarse interior -> parent's octant; gmg_prolongate: the
+      // octant with ng ghosts -> the child's whole coarse buffer
+      const IBox rs = boundary_box(up, c.loc, c.nx, ng, 0, RangeKind::InteriorSend, true, false);
+      const IBox tr = boundary_box(*down, p.loc, p.nx, ng, 0, RangeKind::InteriorRecv, false, false);
+      const IBox ps = boundary_box(*down, p.loc, p.nx, ng, 0, RangeKind::InteriorSend, false, false);
+      const IBox pr = boundary_box(up, c.loc, c.nx, ng, 0, RangeKind::InteriorRecv, false, false);
+      for (int d = 0; d < 3; ++d) {
+        const int h = std::max(1, c.nx[d] / 2);
+        if (rs.lo[d] != ng || rs.hi[d] != ng + h - 1 || tr.hi[d] - tr.lo[d] != h - 1 || ps.lo[d] != tr.lo[d] - ng ||
+            ps.hi[d] != tr.hi[d] + ng || pr.lo[d] != 0 || pr.hi[d] != h + 2 * ng - 1)
+          return fail(kErrUnsupported, "multigrid transfer ranges of unexpected shape");
+      }
+      MgXfer x;
+      x.child = slot0.count(c.gid) && L >= 0 ? slot0.at(c.gid) : (int)i;
+      x.parent = L - 1 >= 0 ? slot0.at(p.gid) : pi;
+      for (int d = 0; d < 3; ++d) x.lo[d] = tr.lo[d];
+      x.pad = 0;
+      G.xfer_h.push_back(x);
+    }
+  }
+  for (auto &kv : g->stores) {
+    pgb_mg::Store &S = kv.second;
+    S.nslots = (int)S.blocks.size();
+    for (auto &kv2 : g->grids)
+      if (kv2.second.store == kv.first) kv2.second.remap.blocks = S.blocks;
+  }
+  // every table must keep its accesses inside the store arrays (checked before upload)
+  for (auto &kv : g->grids) {
+    GridTables scratch;
+    int rc = lower_grid(kv.second.remap, spec, scratch, true);
+    if (rc) return rc;
+  }
+  return kOk;
+}
+
+int mg_upload(pgb_mg *g) {
+  if (g->uploaded) return kOk;
+  const MeshSpec &spec = g->topo->spec();
+  for (auto &kv : g->grids) {
+    int rc = lower_grid(kv.second.remap, spec, kv.second.tab);
+    if (rc) return rc;
+  }
+  int rc = lower_grid(g->topo->leaf(), spec, g->leaf_tab);
+  if (rc) return rc;
+  for (auto &kv : g->stores) {
+    pgb_mg::Store &S = kv.second;
+    const pgb_mg::Grid *G = nullptr;
+    for (auto &kv2 : g->grids)
+      if (kv2.second.store == kv.first) G = &kv2.second;
+    S.dims = G->tab.dims;
+    const int64_t n = (int64_t)S.nslots * S.dims.N[0] * S.dims.N[1] * S.dims.N[2];
+    const int64_t nc = (int64_t)S.nslots * S.dims.Nc[0] * S.dims.Nc[1] * S.dims.Nc[2];
+    for (double **p : {&S.u, &S.res, &S.rhs, &S.temp, &S.u0}) {
+      PGB_CUDA(cudaMalloc((void **)p, n * sizeof(double)));
+      PGB_CUDA(cudaMemset(*p, 0, n * sizeof(double)));
+      g->allocs.push_back(*p);
+    }
+    PGB_CUDA(cudaMalloc((void **)&S.coarse, nc * sizeof(double)));
+    PGB_CUDA(cudaMemset(S.coarse, 0, nc * sizeof(double)));
+    g->allocs.push_back(S.coarse);
+  }
+  // block lists and transfers in one allocation
+  size_t bytes = 0;
+  auto room = [&](size_t n) {
+    const size_t off = bytes;
+    bytes = (bytes + n + 255) & ~size_t(255);
+    return off;
+  };
+  struct Off {
+    size_t fine, internal, xfer;
+  };
+  std::map<int, Off> off;
+  for (auto &kv : g->grids) {
+    Off o;
+    o.fine = room(kv.second.fine_h.size() * sizeof(int));
+    o.internal = room(kv.second.internal_h.size() * sizeof(int));
+    o.xfer = room(kv.second.xfer_h.size() * sizeof(MgXfer));
+    off[kv.first] = o;
+  }
+  std::vector<char> h(std::max<size_t>(bytes, 256), 0);
+  for (auto &kv : g->grids) {
+    const Off &o = off[kv.first];
+    auto &G = kv.second;
+    std::memcpy(h.data() + o.fine, G.fine_h.data(), G.fine_h.size() * sizeof(int));
+    std::memcpy(h.data() + o.internal, G.internal_h.data(), G.internal_h.size() * sizeof(int));
+    std::memcpy(h.data() + o.xfer, G.xfer_h.data(), G.xfer_h.size() * sizeof(MgXfer));
+  }
+  PGB_CUDA(cudaMalloc(&g->lists, h.size()));
+  PGB_CUDA(cudaMemcpy(g->lists, h.data(), h.size(), cudaMemcpyHostToDevice));
+  for (auto &kv : g->grids) {
+    const Off &o = off[kv.first];
+    char *base = static_cast<char *>(g->lists);
+    kv.second.fine = reinterpret_cast<int *>(base + o.fine);
+    kv.second.internal = reinterpret_cast<int *>(base + o.internal);
+    kv.second.xfer = reinterpret_cast<MgXfer *>(base + o.xfer);
+  }
+  const Dims &d0 = g->stores.at(0).dims;
+  g->nparts = (int)grid_for((int64_t)g->nleaf * d0.nx[0] * d0.nx[1] * d0.nx[2]);
+  PGB_CUDA(cudaMalloc((void **)&g->partial, g->nparts * sizeof(double)));
+  g->allocs.push_back(g->partial);
+  PGB_CUDA(cudaMallocHost((void **)&g->partial_h, g->nparts * sizeof(double)));
+  g->uploaded = true;
+  return kOk;
+}
+
+double srj_weight(const GmgConfig &c, int s) {
+  // mg_solver.hpp:312-345, 3D weights (Yang & Mittal)
+  static const double m1[3] = {1.0, 0.0, 0.0};
+  static const double m2[3] = {1.7319, 0.5695, 0.0};
+  static const double m3[3] = {2.2473, 0.8571, 0.5296};
+  if (c.jacobi) return c.weight;
+  return c.stages == 1 ? m1[s] : (c.stages == 2 ? m2[s] : m3[s]);
+}
+
+int exch(pgb_mg *g, int L, double *f, cudaStream_t s) {
+  pgb_mg::Grid &G = g->grids.at(L);
+  // gmg_same exchange of grid L (ProlongateSharedLinear across coarse/fine faces)
+  return exchange_grid(G.tab, f, g->store_of(L).coarse, 1, 1, 1, nullptr, s, nullptr);
+}
+
+int smooth(pgb_mg *g, int L, int stages, cudaStream_t s) {
+  pgb_mg::Grid &G = g->grids.at(L);
+  pgb_mg::Store &S = g->store_of(L);
+  const int nf = (int)G.fine_h.size();
+  const unsigned grid = grid_for((int64_t)nf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]);
+  const MgOp o{g->cfg.D, g->cfg.alpha};
+  for (int st = 0; st < stages; ++st) {
+    int rc = exch(g, L, S.u, s);
+    if (rc) return rc;
+    k_mg_jacobi<<<grid, 256, 0, s>>>(S.view(), G.fine, nf, G.tab.geom, o, srj_weight(g->cfg, st));
+    k_mg_copy<<<grid, 256, 0, s>>>(S.u, S.temp, G.fine, nf, S.dims);
+  }
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+int error_out(pgb_mg *g, int L, cudaStream_t s) {
+  pgb_mg::Grid &G = g->grids.at(L);
+  pgb_mg::Store &S = g->store_of(L);
+  const int nf = (int)G.fine_h.size();
+  k_mg_error<<<grid_for((int64_t)nf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]), 256, 0, s>>>(S.view(), G.fine, nf);
+  PGB_CUDA(cudaGetLastError());
+  return exch(g, L, S.res, s);
+}
+
+// Leaf residual and its partial sums copied to pinned host memory.
+int leaf_residual(pgb_mg *g, cudaStream_t s) {
+  pgb_mg::Store &S = g->stores.at(0);
+  int rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, 1, nullptr, s, nullptr);
+  if (rc) return rc;
+  k_mg_leaf_residual<<<g->nparts, kResThreads, 0, s>>>(S.view(), g->nleaf, g->leaf_tab.geom,
+                                                       MgOp{g->cfg.D, g->cfg.alpha}, g->partial);
+  PGB_CUDA(cudaGetLastError());
+  PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
+  return kOk;
+}
+
+// One V-cycle (AddLinearOperatorTasks, mg_solver.hpp:163-186 and 375-520) then the
+// leaf residual (mg_solver.hpp:131-146).
+int enqueue_iteration(pgb_mg *g, cudaStream_t s) {
+  const MgOp o{g->cfg.D, g->cfg.alpha};
+  const int stages = g->cfg.stages;
+  int rc;
+  for (int L = g->lmax; L >= g->lmin; --L) {
+    pgb_mg::Grid &G = g->grids.at(L);
+    pgb_mg::Store &S = g->store_of(L);
+    const int nf = (int)G.fine_h.size(), ni = (int)G.internal_h.size();
+    const int64_t cells = (int64_t)S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2];
+    if (L < g->lmax) {
+      if ((rc = exch(g, L, S.u, s))) return rc;
+      k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.u0, S.u, G.fine, nf, S.dims);
+      if (ni) k_mg_fas<<<grid_for(ni * cells), 256, 0, s>>>(S.view(), G.internal, ni, G.tab.geom, o);
+    } else {
+      k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.u0, S.u, G.fine, nf, S.dims);
+    }
+    if ((rc = smooth(g, L, stages, s))) return rc;
+    if (L > g->lmin) {
+      if ((rc = exch(g, L, S.u, s))) return rc;
+      k_mg_residual<<<grid_for(nf * cells), 256, 0, s>>>(S.view(), G.fine, nf, G.tab.geom, o);
+      const int nx = (int)G.xfer_h.size();
+      const pgb_mg::Store &P = g->store_of(L - 1);
+      k_mg_restrict<<<grid_for(nx * cells / 8), 256, 0, s>>>(S.view(), P.view(), G.xfer, nx, G.tab.geom);
+    } else {
+      for (int c = 0; c < g->cfg.coarse_sweeps; ++c)
+        if ((rc = smooth(g, L, stages, s))) return rc;
+      k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.res, S.u, G.fine, nf, S.dims);
+      if (L < g->lmax && (rc = error_out(g, L, s))) return rc;
+    }
+    PGB_CUDA(cudaGetLastError());
+  }
+  for (int L = g->lmin + 1; L <= g->lmax; ++L) {
+    pgb_mg::Grid &G = g->grids.at(L);
+    pgb_mg::Store &S = g->store_of(L);
+    const pgb_mg::Store &P = g->store_of(L - 1);
+    const int nx = (int)G.xfer_h.size();
+    const int64_t cells = (int64_t)S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2];
+    k_mg_prolong_add<<<grid_for(nx * cells / 8), 256, 0, s>>>(S.view(), P.view(), G.xfer, nx, G.tab.geom);
+    PGB_CUDA(cudaGetLastError());
+    if ((rc = smooth(g, L, stages, s))) return rc;
+    if (L < g->lmax && (rc = error_out(g, L, s))) return rc;
+  }
+  return leaf_residual(g, s);
+}
+
+double host_rms(pgb_mg *g) {
+  double sum = 0.0;
+  for (int i = 0; i < g->nparts; ++i) sum += g->partial_h[i];
+  double ncell = 0.0;
+  for (auto &b : g->topo->leaf().blocks) ncell += (double)b.nx[0] * b.nx[1] * b.nx[2];
+  return std::sqrt(sum / ncell);
+}
+
+int run_iteration(pgb_mg *g, cudaStream_t s) {
+  if (!g->graph) {
+    cudaGraph_t gr;
+    PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_iteration(g, s);
+    cudaError_t e = cudaStreamEndCapture(s, &gr);
+    if (rc) {
+      if (e == cudaSuccess) cudaGraphDestroy(gr);
+      return rc;
+    }
+    PGB_CUDA(e);
+    e = cudaGraphInstantiate(&g->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    PGB_CUDA(e);
+  }
+  PGB_CUDA(cudaGraphLaunch(g->graph, s));
+  return kOk;
+}
+
+int copy_in(pgb_mg *g, const double *u, const double *rhs, cudaStream_t s) {
+  pgb_mg::Store &S = g->stores.at(0);
+  const size_t n = (size_t)g->nleaf * S.dims.N[0] * S.dims.N[1] * S.dims.N[2] * sizeof(double);
+  PGB_CUDA(cudaMemcpyAsync(S.u, u, n, cudaMemcpyDeviceToDevice, s));
+  PGB_CUDA(cudaMemcpyAsync(S.rhs, rhs, n, cudaMemcpyDeviceToDevice, s));
+  return kOk;
+}
+
+int copy_out(pgb_mg *g, double *u, cudaStream_t s) {
+  pgb_mg::Store &S = g->stores.at(0);
+  const size_t n = (size_t)g->nleaf * S.dims.N[0] * S.dims.N[1] * S.dims.N[2] * sizeof(double);
+  PGB_CUDA(cudaMemcpyAsync(u, S.u, n, cudaMemcpyDeviceToDevice, s));
+  return kOk;
+}
+
+int check_stream(cudaStream_t s) {
+  if (s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread)
+    return fail(kErrInvalid, "the multigrid solve captures a CUDA graph: pass a created stream");
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pgb_mg_create(pgb_mesh *mesh, const pgb_mg_params *p, pgb_mg **out) {
+  if (!mesh || !p || !out) return fail(kErrInvalid, "null argument");
+  *out = nullptr;
+  if (p->stages < 0 || p->stages > 3) return fail(kErrInvalid, "stages must be 0..3");
+  if (!p->jacobi && p->stages == 0) return fail(kErrInvalid, "SRJ needs 1..3 stages");
+  if (p->coarse_sweeps < 0 || p->max_coarsenings < 0) return fail(kErrInvalid, "negative count");
+  MeshState *st = mesh_state(mesh);
+  if (!st || !st->topo) return fail(kErrInvalid, "mesh without topology");
+  const MeshSpec &sp = st->topo->spec();
+  if (sp.ng < 1) return fail(kErrUnsupported, "the operator needs one ghost layer");
+  auto *g = new pgb_mg();
+  g->mesh = mesh;
+  g->topo = st->topo.get();
+  g->cfg.stages = p->stages;
+  g->cfg.jacobi = p->jacobi;
+  g->cfg.weight = p->weight;
+  g->cfg.coarse_sweeps = p->coarse_sweeps;
+  g->cfg.D = p->D;
+  g->cfg.alpha = p->alpha;
+  g->max_coarsenings = p->max_coarsenings;
+  int rc;
+  try {
+    rc = mg_build(g);
+  } catch (std::exception &e) {
+    rc = fail(kErrInvalid, std::string("multigrid grids: ") + e.what());
+  }
+  if (rc) {
+    delete g;
+    return rc;
+  }
+  *out = g;
+  return kOk;
+}
+
+int pgb_mg_destroy(pgb_mg *g) {
+  delete g;
+  return kOk;
+}
+
+int pgb_mg_info(const pgb_mg *g, int32_t *out) {
+  if (!g || !out) return fail(kErrInvalid, "null argument");
+  out[0] = g->lmin;
+  out[1] = g->lmax;
+  out[2] = g->stores.at(0).nslots;
+  out[3] = g->nleaf;
+  out[4] = (int32_t)g->grids.size();
+  return kOk;
+}
+
+int pgb_mg_boundaries(const pgb_mg *g, int32_t level, int32_t *out, int32_t capacity, int32_t *count) {
+  if (!g || !count) return fail(kErrInvalid, "null argument");
+  const auto &mg = g->topo->mg_grids();
+  auto it = mg.find(level);
+  if (it == mg.end() || level < g->lmin || level > g->lmax) return fail(kErrInvalid, "no multigrid grid at that level");
+  const GridTopology &gr = it->second;
+  *count = (int32_t)gr.pairs.size();
+  if (!out) return kOk;
+  if (capacity < (int)gr.pairs.size()) return fail(kErrInvalid, "capacity too small");
+  int r = 0;
+  for (auto &p : gr.pairs) {
+    int32_t *o = out + 23 * r++;
+    o[0] = gr.blocks[p.sender].gid;
+    o[1] = gr.blocks[p.receiver].gid;
+    o[2] = p.loc_index;
+    for (int d = 0; d < 3; ++d) {
+      o[3 + 2 * d] = p.send.lo[d];
+      o[4 + 2 * d] = p.send.hi[d];
+      o[10 + 2 * d] = p.recv.lo[d];
+      o[11 + 2 * d] = p.recv.hi[d];
+    }
+    o[9] = p.send_coarse;
+    o[16] = p.recv_coarse;
+    o[17] = (int32_t)p.recv.mask;
+    o[18] = (int32_t)p.send.count();
+    o[19] = o[20] = o[21] = o[22] = 0;
+  }
+  return kOk;
+}
+
+int pgb_mg_vcycles(pgb_mg *g, double *u, const double *rhs, int32_t ncycles, double *rms, void *stream) {
+  if (!g || !u || !rhs) return fail(kErrInvalid, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc;
+  if ((rc = check_stream(s)) || (rc = mg_upload(g)) || (rc = copy_in(g, u, rhs, s))) return rc;
+  for (int c = 0; c < ncycles; ++c) {
+    if ((rc = run_iteration(g, s))) return rc;
+    PGB_CUDA(cudaStreamSynchronize(s));
+    if (rms) rms[c] = host_rms(g);
+  }
+  if ((rc = copy_out(g, u, s))) return rc;
+  PGB_CUDA(cudaStreamSynchronize(s));
+  return kOk;
+}
+
+int pgb_mg_solve(pgb_mg *g, double *u, const double *rhs, double tol, int32_t relative, int32_t max_cycles,
+                 int32_t *cycles_out, double *rms_out, void *stream) {
+  if (!g || !u || !rhs) return fail(kErrInvalid, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc;
+  if ((rc = check_stream(s)) || (rc = mg_upload(g)) || (rc = copy_in(g, u, rhs, s))) return rc;
+  if ((rc = leaf_residual(g, s))) return rc;
+  PGB_CUDA(cudaStreamSynchronize(s));
+  const double r0 = host_rms(g);
+  const double target = relative ? tol * r0 : tol;
+  double r = r0;
+  int c = 0;
+  // MGSolver::AddTasks: iterate while rms > tolerance (mg_solver.hpp:147-158)
+  while (r > target && c < max_cycles) {
+    if ((rc = run_iteration(g, s))) return rc;
+    PGB_CUDA(cudaStreamSynchronize(s));
+    r = host_rms(g);
+    ++c;
+  }
+  if ((rc = copy_out(g, u, s))) return rc;
+  PGB_CUDA(cudaStreamSynchronize(s));
+  if (cycles_out) *cycles_out = c;
+  if (rms_out) *rms_out = relative ? (r0 > 0 ? r / r0 : 0.0) : r;
+  return kOk;
+}
+
+}  // extern "C"

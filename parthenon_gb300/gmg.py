@@ -80,3 +80,86 @@ class GmgSolver:
                                           int(max_cycles), ctypes.byref(cyc), ctypes.byref(rel), _stream(stream)),
                   "pgb_gmg_solve")
         return cyc.value, rel.value
+
+
+class CompositeMultigrid:
+    """MGSolver on the two-level composite grids of a (refined) mesh.
+
+    Grid L holds every block of level L and the leaves of level L - 1 (mesh-gmg.cpp:
+    103-201); FAS V-cycles smooth the level-L blocks, restrict to the parents and
+    prolongate the correction back (mg_solver.hpp:375-520). Fields are the leaf blocks'
+    arrays in the exchange layout with one component: (nblocks, N3, N2, N1) float64.
+    The operator is div(D grad u) - alpha u with constant D. The host part (grids,
+    index maps) needs no GPU; device memory is taken on the first solve.
+    """
+
+    def __init__(self, mesh, stages=2, jacobi=False, weight=2.0 / 3.0, coarse_sweeps=0, max_coarsenings=30,
+                 D=1.0, alpha=0.0):
+        p = nat.MgParams()
+        p.stages, p.jacobi, p.weight = int(stages), int(bool(jacobi)), float(weight)
+        p.coarse_sweeps, p.max_coarsenings = int(coarse_sweeps), int(max_coarsenings)
+        p.D, p.alpha = float(D), float(alpha)
+        self.mesh = mesh  # the solver reads the mesh's topology
+        h = ctypes.c_void_p()
+        nat.check(nat.lib().pgb_mg_create(mesh.handle, ctypes.byref(p), ctypes.byref(h)), "pgb_mg_create")
+        self._h = h
+        info = (ctypes.c_int32 * 5)()
+        nat.check(nat.lib().pgb_mg_info(self._h, info), "pgb_mg_info")
+        self.lmin, self.lmax, self.nslots, self.nleaf, self.ngrids = (int(x) for x in info)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            nat.lib().pgb_mg_destroy(h)
+            self._h = None
+
+    def boundaries(self, level):
+        """gmg_same index maps of grid `level` (records as Mesh.boundaries)."""
+        import numpy as np
+        n = ctypes.c_int32(0)
+        nat.check(nat.lib().pgb_mg_boundaries(self._h, int(level), None, 0, ctypes.byref(n)), "pgb_mg_boundaries")
+        out = np.zeros((n.value, 23), np.int32)
+        nat.check(nat.lib().pgb_mg_boundaries(self._h, int(level), out.ctypes.data_as(ctypes.c_void_p), n.value,
+                                              ctypes.byref(n)), "pgb_mg_boundaries")
+        return out
+
+    def _check(self, *fields):
+        n = self.nleaf * self.mesh.N[0] * self.mesh.N[1] * self.mesh.N[2]
+        for f in fields:
+            if not (f.is_cuda and f.dtype.is_floating_point and f.element_size() == 8 and f.is_contiguous()
+                    and f.numel() == n):
+                raise ValueError("fields must be contiguous float64 CUDA tensors of the leaf blocks, "
+                                 "(nblocks, N3, N2, N1)")
+
+    def _stream(self, stream):
+        import torch
+        if stream is None:
+            stream = self._own_stream = getattr(self, "_own_stream", None) or torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())
+        return stream
+
+    def vcycles(self, u, rhs, ncycles, stream=None):
+        """ncycles V-cycles on u (in place); the rms leaf residual after each."""
+        import numpy as np
+        import torch
+        self._check(u, rhs)
+        s = self._stream(stream)
+        rms = np.zeros(max(1, ncycles))
+        nat.check(nat.lib().pgb_mg_vcycles(self._h, _ptr(u), _ptr(rhs), int(ncycles),
+                                           rms.ctypes.data_as(ctypes.c_void_p), _stream(s)), "pgb_mg_vcycles")
+        torch.cuda.current_stream().wait_stream(s)
+        return rms[:ncycles]
+
+    def solve(self, u, rhs, tol=1e-10, relative=True, max_cycles=200, stream=None):
+        """V-cycles until the rms leaf residual is below tol (times the initial one when
+        relative); returns (cycles, final rms or relative rms)."""
+        import torch
+        self._check(u, rhs)
+        s = self._stream(stream)
+        cyc = ctypes.c_int32(0)
+        r = ctypes.c_double(0.0)
+        nat.check(nat.lib().pgb_mg_solve(self._h, _ptr(u), _ptr(rhs), float(tol), int(bool(relative)),
+                                         int(max_cycles), ctypes.byref(cyc), ctypes.byref(r), _stream(s)),
+                  "pgb_mg_solve")
+        torch.cuda.current_stream().wait_stream(s)
+        return cyc.value, r.value

@@ -43,3 +43,41 @@ INDEX_MAP_CASES = [
     ("two-per-dim", (32, 32, 32), (16, 16, 16), 4, None),
     ("two-per-dim-refined", (16, 16, 16), (8, 8, 8), 2, refined_cube(1, 0, 1)),
 ]
+
+
+def gaussian_rhs(locs, geom, bnx, ng, ngauss=8, sigma=0.05, seed=5):
+    """Right-hand side on leaf blocks (nblocks, N3, N2, N1): a sum of `ngauss` Gaussians
+    with centres U[0,1]^3 and N(0,1) amplitudes, minus its volume-weighted mean, on the
+    interiors (ghosts zero). locs/geom as Mesh.block_info()."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    cen = rng.random((ngauss, 3))
+    amp = rng.normal(size=ngauss)
+    nb = locs.shape[0]
+    N = [b + 2 * ng for b in bnx]
+    out = np.zeros((nb, N[2], N[1], N[0]))
+    vols = np.prod(geom[:, 3:], axis=1)
+    total = 0.0
+    for b in range(nb):
+        x0, dx = geom[b, :3], geom[b, 3:]
+        xs = [x0[d] + (np.arange(bnx[d]) + 0.5) * dx[d] for d in range(3)]
+        Z, Y, X = np.meshgrid(xs[2], xs[1], xs[0], indexing="ij")
+        val = np.zeros_like(X)
+        for q in range(ngauss):
+            r2 = (X - cen[q, 0]) ** 2 + (Y - cen[q, 1]) ** 2 + (Z - cen[q, 2]) ** 2
+            val += amp[q] * np.exp(-r2 / (2 * sigma ** 2))
+        out[b, ng:ng + bnx[2], ng:ng + bnx[1], ng:ng + bnx[0]] = val
+        total += val.sum() * vols[b]
+    volume = sum(vols[b] * bnx[0] * bnx[1] * bnx[2] for b in range(nb))
+    out[:, ng:ng + bnx[2], ng:ng + bnx[1], ng:ng + bnx[0]] -= total / volume
+    return out
+
+
+# (name, nx, block_nx, nghost, leaves) of the composite-grid multigrid cases
+MG_CASES = [
+    ("uniform-32-b8", (32, 32, 32), (8, 8, 8), 2, None),
+    ("smr-32-b8", (32, 32, 32), (8, 8, 8), 2, refined_cube(2, 1, 3)),
+    ("smr-64-b16-g4", (64, 64, 64), (16, 16, 16), 4, refined_cube(2, 1, 3)),
+    ("smr-corner-32-b8", (32, 32, 32), (8, 8, 8), 2, refined_cube(2, 0, 2)),
+    ("three-level-32-b4", (32, 32, 32), (4, 4, 4), 2, two_level_nested(3, 2, 6, 6, 10)),
+]

@@ -332,3 +332,79 @@ class OracleGmg:
         it = _gmg_lib().orc_bicgstab(self.h, _ptr(b), _ptr(x), int(bool(precondition)), float(rtol),
                                      int(bool(relative)), int(max_iters), _ptr(rms))
         return x.reshape(self.n, self.n, self.n), it, float(rms[0])
+
+
+def _mgb_lib():
+    L = lib()
+    if not getattr(L, "_mgb_ready", False):
+        L.orc_mgb_create.restype = ctypes.c_void_p
+        L.orc_mgb_create.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_mgb_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_mgb_info.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        for name in ["orc_mgb_u", "orc_mgb_rhs", "orc_mgb_res"]:
+            getattr(L, name).argtypes = [ctypes.c_void_p]
+            getattr(L, name).restype = DP
+        L.orc_mgb_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.orc_mgb_residual.argtypes = [ctypes.c_void_p]
+        L.orc_mgb_residual.restype = ctypes.c_double
+        L.orc_mgb_num_boundaries.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_mgb_num_boundaries.restype = ctypes.c_int
+        L.orc_mgb_boundaries.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L._mgb_ready = True
+    return L
+
+
+class OracleMgBlocks:
+    """FP64 FAS V-cycle on the two-level composite grids of a (refined) mesh.
+
+    Fields u and rhs live on the leaf blocks in the exchange layout
+    [block][k][j][i] with ghosts; the multigrid's internal blocks are private."""
+
+    def __init__(self, sim, stages=2, jacobi=False, weight=2.0 / 3.0, coarse_sweeps=0, max_coarsenings=30,
+                 D=1.0, alpha=0.0):
+        L = _mgb_lib()
+        self.sim = sim  # the mesh must outlive the solver
+        self.h = L.orc_mgb_create(sim.h, int(stages), int(bool(jacobi)), float(weight), int(coarse_sweeps),
+                                  int(max_coarsenings), float(D), float(alpha))
+        if not self.h:
+            raise RuntimeError("oracle multigrid construction failed")
+        info = np.zeros(4, np.int32)
+        L.orc_mgb_info(self.h, _ptr(info))
+        self.lmin, self.lmax, self.nslots, self.nleaf = (int(x) for x in info)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _mgb_lib().orc_mgb_destroy(self.h)
+            self.h = None
+
+    def _view(self, fn):
+        N = self.sim.N
+        p = fn(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.nleaf * N[0] * N[1] * N[2],)).reshape(
+            self.nleaf, N[2], N[1], N[0])
+
+    def u(self):
+        return self._view(_mgb_lib().orc_mgb_u)
+
+    def rhs(self):
+        return self._view(_mgb_lib().orc_mgb_rhs)
+
+    def res(self):
+        return self._view(_mgb_lib().orc_mgb_res)
+
+    def run(self, ncycles):
+        rms = np.zeros(max(1, ncycles))
+        _mgb_lib().orc_mgb_run(self.h, int(ncycles), _ptr(rms))
+        return rms[:ncycles]
+
+    def residual(self):
+        return _mgb_lib().orc_mgb_residual(self.h)
+
+    def boundaries(self, level):
+        n = _mgb_lib().orc_mgb_num_boundaries(self.h, int(level))
+        if n < 0:
+            raise ValueError("no multigrid grid at that level")
+        out = np.zeros((n, 23), np.int32)
+        _mgb_lib().orc_mgb_boundaries(self.h, int(level), _ptr(out))
+        return out
