@@ -42,7 +42,7 @@ def test_composite_vcycles_bitwise(name, nx, bnx, ng, leaves):
     om, rms_o, u, rms_p = _pair(nx, bnx, ng, leaves, 4, alpha=10.0)
     assert np.array_equal(_interior(u, ng), _interior(om.u(), ng))
     np.testing.assert_allclose(rms_p, rms_o, rtol=1e-12, atol=0)
-    assert rms_p[-1] < 1e-2 * rms_p[0]
+    assert rms_p[-1] < 5e-2 * rms_p[0]
 
 
 @pytest.mark.parametrize("kw", [dict(stages=3), dict(stages=1), dict(jacobi=True, stages=2, weight=0.8),
