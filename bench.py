@@ -278,6 +278,7 @@ def run_ours(args, ws, rank):
         "autotune": {k: {"choice": c, "ms": ms} for k, (c, ms) in nat.tune_report().items()},
     }
     out["gmg"] = gmg_bench(torch)
+    out["gmg_composite"] = gmg_composite_bench(torch, with_cpu=(rank == 0 and ws == 1))
     if rank == 0 and ws == 1:
         out["cpu_baseline"] = cpu_baseline(steps=1)
     del drv, state, host_in, host_out
@@ -338,6 +339,74 @@ def gmg_bench(torch):
     res["config"] = {"n": GMG_N, "levels": GMG_COARSEN + 1, "smoother": "weighted Jacobi 2/3, 2+2",
                      "coarse": "+16 smoother passes, FP64", "rhs": "32 Gaussians sigma 0.03 seed 4, mean removed"}
     return res
+
+
+GMGC_ROOT, GMGC_BLOCK, GMGC_NG, GMGC_ALPHA = 128, 16, 2, 10.0
+
+
+def _gmgc_mesh(pg):
+    # the statically refined mesh of the 2-level advection workload: 128^3 root in 16^3
+    # blocks with the central 1/8 refined once (448 + 512 leaves)
+    nb = GMGC_ROOT // GMGC_BLOCK
+    root_level = nb.bit_length() - 1
+    leaves = pg.problems.refined_region_leaves(root_level, nb // 4, 3 * nb // 4)
+    return pg.Mesh((GMGC_ROOT,) * 3, (GMGC_BLOCK,) * 3, GMGC_NG, leaves=leaves)
+
+
+def gmg_composite_bench(torch, with_cpu):
+    """Multigrid on the two-level composite grids of the refined mesh: the reference's
+    defaults (FAS, SRJ2, coarsening down to 1^3 blocks), div grad u - alpha u = rhs with
+    alpha 10 (poisson/diagonal_alpha; the periodic refined operator without flux
+    correction is singular and inconsistent at alpha 0), rhs the 32 Gaussians of the
+    uniform leg. Time to a 1e-10 relative leaf residual, and the oracle's time per
+    V-cycle on the host cores."""
+    import parthenon_gb300 as pg
+    mesh = _gmgc_mesh(pg)
+    rhs_h = pg.problems.poisson_rhs_blocks(mesh, ngauss=32, sigma=0.03, seed=4)
+    rhs = torch.tensor(rhs_h, device="cuda")
+    mg = pg.CompositeMultigrid(mesh, stages=2, alpha=GMGC_ALPHA)
+    s = torch.cuda.Stream()
+    best = None
+    for rep in range(3):
+        u = torch.zeros_like(rhs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cyc, rel = mg.solve(u, rhs, tol=1e-10, relative=True, max_cycles=200, stream=s)
+        s.synchronize()
+        dt = time.perf_counter() - t0
+        if rep > 0 and (best is None or dt < best[0]):  # the first solve builds the graph
+            best = (dt, cyc, rel)
+    locs, _ = mesh.block_info()
+    res = {"seconds": best[0], "vcycles": best[1], "rel_residual": best[2],
+           "ms_per_vcycle": 1e3 * best[0] / max(1, best[1]),
+           "config": {"mesh": "128^3 root, 16^3 blocks, central 1/8 refined once", "leaves": int(mesh.nblocks),
+                      "leaves_per_level": {str(int(l)): int((locs[:, 0] == l).sum()) for l in np.unique(locs[:, 0])},
+                      "nghost": GMGC_NG, "grids": mg.ngrids, "levels": [mg.lmin, mg.lmax],
+                      "storage_blocks": mg.nslots, "smoother": "SRJ2 (2+2)", "alpha": GMGC_ALPHA,
+                      "rhs": "32 Gaussians sigma 0.03 seed 4, volume mean removed"}}
+    if with_cpu:
+        res["cpu_baseline"] = gmg_composite_cpu_baseline(mesh, rhs_h, best[1])
+    return res
+
+
+def gmg_composite_cpu_baseline(mesh, rhs_h, vcycles, sample=2):
+    """The oracle's composite V-cycle (oracle/gmg_blocks.hpp) on the same mesh and rhs,
+    `sample` V-cycles with their leaf residuals, scaled to the GPU's cycle count."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as O
+    sim = O.OracleSim((GMGC_ROOT,) * 3, (GMGC_BLOCK,) * 3, GMGC_NG, leaves=_gmgc_leaves_of(mesh))
+    om = O.OracleMgBlocks(sim, stages=2, alpha=GMGC_ALPHA)
+    om.rhs()[:] = rhs_h
+    t0 = time.perf_counter()
+    om.run(sample)
+    per = (time.perf_counter() - t0) / sample
+    return {"seconds_per_vcycle": per, "seconds_to_tolerance": per * vcycles, "kind": "port",
+            "cores": int(O.lib().orc_max_threads()), "sample": "%d V-cycles + leaf residuals" % sample}
+
+
+def _gmgc_leaves_of(mesh):
+    locs, _ = mesh.block_info()
+    return [tuple(int(x) for x in r) for r in locs]
 
 
 AMR_ROOT, AMR_BLOCK, AMR_NUMLEVEL, AMR_NSCALARS, AMR_CHECK = 128, 16, 3, 2, 5
@@ -613,7 +682,7 @@ def main():
     elif args.gmg_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        out = {"gmg": gmg_bench(torch)}
+        out = {"gmg": gmg_bench(torch), "gmg_composite": gmg_composite_bench(torch, with_cpu=False)}
     elif args.sparse_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))

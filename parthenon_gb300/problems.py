@@ -211,3 +211,44 @@ def poisson_rhs(n, ngauss=32, sigma=0.03, seed=4):
         r2 = d[2][:, None, None] ** 2 + d[1][None, :, None] ** 2 + d[0][None, None, :] ** 2
         out += a * np.exp(-r2 / (2.0 * sigma * sigma))
     return out - out.mean()
+
+
+def refined_region_leaves(root_level, lo, hi):
+    """Leaves of a mesh whose root blocks lo..hi-1 (every direction) are refined once:
+    (level, lx1, lx2, lx3) of the 8 children of each (static refinement of a cube)."""
+    out = []
+    for k in range(lo, hi):
+        for j in range(lo, hi):
+            for i in range(lo, hi):
+                for dk in (0, 1):
+                    for dj in (0, 1):
+                        for di in (0, 1):
+                            out.append((root_level + 1, 2 * i + di, 2 * j + dj, 2 * k + dk))
+    return out
+
+
+def poisson_rhs_blocks(mesh, ngauss=32, sigma=0.03, seed=4):
+    """The right-hand side of poisson_rhs on the leaf blocks of `mesh`, (nblocks, N3, N2,
+    N1) with zero ghosts: a sum of `ngauss` Gaussians (periodic images, centres U[0,1]^3,
+    amplitudes N(0,1), seeded) minus its volume-weighted mean."""
+    rng = np.random.default_rng(seed)
+    centres = rng.random((ngauss, 3))
+    amps = rng.standard_normal(ngauss)
+    locs, geom = mesh.block_info()
+    bnx, ng = mesh.block_nx, mesh.nghost
+    out = np.zeros((mesh.nblocks, mesh.N[2], mesh.N[1], mesh.N[0]))
+    vols = np.prod(geom[:, 3:], axis=1)
+    total = 0.0
+    for b in range(mesh.nblocks):
+        x = [geom[b, q] + (np.arange(bnx[q]) + 0.5) * geom[b, 3 + q] for q in range(3)]
+        val = np.zeros((bnx[2], bnx[1], bnx[0]))
+        for c, a in zip(centres, amps):
+            d = [x[q] - c[q] for q in range(3)]
+            d = [dd - np.round(dd) for dd in d]
+            r2 = d[2][:, None, None] ** 2 + d[1][None, :, None] ** 2 + d[0][None, None, :] ** 2
+            val += a * np.exp(-r2 / (2.0 * sigma * sigma))
+        out[b, ng:ng + bnx[2], ng:ng + bnx[1], ng:ng + bnx[0]] = val
+        total += val.sum() * vols[b]
+    volume = float(np.sum(vols)) * bnx[0] * bnx[1] * bnx[2]
+    out[:, ng:ng + bnx[2], ng:ng + bnx[1], ng:ng + bnx[0]] -= total / volume
+    return out
