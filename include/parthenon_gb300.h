@@ -244,7 +244,8 @@ int pgb_gmg_solve_blocks(pgb_gmg *gmg, pgb_mesh *mesh, double *u, const double *
  * the gmg_same ghost exchange (restriction/prolongation across coarse/fine faces) on
  * every grid; the outer residual is taken on the leaf grid. The operator is
  * div(D grad u) - alpha u with constant D (poisson_equation.hpp:41-210, flux correction
- * off as in the package default). FP64, bitwise the reference's arithmetic.
+ * off as in the package default). FP64; the exact build is bitwise the reference's
+ * arithmetic, the fast build within rounding of it.
  * Replaces MGSolver::AddTasks / AddSetupTasks (src/solvers/mg_solver.hpp:119-520) with
  * Mesh::BuildGMGBlockLists / SetGMGNeighbors (src/mesh/mesh-gmg.cpp:103-201). */
 typedef struct pgb_mg pgb_mg;
@@ -256,6 +257,8 @@ typedef struct {
   int32_t max_coarsenings; /* MGParams::max_coarsenings: grids max .. max(max - this, min) */
   double D;                /* constant face coefficient (the poisson D field) */
   double alpha;            /* poisson/diagonal_alpha */
+  int32_t exact;           /* 1: separately rounded reference-order arithmetic (bitwise);
+                              0: FMA 7-point operator with the diagonal's reciprocal */
 } pgb_mg_params;
 /* Host only: builds the composite grids of the mesh (which must outlive the solver);
  * device memory is taken on the first solve. */

@@ -71,31 +71,47 @@ struct MgOp {
   double D, alpha;
 };
 
+// Operator constants of one grid (its fine blocks share one spacing) or of one leaf
+// block, formed once on the host.
+struct MgCoef {
+  double dx[3];  // exact build: the spacings (fluxes formed and divided as the reference does)
+  double c[3];   // fast build: D / dx_d^2
+  double dg;     // SetDiagonal (poisson_equation.hpp:59-102)
+  double den;    // robust::ratio denominator dg + sgn(dg) 10 DBL_MIN (utils/robust.hpp)
+};
+// One Jacobi sweep: weight, 1 - weight, weight / den
+struct MgSweep {
+  double w, omw, wd;
+};
+
 __device__ __forceinline__ int64_t cell_of(const Dims &d, int slot, int k, int j, int i) {
   return ((int64_t)slot * d.N[2] + k) * ((int64_t)d.N[1] * d.N[0]) + (int64_t)j * d.N[0] + i;
 }
 
-// Every interior cell of the listed blocks, consecutive threads on consecutive i.
+// Every interior cell of the listed blocks, consecutive threads on consecutive i; f gets
+// (position in the list, slot, k, j, i). The host keeps cells x blocks below 2^31.
 template <class F>
 __device__ __forceinline__ void for_interior(const int *__restrict__ list, int n, const Dims &d, F &&f) {
-  const int64_t per = (int64_t)d.nx[0] * d.nx[1] * d.nx[2];
-  const int64_t total = per * n;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int q = (int)(e / per);
-    const int64_t c = e - q * per;
-    const int i = (int)(c % d.nx[0]);
-    const int64_t r = c / d.nx[0];
-    const int j = (int)(r % d.nx[1]);
-    const int k = (int)(r / d.nx[1]);
-    f(list[q], k + d.ng, j + d.ng, i + d.ng);
+  const int n0 = d.nx[0], n1 = d.nx[1], ng = d.ng;
+  const int per = n0 * n1 * d.nx[2];
+  const int total = per * n;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int q = e / per;
+    const int c = e - q * per;
+    const int r = c / n0;
+    const int i = c - r * n0;
+    const int k = r / n1;
+    const int j = r - k * n1;
+    f(q, list[q], k + ng, j + ng, i + ng);
   }
 }
 
-// poisson_equation.hpp:104-210: face fluxes D grad u, then their divergence (-alpha u +
-// sum over directions of (F_left - F_right) / dx), in the reference's order
-__device__ __forceinline__ double apply_op(const double *__restrict__ u, int64_t c, int64_t sj, int64_t sk,
-                                           const DevBlockGeom &g, const MgOp &o) {
-  const double D = o.D, dx1 = g.dx[0], dx2 = g.dx[1], dx3 = g.dx[2];
+// Exact build, poisson_equation.hpp:104-210: face fluxes D grad u, then their
+// divergence, -alpha u + sum over directions of (F_left - F_right) / dx, in the
+// reference's order
+__device__ __forceinline__ double ax_exact(const double *__restrict__ u, int64_t c, int64_t sj, int64_t sk,
+                                          const double *dx, const MgOp &o) {
+  const double D = o.D, dx1 = dx[0], dx2 = dx[1], dx3 = dx[2];
   const double uc = u[c];
   const double f1l = div_rn(D, dx1) * (u[c - 1] - uc);
   const double f1r = div_rn(D, dx1) * (uc - u[c + 1]);
@@ -110,58 +126,66 @@ __device__ __forceinline__ double apply_op(const double *__restrict__ u, int64_t
   return out;
 }
 
-// poisson_equation.hpp:59-102 (SetDiagonal)
-__device__ __forceinline__ double diag_of(const DevBlockGeom &g, const MgOp &o) {
-  const double D = o.D;
-  double d = -div_rn(D + D, g.dx[0] * g.dx[0]) - o.alpha;
-  d -= div_rn(D + D, g.dx[1] * g.dx[1]);
-  d -= div_rn(D + D, g.dx[2] * g.dx[2]);
-  return d;
+// Fast build: the constant-coefficient operator as a 7-point stencil, A u = off + dg u
+// with off = sum_d (D/dx_d^2) (u_{-d} + u_{+d}): 3 adds, a multiply and 2 FMAs (the FP64
+// pipe, not HBM, bounds these kernels on GB300)
+__device__ __forceinline__ double off_fast(const double *__restrict__ u, int64_t c, int64_t sj, int64_t sk,
+                                          const MgCoef &cf) {
+  return fma(cf.c[2], u[c - sk] + u[c + sk], fma(cf.c[1], u[c - sj] + u[c + sj], cf.c[0] * (u[c - 1] + u[c + 1])));
 }
 
-// Ax + Jacobi (mg_solver.hpp:222-297): temp = w ratio(rhs - (Ax - D u), D) + (1 - w) u
-__global__ void __launch_bounds__(256) k_mg_jacobi(StoreView s, const int *__restrict__ list, int n,
-                                                   const DevBlockGeom *__restrict__ geom, MgOp o, double w) {
-  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
-  const double small = 10.0 * DBL_MIN;  // robust::ratio (utils/robust.hpp)
-  for_interior(list, n, s.d, [&](int b, int k, int j, int i) {
-    const DevBlockGeom &g = geom[b];
-    const int64_t c = cell_of(s.d, b, k, j, i);
-    const double dg = diag_of(g, o);
-    const double den = dg + (dg >= 0 ? 1.0 : -1.0) * small;
-    const double a = apply_op(s.u, c, sj, sk, g, o);
-    const double off = a - dg * s.u[c];
-    const double val = s.rhs[c] - off;
-    s.temp[c] = w * div_rn(val, den) + (1.0 - w) * s.u[c];
+// Jacobi sweep (mg_solver.hpp:222-297): dst = w ratio(rhs - (A src - dg src), dg) + (1 - w) src
+template <bool kFast>
+__global__ void __launch_bounds__(256) k_mg_jacobi(const double *__restrict__ src, const double *__restrict__ rhs,
+                                                   double *__restrict__ dst, const int *__restrict__ list, int n,
+                                                   Dims d, MgCoef cf, MgOp o, MgSweep sw) {
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
+  for_interior(list, n, d, [&](int, int b, int k, int j, int i) {
+    const int64_t c = cell_of(d, b, k, j, i);
+    if (kFast) {
+      dst[c] = fma(sw.wd, rhs[c] - off_fast(src, c, sj, sk, cf), sw.omw * src[c]);
+    } else {
+      const double a = ax_exact(src, c, sj, sk, cf.dx, o);
+      const double off = a - cf.dg * src[c];
+      const double val = rhs[c] - off;
+      dst[c] = sw.w * div_rn(val, cf.den) + sw.omw * src[c];
+    }
   });
 }
 
 // Ax + AddFieldsAndStoreInteriorSelect<rhs, temp, res_err>(1, -1): res = rhs - A u
-__global__ void __launch_bounds__(256) k_mg_residual(StoreView s, const int *__restrict__ list, int n,
-                                                     const DevBlockGeom *__restrict__ geom, MgOp o) {
+template <bool kFast>
+__global__ void __launch_bounds__(256) k_mg_residual(StoreView s, const int *__restrict__ list, int n, MgCoef cf,
+                                                     MgOp o) {
   const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
-  for_interior(list, n, s.d, [&](int b, int k, int j, int i) {
+  for_interior(list, n, s.d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
-    const double t = apply_op(s.u, c, sj, sk, geom[b], o);
-    s.res[c] = s.rhs[c] - t;
+    if (kFast) s.res[c] = fma(-cf.dg, s.u[c], s.rhs[c] - off_fast(s.u, c, sj, sk, cf));
+    else s.res[c] = s.rhs[c] - ax_exact(s.u, c, sj, sk, cf.dx, o);
   });
 }
 
-// FAS on internal blocks (mg_solver.hpp:413-430): rhs = A u + res_err
-__global__ void __launch_bounds__(256) k_mg_fas(StoreView s, const int *__restrict__ list, int n,
-                                                const DevBlockGeom *__restrict__ geom, MgOp o) {
+// Start of a level below the finest (mg_solver.hpp:405-430): u0 = u on every fine block
+// and, on the first nint (internal) blocks of the list, the FAS right-hand side
+// rhs = A u + res_err
+template <bool kFast>
+__global__ void __launch_bounds__(256) k_mg_fas(StoreView s, const int *__restrict__ list, int n, int nint,
+                                                MgCoef cf, MgOp o) {
   const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
-  for_interior(list, n, s.d, [&](int b, int k, int j, int i) {
+  for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
-    const double t = apply_op(s.u, c, sj, sk, geom[b], o);
-    s.rhs[c] = t + s.res[c];
+    const double uc = s.u[c];
+    s.u0[c] = uc;
+    if (q >= nint) return;
+    if (kFast) s.rhs[c] = fma(cf.dg, uc, off_fast(s.u, c, sj, sk, cf) + s.res[c]);
+    else s.rhs[c] = ax_exact(s.u, c, sj, sk, cf.dx, o) + s.res[c];
   });
 }
 
 // CopyData on the interiors of the listed blocks
 __global__ void __launch_bounds__(256) k_mg_copy(double *__restrict__ dst, const double *__restrict__ src,
                                                  const int *__restrict__ list, int n, Dims d) {
-  for_interior(list, n, d, [&](int b, int k, int j, int i) {
+  for_interior(list, n, d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(d, b, k, j, i);
     dst[c] = src[c];
   });
@@ -169,7 +193,7 @@ __global__ void __launch_bounds__(256) k_mg_copy(double *__restrict__ dst, const
 
 // AddFieldsAndStore<u, u0, res_err>(1, -1): res = u - u0
 __global__ void __launch_bounds__(256) k_mg_error(StoreView s, const int *__restrict__ list, int n) {
-  for_interior(list, n, s.d, [&](int b, int k, int j, int i) {
+  for_interior(list, n, s.d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     s.res[c] = s.u[c] - s.u0[c];
   });
@@ -180,13 +204,13 @@ __global__ void __launch_bounds__(256) k_mg_error(StoreView s, const int *__rest
 __global__ void __launch_bounds__(256) k_mg_restrict(StoreView cs, StoreView ps, const MgXfer *__restrict__ x,
                                                      int n, const DevBlockGeom *__restrict__ cgeom) {
   const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
-  const int64_t per = (int64_t)h0 * h1 * h2, total = per * n;
+  const int per = h0 * h1 * h2, total = per * n;
   const int ng = cs.d.ng;
   const int64_t cj = cs.d.N[0], ck = (int64_t)cs.d.N[0] * cs.d.N[1];
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int q = (int)(e / per);
-    const int64_t r = e - q * per;
-    const int ci = (int)(r % h0), cjj = (int)((r / h0) % h1), ckk = (int)(r / ((int64_t)h0 * h1));
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int q = e / per;
+    const int r = e - q * per;
+    const int ci = r % h0, cjj = (r / h0) % h1, ckk = r / (h0 * h1);
     const MgXfer t = x[q];
     const double vol = cgeom[t.child].vol;
     const int64_t f = cell_of(cs.d, t.child, 2 * ckk + ng, 2 * cjj + ng, 2 * ci + ng);
@@ -208,20 +232,22 @@ __global__ void __launch_bounds__(256) k_mg_restrict(StoreView cs, StoreView ps,
 
 // ProlongateSharedLinear (pr_ops.hpp:166-285) of the parent's res_err (its octant with
 // ghosts is the child's coarse buffer) and AddFieldsAndStore<u, res_err, u>: one thread
-// per coarse cell of the child's interior, eight fine cells each.
+// per coarse cell of the child's interior, eight fine cells each. The exact build forms
+// the slopes from the cell-centre coordinates as the reference does; the fast build
+// uses the uniform-spacing value dx_fine / 2 / dx_coarse = 1/4 of each difference.
+template <bool kFast>
 __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView cs, StoreView ps, const MgXfer *__restrict__ x,
                                                         int n, const DevBlockGeom *__restrict__ cgeom) {
   const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
-  const int64_t per = (int64_t)h0 * h1 * h2, total = per * n;
+  const int per = h0 * h1 * h2, total = per * n;
   const int ng = cs.d.ng;
   const int64_t pj = ps.d.N[0], pk = (int64_t)ps.d.N[0] * ps.d.N[1];
   const int64_t N0 = cs.d.N[0], N01 = (int64_t)cs.d.N[0] * cs.d.N[1];
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int q = (int)(e / per);
-    const int64_t r = e - q * per;
-    const int c0 = (int)(r % h0), c1 = (int)((r / h0) % h1), c2 = (int)(r / ((int64_t)h0 * h1));
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int q = e / per;
+    const int r = e - q * per;
+    const int c0 = r % h0, c1 = (r / h0) % h1, c2 = r / (h0 * h1);
     const MgXfer t = x[q];
-    const DevBlockGeom &g = cgeom[t.child];
     const int c[3] = {c0 + ng, c1 + ng, c2 + ng};  // coarse-buffer index
     const int f[3] = {2 * c0 + ng, 2 * c1 + ng, 2 * c2 + ng};
     const int64_t pe = cell_of(ps.d, t.parent, t.lo[2] + c2, t.lo[1] + c1, t.lo[0] + c0);
@@ -229,17 +255,21 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView cs, StoreView 
     double mq[3], pq[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      auto xcc = [&](int idx) { return g.cxmin[d] + ((double)idx + 0.5) * g.cdx[d]; };
-      auto xfc = [&](int idx) { return g.xmin[d] + ((double)idx + 0.5) * g.dx[d]; };
-      const double xm = xcc(c[d] - 1), xc = xcc(c[d]), xp = xcc(c[d] + 1);
-      const double dxm = xc - xm, dxp = xp - xc;
-      const double dfm = xc - xfc(f[d]);
-      const double dfp = xfc(f[d] + 1) - xc;
       const int64_t st = d == 0 ? 1 : (d == 1 ? pj : pk);
-      const double gm = div_rn(fc - ps.res[pe - st], dxm);
-      const double gp = div_rn(ps.res[pe + st] - fc, dxp);
-      mq[d] = gm * dfm;
-      pq[d] = gp * dfp;
+      if (kFast) {
+        mq[d] = 0.25 * (fc - ps.res[pe - st]);
+        pq[d] = 0.25 * (ps.res[pe + st] - fc);
+      } else {
+        const DevBlockGeom &g = cgeom[t.child];
+        auto xcc = [&](int idx) { return g.cxmin[d] + ((double)idx + 0.5) * g.cdx[d]; };
+        auto xfc = [&](int idx) { return g.xmin[d] + ((double)idx + 0.5) * g.dx[d]; };
+        const double xm = xcc(c[d] - 1), xc = xcc(c[d]), xp = xcc(c[d] + 1);
+        const double dxm = xc - xm, dxp = xp - xc;
+        const double dfm = xc - xfc(f[d]);
+        const double dfp = xfc(f[d] + 1) - xc;
+        mq[d] = div_rn(fc - ps.res[pe - st], dxm) * dfm;
+        pq[d] = div_rn(ps.res[pe + st] - fc, dxp) * dfp;
+      }
     }
     const double m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
     double *U = cs.u + cell_of(cs.d, t.child, f[2], f[1], f[0]);
@@ -255,23 +285,27 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView cs, StoreView 
 }
 
 // Leaf-grid residual of MGSolver::AddTasks (mg_solver.hpp:135-158): res = rhs - A u
-// over every leaf interior and one partial sum of r^2 per CTA (fixed tree order, so
-// the host's fixed-order total is reproducible)
+// over every leaf interior (operator constants per leaf, levels differ) and one partial
+// sum of r^2 per CTA (fixed tree order, so the host's fixed-order total is reproducible)
 constexpr int kResThreads = 256;
+template <bool kFast>
 __global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView s, int nleaf,
-                                                                  const DevBlockGeom *__restrict__ geom, MgOp o,
+                                                                  const MgCoef *__restrict__ lc, MgOp o,
                                                                   double *__restrict__ partial) {
   __shared__ double sh[kResThreads];
   const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
-  const int64_t per = (int64_t)s.d.nx[0] * s.d.nx[1] * s.d.nx[2], total = per * nleaf;
+  const int n0 = s.d.nx[0], n1 = s.d.nx[1], ng = s.d.ng;
+  const int per = n0 * n1 * s.d.nx[2], total = per * nleaf;
   double acc = 0.0;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)(e / per);
-    const int64_t cc = e - b * per;
-    const int i = (int)(cc % s.d.nx[0]), j = (int)((cc / s.d.nx[0]) % s.d.nx[1]);
-    const int k = (int)(cc / ((int64_t)s.d.nx[0] * s.d.nx[1]));
-    const int64_t c = cell_of(s.d, b, k + s.d.ng, j + s.d.ng, i + s.d.ng);
-    const double r = s.rhs[c] - apply_op(s.u, c, sj, sk, geom[b], o);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int b = e / per;
+    const int cc = e - b * per;
+    const int rr = cc / n0, i = cc - rr * n0, k = rr / n1, j = rr - k * n1;
+    const int64_t c = cell_of(s.d, b, k + ng, j + ng, i + ng);
+    const MgCoef &cf = lc[b];
+    double r;
+    if (kFast) r = fma(-cf.dg, s.u[c], s.rhs[c] - off_fast(s.u, c, sj, sk, cf));
+    else r = s.rhs[c] - ax_exact(s.u, c, sj, sk, cf.dx, o);
     s.res[c] = r;
     acc += r * r;
   }
@@ -295,6 +329,7 @@ struct pgb_mg {
   pgb_mesh *mesh = nullptr;
   MeshTopology *topo = nullptr;
   GmgConfig cfg;
+  bool exact = true;  // reference-order arithmetic (bitwise) or the FMA 7-point build
   int max_coarsenings = 30;
   int lmin = 0, lmax = 0, nleaf = 0;
   struct Store {
@@ -309,13 +344,18 @@ struct pgb_mg {
     int level = 0, store = 0;
     GridTopology remap;  // the composite grid's exchange boxes over store slots
     GridTables tab;
-    std::vector<int> fine_h, internal_h;
-    std::vector<MgXfer> xfer_h;  // fine blocks and their parents (grids above the coarsest)
-    int *fine = nullptr, *internal = nullptr;
+    std::vector<int> fine_h;    // slots of the level-L blocks, internal blocks first
+    std::vector<int> coarse_h;  // slots of the leaves of level L-1
+    int nint = 0;               // internal blocks at the head of fine_h
+    std::vector<MgXfer> xfer_h; // fine blocks and their parents (grids above the coarsest)
+    MgCoef coef{};              // operator constants of the fine blocks
+    int *fine = nullptr, *coarse = nullptr;
     MgXfer *xfer = nullptr;
   };
   std::map<int, Grid> grids;
   GridTables leaf_tab;
+  std::vector<MgCoef> leaf_coef_h;  // per leaf block (levels differ)
+  MgCoef *leaf_coef = nullptr;
   void *lists = nullptr;
   double *partial = nullptr, *partial_h = nullptr;
   int nparts = 0;
@@ -337,6 +377,23 @@ struct pgb_mg {
 };
 
 namespace {
+
+// Operator constants for spacing dx, in the order of poisson_equation.hpp:59-102 and
+// utils/robust.hpp (the exact build's values are bitwise those formed per cell there)
+MgCoef make_coef(const double *dx, const GmgConfig &c) {
+  MgCoef o;
+  const double D = c.D;
+  for (int d = 0; d < 3; ++d) {
+    o.dx[d] = dx[d];
+    o.c[d] = D / (dx[d] * dx[d]);
+  }
+  double dg = -(D + D) / (dx[0] * dx[0]) - c.alpha;
+  dg -= (D + D) / (dx[1] * dx[1]);
+  dg -= (D + D) / (dx[2] * dx[2]);
+  o.dg = dg;
+  o.den = dg + (dg >= 0 ? 1.0 : -1.0) * (10 * DBL_MIN);
+  return o;
+}
 
 // Composite grids, store slots and transfer records (host only).
 int mg_build(pgb_mg *g) {
@@ -403,13 +460,25 @@ int mg_build(pgb_mg *g) {
     remap_regions(src.restrict_send, G.remap.restrict_send);
     remap_regions(src.restrict_recv, G.remap.restrict_recv);
     remap_regions(src.prolong, G.remap.prolong);
+    std::vector<int> leaf_fine;
+    const BlockInfo *fb = nullptr;
     for (size_t i = 0; i < src.blocks.size(); ++i) {
       const BlockInfo &b = src.blocks[i];
-      if (b.loc.level != L) continue;
-      G.fine_h.push_back(slot[i]);
-      if (!topo.is_leaf(b.loc)) G.internal_h.push_back(slot[i]);
+      if (b.loc.level != L) {
+        G.coarse_h.push_back(slot[i]);
+        continue;
+      }
+      if (fb && (b.dx[0] != fb->dx[0] || b.dx[1] != fb->dx[1] || b.dx[2] != fb->dx[2]))
+        return fail(kErrUnsupported, "blocks of one level with different spacings");
+      fb = &b;
+      if (topo.is_leaf(b.loc)) leaf_fine.push_back(slot[i]);
+      else G.fine_h.push_back(slot[i]);
     }
+    G.nint = (int)G.fine_h.size();
+    G.fine_h.insert(G.fine_h.end(), leaf_fine.begin(), leaf_fine.end());
+    G.coef = make_coef(fb->dx, g->cfg);
   }
+  for (auto &b : leaves) g->leaf_coef_h.push_back(make_coef(b.dx, g->cfg));
   // transfers between grid L and L - 1, per fine block of grid L
   for (int L = g->lmin + 1; L <= g->lmax; ++L) {
     pgb_mg::Grid &G = g->grids[L];
@@ -478,6 +547,7 @@ int mg_upload(pgb_mg *g) {
       if (kv2.second.store == kv.first) G = &kv2.second;
     S.dims = G->tab.dims;
     const int64_t n = (int64_t)S.nslots * S.dims.N[0] * S.dims.N[1] * S.dims.N[2];
+    if (n >= (int64_t)1 << 31) return fail(kErrUnsupported, "multigrid store above 2^31 cells");
     const int64_t nc = (int64_t)S.nslots * S.dims.Nc[0] * S.dims.Nc[1] * S.dims.Nc[2];
     for (double **p : {&S.u, &S.res, &S.rhs, &S.temp, &S.u0}) {
       PGB_CUDA(cudaMalloc((void **)p, n * sizeof(double)));
@@ -496,22 +566,24 @@ int mg_upload(pgb_mg *g) {
     return off;
   };
   struct Off {
-    size_t fine, internal, xfer;
+    size_t fine, coarse, xfer;
   };
   std::map<int, Off> off;
   for (auto &kv : g->grids) {
     Off o;
     o.fine = room(kv.second.fine_h.size() * sizeof(int));
-    o.internal = room(kv.second.internal_h.size() * sizeof(int));
+    o.coarse = room(kv.second.coarse_h.size() * sizeof(int));
     o.xfer = room(kv.second.xfer_h.size() * sizeof(MgXfer));
     off[kv.first] = o;
   }
+  const size_t lc_off = room(g->leaf_coef_h.size() * sizeof(MgCoef));
   std::vector<char> h(std::max<size_t>(bytes, 256), 0);
+  std::memcpy(h.data() + lc_off, g->leaf_coef_h.data(), g->leaf_coef_h.size() * sizeof(MgCoef));
   for (auto &kv : g->grids) {
     const Off &o = off[kv.first];
     auto &G = kv.second;
     std::memcpy(h.data() + o.fine, G.fine_h.data(), G.fine_h.size() * sizeof(int));
-    std::memcpy(h.data() + o.internal, G.internal_h.data(), G.internal_h.size() * sizeof(int));
+    std::memcpy(h.data() + o.coarse, G.coarse_h.data(), G.coarse_h.size() * sizeof(int));
     std::memcpy(h.data() + o.xfer, G.xfer_h.data(), G.xfer_h.size() * sizeof(MgXfer));
   }
   PGB_CUDA(cudaMalloc(&g->lists, h.size()));
@@ -520,9 +592,10 @@ int mg_upload(pgb_mg *g) {
     const Off &o = off[kv.first];
     char *base = static_cast<char *>(g->lists);
     kv.second.fine = reinterpret_cast<int *>(base + o.fine);
-    kv.second.internal = reinterpret_cast<int *>(base + o.internal);
+    kv.second.coarse = reinterpret_cast<int *>(base + o.coarse);
     kv.second.xfer = reinterpret_cast<MgXfer *>(base + o.xfer);
   }
+  g->leaf_coef = reinterpret_cast<MgCoef *>(static_cast<char *>(g->lists) + lc_off);
   const Dims &d0 = g->stores.at(0).dims;
   g->nparts = (int)grid_for((int64_t)g->nleaf * d0.nx[0] * d0.nx[1] * d0.nx[2]);
   PGB_CUDA(cudaMalloc((void **)&g->partial, g->nparts * sizeof(double)));
@@ -547,18 +620,30 @@ int exch(pgb_mg *g, int L, double *f, cudaStream_t s) {
   return exchange_grid(G.tab, f, g->store_of(L).coarse, 1, 1, 1, nullptr, s, nullptr);
 }
 
-int smooth(pgb_mg *g, int L, int stages, cudaStream_t s) {
+template <bool kFast>
+int smooth_t(pgb_mg *g, int L, int stages, cudaStream_t s) {
+  if (stages == 0) return kOk;
   pgb_mg::Grid &G = g->grids.at(L);
   pgb_mg::Store &S = g->store_of(L);
-  const int nf = (int)G.fine_h.size();
-  const unsigned grid = grid_for((int64_t)nf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]);
+  const int nf = (int)G.fine_h.size(), nc = (int)G.coarse_h.size();
+  const int64_t cells = (int64_t)S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2];
   const MgOp o{g->cfg.D, g->cfg.alpha};
+  // Sweeps alternate between u and temp (odd sweeps write temp). The reference copies u
+  // into temp on every block first and each sweep's result back into u; the exchange
+  // of the second sweep then runs on temp, whose coarser leaves must hold their u.
+  if (stages >= 2 && nc) k_mg_copy<<<grid_for(nc * cells), 256, 0, s>>>(S.temp, S.u, G.coarse, nc, S.dims);
+  double *src = S.u, *dst = S.temp;
   for (int st = 0; st < stages; ++st) {
-    int rc = exch(g, L, S.u, s);
+    int rc = exch(g, L, src, s);
     if (rc) return rc;
-    k_mg_jacobi<<<grid, 256, 0, s>>>(S.view(), G.fine, nf, G.tab.geom, o, srj_weight(g->cfg, st));
-    k_mg_copy<<<grid, 256, 0, s>>>(S.u, S.temp, G.fine, nf, S.dims);
+    MgSweep sw;
+    sw.w = srj_weight(g->cfg, st);
+    sw.omw = 1.0 - sw.w;
+    sw.wd = sw.w / G.coef.den;
+    k_mg_jacobi<kFast><<<grid_for(nf * cells), 256, 0, s>>>(src, S.rhs, dst, G.fine, nf, S.dims, G.coef, o, sw);
+    std::swap(src, dst);
   }
+  if (src != S.u) k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.u, S.temp, G.fine, nf, S.dims);
   PGB_CUDA(cudaGetLastError());
   return kOk;
 }
@@ -573,45 +658,50 @@ int error_out(pgb_mg *g, int L, cudaStream_t s) {
 }
 
 // Leaf residual and its partial sums copied to pinned host memory.
-int leaf_residual(pgb_mg *g, cudaStream_t s) {
+template <bool kFast>
+int leaf_residual_t(pgb_mg *g, cudaStream_t s) {
   pgb_mg::Store &S = g->stores.at(0);
   int rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, 1, nullptr, s, nullptr);
   if (rc) return rc;
-  k_mg_leaf_residual<<<g->nparts, kResThreads, 0, s>>>(S.view(), g->nleaf, g->leaf_tab.geom,
-                                                       MgOp{g->cfg.D, g->cfg.alpha}, g->partial);
+  k_mg_leaf_residual<kFast><<<g->nparts, kResThreads, 0, s>>>(S.view(), g->nleaf, g->leaf_coef,
+                                                              MgOp{g->cfg.D, g->cfg.alpha}, g->partial);
   PGB_CUDA(cudaGetLastError());
   PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
   return kOk;
 }
 
+int leaf_residual(pgb_mg *g, cudaStream_t s) {
+  return g->exact ? leaf_residual_t<false>(g, s) : leaf_residual_t<true>(g, s);
+}
+
 // One V-cycle (AddLinearOperatorTasks, mg_solver.hpp:163-186 and 375-520) then the
 // leaf residual (mg_solver.hpp:131-146).
-int enqueue_iteration(pgb_mg *g, cudaStream_t s) {
+template <bool kFast>
+int enqueue_iteration_t(pgb_mg *g, cudaStream_t s) {
   const MgOp o{g->cfg.D, g->cfg.alpha};
   const int stages = g->cfg.stages;
   int rc;
   for (int L = g->lmax; L >= g->lmin; --L) {
     pgb_mg::Grid &G = g->grids.at(L);
     pgb_mg::Store &S = g->store_of(L);
-    const int nf = (int)G.fine_h.size(), ni = (int)G.internal_h.size();
+    const int nf = (int)G.fine_h.size();
     const int64_t cells = (int64_t)S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2];
     if (L < g->lmax) {
       if ((rc = exch(g, L, S.u, s))) return rc;
-      k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.u0, S.u, G.fine, nf, S.dims);
-      if (ni) k_mg_fas<<<grid_for(ni * cells), 256, 0, s>>>(S.view(), G.internal, ni, G.tab.geom, o);
+      k_mg_fas<kFast><<<grid_for(nf * cells), 256, 0, s>>>(S.view(), G.fine, nf, G.nint, G.coef, o);
     } else {
       k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.u0, S.u, G.fine, nf, S.dims);
     }
-    if ((rc = smooth(g, L, stages, s))) return rc;
+    if ((rc = smooth_t<kFast>(g, L, stages, s))) return rc;
     if (L > g->lmin) {
       if ((rc = exch(g, L, S.u, s))) return rc;
-      k_mg_residual<<<grid_for(nf * cells), 256, 0, s>>>(S.view(), G.fine, nf, G.tab.geom, o);
+      k_mg_residual<kFast><<<grid_for(nf * cells), 256, 0, s>>>(S.view(), G.fine, nf, G.coef, o);
       const int nx = (int)G.xfer_h.size();
       const pgb_mg::Store &P = g->store_of(L - 1);
       k_mg_restrict<<<grid_for(nx * cells / 8), 256, 0, s>>>(S.view(), P.view(), G.xfer, nx, G.tab.geom);
     } else {
       for (int c = 0; c < g->cfg.coarse_sweeps; ++c)
-        if ((rc = smooth(g, L, stages, s))) return rc;
+        if ((rc = smooth_t<kFast>(g, L, stages, s))) return rc;
       k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.res, S.u, G.fine, nf, S.dims);
       if (L < g->lmax && (rc = error_out(g, L, s))) return rc;
     }
@@ -623,12 +713,16 @@ int enqueue_iteration(pgb_mg *g, cudaStream_t s) {
     const pgb_mg::Store &P = g->store_of(L - 1);
     const int nx = (int)G.xfer_h.size();
     const int64_t cells = (int64_t)S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2];
-    k_mg_prolong_add<<<grid_for(nx * cells / 8), 256, 0, s>>>(S.view(), P.view(), G.xfer, nx, G.tab.geom);
+    k_mg_prolong_add<kFast><<<grid_for(nx * cells / 8), 256, 0, s>>>(S.view(), P.view(), G.xfer, nx, G.tab.geom);
     PGB_CUDA(cudaGetLastError());
-    if ((rc = smooth(g, L, stages, s))) return rc;
+    if ((rc = smooth_t<kFast>(g, L, stages, s))) return rc;
     if (L < g->lmax && (rc = error_out(g, L, s))) return rc;
   }
-  return leaf_residual(g, s);
+  return leaf_residual_t<kFast>(g, s);
+}
+
+int enqueue_iteration(pgb_mg *g, cudaStream_t s) {
+  return g->exact ? enqueue_iteration_t<false>(g, s) : enqueue_iteration_t<true>(g, s);
 }
 
 double host_rms(pgb_mg *g) {
@@ -702,6 +796,7 @@ int pgb_mg_create(pgb_mesh *mesh, const pgb_mg_params *p, pgb_mg **out) {
   g->cfg.coarse_sweeps = p->coarse_sweeps;
   g->cfg.D = p->D;
   g->cfg.alpha = p->alpha;
+  g->exact = p->exact != 0;
   g->max_coarsenings = p->max_coarsenings;
   int rc;
   try {

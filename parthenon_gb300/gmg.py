@@ -89,13 +89,16 @@ class CompositeMultigrid:
     103-201); FAS V-cycles smooth the level-L blocks, restrict to the parents and
     prolongate the correction back (mg_solver.hpp:375-520). Fields are the leaf blocks'
     arrays in the exchange layout with one component: (nblocks, N3, N2, N1) float64.
-    The operator is div(D grad u) - alpha u with constant D. The host part (grids,
-    index maps) needs no GPU; device memory is taken on the first solve.
+    The operator is div(D grad u) - alpha u with constant D. exact=True rounds every
+    value as the reference does (bitwise against the oracle); the default fast build
+    uses FMA and the 7-point form of the operator. The host part (grids, index maps)
+    needs no GPU; device memory is taken on the first solve.
     """
 
     def __init__(self, mesh, stages=2, jacobi=False, weight=2.0 / 3.0, coarse_sweeps=0, max_coarsenings=30,
-                 D=1.0, alpha=0.0):
+                 D=1.0, alpha=0.0, exact=False):
         p = nat.MgParams()
+        p.exact = int(bool(exact))
         p.stages, p.jacobi, p.weight = int(stages), int(bool(jacobi)), float(weight)
         p.coarse_sweeps, p.max_coarsenings = int(coarse_sweeps), int(max_coarsenings)
         p.D, p.alpha = float(D), float(alpha)

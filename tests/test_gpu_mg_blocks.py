@@ -17,7 +17,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def _pair(nx, bnx, ng, leaves, ncycles, **kw):
+def _pair(nx, bnx, ng, leaves, ncycles, exact=True, **kw):
     sim = O.OracleSim(nx, bnx, ng, leaves=leaves)
     om = O.OracleMgBlocks(sim, **kw)
     locs, geom = sim.block_info()
@@ -25,7 +25,7 @@ def _pair(nx, bnx, ng, leaves, ncycles, **kw):
     om.rhs()[:] = rhs
     rms_o = om.run(ncycles)
     m = pg.Mesh(nx, bnx, ng, leaves=leaves)
-    pm = pg.CompositeMultigrid(m, **kw)
+    pm = pg.CompositeMultigrid(m, exact=exact, **kw)
     u = torch.zeros(rhs.shape, dtype=torch.float64, device="cuda")
     r = torch.from_numpy(rhs).cuda()
     rms_p = pm.vcycles(u, r, ncycles)
@@ -43,6 +43,16 @@ def test_composite_vcycles_bitwise(name, nx, bnx, ng, leaves):
     assert np.array_equal(_interior(u, ng), _interior(om.u(), ng))
     np.testing.assert_allclose(rms_p, rms_o, rtol=1e-12, atol=0)
     assert rms_p[-1] < 5e-2 * rms_p[0]
+
+
+@pytest.mark.parametrize("name,nx,bnx,ng,leaves", MG_CASES, ids=[c[0] for c in MG_CASES])
+def test_composite_fast_build_within_rounding(name, nx, bnx, ng, leaves):
+    # FMA contraction, the 7-point form and the diagonal's reciprocal: the same
+    # algorithm rounded differently (tolerance on the max-norm of the interiors)
+    om, rms_o, u, rms_p = _pair(nx, bnx, ng, leaves, 4, exact=False, alpha=10.0)
+    ref = _interior(om.u(), ng)
+    assert np.abs(_interior(u, ng) - ref).max() <= 1e-11 * np.abs(ref).max()
+    np.testing.assert_allclose(rms_p, rms_o, rtol=1e-9, atol=0)
 
 
 @pytest.mark.parametrize("kw", [dict(stages=3), dict(stages=1), dict(jacobi=True, stages=2, weight=0.8),
@@ -68,12 +78,17 @@ def test_composite_solve_to_tolerance():
         om.run(1)
         ocyc += 1
     m = pg.Mesh(nx, bnx, ng, leaves=leaves)
-    pm = pg.CompositeMultigrid(m, alpha=10.0)
+    pm = pg.CompositeMultigrid(m, alpha=10.0, exact=True)
     u = torch.zeros(rhs.shape, dtype=torch.float64, device="cuda")
     cyc, rel = pm.solve(u, torch.from_numpy(rhs).cuda(), tol=1e-10, relative=True)
     assert rel <= 1e-10
     assert cyc == ocyc
     assert np.array_equal(_interior(u.cpu().numpy(), ng), _interior(om.u(), ng))
+    # the fast build reaches the tolerance in the same number of cycles
+    u2 = torch.zeros(rhs.shape, dtype=torch.float64, device="cuda")
+    cyc2, rel2 = pg.CompositeMultigrid(m, alpha=10.0).solve(u2, torch.from_numpy(rhs).cuda(), tol=1e-10)
+    assert rel2 <= 1e-10 and abs(cyc2 - ocyc) <= 1
+    assert torch.allclose(u2, u, rtol=0, atol=1e-9 * float(u.abs().max()))
     # ghosts hold the final leaf exchange: a fresh exchange changes nothing
     g = u.clone()
     m.upload()
