@@ -614,10 +614,14 @@ double srj_weight(const GmgConfig &c, int s) {
   return c.stages == 1 ? m1[s] : (c.stages == 2 ? m2[s] : m3[s]);
 }
 
+// exchange_grid's prolongation op: ProlongateSharedLinear with the reference's
+// coordinate arithmetic (exact build) or in its uniform-spacing form (fast build)
+int prolong_op(const pgb_mg *g) { return g->exact ? 1 : 3; }
+
 int exch(pgb_mg *g, int L, double *f, cudaStream_t s) {
   pgb_mg::Grid &G = g->grids.at(L);
   // gmg_same exchange of grid L (ProlongateSharedLinear across coarse/fine faces)
-  return exchange_grid(G.tab, f, g->store_of(L).coarse, 1, 1, 1, nullptr, s, nullptr);
+  return exchange_grid(G.tab, f, g->store_of(L).coarse, 1, 1, prolong_op(g), nullptr, s, nullptr);
 }
 
 template <bool kFast>
@@ -661,7 +665,7 @@ int error_out(pgb_mg *g, int L, cudaStream_t s) {
 template <bool kFast>
 int leaf_residual_t(pgb_mg *g, cudaStream_t s) {
   pgb_mg::Store &S = g->stores.at(0);
-  int rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, 1, nullptr, s, nullptr);
+  int rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr);
   if (rc) return rc;
   k_mg_leaf_residual<kFast><<<g->nparts, kResThreads, 0, s>>>(S.view(), g->nleaf, g->leaf_coef,
                                                               MgOp{g->cfg.D, g->cfg.alpha}, g->partial);
