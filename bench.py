@@ -664,6 +664,8 @@ def main():
     ap.add_argument("--amr-only", action="store_true",
                     help="run only the adaptive leg (profiling runs), no CPU baseline")
     ap.add_argument("--gmg-only", action="store_true", help="run only the multigrid leg (profiling runs)")
+    ap.add_argument("--gmg-composite-only", action="store_true",
+                    help="run only the composite-grid multigrid leg, no CPU baseline (profiling runs)")
     ap.add_argument("--sparse-cycles", type=int, default=100,
                     help="cycles of the adaptive sparse-advection leg (0 skips it)")
     ap.add_argument("--sparse-only", action="store_true",
@@ -683,6 +685,10 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         out = {"gmg": gmg_bench(torch), "gmg_composite": gmg_composite_bench(torch, with_cpu=False)}
+    elif args.gmg_composite_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        out = {"gmg_composite": gmg_composite_bench(torch, with_cpu=False)}
     elif args.sparse_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
