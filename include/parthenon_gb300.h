@@ -275,10 +275,13 @@ int pgb_mg_boundaries(const pgb_mg *mg, int32_t level, int32_t *out, int32_t cap
  * rms (host, may be NULL) receives sqrt(sum r^2 / N) of the leaf residual after each.
  * The stream must be a created stream (each iteration is one CUDA-graph launch). */
 int pgb_mg_vcycles(pgb_mg *mg, double *u, const double *rhs, int32_t ncycles, double *rms, void *stream);
-/* V-cycles until rms(rhs - A u) <= tol (relative = 0, the reference's
- * residual_tolerance) or <= tol * the initial rms (relative = 1), or max_cycles. */
-int pgb_mg_solve(pgb_mg *mg, double *u, const double *rhs, double tol, int32_t relative, int32_t max_cycles,
-                 int32_t *cycles_out, double *rms_out, void *stream);
+/* Iterations until rms(rhs - A u) <= tol (relative = 0, the reference's
+ * residual_tolerance) or <= tol * the initial rms (relative = 1), or max_cycles.
+ * mixed = 0: FP64 V-cycles on u. mixed = 1: iterative refinement, an FP32 V-cycle (the
+ * fast build's arithmetic; the coarsest grid in FP64 when it lies below level 0) on
+ * A e = r from e = 0 with r the FP64 leaf residual, then u += e. */
+int pgb_mg_solve(pgb_mg *mg, double *u, const double *rhs, double tol, int32_t relative, int32_t mixed,
+                 int32_t max_cycles, int32_t *cycles_out, double *rms_out, void *stream);
 
 /* ---- launch-shape autotuner ------------------------------------------------------ */
 

@@ -619,6 +619,74 @@ __global__ void __launch_bounds__(256) k_flux_correct(const DevFluxCorr *__restr
   });
 }
 
+// FP32 exchange of one component on the same tables, for the multigrid's FP32 V-cycle:
+// direct copies, restriction as the mean of the 2x2x2 fine cells and linear
+// prolongation in its uniform-spacing form (the grids of one mesh have uniform spacing).
+__global__ void __launch_bounds__(128) k_copy_f32(const DevPair *__restrict__ pairs,
+                                                  const DevWork *__restrict__ work, Dims d,
+                                                  float *__restrict__ fine, float *__restrict__ coarse) {
+  const DevWork w = work[blockIdx.x];
+  const DevPair p = pairs[w.item];
+  for_work_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], [&](int k, int j, int i) {
+    const int dk = p.dst.lo[2] + k, dj = p.dst.lo[1] + j, di = p.dst.lo[0] + i;
+    if (!p.full_mask && !mask_active(p.mask, p.dst, dk, dj, di)) return;
+    const int sk = p.src.lo[2] + k, sj = p.src.lo[1] + j, si = p.src.lo[0] + i;
+    const float v = p.src_coarse ? coarse[coarse_index(d, 1, p.src_block, 0, sk, sj, si)]
+                                 : fine[fine_index(d, 1, p.src_block, 0, sk, sj, si)];
+    if (p.dst_coarse) coarse[coarse_index(d, 1, p.dst_block, 0, dk, dj, di)] = v;
+    else fine[fine_index(d, 1, p.dst_block, 0, dk, dj, di)] = v;
+  });
+}
+
+__global__ void __launch_bounds__(256) k_restrict_f32(const DevRegion *__restrict__ regs,
+                                                      const DevWork *__restrict__ work, int nwork, Dims d,
+                                                      const float *__restrict__ fine, float *__restrict__ coarse) {
+  const int wi = warp_item();
+  if (wi >= nwork) return;
+  const DevWork w = work[wi];
+  const DevRegion r = regs[w.item];
+  const int ng = d.ng;
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
+  for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
+    const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
+    if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
+    const float *f = fine + fine_index(d, 1, r.block, 0, (ck - ng) * 2 + ng, (cj - ng) * 2 + ng, (ci - ng) * 2 + ng);
+    const float sum = ((f[0] + f[sj]) + (f[1] + f[sj + 1])) + ((f[sk] + f[sk + sj]) + (f[sk + 1] + f[sk + sj + 1]));
+    coarse[coarse_index(d, 1, r.block, 0, ck, cj, ci)] = 0.125f * sum;
+  });
+}
+
+__global__ void __launch_bounds__(256) k_prolong_f32(const DevRegion *__restrict__ regs,
+                                                     const DevWork *__restrict__ work, int nwork, Dims d,
+                                                     float *__restrict__ fine, const float *__restrict__ coarse) {
+  const int wi = warp_item();
+  if (wi >= nwork) return;
+  const DevWork w = work[wi];
+  const DevRegion r = regs[w.item];
+  const int ng = d.ng;
+  const float *__restrict__ cb = coarse + coarse_index(d, 1, r.block, 0, 0, 0, 0);
+  const int64_t cs1 = d.Nc[0], cs2 = (int64_t)d.Nc[0] * d.Nc[1];
+  const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1];
+  for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
+    const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
+    if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
+    const int64_t ce = ck * cs2 + cj * cs1 + ci;
+    const float fc = cb[ce];
+    const float m0 = 0.25f * (fc - cb[ce - 1]), p0 = 0.25f * (cb[ce + 1] - fc);
+    const float m1 = 0.25f * (fc - cb[ce - cs1]), p1 = 0.25f * (cb[ce + cs1] - fc);
+    const float m2 = 0.25f * (fc - cb[ce - cs2]), p2 = 0.25f * (cb[ce + cs2] - fc);
+    float *F = fine + fine_index(d, 1, r.block, 0, (ck - ng) * 2 + ng, (cj - ng) * 2 + ng, (ci - ng) * 2 + ng);
+    F[0] = fc - ((m0 + m1) + m2);
+    F[1] = fc + ((p0 - m1) - m2);
+    F[N0] = fc - ((m0 - p1) + m2);
+    F[N0 + 1] = fc + ((p0 + p1) - m2);
+    F[N01] = fc - ((m0 + m1) - p2);
+    F[N01 + 1] = fc + ((p0 - m1) + p2);
+    F[N01 + N0] = fc - ((m0 - p1) - p2);
+    F[N01 + N0 + 1] = fc + ((p0 + p1) + p2);
+  });
+}
+
 }  // namespace
 
 int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate,
@@ -659,6 +727,22 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
   if (t.multilevel && prolongate && t.npro_work)
     k_prolong<<<warp_item_grid(t.npro_work), 32 * kItemWarps, 0, s>>>(
         t.pro, t.pro_work, t.npro_work, t.geom, t.dims, ncomp, fine, coarse, prolong_op, alloc);
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+int exchange_grid_f32(GridTables &t, float *fine, float *coarse, cudaStream_t s) {
+  if (!fine || (t.multilevel && !coarse)) return fail(kErrInvalid, "null field pointer");
+  if (t.multilevel && t.nrs_work)
+    k_restrict_f32<<<warp_item_grid(t.nrs_work), 32 * kItemWarps, 0, s>>>(t.rs, t.rs_work, t.nrs_work, t.dims,
+                                                                        fine, coarse);
+  if (t.ncopy_work) k_copy_f32<<<t.ncopy_work, 128, 0, s>>>(t.pairs, t.copy_work, t.dims, fine, coarse);
+  if (t.multilevel && t.nrr_work)
+    k_restrict_f32<<<warp_item_grid(t.nrr_work), 32 * kItemWarps, 0, s>>>(t.rr, t.rr_work, t.nrr_work, t.dims,
+                                                                        fine, coarse);
+  if (t.multilevel && t.npro_work)
+    k_prolong_f32<<<warp_item_grid(t.npro_work), 32 * kItemWarps, 0, s>>>(t.pro, t.pro_work, t.npro_work, t.dims,
+                                                                        fine, coarse);
   PGB_CUDA(cudaGetLastError());
   return kOk;
 }

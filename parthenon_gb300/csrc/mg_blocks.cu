@@ -47,6 +47,7 @@ namespace pgb {
 MeshState *mesh_state(pgb_mesh *m);
 int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate, int prolong_op,
                   double *buffer, cudaStream_t s, const SparseDev *sp);
+int exchange_grid_f32(GridTables &t, float *fine, float *coarse, cudaStream_t s);
 }  // namespace pgb
 
 using namespace pgb;
@@ -60,11 +61,6 @@ struct MgXfer {
   int32_t child, parent;
   int32_t lo[3];
   int32_t pad;
-};
-
-struct StoreView {
-  double *u, *res, *rhs, *temp, *u0;
-  Dims d;
 };
 
 struct MgOp {
@@ -84,12 +80,22 @@ struct MgSweep {
   double w, omw, wd;
 };
 
+template <class T>
+struct StoreView {
+  T *u, *res, *rhs, *temp, *u0;
+  Dims d;
+};
+
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+
 __device__ __forceinline__ int64_t cell_of(const Dims &d, int slot, int k, int j, int i) {
   return ((int64_t)slot * d.N[2] + k) * ((int64_t)d.N[1] * d.N[0]) + (int64_t)j * d.N[0] + i;
 }
 
-// Every interior cell of the listed blocks, consecutive threads on consecutive i; f gets
-// (position in the list, slot, k, j, i). The host keeps cells x blocks below 2^31.
+// Every interior cell of the listed blocks (list == null: slots 0 .. n-1), consecutive
+// threads on consecutive i; f gets (position in the list, slot, k, j, i). The host keeps
+// cells x blocks below 2^31.
 template <class F>
 __device__ __forceinline__ void for_interior(const int *__restrict__ list, int n, const Dims &d, F &&f) {
   const int n0 = d.nx[0], n1 = d.nx[1], ng = d.ng;
@@ -102,7 +108,7 @@ __device__ __forceinline__ void for_interior(const int *__restrict__ list, int n
     const int i = c - r * n0;
     const int k = r / n1;
     const int j = r - k * n1;
-    f(q, list[q], k + ng, j + ng, i + ng);
+    f(q, list ? list[q] : q, k + ng, j + ng, i + ng);
   }
 }
 
@@ -129,21 +135,21 @@ __device__ __forceinline__ double ax_exact(const double *__restrict__ u, int64_t
 // Fast build: the constant-coefficient operator as a 7-point stencil, A u = off + dg u
 // with off = sum_d (D/dx_d^2) (u_{-d} + u_{+d}): 3 adds, a multiply and 2 FMAs (the FP64
 // pipe, not HBM, bounds these kernels on GB300)
-__device__ __forceinline__ double off_fast(const double *__restrict__ u, int64_t c, int64_t sj, int64_t sk,
-                                          const MgCoef &cf) {
-  return fma(cf.c[2], u[c - sk] + u[c + sk], fma(cf.c[1], u[c - sj] + u[c + sj], cf.c[0] * (u[c - 1] + u[c + 1])));
+template <class T>
+__device__ __forceinline__ T off_fast(const T *__restrict__ u, int64_t c, int64_t sj, int64_t sk, const MgCoef &cf) {
+  return fma_t((T)cf.c[2], u[c - sk] + u[c + sk], fma_t((T)cf.c[1], u[c - sj] + u[c + sj], (T)cf.c[0] * (u[c - 1] + u[c + 1])));
 }
 
 // Jacobi sweep (mg_solver.hpp:222-297): dst = w ratio(rhs - (A src - dg src), dg) + (1 - w) src
-template <bool kFast>
-__global__ void __launch_bounds__(256) k_mg_jacobi(const double *__restrict__ src, const double *__restrict__ rhs,
-                                                   double *__restrict__ dst, const int *__restrict__ list, int n,
+template <bool kFast, class T>
+__global__ void __launch_bounds__(256) k_mg_jacobi(const T *__restrict__ src, const T *__restrict__ rhs,
+                                                   T *__restrict__ dst, const int *__restrict__ list, int n,
                                                    Dims d, MgCoef cf, MgOp o, MgSweep sw) {
   const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
   for_interior(list, n, d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(d, b, k, j, i);
-    if (kFast) {
-      dst[c] = fma(sw.wd, rhs[c] - off_fast(src, c, sj, sk, cf), sw.omw * src[c]);
+    if constexpr (kFast) {
+      dst[c] = fma_t((T)sw.wd, rhs[c] - off_fast(src, c, sj, sk, cf), (T)sw.omw * src[c]);
     } else {
       const double a = ax_exact(src, c, sj, sk, cf.dx, o);
       const double off = a - cf.dg * src[c];
@@ -154,13 +160,13 @@ __global__ void __launch_bounds__(256) k_mg_jacobi(const double *__restrict__ sr
 }
 
 // Ax + AddFieldsAndStoreInteriorSelect<rhs, temp, res_err>(1, -1): res = rhs - A u
-template <bool kFast>
-__global__ void __launch_bounds__(256) k_mg_residual(StoreView s, const int *__restrict__ list, int n, MgCoef cf,
+template <bool kFast, class T>
+__global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *__restrict__ list, int n, MgCoef cf,
                                                      MgOp o) {
   const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
   for_interior(list, n, s.d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
-    if (kFast) s.res[c] = fma(-cf.dg, s.u[c], s.rhs[c] - off_fast(s.u, c, sj, sk, cf));
+    if constexpr (kFast) s.res[c] = fma_t(-(T)cf.dg, s.u[c], s.rhs[c] - off_fast(s.u, c, sj, sk, cf));
     else s.res[c] = s.rhs[c] - ax_exact(s.u, c, sj, sk, cf.dx, o);
   });
 }
@@ -168,22 +174,23 @@ __global__ void __launch_bounds__(256) k_mg_residual(StoreView s, const int *__r
 // Start of a level below the finest (mg_solver.hpp:405-430): u0 = u on every fine block
 // and, on the first nint (internal) blocks of the list, the FAS right-hand side
 // rhs = A u + res_err
-template <bool kFast>
-__global__ void __launch_bounds__(256) k_mg_fas(StoreView s, const int *__restrict__ list, int n, int nint,
+template <bool kFast, class T>
+__global__ void __launch_bounds__(256) k_mg_fas(StoreView<T> s, const int *__restrict__ list, int n, int nint,
                                                 MgCoef cf, MgOp o) {
   const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
   for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
-    const double uc = s.u[c];
+    const T uc = s.u[c];
     s.u0[c] = uc;
     if (q >= nint) return;
-    if (kFast) s.rhs[c] = fma(cf.dg, uc, off_fast(s.u, c, sj, sk, cf) + s.res[c]);
+    if constexpr (kFast) s.rhs[c] = fma_t((T)cf.dg, uc, off_fast(s.u, c, sj, sk, cf) + s.res[c]);
     else s.rhs[c] = ax_exact(s.u, c, sj, sk, cf.dx, o) + s.res[c];
   });
 }
 
 // CopyData on the interiors of the listed blocks
-__global__ void __launch_bounds__(256) k_mg_copy(double *__restrict__ dst, const double *__restrict__ src,
+template <class T>
+__global__ void __launch_bounds__(256) k_mg_copy(T *__restrict__ dst, const T *__restrict__ src,
                                                  const int *__restrict__ list, int n, Dims d) {
   for_interior(list, n, d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(d, b, k, j, i);
@@ -192,7 +199,8 @@ __global__ void __launch_bounds__(256) k_mg_copy(double *__restrict__ dst, const
 }
 
 // AddFieldsAndStore<u, u0, res_err>(1, -1): res = u - u0
-__global__ void __launch_bounds__(256) k_mg_error(StoreView s, const int *__restrict__ list, int n) {
+template <class T>
+__global__ void __launch_bounds__(256) k_mg_error(StoreView<T> s, const int *__restrict__ list, int n) {
   for_interior(list, n, s.d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     s.res[c] = s.u[c] - s.u0[c];
@@ -201,7 +209,10 @@ __global__ void __launch_bounds__(256) k_mg_error(StoreView s, const int *__rest
 
 // RestrictAverage (pr_ops.hpp:105-164) of the child's interior, u and res_err, into the
 // parent's octant (gmg_restrict_send + gmg_restrict_recv). One thread per parent cell.
-__global__ void __launch_bounds__(256) k_mg_restrict(StoreView cs, StoreView ps, const MgXfer *__restrict__ x,
+// FP64 children: the reference's volume-weighted form; FP32 children (the mixed
+// V-cycle): the mean of the eight cells. TP is the parent's type.
+template <class TC, class TP>
+__global__ void __launch_bounds__(256) k_mg_restrict(StoreView<TC> cs, StoreView<TP> ps, const MgXfer *__restrict__ x,
                                                      int n, const DevBlockGeom *__restrict__ cgeom) {
   const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
   const int per = h0 * h1 * h2, total = per * n;
@@ -212,20 +223,28 @@ __global__ void __launch_bounds__(256) k_mg_restrict(StoreView cs, StoreView ps,
     const int r = e - q * per;
     const int ci = r % h0, cjj = (r / h0) % h1, ckk = r / (h0 * h1);
     const MgXfer t = x[q];
-    const double vol = cgeom[t.child].vol;
     const int64_t f = cell_of(cs.d, t.child, 2 * ckk + ng, 2 * cjj + ng, 2 * ci + ng);
     const int64_t p = cell_of(ps.d, t.parent, t.lo[2] + ckk, t.lo[1] + cjj, t.lo[0] + ci);
-    const double tv = ((vol + vol) + (vol + vol)) + ((vol + vol) + (vol + vol));
 #pragma unroll
     for (int v = 0; v < 2; ++v) {
-      const double *__restrict__ a = v == 0 ? cs.u : cs.res;
-      // t[ok][oj][oi] = vol * fine(k + ok, j + oj, i + oi)
-      const double t000 = vol * a[f], t001 = vol * a[f + 1];
-      const double t010 = vol * a[f + cj], t011 = vol * a[f + cj + 1];
-      const double t100 = vol * a[f + ck], t101 = vol * a[f + ck + 1];
-      const double t110 = vol * a[f + ck + cj], t111 = vol * a[f + ck + cj + 1];
-      const double num = ((t000 + t010) + (t001 + t011)) + ((t100 + t110) + (t101 + t111));
-      (v == 0 ? ps.u : ps.res)[p] = div_rn(num, tv);
+      const TC *__restrict__ a = v == 0 ? cs.u : cs.res;
+      TP out;
+      if constexpr (sizeof(TC) == 8) {
+        const double vol = cgeom[t.child].vol;
+        const double tv = ((vol + vol) + (vol + vol)) + ((vol + vol) + (vol + vol));
+        // t[ok][oj][oi] = vol * fine(k + ok, j + oj, i + oi)
+        const double t000 = vol * a[f], t001 = vol * a[f + 1];
+        const double t010 = vol * a[f + cj], t011 = vol * a[f + cj + 1];
+        const double t100 = vol * a[f + ck], t101 = vol * a[f + ck + 1];
+        const double t110 = vol * a[f + ck + cj], t111 = vol * a[f + ck + cj + 1];
+        const double num = ((t000 + t010) + (t001 + t011)) + ((t100 + t110) + (t101 + t111));
+        out = (TP)div_rn(num, tv);
+      } else {
+        const TC sum = ((a[f] + a[f + cj]) + (a[f + 1] + a[f + cj + 1])) +
+                       ((a[f + ck] + a[f + ck + cj]) + (a[f + ck + 1] + a[f + ck + cj + 1]));
+        out = (TP)((TC)0.125 * sum);
+      }
+      (v == 0 ? ps.u : ps.res)[p] = out;
     }
   }
 }
@@ -235,9 +254,11 @@ __global__ void __launch_bounds__(256) k_mg_restrict(StoreView cs, StoreView ps,
 // per coarse cell of the child's interior, eight fine cells each. The exact build forms
 // the slopes from the cell-centre coordinates as the reference does; the fast build
 // uses the uniform-spacing value dx_fine / 2 / dx_coarse = 1/4 of each difference.
-template <bool kFast>
-__global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView cs, StoreView ps, const MgXfer *__restrict__ x,
-                                                        int n, const DevBlockGeom *__restrict__ cgeom) {
+// TC is the child's type (the arithmetic), TP the parent's.
+template <bool kFast, class TC, class TP>
+__global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreView<TP> ps,
+                                                        const MgXfer *__restrict__ x, int n,
+                                                        const DevBlockGeom *__restrict__ cgeom) {
   const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
   const int per = h0 * h1 * h2, total = per * n;
   const int ng = cs.d.ng;
@@ -251,14 +272,14 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView cs, StoreView 
     const int c[3] = {c0 + ng, c1 + ng, c2 + ng};  // coarse-buffer index
     const int f[3] = {2 * c0 + ng, 2 * c1 + ng, 2 * c2 + ng};
     const int64_t pe = cell_of(ps.d, t.parent, t.lo[2] + c2, t.lo[1] + c1, t.lo[0] + c0);
-    const double fc = ps.res[pe];
-    double mq[3], pq[3];
+    const TC fc = (TC)ps.res[pe];
+    TC mq[3], pq[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int64_t st = d == 0 ? 1 : (d == 1 ? pj : pk);
-      if (kFast) {
-        mq[d] = 0.25 * (fc - ps.res[pe - st]);
-        pq[d] = 0.25 * (ps.res[pe + st] - fc);
+      if constexpr (kFast) {
+        mq[d] = (TC)0.25 * (fc - (TC)ps.res[pe - st]);
+        pq[d] = (TC)0.25 * ((TC)ps.res[pe + st] - fc);
       } else {
         const DevBlockGeom &g = cgeom[t.child];
         auto xcc = [&](int idx) { return g.cxmin[d] + ((double)idx + 0.5) * g.cdx[d]; };
@@ -271,8 +292,8 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView cs, StoreView 
         pq[d] = div_rn(ps.res[pe + st] - fc, dxp) * dfp;
       }
     }
-    const double m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
-    double *U = cs.u + cell_of(cs.d, t.child, f[2], f[1], f[0]);
+    const TC m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
+    TC *U = cs.u + cell_of(cs.d, t.child, f[2], f[1], f[0]);
     U[0] = U[0] + (fc - ((m0 + m1) + m2));
     U[1] = U[1] + (fc + ((p0 - m1) - m2));
     U[N0] = U[N0] + (fc - ((m0 - p1) + m2));
@@ -286,29 +307,31 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView cs, StoreView 
 
 // Leaf-grid residual of MGSolver::AddTasks (mg_solver.hpp:135-158): res = rhs - A u
 // over every leaf interior (operator constants per leaf, levels differ) and one partial
-// sum of r^2 per CTA (fixed tree order, so the host's fixed-order total is reproducible)
+// sum of r^2 per CTA (fixed tree order, so the host's fixed-order total is reproducible).
+// Mixed solve: also the FP32 right-hand side of the next V-cycle (rhs32 = r) and its
+// zero initial guess (u32 = 0) on the leaves.
 constexpr int kResThreads = 256;
 template <bool kFast>
-__global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView s, int nleaf,
+__global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView<double> s, int nleaf,
                                                                   const MgCoef *__restrict__ lc, MgOp o,
-                                                                  double *__restrict__ partial) {
+                                                                  double *__restrict__ partial,
+                                                                  float *__restrict__ rhs32, float *__restrict__ u32) {
   __shared__ double sh[kResThreads];
   const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
-  const int n0 = s.d.nx[0], n1 = s.d.nx[1], ng = s.d.ng;
-  const int per = n0 * n1 * s.d.nx[2], total = per * nleaf;
   double acc = 0.0;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const int b = e / per;
-    const int cc = e - b * per;
-    const int rr = cc / n0, i = cc - rr * n0, k = rr / n1, j = rr - k * n1;
-    const int64_t c = cell_of(s.d, b, k + ng, j + ng, i + ng);
+  for_interior(nullptr, nleaf, s.d, [&](int, int b, int k, int j, int i) {
+    const int64_t c = cell_of(s.d, b, k, j, i);
     const MgCoef &cf = lc[b];
     double r;
-    if (kFast) r = fma(-cf.dg, s.u[c], s.rhs[c] - off_fast(s.u, c, sj, sk, cf));
+    if constexpr (kFast) r = fma(-cf.dg, s.u[c], s.rhs[c] - off_fast(s.u, c, sj, sk, cf));
     else r = s.rhs[c] - ax_exact(s.u, c, sj, sk, cf.dx, o);
     s.res[c] = r;
     acc += r * r;
-  }
+    if (rhs32) {
+      rhs32[c] = (float)r;
+      u32[c] = 0.0f;
+    }
+  });
   sh[threadIdx.x] = acc;
   __syncthreads();
   for (int w = kResThreads / 2; w > 0; w >>= 1) {
@@ -316,6 +339,15 @@ __global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView s, i
     __syncthreads();
   }
   if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// Iterative refinement: u += e on the leaf interiors (e the FP32 V-cycle's result)
+__global__ void __launch_bounds__(256) k_mg_correct(double *__restrict__ u, const float *__restrict__ e, int nleaf,
+                                                    Dims d) {
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t c = cell_of(d, b, k, j, i);
+    u[c] = u[c] + (double)e[c];
+  });
 }
 
 unsigned grid_for(int64_t work) {
@@ -336,8 +368,15 @@ struct pgb_mg {
     int nslots = 0;
     std::vector<BlockInfo> blocks;
     double *u = nullptr, *res = nullptr, *rhs = nullptr, *temp = nullptr, *u0 = nullptr, *coarse = nullptr;
+    // the FP32 copies of the mixed solve (allocated on its first use)
+    float *u32 = nullptr, *res32 = nullptr, *rhs32 = nullptr, *temp32 = nullptr, *u032 = nullptr,
+          *coarse32 = nullptr;
     Dims dims{};
-    StoreView view() const { return StoreView{u, res, rhs, temp, u0, dims}; }
+    template <class T>
+    StoreView<T> view() const {
+      if constexpr (sizeof(T) == 8) return StoreView<T>{u, res, rhs, temp, u0, dims};
+      else return StoreView<T>{u32, res32, rhs32, temp32, u032, dims};
+    }
   };
   std::map<int, Store> stores;  // key 0: full-size blocks; key L < 0: the blocks of level L
   struct Grid {
@@ -359,15 +398,16 @@ struct pgb_mg {
   void *lists = nullptr;
   double *partial = nullptr, *partial_h = nullptr;
   int nparts = 0;
-  bool uploaded = false;
-  cudaGraphExec_t graph = nullptr;
+  bool uploaded = false, uploaded32 = false;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // FP64 and mixed iterations
   std::vector<void *> allocs;
 
   static int key(int level) { return level >= 0 ? 0 : level; }
   Store &store_of(int level) { return stores.at(key(level)); }
 
   ~pgb_mg() {
-    if (graph) cudaGraphExecDestroy(graph);
+    for (auto &gr : graph)
+      if (gr) cudaGraphExecDestroy(gr);
     for (auto &kv : grids) kv.second.tab.release();
     leaf_tab.release();
     for (void *p : allocs) cudaFree(p);
@@ -605,6 +645,26 @@ int mg_upload(pgb_mg *g) {
   return kOk;
 }
 
+// FP32 copies of every store for the mixed solve
+int mg_upload32(pgb_mg *g) {
+  if (g->uploaded32) return kOk;
+  for (auto &kv : g->stores) {
+    pgb_mg::Store &S = kv.second;
+    const int64_t n = (int64_t)S.nslots * S.dims.N[0] * S.dims.N[1] * S.dims.N[2];
+    const int64_t nc = (int64_t)S.nslots * S.dims.Nc[0] * S.dims.Nc[1] * S.dims.Nc[2];
+    for (float **p : {&S.u32, &S.res32, &S.rhs32, &S.temp32, &S.u032}) {
+      PGB_CUDA(cudaMalloc((void **)p, n * sizeof(float)));
+      PGB_CUDA(cudaMemset(*p, 0, n * sizeof(float)));
+      g->allocs.push_back(*p);
+    }
+    PGB_CUDA(cudaMalloc((void **)&S.coarse32, nc * sizeof(float)));
+    PGB_CUDA(cudaMemset(S.coarse32, 0, nc * sizeof(float)));
+    g->allocs.push_back(S.coarse32);
+  }
+  g->uploaded32 = true;
+  return kOk;
+}
+
 double srj_weight(const GmgConfig &c, int s) {
   // mg_solver.hpp:312-345, 3D weights (Yang & Mittal)
   static const double m1[3] = {1.0, 0.0, 0.0};
@@ -618,115 +678,185 @@ double srj_weight(const GmgConfig &c, int s) {
 // coordinate arithmetic (exact build) or in its uniform-spacing form (fast build)
 int prolong_op(const pgb_mg *g) { return g->exact ? 1 : 3; }
 
+// gmg_same exchange of grid L (ProlongateSharedLinear across coarse/fine faces)
 int exch(pgb_mg *g, int L, double *f, cudaStream_t s) {
-  pgb_mg::Grid &G = g->grids.at(L);
-  // gmg_same exchange of grid L (ProlongateSharedLinear across coarse/fine faces)
-  return exchange_grid(G.tab, f, g->store_of(L).coarse, 1, 1, prolong_op(g), nullptr, s, nullptr);
+  return exchange_grid(g->grids.at(L).tab, f, g->store_of(L).coarse, 1, 1, prolong_op(g), nullptr, s, nullptr);
+}
+int exch(pgb_mg *g, int L, float *f, cudaStream_t s) {
+  return exchange_grid_f32(g->grids.at(L).tab, f, g->store_of(L).coarse32, s);
 }
 
+// One V-cycle (AddLinearOperatorTasks, mg_solver.hpp:163-186, and per level
+// AddMultiGridTasksPartitionLevel, :375-520). Every grid runs in FP64, or, in the mixed
+// solve, in FP32 except the coarsest grid when it has a store of its own (FP64).
 template <bool kFast>
-int smooth_t(pgb_mg *g, int L, int stages, cudaStream_t s) {
-  if (stages == 0) return kOk;
-  pgb_mg::Grid &G = g->grids.at(L);
-  pgb_mg::Store &S = g->store_of(L);
-  const int nf = (int)G.fine_h.size(), nc = (int)G.coarse_h.size();
-  const int64_t cells = (int64_t)S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2];
-  const MgOp o{g->cfg.D, g->cfg.alpha};
-  // Sweeps alternate between u and temp (odd sweeps write temp). The reference copies u
-  // into temp on every block first and each sweep's result back into u; the exchange
-  // of the second sweep then runs on temp, whose coarser leaves must hold their u.
-  if (stages >= 2 && nc) k_mg_copy<<<grid_for(nc * cells), 256, 0, s>>>(S.temp, S.u, G.coarse, nc, S.dims);
-  double *src = S.u, *dst = S.temp;
-  for (int st = 0; st < stages; ++st) {
-    int rc = exch(g, L, src, s);
-    if (rc) return rc;
-    MgSweep sw;
-    sw.w = srj_weight(g->cfg, st);
-    sw.omw = 1.0 - sw.w;
-    sw.wd = sw.w / G.coef.den;
-    k_mg_jacobi<kFast><<<grid_for(nf * cells), 256, 0, s>>>(src, S.rhs, dst, G.fine, nf, S.dims, G.coef, o, sw);
-    std::swap(src, dst);
+struct VCycle {
+  pgb_mg *g;
+  cudaStream_t s;
+  bool mixed;
+  MgOp o;
+  bool dbl(int L) const { return !mixed || (L == g->lmin && g->lmin < 0); }
+  int64_t cells(int L) const {
+    const Dims &d = g->store_of(L).dims;
+    return (int64_t)d.nx[0] * d.nx[1] * d.nx[2];
   }
-  if (src != S.u) k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.u, S.temp, G.fine, nf, S.dims);
-  PGB_CUDA(cudaGetLastError());
-  return kOk;
-}
 
-int error_out(pgb_mg *g, int L, cudaStream_t s) {
-  pgb_mg::Grid &G = g->grids.at(L);
-  pgb_mg::Store &S = g->store_of(L);
-  const int nf = (int)G.fine_h.size();
-  k_mg_error<<<grid_for((int64_t)nf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]), 256, 0, s>>>(S.view(), G.fine, nf);
-  PGB_CUDA(cudaGetLastError());
-  return exch(g, L, S.res, s);
-}
+  template <class T>
+  int smooth(int L, int stages) {
+    if (stages == 0) return kOk;
+    pgb_mg::Grid &G = g->grids.at(L);
+    pgb_mg::Store &S = g->store_of(L);
+    const StoreView<T> v = S.template view<T>();
+    const int nf = (int)G.fine_h.size(), nc = (int)G.coarse_h.size();
+    const int64_t cl = cells(L);
+    // Sweeps alternate between u and temp (odd sweeps write temp). The reference copies
+    // u into temp on every block first and each sweep's result back into u; the
+    // exchange of the second sweep then runs on temp, whose coarser leaves must hold
+    // their u.
+    if (stages >= 2 && nc) k_mg_copy<T><<<grid_for(nc * cl), 256, 0, s>>>(v.temp, v.u, G.coarse, nc, v.d);
+    T *src = v.u, *dst = v.temp;
+    for (int st = 0; st < stages; ++st) {
+      int rc = exch(g, L, src, s);
+      if (rc) return rc;
+      MgSweep sw;
+      sw.w = srj_weight(g->cfg, st);
+      sw.omw = 1.0 - sw.w;
+      sw.wd = sw.w / G.coef.den;
+      k_mg_jacobi<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(src, v.rhs, dst, G.fine, nf, v.d, G.coef, o, sw);
+      std::swap(src, dst);
+    }
+    if (src != v.u) k_mg_copy<T><<<grid_for(nf * cl), 256, 0, s>>>(v.u, v.temp, G.fine, nf, v.d);
+    PGB_CUDA(cudaGetLastError());
+    return kOk;
+  }
 
-// Leaf residual and its partial sums copied to pinned host memory.
+  // res_err = u - u0 on the fine blocks and its exchange (mg_solver.hpp:489-517)
+  template <class T>
+  int error_out(int L) {
+    pgb_mg::Grid &G = g->grids.at(L);
+    const StoreView<T> v = g->store_of(L).template view<T>();
+    const int nf = (int)G.fine_h.size();
+    k_mg_error<T><<<grid_for(nf * cells(L)), 256, 0, s>>>(v, G.fine, nf);
+    PGB_CUDA(cudaGetLastError());
+    return exch(g, L, v.res, s);
+  }
+
+  template <class T, class TP>
+  int restrict_down(int L) {
+    pgb_mg::Grid &G = g->grids.at(L);
+    const int nx = (int)G.xfer_h.size();
+    k_mg_restrict<T, TP><<<grid_for(nx * cells(L) / 8), 256, 0, s>>>(
+        g->store_of(L).template view<T>(), g->store_of(L - 1).template view<TP>(), G.xfer, nx, G.tab.geom);
+    PGB_CUDA(cudaGetLastError());
+    return kOk;
+  }
+
+  template <class T>
+  int down(int L) {
+    pgb_mg::Grid &G = g->grids.at(L);
+    const StoreView<T> v = g->store_of(L).template view<T>();
+    const int nf = (int)G.fine_h.size();
+    const int64_t cl = cells(L);
+    int rc;
+    if (L < g->lmax) {
+      // FAS: exchange, u0 = u, rhs = A u + res_err on internal blocks
+      if ((rc = exch(g, L, v.u, s))) return rc;
+      k_mg_fas<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(v, G.fine, nf, G.nint, G.coef, o);
+    } else {
+      k_mg_copy<T><<<grid_for(nf * cl), 256, 0, s>>>(v.u0, v.u, G.fine, nf, v.d);
+    }
+    if ((rc = smooth<T>(L, g->cfg.stages))) return rc;
+    if (L > g->lmin) {
+      if ((rc = exch(g, L, v.u, s))) return rc;
+      k_mg_residual<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(v, G.fine, nf, G.coef, o);
+      if constexpr (kFast) rc = dbl(L - 1) ? restrict_down<T, double>(L) : restrict_down<T, float>(L);
+      else rc = restrict_down<T, double>(L);
+      if (rc) return rc;
+    } else {
+      for (int c = 0; c < g->cfg.coarse_sweeps; ++c)
+        if ((rc = smooth<T>(L, g->cfg.stages))) return rc;
+      k_mg_copy<T><<<grid_for(nf * cl), 256, 0, s>>>(v.res, v.u, G.fine, nf, v.d);
+      if (L < g->lmax && (rc = error_out<T>(L))) return rc;
+    }
+    PGB_CUDA(cudaGetLastError());
+    return kOk;
+  }
+
+  template <class T, class TP>
+  int prolong_add(int L) {
+    pgb_mg::Grid &G = g->grids.at(L);
+    const int nx = (int)G.xfer_h.size();
+    k_mg_prolong_add<kFast, T, TP><<<grid_for(nx * cells(L) / 8), 256, 0, s>>>(
+        g->store_of(L).template view<T>(), g->store_of(L - 1).template view<TP>(), G.xfer, nx, G.tab.geom);
+    PGB_CUDA(cudaGetLastError());
+    return kOk;
+  }
+
+  template <class T>
+  int up(int L) {
+    int rc;
+    if constexpr (kFast) rc = dbl(L - 1) ? prolong_add<T, double>(L) : prolong_add<T, float>(L);
+    else rc = prolong_add<T, double>(L);
+    if (rc) return rc;
+    if ((rc = smooth<T>(L, g->cfg.stages))) return rc;
+    if (L < g->lmax && (rc = error_out<T>(L))) return rc;
+    return kOk;
+  }
+
+  int run() {
+    int rc;
+    for (int L = g->lmax; L >= g->lmin; --L) {
+      if constexpr (kFast) rc = dbl(L) ? down<double>(L) : down<float>(L);
+      else rc = down<double>(L);  // the exact build is FP64 only
+      if (rc) return rc;
+    }
+    for (int L = g->lmin + 1; L <= g->lmax; ++L) {
+      if constexpr (kFast) rc = dbl(L) ? up<double>(L) : up<float>(L);
+      else rc = up<double>(L);
+      if (rc) return rc;
+    }
+    return kOk;
+  }
+};
+
+// Leaf residual (exchange and rhs - A u on the leaf grid, mg_solver.hpp:131-146) with
+// its partial sums copied to pinned host memory; mixed: also the FP32 right-hand side
+// and zero guess of the next V-cycle.
 template <bool kFast>
-int leaf_residual_t(pgb_mg *g, cudaStream_t s) {
+int leaf_residual_t(pgb_mg *g, bool mixed, cudaStream_t s) {
   pgb_mg::Store &S = g->stores.at(0);
   int rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr);
   if (rc) return rc;
-  k_mg_leaf_residual<kFast><<<g->nparts, kResThreads, 0, s>>>(S.view(), g->nleaf, g->leaf_coef,
-                                                              MgOp{g->cfg.D, g->cfg.alpha}, g->partial);
+  k_mg_leaf_residual<kFast><<<g->nparts, kResThreads, 0, s>>>(S.template view<double>(), g->nleaf, g->leaf_coef,
+                                                              MgOp{g->cfg.D, g->cfg.alpha}, g->partial,
+                                                              mixed ? S.rhs32 : nullptr, mixed ? S.u32 : nullptr);
   PGB_CUDA(cudaGetLastError());
   PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
   return kOk;
 }
 
-int leaf_residual(pgb_mg *g, cudaStream_t s) {
-  return g->exact ? leaf_residual_t<false>(g, s) : leaf_residual_t<true>(g, s);
+int leaf_residual(pgb_mg *g, bool mixed, cudaStream_t s) {
+  return g->exact ? leaf_residual_t<false>(g, mixed, s) : leaf_residual_t<true>(g, mixed, s);
 }
 
-// One V-cycle (AddLinearOperatorTasks, mg_solver.hpp:163-186 and 375-520) then the
-// leaf residual (mg_solver.hpp:131-146).
+// One iteration of the solve: the V-cycle then the leaf residual. FP64: V-cycle on u;
+// mixed: FP32 V-cycle on A e = r from e = 0, u += e, residual (iterative refinement).
 template <bool kFast>
-int enqueue_iteration_t(pgb_mg *g, cudaStream_t s) {
-  const MgOp o{g->cfg.D, g->cfg.alpha};
-  const int stages = g->cfg.stages;
-  int rc;
-  for (int L = g->lmax; L >= g->lmin; --L) {
-    pgb_mg::Grid &G = g->grids.at(L);
-    pgb_mg::Store &S = g->store_of(L);
-    const int nf = (int)G.fine_h.size();
-    const int64_t cells = (int64_t)S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2];
-    if (L < g->lmax) {
-      if ((rc = exch(g, L, S.u, s))) return rc;
-      k_mg_fas<kFast><<<grid_for(nf * cells), 256, 0, s>>>(S.view(), G.fine, nf, G.nint, G.coef, o);
-    } else {
-      k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.u0, S.u, G.fine, nf, S.dims);
-    }
-    if ((rc = smooth_t<kFast>(g, L, stages, s))) return rc;
-    if (L > g->lmin) {
-      if ((rc = exch(g, L, S.u, s))) return rc;
-      k_mg_residual<kFast><<<grid_for(nf * cells), 256, 0, s>>>(S.view(), G.fine, nf, G.coef, o);
-      const int nx = (int)G.xfer_h.size();
-      const pgb_mg::Store &P = g->store_of(L - 1);
-      k_mg_restrict<<<grid_for(nx * cells / 8), 256, 0, s>>>(S.view(), P.view(), G.xfer, nx, G.tab.geom);
-    } else {
-      for (int c = 0; c < g->cfg.coarse_sweeps; ++c)
-        if ((rc = smooth_t<kFast>(g, L, stages, s))) return rc;
-      k_mg_copy<<<grid_for(nf * cells), 256, 0, s>>>(S.res, S.u, G.fine, nf, S.dims);
-      if (L < g->lmax && (rc = error_out(g, L, s))) return rc;
-    }
+int enqueue_iteration_t(pgb_mg *g, bool mixed, cudaStream_t s) {
+  VCycle<kFast> vc{g, s, mixed, MgOp{g->cfg.D, g->cfg.alpha}};
+  int rc = vc.run();
+  if (rc) return rc;
+  if (mixed) {
+    pgb_mg::Store &S = g->stores.at(0);
+    k_mg_correct<<<grid_for((int64_t)g->nleaf * vc.cells(g->lmax)), 256, 0, s>>>(S.u, S.u32, g->nleaf, S.dims);
     PGB_CUDA(cudaGetLastError());
   }
-  for (int L = g->lmin + 1; L <= g->lmax; ++L) {
-    pgb_mg::Grid &G = g->grids.at(L);
-    pgb_mg::Store &S = g->store_of(L);
-    const pgb_mg::Store &P = g->store_of(L - 1);
-    const int nx = (int)G.xfer_h.size();
-    const int64_t cells = (int64_t)S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2];
-    k_mg_prolong_add<kFast><<<grid_for(nx * cells / 8), 256, 0, s>>>(S.view(), P.view(), G.xfer, nx, G.tab.geom);
-    PGB_CUDA(cudaGetLastError());
-    if ((rc = smooth_t<kFast>(g, L, stages, s))) return rc;
-    if (L < g->lmax && (rc = error_out(g, L, s))) return rc;
-  }
-  return leaf_residual_t<kFast>(g, s);
+  return leaf_residual_t<kFast>(g, mixed, s);
 }
 
-int enqueue_iteration(pgb_mg *g, cudaStream_t s) {
-  return g->exact ? enqueue_iteration_t<false>(g, s) : enqueue_iteration_t<true>(g, s);
+int enqueue_iteration(pgb_mg *g, bool mixed, cudaStream_t s) {
+  if (mixed) return enqueue_iteration_t<true>(g, true, s);
+  return g->exact ? enqueue_iteration_t<false>(g, false, s) : enqueue_iteration_t<true>(g, false, s);
 }
 
 double host_rms(pgb_mg *g) {
@@ -737,22 +867,23 @@ double host_rms(pgb_mg *g) {
   return std::sqrt(sum / ncell);
 }
 
-int run_iteration(pgb_mg *g, cudaStream_t s) {
-  if (!g->graph) {
+int run_iteration(pgb_mg *g, bool mixed, cudaStream_t s) {
+  cudaGraphExec_t &graph = g->graph[mixed ? 1 : 0];
+  if (!graph) {
     cudaGraph_t gr;
     PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_iteration(g, s);
+    int rc = enqueue_iteration(g, mixed, s);
     cudaError_t e = cudaStreamEndCapture(s, &gr);
     if (rc) {
       if (e == cudaSuccess) cudaGraphDestroy(gr);
       return rc;
     }
     PGB_CUDA(e);
-    e = cudaGraphInstantiate(&g->graph, gr, 0);
+    e = cudaGraphInstantiate(&graph, gr, 0);
     cudaGraphDestroy(gr);
     PGB_CUDA(e);
   }
-  PGB_CUDA(cudaGraphLaunch(g->graph, s));
+  PGB_CUDA(cudaGraphLaunch(graph, s));
   return kOk;
 }
 
@@ -867,7 +998,7 @@ int pgb_mg_vcycles(pgb_mg *g, double *u, const double *rhs, int32_t ncycles, dou
   int rc;
   if ((rc = check_stream(s)) || (rc = mg_upload(g)) || (rc = copy_in(g, u, rhs, s))) return rc;
   for (int c = 0; c < ncycles; ++c) {
-    if ((rc = run_iteration(g, s))) return rc;
+    if ((rc = run_iteration(g, false, s))) return rc;
     PGB_CUDA(cudaStreamSynchronize(s));
     if (rms) rms[c] = host_rms(g);
   }
@@ -876,13 +1007,16 @@ int pgb_mg_vcycles(pgb_mg *g, double *u, const double *rhs, int32_t ncycles, dou
   return kOk;
 }
 
-int pgb_mg_solve(pgb_mg *g, double *u, const double *rhs, double tol, int32_t relative, int32_t max_cycles,
-                 int32_t *cycles_out, double *rms_out, void *stream) {
+int pgb_mg_solve(pgb_mg *g, double *u, const double *rhs, double tol, int32_t relative, int32_t mixed,
+                 int32_t max_cycles, int32_t *cycles_out, double *rms_out, void *stream) {
   if (!g || !u || !rhs) return fail(kErrInvalid, "null argument");
   cudaStream_t s = (cudaStream_t)stream;
+  const bool mx = mixed != 0;
   int rc;
-  if ((rc = check_stream(s)) || (rc = mg_upload(g)) || (rc = copy_in(g, u, rhs, s))) return rc;
-  if ((rc = leaf_residual(g, s))) return rc;
+  if ((rc = check_stream(s)) || (rc = mg_upload(g)) || (mx && (rc = mg_upload32(g))) ||
+      (rc = copy_in(g, u, rhs, s)))
+    return rc;
+  if ((rc = mx ? leaf_residual_t<true>(g, true, s) : leaf_residual(g, false, s))) return rc;
   PGB_CUDA(cudaStreamSynchronize(s));
   const double r0 = host_rms(g);
   const double target = relative ? tol * r0 : tol;
@@ -890,7 +1024,7 @@ int pgb_mg_solve(pgb_mg *g, double *u, const double *rhs, double tol, int32_t re
   int c = 0;
   // MGSolver::AddTasks: iterate while rms > tolerance (mg_solver.hpp:147-158)
   while (r > target && c < max_cycles) {
-    if ((rc = run_iteration(g, s))) return rc;
+    if ((rc = run_iteration(g, mx, s))) return rc;
     PGB_CUDA(cudaStreamSynchronize(s));
     r = host_rms(g);
     ++c;

@@ -153,16 +153,18 @@ class CompositeMultigrid:
         torch.cuda.current_stream().wait_stream(s)
         return rms[:ncycles]
 
-    def solve(self, u, rhs, tol=1e-10, relative=True, max_cycles=200, stream=None):
-        """V-cycles until the rms leaf residual is below tol (times the initial one when
-        relative); returns (cycles, final rms or relative rms)."""
+    def solve(self, u, rhs, tol=1e-10, relative=True, max_cycles=200, mixed=False, stream=None):
+        """Iterations until the rms leaf residual is below tol (times the initial one when
+        relative); mixed: an FP32 V-cycle inside FP64 iterative refinement. Returns
+        (iterations, final rms or relative rms)."""
         import torch
         self._check(u, rhs)
         s = self._stream(stream)
         cyc = ctypes.c_int32(0)
         r = ctypes.c_double(0.0)
         nat.check(nat.lib().pgb_mg_solve(self._h, _ptr(u), _ptr(rhs), float(tol), int(bool(relative)),
-                                         int(max_cycles), ctypes.byref(cyc), ctypes.byref(r), _stream(s)),
+                                         int(bool(mixed)), int(max_cycles), ctypes.byref(cyc), ctypes.byref(r),
+                                         _stream(s)),
                   "pgb_mg_solve")
         torch.cuda.current_stream().wait_stream(s)
         return cyc.value, r.value

@@ -106,3 +106,20 @@ def test_composite_requires_created_stream():
     u = torch.zeros((m.nblocks, N[2], N[1], N[0]), dtype=torch.float64, device="cuda")
     with pytest.raises(pg.NativeError):
         pm.vcycles(u, u.clone(), 1, stream=torch.cuda.default_stream())
+
+
+@pytest.mark.parametrize("name,nx,bnx,ng,leaves", MG_CASES, ids=[c[0] for c in MG_CASES])
+def test_composite_mixed_precision_solve(name, nx, bnx, ng, leaves):
+    # an FP32 V-cycle on A e = r inside FP64 iterative refinement reaches the FP64
+    # tolerance and the FP64 solve's solution
+    m = pg.Mesh(nx, bnx, ng, leaves=leaves)
+    locs, geom = m.block_info()
+    r = torch.from_numpy(gaussian_rhs(locs, geom, bnx, ng)).cuda()
+    u64 = torch.zeros_like(r)
+    c64, rel64 = pg.CompositeMultigrid(m, alpha=10.0).solve(u64, r, tol=1e-10)
+    u32 = torch.zeros_like(r)
+    c32, rel32 = pg.CompositeMultigrid(m, alpha=10.0).solve(u32, r, tol=1e-10, mixed=True)
+    assert rel64 <= 1e-10 and rel32 <= 1e-10
+    assert c32 <= c64 + 2
+    a, b = _interior(u64.cpu().numpy(), ng), _interior(u32.cpu().numpy(), ng)
+    assert np.abs(a - b).max() <= 1e-8 * np.abs(a).max()
