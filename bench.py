@@ -366,19 +366,28 @@ def gmg_composite_bench(torch, with_cpu):
     rhs = torch.tensor(rhs_h, device="cuda")
     mg = pg.CompositeMultigrid(mesh, stages=2, alpha=GMGC_ALPHA)
     s = torch.cuda.Stream()
-    best = None
-    for rep in range(3):
-        u = torch.zeros_like(rhs)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        cyc, rel = mg.solve(u, rhs, tol=1e-10, relative=True, max_cycles=200, stream=s)
-        s.synchronize()
-        dt = time.perf_counter() - t0
-        if rep > 0 and (best is None or dt < best[0]):  # the first solve builds the graph
-            best = (dt, cyc, rel)
+    runs, sols = {}, {}
+    for mixed in (False, True):
+        best = None
+        for rep in range(3):
+            u = torch.zeros_like(rhs)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            cyc, rel = mg.solve(u, rhs, tol=1e-10, relative=True, max_cycles=200, mixed=mixed, stream=s)
+            s.synchronize()
+            dt = time.perf_counter() - t0
+            if rep > 0 and (best is None or dt < best[0]):  # the first solve builds the graph
+                best = (dt, cyc, rel)
+        runs[mixed] = best
+        sols[mixed] = u[:, GMGC_NG:-GMGC_NG, GMGC_NG:-GMGC_NG, GMGC_NG:-GMGC_NG].cpu()
+    best = runs[False]
     locs, _ = mesh.block_info()
     res = {"seconds": best[0], "vcycles": best[1], "rel_residual": best[2],
            "ms_per_vcycle": 1e3 * best[0] / max(1, best[1]),
+           "mixed": {"seconds": runs[True][0], "iterations": runs[True][1], "rel_residual": runs[True][2],
+                     "ms_per_iteration": 1e3 * runs[True][0] / max(1, runs[True][1])},
+           "time_ratio_mixed_over_fp64": runs[True][0] / best[0],
+           "mixed_vs_fp64_rel_err": float((sols[True] - sols[False]).abs().max() / sols[False].abs().max()),
            "config": {"mesh": "128^3 root, 16^3 blocks, central 1/8 refined once", "leaves": int(mesh.nblocks),
                       "leaves_per_level": {str(int(l)): int((locs[:, 0] == l).sum()) for l in np.unique(locs[:, 0])},
                       "nghost": GMGC_NG, "grids": mg.ngrids, "levels": [mg.lmin, mg.lmax],

@@ -36,6 +36,7 @@
 #include <map>
 #include <set>
 #include <stdexcept>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/parthenon_gb300.h"
@@ -60,6 +61,7 @@ namespace {
 struct MgXfer {
   int32_t child, parent;
   int32_t lo[3];
+  int32_t pnb[6];  // the parent's face neighbours when its grid reads them directly, else -1
   int32_t pad;
 };
 
@@ -112,19 +114,53 @@ __device__ __forceinline__ void for_interior(const int *__restrict__ list, int n
   }
 }
 
+// A cell and its six face neighbours. nb == null: the neighbours outside the block are
+// its ghosts, filled by the grid's exchange. Otherwise nb holds the block's six
+// face-neighbour slots (-x, +x, -y, +y, -z, +z): on a grid of one level (no coarse/fine
+// faces) a ghost cell is a copy of the neighbour's interior cell, which is read instead,
+// so those grids need no exchange before a stencil.
+template <class T>
+struct Faces {
+  T c, xm, xp, ym, yp, zm, zp;
+};
+template <class T>
+__device__ __forceinline__ Faces<T> faces(const T *__restrict__ u, const Dims &d, const int *__restrict__ nb, int b,
+                                          int k, int j, int i) {
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
+  const int64_t c = cell_of(d, b, k, j, i);
+  Faces<T> f;
+  f.c = u[c];
+  if (!nb) {
+    f.xm = u[c - 1];
+    f.xp = u[c + 1];
+    f.ym = u[c - sj];
+    f.yp = u[c + sj];
+    f.zm = u[c - sk];
+    f.zp = u[c + sk];
+    return f;
+  }
+  const int lo = d.ng, h0 = d.ng + d.nx[0] - 1, h1 = d.ng + d.nx[1] - 1, h2 = d.ng + d.nx[2] - 1;
+  f.xm = i > lo ? u[c - 1] : u[cell_of(d, nb[0], k, j, h0)];
+  f.xp = i < h0 ? u[c + 1] : u[cell_of(d, nb[1], k, j, lo)];
+  f.ym = j > lo ? u[c - sj] : u[cell_of(d, nb[2], k, h1, i)];
+  f.yp = j < h1 ? u[c + sj] : u[cell_of(d, nb[3], k, lo, i)];
+  f.zm = k > lo ? u[c - sk] : u[cell_of(d, nb[4], h2, j, i)];
+  f.zp = k < h2 ? u[c + sk] : u[cell_of(d, nb[5], lo, j, i)];
+  return f;
+}
+
 // Exact build, poisson_equation.hpp:104-210: face fluxes D grad u, then their
 // divergence, -alpha u + sum over directions of (F_left - F_right) / dx, in the
 // reference's order
-__device__ __forceinline__ double ax_exact(const double *__restrict__ u, int64_t c, int64_t sj, int64_t sk,
-                                          const double *dx, const MgOp &o) {
+__device__ __forceinline__ double ax_exact(const Faces<double> &f, const double *dx, const MgOp &o) {
   const double D = o.D, dx1 = dx[0], dx2 = dx[1], dx3 = dx[2];
-  const double uc = u[c];
-  const double f1l = div_rn(D, dx1) * (u[c - 1] - uc);
-  const double f1r = div_rn(D, dx1) * (uc - u[c + 1]);
-  const double f2l = div_rn(D * (u[c - sj] - uc), dx2);
-  const double f2r = div_rn(D * (uc - u[c + sj]), dx2);
-  const double f3l = div_rn(D * (u[c - sk] - uc), dx3);
-  const double f3r = div_rn(D * (uc - u[c + sk]), dx3);
+  const double uc = f.c;
+  const double f1l = div_rn(D, dx1) * (f.xm - uc);
+  const double f1r = div_rn(D, dx1) * (uc - f.xp);
+  const double f2l = div_rn(D * (f.ym - uc), dx2);
+  const double f2r = div_rn(D * (uc - f.yp), dx2);
+  const double f3l = div_rn(D * (f.zm - uc), dx3);
+  const double f3r = div_rn(D * (uc - f.zp), dx3);
   double out = -o.alpha * uc;
   out += div_rn(f1l - f1r, dx1);
   out += div_rn(f2l - f2r, dx2);
@@ -136,38 +172,39 @@ __device__ __forceinline__ double ax_exact(const double *__restrict__ u, int64_t
 // with off = sum_d (D/dx_d^2) (u_{-d} + u_{+d}): 3 adds, a multiply and 2 FMAs (the FP64
 // pipe, not HBM, bounds these kernels on GB300)
 template <class T>
-__device__ __forceinline__ T off_fast(const T *__restrict__ u, int64_t c, int64_t sj, int64_t sk, const MgCoef &cf) {
-  return fma_t((T)cf.c[2], u[c - sk] + u[c + sk], fma_t((T)cf.c[1], u[c - sj] + u[c + sj], (T)cf.c[0] * (u[c - 1] + u[c + 1])));
+__device__ __forceinline__ T off_fast(const Faces<T> &f, const MgCoef &cf) {
+  return fma_t((T)cf.c[2], f.zm + f.zp, fma_t((T)cf.c[1], f.ym + f.yp, (T)cf.c[0] * (f.xm + f.xp)));
 }
 
 // Jacobi sweep (mg_solver.hpp:222-297): dst = w ratio(rhs - (A src - dg src), dg) + (1 - w) src
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_jacobi(const T *__restrict__ src, const T *__restrict__ rhs,
                                                    T *__restrict__ dst, const int *__restrict__ list, int n,
-                                                   Dims d, MgCoef cf, MgOp o, MgSweep sw) {
-  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
-  for_interior(list, n, d, [&](int, int b, int k, int j, int i) {
+                                                   const int *__restrict__ nbr, Dims d, MgCoef cf, MgOp o,
+                                                   MgSweep sw) {
+  for_interior(list, n, d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(d, b, k, j, i);
+    const Faces<T> f = faces(src, d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
     if constexpr (kFast) {
-      dst[c] = fma_t((T)sw.wd, rhs[c] - off_fast(src, c, sj, sk, cf), (T)sw.omw * src[c]);
+      dst[c] = fma_t((T)sw.wd, rhs[c] - off_fast(f, cf), (T)sw.omw * f.c);
     } else {
-      const double a = ax_exact(src, c, sj, sk, cf.dx, o);
-      const double off = a - cf.dg * src[c];
+      const double a = ax_exact(f, cf.dx, o);
+      const double off = a - cf.dg * f.c;
       const double val = rhs[c] - off;
-      dst[c] = sw.w * div_rn(val, cf.den) + sw.omw * src[c];
+      dst[c] = sw.w * div_rn(val, cf.den) + sw.omw * f.c;
     }
   });
 }
 
 // Ax + AddFieldsAndStoreInteriorSelect<rhs, temp, res_err>(1, -1): res = rhs - A u
 template <bool kFast, class T>
-__global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *__restrict__ list, int n, MgCoef cf,
-                                                     MgOp o) {
-  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
-  for_interior(list, n, s.d, [&](int, int b, int k, int j, int i) {
+__global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *__restrict__ list, int n,
+                                                     const int *__restrict__ nbr, MgCoef cf, MgOp o) {
+  for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
-    if constexpr (kFast) s.res[c] = fma_t(-(T)cf.dg, s.u[c], s.rhs[c] - off_fast(s.u, c, sj, sk, cf));
-    else s.res[c] = s.rhs[c] - ax_exact(s.u, c, sj, sk, cf.dx, o);
+    const Faces<T> f = faces(s.u, s.d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
+    if constexpr (kFast) s.res[c] = fma_t(-(T)cf.dg, f.c, s.rhs[c] - off_fast(f, cf));
+    else s.res[c] = s.rhs[c] - ax_exact(f, cf.dx, o);
   });
 }
 
@@ -176,15 +213,15 @@ __global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *
 // rhs = A u + res_err
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_fas(StoreView<T> s, const int *__restrict__ list, int n, int nint,
-                                                MgCoef cf, MgOp o) {
-  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
+                                                const int *__restrict__ nbr, MgCoef cf, MgOp o) {
   for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     const T uc = s.u[c];
     s.u0[c] = uc;
     if (q >= nint) return;
-    if constexpr (kFast) s.rhs[c] = fma_t((T)cf.dg, uc, off_fast(s.u, c, sj, sk, cf) + s.res[c]);
-    else s.rhs[c] = ax_exact(s.u, c, sj, sk, cf.dx, o) + s.res[c];
+    const Faces<T> f = faces(s.u, s.d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
+    if constexpr (kFast) s.rhs[c] = fma_t((T)cf.dg, uc, off_fast(f, cf) + s.res[c]);
+    else s.rhs[c] = ax_exact(f, cf.dx, o) + s.res[c];
   });
 }
 
@@ -271,15 +308,25 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreV
     const MgXfer t = x[q];
     const int c[3] = {c0 + ng, c1 + ng, c2 + ng};  // coarse-buffer index
     const int f[3] = {2 * c0 + ng, 2 * c1 + ng, 2 * c2 + ng};
-    const int64_t pe = cell_of(ps.d, t.parent, t.lo[2] + c2, t.lo[1] + c1, t.lo[0] + c0);
+    const int p[3] = {t.lo[0] + c0, t.lo[1] + c1, t.lo[2] + c2};
+    const int64_t pe = cell_of(ps.d, t.parent, p[2], p[1], p[0]);
     const TC fc = (TC)ps.res[pe];
+    // the parent's cells next to p along d: its ghosts, or on a grid read directly the
+    // face neighbour's interior cell
+    auto side = [&](int d, int s) -> TC {
+      const int64_t st = d == 0 ? 1 : (d == 1 ? pj : pk);
+      const int lo = ps.d.ng, hi = ps.d.ng + ps.d.nx[d] - 1;
+      if (t.pnb[0] < 0 || (s < 0 ? p[d] > lo : p[d] < hi)) return (TC)ps.res[pe + s * st];
+      int q[3] = {p[0], p[1], p[2]};
+      q[d] = s < 0 ? hi : lo;
+      return (TC)ps.res[cell_of(ps.d, t.pnb[2 * d + (s > 0)], q[2], q[1], q[0])];
+    };
     TC mq[3], pq[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const int64_t st = d == 0 ? 1 : (d == 1 ? pj : pk);
       if constexpr (kFast) {
-        mq[d] = (TC)0.25 * (fc - (TC)ps.res[pe - st]);
-        pq[d] = (TC)0.25 * ((TC)ps.res[pe + st] - fc);
+        mq[d] = (TC)0.25 * (fc - side(d, -1));
+        pq[d] = (TC)0.25 * (side(d, 1) - fc);
       } else {
         const DevBlockGeom &g = cgeom[t.child];
         auto xcc = [&](int idx) { return g.cxmin[d] + ((double)idx + 0.5) * g.cdx[d]; };
@@ -288,8 +335,8 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreV
         const double dxm = xc - xm, dxp = xp - xc;
         const double dfm = xc - xfc(f[d]);
         const double dfp = xfc(f[d] + 1) - xc;
-        mq[d] = div_rn(fc - ps.res[pe - st], dxm) * dfm;
-        pq[d] = div_rn(ps.res[pe + st] - fc, dxp) * dfp;
+        mq[d] = div_rn(fc - side(d, -1), dxm) * dfm;
+        pq[d] = div_rn(side(d, 1) - fc, dxp) * dfp;
       }
     }
     const TC m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
@@ -316,15 +363,15 @@ __global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView<doub
                                                                   const MgCoef *__restrict__ lc, MgOp o,
                                                                   double *__restrict__ partial,
                                                                   float *__restrict__ rhs32, float *__restrict__ u32) {
-  __shared__ double sh[kResThreads];
-  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
+  __shared__ double sh[kResThreads / 32];
   double acc = 0.0;
   for_interior(nullptr, nleaf, s.d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     const MgCoef &cf = lc[b];
+    const Faces<double> f = faces<double>(s.u, s.d, nullptr, b, k, j, i);
     double r;
-    if constexpr (kFast) r = fma(-cf.dg, s.u[c], s.rhs[c] - off_fast(s.u, c, sj, sk, cf));
-    else r = s.rhs[c] - ax_exact(s.u, c, sj, sk, cf.dx, o);
+    if constexpr (kFast) r = fma(-cf.dg, f.c, s.rhs[c] - off_fast(f, cf));
+    else r = s.rhs[c] - ax_exact(f, cf.dx, o);
     s.res[c] = r;
     acc += r * r;
     if (rhs32) {
@@ -332,13 +379,15 @@ __global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView<doub
       u32[c] = 0.0f;
     }
   });
-  sh[threadIdx.x] = acc;
+  // warp-shuffle tree within each warp, then the warps' sums in order (fixed order)
+  for (int w = 16; w > 0; w >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, w);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
   __syncthreads();
-  for (int w = kResThreads / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kResThreads / 32; ++w) t += sh[w];
+    partial[blockIdx.x] = t;
   }
-  if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
 }
 
 // Iterative refinement: u += e on the leaf interiors (e the FP32 V-cycle's result)
@@ -388,8 +437,11 @@ struct pgb_mg {
     int nint = 0;               // internal blocks at the head of fine_h
     std::vector<MgXfer> xfer_h; // fine blocks and their parents (grids above the coarsest)
     MgCoef coef{};              // operator constants of the fine blocks
-    int *fine = nullptr, *coarse = nullptr;
+    bool halofree = false;      // one level: stencils read the face neighbours directly
+    std::vector<int> nbr_h;     // 6 face-neighbour slots per entry of fine_h (halofree)
+    int *fine = nullptr, *coarse = nullptr, *nbr = nullptr;
     MgXfer *xfer = nullptr;
+    const int *nb() const { return halofree ? nbr : nullptr; }
   };
   std::map<int, Grid> grids;
   GridTables leaf_tab;
@@ -500,7 +552,7 @@ int mg_build(pgb_mg *g) {
     remap_regions(src.restrict_send, G.remap.restrict_send);
     remap_regions(src.restrict_recv, G.remap.restrict_recv);
     remap_regions(src.prolong, G.remap.prolong);
-    std::vector<int> leaf_fine;
+    std::vector<int> fine_idx, leaf_idx;  // block indices, internal blocks first
     const BlockInfo *fb = nullptr;
     for (size_t i = 0; i < src.blocks.size(); ++i) {
       const BlockInfo &b = src.blocks[i];
@@ -511,12 +563,32 @@ int mg_build(pgb_mg *g) {
       if (fb && (b.dx[0] != fb->dx[0] || b.dx[1] != fb->dx[1] || b.dx[2] != fb->dx[2]))
         return fail(kErrUnsupported, "blocks of one level with different spacings");
       fb = &b;
-      if (topo.is_leaf(b.loc)) leaf_fine.push_back(slot[i]);
-      else G.fine_h.push_back(slot[i]);
+      (topo.is_leaf(b.loc) ? leaf_idx : fine_idx).push_back((int)i);
     }
-    G.nint = (int)G.fine_h.size();
-    G.fine_h.insert(G.fine_h.end(), leaf_fine.begin(), leaf_fine.end());
+    G.nint = (int)fine_idx.size();
+    fine_idx.insert(fine_idx.end(), leaf_idx.begin(), leaf_idx.end());
+    for (int i : fine_idx) G.fine_h.push_back(slot[i]);
     G.coef = make_coef(fb->dx, g->cfg);
+    // A grid without coarser leaves is one level tiling the periodic domain (2:1
+    // balance leaves no gap), so every face neighbour of a block is a block of the grid
+    G.halofree = G.coarse_h.empty();
+    if (G.halofree) {
+      std::unordered_map<int, int> pos;
+      for (size_t i = 0; i < src.blocks.size(); ++i) pos[src.blocks[i].gid] = (int)i;
+      const int64_t n = L >= 0 ? (int64_t)1 << L : 1;
+      for (int i : fine_idx) {
+        const LLoc &l = src.blocks[i].loc;
+        for (int d = 0; d < 3; ++d)
+          for (int sgn : {-1, 1}) {
+            std::array<int64_t, 3> x = l.lx;
+            x[d] = (x[d] + sgn + n) % n;
+            const int gid = topo.gid_of(LLoc(L, x[0], x[1], x[2]));
+            auto it = pos.find(gid);
+            if (gid < 0 || it == pos.end()) return fail(kErrInvalid, "face neighbour outside a one-level grid");
+            G.nbr_h.push_back(slot[it->second]);
+          }
+      }
+    }
   }
   for (auto &b : leaves) g->leaf_coef_h.push_back(make_coef(b.dx, g->cfg));
   // transfers between grid L and L - 1, per fine block of grid L
@@ -552,6 +624,14 @@ int mg_build(pgb_mg *g) {
       x.child = slot0.count(c.gid) && L >= 0 ? slot0.at(c.gid) : (int)i;
       x.parent = L - 1 >= 0 ? slot0.at(p.gid) : pi;
       for (int d = 0; d < 3; ++d) x.lo[d] = tr.lo[d];
+      const pgb_mg::Grid &PG = g->grids.at(L - 1);
+      for (int q = 0; q < 6; ++q) x.pnb[q] = -1;
+      if (PG.halofree) {
+        const auto it = std::find(PG.fine_h.begin(), PG.fine_h.end(), x.parent);
+        if (it == PG.fine_h.end()) return fail(kErrInvalid, "parent outside its grid's block list");
+        const size_t q0 = 6 * (size_t)(it - PG.fine_h.begin());
+        for (int q = 0; q < 6; ++q) x.pnb[q] = PG.nbr_h[q0 + q];
+      }
       x.pad = 0;
       G.xfer_h.push_back(x);
     }
@@ -606,7 +686,7 @@ int mg_upload(pgb_mg *g) {
     return off;
   };
   struct Off {
-    size_t fine, coarse, xfer;
+    size_t fine, coarse, xfer, nbr;
   };
   std::map<int, Off> off;
   for (auto &kv : g->grids) {
@@ -614,6 +694,7 @@ int mg_upload(pgb_mg *g) {
     o.fine = room(kv.second.fine_h.size() * sizeof(int));
     o.coarse = room(kv.second.coarse_h.size() * sizeof(int));
     o.xfer = room(kv.second.xfer_h.size() * sizeof(MgXfer));
+    o.nbr = room(kv.second.nbr_h.size() * sizeof(int));
     off[kv.first] = o;
   }
   const size_t lc_off = room(g->leaf_coef_h.size() * sizeof(MgCoef));
@@ -625,6 +706,7 @@ int mg_upload(pgb_mg *g) {
     std::memcpy(h.data() + o.fine, G.fine_h.data(), G.fine_h.size() * sizeof(int));
     std::memcpy(h.data() + o.coarse, G.coarse_h.data(), G.coarse_h.size() * sizeof(int));
     std::memcpy(h.data() + o.xfer, G.xfer_h.data(), G.xfer_h.size() * sizeof(MgXfer));
+    std::memcpy(h.data() + o.nbr, G.nbr_h.data(), G.nbr_h.size() * sizeof(int));
   }
   PGB_CUDA(cudaMalloc(&g->lists, h.size()));
   PGB_CUDA(cudaMemcpy(g->lists, h.data(), h.size(), cudaMemcpyHostToDevice));
@@ -634,6 +716,7 @@ int mg_upload(pgb_mg *g) {
     kv.second.fine = reinterpret_cast<int *>(base + o.fine);
     kv.second.coarse = reinterpret_cast<int *>(base + o.coarse);
     kv.second.xfer = reinterpret_cast<MgXfer *>(base + o.xfer);
+    kv.second.nbr = reinterpret_cast<int *>(base + o.nbr);
   }
   g->leaf_coef = reinterpret_cast<MgCoef *>(static_cast<char *>(g->lists) + lc_off);
   const Dims &d0 = g->stores.at(0).dims;
@@ -716,13 +799,14 @@ struct VCycle {
     if (stages >= 2 && nc) k_mg_copy<T><<<grid_for(nc * cl), 256, 0, s>>>(v.temp, v.u, G.coarse, nc, v.d);
     T *src = v.u, *dst = v.temp;
     for (int st = 0; st < stages; ++st) {
-      int rc = exch(g, L, src, s);
+      int rc = G.halofree ? kOk : exch(g, L, src, s);
       if (rc) return rc;
       MgSweep sw;
       sw.w = srj_weight(g->cfg, st);
       sw.omw = 1.0 - sw.w;
       sw.wd = sw.w / G.coef.den;
-      k_mg_jacobi<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(src, v.rhs, dst, G.fine, nf, v.d, G.coef, o, sw);
+      k_mg_jacobi<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(src, v.rhs, dst, G.fine, nf, G.nb(), v.d, G.coef, o,
+                                                              sw);
       std::swap(src, dst);
     }
     if (src != v.u) k_mg_copy<T><<<grid_for(nf * cl), 256, 0, s>>>(v.u, v.temp, G.fine, nf, v.d);
@@ -738,7 +822,8 @@ struct VCycle {
     const int nf = (int)G.fine_h.size();
     k_mg_error<T><<<grid_for(nf * cells(L)), 256, 0, s>>>(v, G.fine, nf);
     PGB_CUDA(cudaGetLastError());
-    return exch(g, L, v.res, s);
+    // a one-level grid's res_err ghosts are read from the neighbours by the prolongation
+    return G.halofree ? kOk : exch(g, L, v.res, s);
   }
 
   template <class T, class TP>
@@ -760,15 +845,15 @@ struct VCycle {
     int rc;
     if (L < g->lmax) {
       // FAS: exchange, u0 = u, rhs = A u + res_err on internal blocks
-      if ((rc = exch(g, L, v.u, s))) return rc;
-      k_mg_fas<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(v, G.fine, nf, G.nint, G.coef, o);
+      if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
+      k_mg_fas<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(v, G.fine, nf, G.nint, G.nb(), G.coef, o);
     } else {
       k_mg_copy<T><<<grid_for(nf * cl), 256, 0, s>>>(v.u0, v.u, G.fine, nf, v.d);
     }
     if ((rc = smooth<T>(L, g->cfg.stages))) return rc;
     if (L > g->lmin) {
-      if ((rc = exch(g, L, v.u, s))) return rc;
-      k_mg_residual<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(v, G.fine, nf, G.coef, o);
+      if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
+      k_mg_residual<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(v, G.fine, nf, G.nb(), G.coef, o);
       if constexpr (kFast) rc = dbl(L - 1) ? restrict_down<T, double>(L) : restrict_down<T, float>(L);
       else rc = restrict_down<T, double>(L);
       if (rc) return rc;
