@@ -91,6 +91,17 @@ struct StoreView {
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 
+// Programmatic dependent launch: the multigrid kernels are launched so that each may
+// start while its predecessor in the stream drains. Each first waits for the
+// predecessor's completion and memory (griddepcontrol.wait, before any access), then
+// lets its own successor launch (griddepcontrol.launch_dependents); this hides the
+// launch latency of the hundreds of small launches of a V-cycle. A plain launch makes
+// the wait a no-op.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ int64_t cell_of(const Dims &d, int slot, int k, int j, int i) {
   return ((int64_t)slot * d.N[2] + k) * ((int64_t)d.N[1] * d.N[0]) + (int64_t)j * d.N[0] + i;
 }
@@ -182,6 +193,7 @@ __global__ void __launch_bounds__(256) k_mg_jacobi(const T *__restrict__ src, co
                                                    T *__restrict__ dst, const int *__restrict__ list, int n,
                                                    const int *__restrict__ nbr, Dims d, MgCoef cf, MgOp o,
                                                    MgSweep sw) {
+  pdl_enter();
   for_interior(list, n, d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(d, b, k, j, i);
     const Faces<T> f = faces(src, d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
@@ -200,6 +212,7 @@ __global__ void __launch_bounds__(256) k_mg_jacobi(const T *__restrict__ src, co
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *__restrict__ list, int n,
                                                      const int *__restrict__ nbr, MgCoef cf, MgOp o) {
+  pdl_enter();
   for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     const Faces<T> f = faces(s.u, s.d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
@@ -214,6 +227,7 @@ __global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_fas(StoreView<T> s, const int *__restrict__ list, int n, int nint,
                                                 const int *__restrict__ nbr, MgCoef cf, MgOp o) {
+  pdl_enter();
   for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     const T uc = s.u[c];
@@ -229,6 +243,7 @@ __global__ void __launch_bounds__(256) k_mg_fas(StoreView<T> s, const int *__res
 template <class T>
 __global__ void __launch_bounds__(256) k_mg_copy(T *__restrict__ dst, const T *__restrict__ src,
                                                  const int *__restrict__ list, int n, Dims d) {
+  pdl_enter();
   for_interior(list, n, d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(d, b, k, j, i);
     dst[c] = src[c];
@@ -238,6 +253,7 @@ __global__ void __launch_bounds__(256) k_mg_copy(T *__restrict__ dst, const T *_
 // AddFieldsAndStore<u, u0, res_err>(1, -1): res = u - u0
 template <class T>
 __global__ void __launch_bounds__(256) k_mg_error(StoreView<T> s, const int *__restrict__ list, int n) {
+  pdl_enter();
   for_interior(list, n, s.d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     s.res[c] = s.u[c] - s.u0[c];
@@ -251,6 +267,7 @@ __global__ void __launch_bounds__(256) k_mg_error(StoreView<T> s, const int *__r
 template <class TC, class TP>
 __global__ void __launch_bounds__(256) k_mg_restrict(StoreView<TC> cs, StoreView<TP> ps, const MgXfer *__restrict__ x,
                                                      int n, const DevBlockGeom *__restrict__ cgeom) {
+  pdl_enter();
   const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
   const int per = h0 * h1 * h2, total = per * n;
   const int ng = cs.d.ng;
@@ -296,6 +313,7 @@ template <bool kFast, class TC, class TP>
 __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreView<TP> ps,
                                                         const MgXfer *__restrict__ x, int n,
                                                         const DevBlockGeom *__restrict__ cgeom) {
+  pdl_enter();
   const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
   const int per = h0 * h1 * h2, total = per * n;
   const int ng = cs.d.ng;
@@ -363,6 +381,7 @@ __global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView<doub
                                                                   const MgCoef *__restrict__ lc, MgOp o,
                                                                   double *__restrict__ partial,
                                                                   float *__restrict__ rhs32, float *__restrict__ u32) {
+  pdl_enter();
   __shared__ double sh[kResThreads / 32];
   double acc = 0.0;
   for_interior(nullptr, nleaf, s.d, [&](int, int b, int k, int j, int i) {
@@ -393,6 +412,7 @@ __global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView<doub
 // Iterative refinement: u += e on the leaf interiors (e the FP32 V-cycle's result)
 __global__ void __launch_bounds__(256) k_mg_correct(double *__restrict__ u, const float *__restrict__ e, int nleaf,
                                                     Dims d) {
+  pdl_enter();
   for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(d, b, k, j, i);
     u[c] = u[c] + (double)e[c];
@@ -757,6 +777,29 @@ double srj_weight(const GmgConfig &c, int s) {
   return c.stages == 1 ? m1[s] : (c.stages == 2 ? m2[s] : m3[s]);
 }
 
+// Launch with programmatic stream serialization (the kernel begins with pdl_enter).
+#define PGB_TRY(...)               \
+  do {                             \
+    const int rc__ = (__VA_ARGS__); \
+    if (rc__) return rc__;          \
+  } while (0)
+
+template <class... P, class... A>
+int launch_pdl(void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  PGB_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...));
+  return kOk;
+}
+
 // exchange_grid's prolongation op: ProlongateSharedLinear with the reference's
 // coordinate arithmetic (exact build) or in its uniform-spacing form (fast build)
 int prolong_op(const pgb_mg *g) { return g->exact ? 1 : 3; }
@@ -796,7 +839,7 @@ struct VCycle {
     // u into temp on every block first and each sweep's result back into u; the
     // exchange of the second sweep then runs on temp, whose coarser leaves must hold
     // their u.
-    if (stages >= 2 && nc) k_mg_copy<T><<<grid_for(nc * cl), 256, 0, s>>>(v.temp, v.u, G.coarse, nc, v.d);
+    if (stages >= 2 && nc) PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nc * cl), 256, s, v.temp, v.u, G.coarse, nc, v.d));
     T *src = v.u, *dst = v.temp;
     for (int st = 0; st < stages; ++st) {
       int rc = G.halofree ? kOk : exch(g, L, src, s);
@@ -805,11 +848,11 @@ struct VCycle {
       sw.w = srj_weight(g->cfg, st);
       sw.omw = 1.0 - sw.w;
       sw.wd = sw.w / G.coef.den;
-      k_mg_jacobi<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(src, v.rhs, dst, G.fine, nf, G.nb(), v.d, G.coef, o,
-                                                              sw);
+      PGB_TRY(launch_pdl(k_mg_jacobi<kFast, T>, grid_for(nf * cl), 256, s, src, v.rhs, dst, G.fine, nf, G.nb(), v.d, G.coef, o,
+                                                              sw));
       std::swap(src, dst);
     }
-    if (src != v.u) k_mg_copy<T><<<grid_for(nf * cl), 256, 0, s>>>(v.u, v.temp, G.fine, nf, v.d);
+    if (src != v.u) PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nf * cl), 256, s, v.u, v.temp, G.fine, nf, v.d));
     PGB_CUDA(cudaGetLastError());
     return kOk;
   }
@@ -820,7 +863,7 @@ struct VCycle {
     pgb_mg::Grid &G = g->grids.at(L);
     const StoreView<T> v = g->store_of(L).template view<T>();
     const int nf = (int)G.fine_h.size();
-    k_mg_error<T><<<grid_for(nf * cells(L)), 256, 0, s>>>(v, G.fine, nf);
+    PGB_TRY(launch_pdl(k_mg_error<T>, grid_for(nf * cells(L)), 256, s, v, G.fine, nf));
     PGB_CUDA(cudaGetLastError());
     // a one-level grid's res_err ghosts are read from the neighbours by the prolongation
     return G.halofree ? kOk : exch(g, L, v.res, s);
@@ -830,8 +873,8 @@ struct VCycle {
   int restrict_down(int L) {
     pgb_mg::Grid &G = g->grids.at(L);
     const int nx = (int)G.xfer_h.size();
-    k_mg_restrict<T, TP><<<grid_for(nx * cells(L) / 8), 256, 0, s>>>(
-        g->store_of(L).template view<T>(), g->store_of(L - 1).template view<TP>(), G.xfer, nx, G.tab.geom);
+    PGB_TRY(launch_pdl(k_mg_restrict<T, TP>, grid_for(nx * cells(L) / 8), 256, s, 
+        g->store_of(L).template view<T>(), g->store_of(L - 1).template view<TP>(), G.xfer, nx, G.tab.geom));
     PGB_CUDA(cudaGetLastError());
     return kOk;
   }
@@ -846,21 +889,21 @@ struct VCycle {
     if (L < g->lmax) {
       // FAS: exchange, u0 = u, rhs = A u + res_err on internal blocks
       if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
-      k_mg_fas<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(v, G.fine, nf, G.nint, G.nb(), G.coef, o);
+      PGB_TRY(launch_pdl(k_mg_fas<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nint, G.nb(), G.coef, o));
     } else {
-      k_mg_copy<T><<<grid_for(nf * cl), 256, 0, s>>>(v.u0, v.u, G.fine, nf, v.d);
+      PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nf * cl), 256, s, v.u0, v.u, G.fine, nf, v.d));
     }
     if ((rc = smooth<T>(L, g->cfg.stages))) return rc;
     if (L > g->lmin) {
       if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
-      k_mg_residual<kFast, T><<<grid_for(nf * cl), 256, 0, s>>>(v, G.fine, nf, G.nb(), G.coef, o);
+      PGB_TRY(launch_pdl(k_mg_residual<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nb(), G.coef, o));
       if constexpr (kFast) rc = dbl(L - 1) ? restrict_down<T, double>(L) : restrict_down<T, float>(L);
       else rc = restrict_down<T, double>(L);
       if (rc) return rc;
     } else {
       for (int c = 0; c < g->cfg.coarse_sweeps; ++c)
         if ((rc = smooth<T>(L, g->cfg.stages))) return rc;
-      k_mg_copy<T><<<grid_for(nf * cl), 256, 0, s>>>(v.res, v.u, G.fine, nf, v.d);
+      PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nf * cl), 256, s, v.res, v.u, G.fine, nf, v.d));
       if (L < g->lmax && (rc = error_out<T>(L))) return rc;
     }
     PGB_CUDA(cudaGetLastError());
@@ -871,8 +914,8 @@ struct VCycle {
   int prolong_add(int L) {
     pgb_mg::Grid &G = g->grids.at(L);
     const int nx = (int)G.xfer_h.size();
-    k_mg_prolong_add<kFast, T, TP><<<grid_for(nx * cells(L) / 8), 256, 0, s>>>(
-        g->store_of(L).template view<T>(), g->store_of(L - 1).template view<TP>(), G.xfer, nx, G.tab.geom);
+    PGB_TRY(launch_pdl(k_mg_prolong_add<kFast, T, TP>, grid_for(nx * cells(L) / 8), 256, s, 
+        g->store_of(L).template view<T>(), g->store_of(L - 1).template view<TP>(), G.xfer, nx, G.tab.geom));
     PGB_CUDA(cudaGetLastError());
     return kOk;
   }
@@ -912,9 +955,9 @@ int leaf_residual_t(pgb_mg *g, bool mixed, cudaStream_t s) {
   pgb_mg::Store &S = g->stores.at(0);
   int rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr);
   if (rc) return rc;
-  k_mg_leaf_residual<kFast><<<g->nparts, kResThreads, 0, s>>>(S.template view<double>(), g->nleaf, g->leaf_coef,
+  PGB_TRY(launch_pdl(k_mg_leaf_residual<kFast>, g->nparts, kResThreads, s, S.template view<double>(), g->nleaf, g->leaf_coef,
                                                               MgOp{g->cfg.D, g->cfg.alpha}, g->partial,
-                                                              mixed ? S.rhs32 : nullptr, mixed ? S.u32 : nullptr);
+                                                              mixed ? S.rhs32 : nullptr, mixed ? S.u32 : nullptr));
   PGB_CUDA(cudaGetLastError());
   PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
   return kOk;
@@ -933,7 +976,7 @@ int enqueue_iteration_t(pgb_mg *g, bool mixed, cudaStream_t s) {
   if (rc) return rc;
   if (mixed) {
     pgb_mg::Store &S = g->stores.at(0);
-    k_mg_correct<<<grid_for((int64_t)g->nleaf * vc.cells(g->lmax)), 256, 0, s>>>(S.u, S.u32, g->nleaf, S.dims);
+    PGB_TRY(launch_pdl(k_mg_correct, grid_for((int64_t)g->nleaf * vc.cells(g->lmax)), 256, s, S.u, S.u32, g->nleaf, S.dims));
     PGB_CUDA(cudaGetLastError());
   }
   return leaf_residual_t<kFast>(g, mixed, s);
