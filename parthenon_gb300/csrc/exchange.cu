@@ -622,16 +622,12 @@ __global__ void __launch_bounds__(256) k_flux_correct(const DevFluxCorr *__restr
 // FP32 exchange of one component on the same tables, for the multigrid's FP32 V-cycle:
 // direct copies, restriction as the mean of the 2x2x2 fine cells and linear
 // prolongation in its uniform-spacing form (the grids of one mesh have uniform spacing).
-// one warp per work item (the boxes of 16^3 blocks with 2 ghosts hold tens to hundreds
-// of values, so a CTA per box leaves most threads idle)
-__global__ void __launch_bounds__(256) k_copy_f32(const DevPair *__restrict__ pairs,
-                                                  const DevWork *__restrict__ work, int nwork, Dims d,
+__global__ void __launch_bounds__(128) k_copy_f32(const DevPair *__restrict__ pairs,
+                                                  const DevWork *__restrict__ work, Dims d,
                                                   float *__restrict__ fine, float *__restrict__ coarse) {
-  const int wi = warp_item();
-  if (wi >= nwork) return;
-  const DevWork w = work[wi];
+  const DevWork w = work[blockIdx.x];
   const DevPair p = pairs[w.item];
-  for_item_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
+  for_work_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], [&](int k, int j, int i) {
     const int dk = p.dst.lo[2] + k, dj = p.dst.lo[1] + j, di = p.dst.lo[0] + i;
     if (!p.full_mask && !mask_active(p.mask, p.dst, dk, dj, di)) return;
     const int sk = p.src.lo[2] + k, sj = p.src.lo[1] + j, si = p.src.lo[0] + i;
@@ -740,9 +736,7 @@ int exchange_grid_f32(GridTables &t, float *fine, float *coarse, cudaStream_t s)
   if (t.multilevel && t.nrs_work)
     k_restrict_f32<<<warp_item_grid(t.nrs_work), 32 * kItemWarps, 0, s>>>(t.rs, t.rs_work, t.nrs_work, t.dims,
                                                                         fine, coarse);
-  if (t.ncopy_work)
-    k_copy_f32<<<warp_item_grid(t.ncopy_work), 32 * kItemWarps, 0, s>>>(t.pairs, t.copy_work, t.ncopy_work, t.dims,
-                                                                      fine, coarse);
+  if (t.ncopy_work) k_copy_f32<<<t.ncopy_work, 128, 0, s>>>(t.pairs, t.copy_work, t.dims, fine, coarse);
   if (t.multilevel && t.nrr_work)
     k_restrict_f32<<<warp_item_grid(t.nrr_work), 32 * kItemWarps, 0, s>>>(t.rr, t.rr_work, t.nrr_work, t.dims,
                                                                         fine, coarse);
