@@ -282,6 +282,15 @@ int pgb_mg_vcycles(pgb_mg *mg, double *u, const double *rhs, int32_t ncycles, do
  * A e = r from e = 0 with r the FP64 leaf residual, then u += e. */
 int pgb_mg_solve(pgb_mg *mg, double *u, const double *rhs, double tol, int32_t relative, int32_t mixed,
                  int32_t max_cycles, int32_t *cycles_out, double *rms_out, void *stream);
+/* Right-preconditioned BiCGSTAB on the leaf grid from u = 0 (the result, with exchanged
+ * ghosts, is written to u): precondition 0: none; 1: one FP64 V-cycle on the composite
+ * grids from zero per application; 2: one FP32 V-cycle (the coarsest grid in FP64 below
+ * level 0). Stops when sqrt((r,r)/N) < rtol (relative = 0) or < rtol * sqrt((rhs,rhs)/N)
+ * (relative = 1), or after max_iters; one CUDA-graph launch per iteration, the host
+ * reads one double. Replaces BiCGSTABSolver::AddTasks (src/solvers/bicgstab_solver.hpp:
+ * 116-315) with MGSolver on the composite grids as its preconditioner. */
+int pgb_mg_bicgstab(pgb_mg *mg, double *u, const double *rhs, int32_t precondition, double rtol, int32_t relative,
+                    int32_t max_iters, int32_t *iters_out, double *rms_out, void *stream);
 
 /* ---- launch-shape autotuner ------------------------------------------------------ */
 

@@ -14,6 +14,7 @@
 //   src/bvals/comms/bnd_info.cpp:308-385     Get{Send,Set}BndInfo, GetInterior{Restrict,Prolongate}
 //   example/poisson_gmg/poisson_equation.hpp:41-210  Ax (flux correction off on composite grids)
 //   example/poisson_gmg/poisson_package.cpp:112-128  u and res_err: ProlongateSharedLinear
+//   src/solvers/bicgstab_solver.hpp:116-315  BiCGSTAB with the V-cycle as preconditioner
 //
 // Grid L holds every block of level L (leaves and internal blocks) and the leaves of
 // level L - 1. Its active ("fine") blocks are those of level L; the coarser leaves
@@ -351,6 +352,78 @@ struct BlockGmg {
     double n = 0.0;
     for (auto &b : m.blocks) n += (double)b.nx[0] * b.nx[1] * b.nx[2];
     return n;
+  }
+
+  // ---- BiCGSTAB on the leaf grid with one composite V-cycle as preconditioner
+  // (bicgstab_solver.hpp:116-315). Vectors hold the leaf interiors in block, k, j, i
+  // order; the dot products are compensated sums (the accurate values).
+  template <class F>
+  void leaf_cells(F fn) {
+    Store &S = store.at(0);
+    bind(S, &leaf_slot);
+    int64_t q = 0;
+    for (int b = 0; b < nleaf; ++b) interior(m.blocks[b], [&](int k, int j, int i) { fn(q++, b, k, j, i); });
+  }
+  // v <- A u: u into the leaf blocks, exchange (BoundaryType::any), Ax
+  void apply(const std::vector<double> &u, std::vector<double> &v) {
+    Store &S = store.at(0);
+    leaf_cells([&](int64_t q, int b, int k, int j, int i) { S.u.at(b, 0, k, j, i) = u[q]; });
+    exchange(S.u, m.blocks, BAny, 0, leaf_recs, true, PLinear, m.multilevel);
+    v.resize(u.size());
+    leaf_cells([&](int64_t q, int b, int k, int j, int i) { v[q] = ax(S.u, b, m.blocks[b], k, j, i); });
+  }
+  // out <- M b: rhs <- b, u <- 0 on the leaves, one V-cycle (bicgstab_solver.hpp:175-184)
+  void precondition(const std::vector<double> &bv, std::vector<double> &out) {
+    Store &S = store.at(0);
+    leaf_cells([&](int64_t q, int b, int k, int j, int i) {
+      S.rhs.at(b, 0, k, j, i) = bv[q];
+      S.u.at(b, 0, k, j, i) = 0.0;
+    });
+    vcycle();
+    out.resize(bv.size());
+    leaf_cells([&](int64_t q, int b, int k, int j, int i) { out[q] = S.u.at(b, 0, k, j, i); });
+  }
+  int bicgstab(const std::vector<double> &rhs, std::vector<double> &x, bool precondition_on, double rtol,
+               bool relative, int max_iters, double &rms_out) {
+    const size_t n = rhs.size();
+    const double N = ncells();
+    std::vector<double> r = rhs, p = rhs, rhat0 = rhs, v(n), h(n), s(n), t(n), u(n);
+    x.assign(n, 0.0);
+    double rhat0r = Gmg::dot(rhat0, r);
+    const double tol = relative ? rtol * std::sqrt(Gmg::dot(rhs, rhs) / N) : rtol;
+    int it = 0;
+    rms_out = 0.0;
+    for (it = 0; it < max_iters; ++it) {
+      const double rhat0r_old = rhat0r;
+      if (precondition_on) precondition(p, u);
+      else u = p;
+      apply(u, v);
+      const double rhat0v = Gmg::dot(rhat0, v);
+      const double alpha = rhat0r_old / rhat0v;
+      for (size_t q = 0; q < n; ++q) {
+        h[q] = 1.0 * x[q] + alpha * u[q];
+        s[q] = 1.0 * r[q] + -alpha * v[q];
+      }
+      if (precondition_on) precondition(s, u);
+      else u = s;
+      apply(u, t);
+      const double ts = Gmg::dot(t, s), tt = Gmg::dot(t, t);
+      const double omega = ts / tt;
+      for (size_t q = 0; q < n; ++q) {
+        x[q] = 1.0 * h[q] + omega * u[q];
+        r[q] = 1.0 * s[q] + -omega * t[q];
+      }
+      const double res = Gmg::dot(r, r);
+      rhat0r = Gmg::dot(rhat0, r);
+      const double beta = rhat0r / rhat0r_old * alpha / omega;
+      for (size_t q = 0; q < n; ++q) {
+        p[q] = 1.0 * p[q] + -omega * v[q];
+        p[q] = 1.0 * r[q] + beta * p[q];
+      }
+      rms_out = std::sqrt(res / N);
+      if (rms_out < tol) return it + 1;
+    }
+    return it;
   }
 };
 

@@ -1484,6 +1484,24 @@ double orc_mgb_residual(void *h) {
   BlockGmg *g = (BlockGmg *)h;
   return std::sqrt(g->residual() / g->ncells());
 }
+// BiCGSTAB on the leaf grid (rhs and x in the leaf layout [nleaf][N3][N2][N1], x
+// receives the interior solution); returns the iterations, *rms the final rms residual
+int orc_mgb_bicgstab(void *h, const double *rhs, double *x, int precondition, double rtol, int relative,
+                     int max_iters, double *rms) {
+  BlockGmg *g = (BlockGmg *)h;
+  Field &F = g->store.at(0).rhs;
+  const int64_t bs = F.bstride();
+  std::vector<double> b, sol;
+  g->leaf_cells([&](int64_t, int blk, int k, int j, int i) {
+    b.push_back(rhs[blk * bs + ((int64_t)k * F.N[1] + j) * F.N[0] + i]);
+  });
+  double r = 0.0;
+  const int it = g->bicgstab(b, sol, precondition != 0, rtol, relative != 0, max_iters, r);
+  g->leaf_cells([&](int64_t q, int blk, int k, int j, int i) { x[blk * bs + ((int64_t)k * F.N[1] + j) * F.N[0] + i] = sol[q]; });
+  if (rms) *rms = r;
+  return it;
+}
+
 // gmg_same boundary records of composite grid `level` (the orc_boundaries format)
 int orc_mgb_num_boundaries(void *h, int level) {
   BlockGmg *g = (BlockGmg *)h;

@@ -419,6 +419,201 @@ __global__ void __launch_bounds__(256) k_mg_correct(double *__restrict__ u, cons
   });
 }
 
+// ---- BiCGSTAB on the leaf grid (bicgstab_solver.hpp:116-315). Vectors live in the leaf
+// layout; every kernel touches the leaf interiors only. Scalars stay on the device:
+// ks[0] (rhat0, r), ks[1] its previous value, ks[2] (rhat0, v), ks[3] (t, s), ks[4] (t, t),
+// ks[5] (r, r), ks[6] (rhs, rhs).
+enum { kRr = 0, kRrOld, kRv, kTs, kTt, kRes, kRhs2, kNumScalars };
+
+// partial sums of a.b (and c.e when c is not null) per CTA, in a fixed order
+__global__ void __launch_bounds__(kResThreads) k_bi_dot2(const double *__restrict__ a, const double *__restrict__ b,
+                                                         const double *__restrict__ c, const double *__restrict__ e,
+                                                         int nleaf, Dims d, double *__restrict__ part) {
+  pdl_enter();
+  __shared__ double sh[2][kResThreads / 32];
+  double s0 = 0.0, s1 = 0.0;
+  for_interior(nullptr, nleaf, d, [&](int, int blk, int k, int j, int i) {
+    const int64_t q = cell_of(d, blk, k, j, i);
+    s0 = fma(a[q], b[q], s0);
+    if (c) s1 = fma(c[q], e[q], s1);
+  });
+  for (int w = 16; w > 0; w >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, w);
+    s1 += __shfl_down_sync(0xffffffffu, s1, w);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = s0;
+    sh[1][threadIdx.x >> 5] = s1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int w = 0; w < kResThreads / 32; ++w) {
+      t0 += sh[0][w];
+      t1 += sh[1][w];
+    }
+    part[blockIdx.x] = t0;
+    part[gridDim.x + blockIdx.x] = t1;
+  }
+}
+
+// the partial sums of k_bi_dot2 (np per dot) into ks[i0] and ks[i1] (i1 < 0: one dot);
+// one CTA, fixed order
+__global__ void __launch_bounds__(256) k_bi_final(const double *__restrict__ part, int np, double *__restrict__ ks,
+                                                  int i0, int i1) {
+  pdl_enter();
+  __shared__ double sh[2][8];
+  double s0 = 0.0, s1 = 0.0;
+  for (int q = threadIdx.x; q < np; q += blockDim.x) {
+    s0 += part[q];
+    s1 += part[np + q];
+  }
+  for (int w = 16; w > 0; w >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, w);
+    s1 += __shfl_down_sync(0xffffffffu, s1, w);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = s0;
+    sh[1][threadIdx.x >> 5] = s1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t0 += sh[0][w];
+      t1 += sh[1][w];
+    }
+    ks[i0] = t0;
+    if (i1 >= 0) ks[i1] = t1;
+  }
+}
+
+// x = 0; r = rhat0 = p = rhs
+__global__ void __launch_bounds__(256) k_bi_init(const double *__restrict__ rhs, double *__restrict__ x,
+                                                 double *__restrict__ r, double *__restrict__ rhat0,
+                                                 double *__restrict__ p, int nleaf, Dims d) {
+  pdl_enter();
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t q = cell_of(d, b, k, j, i);
+    const double v = rhs[q];
+    x[q] = 0.0;
+    r[q] = v;
+    rhat0[q] = v;
+    p[q] = v;
+  });
+}
+
+__global__ void k_bi_begin(double *__restrict__ ks) {
+  pdl_enter();
+  ks[kRrOld] = ks[kRr];
+}
+
+// the preconditioner's input: rhs <- src and u <- 0 on the leaves (FP64 or FP32 copies),
+// or, without a preconditioner, u <- src
+template <class T>
+__global__ void __launch_bounds__(256) k_bi_in(const double *__restrict__ src, T *__restrict__ rhs,
+                                               T *__restrict__ u, int nleaf, Dims d) {
+  pdl_enter();
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t q = cell_of(d, b, k, j, i);
+    if (rhs) {
+      rhs[q] = (T)src[q];
+      u[q] = (T)0;
+    } else {
+      u[q] = (T)src[q];
+    }
+  });
+}
+
+// the FP32 preconditioner's output into the FP64 u
+__global__ void __launch_bounds__(256) k_bi_out32(const float *__restrict__ e, double *__restrict__ u, int nleaf,
+                                                  Dims d) {
+  pdl_enter();
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t q = cell_of(d, b, k, j, i);
+    u[q] = (double)e[q];
+  });
+}
+
+// out = A u on the leaves (u's ghosts exchanged before)
+__global__ void __launch_bounds__(256) k_bi_apply(const double *__restrict__ u, double *__restrict__ out, int nleaf,
+                                                  Dims d, const MgCoef *__restrict__ lc) {
+  pdl_enter();
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t q = cell_of(d, b, k, j, i);
+    const MgCoef &cf = lc[b];
+    const Faces<double> f = faces<double>(u, d, nullptr, b, k, j, i);
+    out[q] = fma(cf.dg, f.c, off_fast(f, cf));
+  });
+}
+
+// alpha = (rhat0, r)_old / (rhat0, v); h = x + alpha u; s = r - alpha v
+__global__ void __launch_bounds__(256) k_bi_hs(const double *__restrict__ x, const double *__restrict__ u,
+                                               const double *__restrict__ r, const double *__restrict__ v,
+                                               double *__restrict__ h, double *__restrict__ s,
+                                               const double *__restrict__ ks, int nleaf, Dims d) {
+  pdl_enter();
+  const double alpha = ks[kRrOld] / ks[kRv];
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t q = cell_of(d, b, k, j, i);
+    h[q] = fma(alpha, u[q], x[q]);
+    s[q] = fma(-alpha, v[q], r[q]);
+  });
+}
+
+// omega = (t, s) / (t, t); x = h + omega u; r = s - omega t; partial sums of (r, r) and
+// (rhat0, r)
+__global__ void __launch_bounds__(kResThreads) k_bi_xr(const double *__restrict__ h, const double *__restrict__ u,
+                                                       const double *__restrict__ s, const double *__restrict__ t,
+                                                       const double *__restrict__ rhat0, double *__restrict__ x,
+                                                       double *__restrict__ r, const double *__restrict__ ks,
+                                                       int nleaf, Dims d, double *__restrict__ part) {
+  pdl_enter();
+  __shared__ double sh[2][kResThreads / 32];
+  const double omega = ks[kTs] / ks[kTt];
+  double s0 = 0.0, s1 = 0.0;
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t q = cell_of(d, b, k, j, i);
+    x[q] = fma(omega, u[q], h[q]);
+    const double rq = fma(-omega, t[q], s[q]);
+    r[q] = rq;
+    s0 = fma(rq, rq, s0);
+    s1 = fma(rhat0[q], rq, s1);
+  });
+  for (int w = 16; w > 0; w >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, w);
+    s1 += __shfl_down_sync(0xffffffffu, s1, w);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = s0;
+    sh[1][threadIdx.x >> 5] = s1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t0 = 0.0, t1 = 0.0;
+    for (int w = 0; w < kResThreads / 32; ++w) {
+      t0 += sh[0][w];
+      t1 += sh[1][w];
+    }
+    part[blockIdx.x] = t0;
+    part[gridDim.x + blockIdx.x] = t1;
+  }
+}
+
+// beta = (rhat0, r) / (rhat0, r)_old * alpha / omega; p = r + beta (p - omega v)
+__global__ void __launch_bounds__(256) k_bi_p(const double *__restrict__ r, const double *__restrict__ v,
+                                              double *__restrict__ p, const double *__restrict__ ks, int nleaf,
+                                              Dims d) {
+  pdl_enter();
+  const double alpha = ks[kRrOld] / ks[kRv];
+  const double omega = ks[kTs] / ks[kTt];
+  const double beta = ks[kRr] / ks[kRrOld] * alpha / omega;
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t q = cell_of(d, b, k, j, i);
+    p[q] = fma(beta, fma(-omega, v[q], p[q]), r[q]);
+  });
+}
+
 unsigned grid_for(int64_t work) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 16));
 }
@@ -470,6 +665,11 @@ struct pgb_mg {
   void *lists = nullptr;
   double *partial = nullptr, *partial_h = nullptr;
   int nparts = 0;
+  // BiCGSTAB (allocated on first use): leaf-layout vectors x r rhat0 p v h s t, device
+  // scalars, dot-product partials, pinned copies of (r, r) and (rhs, rhs)
+  double *kv[8] = {};
+  double *ks = nullptr, *kpart = nullptr, *kres_h = nullptr;
+  cudaGraphExec_t kgraph[3] = {nullptr, nullptr, nullptr};  // per preconditioner
   bool uploaded = false, uploaded32 = false;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // FP64 and mixed iterations
   std::vector<void *> allocs;
@@ -480,6 +680,9 @@ struct pgb_mg {
   ~pgb_mg() {
     for (auto &gr : graph)
       if (gr) cudaGraphExecDestroy(gr);
+    for (auto &gr : kgraph)
+      if (gr) cudaGraphExecDestroy(gr);
+    if (kres_h) cudaFreeHost(kres_h);
     for (auto &kv : grids) kv.second.tab.release();
     leaf_tab.release();
     for (void *p : allocs) cudaFree(p);
@@ -987,6 +1190,106 @@ int enqueue_iteration(pgb_mg *g, bool mixed, cudaStream_t s) {
   return g->exact ? enqueue_iteration_t<false>(g, false, s) : enqueue_iteration_t<true>(g, false, s);
 }
 
+// ---- BiCGSTAB with the composite V-cycle as preconditioner
+enum { kX = 0, kR, kRhat0, kP, kV, kH, kS, kT, kNumVectors };
+
+int bicg_alloc(pgb_mg *g) {
+  if (g->kv[0]) return kOk;
+  const Dims &d = g->stores.at(0).dims;
+  const int64_t n = (int64_t)g->nleaf * d.N[0] * d.N[1] * d.N[2];
+  for (int q = 0; q < kNumVectors; ++q) {
+    PGB_CUDA(cudaMalloc((void **)&g->kv[q], n * sizeof(double)));
+    PGB_CUDA(cudaMemset(g->kv[q], 0, n * sizeof(double)));
+    g->allocs.push_back(g->kv[q]);
+  }
+  PGB_CUDA(cudaMalloc((void **)&g->ks, kNumScalars * sizeof(double)));
+  PGB_CUDA(cudaMemset(g->ks, 0, kNumScalars * sizeof(double)));
+  g->allocs.push_back(g->ks);
+  PGB_CUDA(cudaMalloc((void **)&g->kpart, 2 * (size_t)g->nparts * sizeof(double)));
+  g->allocs.push_back(g->kpart);
+  PGB_CUDA(cudaMallocHost((void **)&g->kres_h, 2 * sizeof(double)));
+  return kOk;
+}
+
+// u <- M src with u the leaves of store 0: mode 1 one FP64 V-cycle from u = 0, mode 2 one
+// FP32 V-cycle (FP64 coarsest grid below level 0), mode 0 no preconditioner (u <- src)
+int bicg_precond(pgb_mg *g, int mode, const double *src, cudaStream_t s) {
+  pgb_mg::Store &S = g->stores.at(0);
+  const unsigned grid = grid_for((int64_t)g->nleaf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]);
+  if (mode == 0) return launch_pdl(k_bi_in<double>, grid, 256, s, src, (double *)nullptr, S.u, g->nleaf, S.dims);
+  if (mode == 1) {
+    PGB_TRY(launch_pdl(k_bi_in<double>, grid, 256, s, src, S.rhs, S.u, g->nleaf, S.dims));
+    VCycle<true> vc{g, s, false, MgOp{g->cfg.D, g->cfg.alpha}};
+    return vc.run();
+  }
+  PGB_TRY(launch_pdl(k_bi_in<float>, grid, 256, s, src, S.rhs32, S.u32, g->nleaf, S.dims));
+  VCycle<true> vc{g, s, true, MgOp{g->cfg.D, g->cfg.alpha}};
+  PGB_TRY(vc.run());
+  return launch_pdl(k_bi_out32, grid, 256, s, (const float *)S.u32, S.u, g->nleaf, S.dims);
+}
+
+// out <- A u on the leaf grid (exchange, then the operator)
+int bicg_apply(pgb_mg *g, double *out, cudaStream_t s) {
+  pgb_mg::Store &S = g->stores.at(0);
+  PGB_TRY(exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr));
+  const unsigned grid = grid_for((int64_t)g->nleaf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]);
+  return launch_pdl(k_bi_apply, grid, 256, s, (const double *)S.u, out, g->nleaf, S.dims,
+                    (const MgCoef *)g->leaf_coef);
+}
+
+int bicg_dots(pgb_mg *g, const double *a, const double *b, const double *c, const double *e, int i0, int i1,
+              cudaStream_t s) {
+  const Dims &d = g->stores.at(0).dims;
+  PGB_TRY(launch_pdl(k_bi_dot2, g->nparts, kResThreads, s, a, b, c, e, g->nleaf, d, g->kpart));
+  return launch_pdl(k_bi_final, 1u, 256u, s, (const double *)g->kpart, g->nparts, g->ks, i0, i1);
+}
+
+// One BiCGSTAB iteration (bicgstab_solver.hpp:170-306); the host reads (r, r) after it.
+int bicg_iteration(pgb_mg *g, int mode, cudaStream_t s) {
+  pgb_mg::Store &S = g->stores.at(0);
+  double *const *v = g->kv;
+  const Dims &d = S.dims;
+  const unsigned grid = grid_for((int64_t)g->nleaf * d.nx[0] * d.nx[1] * d.nx[2]);
+  PGB_TRY(launch_pdl(k_bi_begin, 1u, 1u, s, g->ks));
+  PGB_TRY(bicg_precond(g, mode, v[kP], s));                                      // 1. u <- M p
+  PGB_TRY(bicg_apply(g, v[kV], s));                                              // 2. v <- A u
+  PGB_TRY(bicg_dots(g, v[kRhat0], v[kV], nullptr, nullptr, kRv, -1, s));         // 3. (rhat0, v)
+  PGB_TRY(launch_pdl(k_bi_hs, grid, 256, s, (const double *)v[kX], (const double *)S.u, (const double *)v[kR],
+                     (const double *)v[kV], v[kH], v[kS], (const double *)g->ks, g->nleaf, d));  // 4, 5
+  PGB_TRY(bicg_precond(g, mode, v[kS], s));                                      // 6. u <- M s
+  PGB_TRY(bicg_apply(g, v[kT], s));                                              // 7. t <- A u
+  PGB_TRY(bicg_dots(g, v[kT], v[kS], v[kT], v[kT], kTs, kTt, s));                // 8. (t, s), (t, t)
+  PGB_TRY(launch_pdl(k_bi_xr, g->nparts, kResThreads, s, (const double *)v[kH], (const double *)S.u,
+                     (const double *)v[kS], (const double *)v[kT], (const double *)v[kRhat0], v[kX], v[kR],
+                     (const double *)g->ks, g->nleaf, d, g->kpart));            // 9, 10
+  PGB_TRY(launch_pdl(k_bi_final, 1u, 256u, s, (const double *)g->kpart, g->nparts, g->ks, (int)kRes,
+                     (int)kRr));                                                 // (r, r), 11. (rhat0, r)
+  PGB_TRY(launch_pdl(k_bi_p, grid, 256, s, (const double *)v[kR], (const double *)v[kV], v[kP],
+                     (const double *)g->ks, g->nleaf, d));                       // 12, 13
+  PGB_CUDA(cudaMemcpyAsync(g->kres_h, g->ks + kRes, sizeof(double), cudaMemcpyDeviceToHost, s));
+  return kOk;
+}
+
+int run_bicg_iteration(pgb_mg *g, int mode, cudaStream_t s) {
+  cudaGraphExec_t &graph = g->kgraph[mode];
+  if (!graph) {
+    cudaGraph_t gr;
+    PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = bicg_iteration(g, mode, s);
+    cudaError_t e = cudaStreamEndCapture(s, &gr);
+    if (rc) {
+      if (e == cudaSuccess) cudaGraphDestroy(gr);
+      return rc;
+    }
+    PGB_CUDA(e);
+    e = cudaGraphInstantiate(&graph, gr, 0);
+    cudaGraphDestroy(gr);
+    PGB_CUDA(e);
+  }
+  PGB_CUDA(cudaGraphLaunch(graph, s));
+  return kOk;
+}
+
 double host_rms(pgb_mg *g) {
   double sum = 0.0;
   for (int i = 0; i < g->nparts; ++i) sum += g->partial_h[i];
@@ -1161,6 +1464,48 @@ int pgb_mg_solve(pgb_mg *g, double *u, const double *rhs, double tol, int32_t re
   PGB_CUDA(cudaStreamSynchronize(s));
   if (cycles_out) *cycles_out = c;
   if (rms_out) *rms_out = relative ? (r0 > 0 ? r / r0 : 0.0) : r;
+  return kOk;
+}
+
+int pgb_mg_bicgstab(pgb_mg *g, double *u, const double *rhs, int32_t precondition, double rtol, int32_t relative,
+                    int32_t max_iters, int32_t *iters_out, double *rms_out, void *stream) {
+  if (!g || !u || !rhs) return fail(kErrInvalid, "null argument");
+  if (precondition < 0 || precondition > 2) return fail(kErrInvalid, "precondition must be 0, 1 or 2");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc;
+  if ((rc = check_stream(s)) || (rc = mg_upload(g)) || (precondition == 2 && (rc = mg_upload32(g))) ||
+      (rc = bicg_alloc(g)))
+    return rc;
+  pgb_mg::Store &S = g->stores.at(0);
+  const Dims &d = S.dims;
+  const unsigned grid = grid_for((int64_t)g->nleaf * d.nx[0] * d.nx[1] * d.nx[2]);
+  double *const *v = g->kv;
+  // x <- 0, r, rhat0, p <- rhs; (rhat0, r) and (rhs, rhs) (bicgstab_solver.hpp:125-140)
+  if ((rc = launch_pdl(k_bi_init, grid, 256, s, rhs, v[kX], v[kR], v[kRhat0], v[kP], g->nleaf, d)) ||
+      (rc = bicg_dots(g, v[kRhat0], v[kR], rhs, rhs, kRr, kRhs2, s)))
+    return rc;
+  PGB_CUDA(cudaMemcpyAsync(g->kres_h + 1, g->ks + kRhs2, sizeof(double), cudaMemcpyDeviceToHost, s));
+  PGB_CUDA(cudaStreamSynchronize(s));
+  double ncell = 0.0;
+  for (auto &b : g->topo->leaf().blocks) ncell += (double)b.nx[0] * b.nx[1] * b.nx[2];
+  const double tol = relative ? rtol * std::sqrt(g->kres_h[1] / ncell) : rtol;
+  int it = 0;
+  double rms = 0.0;
+  while (it < max_iters) {
+    if ((rc = run_bicg_iteration(g, precondition, s))) return rc;
+    PGB_CUDA(cudaStreamSynchronize(s));
+    rms = std::sqrt(g->kres_h[0] / ncell);
+    ++it;
+    if (rms < tol) break;
+  }
+  // u <- x, with its ghosts exchanged on the leaf grid
+  if ((rc = launch_pdl(k_bi_in<double>, grid, 256, s, (const double *)v[kX], (double *)nullptr, S.u, g->nleaf, d)) ||
+      (rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr)) ||
+      (rc = copy_out(g, u, s)))
+    return rc;
+  PGB_CUDA(cudaStreamSynchronize(s));
+  if (iters_out) *iters_out = it;
+  if (rms_out) *rms_out = rms;
   return kOk;
 }
 

@@ -168,3 +168,19 @@ class CompositeMultigrid:
                   "pgb_mg_solve")
         torch.cuda.current_stream().wait_stream(s)
         return cyc.value, r.value
+
+    def bicgstab(self, u, rhs, precondition="fp64", rtol=1e-10, relative=True, max_iters=1000, stream=None):
+        """BiCGSTABSolver on the leaf grid from u = 0 with one composite V-cycle per
+        preconditioner application ("fp64", "fp32" or None); returns (iterations, final
+        rms residual)."""
+        import torch
+        self._check(u, rhs)
+        s = self._stream(stream)
+        mode = {None: 0, "none": 0, "fp64": 1, "fp32": 2}[precondition]
+        it = ctypes.c_int32(0)
+        rms = ctypes.c_double(0.0)
+        nat.check(nat.lib().pgb_mg_bicgstab(self._h, _ptr(u), _ptr(rhs), mode, float(rtol), int(bool(relative)),
+                                            int(max_iters), ctypes.byref(it), ctypes.byref(rms), _stream(s)),
+                  "pgb_mg_bicgstab")
+        torch.cuda.current_stream().wait_stream(s)
+        return it.value, rms.value

@@ -351,6 +351,9 @@ def _mgb_lib():
         L.orc_mgb_num_boundaries.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_mgb_num_boundaries.restype = ctypes.c_int
         L.orc_mgb_boundaries.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.orc_mgb_bicgstab.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        L.orc_mgb_bicgstab.restype = ctypes.c_int
         L._mgb_ready = True
     return L
 
@@ -408,3 +411,13 @@ class OracleMgBlocks:
         out = np.zeros((n, 23), np.int32)
         _mgb_lib().orc_mgb_boundaries(self.h, int(level), _ptr(out))
         return out
+
+    def bicgstab(self, rhs, precondition=True, rtol=1e-10, relative=True, max_iters=1000):
+        """(solution in the leaf layout, iterations, final rms residual) of BiCGSTAB with
+        one composite V-cycle per preconditioner application."""
+        b = np.ascontiguousarray(rhs, np.float64)
+        x = np.zeros_like(b)
+        rms = np.zeros(1)
+        it = _mgb_lib().orc_mgb_bicgstab(self.h, _ptr(b), _ptr(x), int(bool(precondition)), float(rtol),
+                                         int(bool(relative)), int(max_iters), _ptr(rms))
+        return x, it, float(rms[0])

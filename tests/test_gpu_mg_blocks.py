@@ -123,3 +123,28 @@ def test_composite_mixed_precision_solve(name, nx, bnx, ng, leaves):
     assert c32 <= c64 + 2
     a, b = _interior(u64.cpu().numpy(), ng), _interior(u32.cpu().numpy(), ng)
     assert np.abs(a - b).max() <= 1e-8 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", None], ids=["mg-fp64", "mg-fp32", "none"])
+def test_composite_bicgstab(prec):
+    # BiCGSTABSolver on the leaf grid with one composite V-cycle per preconditioner
+    # application, against the oracle's restatement (compensated dot products there,
+    # fixed-order sums here, so iteration counts may differ by one)
+    name, nx, bnx, ng, leaves = MG_CASES[1]
+    sim = O.OracleSim(nx, bnx, ng, leaves=leaves)
+    om = O.OracleMgBlocks(sim, alpha=10.0)
+    locs, geom = sim.block_info()
+    rhs = gaussian_rhs(locs, geom, bnx, ng)
+    xo, it_o, rms_o = om.bicgstab(rhs, precondition=prec is not None, rtol=1e-10, max_iters=600)
+    m = pg.Mesh(nx, bnx, ng, leaves=leaves)
+    pm = pg.CompositeMultigrid(m, alpha=10.0)
+    u = torch.zeros(rhs.shape, dtype=torch.float64, device="cuda")
+    it, rms = pm.bicgstab(u, torch.from_numpy(rhs).cuda(), precondition=prec, rtol=1e-10, max_iters=600)
+    assert it < 600 and it_o < 600
+    if prec is None:
+        assert it <= 1.2 * it_o + 5
+    else:
+        assert abs(it - it_o) <= (1 if prec == "fp64" else 2)
+    ref = _interior(xo, ng)
+    tol = 1e-8 if prec is not None else 1e-7
+    assert np.abs(_interior(u.cpu().numpy(), ng) - ref).max() <= tol * np.abs(ref).max()
