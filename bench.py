@@ -380,6 +380,23 @@ def gmg_composite_bench(torch, with_cpu):
                 best = (dt, cyc, rel)
         runs[mixed] = best
         sols[mixed] = u[:, GMGC_NG:-GMGC_NG, GMGC_NG:-GMGC_NG, GMGC_NG:-GMGC_NG].cpu()
+    # BiCGSTAB with one composite V-cycle per preconditioner application (FP64, FP32)
+    bicg = {}
+    for prec in ("fp64", "fp32"):
+        bb = None
+        for rep in range(3):
+            u = torch.zeros_like(rhs)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            it, rms = mg.bicgstab(u, rhs, precondition=prec, rtol=1e-10, relative=True, max_iters=200, stream=s)
+            s.synchronize()
+            dt = time.perf_counter() - t0
+            if rep > 0 and (bb is None or dt < bb[0]):
+                bb = (dt, it, rms)
+        x = u[:, GMGC_NG:-GMGC_NG, GMGC_NG:-GMGC_NG, GMGC_NG:-GMGC_NG].cpu()
+        bicg["bicgstab_mg_" + prec] = {"seconds": bb[0], "iterations": bb[1], "rms_residual": bb[2],
+                                       "vs_fp64_vcycle_rel_err": float((x - sols[False]).abs().max() /
+                                                                       sols[False].abs().max())}
     best = runs[False]
     locs, _ = mesh.block_info()
     res = {"seconds": best[0], "vcycles": best[1], "rel_residual": best[2],
@@ -388,6 +405,7 @@ def gmg_composite_bench(torch, with_cpu):
                      "ms_per_iteration": 1e3 * runs[True][0] / max(1, runs[True][1])},
            "time_ratio_mixed_over_fp64": runs[True][0] / best[0],
            "mixed_vs_fp64_rel_err": float((sols[True] - sols[False]).abs().max() / sols[False].abs().max()),
+           **bicg,
            "config": {"mesh": "128^3 root, 16^3 blocks, central 1/8 refined once", "leaves": int(mesh.nblocks),
                       "leaves_per_level": {str(int(l)): int((locs[:, 0] == l).sum()) for l in np.unique(locs[:, 0])},
                       "nghost": GMGC_NG, "grids": mg.ngrids, "levels": [mg.lmin, mg.lmax],
