@@ -270,6 +270,13 @@ int pgb_mg_info(const pgb_mg *mg, int32_t *out);
 /* gmg_same boundary index maps of grid `level` in the pgb_mesh_boundaries record
  * format; *count receives the number of records (out may be NULL to query it). */
 int pgb_mg_boundaries(const pgb_mg *mg, int32_t level, int32_t *out, int32_t capacity, int32_t *count);
+/* A spatially varying coefficient: the poisson_gmg package's face field D, D grad u on
+ * every face. d: device array of the leaf blocks, [block][3][k][j][i] with the block
+ * extents of the cell arrays (x1, x2, x3 faces; face i is the low face of cell i, the
+ * block's last face sits at nghost + nx). Restricted to the internal blocks of every
+ * grid as MGSolver::AddSetupTasks does (mg_solver.hpp:188-203, RestrictAverage on faces);
+ * the constant D of the parameters is no longer used. Synchronises the stream. */
+int pgb_mg_set_coefficient(pgb_mg *mg, const double *d, void *stream);
 /* u, rhs: device arrays of the leaf blocks, [block][k][j][i] with ghosts (one
  * component). ncycles V-cycles on u (in/out: interior result, ghosts exchanged);
  * rms (host, may be NULL) receives sqrt(sum r^2 / N) of the leaf residual after each.

@@ -42,7 +42,9 @@ struct BlockGmg {
   int lmin = 0, lmax = 0, nleaf = 0, nslot0 = 0;
   struct Store {
     Field u, res, rhs, temp, u0;
+    Field d[3];  // face coefficient D (x1, x2, x3 faces; face i is the low face of cell i)
   };
+  bool varD = false;  // D set per face (set_coefficient); otherwise the constant p.D
   std::map<int, Store> store;               // key 0: blocks of levels >= 0; key L < 0: level L
   std::map<int, std::vector<int>> slot;     // per grid: block index -> storage slot
   std::map<int, std::map<int, int>> index;  // per grid: gid -> block index
@@ -82,7 +84,8 @@ struct BlockGmg {
       if (!store.count(k)) {
         Store &st = store[k];
         const int ns = k == 0 ? nslot0 : (int)bl.size();
-        for (Field *f : {&st.u, &st.res, &st.rhs, &st.temp, &st.u0}) f->init_store(&m, bl[0].nx, ns);
+        for (Field *f : {&st.u, &st.res, &st.rhs, &st.temp, &st.u0, &st.d[0], &st.d[1], &st.d[2]})
+          f->init_store(&m, bl[0].nx, ns);
       }
     }
     for (int b = 0; b < nleaf; ++b) leaf_slot.push_back(b);
@@ -91,9 +94,12 @@ struct BlockGmg {
 
   Store &st(int L) { return store.at(key(L)); }
   void bind(Store &s, const std::vector<int> *sl) {
-    for (Field *f : {&s.u, &s.res, &s.rhs, &s.temp, &s.u0}) f->slot = sl;
+    for (Field *f : {&s.u, &s.res, &s.rhs, &s.temp, &s.u0, &s.d[0], &s.d[1], &s.d[2]}) f->slot = sl;
   }
-  void bind(int L) { bind(st(L), &slot[L]); }
+  void bind(int L) {
+    bind(st(L), &slot[L]);
+    cur_d = st(L).d;
+  }
   static double &cell(Field &f, int64_t s, int k, int j, int i) {
     return f.data[s * f.bstride() + ((int64_t)k * f.N[1] + j) * f.N[0] + i];
   }
@@ -113,29 +119,48 @@ struct BlockGmg {
         for (int i = 0; i < f.N[0]; ++i) fn(k, j, i);
   }
 
+  // D on the six faces of a cell: x1 low/high, x2 low/high, x3 low/high
+  void faceD(int b, int k, int j, int i, double *D6) {
+    if (!varD) {
+      for (int q = 0; q < 6; ++q) D6[q] = p.D;
+      return;
+    }
+    Field *d = cur_d;  // the face fields of the store whose binding is in effect
+    D6[0] = d[0].at(b, 0, k, j, i);
+    D6[1] = d[0].at(b, 0, k, j, i + 1);
+    D6[2] = d[1].at(b, 0, k, j, i);
+    D6[3] = d[1].at(b, 0, k, j + 1, i);
+    D6[4] = d[2].at(b, 0, k, j, i);
+    D6[5] = d[2].at(b, 0, k + 1, j, i);
+  }
+  Field *cur_d = nullptr;  // the face fields of the store whose binding is in effect
+
   // poisson_equation.hpp:104-210: face fluxes D grad u, then their divergence
-  double ax(Field &u, int b, const Block &blk, int k, int j, int i) const {
-    const double D = p.D;
+  double ax(Field &u, int b, const Block &blk, int k, int j, int i) {
+    double D6[6];
+    faceD(b, k, j, i, D6);
     const double dx1 = blk.coords.dx[0], dx2 = blk.coords.dx[1], dx3 = blk.coords.dx[2];
     const double uc = u.at(b, 0, k, j, i);
-    const double f1l = D / dx1 * (u.at(b, 0, k, j, i - 1) - uc);
-    const double f1r = D / dx1 * (uc - u.at(b, 0, k, j, i + 1));
-    const double f2l = D * (u.at(b, 0, k, j - 1, i) - uc) / dx2;
-    const double f2r = D * (uc - u.at(b, 0, k, j + 1, i)) / dx2;
-    const double f3l = D * (u.at(b, 0, k - 1, j, i) - uc) / dx3;
-    const double f3r = D * (uc - u.at(b, 0, k + 1, j, i)) / dx3;
+    const double f1l = D6[0] / dx1 * (u.at(b, 0, k, j, i - 1) - uc);
+    const double f1r = D6[1] / dx1 * (uc - u.at(b, 0, k, j, i + 1));
+    const double f2l = D6[2] * (u.at(b, 0, k, j - 1, i) - uc) / dx2;
+    const double f2r = D6[3] * (uc - u.at(b, 0, k, j + 1, i)) / dx2;
+    const double f3l = D6[4] * (u.at(b, 0, k - 1, j, i) - uc) / dx3;
+    const double f3r = D6[5] * (uc - u.at(b, 0, k + 1, j, i)) / dx3;
     double out = -p.alpha * uc;
     out += (f1l - f1r) / dx1;
     out += (f2l - f2r) / dx2;
     out += (f3l - f3r) / dx3;
     return out;
   }
-  // poisson_equation.hpp:59-102
-  double diag(const Block &blk) const {
-    const double D = p.D, dx1 = blk.coords.dx[0], dx2 = blk.coords.dx[1], dx3 = blk.coords.dx[2];
-    double d = -(D + D) / (dx1 * dx1) - p.alpha;
-    d -= (D + D) / (dx2 * dx2);
-    d -= (D + D) / (dx3 * dx3);
+  // poisson_equation.hpp:59-102 (SetDiagonal)
+  double diag(int b, const Block &blk, int k, int j, int i) {
+    double D6[6];
+    faceD(b, k, j, i, D6);
+    const double dx1 = blk.coords.dx[0], dx2 = blk.coords.dx[1], dx3 = blk.coords.dx[2];
+    double d = -(D6[0] + D6[1]) / (dx1 * dx1) - p.alpha;
+    d -= (D6[2] + D6[3]) / (dx2 * dx2);
+    d -= (D6[4] + D6[5]) / (dx3 * dx3);
     return d;
   }
   // mg_solver.hpp:312-345 (3D weights)
@@ -171,9 +196,9 @@ struct BlockGmg {
         const Block &blk = bl[b];
         if (blk.loc.level != L) continue;
         interior(blk, [&](int k, int j, int i) { S.temp.at(b, 0, k, j, i) = ax(S.u, b, blk, k, j, i); });
-        const double dg = diag(blk);
-        const double den = dg + (dg >= 0 ? 1.0 : -1.0) * small;  // robust::ratio
         interior(blk, [&](int k, int j, int i) {
+          const double dg = diag(b, blk, k, j, i);
+          const double den = dg + (dg >= 0 ? 1.0 : -1.0) * small;  // robust::ratio
           const double off = S.temp.at(b, 0, k, j, i) - dg * S.u.at(b, 0, k, j, i);
           const double val = S.rhs.at(b, 0, k, j, i) - off;
           S.temp.at(b, 0, k, j, i) = w * (val / den) + (1.0 - w) * S.u.at(b, 0, k, j, i);
@@ -335,6 +360,7 @@ struct BlockGmg {
   double residual() {
     Store &S = store.at(0);
     bind(S, &leaf_slot);
+    cur_d = S.d;
     exchange(S.u, m.blocks, BAny, 0, leaf_recs, true, PLinear, m.multilevel);
     double s = 0.0;
     for (int b = 0; b < nleaf; ++b) {
@@ -354,6 +380,59 @@ struct BlockGmg {
     return n;
   }
 
+  // ---- spatially varying coefficient (the poisson_gmg package's face field D)
+  // Leaf faces from `d` ([nleaf][3][N3][N2][N1], face i the low face of cell i), then
+  // AddSetupTasks (mg_solver.hpp:188-203, 347-370): from the finest grid down, every
+  // fine block restricts its faces (RestrictAverage on F1/F2/F3: area-weighted mean of
+  // the 2x2 fine faces in the face's plane, pr_ops.hpp:105-164) into its parent's octant.
+  void set_coefficient(const double *dl) {
+    varD = true;
+    Store &S0 = store.at(0);
+    const int64_t n = (int64_t)S0.u.N[0] * S0.u.N[1] * S0.u.N[2];
+    for (int b = 0; b < nleaf; ++b)
+      for (int dir = 0; dir < 3; ++dir)
+        std::copy(dl + ((int64_t)b * 3 + dir) * n, dl + ((int64_t)b * 3 + dir + 1) * n,
+                  S0.d[dir].data.begin() + (int64_t)b * n);
+    const int ng = m.p.ng;
+    for (int L = lmax; L > lmin; --L) {
+      auto &bl = m.gmg_levels[L];
+      Store &S = st(L), &P = st(L - 1);
+      for (int b = 0; b < (int)bl.size(); ++b) {
+        const Block &c = bl[b];
+        if (c.loc.level != L) continue;
+        int pb;
+        const NeighborBlock *up, *down;
+        family(L, c, pb, up, down);
+        const Block &par = m.gmg_levels[L - 1][pb];
+        const int64_t cs = slot[L][b], ps = slot[L - 1][pb];
+        const Box tb = calc_indices(*down, par.loc, par.nx, ng, CC, InteriorRecv, false, false);
+        const int h[3] = {std::max(1, c.nx[0] / 2), std::max(1, c.nx[1] / 2), std::max(1, c.nx[2] / 2)};
+        for (int dir = 0; dir < 3; ++dir) {
+          const double a = c.coords.area[dir];
+          const int e[3] = {h[0] + (dir == 0), h[1] + (dir == 1), h[2] + (dir == 2)};
+          for (int ck = 0; ck < e[2]; ++ck)
+            for (int cj = 0; cj < e[1]; ++cj)
+              for (int ci = 0; ci < e[0]; ++ci) {
+                const int i = 2 * ci + ng, j = 2 * cj + ng, k = 2 * ck + ng;
+                double vol[2][2][2] = {}, t[2][2][2] = {};
+                for (int ok = 0; ok < 1 + (dir != 2); ++ok)
+                  for (int oj = 0; oj < 1 + (dir != 1); ++oj)
+                    for (int oi = 0; oi < 1 + (dir != 0); ++oi) {
+                      vol[ok][oj][oi] = a;
+                      t[ok][oj][oi] = a * cell(S.d[dir], cs, k + ok, j + oj, i + oi);
+                    }
+                const double tv = ((vol[0][0][0] + vol[0][1][0]) + (vol[0][0][1] + vol[0][1][1])) +
+                                  ((vol[1][0][0] + vol[1][1][0]) + (vol[1][0][1] + vol[1][1][1]));
+                cell(P.d[dir], ps, tb.s[2] + ck, tb.s[1] + cj, tb.s[0] + ci) =
+                    (((t[0][0][0] + t[0][1][0]) + (t[0][0][1] + t[0][1][1])) +
+                     ((t[1][0][0] + t[1][1][0]) + (t[1][0][1] + t[1][1][1]))) /
+                    tv;
+              }
+        }
+      }
+    }
+  }
+
   // ---- BiCGSTAB on the leaf grid with one composite V-cycle as preconditioner
   // (bicgstab_solver.hpp:116-315). Vectors hold the leaf interiors in block, k, j, i
   // order; the dot products are compensated sums (the accurate values).
@@ -361,6 +440,7 @@ struct BlockGmg {
   void leaf_cells(F fn) {
     Store &S = store.at(0);
     bind(S, &leaf_slot);
+    cur_d = S.d;
     int64_t q = 0;
     for (int b = 0; b < nleaf; ++b) interior(m.blocks[b], [&](int k, int j, int i) { fn(q++, b, k, j, i); });
   }

@@ -1484,6 +1484,9 @@ double orc_mgb_residual(void *h) {
   BlockGmg *g = (BlockGmg *)h;
   return std::sqrt(g->residual() / g->ncells());
 }
+// face coefficient D of the leaves, [nleaf][3][N3][N2][N1] (face i the low face of cell i)
+void orc_mgb_set_coefficient(void *h, const double *d) { ((BlockGmg *)h)->set_coefficient(d); }
+
 // BiCGSTAB on the leaf grid (rhs and x in the leaf layout [nleaf][N3][N2][N1], x
 // receives the interior solution); returns the iterations, *rms the final rms residual
 int orc_mgb_bicgstab(void *h, const double *rhs, double *x, int precondition, double rtol, int relative,

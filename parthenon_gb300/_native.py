@@ -88,6 +88,7 @@ _SIGNATURES = {
     "pgb_mg_vcycles": [VP, VP, VP, ctypes.c_int32, VP, VP],
     "pgb_mg_solve": [VP, VP, VP, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                      ctypes.POINTER(ctypes.c_int32), DP, VP],
+    "pgb_mg_set_coefficient": [VP, VP, VP],
     "pgb_mg_bicgstab": [VP, VP, VP, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
                         ctypes.POINTER(ctypes.c_int32), DP, VP],
     "pgb_history_mass": [VP, VP, ctypes.c_int32, VP, ctypes.c_int32, ctypes.c_double, VP, VP],

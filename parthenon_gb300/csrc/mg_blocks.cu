@@ -74,6 +74,7 @@ struct MgOp {
 struct MgCoef {
   double dx[3];  // exact build: the spacings (fluxes formed and divided as the reference does)
   double c[3];   // fast build: D / dx_d^2
+  double ic[3];  // fast build, face coefficient: 1 / dx_d^2
   double dg;     // SetDiagonal (poisson_equation.hpp:59-102)
   double den;    // robust::ratio denominator dg + sgn(dg) 10 DBL_MIN (utils/robust.hpp)
 };
@@ -160,23 +161,75 @@ __device__ __forceinline__ Faces<T> faces(const T *__restrict__ u, const Dims &d
   return f;
 }
 
+// The face coefficient of the poisson_gmg package (a Face field D): per block arrays in
+// the cell layout, face i the low face of cell i (the block's last face at ng + nx).
+// Null pointers: the constant MgOp::D.
+template <class T>
+struct FaceD {
+  const T *d0, *d1, *d2;
+};
+// D on the low and high x1, x2, x3 faces of cell c
+__device__ __forceinline__ void face_d6(const FaceD<double> &fd, int64_t c, int64_t sj, int64_t sk, double D,
+                                        double *D6) {
+  if (fd.d0) {
+    D6[0] = fd.d0[c];
+    D6[1] = fd.d0[c + 1];
+    D6[2] = fd.d1[c];
+    D6[3] = fd.d1[c + sj];
+    D6[4] = fd.d2[c];
+    D6[5] = fd.d2[c + sk];
+  } else {
+    for (int q = 0; q < 6; ++q) D6[q] = D;
+  }
+}
+
 // Exact build, poisson_equation.hpp:104-210: face fluxes D grad u, then their
 // divergence, -alpha u + sum over directions of (F_left - F_right) / dx, in the
 // reference's order
-__device__ __forceinline__ double ax_exact(const Faces<double> &f, const double *dx, const MgOp &o) {
-  const double D = o.D, dx1 = dx[0], dx2 = dx[1], dx3 = dx[2];
+__device__ __forceinline__ double ax_exact(const Faces<double> &f, const double *dx, const MgOp &o,
+                                          const double *D6) {
+  const double dx1 = dx[0], dx2 = dx[1], dx3 = dx[2];
   const double uc = f.c;
-  const double f1l = div_rn(D, dx1) * (f.xm - uc);
-  const double f1r = div_rn(D, dx1) * (uc - f.xp);
-  const double f2l = div_rn(D * (f.ym - uc), dx2);
-  const double f2r = div_rn(D * (uc - f.yp), dx2);
-  const double f3l = div_rn(D * (f.zm - uc), dx3);
-  const double f3r = div_rn(D * (uc - f.zp), dx3);
+  const double f1l = div_rn(D6[0], dx1) * (f.xm - uc);
+  const double f1r = div_rn(D6[1], dx1) * (uc - f.xp);
+  const double f2l = div_rn(D6[2] * (f.ym - uc), dx2);
+  const double f2r = div_rn(D6[3] * (uc - f.yp), dx2);
+  const double f3l = div_rn(D6[4] * (f.zm - uc), dx3);
+  const double f3r = div_rn(D6[5] * (uc - f.zp), dx3);
   double out = -o.alpha * uc;
   out += div_rn(f1l - f1r, dx1);
   out += div_rn(f2l - f2r, dx2);
   out += div_rn(f3l - f3r, dx3);
   return out;
+}
+
+// Exact build, SetDiagonal (poisson_equation.hpp:59-102) from the faces
+__device__ __forceinline__ double diag_exact(const double *dx, const MgOp &o, const double *D6) {
+  double d = -div_rn(D6[0] + D6[1], dx[0] * dx[0]) - o.alpha;
+  d -= div_rn(D6[2] + D6[3], dx[1] * dx[1]);
+  d -= div_rn(D6[4] + D6[5], dx[2] * dx[2]);
+  return d;
+}
+
+// Exact build: the operator, its diagonal and the robust::ratio denominator at cell c
+// (the grid's host-formed constants when D is constant)
+struct ExactOp {
+  double ax, dg, den;
+};
+__device__ __forceinline__ ExactOp exact_op(const Faces<double> &f, const MgCoef &cf, const MgOp &o,
+                                            const FaceD<double> &fd, int64_t c, int64_t sj, int64_t sk) {
+  double D6[6];
+  face_d6(fd, c, sj, sk, o.D, D6);
+  ExactOp r;
+  r.ax = ax_exact(f, cf.dx, o, D6);
+  if (fd.d0) {
+    r.dg = diag_exact(cf.dx, o, D6);
+    r.den = r.dg + (r.dg >= 0 ? 1.0 : -1.0) * (10.0 * DBL_MIN);
+  } else {
+    r.dg = cf.dg;
+    r.den = cf.den;
+  }
+  return r;
 }
 
 // Fast build: the constant-coefficient operator as a 7-point stencil, A u = off + dg u
@@ -186,24 +239,48 @@ template <class T>
 __device__ __forceinline__ T off_fast(const Faces<T> &f, const MgCoef &cf) {
   return fma_t((T)cf.c[2], f.zm + f.zp, fma_t((T)cf.c[1], f.ym + f.yp, (T)cf.c[0] * (f.xm + f.xp)));
 }
+// Fast build with face coefficients: off = sum_d (D_low u_{-d} + D_high u_{+d}) / dx_d^2,
+// dg = -sum_d (D_low + D_high) / dx_d^2 - alpha
+template <class T>
+__device__ __forceinline__ void fast_op(const Faces<T> &f, const MgCoef &cf, const MgOp &o, const FaceD<T> &fd,
+                                        int64_t c, int64_t sj, int64_t sk, T &off, T &dg) {
+  if (fd.d0) {
+    const T a0 = fd.d0[c], a1 = fd.d0[c + 1], b0 = fd.d1[c], b1 = fd.d1[c + sj], e0 = fd.d2[c], e1 = fd.d2[c + sk];
+    const T i1 = (T)cf.ic[0], i2 = (T)cf.ic[1], i3 = (T)cf.ic[2];
+    off = fma_t(fma_t(e0, f.zm, e1 * f.zp), i3, fma_t(fma_t(b0, f.ym, b1 * f.yp), i2, fma_t(a0, f.xm, a1 * f.xp) * i1));
+    dg = -fma_t(e0 + e1, i3, fma_t(b0 + b1, i2, (a0 + a1) * i1)) - (T)o.alpha;
+  } else {
+    off = off_fast(f, cf);
+    dg = (T)cf.dg;
+  }
+}
 
 // Jacobi sweep (mg_solver.hpp:222-297): dst = w ratio(rhs - (A src - dg src), dg) + (1 - w) src
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_jacobi(const T *__restrict__ src, const T *__restrict__ rhs,
                                                    T *__restrict__ dst, const int *__restrict__ list, int n,
                                                    const int *__restrict__ nbr, Dims d, MgCoef cf, MgOp o,
-                                                   MgSweep sw) {
+                                                   MgSweep sw, FaceD<T> fd) {
   pdl_enter();
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
   for_interior(list, n, d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(d, b, k, j, i);
     const Faces<T> f = faces(src, d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
     if constexpr (kFast) {
-      dst[c] = fma_t((T)sw.wd, rhs[c] - off_fast(f, cf), (T)sw.omw * f.c);
+      T off, dg;
+      fast_op(f, cf, o, fd, c, sj, sk, off, dg);
+      if (fd.d0) {
+        const T small = (T)10 * (sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN);
+        const T den = dg + (dg >= (T)0 ? (T)1 : (T)-1) * small;
+        dst[c] = fma_t((T)sw.w / den, rhs[c] - off, (T)sw.omw * f.c);
+      } else {
+        dst[c] = fma_t((T)sw.wd, rhs[c] - off, (T)sw.omw * f.c);
+      }
     } else {
-      const double a = ax_exact(f, cf.dx, o);
-      const double off = a - cf.dg * f.c;
+      const ExactOp e = exact_op(f, cf, o, fd, c, sj, sk);
+      const double off = e.ax - e.dg * f.c;
       const double val = rhs[c] - off;
-      dst[c] = sw.w * div_rn(val, cf.den) + sw.omw * f.c;
+      dst[c] = sw.w * div_rn(val, e.den) + sw.omw * f.c;
     }
   });
 }
@@ -211,13 +288,20 @@ __global__ void __launch_bounds__(256) k_mg_jacobi(const T *__restrict__ src, co
 // Ax + AddFieldsAndStoreInteriorSelect<rhs, temp, res_err>(1, -1): res = rhs - A u
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *__restrict__ list, int n,
-                                                     const int *__restrict__ nbr, MgCoef cf, MgOp o) {
+                                                     const int *__restrict__ nbr, MgCoef cf, MgOp o,
+                                                     FaceD<T> fd) {
   pdl_enter();
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
   for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     const Faces<T> f = faces(s.u, s.d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
-    if constexpr (kFast) s.res[c] = fma_t(-(T)cf.dg, f.c, s.rhs[c] - off_fast(f, cf));
-    else s.res[c] = s.rhs[c] - ax_exact(f, cf.dx, o);
+    if constexpr (kFast) {
+      T off, dg;
+      fast_op(f, cf, o, fd, c, sj, sk, off, dg);
+      s.res[c] = fma_t(-dg, f.c, s.rhs[c] - off);
+    } else {
+      s.res[c] = s.rhs[c] - exact_op(f, cf, o, fd, c, sj, sk).ax;
+    }
   });
 }
 
@@ -226,16 +310,22 @@ __global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *
 // rhs = A u + res_err
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_fas(StoreView<T> s, const int *__restrict__ list, int n, int nint,
-                                                const int *__restrict__ nbr, MgCoef cf, MgOp o) {
+                                                const int *__restrict__ nbr, MgCoef cf, MgOp o, FaceD<T> fd) {
   pdl_enter();
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
   for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     const T uc = s.u[c];
     s.u0[c] = uc;
     if (q >= nint) return;
     const Faces<T> f = faces(s.u, s.d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
-    if constexpr (kFast) s.rhs[c] = fma_t((T)cf.dg, uc, off_fast(f, cf) + s.res[c]);
-    else s.rhs[c] = ax_exact(f, cf.dx, o) + s.res[c];
+    if constexpr (kFast) {
+      T off, dg;
+      fast_op(f, cf, o, fd, c, sj, sk, off, dg);
+      s.rhs[c] = fma_t(dg, uc, off + s.res[c]);
+    } else {
+      s.rhs[c] = exact_op(f, cf, o, fd, c, sj, sk).ax + s.res[c];
+    }
   });
 }
 
@@ -379,18 +469,24 @@ constexpr int kResThreads = 256;
 template <bool kFast>
 __global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual(StoreView<double> s, int nleaf,
                                                                   const MgCoef *__restrict__ lc, MgOp o,
-                                                                  double *__restrict__ partial,
+                                                                  FaceD<double> fd, double *__restrict__ partial,
                                                                   float *__restrict__ rhs32, float *__restrict__ u32) {
   pdl_enter();
   __shared__ double sh[kResThreads / 32];
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
   double acc = 0.0;
   for_interior(nullptr, nleaf, s.d, [&](int, int b, int k, int j, int i) {
     const int64_t c = cell_of(s.d, b, k, j, i);
     const MgCoef &cf = lc[b];
     const Faces<double> f = faces<double>(s.u, s.d, nullptr, b, k, j, i);
     double r;
-    if constexpr (kFast) r = fma(-cf.dg, f.c, s.rhs[c] - off_fast(f, cf));
-    else r = s.rhs[c] - ax_exact(f, cf.dx, o);
+    if constexpr (kFast) {
+      double off, dg;
+      fast_op(f, cf, o, fd, c, sj, sk, off, dg);
+      r = fma(-dg, f.c, s.rhs[c] - off);
+    } else {
+      r = s.rhs[c] - exact_op(f, cf, o, fd, c, sj, sk).ax;
+    }
     s.res[c] = r;
     acc += r * r;
     if (rhs32) {
@@ -537,14 +633,61 @@ __global__ void __launch_bounds__(256) k_bi_out32(const float *__restrict__ e, d
 
 // out = A u on the leaves (u's ghosts exchanged before)
 __global__ void __launch_bounds__(256) k_bi_apply(const double *__restrict__ u, double *__restrict__ out, int nleaf,
-                                                  Dims d, const MgCoef *__restrict__ lc) {
+                                                  Dims d, const MgCoef *__restrict__ lc, MgOp o, FaceD<double> fd) {
   pdl_enter();
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
   for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
     const int64_t q = cell_of(d, b, k, j, i);
     const MgCoef &cf = lc[b];
     const Faces<double> f = faces<double>(u, d, nullptr, b, k, j, i);
-    out[q] = fma(cf.dg, f.c, off_fast(f, cf));
+    double off, dg;
+    fast_op(f, cf, o, fd, q, sj, sk, off, dg);
+    out[q] = fma(dg, f.c, off);
   });
+}
+
+// Setup restriction of the face coefficient (AddSetupTasks, mg_solver.hpp:188-203, 347-370,
+// of the GMGRestrict field D): RestrictAverage on the faces of direction dir, the
+// area-weighted mean of the 2x2 fine faces in the face's plane in the reference's
+// pairing order, into the parent's octant. One thread per parent face.
+__global__ void __launch_bounds__(256) k_mg_restrict_faces(const double *__restrict__ cd, Dims cdims,
+                                                           double *__restrict__ pd, Dims pdims,
+                                                           const MgXfer *__restrict__ x, int n,
+                                                           const DevBlockGeom *__restrict__ cgeom, int dir) {
+  const int e0 = max(1, cdims.nx[0] / 2) + (dir == 0), e1 = max(1, cdims.nx[1] / 2) + (dir == 1);
+  const int e2 = max(1, cdims.nx[2] / 2) + (dir == 2);
+  const int per = e0 * e1 * e2, total = per * n;
+  const int ng = cdims.ng;
+  const int64_t sj = cdims.N[0], sk = (int64_t)cdims.N[0] * cdims.N[1];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int q = e / per;
+    const int r = e - q * per;
+    const int ci = r % e0, cj = (r / e0) % e1, ck = r / (e0 * e1);
+    const MgXfer t = x[q];
+    const double a = cgeom[t.child].area[dir];
+    const int64_t f = cell_of(cdims, t.child, 2 * ck + ng, 2 * cj + ng, 2 * ci + ng);
+    double v[2][2][2] = {}, tt[2][2][2] = {};
+#pragma unroll
+    for (int ok = 0; ok < 2; ++ok)
+#pragma unroll
+      for (int oj = 0; oj < 2; ++oj)
+#pragma unroll
+        for (int oi = 0; oi < 2; ++oi) {
+          if ((dir == 2 && ok) || (dir == 1 && oj) || (dir == 0 && oi)) continue;
+          v[ok][oj][oi] = a;
+          tt[ok][oj][oi] = a * cd[f + ok * sk + oj * sj + oi];
+        }
+    const double tv = ((v[0][0][0] + v[0][1][0]) + (v[0][0][1] + v[0][1][1])) +
+                      ((v[1][0][0] + v[1][1][0]) + (v[1][0][1] + v[1][1][1]));
+    const double num = ((tt[0][0][0] + tt[0][1][0]) + (tt[0][0][1] + tt[0][1][1])) +
+                       ((tt[1][0][0] + tt[1][1][0]) + (tt[1][0][1] + tt[1][1][1]));
+    pd[cell_of(pdims, t.parent, t.lo[2] + ck, t.lo[1] + cj, t.lo[0] + ci)] = div_rn(num, tv);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_to_f32(const double *__restrict__ a, float *__restrict__ b, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    b[q] = (float)a[q];
 }
 
 // alpha = (rhat0, r)_old / (rhat0, v); h = x + alpha u; s = r - alpha v
@@ -635,6 +778,14 @@ struct pgb_mg {
     // the FP32 copies of the mixed solve (allocated on its first use)
     float *u32 = nullptr, *res32 = nullptr, *rhs32 = nullptr, *temp32 = nullptr, *u032 = nullptr,
           *coarse32 = nullptr;
+    // face coefficient D per slot (pgb_mg_set_coefficient), FP64 and FP32
+    double *d[3] = {nullptr, nullptr, nullptr};
+    float *d32[3] = {nullptr, nullptr, nullptr};
+    template <class T>
+    FaceD<T> fd() const {
+      if constexpr (sizeof(T) == 8) return FaceD<T>{d[0], d[1], d[2]};
+      else return FaceD<T>{d32[0], d32[1], d32[2]};
+    }
     Dims dims{};
     template <class T>
     StoreView<T> view() const {
@@ -701,6 +852,7 @@ MgCoef make_coef(const double *dx, const GmgConfig &c) {
   for (int d = 0; d < 3; ++d) {
     o.dx[d] = dx[d];
     o.c[d] = D / (dx[d] * dx[d]);
+    o.ic[d] = 1.0 / (dx[d] * dx[d]);
   }
   double dg = -(D + D) / (dx[0] * dx[0]) - c.alpha;
   dg -= (D + D) / (dx[1] * dx[1]);
@@ -1051,8 +1203,8 @@ struct VCycle {
       sw.w = srj_weight(g->cfg, st);
       sw.omw = 1.0 - sw.w;
       sw.wd = sw.w / G.coef.den;
-      PGB_TRY(launch_pdl(k_mg_jacobi<kFast, T>, grid_for(nf * cl), 256, s, src, v.rhs, dst, G.fine, nf, G.nb(), v.d, G.coef, o,
-                                                              sw));
+      PGB_TRY(launch_pdl(k_mg_jacobi<kFast, T>, grid_for(nf * cl), 256, s, src, v.rhs, dst, G.fine, nf, G.nb(), v.d,
+                         G.coef, o, sw, g->store_of(L).template fd<T>()));
       std::swap(src, dst);
     }
     if (src != v.u) PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nf * cl), 256, s, v.u, v.temp, G.fine, nf, v.d));
@@ -1092,14 +1244,16 @@ struct VCycle {
     if (L < g->lmax) {
       // FAS: exchange, u0 = u, rhs = A u + res_err on internal blocks
       if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
-      PGB_TRY(launch_pdl(k_mg_fas<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nint, G.nb(), G.coef, o));
+      PGB_TRY(launch_pdl(k_mg_fas<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nint, G.nb(), G.coef, o,
+                         g->store_of(L).template fd<T>()));
     } else {
       PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nf * cl), 256, s, v.u0, v.u, G.fine, nf, v.d));
     }
     if ((rc = smooth<T>(L, g->cfg.stages))) return rc;
     if (L > g->lmin) {
       if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
-      PGB_TRY(launch_pdl(k_mg_residual<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nb(), G.coef, o));
+      PGB_TRY(launch_pdl(k_mg_residual<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nb(), G.coef, o,
+                         g->store_of(L).template fd<T>()));
       if constexpr (kFast) rc = dbl(L - 1) ? restrict_down<T, double>(L) : restrict_down<T, float>(L);
       else rc = restrict_down<T, double>(L);
       if (rc) return rc;
@@ -1159,7 +1313,7 @@ int leaf_residual_t(pgb_mg *g, bool mixed, cudaStream_t s) {
   int rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr);
   if (rc) return rc;
   PGB_TRY(launch_pdl(k_mg_leaf_residual<kFast>, g->nparts, kResThreads, s, S.template view<double>(), g->nleaf, g->leaf_coef,
-                                                              MgOp{g->cfg.D, g->cfg.alpha}, g->partial,
+                                                              MgOp{g->cfg.D, g->cfg.alpha}, S.template fd<double>(), g->partial,
                                                               mixed ? S.rhs32 : nullptr, mixed ? S.u32 : nullptr));
   PGB_CUDA(cudaGetLastError());
   PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1234,7 +1388,7 @@ int bicg_apply(pgb_mg *g, double *out, cudaStream_t s) {
   PGB_TRY(exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr));
   const unsigned grid = grid_for((int64_t)g->nleaf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]);
   return launch_pdl(k_bi_apply, grid, 256, s, (const double *)S.u, out, g->nleaf, S.dims,
-                    (const MgCoef *)g->leaf_coef);
+                    (const MgCoef *)g->leaf_coef, MgOp{g->cfg.D, g->cfg.alpha}, S.template fd<double>());
 }
 
 int bicg_dots(pgb_mg *g, const double *a, const double *b, const double *c, const double *e, int i0, int i1,
@@ -1464,6 +1618,61 @@ int pgb_mg_solve(pgb_mg *g, double *u, const double *rhs, double tol, int32_t re
   PGB_CUDA(cudaStreamSynchronize(s));
   if (cycles_out) *cycles_out = c;
   if (rms_out) *rms_out = relative ? (r0 > 0 ? r / r0 : 0.0) : r;
+  return kOk;
+}
+
+int pgb_mg_set_coefficient(pgb_mg *g, const double *d, void *stream) {
+  if (!g || !d) return fail(kErrInvalid, "null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc;
+  if ((rc = mg_upload(g))) return rc;
+  for (auto &kv : g->stores) {
+    pgb_mg::Store &S = kv.second;
+    const int64_t n = (int64_t)S.nslots * S.dims.N[0] * S.dims.N[1] * S.dims.N[2];
+    for (int q = 0; q < 3; ++q)
+      if (!S.d[q]) {
+        PGB_CUDA(cudaMalloc((void **)&S.d[q], n * sizeof(double)));
+        PGB_CUDA(cudaMemset(S.d[q], 0, n * sizeof(double)));
+        PGB_CUDA(cudaMalloc((void **)&S.d32[q], n * sizeof(float)));
+        g->allocs.push_back(S.d[q]);
+        g->allocs.push_back(S.d32[q]);
+      }
+  }
+  // the leaves' faces: [nleaf][3][N3][N2][N1] into the three face arrays of store 0
+  pgb_mg::Store &S0 = g->stores.at(0);
+  const size_t cells = (size_t)S0.dims.N[0] * S0.dims.N[1] * S0.dims.N[2];
+  for (int q = 0; q < 3; ++q)
+    PGB_CUDA(cudaMemcpy2DAsync(S0.d[q], cells * sizeof(double), d + q * cells, 3 * cells * sizeof(double),
+                               cells * sizeof(double), g->nleaf, cudaMemcpyDeviceToDevice, s));
+  // AddSetupTasks: from the finest grid down, each level's faces restricted into the next
+  for (int L = g->lmax; L > g->lmin; --L) {
+    pgb_mg::Grid &G = g->grids.at(L);
+    const pgb_mg::Store &C = g->store_of(L), &P = g->store_of(L - 1);
+    const int nx = (int)G.xfer_h.size();
+    const int64_t per = (int64_t)(C.dims.nx[0] / 2 + 1) * (C.dims.nx[1] / 2 + 1) * (C.dims.nx[2] / 2 + 1);
+    for (int q = 0; q < 3; ++q)
+      k_mg_restrict_faces<<<grid_for(nx * per), 256, 0, s>>>(C.d[q], C.dims, P.d[q], P.dims, G.xfer, nx, G.tab.geom,
+                                                              q);
+    PGB_CUDA(cudaGetLastError());
+  }
+  for (auto &kv : g->stores) {
+    pgb_mg::Store &S = kv.second;
+    const int64_t n = (int64_t)S.nslots * S.dims.N[0] * S.dims.N[1] * S.dims.N[2];
+    for (int q = 0; q < 3; ++q) k_to_f32<<<grid_for(n), 256, 0, s>>>(S.d[q], S.d32[q], n);
+  }
+  PGB_CUDA(cudaGetLastError());
+  PGB_CUDA(cudaStreamSynchronize(s));
+  // graphs captured before hold the constant-coefficient kernels
+  for (auto &gr : g->graph)
+    if (gr) {
+      cudaGraphExecDestroy(gr);
+      gr = nullptr;
+    }
+  for (auto &gr : g->kgraph)
+    if (gr) {
+      cudaGraphExecDestroy(gr);
+      gr = nullptr;
+    }
   return kOk;
 }
 

@@ -141,6 +141,15 @@ class CompositeMultigrid:
         stream.wait_stream(torch.cuda.current_stream())
         return stream
 
+    def set_coefficient(self, d, stream=None):
+        """The face coefficient D of the leaves, (nblocks, 3, N3, N2, N1) float64 on the
+        device (face i the low face of cell i); restricted to every grid."""
+        n = self.nleaf * 3 * self.mesh.N[0] * self.mesh.N[1] * self.mesh.N[2]
+        if not (d.is_cuda and d.element_size() == 8 and d.is_contiguous() and d.numel() == n):
+            raise ValueError("D must be a contiguous float64 CUDA tensor (nblocks, 3, N3, N2, N1)")
+        s = self._stream(stream)
+        nat.check(nat.lib().pgb_mg_set_coefficient(self._h, _ptr(d), _stream(s)), "pgb_mg_set_coefficient")
+
     def vcycles(self, u, rhs, ncycles, stream=None):
         """ncycles V-cycles on u (in place); the rms leaf residual after each."""
         import numpy as np

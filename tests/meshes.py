@@ -81,3 +81,29 @@ MG_CASES = [
     ("smr-corner-32-b8", (32, 32, 32), (8, 8, 8), 2, refined_cube(2, 0, 2)),
     ("three-level-32-b4", (32, 32, 32), (4, 4, 4), 2, two_level_nested(3, 2, 6, 6, 10)),
 ]
+
+
+def region_coefficient(locs, geom, bnx, ng, inside=10.0, outside=1.0):
+    """Face coefficient D on leaf blocks (nblocks, 3, N3, N2, N1), face i the low face of
+    cell i: `inside` where the face centre lies in the union of two boxes (the shape of
+    the poisson_gmg example's inside_region, moved into the unit cube), else `outside`."""
+    import numpy as np
+    nb = locs.shape[0]
+    N = [b + 2 * ng for b in bnx]
+    out = np.full((nb, 3, N[2], N[1], N[0]), outside)
+
+    def inside_region(x, y, z):
+        a = (x > 0.125) & (x < 0.375) & (y > 0.25) & (y < 0.75) & (z > 0.375) & (z < 0.625)
+        b = (x > 0.125) & (x < 0.75) & (y > 0.125) & (y < 0.375) & (z > 0.375) & (z < 0.625)
+        return a | b
+
+    for b in range(nb):
+        x0, dx = geom[b, :3], geom[b, 3:]
+        idx = [np.arange(N[d]) - ng for d in range(3)]
+        cc = [x0[d] + (idx[d] + 0.5) * dx[d] for d in range(3)]
+        fc = [x0[d] + idx[d] * dx[d] for d in range(3)]
+        for dirn in range(3):
+            c = [fc[d] if d == dirn else cc[d] for d in range(3)]
+            Z, Y, X = np.meshgrid(c[2], c[1], c[0], indexing="ij")
+            out[b, dirn] = np.where(inside_region(X, Y, Z), inside, outside)
+    return out

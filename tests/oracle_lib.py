@@ -354,6 +354,7 @@ def _mgb_lib():
         L.orc_mgb_bicgstab.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                        ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.orc_mgb_bicgstab.restype = ctypes.c_int
+        L.orc_mgb_set_coefficient.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
         L._mgb_ready = True
     return L
 
@@ -421,3 +422,10 @@ class OracleMgBlocks:
         it = _mgb_lib().orc_mgb_bicgstab(self.h, _ptr(b), _ptr(x), int(bool(precondition)), float(rtol),
                                          int(bool(relative)), int(max_iters), _ptr(rms))
         return x, it, float(rms[0])
+
+    def set_coefficient(self, d):
+        """Face coefficient D of the leaves, (nleaf, 3, N3, N2, N1); face i is the low face
+        of cell i. Restricted to the internal blocks as the setup tasks do."""
+        d = np.ascontiguousarray(d, np.float64)
+        self._d = d
+        _mgb_lib().orc_mgb_set_coefficient(self.h, _ptr(d))

@@ -148,3 +148,58 @@ def test_composite_bicgstab(prec):
     ref = _interior(xo, ng)
     tol = 1e-8 if prec is not None else 1e-7
     assert np.abs(_interior(u.cpu().numpy(), ng) - ref).max() <= tol * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name,nx,bnx,ng,leaves", MG_CASES, ids=[c[0] for c in MG_CASES])
+def test_composite_face_coefficient_bitwise(name, nx, bnx, ng, leaves):
+    # D on the faces (the poisson_gmg package's Face field), 10 inside two boxes and 1
+    # outside, restricted to every grid by the setup tasks: exact build bitwise
+    from meshes import region_coefficient
+    sim = O.OracleSim(nx, bnx, ng, leaves=leaves)
+    om = O.OracleMgBlocks(sim, alpha=10.0)
+    locs, geom = sim.block_info()
+    rhs = gaussian_rhs(locs, geom, bnx, ng)
+    dcoef = region_coefficient(locs, geom, bnx, ng)
+    om.rhs()[:] = rhs
+    om.set_coefficient(dcoef)
+    rms_o = om.run(4)
+    m = pg.Mesh(nx, bnx, ng, leaves=leaves)
+    pm = pg.CompositeMultigrid(m, alpha=10.0, exact=True)
+    pm.set_coefficient(torch.from_numpy(dcoef).cuda())
+    u = torch.zeros(rhs.shape, dtype=torch.float64, device="cuda")
+    rms_p = pm.vcycles(u, torch.from_numpy(rhs).cuda(), 4)
+    assert np.array_equal(_interior(u.cpu().numpy(), ng), _interior(om.u(), ng))
+    np.testing.assert_allclose(rms_p, rms_o, rtol=1e-12, atol=0)
+
+
+def test_composite_face_coefficient_fast_mixed_bicgstab():
+    from meshes import region_coefficient
+    name, nx, bnx, ng, leaves = MG_CASES[1]
+    sim = O.OracleSim(nx, bnx, ng, leaves=leaves)
+    om = O.OracleMgBlocks(sim, alpha=10.0)
+    locs, geom = sim.block_info()
+    rhs = gaussian_rhs(locs, geom, bnx, ng)
+    dcoef = region_coefficient(locs, geom, bnx, ng)
+    om.rhs()[:] = rhs
+    om.set_coefficient(dcoef)
+    om.run(4)
+    ref4 = _interior(om.u(), ng).copy()
+    xo, it_o, _ = om.bicgstab(rhs, precondition=True, rtol=1e-10, max_iters=200)
+    m = pg.Mesh(nx, bnx, ng, leaves=leaves)
+    r = torch.from_numpy(rhs).cuda()
+    pm = pg.CompositeMultigrid(m, alpha=10.0)
+    pm.set_coefficient(torch.from_numpy(dcoef).cuda())
+    u = torch.zeros_like(r)
+    pm.vcycles(u, r, 4)
+    assert np.abs(_interior(u.cpu().numpy(), ng) - ref4).max() <= 1e-11 * np.abs(ref4).max()
+    u64 = torch.zeros_like(r)
+    c64, rel64 = pm.solve(u64, r, tol=1e-10)
+    u32 = torch.zeros_like(r)
+    c32, rel32 = pm.solve(u32, r, tol=1e-10, mixed=True)
+    assert rel64 <= 1e-10 and rel32 <= 1e-10 and c32 <= c64 + 2
+    ub = torch.zeros_like(r)
+    it, rms = pm.bicgstab(ub, r, precondition="fp64", rtol=1e-10, max_iters=200)
+    assert abs(it - it_o) <= 1
+    ref = _interior(xo, ng)
+    for x in (u64, u32, ub):
+        assert np.abs(_interior(x.cpu().numpy(), ng) - ref).max() <= 1e-8 * np.abs(ref).max()

@@ -89,3 +89,28 @@ def test_invalid_parameters_rejected():
         pg.CompositeMultigrid(m, stages=0)
     with pytest.raises(pg.NativeError):
         pg.CompositeMultigrid(m, coarse_sweeps=-1)
+
+
+def test_face_coefficient_constant_equals_constant_path():
+    # the face-coefficient operator with D = 2 on every face is the constant-D operator
+    from meshes import region_coefficient
+    name, nx, bnx, ng, leaves = MG_CASES[1]
+    a = O.OracleMgBlocks(O.OracleSim(nx, bnx, ng, leaves=leaves), alpha=10.0, D=2.0)
+    b = O.OracleMgBlocks(O.OracleSim(nx, bnx, ng, leaves=leaves), alpha=10.0, D=1.0)
+    locs, geom = a.sim.block_info()
+    r = gaussian_rhs(locs, geom, bnx, ng)
+    a.rhs()[:] = r
+    b.rhs()[:] = r
+    b.set_coefficient(region_coefficient(locs, geom, bnx, ng, inside=2.0, outside=2.0))
+    assert np.array_equal(a.run(3), b.run(3))
+    assert np.array_equal(a.u(), b.u())
+
+
+def test_face_coefficient_converges():
+    from meshes import region_coefficient
+    name, nx, bnx, ng, leaves = MG_CASES[1]
+    _, mg = _oracle(nx, bnx, ng, leaves, alpha=10.0)
+    locs, geom = mg.sim.block_info()
+    mg.set_coefficient(region_coefficient(locs, geom, bnx, ng, inside=10.0, outside=1.0))
+    rms = mg.run(8)
+    assert np.all(np.diff(rms) < 0) and rms[-1] < 1e-3 * rms[0]
