@@ -259,6 +259,9 @@ typedef struct {
   double alpha;            /* poisson/diagonal_alpha */
   int32_t exact;           /* 1: separately rounded reference-order arithmetic (bitwise);
                               0: FMA 7-point operator with the diagonal's reciprocal */
+  int32_t flux_correct;    /* poisson/flux_correct: flux correction inside Ax on the leaf
+                              grid (the outer residual and BiCGSTAB's operator); the
+                              composite grids' operator has none, as in the reference */
 } pgb_mg_params;
 /* Host only: builds the composite grids of the mesh (which must outlive the solver);
  * device memory is taken on the first solve. */

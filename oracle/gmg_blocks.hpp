@@ -45,6 +45,8 @@ struct BlockGmg {
     Field d[3];  // face coefficient D (x1, x2, x3 faces; face i is the low face of cell i)
   };
   bool varD = false;  // D set per face (set_coefficient); otherwise the constant p.D
+  bool flux_correct = false;  // poisson/flux_correct: flux correction inside Ax on the leaf grid
+  FluxField flux;             // leaf face fluxes when flux_correct
   std::map<int, Store> store;               // key 0: blocks of levels >= 0; key L < 0: level L
   std::map<int, std::vector<int>> slot;     // per grid: block index -> storage slot
   std::map<int, std::map<int, int>> index;  // per grid: gid -> block index
@@ -355,6 +357,48 @@ struct BlockGmg {
     }
   }
 
+  // Ax on the leaf grid with flux correction (poisson_equation.hpp:41-58, do_flux_cor):
+  // CalculateFluxes (each cell its low faces, the last cell also its high face), the
+  // flux-correction exchange (fine fluxes restricted onto the coarse side of every
+  // coarse/fine face), then FluxMultiplyMatrix. Without it, Ax is formed per cell.
+  void leaf_fluxes(Field &u) {
+    if (flux.f.empty()) {
+      flux.ncomp = 1;
+      for (int d = 0; d < 3; ++d) {
+        flux.N[d] = u.N[d];
+        flux.Nc[d] = u.Nc[d];
+      }
+      flux.f.assign((size_t)nleaf * flux.bs(), 0.0);
+      flux.fc.assign((size_t)nleaf * flux.cbs(), 0.0);
+    }
+    const int ng = m.p.ng;
+    for (int b = 0; b < nleaf; ++b) {
+      const Block &blk = m.blocks[b];
+      const double dx1 = blk.coords.dx[0], dx2 = blk.coords.dx[1], dx3 = blk.coords.dx[2];
+      interior(blk, [&](int k, int j, int i) {
+        double D6[6];
+        faceD(b, k, j, i, D6);
+        const double uc = u.at(b, 0, k, j, i);
+        flux.at(b, 0, 0, k, j, i) = D6[0] / dx1 * (u.at(b, 0, k, j, i - 1) - uc);
+        if (i == ng + blk.nx[0] - 1) flux.at(b, 0, 0, k, j, i + 1) = D6[1] / dx1 * (uc - u.at(b, 0, k, j, i + 1));
+        flux.at(b, 1, 0, k, j, i) = D6[2] * (u.at(b, 0, k, j - 1, i) - uc) / dx2;
+        if (j == ng + blk.nx[1] - 1) flux.at(b, 1, 0, k, j + 1, i) = D6[3] * (uc - u.at(b, 0, k, j + 1, i)) / dx2;
+        flux.at(b, 2, 0, k, j, i) = D6[4] * (u.at(b, 0, k - 1, j, i) - uc) / dx3;
+        if (k == ng + blk.nx[2] - 1) flux.at(b, 2, 0, k + 1, j, i) = D6[5] * (uc - u.at(b, 0, k + 1, j, i)) / dx3;
+      });
+    }
+    flux_correction(flux, m, m.blocks);
+  }
+  double leaf_ax(Field &u, int b, const Block &blk, int k, int j, int i) {
+    if (!flux_correct) return ax(u, b, blk, k, j, i);
+    const double dx1 = blk.coords.dx[0], dx2 = blk.coords.dx[1], dx3 = blk.coords.dx[2];
+    double out = -p.alpha * u.at(b, 0, k, j, i);
+    out += (flux.at(b, 0, 0, k, j, i) - flux.at(b, 0, 0, k, j, i + 1)) / dx1;
+    out += (flux.at(b, 1, 0, k, j, i) - flux.at(b, 1, 0, k, j + 1, i)) / dx2;
+    out += (flux.at(b, 2, 0, k, j, i) - flux.at(b, 2, 0, k + 1, j, i)) / dx3;
+    return out;
+  }
+
   // Leaf-grid residual of MGSolver::AddTasks: exchange, res_err = rhs - A u, sum of
   // squares over the leaf interiors in block, k, j, i order
   double residual() {
@@ -362,11 +406,12 @@ struct BlockGmg {
     bind(S, &leaf_slot);
     cur_d = S.d;
     exchange(S.u, m.blocks, BAny, 0, leaf_recs, true, PLinear, m.multilevel);
+    if (flux_correct) leaf_fluxes(S.u);
     double s = 0.0;
     for (int b = 0; b < nleaf; ++b) {
       const Block &blk = m.blocks[b];
       interior(blk, [&](int k, int j, int i) {
-        const double t = ax(S.u, b, blk, k, j, i);
+        const double t = leaf_ax(S.u, b, blk, k, j, i);
         const double r = 1.0 * S.rhs.at(b, 0, k, j, i) + -1.0 * t;
         S.res.at(b, 0, k, j, i) = r;
         s += r * r;
@@ -449,8 +494,9 @@ struct BlockGmg {
     Store &S = store.at(0);
     leaf_cells([&](int64_t q, int b, int k, int j, int i) { S.u.at(b, 0, k, j, i) = u[q]; });
     exchange(S.u, m.blocks, BAny, 0, leaf_recs, true, PLinear, m.multilevel);
+    if (flux_correct) leaf_fluxes(S.u);
     v.resize(u.size());
-    leaf_cells([&](int64_t q, int b, int k, int j, int i) { v[q] = ax(S.u, b, m.blocks[b], k, j, i); });
+    leaf_cells([&](int64_t q, int b, int k, int j, int i) { v[q] = leaf_ax(S.u, b, m.blocks[b], k, j, i); });
   }
   // out <- M b: rhs <- b, u <- 0 on the leaves, one V-cycle (bicgstab_solver.hpp:175-184)
   void precondition(const std::vector<double> &bv, std::vector<double> &out) {

@@ -1484,6 +1484,9 @@ double orc_mgb_residual(void *h) {
   BlockGmg *g = (BlockGmg *)h;
   return std::sqrt(g->residual() / g->ncells());
 }
+// poisson/flux_correct: flux correction inside Ax on the leaf grid
+void orc_mgb_set_flux_correct(void *h, int on) { ((BlockGmg *)h)->flux_correct = on != 0; }
+
 // face coefficient D of the leaves, [nleaf][3][N3][N2][N1] (face i the low face of cell i)
 void orc_mgb_set_coefficient(void *h, const double *d) { ((BlockGmg *)h)->set_coefficient(d); }
 

@@ -37,7 +37,7 @@ class GmgParams(ctypes.Structure):
 class MgParams(ctypes.Structure):
     _fields_ = [("stages", ctypes.c_int32), ("jacobi", ctypes.c_int32), ("weight", ctypes.c_double),
                 ("coarse_sweeps", ctypes.c_int32), ("max_coarsenings", ctypes.c_int32), ("D", ctypes.c_double),
-                ("alpha", ctypes.c_double), ("exact", ctypes.c_int32)]
+                ("alpha", ctypes.c_double), ("exact", ctypes.c_int32), ("flux_correct", ctypes.c_int32)]
 
 
 class StageParams(ctypes.Structure):

@@ -49,6 +49,7 @@ MeshState *mesh_state(pgb_mesh *m);
 int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int prolongate, int prolong_op,
                   double *buffer, cudaStream_t s, const SparseDev *sp);
 int exchange_grid_f32(GridTables &t, float *fine, float *coarse, cudaStream_t s);
+int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s, const SparseDev *sp);
 }  // namespace pgb
 
 using namespace pgb;
@@ -757,6 +758,86 @@ __global__ void __launch_bounds__(256) k_bi_p(const double *__restrict__ r, cons
   });
 }
 
+// ---- flux correction inside Ax on the leaf grid (poisson/flux_correct,
+// poisson_equation.hpp:41-58): CalculateFluxes (each cell its low faces, the last cell of
+// a row also its high face; fluxes [block][dir][N3][N2][N1], face i the low face of cell
+// i), the flux-correction exchange (exchange.cu), then FluxMultiplyMatrix. The reference's
+// order and divisions, in both builds.
+__global__ void __launch_bounds__(256) k_mg_leaf_fluxes(const double *__restrict__ u, double *__restrict__ F,
+                                                        int nleaf, Dims d, const MgCoef *__restrict__ lc, MgOp o,
+                                                        FaceD<double> fd) {
+  pdl_enter();
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1], cs = sk * d.N[2];
+  const int hi0 = d.ng + d.nx[0] - 1, hi1 = d.ng + d.nx[1] - 1, hi2 = d.ng + d.nx[2] - 1;
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t c = cell_of(d, b, k, j, i);
+    const int64_t cf0 = ((int64_t)b * 3) * cs + (c - (int64_t)b * cs);
+    double D6[6];
+    face_d6(fd, c, sj, sk, o.D, D6);
+    const double *dx = lc[b].dx;
+    const double uc = u[c];
+    F[cf0] = div_rn(D6[0], dx[0]) * (u[c - 1] - uc);
+    if (i == hi0) F[cf0 + 1] = div_rn(D6[1], dx[0]) * (uc - u[c + 1]);
+    F[cf0 + cs] = div_rn(D6[2] * (u[c - sj] - uc), dx[1]);
+    if (j == hi1) F[cf0 + cs + sj] = div_rn(D6[3] * (uc - u[c + sj]), dx[1]);
+    F[cf0 + 2 * cs] = div_rn(D6[4] * (u[c - sk] - uc), dx[2]);
+    if (k == hi2) F[cf0 + 2 * cs + sk] = div_rn(D6[5] * (uc - u[c + sk]), dx[2]);
+  });
+}
+
+// FluxMultiplyMatrix: A u = -alpha u + sum_d (F_low - F_high) / dx_d
+__device__ __forceinline__ double flux_div(const double *__restrict__ F, const double *__restrict__ u, int64_t c,
+                                          int b, const Dims &d, const double *dx, double alpha) {
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1], cs = sk * d.N[2];
+  const int64_t f = ((int64_t)b * 3) * cs + (c - (int64_t)b * cs);
+  double out = -alpha * u[c];
+  out += div_rn(F[f] - F[f + 1], dx[0]);
+  out += div_rn(F[f + cs] - F[f + cs + sj], dx[1]);
+  out += div_rn(F[f + 2 * cs] - F[f + 2 * cs + sk], dx[2]);
+  return out;
+}
+
+// the leaf residual (as k_mg_leaf_residual) from the corrected fluxes
+__global__ void __launch_bounds__(kResThreads) k_mg_leaf_residual_flux(StoreView<double> s, int nleaf,
+                                                                       const MgCoef *__restrict__ lc, MgOp o,
+                                                                       const double *__restrict__ F,
+                                                                       double *__restrict__ partial,
+                                                                       float *__restrict__ rhs32,
+                                                                       float *__restrict__ u32) {
+  pdl_enter();
+  __shared__ double sh[kResThreads / 32];
+  double acc = 0.0;
+  for_interior(nullptr, nleaf, s.d, [&](int, int b, int k, int j, int i) {
+    const int64_t c = cell_of(s.d, b, k, j, i);
+    const double r = s.rhs[c] - flux_div(F, s.u, c, b, s.d, lc[b].dx, o.alpha);
+    s.res[c] = r;
+    acc += r * r;
+    if (rhs32) {
+      rhs32[c] = (float)r;
+      u32[c] = 0.0f;
+    }
+  });
+  for (int w = 16; w > 0; w >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, w);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kResThreads / 32; ++w) t += sh[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// BiCGSTAB's A u from the corrected fluxes
+__global__ void __launch_bounds__(256) k_bi_apply_flux(const double *__restrict__ u, double *__restrict__ out,
+                                                       int nleaf, Dims d, const MgCoef *__restrict__ lc, MgOp o,
+                                                       const double *__restrict__ F) {
+  pdl_enter();
+  for_interior(nullptr, nleaf, d, [&](int, int b, int k, int j, int i) {
+    const int64_t c = cell_of(d, b, k, j, i);
+    out[c] = flux_div(F, u, c, b, d, lc[b].dx, o.alpha);
+  });
+}
+
 unsigned grid_for(int64_t work) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 16));
 }
@@ -769,6 +850,8 @@ struct pgb_mg {
   MeshTopology *topo = nullptr;
   GmgConfig cfg;
   bool exact = true;  // reference-order arithmetic (bitwise) or the FMA 7-point build
+  bool flux_correct = false;   // poisson/flux_correct on the leaf grid
+  double *lflux = nullptr;     // leaf face fluxes [nleaf][3][N3][N2][N1] (flux_correct)
   int max_coarsenings = 30;
   int lmin = 0, lmax = 0, nleaf = 0;
   struct Store {
@@ -1094,6 +1177,13 @@ int mg_upload(pgb_mg *g) {
     kv.second.nbr = reinterpret_cast<int *>(base + o.nbr);
   }
   g->leaf_coef = reinterpret_cast<MgCoef *>(static_cast<char *>(g->lists) + lc_off);
+  if (g->flux_correct) {
+    const Dims &dl = g->stores.at(0).dims;
+    const int64_t nf = (int64_t)g->nleaf * 3 * dl.N[0] * dl.N[1] * dl.N[2];
+    PGB_CUDA(cudaMalloc((void **)&g->lflux, nf * sizeof(double)));
+    PGB_CUDA(cudaMemset(g->lflux, 0, nf * sizeof(double)));
+    g->allocs.push_back(g->lflux);
+  }
   const Dims &d0 = g->stores.at(0).dims;
   g->nparts = (int)grid_for((int64_t)g->nleaf * d0.nx[0] * d0.nx[1] * d0.nx[2]);
   PGB_CUDA(cudaMalloc((void **)&g->partial, g->nparts * sizeof(double)));
@@ -1312,6 +1402,18 @@ int leaf_residual_t(pgb_mg *g, bool mixed, cudaStream_t s) {
   pgb_mg::Store &S = g->stores.at(0);
   int rc = exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr);
   if (rc) return rc;
+  if (g->flux_correct) {
+    const unsigned grid = grid_for((int64_t)g->nleaf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]);
+    const MgOp o{g->cfg.D, g->cfg.alpha};
+    PGB_TRY(launch_pdl(k_mg_leaf_fluxes, grid, 256, s, (const double *)S.u, g->lflux, g->nleaf, S.dims,
+                       (const MgCoef *)g->leaf_coef, o, S.template fd<double>()));
+    PGB_TRY(flux_correct_grid(g->leaf_tab, g->lflux, 1, s, nullptr));
+    PGB_TRY(launch_pdl(k_mg_leaf_residual_flux, g->nparts, kResThreads, s, S.template view<double>(), g->nleaf,
+                       (const MgCoef *)g->leaf_coef, o, (const double *)g->lflux, g->partial,
+                       mixed ? S.rhs32 : nullptr, mixed ? S.u32 : nullptr));
+    PGB_CUDA(cudaMemcpyAsync(g->partial_h, g->partial, g->nparts * sizeof(double), cudaMemcpyDeviceToHost, s));
+    return kOk;
+  }
   PGB_TRY(launch_pdl(k_mg_leaf_residual<kFast>, g->nparts, kResThreads, s, S.template view<double>(), g->nleaf, g->leaf_coef,
                                                               MgOp{g->cfg.D, g->cfg.alpha}, S.template fd<double>(), g->partial,
                                                               mixed ? S.rhs32 : nullptr, mixed ? S.u32 : nullptr));
@@ -1387,6 +1489,14 @@ int bicg_apply(pgb_mg *g, double *out, cudaStream_t s) {
   pgb_mg::Store &S = g->stores.at(0);
   PGB_TRY(exchange_grid(g->leaf_tab, S.u, S.coarse, 1, 1, prolong_op(g), nullptr, s, nullptr));
   const unsigned grid = grid_for((int64_t)g->nleaf * S.dims.nx[0] * S.dims.nx[1] * S.dims.nx[2]);
+  if (g->flux_correct) {
+    const MgOp o{g->cfg.D, g->cfg.alpha};
+    PGB_TRY(launch_pdl(k_mg_leaf_fluxes, grid, 256, s, (const double *)S.u, g->lflux, g->nleaf, S.dims,
+                       (const MgCoef *)g->leaf_coef, o, S.template fd<double>()));
+    PGB_TRY(flux_correct_grid(g->leaf_tab, g->lflux, 1, s, nullptr));
+    return launch_pdl(k_bi_apply_flux, grid, 256, s, (const double *)S.u, out, g->nleaf, S.dims,
+                      (const MgCoef *)g->leaf_coef, o, (const double *)g->lflux);
+  }
   return launch_pdl(k_bi_apply, grid, 256, s, (const double *)S.u, out, g->nleaf, S.dims,
                     (const MgCoef *)g->leaf_coef, MgOp{g->cfg.D, g->cfg.alpha}, S.template fd<double>());
 }
@@ -1517,6 +1627,7 @@ int pgb_mg_create(pgb_mesh *mesh, const pgb_mg_params *p, pgb_mg **out) {
   g->cfg.D = p->D;
   g->cfg.alpha = p->alpha;
   g->exact = p->exact != 0;
+  g->flux_correct = p->flux_correct != 0;
   g->max_coarsenings = p->max_coarsenings;
   int rc;
   try {

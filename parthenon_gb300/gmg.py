@@ -96,9 +96,10 @@ class CompositeMultigrid:
     """
 
     def __init__(self, mesh, stages=2, jacobi=False, weight=2.0 / 3.0, coarse_sweeps=0, max_coarsenings=30,
-                 D=1.0, alpha=0.0, exact=False):
+                 D=1.0, alpha=0.0, exact=False, flux_correct=False):
         p = nat.MgParams()
         p.exact = int(bool(exact))
+        p.flux_correct = int(bool(flux_correct))
         p.stages, p.jacobi, p.weight = int(stages), int(bool(jacobi)), float(weight)
         p.coarse_sweeps, p.max_coarsenings = int(coarse_sweeps), int(max_coarsenings)
         p.D, p.alpha = float(D), float(alpha)

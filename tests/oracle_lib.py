@@ -355,6 +355,7 @@ def _mgb_lib():
                                        ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         L.orc_mgb_bicgstab.restype = ctypes.c_int
         L.orc_mgb_set_coefficient.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_mgb_set_flux_correct.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L._mgb_ready = True
     return L
 
@@ -366,13 +367,14 @@ class OracleMgBlocks:
     [block][k][j][i] with ghosts; the multigrid's internal blocks are private."""
 
     def __init__(self, sim, stages=2, jacobi=False, weight=2.0 / 3.0, coarse_sweeps=0, max_coarsenings=30,
-                 D=1.0, alpha=0.0):
+                 D=1.0, alpha=0.0, flux_correct=False):
         L = _mgb_lib()
         self.sim = sim  # the mesh must outlive the solver
         self.h = L.orc_mgb_create(sim.h, int(stages), int(bool(jacobi)), float(weight), int(coarse_sweeps),
                                   int(max_coarsenings), float(D), float(alpha))
         if not self.h:
             raise RuntimeError("oracle multigrid construction failed")
+        L.orc_mgb_set_flux_correct(self.h, int(bool(flux_correct)))
         info = np.zeros(4, np.int32)
         L.orc_mgb_info(self.h, _ptr(info))
         self.lmin, self.lmax, self.nslots, self.nleaf = (int(x) for x in info)

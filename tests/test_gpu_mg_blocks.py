@@ -203,3 +203,39 @@ def test_composite_face_coefficient_fast_mixed_bicgstab():
     ref = _interior(xo, ng)
     for x in (u64, u32, ub):
         assert np.abs(_interior(x.cpu().numpy(), ng) - ref).max() <= 1e-8 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("case", [MG_CASES[1], MG_CASES[2], MG_CASES[4]], ids=[MG_CASES[i][0] for i in (1, 2, 4)])
+def test_composite_flux_correct(case):
+    # poisson/flux_correct: the leaf-grid operator (outer residual, BiCGSTAB) with flux
+    # correction at coarse/fine faces. The V-cycle's own operator has none, so the
+    # V-cycle iteration stalls at its fixed point while BiCGSTAB converges, at alpha = 0
+    # too (the corrected operator is conservative).
+    name, nx, bnx, ng, leaves = case
+    for alpha in (10.0, 0.0):
+        sim = O.OracleSim(nx, bnx, ng, leaves=leaves)
+        om = O.OracleMgBlocks(sim, alpha=alpha, flux_correct=True)
+        locs, geom = sim.block_info()
+        rhs = gaussian_rhs(locs, geom, bnx, ng)
+        om.rhs()[:] = rhs
+        rms_o = om.run(3)
+        m = pg.Mesh(nx, bnx, ng, leaves=leaves)
+        r = torch.from_numpy(rhs).cuda()
+        pe = pg.CompositeMultigrid(m, alpha=alpha, exact=True, flux_correct=True)
+        u = torch.zeros_like(r)
+        rms_p = pe.vcycles(u, r, 3)
+        np.testing.assert_allclose(rms_p, rms_o, rtol=1e-12, atol=0)
+        xo, it_o, _ = O.OracleMgBlocks(O.OracleSim(nx, bnx, ng, leaves=leaves), alpha=alpha,
+                                       flux_correct=True).bicgstab(rhs, rtol=1e-10, max_iters=100)
+        pf = pg.CompositeMultigrid(m, alpha=alpha, flux_correct=True)
+        ub = torch.zeros_like(r)
+        it, rms = pf.bicgstab(ub, r, precondition="fp64", rtol=1e-10, max_iters=100)
+        assert it < 100 and abs(it - it_o) <= 1
+        ref = _interior(xo, ng)
+        if alpha == 0.0:  # defined up to a constant
+            ref = ref - ref.mean()
+            got = _interior(ub.cpu().numpy(), ng)
+            got = got - got.mean()
+        else:
+            got = _interior(ub.cpu().numpy(), ng)
+        assert np.abs(got - ref).max() <= 1e-7 * np.abs(ref).max()
