@@ -1,4 +1,4 @@
-// Multigrid on the two-level composite grids of a refined mesh (FP64).
+// Multigrid on the two-level composite grids of a refined mesh.
 //
 // MGSolver on a mesh with refinement (src/solvers/mg_solver.hpp:119-520) runs its FAS
 // V-cycle over the grids of src/mesh/mesh-gmg.cpp:103-201: grid L holds every block of
@@ -12,21 +12,27 @@
 // res_err, rhs, temp, u0) with ghosts, one component, x fastest; the blocks below level
 // 0 are smaller and have a store per level. A leaf in two grids is one slot, as the
 // reference shares the MeshBlock between the two lists, so nothing moves between grids
-// but the restriction and the prolongation. Each grid's gmg_same exchange runs the
+// but the restriction and the prolongation. A grid with coarse/fine faces runs the
 // leaf-grid exchange kernels (exchange.cu) on tables whose block indices are store
-// slots.
+// slots; a grid of one level reads its blocks' face neighbours directly instead.
 //
-// Fused steps per level: Ax + Jacobi, Ax + residual, Ax + FAS right-hand side; the
-// restriction of u and res_err writes the parent's octant directly (the child's coarse
-// buffer and the message buffer hold the same values); the linear prolongation of
-// res_err is added straight into u over the child's interior. The values the reference
-// also prolongates into the child's ghosts, and the child's res_err after the update,
-// are never read again and are not written. Every read of a ghost cell follows an
-// exchange that writes it. One V-cycle plus the leaf-grid residual is one CUDA graph.
+// Fused steps per level: Ax + Jacobi, Ax + residual, u0 copy + Ax + FAS right-hand
+// side; the restriction of u and res_err writes the parent's octant directly (the
+// child's coarse buffer and the message buffer hold the same values); the linear
+// prolongation of res_err is added straight into u over the child's interior. The values
+// the reference also prolongates into the child's ghosts, and the child's res_err after
+// the update, are never read again and are not written. Every read of a ghost cell
+// follows an exchange that writes it. One solver iteration (V-cycle plus leaf-grid
+// residual, or one BiCGSTAB iteration) is one CUDA graph whose kernels use programmatic
+// dependent launch.
 //
-// The file is compiled with -fmad=false and divides by powers of two as exact
-// multiplications (div_rn), so every value rounds as in the reference's host arithmetic
-// and the interiors are bitwise those of the CPU restatement.
+// Builds: exact (reference expression order, separately rounded: this file is compiled
+// with -fmad=false and divides by powers of two as exact multiplications, so interiors
+// are bitwise those of the CPU restatement) and fast (FMA, the 7-point form, the
+// diagonal's reciprocal). The mixed solve runs the V-cycle on FP32 copies of the stores
+// inside FP64 iterative refinement. Also here: the package's face coefficient D
+// (restricted by the setup step), flux correction inside the leaf-grid operator, and
+// BiCGSTAB with the V-cycle as preconditioner (src/solvers/bicgstab_solver.hpp:116-315).
 #include <cuda_runtime.h>
 
 #include <algorithm>
