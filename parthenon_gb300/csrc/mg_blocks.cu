@@ -263,76 +263,191 @@ __device__ __forceinline__ void fast_op(const Faces<T> &f, const MgCoef &cf, con
 }
 
 // Jacobi sweep (mg_solver.hpp:222-297): dst = w ratio(rhs - (A src - dg src), dg) + (1 - w) src
+// ---- per-cell steps, shared by the grid kernels below and the one-CTA coarse end
+
+// Jacobi sweep (mg_solver.hpp:222-297): dst = w ratio(rhs - (A src - dg src), dg) + (1 - w) src
+template <bool kFast, class T>
+__device__ __forceinline__ void jacobi_cell(const T *__restrict__ src, const T *__restrict__ rhs, T *__restrict__ dst,
+                                            const Dims &d, const int *__restrict__ nb, const MgCoef &cf,
+                                            const MgOp &o, const MgSweep &sw, const FaceD<T> &fd, int b, int k,
+                                            int j, int i) {
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
+  const int64_t c = cell_of(d, b, k, j, i);
+  const Faces<T> f = faces(src, d, nb, b, k, j, i);
+  if constexpr (kFast) {
+    T off, dg;
+    fast_op(f, cf, o, fd, c, sj, sk, off, dg);
+    if (fd.d0) {
+      const T small = (T)10 * (sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN);
+      const T den = dg + (dg >= (T)0 ? (T)1 : (T)-1) * small;
+      dst[c] = fma_t((T)sw.w / den, rhs[c] - off, (T)sw.omw * f.c);
+    } else {
+      dst[c] = fma_t((T)sw.wd, rhs[c] - off, (T)sw.omw * f.c);
+    }
+  } else {
+    const ExactOp e = exact_op(f, cf, o, fd, c, sj, sk);
+    const double off = e.ax - e.dg * f.c;
+    const double val = rhs[c] - off;
+    dst[c] = sw.w * div_rn(val, e.den) + sw.omw * f.c;
+  }
+}
+
+// Ax + AddFieldsAndStoreInteriorSelect<rhs, temp, res_err>(1, -1): res = rhs - A u
+template <bool kFast, class T>
+__device__ __forceinline__ void residual_cell(const StoreView<T> &s, const int *__restrict__ nb, const MgCoef &cf,
+                                              const MgOp &o, const FaceD<T> &fd, int b, int k, int j, int i) {
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
+  const int64_t c = cell_of(s.d, b, k, j, i);
+  const Faces<T> f = faces(s.u, s.d, nb, b, k, j, i);
+  if constexpr (kFast) {
+    T off, dg;
+    fast_op(f, cf, o, fd, c, sj, sk, off, dg);
+    s.res[c] = fma_t(-dg, f.c, s.rhs[c] - off);
+  } else {
+    s.res[c] = s.rhs[c] - exact_op(f, cf, o, fd, c, sj, sk).ax;
+  }
+}
+
+// Start of a level below the finest (mg_solver.hpp:405-430): u0 = u and, on internal
+// blocks, the FAS right-hand side rhs = A u + res_err
+template <bool kFast, class T>
+__device__ __forceinline__ void fas_cell(const StoreView<T> &s, bool internal, const int *__restrict__ nb,
+                                         const MgCoef &cf, const MgOp &o, const FaceD<T> &fd, int b, int k, int j,
+                                         int i) {
+  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
+  const int64_t c = cell_of(s.d, b, k, j, i);
+  const T uc = s.u[c];
+  s.u0[c] = uc;
+  if (!internal) return;
+  const Faces<T> f = faces(s.u, s.d, nb, b, k, j, i);
+  if constexpr (kFast) {
+    T off, dg;
+    fast_op(f, cf, o, fd, c, sj, sk, off, dg);
+    s.rhs[c] = fma_t(dg, uc, off + s.res[c]);
+  } else {
+    s.rhs[c] = exact_op(f, cf, o, fd, c, sj, sk).ax + s.res[c];
+  }
+}
+
+// RestrictAverage (pr_ops.hpp:105-164) of the child's interior, u and res_err, into the
+// parent's octant (gmg_restrict_send + gmg_restrict_recv), one parent cell. FP64
+// children: the reference's volume-weighted form; FP32 children (the mixed V-cycle): the
+// mean of the eight cells. TP is the parent's type.
+template <class TC, class TP>
+__device__ __forceinline__ void restrict_cell(const StoreView<TC> &cs, const StoreView<TP> &ps, const MgXfer &t,
+                                              double vol, int ci, int cjj, int ckk) {
+  const int ng = cs.d.ng;
+  const int64_t cj = cs.d.N[0], ck = (int64_t)cs.d.N[0] * cs.d.N[1];
+  const int64_t f = cell_of(cs.d, t.child, 2 * ckk + ng, 2 * cjj + ng, 2 * ci + ng);
+  const int64_t p = cell_of(ps.d, t.parent, t.lo[2] + ckk, t.lo[1] + cjj, t.lo[0] + ci);
+#pragma unroll
+  for (int v = 0; v < 2; ++v) {
+    const TC *__restrict__ a = v == 0 ? cs.u : cs.res;
+    TP out;
+    if constexpr (sizeof(TC) == 8) {
+      const double tv = ((vol + vol) + (vol + vol)) + ((vol + vol) + (vol + vol));
+      // t[ok][oj][oi] = vol * fine(k + ok, j + oj, i + oi)
+      const double t000 = vol * a[f], t001 = vol * a[f + 1];
+      const double t010 = vol * a[f + cj], t011 = vol * a[f + cj + 1];
+      const double t100 = vol * a[f + ck], t101 = vol * a[f + ck + 1];
+      const double t110 = vol * a[f + ck + cj], t111 = vol * a[f + ck + cj + 1];
+      const double num = ((t000 + t010) + (t001 + t011)) + ((t100 + t110) + (t101 + t111));
+      out = (TP)div_rn(num, tv);
+    } else {
+      const TC sum = ((a[f] + a[f + cj]) + (a[f + 1] + a[f + cj + 1])) +
+                     ((a[f + ck] + a[f + ck + cj]) + (a[f + ck + 1] + a[f + ck + cj + 1]));
+      out = (TP)((TC)0.125 * sum);
+    }
+    (v == 0 ? ps.u : ps.res)[p] = out;
+  }
+}
+
+// ProlongateSharedLinear (pr_ops.hpp:166-285) of the parent's res_err (its octant with
+// ghosts is the child's coarse buffer) and AddFieldsAndStore<u, res_err, u>, one coarse
+// cell of the child's interior (eight fine cells). The exact build forms the slopes from
+// the cell-centre coordinates as the reference does (g: the child's geometry); the fast
+// build uses the uniform-spacing value dx_fine / 2 / dx_coarse = 1/4 of each difference.
+// TC is the child's type (the arithmetic), TP the parent's.
+template <bool kFast, class TC, class TP>
+__device__ __forceinline__ void prolong_add_cell(const StoreView<TC> &cs, const StoreView<TP> &ps, const MgXfer &t,
+                                                 const DevBlockGeom *__restrict__ g, int c0, int c1, int c2) {
+  const int ng = cs.d.ng;
+  const int64_t pj = ps.d.N[0], pk = (int64_t)ps.d.N[0] * ps.d.N[1];
+  const int64_t N0 = cs.d.N[0], N01 = (int64_t)cs.d.N[0] * cs.d.N[1];
+  const int c[3] = {c0 + ng, c1 + ng, c2 + ng};  // coarse-buffer index
+  const int f[3] = {2 * c0 + ng, 2 * c1 + ng, 2 * c2 + ng};
+  const int p[3] = {t.lo[0] + c0, t.lo[1] + c1, t.lo[2] + c2};
+  const int64_t pe = cell_of(ps.d, t.parent, p[2], p[1], p[0]);
+  const TC fc = (TC)ps.res[pe];
+  // the parent's cells next to p along d: its ghosts, or on a grid read directly the
+  // face neighbour's interior cell
+  auto side = [&](int d, int s) -> TC {
+    const int64_t st = d == 0 ? 1 : (d == 1 ? pj : pk);
+    const int lo = ps.d.ng, hi = ps.d.ng + ps.d.nx[d] - 1;
+    if (t.pnb[0] < 0 || (s < 0 ? p[d] > lo : p[d] < hi)) return (TC)ps.res[pe + s * st];
+    int q[3] = {p[0], p[1], p[2]};
+    q[d] = s < 0 ? hi : lo;
+    return (TC)ps.res[cell_of(ps.d, t.pnb[2 * d + (s > 0)], q[2], q[1], q[0])];
+  };
+  TC mq[3], pq[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if constexpr (kFast) {
+      mq[d] = (TC)0.25 * (fc - side(d, -1));
+      pq[d] = (TC)0.25 * (side(d, 1) - fc);
+    } else {
+      auto xcc = [&](int idx) { return g->cxmin[d] + ((double)idx + 0.5) * g->cdx[d]; };
+      auto xfc = [&](int idx) { return g->xmin[d] + ((double)idx + 0.5) * g->dx[d]; };
+      const double xm = xcc(c[d] - 1), xc = xcc(c[d]), xp = xcc(c[d] + 1);
+      const double dxm = xc - xm, dxp = xp - xc;
+      const double dfm = xc - xfc(f[d]);
+      const double dfp = xfc(f[d] + 1) - xc;
+      mq[d] = div_rn(fc - side(d, -1), dxm) * dfm;
+      pq[d] = div_rn(side(d, 1) - fc, dxp) * dfp;
+    }
+  }
+  const TC m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
+  TC *U = cs.u + cell_of(cs.d, t.child, f[2], f[1], f[0]);
+  U[0] = U[0] + (fc - ((m0 + m1) + m2));
+  U[1] = U[1] + (fc + ((p0 - m1) - m2));
+  U[N0] = U[N0] + (fc - ((m0 - p1) + m2));
+  U[N0 + 1] = U[N0 + 1] + (fc + ((p0 + p1) - m2));
+  U[N01] = U[N01] + (fc - ((m0 + m1) - p2));
+  U[N01 + 1] = U[N01 + 1] + (fc + ((p0 - m1) + p2));
+  U[N01 + N0] = U[N01 + N0] + (fc - ((m0 - p1) - p2));
+  U[N01 + N0 + 1] = U[N01 + N0 + 1] + (fc + ((p0 + p1) + p2));
+}
+
+// ---- grid kernels: every interior cell of the listed blocks
+
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_jacobi(const T *__restrict__ src, const T *__restrict__ rhs,
                                                    T *__restrict__ dst, const int *__restrict__ list, int n,
                                                    const int *__restrict__ nbr, Dims d, MgCoef cf, MgOp o,
                                                    MgSweep sw, FaceD<T> fd) {
   pdl_enter();
-  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
   for_interior(list, n, d, [&](int q, int b, int k, int j, int i) {
-    const int64_t c = cell_of(d, b, k, j, i);
-    const Faces<T> f = faces(src, d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
-    if constexpr (kFast) {
-      T off, dg;
-      fast_op(f, cf, o, fd, c, sj, sk, off, dg);
-      if (fd.d0) {
-        const T small = (T)10 * (sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN);
-        const T den = dg + (dg >= (T)0 ? (T)1 : (T)-1) * small;
-        dst[c] = fma_t((T)sw.w / den, rhs[c] - off, (T)sw.omw * f.c);
-      } else {
-        dst[c] = fma_t((T)sw.wd, rhs[c] - off, (T)sw.omw * f.c);
-      }
-    } else {
-      const ExactOp e = exact_op(f, cf, o, fd, c, sj, sk);
-      const double off = e.ax - e.dg * f.c;
-      const double val = rhs[c] - off;
-      dst[c] = sw.w * div_rn(val, e.den) + sw.omw * f.c;
-    }
+    jacobi_cell<kFast>(src, rhs, dst, d, nbr ? nbr + 6 * q : nullptr, cf, o, sw, fd, b, k, j, i);
   });
 }
 
-// Ax + AddFieldsAndStoreInteriorSelect<rhs, temp, res_err>(1, -1): res = rhs - A u
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_residual(StoreView<T> s, const int *__restrict__ list, int n,
                                                      const int *__restrict__ nbr, MgCoef cf, MgOp o,
                                                      FaceD<T> fd) {
   pdl_enter();
-  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
   for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
-    const int64_t c = cell_of(s.d, b, k, j, i);
-    const Faces<T> f = faces(s.u, s.d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
-    if constexpr (kFast) {
-      T off, dg;
-      fast_op(f, cf, o, fd, c, sj, sk, off, dg);
-      s.res[c] = fma_t(-dg, f.c, s.rhs[c] - off);
-    } else {
-      s.res[c] = s.rhs[c] - exact_op(f, cf, o, fd, c, sj, sk).ax;
-    }
+    residual_cell<kFast>(s, nbr ? nbr + 6 * q : nullptr, cf, o, fd, b, k, j, i);
   });
 }
 
-// Start of a level below the finest (mg_solver.hpp:405-430): u0 = u on every fine block
-// and, on the first nint (internal) blocks of the list, the FAS right-hand side
-// rhs = A u + res_err
+// the first nint blocks of the list are the internal ones
 template <bool kFast, class T>
 __global__ void __launch_bounds__(256) k_mg_fas(StoreView<T> s, const int *__restrict__ list, int n, int nint,
                                                 const int *__restrict__ nbr, MgCoef cf, MgOp o, FaceD<T> fd) {
   pdl_enter();
-  const int64_t sj = s.d.N[0], sk = (int64_t)s.d.N[0] * s.d.N[1];
   for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
-    const int64_t c = cell_of(s.d, b, k, j, i);
-    const T uc = s.u[c];
-    s.u0[c] = uc;
-    if (q >= nint) return;
-    const Faces<T> f = faces(s.u, s.d, nbr ? nbr + 6 * q : nullptr, b, k, j, i);
-    if constexpr (kFast) {
-      T off, dg;
-      fast_op(f, cf, o, fd, c, sj, sk, off, dg);
-      s.rhs[c] = fma_t(dg, uc, off + s.res[c]);
-    } else {
-      s.rhs[c] = exact_op(f, cf, o, fd, c, sj, sk).ax + s.res[c];
-    }
+    fas_cell<kFast>(s, q < nint, nbr ? nbr + 6 * q : nullptr, cf, o, fd, b, k, j, i);
   });
 }
 
@@ -357,55 +472,22 @@ __global__ void __launch_bounds__(256) k_mg_error(StoreView<T> s, const int *__r
   });
 }
 
-// RestrictAverage (pr_ops.hpp:105-164) of the child's interior, u and res_err, into the
-// parent's octant (gmg_restrict_send + gmg_restrict_recv). One thread per parent cell.
-// FP64 children: the reference's volume-weighted form; FP32 children (the mixed
-// V-cycle): the mean of the eight cells. TP is the parent's type.
+// restriction of every fine block of a grid into its parent: one thread per parent cell
 template <class TC, class TP>
 __global__ void __launch_bounds__(256) k_mg_restrict(StoreView<TC> cs, StoreView<TP> ps, const MgXfer *__restrict__ x,
                                                      int n, const DevBlockGeom *__restrict__ cgeom) {
   pdl_enter();
   const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
   const int per = h0 * h1 * h2, total = per * n;
-  const int ng = cs.d.ng;
-  const int64_t cj = cs.d.N[0], ck = (int64_t)cs.d.N[0] * cs.d.N[1];
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int q = e / per;
     const int r = e - q * per;
-    const int ci = r % h0, cjj = (r / h0) % h1, ckk = r / (h0 * h1);
     const MgXfer t = x[q];
-    const int64_t f = cell_of(cs.d, t.child, 2 * ckk + ng, 2 * cjj + ng, 2 * ci + ng);
-    const int64_t p = cell_of(ps.d, t.parent, t.lo[2] + ckk, t.lo[1] + cjj, t.lo[0] + ci);
-#pragma unroll
-    for (int v = 0; v < 2; ++v) {
-      const TC *__restrict__ a = v == 0 ? cs.u : cs.res;
-      TP out;
-      if constexpr (sizeof(TC) == 8) {
-        const double vol = cgeom[t.child].vol;
-        const double tv = ((vol + vol) + (vol + vol)) + ((vol + vol) + (vol + vol));
-        // t[ok][oj][oi] = vol * fine(k + ok, j + oj, i + oi)
-        const double t000 = vol * a[f], t001 = vol * a[f + 1];
-        const double t010 = vol * a[f + cj], t011 = vol * a[f + cj + 1];
-        const double t100 = vol * a[f + ck], t101 = vol * a[f + ck + 1];
-        const double t110 = vol * a[f + ck + cj], t111 = vol * a[f + ck + cj + 1];
-        const double num = ((t000 + t010) + (t001 + t011)) + ((t100 + t110) + (t101 + t111));
-        out = (TP)div_rn(num, tv);
-      } else {
-        const TC sum = ((a[f] + a[f + cj]) + (a[f + 1] + a[f + cj + 1])) +
-                       ((a[f + ck] + a[f + ck + cj]) + (a[f + ck + 1] + a[f + ck + cj + 1]));
-        out = (TP)((TC)0.125 * sum);
-      }
-      (v == 0 ? ps.u : ps.res)[p] = out;
-    }
+    restrict_cell(cs, ps, t, cgeom[t.child].vol, r % h0, (r / h0) % h1, r / (h0 * h1));
   }
 }
 
-// ProlongateSharedLinear (pr_ops.hpp:166-285) of the parent's res_err (its octant with
-// ghosts is the child's coarse buffer) and AddFieldsAndStore<u, res_err, u>: one thread
-// per coarse cell of the child's interior, eight fine cells each. The exact build forms
-// the slopes from the cell-centre coordinates as the reference does; the fast build
-// uses the uniform-spacing value dx_fine / 2 / dx_coarse = 1/4 of each difference.
-// TC is the child's type (the arithmetic), TP the parent's.
+// prolongation into every fine block of a grid: one thread per coarse cell of a child
 template <bool kFast, class TC, class TP>
 __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreView<TP> ps,
                                                         const MgXfer *__restrict__ x, int n,
@@ -413,57 +495,161 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreV
   pdl_enter();
   const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
   const int per = h0 * h1 * h2, total = per * n;
-  const int ng = cs.d.ng;
-  const int64_t pj = ps.d.N[0], pk = (int64_t)ps.d.N[0] * ps.d.N[1];
-  const int64_t N0 = cs.d.N[0], N01 = (int64_t)cs.d.N[0] * cs.d.N[1];
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int q = e / per;
     const int r = e - q * per;
-    const int c0 = r % h0, c1 = (r / h0) % h1, c2 = r / (h0 * h1);
     const MgXfer t = x[q];
-    const int c[3] = {c0 + ng, c1 + ng, c2 + ng};  // coarse-buffer index
-    const int f[3] = {2 * c0 + ng, 2 * c1 + ng, 2 * c2 + ng};
-    const int p[3] = {t.lo[0] + c0, t.lo[1] + c1, t.lo[2] + c2};
-    const int64_t pe = cell_of(ps.d, t.parent, p[2], p[1], p[0]);
-    const TC fc = (TC)ps.res[pe];
-    // the parent's cells next to p along d: its ghosts, or on a grid read directly the
-    // face neighbour's interior cell
-    auto side = [&](int d, int s) -> TC {
-      const int64_t st = d == 0 ? 1 : (d == 1 ? pj : pk);
-      const int lo = ps.d.ng, hi = ps.d.ng + ps.d.nx[d] - 1;
-      if (t.pnb[0] < 0 || (s < 0 ? p[d] > lo : p[d] < hi)) return (TC)ps.res[pe + s * st];
-      int q[3] = {p[0], p[1], p[2]};
-      q[d] = s < 0 ? hi : lo;
-      return (TC)ps.res[cell_of(ps.d, t.pnb[2 * d + (s > 0)], q[2], q[1], q[0])];
-    };
-    TC mq[3], pq[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      if constexpr (kFast) {
-        mq[d] = (TC)0.25 * (fc - side(d, -1));
-        pq[d] = (TC)0.25 * (side(d, 1) - fc);
-      } else {
-        const DevBlockGeom &g = cgeom[t.child];
-        auto xcc = [&](int idx) { return g.cxmin[d] + ((double)idx + 0.5) * g.cdx[d]; };
-        auto xfc = [&](int idx) { return g.xmin[d] + ((double)idx + 0.5) * g.dx[d]; };
-        const double xm = xcc(c[d] - 1), xc = xcc(c[d]), xp = xcc(c[d] + 1);
-        const double dxm = xc - xm, dxp = xp - xc;
-        const double dfm = xc - xfc(f[d]);
-        const double dfp = xfc(f[d] + 1) - xc;
-        mq[d] = div_rn(fc - side(d, -1), dxm) * dfm;
-        pq[d] = div_rn(side(d, 1) - fc, dxp) * dfp;
-      }
+    prolong_add_cell<kFast>(cs, ps, t, cgeom + t.child, r % h0, (r / h0) % h1, r / (h0 * h1));
+  }
+}
+
+// ---- the coarse end of the V-cycle in one launch
+// The trailing grids that hold one block each (a single tree's levels at and below 0)
+// run their down and up steps in one CTA, the steps separated by CTA barriers, instead
+// of about a dozen launches per grid. Fast build only; FP64 grids of at most 8^3 cells
+// (one SM's FP64 rate bounds them), FP32 grids of at most 16^3.
+constexpr int kTailMax = 8;
+constexpr int kTailThreads = 1024;
+struct TailGrid {
+  int slot;      // the grid's block
+  int nb[6];     // its face neighbours (itself: one block tiles the periodic domain)
+  int dbl;       // FP64 (else FP32)
+  int internal;  // not a leaf: the FAS right-hand side is formed
+  int top;       // the finest grid of the solve: no FAS, no error
+  double vol;    // cell volume (restriction weights)
+  MgCoef coef;
+  MgSweep sw[3];
+  StoreView<double> v64;
+  StoreView<float> v32;
+  FaceD<double> fd64;
+  FaceD<float> fd32;
+  MgXfer up;  // this block and its parent in the next entry (unused for the last)
+};
+struct TailArgs {
+  int n, stages, coarse_sweeps, pad;
+  MgOp o;
+  TailGrid g[kTailMax];
+};
+
+template <class T>
+__device__ __forceinline__ const StoreView<T> &tview(const TailGrid &g) {
+  if constexpr (sizeof(T) == 8) return g.v64;
+  else return g.v32;
+}
+template <class T>
+__device__ __forceinline__ const FaceD<T> &tfd(const TailGrid &g) {
+  if constexpr (sizeof(T) == 8) return g.fd64;
+  else return g.fd32;
+}
+
+// every interior cell of one block, the whole CTA
+template <class F>
+__device__ __forceinline__ void for_block(const Dims &d, F &&f) {
+  const int n0 = d.nx[0], n1 = d.nx[1], per = n0 * n1 * d.nx[2];
+  for (int e = threadIdx.x; e < per; e += blockDim.x) {
+    const int r = e / n0, i = e - r * n0, k = r / n1, j = r - k * n1;
+    f(k + d.ng, j + d.ng, i + d.ng);
+  }
+}
+
+template <class T>
+__device__ void tail_smooth(const TailArgs &a, const TailGrid &g, int stages) {
+  const StoreView<T> &v = tview<T>(g);
+  T *src = v.u, *dst = v.temp;
+  for (int st = 0; st < stages; ++st) {
+    for_block(v.d, [&](int k, int j, int i) {
+      jacobi_cell<true>(src, v.rhs, dst, v.d, g.nb, g.coef, a.o, g.sw[st], tfd<T>(g), g.slot, k, j, i);
+    });
+    __syncthreads();
+    T *tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+  if (src != v.u) {
+    for_block(v.d, [&](int k, int j, int i) {
+      const int64_t c = cell_of(v.d, g.slot, k, j, i);
+      v.u[c] = v.temp[c];
+    });
+    __syncthreads();
+  }
+}
+
+template <class T>
+__device__ void tail_error(const TailGrid &g) {
+  const StoreView<T> &v = tview<T>(g);
+  for_block(v.d, [&](int k, int j, int i) {
+    const int64_t c = cell_of(v.d, g.slot, k, j, i);
+    v.res[c] = v.u[c] - v.u0[c];
+  });
+  __syncthreads();
+}
+
+template <class T, class TP>
+__device__ void tail_down(const TailArgs &a, int t) {
+  const TailGrid &g = a.g[t];
+  const StoreView<T> &v = tview<T>(g);
+  for_block(v.d, [&](int k, int j, int i) {
+    if (g.top) {
+      const int64_t c = cell_of(v.d, g.slot, k, j, i);
+      v.u0[c] = v.u[c];
+    } else {
+      fas_cell<true>(v, g.internal != 0, g.nb, g.coef, a.o, tfd<T>(g), g.slot, k, j, i);
     }
-    const TC m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
-    TC *U = cs.u + cell_of(cs.d, t.child, f[2], f[1], f[0]);
-    U[0] = U[0] + (fc - ((m0 + m1) + m2));
-    U[1] = U[1] + (fc + ((p0 - m1) - m2));
-    U[N0] = U[N0] + (fc - ((m0 - p1) + m2));
-    U[N0 + 1] = U[N0 + 1] + (fc + ((p0 + p1) - m2));
-    U[N01] = U[N01] + (fc - ((m0 + m1) - p2));
-    U[N01 + 1] = U[N01 + 1] + (fc + ((p0 - m1) + p2));
-    U[N01 + N0] = U[N01 + N0] + (fc - ((m0 - p1) - p2));
-    U[N01 + N0 + 1] = U[N01 + N0 + 1] + (fc + ((p0 + p1) + p2));
+  });
+  __syncthreads();
+  tail_smooth<T>(a, g, a.stages);
+  if (t < a.n - 1) {
+    for_block(v.d, [&](int k, int j, int i) { residual_cell<true>(v, g.nb, g.coef, a.o, tfd<T>(g), g.slot, k, j, i); });
+    __syncthreads();
+    const int h0 = max(1, v.d.nx[0] / 2), h1 = max(1, v.d.nx[1] / 2), h2 = max(1, v.d.nx[2] / 2);
+    for (int e = threadIdx.x; e < h0 * h1 * h2; e += blockDim.x)
+      restrict_cell(v, tview<TP>(a.g[t + 1]), g.up, g.vol, e % h0, (e / h0) % h1, e / (h0 * h1));
+    __syncthreads();
+  } else {
+    for (int c = 0; c < a.coarse_sweeps; ++c) tail_smooth<T>(a, g, a.stages);
+    // res = u (the coarsest level's post-smooth copy), then res = u - u0 below the top
+    for_block(v.d, [&](int k, int j, int i) {
+      const int64_t c = cell_of(v.d, g.slot, k, j, i);
+      v.res[c] = g.top ? v.u[c] : v.u[c] - v.u0[c];
+    });
+    __syncthreads();
+  }
+}
+
+template <class T, class TP>
+__device__ void tail_up(const TailArgs &a, int t) {
+  const TailGrid &g = a.g[t];
+  const StoreView<T> &v = tview<T>(g);
+  const int h0 = max(1, v.d.nx[0] / 2), h1 = max(1, v.d.nx[1] / 2), h2 = max(1, v.d.nx[2] / 2);
+  for (int e = threadIdx.x; e < h0 * h1 * h2; e += blockDim.x)
+    prolong_add_cell<true>(v, tview<TP>(a.g[t + 1]), g.up, nullptr, e % h0, (e / h0) % h1, e / (h0 * h1));
+  __syncthreads();
+  tail_smooth<T>(a, g, a.stages);
+  if (!g.top) tail_error<T>(g);
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_mg_tail(TailArgs args) {
+  pdl_enter();
+  __shared__ TailArgs a;
+  {
+    const int *src = reinterpret_cast<const int *>(&args);
+    int *dst = reinterpret_cast<int *>(&a);
+    for (int w = threadIdx.x; w < (int)(sizeof(TailArgs) / sizeof(int)); w += blockDim.x) dst[w] = src[w];
+  }
+  __syncthreads();
+  // a grid in FP64 has FP64 grids below it (only the coarsest runs in FP64 in the mixed
+  // solve), so the type pairs are (double, double), (float, double), (float, float)
+  for (int t = 0; t < a.n; ++t) {
+    const bool d = a.g[t].dbl, dp = t + 1 < a.n ? a.g[t + 1].dbl : d;
+    if (d) tail_down<double, double>(a, t);
+    else if (dp) tail_down<float, double>(a, t);
+    else tail_down<float, float>(a, t);
+  }
+  for (int t = a.n - 2; t >= 0; --t) {
+    const bool d = a.g[t].dbl, dp = a.g[t + 1].dbl;
+    if (d) tail_up<double, double>(a, t);
+    else if (dp) tail_up<float, double>(a, t);
+    else tail_up<float, float>(a, t);
   }
 }
 
@@ -1384,14 +1570,64 @@ struct VCycle {
     return kOk;
   }
 
+  // The highest level of the trailing one-block grids that k_mg_tail takes (the fast
+  // build), or lmin - 1 when fewer than two qualify.
+  int tail_top() const {
+    int top = g->lmin - 1;
+    for (int L = g->lmin; L <= g->lmax; ++L) {
+      const pgb_mg::Grid &G = g->grids.at(L);
+      if (G.fine_h.size() != 1 || !G.coarse_h.empty() || !G.halofree) break;
+      if (cells(L) > (dbl(L) ? 512 : 4096)) break;
+      top = L;
+    }
+    const int n = top - g->lmin + 1;
+    return (n >= 2 && n <= kTailMax) ? top : g->lmin - 1;
+  }
+
+  int tail(int top) {
+    TailArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n = top - g->lmin + 1;
+    a.stages = g->cfg.stages;
+    a.coarse_sweeps = g->cfg.coarse_sweeps;
+    a.o = o;
+    for (int t = 0; t < a.n; ++t) {
+      const int L = top - t;
+      const pgb_mg::Grid &G = g->grids.at(L);
+      const pgb_mg::Store &S = g->store_of(L);
+      TailGrid &T = a.g[t];
+      T.slot = G.fine_h[0];
+      for (int q = 0; q < 6; ++q) T.nb[q] = G.nbr_h[q];
+      T.dbl = dbl(L) ? 1 : 0;
+      T.internal = G.nint > 0 ? 1 : 0;
+      T.top = L == g->lmax ? 1 : 0;
+      T.vol = G.tab.geom_h.at(T.slot).vol;
+      T.coef = G.coef;
+      for (int st = 0; st < 3; ++st) {
+        T.sw[st].w = srj_weight(g->cfg, st);
+        T.sw[st].omw = 1.0 - T.sw[st].w;
+        T.sw[st].wd = T.sw[st].w / G.coef.den;
+      }
+      T.v64 = S.template view<double>();
+      T.v32 = S.template view<float>();
+      T.fd64 = S.template fd<double>();
+      T.fd32 = S.template fd<float>();
+      if (L > g->lmin) T.up = G.xfer_h.at(0);
+    }
+    return launch_pdl(k_mg_tail, 1u, (unsigned)kTailThreads, s, a);
+  }
+
   int run() {
     int rc;
-    for (int L = g->lmax; L >= g->lmin; --L) {
+    const int top = kFast ? tail_top() : g->lmin - 1;
+    const int last_down = top >= g->lmin ? top + 1 : g->lmin;
+    for (int L = g->lmax; L >= last_down; --L) {
       if constexpr (kFast) rc = dbl(L) ? down<double>(L) : down<float>(L);
       else rc = down<double>(L);  // the exact build is FP64 only
       if (rc) return rc;
     }
-    for (int L = g->lmin + 1; L <= g->lmax; ++L) {
+    if (top >= g->lmin && (rc = tail(top))) return rc;
+    for (int L = (top >= g->lmin ? top + 1 : g->lmin + 1); L <= g->lmax; ++L) {
       if constexpr (kFast) rc = dbl(L) ? up<double>(L) : up<float>(L);
       else rc = up<double>(L);
       if (rc) return rc;
