@@ -506,8 +506,9 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreV
 // ---- the coarse end of the V-cycle in one launch
 // The trailing grids that hold one block each (a single tree's levels at and below 0)
 // run their down and up steps in one CTA, the steps separated by CTA barriers, instead
-// of about a dozen launches per grid. Fast build only; FP64 grids of at most 8^3 cells
-// (one SM's FP64 rate bounds them), FP32 grids of at most 16^3.
+// of about a dozen launches per grid. Fast build only; grids of at most 8^3 cells (on one
+// SM a 16^3 grid's steps cost more than their launches: measured on the refined 128^3
+// mesh, the mixed iteration took 0.85 ms with the 16^3 grid in the CTA, 0.79 ms without).
 constexpr int kTailMax = 8;
 constexpr int kTailThreads = 1024;
 struct TailGrid {
@@ -1577,7 +1578,7 @@ struct VCycle {
     for (int L = g->lmin; L <= g->lmax; ++L) {
       const pgb_mg::Grid &G = g->grids.at(L);
       if (G.fine_h.size() != 1 || !G.coarse_h.empty() || !G.halofree) break;
-      if (cells(L) > (dbl(L) ? 512 : 4096)) break;
+      if (cells(L) > 512) break;
       top = L;
     }
     const int n = top - g->lmin + 1;
