@@ -506,9 +506,11 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreV
 // ---- the coarse end of the V-cycle in one launch
 // The trailing grids that hold one block each (a single tree's levels at and below 0)
 // run their down and up steps in one CTA, the steps separated by CTA barriers, instead
-// of about a dozen launches per grid. Fast build only; grids of at most 8^3 cells (on one
-// SM a 16^3 grid's steps cost more than their launches: measured on the refined 128^3
-// mesh, the mixed iteration took 0.85 ms with the 16^3 grid in the CTA, 0.79 ms without).
+// of about a dozen launches per grid. FP64 solves of the fast build only, grids of at
+// most 8^3 cells. Measured on the refined 128^3 mesh: the FP64 V-cycle 1.19 ms with it,
+// 1.22 ms without; the mixed iteration was slower with its FP32 grids in the CTA (0.85
+// ms with the 16^3 grid, 0.82 ms with grids up to 8^3, 0.79 ms without), so the mixed
+// solve keeps one launch per step.
 constexpr int kTailMax = 8;
 constexpr int kTailThreads = 1024;
 struct TailGrid {
@@ -1575,6 +1577,7 @@ struct VCycle {
   // build), or lmin - 1 when fewer than two qualify.
   int tail_top() const {
     int top = g->lmin - 1;
+    if (mixed) return top;  // the FP32 grids' launches are cheaper than their steps on one SM
     for (int L = g->lmin; L <= g->lmax; ++L) {
       const pgb_mg::Grid &G = g->grids.at(L);
       if (G.fine_h.size() != 1 || !G.coarse_h.empty() || !G.halofree) break;
