@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 
 #include "device_tables.hpp"
 
@@ -82,5 +83,39 @@ __device__ __forceinline__ double div_rn(double x, double d) {
 // signed zeros and NaNs propagate exactly as in the reference host code.
 __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+
+// Programmatic dependent launch: a kernel launched with launch_pdl may start while its
+// predecessor in the stream drains. It first waits for the predecessor's completion and
+// memory (griddepcontrol.wait, before any access), then lets its own successor launch
+// (griddepcontrol.launch_dependents); this hides the launch latency of the hundreds of
+// small launches of a multigrid V-cycle. In a plain launch the wait is a no-op.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Returns from the calling function with the status when it is not kOk.
+#define PGB_TRY(...)               \
+  do {                             \
+    const int rc__ = (__VA_ARGS__); \
+    if (rc__) return rc__;          \
+  } while (0)
+
+// Launch with programmatic stream serialization (the kernel must begin with pdl_enter).
+template <class... P, class... A>
+int launch_pdl(void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  PGB_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...));
+  return kOk;
+}
 
 }  // namespace pgb

@@ -120,6 +120,7 @@ __device__ __forceinline__ void jacobi_at(int64_t c, const T *u, const T *rhs,
 template <class T>
 __global__ void __launch_bounds__(256) k_jacobi(const T *__restrict__ u, const T *__restrict__ rhs, T *__restrict__ out,
                                                 LevelGeom g, T D, T alpha, T w, T wd, T omw) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < (int64_t)g.n * g.n * g.n) jacobi_at(c, u, rhs, out, g, D, alpha, w, wd, omw);
 }
@@ -140,6 +141,7 @@ __device__ __forceinline__ void residual_at(int64_t c, const T *u, const T *rhs,
 template <class T>
 __global__ void __launch_bounds__(256) k_residual(const T *__restrict__ u, const T *__restrict__ rhs, T *__restrict__ res,
                                                   LevelGeom g, T D, T alpha) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < (int64_t)g.n * g.n * g.n) residual_at(c, u, rhs, res, g, D, alpha);
 }
@@ -148,6 +150,7 @@ __global__ void __launch_bounds__(256) k_residual(const T *__restrict__ u, const
 template <class T>
 __global__ void __launch_bounds__(256) k_apply(const T *__restrict__ u, T *__restrict__ out, LevelGeom g, T D,
                                                T alpha) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= (int64_t)g.n * g.n * g.n) return;
   int k, j, i;
@@ -172,6 +175,7 @@ __device__ __forceinline__ void fas_at(int64_t c, const T *u, const T *res,
 template <class T>
 __global__ void __launch_bounds__(256) k_fas_rhs(const T *__restrict__ u, const T *__restrict__ res, T *__restrict__ rhs,
                                                  T *__restrict__ u0, LevelGeom g, T D, T alpha) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < (int64_t)g.n * g.n * g.n) fas_at(c, u, res, rhs, u0, g, D, alpha);
 }
@@ -216,6 +220,7 @@ __device__ __forceinline__ void restrict2_at(int64_t c, const T *fu, const T *fr
 template <class T>
 __global__ void __launch_bounds__(256) k_restrict2(const T *__restrict__ fu, const T *__restrict__ fr, T *__restrict__ cu,
                                                    T *__restrict__ cr, LevelGeom fg, LevelGeom cg) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < (int64_t)cg.n * cg.n * cg.n) restrict2_at(c, fu, fr, cu, cr, fg, cg);
 }
@@ -277,6 +282,7 @@ __device__ __forceinline__ void prolong_add_at(int64_t c, const T *cres, T *fu,
 template <class T>
 __global__ void __launch_bounds__(256) k_prolong_add(const T *__restrict__ cres, T *__restrict__ fu, LevelGeom cg,
                                                      LevelGeom fg) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < (int64_t)cg.n * cg.n * cg.n) prolong_add_at(c, cres, fu, cg, fg);
 }
@@ -284,12 +290,14 @@ __global__ void __launch_bounds__(256) k_prolong_add(const T *__restrict__ cres,
 // out <- 1 a + (-1) b
 template <class T>
 __global__ void __launch_bounds__(256) k_sub(const T *__restrict__ a, const T *__restrict__ b, T *__restrict__ out, int64_t n) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n) out[c] = (T)1 * a[c] + (T)-1 * b[c];
 }
 
 template <class T>
 __global__ void __launch_bounds__(256) k_copy_arr(const T *__restrict__ a, T *__restrict__ out, int64_t n) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n) out[c] = a[c];
 }
@@ -301,6 +309,7 @@ template <class T>
 __global__ void __launch_bounds__(256) k_residual_sumsq(const T *__restrict__ u, const T *__restrict__ rhs,
                                                         T *__restrict__ res, float *__restrict__ rhs32, LevelGeom g,
                                                         T D, T alpha, double *__restrict__ partial) {
+  pdl_enter();
   __shared__ double sm[256];
   double acc = 0.0;
   const int64_t n = (int64_t)g.n * g.n * g.n;
@@ -328,6 +337,7 @@ __global__ void __launch_bounds__(256) k_residual_sumsq(const T *__restrict__ u,
 // Per-CTA partial sums of a^2 (FP64 accumulation); a second pass sums them in order.
 template <class T>
 __global__ void __launch_bounds__(256) k_sumsq_partial(const T *__restrict__ a, int64_t n, double *__restrict__ partial) {
+  pdl_enter();
   __shared__ double sm[256];
   double s = 0.0;
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
@@ -397,16 +407,17 @@ void smooth(GmgLevelBuf<T> &L, const GmgConfig &c, cudaStream_t s) {
   T *a = L.u, *b = L.temp;
   for (int st = 0; st < c.stages; ++st) {
     const double w = smoother_weight(c, st);
-    k_jacobi<T><<<nblk(n), 256, 0, s>>>(a, L.rhs, b, g, (T)c.D, (T)c.alpha, (T)w, (T)(w * g.inv_den), (T)(1.0 - w));
+    (void)launch_pdl(k_jacobi<T>, nblk(n), 256, s, a, L.rhs, b, g, (T)c.D, (T)c.alpha, (T)w, (T)(w * g.inv_den), (T)(1.0 - w));
     T *t = a;
     a = b;
     b = t;
   }
-  if (a != L.u) k_copy_arr<T><<<nblk(n), 256, 0, s>>>(a, L.u, n);
+  if (a != L.u) (void)launch_pdl(k_copy_arr<T>, nblk(n), 256, s, a, L.u, n);
 }
 
 template <class Tf, class Tc>
 __global__ void k_convert(const Tf *__restrict__ a, Tc *__restrict__ b, int64_t n) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n) b[c] = (Tc)a[c];
 }
@@ -733,49 +744,49 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
     const LevelGeom lg = geom_with(g, c);
     if (l > 0) {
       GmgLevelBuf<T> &f = L[l - 1];
-      k_restrict2<T><<<nblk(n), 256, 0, s>>>(f.u, f.res, g.u, g.res, geom_of(f), lg);
+      (void)launch_pdl(k_restrict2<T>, nblk(n), 256, s, f.u, f.res, g.u, g.res, geom_of(f), lg);
     }
     const bool coarsest = (l == nl - 1);
     if (coarsest && c64) {
       // coarsest level in FP64: convert, solve there, convert the error back
       GmgLevelBuf<double> &h = *c64;
       const LevelGeom hg = geom_with(h, c);
-      k_convert<T, double><<<nblk(n), 256, 0, s>>>(g.u, h.u, n);
-      k_convert<T, double><<<nblk(n), 256, 0, s>>>(g.res, h.res, n);
+      (void)launch_pdl(k_convert<T, double>, nblk(n), 256, s, g.u, h.u, n);
+      (void)launch_pdl(k_convert<T, double>, nblk(n), 256, s, g.res, h.res, n);
       if (l > 0) {
-        k_fas_rhs<double><<<nblk(n), 256, 0, s>>>(h.u, h.res, h.rhs, h.u0, hg, c.D, c.alpha);
+        (void)launch_pdl(k_fas_rhs<double>, nblk(n), 256, s, h.u, h.res, h.rhs, h.u0, hg, c.D, c.alpha);
       } else {
-        k_convert<T, double><<<nblk(n), 256, 0, s>>>(g.rhs, h.rhs, n);
-        k_copy_arr<double><<<nblk(n), 256, 0, s>>>(h.u, h.u0, n);
+        (void)launch_pdl(k_convert<T, double>, nblk(n), 256, s, g.rhs, h.rhs, n);
+        (void)launch_pdl(k_copy_arr<double>, nblk(n), 256, s, h.u, h.u0, n);
       }
       smooth<double>(h, c, s);
       for (int q = 0; q < c.coarse_sweeps; ++q) smooth<double>(h, c, s);
-      if (l > 0) k_sub<double><<<nblk(n), 256, 0, s>>>(h.u, h.u0, h.res, n);
-      else k_copy_arr<double><<<nblk(n), 256, 0, s>>>(h.u, h.res, n);
-      k_convert<double, T><<<nblk(n), 256, 0, s>>>(h.res, g.res, n);
-      if (l == 0) k_convert<double, T><<<nblk(n), 256, 0, s>>>(h.u, g.u, n);
+      if (l > 0) (void)launch_pdl(k_sub<double>, nblk(n), 256, s, h.u, h.u0, h.res, n);
+      else (void)launch_pdl(k_copy_arr<double>, nblk(n), 256, s, h.u, h.res, n);
+      (void)launch_pdl(k_convert<double, T>, nblk(n), 256, s, h.res, g.res, n);
+      if (l == 0) (void)launch_pdl(k_convert<double, T>, nblk(n), 256, s, h.u, g.u, n);
       break;
     }
-    if (l > 0) k_fas_rhs<T><<<nblk(n), 256, 0, s>>>(g.u, g.res, g.rhs, g.u0, lg, D, alpha);
+    if (l > 0) (void)launch_pdl(k_fas_rhs<T>, nblk(n), 256, s, g.u, g.res, g.rhs, g.u0, lg, D, alpha);
 #ifdef PGB_GMG_EXACT
-    else k_copy_arr<T><<<nblk(n), 256, 0, s>>>(g.u, g.u0, n);  // the reference copies; the finest u0 is unused
+    else (void)launch_pdl(k_copy_arr<T>, nblk(n), 256, s, g.u, g.u0, n);  // the reference copies; the finest u0 is unused
 #endif
     smooth<T>(g, c, s);
     if (!coarsest) {
-      k_residual<T><<<nblk(n), 256, 0, s>>>(g.u, g.rhs, g.res, lg, D, alpha);
+      (void)launch_pdl(k_residual<T>, nblk(n), 256, s, g.u, g.rhs, g.res, lg, D, alpha);
     } else {
       for (int q = 0; q < c.coarse_sweeps; ++q) smooth<T>(g, c, s);
-      if (l > 0) k_sub<T><<<nblk(n), 256, 0, s>>>(g.u, g.u0, g.res, n);
-      else k_copy_arr<T><<<nblk(n), 256, 0, s>>>(g.u, g.res, n);
+      if (l > 0) (void)launch_pdl(k_sub<T>, nblk(n), 256, s, g.u, g.u0, g.res, n);
+      else (void)launch_pdl(k_copy_arr<T>, nblk(n), 256, s, g.u, g.res, n);
     }
   }
   // up-sweep of the levels above the tail (the tail did its own)
   for (int l = std::min(nl - 2, lt - 1); l >= 0; --l) {
     GmgLevelBuf<T> &g = L[l], &cl = L[l + 1];
     const int64_t n = g.cells();
-    k_prolong_add<T><<<nblk(cl.cells()), 256, 0, s>>>(cl.res, g.u, geom_of(cl), geom_of(g));
+    (void)launch_pdl(k_prolong_add<T>, nblk(cl.cells()), 256, s, cl.res, g.u, geom_of(cl), geom_of(g));
     smooth<T>(g, c, s);
-    if (l > 0) k_sub<T><<<nblk(n), 256, 0, s>>>(g.u, g.u0, g.res, n);
+    if (l > 0) (void)launch_pdl(k_sub<T>, nblk(n), 256, s, g.u, g.u0, g.res, n);
   }
 }
 
@@ -784,34 +795,35 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
 template <class T>
 void residual_sumsq(GmgLevelBuf<T> &L, const GmgConfig &c, double *partial, int nparts, T *res, float *rhs32,
                     cudaStream_t s) {
-  k_residual_sumsq<T><<<nparts, 256, 0, s>>>(L.u, L.rhs, res, rhs32, geom_with(L, c), (T)c.D, (T)c.alpha, partial);
+  (void)launch_pdl(k_residual_sumsq<T>, nparts, 256, s, L.u, L.rhs, res, rhs32, geom_with(L, c), (T)c.D, (T)c.alpha, partial);
 }
 
 template <class T>
 void apply(const GmgLevelBuf<T> &L, const GmgConfig &c, const T *u, T *out, cudaStream_t s) {
-  k_apply<T><<<nblk(L.cells()), 256, 0, s>>>(u, out, geom_with(L, c), (T)c.D, (T)c.alpha);
+  (void)launch_pdl(k_apply<T>, nblk(L.cells()), 256, s, u, out, geom_with(L, c), (T)c.D, (T)c.alpha);
 }
 
 template <class T>
 void launch_sumsq(const T *a, int64_t n, double *partial, int nparts, cudaStream_t s) {
-  k_sumsq_partial<T><<<nparts, 256, 0, s>>>(a, n, partial);
+  (void)launch_pdl(k_sumsq_partial<T>, nparts, 256, s, a, n, partial);
 }
 
 // x <- x + (double) e  (iterative refinement update)
 template <class T>
 __global__ void k_add_correction(double *__restrict__ x, const T *__restrict__ e, int64_t n) {
+  pdl_enter();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n) x[c] = x[c] + (double)e[c];
 }
 
 inline void launch_mixed_prepare(const double *r64, GmgLevelBuf<float> &L0, cudaStream_t s) {
   const int64_t n = L0.cells();
-  if (r64) k_convert<double, float><<<nblk(n), 256, 0, s>>>(r64, L0.rhs, n);
+  if (r64) (void)launch_pdl(k_convert<double, float>, nblk(n), 256, s, r64, L0.rhs, n);
   cudaMemsetAsync(L0.u, 0, n * sizeof(float), s);
 }
 inline void launch_mixed_update(double *x, const GmgLevelBuf<float> &L0, cudaStream_t s) {
   const int64_t n = L0.cells();
-  k_add_correction<float><<<nblk(n), 256, 0, s>>>(x, L0.u, n);
+  (void)launch_pdl(k_add_correction<float>, nblk(n), 256, s, x, L0.u, n);
 }
 
 }  // namespace PGB_GMG_NS

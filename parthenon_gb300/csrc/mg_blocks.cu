@@ -99,17 +99,6 @@ struct StoreView {
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 
-// Programmatic dependent launch: the multigrid kernels are launched so that each may
-// start while its predecessor in the stream drains. Each first waits for the
-// predecessor's completion and memory (griddepcontrol.wait, before any access), then
-// lets its own successor launch (griddepcontrol.launch_dependents); this hides the
-// launch latency of the hundreds of small launches of a V-cycle. A plain launch makes
-// the wait a no-op.
-__device__ __forceinline__ void pdl_enter() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 __device__ __forceinline__ int64_t cell_of(const Dims &d, int slot, int k, int j, int i) {
   return ((int64_t)slot * d.N[2] + k) * ((int64_t)d.N[1] * d.N[0]) + (int64_t)j * d.N[0] + i;
 }
@@ -1415,29 +1404,6 @@ double srj_weight(const GmgConfig &c, int s) {
   static const double m3[3] = {2.2473, 0.8571, 0.5296};
   if (c.jacobi) return c.weight;
   return c.stages == 1 ? m1[s] : (c.stages == 2 ? m2[s] : m3[s]);
-}
-
-// Launch with programmatic stream serialization (the kernel begins with pdl_enter).
-#define PGB_TRY(...)               \
-  do {                             \
-    const int rc__ = (__VA_ARGS__); \
-    if (rc__) return rc__;          \
-  } while (0)
-
-template <class... P, class... A>
-int launch_pdl(void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A &&...args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  PGB_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...));
-  return kOk;
 }
 
 // exchange_grid's prolongation op: ProlongateSharedLinear with the reference's
