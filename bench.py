@@ -286,6 +286,7 @@ def run_ours(args, ws, rank):
         out["amr"] = amr_bench(torch, args.amr_cycles, with_cpu=(rank == 0 and ws == 1), root=args.amr_root)
     if args.sparse_cycles > 0:
         out["sparse"] = sparse_bench(torch, args.sparse_cycles, with_cpu=(rank == 0 and ws == 1))
+    out["smr"] = smr_bench(torch, with_cpu=(rank == 0 and ws == 1))
     return out
 
 
@@ -338,6 +339,54 @@ def gmg_bench(torch):
                                       "vs_fp64_vcycle_rel_err": float((x - a).abs().max() / a.abs().max())}
     res["config"] = {"n": GMG_N, "levels": GMG_COARSEN + 1, "smoother": "weighted Jacobi 2/3, 2+2",
                      "coarse": "+16 smoother passes, FP64", "rhs": "32 Gaussians sigma 0.03 seed 4, mean removed"}
+    return res
+
+
+SMR_ROOT, SMR_BLOCK, SMR_NG, SMR_NSCALARS, SMR_CYCLES = 128, 16, 4, 4, 20
+
+
+def _smr_leaves(pg):
+    nb = SMR_ROOT // SMR_BLOCK
+    return pg.problems.refined_region_leaves(nb.bit_length() - 1, nb // 4, 3 * nb // 4)
+
+
+def smr_bench(torch, with_cpu):
+    """The 2-level static-refinement advection workload: 128^3 root in 16^3 blocks with
+    the central 1/8 refined once (448 + 512 blocks, 4 ghosts), a Gaussian plus 4 U(0,1)
+    scalars, PLM, RK2, CFL 0.3, 20 cycles; prolongation/restriction at the fine/coarse
+    faces and flux correction inside every stage (one CUDA graph per cycle)."""
+    import parthenon_gb300 as pg
+    mesh = pg.Mesh((SMR_ROOT,) * 3, (SMR_BLOCK,) * 3, SMR_NG, leaves=_smr_leaves(pg))
+    ncomp = 1 + SMR_NSCALARS
+    state = pg.problems.advection_state(mesh, nscalars=SMR_NSCALARS, seed=3)
+    drv = pg.RK2Driver(mesh, ncomp, pg.StageConfig("advection", "plm", 0.3))
+    drv.set_state(state)
+    drv.run(3)  # warm-up: graph capture and tuning
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(drv.stream)
+    drv.run(SMR_CYCLES)
+    ev1.record(drv.stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    res = {"metric": "zone-cycles/s", "value": drv.zone_cycles(SMR_CYCLES) / (ms * 1e-3),
+           "ms_per_cycle": ms / SMR_CYCLES,
+           "config": {"workload": "advection3d-plm-rk2-smr-128^3-root-16^3blocks-central-eighth-refined",
+                      "blocks": int(mesh.nblocks), "nghost": SMR_NG, "ncomp": ncomp, "cycles": SMR_CYCLES}}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib as O
+        o = O.OracleSim((SMR_ROOT,) * 3, (SMR_BLOCK,) * 3, SMR_NG, leaves=_smr_leaves(pg), ncomp=ncomp,
+                        physics="advection", recon=1, cfl=0.3)
+        o.base()[:] = state
+        o.exchange(True, 0)
+        o.init_dt()
+        threads = O.lib().orc_max_threads()
+        t0 = time.perf_counter()
+        o.run(1, nthreads=threads)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": drv.zone_cycles(1) / dt, "unit": "zone-cycles/s", "cores": threads,
+                               "kind": "port", "sample": "1 RK2 cycle of the same mesh and state"}
     return res
 
 
@@ -706,6 +755,8 @@ def main():
     ap.add_argument("--amr-only", action="store_true",
                     help="run only the adaptive leg (profiling runs), no CPU baseline")
     ap.add_argument("--gmg-only", action="store_true", help="run only the multigrid leg (profiling runs)")
+    ap.add_argument("--smr-only", action="store_true",
+                    help="run only the 2-level static-refinement advection leg (with its CPU baseline)")
     ap.add_argument("--gmg-composite-only", action="store_true",
                     help="run only the composite-grid multigrid leg, no CPU baseline (profiling runs)")
     ap.add_argument("--sparse-cycles", type=int, default=100,
@@ -727,6 +778,10 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         out = {"gmg": gmg_bench(torch), "gmg_composite": gmg_composite_bench(torch, with_cpu=False)}
+    elif args.smr_only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        out = {"smr": smr_bench(torch, with_cpu=(rank == 0))}
     elif args.gmg_composite_only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
