@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(128) k_march(StageArgs a) {
               a.dudt[e] = a.dudt[e] + du;
             } else {
               if (MODE == kFinishUpdate) du = a.dudt[e] + du;
-              const double dudt = -du / g.vol;
+              const double dudt = div_rn(-du, g.vol);
               const double avg = a.w_in * __ldg(a.u_in + e) + a.w_base * __ldg(a.u_base + e);
               const double bdt = a.beta * a.dt[0];
               a.u_out[e] = 1.0 * avg + bdt * dudt;
@@ -207,11 +207,18 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
       const double xc = g.xmin[D] + (pos + 0.5) * g.dx[D];
       const double xfp = g.xmin[D] + (pos + 1) * g.dx[D];
       const double xfm = g.xmin[D] + pos * g.dx[D];
-      const double cp_ = (xfp - xc) / g.dx[D];
-      const double cm_ = (xc - xfm) / g.dx[D];
+      // x / dx as an exact multiplication when dx is a power of two (div_rn)
+      const double cp_ = div_rn(xfp - xc, g.dx[D]);
+      const double cm_ = div_rn(xc - xfm, g.dx[D]);
       const double dql = q0 - ld<D>(u, e - step), dqr = ld<D>(u, e + step) - q0;
       const double dq2 = dql * dqr;
+#ifdef PGB_EXACT_ARITH
       double dqm = 2.0 * dq2 / (dql + dqr);
+#else
+      // the van Leer slope with a refined reciprocal (FP64 divides bound this sweep); a
+      // zero denominator means dq2 <= 0, which zeroes the slope below
+      double dqm = 2.0 * dq2 * recip(dql + dqr);
+#endif
       if (dq2 <= 0.0) dqm = 0.0;
       Lc = q0 + cp_ * dqm;
       Rc = q0 - cm_ * dqm;
@@ -232,7 +239,7 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
             a.dudt[ec] = a.dudt[ec] + du;
           } else {
             if (MODE == kFinishUpdate) du = a.dudt[ec] + du;
-            const double dudt = -du / g.vol;
+            const double dudt = div_rn(-du, g.vol);
             const double avg = a.w_in * __ldg(a.u_in + ec) + a.w_base * __ldg(a.u_base + ec);
             const double bdt = a.beta * a.dt[0];
             a.u_out[ec] = 1.0 * avg + bdt * dudt;
@@ -275,7 +282,7 @@ __global__ void __launch_bounds__(128) k_div_update(StageArgs a) {
     double du = (g.area[0] * F0[o + 1] - g.area[0] * F0[o]);
     du += (g.area[1] * F1[o + N0] - g.area[1] * F1[o]);
     du += (g.area[2] * F2[o + N01] - g.area[2] * F2[o]);
-    const double dudt = -du / g.vol;
+    const double dudt = div_rn(-du, g.vol);
     const double avg = a.w_in * a.u_in[e] + a.w_base * a.u_base[e];
     a.u_out[e] = 1.0 * avg + bdt * dudt;
   }
