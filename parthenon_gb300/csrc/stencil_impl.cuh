@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
   const double area = g.area[D];
   const double *__restrict__ u = a.u_in;
   const double vd = a.ncvel ? a.cvel[v][D] : a.vel[D];
-  const int pos0 = D == 0 ? m.i0 : (D == 1 ? m.j0 : m.k0);
+  [[maybe_unused]] const int pos0 = D == 0 ? m.i0 : (D == 1 ? m.j0 : m.k0);
   double Lprev = 0.0, AFprev = 0.0;
   for (int p = -1; p <= n; ++p) {
     const int64_t e = c0 + (int64_t)p * step;
@@ -203,13 +203,20 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
       Lc = q0;
       Rc = q0;
     } else {
+#ifdef PGB_EXACT_ARITH
+      // the face weights from the cell-centre and face coordinates (plm_inline.hpp); x / dx
+      // as an exact multiplication when dx is a power of two (div_rn)
       const int pos = pos0 + p;
       const double xc = g.xmin[D] + (pos + 0.5) * g.dx[D];
       const double xfp = g.xmin[D] + (pos + 1) * g.dx[D];
       const double xfm = g.xmin[D] + pos * g.dx[D];
-      // x / dx as an exact multiplication when dx is a power of two (div_rn)
       const double cp_ = div_rn(xfp - xc, g.dx[D]);
       const double cm_ = div_rn(xc - xfm, g.dx[D]);
+#else
+      // uniform Cartesian cells: both weights are 1/2 (the coordinate form rounds to
+      // within an ulp of it)
+      constexpr double cp_ = 0.5, cm_ = 0.5;
+#endif
       const double dql = q0 - ld<D>(u, e - step), dqr = ld<D>(u, e + step) - q0;
       const double dq2 = dql * dqr;
 #ifdef PGB_EXACT_ARITH
