@@ -154,9 +154,13 @@ int check_params(const pgb_mesh *m, const pgb_stage_params *p, int ncomp) {
   return kOk;
 }
 
-int exchange_leaf(pgb_mesh *m, double *data, double *coarse, int ncomp, int flags, double *buffer, cudaStream_t s) {
+// uniform_ops: the stage exchanges of the fast build prolongate with the uniform-spacing
+// forms of the ops (exchange.cu ops 3 and 4)
+int exchange_leaf(pgb_mesh *m, double *data, double *coarse, int ncomp, int flags, double *buffer, cudaStream_t s,
+                  bool uniform_ops = false) {
   const int prolongate = flags & PGB_EXCHANGE_PROLONGATE;
-  const int op = (flags >> 1) & 3;
+  int op = (flags >> 1) & 3;
+  if (uniform_ops && (op == 0 || op == 1)) op = op == 0 ? 4 : 3;
   return exchange_grid(m->st.leaf, data, coarse, ncomp, prolongate, op, buffer, s, m->st.sparse_dev());
 }
 
@@ -168,9 +172,9 @@ int cycle_impl(pgb_mesh *m, const pgb_stage_params *p, double *base, double *sta
   const int xflags = p->physics == 1 ? 0 : PGB_EXCHANGE_PROLONGATE;
   int rc;
   if ((rc = stage_impl(m, p, base, base, stage, dudt, flux, dt, 1.0, 0.0, 1.0, ncomp, s))) return rc;
-  if ((rc = exchange_leaf(m, stage, cstage, ncomp, xflags, nullptr, s))) return rc;
+  if ((rc = exchange_leaf(m, stage, cstage, ncomp, xflags, nullptr, s, !p->exact))) return rc;
   if ((rc = stage_impl(m, p, stage, base, base, dudt, flux, dt, 0.5, 0.5, 0.5, ncomp, s))) return rc;
-  if ((rc = exchange_leaf(m, base, cbase, ncomp, xflags, nullptr, s))) return rc;
+  if ((rc = exchange_leaf(m, base, cbase, ncomp, xflags, nullptr, s, !p->exact))) return rc;
   // sparse variables: the last stage checks for deallocation after its exchange
   // (sparse_advection_driver.cpp:120-123)
   if (const SparseDev *sp = m->st.sparse_dev()) {

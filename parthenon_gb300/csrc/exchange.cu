@@ -497,7 +497,8 @@ __global__ void __launch_bounds__(256) k_restrict(const DevRegion *__restrict__ 
 __device__ __forceinline__ double sign1(double x) { return x < 0.0 ? -1.0 : 1.0; }
 
 // ProlongateSharedGeneral (pr_ops.hpp:166-285): op 0 minmod, 1 linear, 2 constant;
-// op 3 is the linear op in its uniform-spacing form (slopes a quarter of the differences).
+// ops 3 and 4 are the linear and minmod ops in their uniform-spacing form (slopes a
+// quarter of the differences).
 // Written with explicit round-to-nearest intrinsics so no FMA contraction changes
 // the result relative to the reference's separately rounded host arithmetic.
 // One warp per work item, components in turn.
@@ -529,12 +530,20 @@ __global__ void __launch_bounds__(256, 2) k_prolong(const DevRegion *__restrict_
       double mq[3], pq[3];
   #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        if (op == 3) {
-          // linear slopes on a uniform grid: (difference / coarse dx) * (fine dx / 2) is
-          // a quarter of the difference (the multigrid's fast build)
+        if (op >= 3) {
+          // slopes on a uniform grid: (difference / coarse dx) * (fine dx / 2) is a quarter
+          // of the difference, linear (op 3) or minmod-limited (op 4); every factor is a
+          // power of two, so on dyadic coordinates this is bitwise the coordinate form
           const int64_t st = q == 0 ? 1 : (q == 1 ? cs1 : cs2);
-          mq[q] = 0.25 * (fc - cb[ce - st]);
-          pq[q] = 0.25 * (cb[ce + st] - fc);
+          const double a = fc - cb[ce - st], b = cb[ce + st] - fc;
+          if (op == 3) {
+            mq[q] = 0.25 * a;
+            pq[q] = 0.25 * b;
+          } else {
+            const double mm = (0.5 * (sign1(a) + sign1(b))) * smin(fabs(a), fabs(b));
+            mq[q] = 0.25 * mm;
+            pq[q] = 0.25 * mm;
+          }
           continue;
         }
         const double cx0 = g->cxmin[q], cdx = g->cdx[q], x0 = g->xmin[q], dx = g->dx[q];
