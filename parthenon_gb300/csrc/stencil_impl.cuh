@@ -278,6 +278,10 @@ __global__ void __launch_bounds__(128) k_div_update(StageArgs a) {
   const int64_t cs = N01 * d.N[2];
   const DevBlockGeom g = a.geom[b];
   const double bdt = a.beta * a.dt[0];
+#ifndef PGB_EXACT_ARITH
+  const double nbv = div_rn(-bdt, g.vol);
+  const double s0 = nbv * g.area[0], s1 = nbv * g.area[1], s2 = nbv * g.area[2];
+#endif
 #pragma unroll
   for (int v = 0; v < NC; ++v) {
     if (a.alloc && !a.alloc[b * NC + v]) continue;  // unallocated sparse variable
@@ -286,12 +290,21 @@ __global__ void __launch_bounds__(128) k_div_update(StageArgs a) {
     const double *F1 = a.flux + ((int64_t)b * 3 + 1) * NC * cs + v * cs;
     const double *F2 = a.flux + ((int64_t)b * 3 + 2) * NC * cs + v * cs;
     const int64_t o = (int64_t)k * N01 + (int64_t)j * N0 + i;
+#ifdef PGB_EXACT_ARITH
     double du = (g.area[0] * F0[o + 1] - g.area[0] * F0[o]);
     du += (g.area[1] * F1[o + N0] - g.area[1] * F1[o]);
     du += (g.area[2] * F2[o + N01] - g.area[2] * F2[o]);
     const double dudt = div_rn(-du, g.vol);
     const double avg = a.w_in * a.u_in[e] + a.w_base * a.u_base[e];
     a.u_out[e] = 1.0 * avg + bdt * dudt;
+#else
+    // avg + sum_d (-bdt area_d / vol) (F_high - F_low): the update folded into one
+    // constant per direction (FP64 issue bounds this kernel)
+    const double avg = fma(a.w_in, a.u_in[e], a.w_base * a.u_base[e]);
+    double out = fma(s0, F0[o + 1] - F0[o], avg);
+    out = fma(s1, F1[o + N0] - F1[o], out);
+    a.u_out[e] = fma(s2, F2[o + N01] - F2[o], out);
+#endif
   }
 }
 
