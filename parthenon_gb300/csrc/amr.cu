@@ -368,13 +368,13 @@ int pgb_amr_transfer(pgb_mesh *oldm, pgb_mesh *newm, const double *old_data, dou
     map.push_back(r);
   }
   cudaStream_t s = (cudaStream_t)stream;
-  DevRemap *dmap = nullptr;
-  PGB_CUDA(cudaMallocAsync((void **)&dmap, map.size() * sizeof(DevRemap), s));
+  AsyncScratch scratch(s);
+  PGB_CUDA(scratch.alloc(map.size() * sizeof(DevRemap)));
+  DevRemap *dmap = (DevRemap *)scratch.p;
   PGB_CUDA(cudaMemcpyAsync(dmap, map.data(), map.size() * sizeof(DevRemap), cudaMemcpyHostToDevice, s));
   k_transfer<<<dim3((unsigned)map.size(), ncomp), 256, 0, s>>>(dmap, tn->geom, to->geom, tn->dims, ncomp, old_data,
                                                                new_data);
   const cudaError_t le = cudaGetLastError();
-  PGB_CUDA(cudaFreeAsync(dmap, s));
   // the pageable host map must outlive the copy
   PGB_CUDA(cudaStreamSynchronize(s));
   if (le != cudaSuccess) return check_cuda(le, "k_transfer");

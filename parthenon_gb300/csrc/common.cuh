@@ -101,6 +101,20 @@ __device__ __forceinline__ void pdl_enter() {
     if (rc__) return rc__;          \
   } while (0)
 
+// Stream-ordered scratch allocation released on every return path: the free is
+// enqueued on the stream when the scope ends, after the work that uses the buffer.
+struct AsyncScratch {
+  void *p = nullptr;
+  cudaStream_t s;
+  explicit AsyncScratch(cudaStream_t st) : s(st) {}
+  AsyncScratch(const AsyncScratch &) = delete;
+  AsyncScratch &operator=(const AsyncScratch &) = delete;
+  ~AsyncScratch() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  cudaError_t alloc(size_t bytes) { return cudaMallocAsync(&p, bytes, s); }
+};
+
 // Launch with programmatic stream serialization (the kernel must begin with pdl_enter).
 template <class... P, class... A>
 int launch_pdl(void (*k)(P...), unsigned grid, unsigned block, cudaStream_t s, A &&...args) {

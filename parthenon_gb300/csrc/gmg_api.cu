@@ -71,8 +71,8 @@ struct pgb_gmg {
   template <class T>
   int alloc(T **p, int64_t n) {
     PGB_CUDA(cudaMalloc((void **)p, n * sizeof(T)));
-    PGB_CUDA(cudaMemset(*p, 0, n * sizeof(T)));
     allocs.push_back(*p);
+    PGB_CUDA(cudaMemset(*p, 0, n * sizeof(T)));
     return kOk;
   }
   template <class T>
@@ -511,8 +511,9 @@ extern "C" int pgb_gmg_solve_blocks(pgb_gmg *g, pgb_mesh *mesh, double *u, const
   std::vector<int> off;
   for (auto &b : topo.leaf().blocks)
     for (int q = 0; q < 3; ++q) off.push_back((int)(b.loc.lx[q] * sp.bnx[q]));
-  int *doff = nullptr;
-  PGB_CUDA(cudaMallocAsync((void **)&doff, off.size() * sizeof(int), s));
+  AsyncScratch scratch(s);
+  PGB_CUDA(scratch.alloc(off.size() * sizeof(int)));
+  int *doff = (int *)scratch.p;
   PGB_CUDA(cudaMemcpyAsync(doff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, s));
   const int nb = t->nblocks;
   const unsigned grid = (unsigned)std::min<int64_t>((n3 + 255) / 256, 4096);
@@ -528,7 +529,6 @@ extern "C" int pgb_gmg_solve_blocks(pgb_gmg *g, pgb_mesh *mesh, double *u, const
     const cudaError_t le = cudaGetLastError();
     if (le != cudaSuccess) rc = check_cuda(le, "scatter");
   }
-  cudaFreeAsync(doff, s);
   if (rc) return rc;
   PGB_CUDA(cudaStreamSynchronize(s));
   if (iters_out) *iters_out = it;

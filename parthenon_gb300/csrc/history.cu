@@ -115,8 +115,9 @@ extern "C" int pgb_history_mass(pgb_mesh *mesh, const double *u, int32_t ncomp, 
   PGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const int64_t total = (int64_t)t->nblocks * ncomp * t->dims.nx[0] * t->dims.nx[1] * t->dims.nx[2];
   const int nparts = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)nsm * 4, (total + kThreads - 1) / kThreads));
-  double *buf = nullptr;
-  PGB_CUDA(cudaMallocAsync((void **)&buf, sizeof(double) * ((size_t)nparts * nregions + nregions), s));
+  AsyncScratch scratch(s);
+  PGB_CUDA(scratch.alloc(sizeof(double) * ((size_t)nparts * nregions + nregions)));
+  double *buf = (double *)scratch.p;
   const double den = mesh_volume + 1e-20;
   auto go = [&](auto kern) {
     kern<<<nparts, kThreads, 0, s>>>(u, t->geom, t->dims, ncomp, t->nblocks, rg, den, buf);
@@ -135,7 +136,6 @@ extern "C" int pgb_history_mass(pgb_mesh *mesh, const double *u, int32_t ncomp, 
   const cudaError_t le = cudaGetLastError();
   PGB_CUDA(cudaMemcpyAsync(out, buf + (size_t)nparts * nregions, sizeof(double) * nregions, cudaMemcpyDeviceToHost,
                            s));
-  PGB_CUDA(cudaFreeAsync(buf, s));
   PGB_CUDA(cudaStreamSynchronize(s));
   if (le != cudaSuccess) return check_cuda(le, "history launch");
   return kOk;

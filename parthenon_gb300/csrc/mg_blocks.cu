@@ -1111,6 +1111,16 @@ struct pgb_mg {
 
 namespace {
 
+// A zeroed device array of n elements, owned by g (recorded before anything can fail,
+// so that pgb_mg_destroy frees it whatever happens after).
+template <class T>
+int dev_zeros(pgb_mg *g, T **p, int64_t n) {
+  PGB_CUDA(cudaMalloc((void **)p, (size_t)n * sizeof(T)));
+  g->allocs.push_back(*p);
+  PGB_CUDA(cudaMemset(*p, 0, (size_t)n * sizeof(T)));
+  return kOk;
+}
+
 // Operator constants for spacing dx, in the order of poisson_equation.hpp:59-102 and
 // utils/robust.hpp (the exact build's values are bitwise those formed per cell there)
 MgCoef make_coef(const double *dx, const GmgConfig &c) {
@@ -1312,13 +1322,9 @@ int mg_upload(pgb_mg *g) {
     if (n >= (int64_t)1 << 31) return fail(kErrUnsupported, "multigrid store above 2^31 cells");
     const int64_t nc = (int64_t)S.nslots * S.dims.Nc[0] * S.dims.Nc[1] * S.dims.Nc[2];
     for (double **p : {&S.u, &S.res, &S.rhs, &S.temp, &S.u0}) {
-      PGB_CUDA(cudaMalloc((void **)p, n * sizeof(double)));
-      PGB_CUDA(cudaMemset(*p, 0, n * sizeof(double)));
-      g->allocs.push_back(*p);
+      PGB_TRY(dev_zeros(g, p, n));
     }
-    PGB_CUDA(cudaMalloc((void **)&S.coarse, nc * sizeof(double)));
-    PGB_CUDA(cudaMemset(S.coarse, 0, nc * sizeof(double)));
-    g->allocs.push_back(S.coarse);
+    PGB_TRY(dev_zeros(g, &S.coarse, nc));
   }
   // block lists and transfers in one allocation
   size_t bytes = 0;
@@ -1364,14 +1370,11 @@ int mg_upload(pgb_mg *g) {
   if (g->flux_correct) {
     const Dims &dl = g->stores.at(0).dims;
     const int64_t nf = (int64_t)g->nleaf * 3 * dl.N[0] * dl.N[1] * dl.N[2];
-    PGB_CUDA(cudaMalloc((void **)&g->lflux, nf * sizeof(double)));
-    PGB_CUDA(cudaMemset(g->lflux, 0, nf * sizeof(double)));
-    g->allocs.push_back(g->lflux);
+    PGB_TRY(dev_zeros(g, &g->lflux, nf));
   }
   const Dims &d0 = g->stores.at(0).dims;
   g->nparts = (int)grid_for((int64_t)g->nleaf * d0.nx[0] * d0.nx[1] * d0.nx[2]);
-  PGB_CUDA(cudaMalloc((void **)&g->partial, g->nparts * sizeof(double)));
-  g->allocs.push_back(g->partial);
+  PGB_TRY(dev_zeros(g, &g->partial, g->nparts));
   PGB_CUDA(cudaMallocHost((void **)&g->partial_h, g->nparts * sizeof(double)));
   g->uploaded = true;
   return kOk;
@@ -1385,13 +1388,9 @@ int mg_upload32(pgb_mg *g) {
     const int64_t n = (int64_t)S.nslots * S.dims.N[0] * S.dims.N[1] * S.dims.N[2];
     const int64_t nc = (int64_t)S.nslots * S.dims.Nc[0] * S.dims.Nc[1] * S.dims.Nc[2];
     for (float **p : {&S.u32, &S.res32, &S.rhs32, &S.temp32, &S.u032}) {
-      PGB_CUDA(cudaMalloc((void **)p, n * sizeof(float)));
-      PGB_CUDA(cudaMemset(*p, 0, n * sizeof(float)));
-      g->allocs.push_back(*p);
+      PGB_TRY(dev_zeros(g, p, n));
     }
-    PGB_CUDA(cudaMalloc((void **)&S.coarse32, nc * sizeof(float)));
-    PGB_CUDA(cudaMemset(S.coarse32, 0, nc * sizeof(float)));
-    g->allocs.push_back(S.coarse32);
+    PGB_TRY(dev_zeros(g, &S.coarse32, nc));
   }
   g->uploaded32 = true;
   return kOk;
@@ -1662,19 +1661,14 @@ int enqueue_iteration(pgb_mg *g, bool mixed, cudaStream_t s) {
 enum { kX = 0, kR, kRhat0, kP, kV, kH, kS, kT, kNumVectors };
 
 int bicg_alloc(pgb_mg *g) {
-  if (g->kv[0]) return kOk;
+  if (g->kres_h) return kOk;  // allocated last: set only when every step succeeded
   const Dims &d = g->stores.at(0).dims;
   const int64_t n = (int64_t)g->nleaf * d.N[0] * d.N[1] * d.N[2];
   for (int q = 0; q < kNumVectors; ++q) {
-    PGB_CUDA(cudaMalloc((void **)&g->kv[q], n * sizeof(double)));
-    PGB_CUDA(cudaMemset(g->kv[q], 0, n * sizeof(double)));
-    g->allocs.push_back(g->kv[q]);
+    PGB_TRY(dev_zeros(g, &g->kv[q], n));
   }
-  PGB_CUDA(cudaMalloc((void **)&g->ks, kNumScalars * sizeof(double)));
-  PGB_CUDA(cudaMemset(g->ks, 0, kNumScalars * sizeof(double)));
-  g->allocs.push_back(g->ks);
-  PGB_CUDA(cudaMalloc((void **)&g->kpart, 2 * (size_t)g->nparts * sizeof(double)));
-  g->allocs.push_back(g->kpart);
+  PGB_TRY(dev_zeros(g, &g->ks, kNumScalars));
+  PGB_TRY(dev_zeros(g, &g->kpart, 2 * (int64_t)g->nparts));
   PGB_CUDA(cudaMallocHost((void **)&g->kres_h, 2 * sizeof(double)));
   return kOk;
 }
@@ -1953,12 +1947,9 @@ int pgb_mg_set_coefficient(pgb_mg *g, const double *d, void *stream) {
     pgb_mg::Store &S = kv.second;
     const int64_t n = (int64_t)S.nslots * S.dims.N[0] * S.dims.N[1] * S.dims.N[2];
     for (int q = 0; q < 3; ++q)
-      if (!S.d[q]) {
-        PGB_CUDA(cudaMalloc((void **)&S.d[q], n * sizeof(double)));
-        PGB_CUDA(cudaMemset(S.d[q], 0, n * sizeof(double)));
-        PGB_CUDA(cudaMalloc((void **)&S.d32[q], n * sizeof(float)));
-        g->allocs.push_back(S.d[q]);
-        g->allocs.push_back(S.d32[q]);
+      if (!S.d32[q]) {  // allocated second: null unless both exist
+        if (!S.d[q]) PGB_TRY(dev_zeros(g, &S.d[q], n));
+        PGB_TRY(dev_zeros(g, &S.d32[q], n));
       }
   }
   // the leaves' faces: [nleaf][3][N3][N2][N1] into the three face arrays of store 0
