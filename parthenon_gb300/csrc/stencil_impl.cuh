@@ -194,10 +194,23 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
   const double vd = a.ncvel ? a.cvel[v][D] : a.vel[D];
   [[maybe_unused]] const int pos0 = D == 0 ? m.i0 : (D == 1 ? m.j0 : m.k0);
   double Lprev = 0.0, AFprev = 0.0;
+#ifndef PGB_EXACT_ARITH
+  // PLM: the window is carried along the line, so each cell costs one load and one
+  // difference (its left difference is the previous cell's right one)
+  double qc = 0.0, dql = 0.0;
+  if (a.recon != 0) {
+    qc = ld<D>(u, c0 - step);
+    dql = qc - ld<D>(u, c0 - 2 * step);
+  }
+#endif
   for (int p = -1; p <= n; ++p) {
     const int64_t e = c0 + (int64_t)p * step;
     // donor cell or PLM (plm_inline.hpp, uniform van Leer)
+#ifdef PGB_EXACT_ARITH
     const double q0 = ld<D>(u, e);
+#else
+    const double q0 = a.recon != 0 ? qc : ld<D>(u, e);
+#endif
     double Lc, Rc;
     if (a.recon == 0) {
       Lc = q0;
@@ -212,23 +225,27 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
       const double xfm = g.xmin[D] + pos * g.dx[D];
       const double cp_ = div_rn(xfp - xc, g.dx[D]);
       const double cm_ = div_rn(xc - xfm, g.dx[D]);
-#else
-      // uniform Cartesian cells: both weights are 1/2 (the coordinate form rounds to
-      // within an ulp of it)
-      constexpr double cp_ = 0.5, cm_ = 0.5;
-#endif
       const double dql = q0 - ld<D>(u, e - step), dqr = ld<D>(u, e + step) - q0;
       const double dq2 = dql * dqr;
-#ifdef PGB_EXACT_ARITH
       double dqm = 2.0 * dq2 / (dql + dqr);
-#else
-      // the van Leer slope with a refined reciprocal (FP64 divides bound this sweep); a
-      // zero denominator means dq2 <= 0, which zeroes the slope below
-      double dqm = 2.0 * dq2 * recip(dql + dqr);
-#endif
       if (dq2 <= 0.0) dqm = 0.0;
       Lc = q0 + cp_ * dqm;
       Rc = q0 - cm_ * dqm;
+#else
+      // uniform Cartesian cells: both face weights are 1/2 (the coordinate form rounds
+      // to within an ulp of it), so the face values are q0 +- dq2 / (dql + dqr), half
+      // the van Leer slope, with a refined reciprocal (FP64 divides bound this sweep).
+      // A zero denominator means dq2 <= 0, where the slope is zero.
+      const double qn = ld<D>(u, e + step);
+      const double dqr = qn - q0;
+      const double dq2 = dql * dqr;
+      double r = recip(dql + dqr);
+      if (dq2 <= 0.0) r = 0.0;
+      Lc = fma(dq2, r, q0);
+      Rc = fma(-dq2, r, q0);
+      dql = dqr;
+      qc = qn;
+#endif
     }
     if (p >= 0) {
       const double F = vd > 0.0 ? Lprev * vd : Rc * vd;
