@@ -13,8 +13,9 @@ namespace pgb {
 namespace fast {
 
 // Reciprocal: hardware approximation (about 2^-22 relative error) refined by two
-// Newton-Raphson iterations. Inputs here are normal, positive or negative, never zero
-// (denominators carry +eps or a +1 guard).
+// Newton-Raphson iterations. Meant for normal inputs of either sign (the WENO and HLL
+// denominators carry +eps or a +1 guard); a zero or subnormal input gives inf or NaN,
+// so the PLM slope, whose denominator is zero only where dq2 <= 0, discards it there.
 __device__ __forceinline__ double recip(double x) {
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
