@@ -31,10 +31,10 @@ def two_level_nested(root_level, lo, hi, inner_lo, inner_hi):
 
 # (name, nx, block_nx, nghost, leaves)
 INDEX_MAP_CASES = [
-    ("C1-uniform-64", (64, 64, 64), (16, 16, 16), 2, None),
+    ("uniform-64-16cubed-ng2", (64, 64, 64), (16, 16, 16), 2, None),
     ("uniform-g4", (64, 64, 64), (16, 16, 16), 4, None),
     ("smr-small", (64, 64, 64), (16, 16, 16), 4, refined_cube(2, 1, 3)),
-    ("C3-smr-128", (128, 128, 128), (16, 16, 16), 4, refined_cube(3, 2, 6)),
+    ("smr-128root-16cubed-ng4", (128, 128, 128), (16, 16, 16), 4, refined_cube(3, 2, 6)),
     ("smr-corner", (64, 64, 64), (8, 8, 8), 2, refined_cube(3, 0, 2)),
     ("three-level", (64, 64, 64), (8, 8, 8), 4, two_level_nested(3, 2, 6, 6, 10)),
     # smallest meshes: one block that is its own neighbour in all 26 directions, and

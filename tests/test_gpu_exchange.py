@@ -73,7 +73,7 @@ def test_packed_buffers_match_reference_layout(name, nx, bnx, ng, leaves):
 
 
 def test_large_uniform_exchange_periodic_identity():
-    """C2-shaped mesh (32^3 blocks, 4 ghosts) at reduced block count: every ghost
+    """A mesh of 32^3 blocks with 4 ghosts and 11 components at reduced block count: every ghost
     equals the periodic image of an interior cell."""
     import torch
     n, ng, nb = 32, 4, 4

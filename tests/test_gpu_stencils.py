@@ -40,7 +40,7 @@ def _run(case, exact, ncycles):
     return got, np.array(o.base()), float(drv.dt.cpu()[0]), o.dt(), dt0, dts
 
 
-def _advection_c1(m):
+def _advection_gaussian(m):
     return pg.problems.advection_state(m)
 
 
@@ -57,8 +57,8 @@ def _burgers5(m):
 
 
 CASES = {
-    "C1-advection-dc": ((64,) * 3, (16,) * 3, 2, None, "advection", "dc", 1, 0.3, _advection_c1),
-    "C1-advection-plm": ((64,) * 3, (16,) * 3, 2, None, "advection", "plm", 1, 0.3, _advection_c1),
+    "advection-dc-64": ((64,) * 3, (16,) * 3, 2, None, "advection", "dc", 1, 0.3, _advection_gaussian),
+    "advection-plm-64": ((64,) * 3, (16,) * 3, 2, None, "advection", "plm", 1, 0.3, _advection_gaussian),
     "burgers-weno5": ((32,) * 3, (16,) * 3, 4, None, "burgers", "weno5", 11, 0.8, _burgers),
     "burgers-linear": ((32,) * 3, (16,) * 3, 4, None, "burgers", "linear", 11, 0.8, _burgers),
     "burgers-5comp": ((32,) * 3, (16,) * 3, 4, None, "burgers", "weno5", 5, 0.8, _burgers5),

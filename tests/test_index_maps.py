@@ -34,7 +34,7 @@ def test_index_maps_match_oracle(name, nx, bnx, ng, leaves):
 
 
 def test_c3_block_counts():
-    """BASELINE C3: 128^3 root in 16^3 blocks, central 1/8 refined once -> 448 + 512."""
+    """The static-refinement advection mesh: 128^3 root in 16^3 blocks, central 1/8 refined once -> 448 + 512."""
     from meshes import refined_cube
     m = pg.Mesh((128,) * 3, (16,) * 3, 4, leaves=refined_cube(3, 2, 6))
     locs, _ = m.block_info()
