@@ -122,7 +122,9 @@ int pgb_exchange(pgb_mesh *mesh, double *data, double *coarse, int32_t ncomp, in
  * the call allocates nothing; for callers that cannot allocate device memory (another
  * runtime owns the allocator, or the loop must never allocate). No counterpart in the
  * reference. Requests needing more than buffer_elems * ncomp = 4,194,304 doubles are
- * rejected (PGB_ERR_INVALID). The first call on each device looks up the array's
+ * rejected (PGB_ERR_INVALID), and so is a mesh with sparse variables
+ * (PGB_ERR_UNSUPPORTED: the packed-buffer exchange has no sparse form; such meshes
+ * exchange through pgb_exchange with buffer == NULL). The first call on each device looks up the array's
  * device address (make that first call before any stream capture); all calls share
  * the array, so calls that overlap on the GPU race with each other. */
 int pgb_exchange_static_buffer(pgb_mesh *mesh, double *data, double *coarse, int32_t ncomp, int32_t flags,
@@ -160,6 +162,18 @@ int pgb_stage(pgb_mesh *mesh, const pgb_stage_params *p, const double *u_in, con
  * InitializeBlockTimeSteps after a remesh (driver.cpp:129-131,194-204). */
 int pgb_estimate_dt(pgb_mesh *mesh, const pgb_stage_params *p, const double *u, int32_t ncomp, double *dt,
                     int32_t first, void *stream);
+
+/* The Burgers package's FillDerived on the device: derived = 0.5 * U(3) * (U(0)^2 +
+ * U(1)^2 + U(2)^2) on the interior cells of every block (derived: one component in the
+ * field layout, ghosts untouched), separately rounded in the reference's order.
+ * Replaces FillDerived<MeshData> (src/interface/update.hpp) with the package's
+ * CalculateDerived (benchmarks/burgers/burgers_package.cpp:143-167). */
+int pgb_fill_derived(pgb_mesh *mesh, const double *u, int32_t ncomp, double *derived, void *stream);
+/* Attach the Burgers derived field to the mesh (NULL detaches): pgb_rk2_cycles then runs
+ * pgb_fill_derived on each stage's output after its update, as the Burgers task list
+ * does (benchmarks/burgers/burgers_driver.cpp:121). pgb_run_host* fill a derived field
+ * of their own for Burgers. */
+int pgb_set_derived(pgb_mesh *mesh, double *derived);
 
 /* ncycles RK2 cycles (two stages with a ghost exchange after each, then the dt update)
  * on device arrays. base/stage: fields; dudt: scratch of the field's size; flux:

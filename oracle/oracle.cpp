@@ -897,6 +897,7 @@ struct Sim {
   int ncomp = 1;
   bool prolong_in_stage = true;
   Field base, stage, dudt;
+  Field derived;  // Burgers "derived" (Metadata::OneCopy, one component)
   FluxField flux;
   double dt = std::numeric_limits<double>::max();
   double dt_prev = std::numeric_limits<double>::max();  // dt before the last SetGlobalTimeStep
@@ -1003,6 +1004,25 @@ inline void weighted_sum(Field &z, Field &x, Field &y, double w1, double w2, con
     }
 }
 
+// Burgers FillDerived, CalculateDerived (burgers_package.cpp:143-167): on the interior,
+// derived = 0.5 * d * (u1^2 + u2^2 + u3^2) with the velocity components u1..u3 and
+// d = U(3), the first passive scalar; the expression is evaluated left to right as
+// written there.
+inline void fill_derived(Sim &s, Field &U) {
+  Field &D = s.derived;
+  const int ng = s.mesh->p.ng;
+  const int nblk = (int)U.blocks->size();
+#pragma omp parallel for schedule(static)
+  for (int b = 0; b < nblk; ++b)
+    for (int k = ng; k < U.N[2] - ng; ++k)
+      for (int j = ng; j < U.N[1] - ng; ++j)
+        for (int i = ng; i < U.N[0] - ng; ++i) {
+          const double u1 = U.at(b, 0, k, j, i), u2 = U.at(b, 1, k, j, i), u3 = U.at(b, 2, k, j, i);
+          const double d = U.at(b, 3, k, j, i);
+          D.at(b, 0, k, j, i) = 0.5 * d * (u1 * u1 + u2 * u2 + u3 * u3);
+        }
+}
+
 // One RK2 cycle (advection_driver.cpp:56-164, burgers_driver.cpp:53-148 task order)
 inline void cycle(Sim &s) {
   Mesh &m = *s.mesh;
@@ -1031,6 +1051,8 @@ inline void cycle(Sim &s) {
     }
     weighted_sum(mc0, mc0, s.base, beta, 1.0 - beta, sp);
     weighted_sum(mc1, mc0, s.dudt, 1.0, beta * s.dt, sp);
+    // Burgers: FillDerived after the update of every stage (burgers_driver.cpp:121)
+    if (s.physics == 1) fill_derived(s, mc1);
     exchange(mc1, m.blocks, BAny, 0, s.recs, s.prolong_in_stage, PMinMod, m.multilevel, false, sp);
     // the last stage checks for deallocation after its exchange
     // (sparse_advection_driver.cpp:120-123)
@@ -1082,6 +1104,7 @@ void *orc_sim_create(const int *nx, const int *bnx, int ng, const double *xmin,
     s->base.init(s->mesh.get(), &s->mesh->blocks, ncomp);
     s->stage.init(s->mesh.get(), &s->mesh->blocks, ncomp);
     s->dudt.init(s->mesh.get(), &s->mesh->blocks, ncomp);
+    if (physics == 1) s->derived.init(s->mesh.get(), &s->mesh->blocks, 1);
     s->flux.init(s->base);
     s->recs = build_boundaries(*s->mesh, s->mesh->blocks, BAny, 0);
     return s;
@@ -1111,6 +1134,11 @@ void orc_block_info(void *h, int64_t *locs, double *geom) {
 }
 
 double *orc_base(void *h) { return ((Sim *)h)->base.data.data(); }
+// Burgers "derived" field (one component, the field layout), or null for advection
+double *orc_derived(void *h) {
+  Sim *s = (Sim *)h;
+  return s->derived.data.empty() ? nullptr : s->derived.data.data();
+}
 double *orc_base_coarse(void *h) { return ((Sim *)h)->base.coarse.data(); }
 int64_t orc_field_size(void *h) { return (int64_t)((Sim *)h)->base.data.size(); }
 int64_t orc_coarse_size(void *h) { return (int64_t)((Sim *)h)->base.coarse.size(); }
@@ -1377,6 +1405,7 @@ int orc_remesh(void *h, const int *flags) {
     }
     s->stage.init(s->mesh.get(), &s->mesh->blocks, s->ncomp);
     s->dudt.init(s->mesh.get(), &s->mesh->blocks, s->ncomp);
+    if (s->physics == 1) s->derived.init(s->mesh.get(), &s->mesh->blocks, 1);
     s->flux.init(s->base);
     s->recs = build_boundaries(*s->mesh, s->mesh->blocks, BAny, 0);
     return 1;

@@ -68,6 +68,8 @@ _SIGNATURES = {
     "pgb_stage": [VP, ctypes.POINTER(StageParams), VP, VP, VP, VP, VP, VP, ctypes.c_double, ctypes.c_double,
                   ctypes.c_double, ctypes.c_int32, VP],
     "pgb_estimate_dt": [VP, ctypes.POINTER(StageParams), VP, ctypes.c_int32, VP, ctypes.c_int32, VP],
+    "pgb_fill_derived": [VP, VP, ctypes.c_int32, VP, VP],
+    "pgb_set_derived": [VP, VP],
     "pgb_rk2_cycles": [VP, ctypes.POINTER(StageParams), VP, VP, VP, VP, VP, VP, ctypes.c_int32, VP,
                        ctypes.c_int32, ctypes.c_int32, VP],
     "pgb_run_host": [VP, ctypes.POINTER(StageParams), VP, VP, ctypes.c_int32, ctypes.c_int32, DP],

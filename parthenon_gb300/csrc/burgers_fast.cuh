@@ -287,21 +287,27 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
 template <int NC>
 int launch_burgers_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
   const Dims &d = a.d;
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (nsm <= 0) nsm = 152;
-  }
+  // SM count of the current device (the runtime caches device attributes, so the query
+  // is cheap; a process may drive several devices)
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return kErrCuda;
+  if (nsm <= 0) nsm = 152;
+  cudaError_t attr = cudaSuccess;
   auto go = [&](auto kern, int D) {
+    if (attr != cudaSuccess) return;
     const int n = D == 0 ? d.nx[0] : (D == 1 ? d.nx[1] : d.nx[2]);
     const int64_t nf = D == 0 ? d.nx[1] : d.nx[0];
     const int64_t ns = D == 2 ? d.nx[1] : d.nx[2];
     const int64_t lines = (int64_t)a.nblocks * nf * ns;
     const int64_t groups = (lines + 31) / 32;
     const size_t smem = 2 * 3 * (size_t)(n + 1) * 32 * sizeof(double);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // more than the default 48 KB of dynamic shared memory (n = 32: 50.7 KB) needs the
+    // opt-in attribute; a failure here stops the stage before any launch of it
+    if (smem > 48 * 1024) {
+      attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (attr != cudaSuccess) return;
+    }
     const int pick = g_tune_force >= 0 ? g_tune_force
                                        : tuned_choice(burgers_tune_key(NC, n, store_flux, a.nblocks), kBurgersGridDefault);
     const int64_t grid = std::min<int64_t>(groups, (int64_t)nsm * kBurgersGridMult[pick]);
@@ -316,6 +322,7 @@ int launch_burgers_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
     go(k_burgers_dir<NC, 1, kAddDu>, 1);
     go(k_burgers_dir<NC, 2, kFinishUpdate>, 2);
   }
+  if (attr != cudaSuccess) return kErrCuda;
   return cudaGetLastError() == cudaSuccess ? kOk : kErrCuda;
 }
 

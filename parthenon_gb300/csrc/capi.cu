@@ -35,6 +35,7 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
 int pack_grid(GridTables &t, const double *fine, const double *coarse, int ncomp, double *buffer, cudaStream_t s);
 int flux_correct_grid(GridTables &t, double *flux, int ncomp, cudaStream_t s, const SparseDev *sp);
 // reduce.cu
+int fill_derived(const GridTables &t, const double *u, int ncomp, double *derived, cudaStream_t s);
 int estimate_dt(MeshState &m, int physics, const double *u, int ncomp, const double vel[3], double cfl, double *dt,
                 int first, cudaStream_t s, int ncvel, const double *cvel);
 // sparse.cu
@@ -167,13 +168,18 @@ int exchange_leaf(pgb_mesh *m, double *data, double *coarse, int ncomp, int flag
 // One RK2 cycle: stage names base, "1", base (low_storage_integrator.cpp:67-86 rk2:
 // beta = {1, 0.5}); Burgers omits the prolongation step of the exchange
 // (burgers_driver.cpp:108-120 wires Send/Receive/Set only).
+// Burgers runs FillDerived on each stage's output after its update (burgers_driver.cpp:121)
+// when `derived` is given.
 int cycle_impl(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage, double *dudt, double *flux,
-               double *cbase, double *cstage, int ncomp, double *dt, cudaStream_t s) {
+               double *cbase, double *cstage, int ncomp, double *dt, cudaStream_t s, double *derived = nullptr) {
   const int xflags = p->physics == 1 ? 0 : PGB_EXCHANGE_PROLONGATE;
+  const bool derive = p->physics == 1 && derived;
   int rc;
   if ((rc = stage_impl(m, p, base, base, stage, dudt, flux, dt, 1.0, 0.0, 1.0, ncomp, s))) return rc;
+  if (derive && (rc = fill_derived(m->st.leaf, stage, ncomp, derived, s))) return rc;
   if ((rc = exchange_leaf(m, stage, cstage, ncomp, xflags, nullptr, s, !p->exact))) return rc;
   if ((rc = stage_impl(m, p, stage, base, base, dudt, flux, dt, 0.5, 0.5, 0.5, ncomp, s))) return rc;
+  if (derive && (rc = fill_derived(m->st.leaf, base, ncomp, derived, s))) return rc;
   if ((rc = exchange_leaf(m, base, cbase, ncomp, xflags, nullptr, s, !p->exact))) return rc;
   // sparse variables: the last stage checks for deallocation after its exchange
   // (sparse_advection_driver.cpp:120-123)
@@ -383,6 +389,21 @@ int pgb_estimate_dt(pgb_mesh *m, const pgb_stage_params *p, const double *u, int
                      p->comp_vel);
 }
 
+int pgb_fill_derived(pgb_mesh *m, const double *u, int32_t ncomp, double *derived, void *stream) {
+  if (!m || !u || !derived) return fail(kErrInvalid, "null argument");
+  if (!m->st.uploaded) return fail(kErrState, "mesh tables not uploaded (call pgb_mesh_upload)");
+  return fill_derived(m->st.leaf, u, ncomp, derived, (cudaStream_t)stream);
+}
+
+int pgb_set_derived(pgb_mesh *m, double *derived) {
+  if (!m) return fail(kErrInvalid, "null mesh");
+  if (m->st.derived != derived) {
+    m->st.derived = derived;
+    mesh_clear_graphs(m);
+  }
+  return kOk;
+}
+
 int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage, double *dudt, double *flux,
                    double *cbase, double *cstage, int32_t ncomp, double *dt, int32_t ncycles, int32_t use_graph,
                    void *stream) {
@@ -391,9 +412,10 @@ int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double 
   if (!base || !stage || !dt) return fail(kErrInvalid, "null field pointer");
   if (m->st.leaf.multilevel && (!cbase || !cstage)) return fail(kErrInvalid, "multilevel mesh needs coarse buffers");
   cudaStream_t s = (cudaStream_t)stream;
+  double *derived = m->st.derived;
   if (!use_graph) {
     for (int c = 0; c < ncycles; ++c)
-      if ((rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s))) return rc;
+      if ((rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s, derived))) return rc;
     return kOk;
   }
   if (!s) return fail(kErrInvalid, "graph replay needs a non-default stream");
@@ -401,7 +423,7 @@ int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double 
   // velocity table by value) and whether sparse variables are on
   std::string key;
   auto put = [&](const void *q, size_t n) { key.append((const char *)q, n); };
-  const void *ptrs[] = {base, stage, dudt, flux, cbase, cstage, dt};
+  const void *ptrs[] = {base, stage, dudt, flux, cbase, cstage, dt, derived};
   put(ptrs, sizeof(ptrs));
   put(p, offsetof(pgb_stage_params, comp_vel));
   if (p->physics == 0 && p->ncomp_vel) put(p->comp_vel, 3 * sizeof(double) * p->ncomp_vel);
@@ -413,9 +435,13 @@ int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double 
     if ((rc = autotune(m, p, base, stage, dudt, flux, cbase, ncomp, dt, s))) return rc;
     cudaGraph_t g;
     PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s);
+    rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s, derived);
     cudaError_t ce = cudaStreamEndCapture(s, &g);
-    if (rc) return rc;
+    if (rc) {
+      // the capture ended with a graph of the launches made before the failure
+      if (ce == cudaSuccess) cudaGraphDestroy(g);
+      return rc;
+    }
     if (ce != cudaSuccess) return check_cuda(ce, "cudaStreamEndCapture");
     cudaGraphExec_t ge;
     ce = cudaGraphInstantiate(&ge, g, 0);
@@ -443,10 +469,10 @@ int pgb_run_host_dt(pgb_mesh *m, const pgb_stage_params *p, const double *host_i
   const size_t nc = (size_t)t.nblocks * ncomp * t.dims.Nc[0] * t.dims.Nc[1] * t.dims.Nc[2];
   const bool ml = t.multilevel;
   double *base = nullptr, *stage = nullptr, *dudt = nullptr, *flux = nullptr, *cb = nullptr, *cs = nullptr,
-         *dt = nullptr, *dt_pinned = nullptr;
+         *dt = nullptr, *dt_pinned = nullptr, *derived = nullptr;
   cudaStream_t s = nullptr;
   auto cleanup = [&]() {
-    double *ps[] = {base, stage, dudt, flux, cb, cs, dt};
+    double *ps[] = {base, stage, dudt, flux, cb, cs, dt, derived};
     for (double *q : ps)
       if (q) cudaFree(q);
     if (dt_pinned) cudaFreeHost(dt_pinned);
@@ -472,6 +498,9 @@ int pgb_run_host_dt(pgb_mesh *m, const pgb_stage_params *p, const double *host_i
   } else if ((rc = guard(cudaMalloc(&dudt, n * 8), "malloc"))) {
     return rc;
   }
+  // Burgers: the package's derived field, filled after every stage (FillDerived)
+  const size_t nd = (size_t)t.nblocks * t.dims.N[0] * t.dims.N[1] * t.dims.N[2];
+  if (p->physics == 1 && (rc = guard(cudaMalloc(&derived, nd * 8), "malloc"))) return rc;
   if ((rc = guard(cudaMemcpyAsync(base, host_in, n * 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
   if ((rc = guard(cudaMemcpyAsync(stage, base, n * 8, cudaMemcpyDeviceToDevice, s), "d2d"))) return rc;
   // initial fill: Mesh::CommunicateBoundaries prolongates for every package
@@ -491,7 +520,7 @@ int pgb_run_host_dt(pgb_mesh *m, const pgb_stage_params *p, const double *host_i
       (rc = guard(cudaMallocHost(&dt_pinned, (size_t)ncycles * sizeof(double)), "pinned dt")))
     return rc;
   for (int c = 0; c < ncycles; ++c) {
-    if ((rc = cycle_impl(m, p, base, stage, dudt, flux, cb, cs, ncomp, dt, s))) {
+    if ((rc = cycle_impl(m, p, base, stage, dudt, flux, cb, cs, ncomp, dt, s, derived))) {
       cleanup();
       return rc;
     }

@@ -58,6 +58,10 @@ extern "C" int pgb_exchange_static_buffer(pgb_mesh *mesh, double *data, double *
   GridTables *t = mesh_leaf_tables(mesh);
   if (!t) return fail(kErrState, "mesh is null or its tables are not uploaded (call pgb_mesh_upload)");
   if (ncomp < 1) return fail(kErrInvalid, "ncomp must be positive");
+  // the packed-buffer exchange has no sparse form (null buffers are decided per pair
+  // by the direct exchange)
+  if (mesh_state(mesh)->sparse_dev())
+    return fail(kErrUnsupported, "meshes with sparse variables exchange through pgb_exchange without a buffer");
   const size_t need = (size_t)t->buffer_elems * (size_t)ncomp;
   if (need > kStaticPackDoubles)
     return fail(kErrInvalid, "packed exchange needs " + std::to_string(need) +

@@ -732,7 +732,11 @@ void vcycle(GmgLevelBuf<T> *L, int nl, const GmgConfig &c, GmgLevelBuf<double> *
         int64_t ns[kClusterLevels];
         for (int q = 0; q < ta.nlev; ++q) ns[q] = ta.lv[q].n;
         const size_t smem = cluster_tail_smem<T>(ns, ta.nlev, ta.use_c64 != 0);
-        cudaFuncSetAttribute(k_tail_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const cudaError_t attr =
+            cudaFuncSetAttribute(k_tail_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        // on failure skip the launch: the error stays the runtime's last error, which
+        // the solver's caller reads after the V-cycle is enqueued
+        if (attr != cudaSuccess) return;
         k_tail_cluster<T><<<kClusterCtas, kClusterThreads, smem, s>>>(ta);
       } else {
         k_tail<T><<<1, kTailThreads, 0, s>>>(ta);

@@ -60,6 +60,9 @@ struct MeshState {
   unsigned long long *d_minbits = nullptr;
   int *d_status = nullptr;
   std::vector<int> deref_count;     // per leaf block, MeshRefinement::deref_count_
+  // Burgers "derived" field (one component, field layout) that the RK2 cycles fill after
+  // every stage's update (pgb_set_derived); null: FillDerived is not run
+  double *derived = nullptr;
   SparseState sparse;
   // device view for the kernels, or null when the mesh has no sparse variables
   const SparseDev *sparse_dev() const { return sparse.on && sparse.dev.alloc ? &sparse.dev : nullptr; }

@@ -78,6 +78,10 @@ class RK2Driver:
                 self.dudt = mesh.new_field(ncomp)
                 self.flux = None
                 self.cbase = self.cstage = None
+            # Burgers: the package's "derived" field (one component), filled after every
+            # stage's update (FillDerived, burgers_driver.cpp:121)
+            self.derived = mesh.new_field(1) if self.cfg.physics == "burgers" else None
+        nat.check(nat.lib().pgb_set_derived(self.mesh.handle, _ptr(self.derived)), "pgb_set_derived")
 
     def rebind(self, mesh, base):
         """Continue on a new mesh (after a remesh) with `base` already on it: fresh

@@ -42,7 +42,7 @@ def lib():
             getattr(L, name).argtypes = [ctypes.c_void_p]
             getattr(L, name).restype = ctypes.c_int
         L.orc_block_info.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
-        for name in ["orc_base", "orc_base_coarse"]:
+        for name in ["orc_base", "orc_base_coarse", "orc_derived"]:
             getattr(L, name).argtypes = [ctypes.c_void_p]
             getattr(L, name).restype = DP
         for name in ["orc_field_size", "orc_coarse_size"]:
@@ -136,6 +136,14 @@ class OracleSim:
         geom = np.zeros((self.nblocks, 6), np.float64)
         lib().orc_block_info(self.h, _ptr(locs), _ptr(geom))
         return locs, geom
+
+    def derived(self):
+        """The Burgers "derived" field (nblocks, N3, N2, N1), filled after every stage."""
+        p = lib().orc_derived(self.h)
+        if not p:
+            raise RuntimeError("no derived field (advection)")
+        n = self.nblocks * self.N[0] * self.N[1] * self.N[2]
+        return np.ctypeslib.as_array(p, shape=(n,)).reshape((self.nblocks,) + self.N[::-1])
 
     def base(self):
         n = lib().orc_field_size(self.h)

@@ -132,3 +132,54 @@ def test_block_layout_solve_matches_global(method):
     for b, (lev, i, j, k) in enumerate(locs):
         assert np.array_equal(got[b, 0, 2:-2, 2:-2, 2:-2], ref[8 * k:8 * k + 8, 8 * j:8 * j + 8, 8 * i:8 * i + 8])
     assert np.array_equal(got[:, 1], fld[:, 1])  # right-hand side untouched
+
+
+# The multigrid benchmark's own configuration: 128^3 periodic Poisson, 32 Gaussians
+# (sigma 0.03, seed 4), levels down to 8^3 (max_coarsenings 4), weighted Jacobi 2/3 with
+# 2 pre + 2 post sweeps, 16 extra passes on the coarsest level.
+C4 = dict(stages=2, jacobi=True, weight=2.0 / 3.0, coarse_sweeps=16)
+
+
+def _c4_rhs():
+    return pg.problems.poisson_rhs(128, ngauss=32, sigma=0.03, seed=4)
+
+
+def test_c4_shape_exact_vcycles_bit_exact():
+    import torch
+    rhs = _c4_rhs()
+    o = O.OracleGmg(128, 4, **C4)
+    o.rhs()[:] = rhs
+    rms_o = o.run(2)
+    g = pg.GmgSolver(128, 4, exact=True, **C4)
+    u = torch.zeros((128,) * 3, dtype=torch.float64, device="cuda")
+    rms_g = g.vcycles(u, torch.tensor(rhs, device="cuda"), 2)
+    torch.cuda.synchronize()
+    assert np.array_equal(u.cpu().numpy(), o.u())
+    assert np.allclose(rms_g, rms_o, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_c4_shape_solve_to_1e10_matches_oracle(mixed):
+    import torch
+    rhs = _c4_rhs()
+    g = pg.GmgSolver(128, 4, **C4)
+    u = torch.zeros((128,) * 3, dtype=torch.float64, device="cuda")
+    cycles, rel = g.solve(u, torch.tensor(rhs, device="cuda"), mixed=mixed, rtol=1e-10, max_cycles=200)
+    assert rel <= 1e-10 and cycles < 200
+    o = O.OracleGmg(128, 4, **C4)
+    o.rhs()[:] = rhs
+    r0 = o.residual()
+    for ncyc in range(1, 201):
+        if o.run(1)[0] / r0 <= 1e-10:
+            break
+    # same smoother and tolerance: the FP64 solve (fast build) takes the oracle's cycle
+    # count within one, the mixed one at most two more
+    if mixed:
+        assert cycles <= ncyc + 2
+    else:
+        assert abs(cycles - ncyc) <= 1
+    ref = o.u() - o.u().mean()
+    got = u.cpu().numpy()
+    got = got - got.mean()
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err <= 1e-8, err

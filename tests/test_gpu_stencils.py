@@ -37,7 +37,13 @@ def _run(case, exact, ncycles):
     drv.run(ncycles, graph=True)
     drv.stream.synchronize()
     got = drv.base.cpu().numpy()
+    if physics == "burgers":
+        # FillDerived after every stage: the last stage's output
+        _DERIVED[(exact, id(case))] = (drv.derived.cpu().numpy()[:, 0], np.array(o.derived()))
     return got, np.array(o.base()), float(drv.dt.cpu()[0]), o.dt(), dt0, dts
+
+
+_DERIVED = {}
 
 
 def _advection_gaussian(m):
@@ -69,25 +75,44 @@ CASES = {
     # multilevel Burgers: stored face fluxes, flux correction, divergence update
     "smr-burgers-weno5": ((32,) * 3, (8,) * 3, 4, refined_cube(2, 1, 3), "burgers", "weno5", 5, 0.8, _burgers5),
     "smr-burgers-11": ((32,) * 3, (8,) * 3, 4, refined_cube(2, 0, 2), "burgers", "weno5", 11, 0.8, _burgers),
+    # the uniform Burgers benchmark's block shape: 32^3 blocks, 4 ghosts, 11 components
+    # (the fast sweep's shared-memory line buffers exceed 48 KB at n = 32)
+    "burgers-weno5-64-32cubed-blocks": ((64,) * 3, (32,) * 3, 4, None, "burgers", "weno5", 11, 0.8, _burgers),
+    # the static-refinement advection benchmark's own mesh: 128^3 root in 16^3 blocks,
+    # central 1/8 refined once (448 + 512 blocks), 4 ghosts, 5 components, PLM
+    "smr-advection-plm-128root-16cubed": ((128,) * 3, (16,) * 3, 4, refined_cube(3, 2, 6), "advection", "plm", 5,
+                                          0.3, _advection_smr),
 }
+
+# cycles per case (default: 10 for advection, 3 for Burgers)
+NCYCLES = {"smr-advection-plm-128root-16cubed": 2}
+
+
+def _ncycles(name):
+    return NCYCLES.get(name, 10 if "advection" in name else 3)
 
 
 @pytest.mark.parametrize("name", list(CASES))
 def test_exact_build_bit_exact(name):
-    ncycles = 10 if "advection" in name else 3
-    got, ref, dtg, dto, _, _ = _run(CASES[name], True, ncycles)
+    got, ref, dtg, dto, _, _ = _run(CASES[name], True, _ncycles(name))
     ng = CASES[name][2]
     assert dtg == dto
     assert np.array_equal(_interior(got, ng), _interior(ref, ng))
+    if CASES[name][4] == "burgers":
+        dg, do = _DERIVED.pop((True, id(CASES[name])))
+        assert np.array_equal(dg[:, ng:-ng, ng:-ng, ng:-ng], do[:, ng:-ng, ng:-ng, ng:-ng])
 
 
 @pytest.mark.parametrize("name", list(CASES))
 def test_fast_build_within_tolerance(name):
-    ncycles = 10 if "advection" in name else 3
-    got, ref, dtg, dto, _, _ = _run(CASES[name], False, ncycles)
+    got, ref, dtg, dto, _, _ = _run(CASES[name], False, _ncycles(name))
     ng = CASES[name][2]
     g, r = _interior(got, ng), _interior(ref, ng)
     scale = np.abs(r).max(axis=(0, 2, 3, 4), keepdims=True)
     err = np.abs(g - r) / scale
     assert err.max() <= REL_TOL, err.max()
     assert abs(dtg - dto) <= REL_TOL * dto
+    if CASES[name][4] == "burgers":
+        dg, do = _DERIVED.pop((False, id(CASES[name])))
+        dg, do = dg[:, ng:-ng, ng:-ng, ng:-ng], do[:, ng:-ng, ng:-ng, ng:-ng]
+        assert np.abs(dg - do).max() <= REL_TOL * np.abs(do).max()

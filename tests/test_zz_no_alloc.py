@@ -55,3 +55,14 @@ def test_static_buffer_rejects_oversized_requests():
                                               _stream(torch.cuda.current_stream()))
     assert rc == -1
     assert b"static buffer" in nat.lib().pgb_last_error()
+
+
+def test_static_buffer_rejects_sparse_meshes():
+    import torch
+    mesh = pg.Mesh((32,) * 3, (16,) * 3, 2).upload()
+    mesh.enable_sparse(2, 1e-5, 1e-6, dealloc_count=5)
+    f = torch.zeros((mesh.nblocks, 2) + tuple(mesh.N[::-1]), dtype=torch.float64, device="cuda")
+    rc = nat.lib().pgb_exchange_static_buffer(mesh.handle, _ptr(f), None, 2, 0,
+                                              _stream(torch.cuda.current_stream()))
+    assert rc == -3
+    assert b"sparse" in nat.lib().pgb_last_error()
