@@ -55,6 +55,33 @@ def sinusoid_modes(nmodes, kmax, seed):
     return modes
 
 
+def burgers_reference_state(mesh, nscalars=8, center=(0.0, 0.0, 0.0)):
+    """The Burgers benchmark's own initial condition (ProblemGenerator,
+    benchmarks/burgers/parthenon_app_inputs.cpp:34-70, with kx_fact = ky_fact = kz_fact
+    = 1) about `center` (the reference's domain is [-0.5, 0.5]^3, centre 0): tanh fronts
+    under Gaussian envelopes for the three velocity components, and scalars equal to 1
+    with 10 added in a thin box -- exactly constant regions with jumps at the box."""
+    ncomp = 3 + nscalars
+    out = np.zeros((mesh.nblocks, ncomp) + tuple(mesh.N[::-1]), np.float64)
+    sk, sj, si = _interior(mesh)
+    xs, ys, zs = _centers(mesh)
+    g = mesh.nghost
+    n = mesh.block_nx
+    x = (xs[:, g:g + n[0]] - center[0])[:, None, None, :]
+    y = (ys[:, g:g + n[1]] - center[1])[:, None, :, None]
+    z = (zs[:, g:g + n[2]] - center[2])[:, :, None, None]
+    shape = (mesh.nblocks, n[2], n[1], n[0])
+    out[:, 0, sk, sj, si] = np.broadcast_to(
+        (np.tanh(-20.0 * x) * np.cos(np.pi * x) + 1.0) * np.exp(-30.0 * y * y) * np.exp(-30.0 * z * z), shape)
+    out[:, 1, sk, sj, si] = np.broadcast_to(
+        (np.sin(np.pi * y) + 0.2) * np.exp(-30.0 * x * x) * np.exp(-30.0 * z * z), shape)
+    out[:, 2, sk, sj, si] = np.broadcast_to(
+        (np.tanh(-20.0 * z) * np.cos(np.pi * z) + 0.5) * np.exp(-30.0 * x * x) * np.exp(-30.0 * y * y), shape)
+    box = (np.abs(x) < 0.025) & (np.abs(y) < 0.15) & (np.abs(z) < 0.025)
+    out[:, 3:, sk, sj, si] = np.broadcast_to(np.where(box, 11.0, 1.0), shape)[:, None]
+    return out
+
+
 def burgers_state(mesh, nscalars=8, nmodes=8, kmax=4, seed=2):
     """Burgers velocity as a sum of random-phase sinusoids per component plus
     `nscalars` U(0,1) passive scalars, all seeded; interior filled."""

@@ -58,6 +58,11 @@ def _burgers(m):
     return pg.problems.burgers_state(m, nscalars=8, nmodes=8, kmax=4, seed=2)
 
 
+def _burgers_reference_ic(m):
+    # the reference benchmark's own initial condition, centred in the unit cube
+    return pg.problems.burgers_reference_state(m, nscalars=8, center=(0.5, 0.5, 0.5))
+
+
 def _burgers5(m):
     return pg.problems.burgers_state(m, nscalars=2, nmodes=16, kmax=6, seed=5)
 
@@ -78,6 +83,9 @@ CASES = {
     # the uniform Burgers benchmark's block shape: 32^3 blocks, 4 ghosts, 11 components
     # (the fast sweep's shared-memory line buffers exceed 48 KB at n = 32)
     "burgers-weno5-64-32cubed-blocks": ((64,) * 3, (32,) * 3, 4, None, "burgers", "weno5", 11, 0.8, _burgers),
+    # the reference's own Burgers initial condition: exactly constant scalars with a
+    # box of +10 (jumps next to constant stretches) and tanh fronts
+    "burgers-reference-ic-32": ((32,) * 3, (8,) * 3, 4, None, "burgers", "weno5", 11, 0.8, _burgers_reference_ic),
     # the static-refinement advection benchmark's own mesh: 128^3 root in 16^3 blocks,
     # central 1/8 refined once (448 + 512 blocks), 4 ghosts, 5 components, PLM
     "smr-advection-plm-128root-16cubed": ((128,) * 3, (16,) * 3, 4, refined_cube(3, 2, 6), "advection", "plm", 5,
