@@ -198,12 +198,16 @@ HLL_SCALAR_OPS = 10
 DIVUPD_OPS = 12    # per component: 3 face differences, sum, /V, average, update
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per 32^3 block with 11
-# components, from one ncu capture of the same kernels on the 128^3 mesh (64 blocks):
-# the three directional launches of one stage (414.1 + 664.3 + 670.4 MB) and one direct
-# exchange launch (319.6 MB). Traffic grows in proportion to the blocks processed.
-STAGE_DRAM_BYTES_PER_BLOCK = (414.1e6 + 664.3e6 + 670.4e6) / 64
+# From one ncu capture of the three directional launches of a stage on the 128^3 mesh
+# (64 blocks of 32^3, 11 components; profiles/burgers_dir_128cubed.md): warp
+# instructions executed (920.3 + 950.4 + 972.7 M) and DRAM bytes read + written
+# (428.2 + 681.5 + 943.2 MB), and one direct exchange launch (319.6 MB). Instructions
+# and traffic grow in proportion to the blocks processed.
+STAGE_WARP_INSTR_PER_BLOCK = (920.3e6 + 950.4e6 + 972.7e6) / 64
+STAGE_DRAM_BYTES_PER_BLOCK = (428.2e6 + 681.5e6 + 943.2e6) / 64
 EXCHANGE_DRAM_BYTES_PER_BLOCK = 319.6e6 / 64
+# instruction issue of a GB300: 152 SMs x 4 schedulers x one warp instruction per cycle
+ISSUE_PER_SM_CYCLE = 4
 
 
 def burgers_ops_per_cell_stage(n, nc):
@@ -308,6 +312,11 @@ def run_ours(args, ws, rank):
     stage_tflops = stage_flops / (stage_ms * 1e-3) / 1e12
     fp64_peak = fp64_peak_tflops(torch)
     peaks, peak_src = measured_peaks()
+    clk_summary = clk.summary()
+    sm_mhz = clk_summary.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    issue_peak = ISSUE_PER_SM_CYCLE * nsm * sm_mhz * 1e6  # warp instructions per second
+    issue_achieved = STAGE_WARP_INSTR_PER_BLOCK * mesh.nblocks / (stage_ms * 1e-3)
 
     # --- end-to-end through the C ABI with host buffers ----------------------------
     host_in = torch.from_numpy(state).pin_memory()
@@ -335,14 +344,17 @@ def run_ours(args, ws, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "parallelism": "replicas" if ws > 1 else "single-gpu",
         "config": workload_config(args.mesh),
-        "roofline": {"kernel": "k_burgers_dir (3 directional launches per stage)", "bound": "fp64",
-                     "achieved": stage_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
-                     "frac": stage_tflops / fp64_peak, "traffic": STAGE_DRAM_BYTES_PER_BLOCK * mesh.nblocks,
+        "roofline": {"kernel": "k_burgers_dir (3 directional launches per stage)", "bound": "issue",
+                     "achieved": issue_achieved, "peak": issue_peak, "unit": "warp instructions/s",
+                     "frac": issue_achieved / issue_peak, "traffic": STAGE_DRAM_BYTES_PER_BLOCK * mesh.nblocks,
                      "traffic_unit": "DRAM bytes per stage (ncu, scaled by blocks)",
-                     "peak_source": "cuBLAS DGEMM measured in this run",
-                     "ops_per_cell_stage": ops_cell, "stage_ms": stage_ms,
+                     "peak_source": "4 warp instructions per SM cycle x SMs x sampled SM clock",
+                     "instructions_source": "ncu warp instructions per launch on 64 blocks, scaled by blocks",
+                     "stage_ms": stage_ms,
                      "hbm_achieved_gbs": stage_hbm_bytes / (stage_ms * 1e-3) / 1e9,
-                     "hbm_frac": stage_hbm_bytes / (stage_ms * 1e-3) / 1e9 / peak_hbm},
+                     "hbm_frac": stage_hbm_bytes / (stage_ms * 1e-3) / 1e9 / peak_hbm,
+                     "reference_fp64_ops_per_cell_stage": ops_cell,
+                     "reference_fp64_tflops_equivalent": stage_tflops, "fp64_dgemm_tflops": fp64_peak},
         "exchange_roofline": {"kernel": "k_copy (direct ghost copy)", "bound": "hbm", "achieved": xchg_gbs,
                               "peak": peak_hbm, "unit": "GB/s", "frac": xchg_gbs / peak_hbm,
                               "traffic": EXCHANGE_DRAM_BYTES_PER_BLOCK * mesh.nblocks,
@@ -353,7 +365,7 @@ def run_ours(args, ws, rank):
                                        "ms": bxchg_ms, "peak_source": peak_src},
         "e2e": e2e,
         "gpu_launches": 12 * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clk_summary,
     }
     detail = {"autotune": {k: {"choice": c, "ms": t} for k, (c, t) in nat.tune_report().items()}}
     if rank == 0 and ws == 1:

@@ -1,0 +1,131 @@
+// Package-facing compatibility layer: basic types, error macros and the device stream.
+//
+// The compatibility layer gives package code written for Parthenon (StateDescriptor,
+// Metadata, Params, TaskList, MeshData packs, par_for / par_for_outer / par_reduce) a
+// GB300 implementation: device lambdas run as CUDA kernels written here, ghost
+// exchanges and flux correction go through the library's C ABI
+// (include/parthenon_gb300.h). Names, signatures and semantics follow the reference
+// interfaces cited in each header; the implementation is this project's own.
+//
+// Reference: src/basic_types.hpp (Real, TaskStatus, IndexRange), src/defs.hpp
+// (CoordinateDirection), src/utils/error_checking.hpp (PARTHENON_REQUIRE & co.),
+// src/kokkos_abstraction.hpp (DevExecSpace).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cassert>
+#include <cstdio>
+#include <cstdlib>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+
+#include "parthenon_gb300.h"
+
+#ifndef KOKKOS_LAMBDA
+#define KOKKOS_LAMBDA [=] __host__ __device__
+#endif
+#ifndef KOKKOS_INLINE_FUNCTION
+#define KOKKOS_INLINE_FUNCTION __host__ __device__ inline
+#endif
+#ifndef KOKKOS_FORCEINLINE_FUNCTION
+#define KOKKOS_FORCEINLINE_FUNCTION __host__ __device__ __forceinline__
+#endif
+#ifndef KOKKOS_FUNCTION
+#define KOKKOS_FUNCTION __host__ __device__
+#endif
+
+// Kernel labels: the reference passes a "file::line::function" string; here any string
+#define PARTHENON_AUTO_LABEL (__FILE__ "::" PGB_COMPAT_STR(__LINE__))
+#define PGB_COMPAT_STR2(x) #x
+#define PGB_COMPAT_STR(x) PGB_COMPAT_STR2(x)
+// Profiling regions (src/utils/instrument.hpp): no-ops
+#define PARTHENON_INSTRUMENT
+#define PARTHENON_INSTRUMENT_REGION(name)
+
+namespace parthenon {
+
+using Real = double;
+
+// src/basic_types.hpp
+enum class TaskStatus { complete, incomplete, iterate, fail };
+enum class IndexDomain {
+  entire,
+  interior,
+  inner_x1,
+  outer_x1,
+  inner_x2,
+  outer_x2,
+  inner_x3,
+  outer_x3
+};
+enum class TopologicalElement { CC, F1, F2, F3, E1, E2, E3, NN };
+
+struct IndexRange {
+  int s = 0;  // first index
+  int e = 0;  // last index (inclusive)
+  KOKKOS_INLINE_FUNCTION int size() const { return e - s + 1; }
+  KOKKOS_INLINE_FUNCTION operator bool() const { return e >= s; }
+};
+
+// src/defs.hpp CoordinateDirection
+enum CoordinateDirection { NODIR = -1, X0DIR = 0, X1DIR = 1, X2DIR = 2, X3DIR = 3 };
+
+// src/utils/error_checking.hpp
+namespace ErrorChecking {
+[[noreturn]] inline void fail_throws(const char *cond, const std::string &msg, const char *file, int line) {
+  std::ostringstream os;
+  os << "### PARTHENON ERROR\n  Condition:   " << cond << "\n  Message:     " << msg << "\n  File:        " << file
+     << "\n  Line number: " << line;
+  throw std::runtime_error(os.str());
+}
+inline void warn(const std::string &msg, const char *file, int line) {
+  std::fprintf(stderr, "### PARTHENON WARNING\n  Message:     %s\n  File:        %s\n  Line number: %d\n", msg.c_str(),
+               file, line);
+}
+}  // namespace ErrorChecking
+
+// src/kokkos_abstraction.hpp: the execution space the kernels run on. Every compat
+// kernel and library call is ordered on one CUDA stream, created at start-up.
+struct DevExecSpace {
+  cudaStream_t stream() const;
+  void fence() const;
+};
+
+// The layer's stream (created on first use; graph capture and the library's calls use it).
+inline cudaStream_t &compat_stream_ref() {
+  static cudaStream_t s = nullptr;
+  return s;
+}
+inline cudaStream_t compat_stream() {
+  cudaStream_t &s = compat_stream_ref();
+  if (!s && cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+    throw std::runtime_error("cannot create the compatibility layer's CUDA stream");
+  return s;
+}
+inline cudaStream_t DevExecSpace::stream() const { return compat_stream(); }
+inline void DevExecSpace::fence() const {
+  const cudaError_t e = cudaStreamSynchronize(compat_stream());
+  if (e != cudaSuccess) throw std::runtime_error(std::string("device fault: ") + cudaGetErrorString(e));
+}
+
+inline void check_cuda(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+inline void check_pgb(int rc, const char *what) {
+  if (rc != PGB_OK) throw std::runtime_error(std::string(what) + ": " + pgb_last_error());
+}
+
+}  // namespace parthenon
+
+#define PARTHENON_REQUIRE(cond, msg)                                                         \
+  do {                                                                                       \
+    if (!(cond)) ::parthenon::ErrorChecking::fail_throws(#cond, msg, __FILE__, __LINE__);    \
+  } while (0)
+#define PARTHENON_REQUIRE_THROWS(cond, msg) PARTHENON_REQUIRE(cond, msg)
+#define PARTHENON_FAIL(msg) ::parthenon::ErrorChecking::fail_throws("false", msg, __FILE__, __LINE__)
+#define PARTHENON_THROW(msg) PARTHENON_FAIL(msg)
+#define PARTHENON_WARN(msg) ::parthenon::ErrorChecking::warn(msg, __FILE__, __LINE__)
+#define PARTHENON_DEBUG_REQUIRE(cond, msg)
+#define PARTHENON_DEBUG_REQUIRE_THROWS(cond, msg)

@@ -1,0 +1,196 @@
+// Package-facing compatibility layer: Metadata flags, StateDescriptor (a package's
+// fields, parameters and hooks), the package registry and history-output records.
+//
+// Reference: src/interface/metadata.hpp:40-110 (flag list), :201 (Metadata),
+// src/interface/state_descriptor.hpp:79-391 (AddField, AddParam/Param/AllParams,
+// EstimateTimestepMesh/Block, FillDerivedMesh/Block, CheckRefinementBlock hooks),
+// src/interface/packages.hpp (Packages_t), src/outputs/output_utils.hpp and
+// src/interface/params.hpp (HistoryOutputVar, UserHistoryOperation, hist_param_key).
+#pragma once
+
+#include <functional>
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "core.hpp"
+#include "params.hpp"
+
+namespace parthenon {
+
+template <typename T>
+class MeshData;
+template <typename T>
+class MeshBlockData;
+class Mesh;
+class MeshBlock;
+
+class MetadataFlag {
+ public:
+  constexpr explicit MetadataFlag(int id) : id_(id) {}
+  constexpr int id() const { return id_; }
+  bool operator==(const MetadataFlag &o) const { return id_ == o.id_; }
+  bool operator!=(const MetadataFlag &o) const { return id_ != o.id_; }
+  bool operator<(const MetadataFlag &o) const { return id_ < o.id_; }
+
+ private:
+  int id_;
+};
+
+class Metadata {
+ public:
+  // the reference's flag set (metadata.hpp:40-110)
+  static inline const MetadataFlag None{0}, Cell{1}, Face{2}, Edge{3}, Node{4}, Particle{5}, Swarm{6}, Private{7},
+      Provides{8}, Requires{9}, Overridable{10}, Vector{11}, Tensor{12}, Boolean{13}, Integer{14}, Real{15},
+      Independent{16}, Derived{17}, Advected{18}, Conserved{19}, Intensive{20}, Restart{21}, Sparse{22},
+      SparseCommunication{23}, OneCopy{24}, FillGhost{25}, WithFluxes{26}, Flux{27}, ForceRemeshComm{28},
+      GMGProlongate{29}, GMGRestrict{30}, Fine{31}, CellMemAligned{32}, Ignore{33};
+
+  Metadata() = default;
+  Metadata(const std::vector<MetadataFlag> &bits, const std::vector<int> &shape = {},
+           const std::vector<std::string> &component_labels = {})
+      : shape_(shape), labels_(component_labels) {
+    for (const auto &b : bits) flags_.insert(b);
+    if (!IsSet(Cell) && !IsSet(Face) && !IsSet(Edge) && !IsSet(Node)) flags_.insert(Cell);
+  }
+  bool IsSet(const MetadataFlag &f) const { return flags_.count(f) > 0; }
+  bool AllFlagsSet(const std::vector<MetadataFlag> &fs) const {
+    for (const auto &f : fs)
+      if (!IsSet(f)) return false;
+    return true;
+  }
+  bool AnyFlagsSet(const std::vector<MetadataFlag> &fs) const {
+    for (const auto &f : fs)
+      if (IsSet(f)) return true;
+    return false;
+  }
+  void Set(const MetadataFlag &f) { flags_.insert(f); }
+  void Unset(const MetadataFlag &f) { flags_.erase(f); }
+  const std::vector<int> &Shape() const { return shape_; }
+  // number of components: the product of the shape (a scalar when empty)
+  int NumComponents() const {
+    int n = 1;
+    for (int s : shape_) n *= s;
+    return n;
+  }
+  const std::vector<std::string> &getComponentLabels() const { return labels_; }
+
+ private:
+  std::set<MetadataFlag> flags_;
+  std::vector<int> shape_;
+  std::vector<std::string> labels_;
+};
+
+// refinement tags (src/amr_criteria/amr_criteria.hpp AmrTag)
+enum class AmrTag : int { derefine = -1, same = 0, refine = 1 };
+
+enum class UserHistoryOperation { sum, max, min };
+using HstFun = std::function<Real(MeshData<Real> *md)>;
+struct HistoryOutputVar {
+  UserHistoryOperation hst_op;
+  HstFun hst_fun;
+  std::string label;
+  HistoryOutputVar(const UserHistoryOperation &op, const HstFun &f, const std::string &l)
+      : hst_op(op), hst_fun(f), label(l) {}
+};
+using HstVar_list = std::vector<HistoryOutputVar>;
+inline const std::string hist_param_key = "HistoryFunctions";
+
+class StateDescriptor {
+ public:
+  explicit StateDescriptor(const std::string &label) : label_(label) {}
+  const std::string &label() const { return label_; }
+
+  template <class T>
+  void AddParam(const std::string &key, T value, Params::Mutability m) {
+    params_.Add(key, std::move(value), m);
+  }
+  template <class T>
+  void AddParam(const std::string &key, T value, bool is_mutable = false) {
+    params_.Add(key, std::move(value), is_mutable);
+  }
+  template <class T>
+  void UpdateParam(const std::string &key, T value) {
+    params_.Update(key, std::move(value));
+  }
+  template <class T>
+  const T &Param(const std::string &key) const {
+    return params_.Get<T>(key);
+  }
+  template <class T>
+  T *MutableParam(const std::string &key) const {
+    return params_.GetMutable<T>(key);
+  }
+  Params &AllParams() noexcept { return params_; }
+  const Params &AllParams() const noexcept { return params_; }
+
+  // a cell-centred field; returns false when the name is taken
+  bool AddField(const std::string &name, const Metadata &m) {
+    for (const auto &f : fields_)
+      if (f.first == name) return false;
+    PARTHENON_REQUIRE_THROWS(m.IsSet(Metadata::Cell),
+                             "field " + name + ": only cell-centred fields are on this path");
+    PARTHENON_REQUIRE_THROWS(!m.IsSet(Metadata::Sparse), "field " + name + ": sparse fields go through the C ABI");
+    fields_.emplace_back(name, m);
+    return true;
+  }
+  const std::vector<std::pair<std::string, Metadata>> &AllFields() const { return fields_; }
+
+  // hooks (state_descriptor.hpp:297-391)
+  void PreCommFillDerived(MeshData<Real> *rc) const {
+    if (PreCommFillDerivedMesh) PreCommFillDerivedMesh(rc);
+  }
+  void PreFillDerived(MeshData<Real> *rc) const {
+    if (PreFillDerivedMesh) PreFillDerivedMesh(rc);
+  }
+  void FillDerived(MeshData<Real> *rc) const {
+    if (FillDerivedMesh) FillDerivedMesh(rc);
+  }
+  void PostFillDerived(MeshData<Real> *rc) const {
+    if (PostFillDerivedMesh) PostFillDerivedMesh(rc);
+  }
+  Real EstimateTimestep(MeshData<Real> *rc) const;  // mesh.hpp: block hooks need the blocks
+
+  std::function<void(MeshBlockData<Real> *rc)> PreCommFillDerivedBlock = nullptr;
+  std::function<void(MeshData<Real> *rc)> PreCommFillDerivedMesh = nullptr;
+  std::function<void(MeshBlockData<Real> *rc)> PreFillDerivedBlock = nullptr;
+  std::function<void(MeshData<Real> *rc)> PreFillDerivedMesh = nullptr;
+  std::function<void(MeshBlockData<Real> *rc)> PostFillDerivedBlock = nullptr;
+  std::function<void(MeshData<Real> *rc)> PostFillDerivedMesh = nullptr;
+  std::function<void(MeshBlockData<Real> *rc)> FillDerivedBlock = nullptr;
+  std::function<void(MeshData<Real> *rc)> FillDerivedMesh = nullptr;
+  std::function<Real(MeshBlockData<Real> *rc)> EstimateTimestepBlock = nullptr;
+  std::function<Real(MeshData<Real> *rc)> EstimateTimestepMesh = nullptr;
+  std::function<AmrTag(MeshBlockData<Real> *rc)> CheckRefinementBlock = nullptr;
+
+ private:
+  std::string label_;
+  Params params_;
+  std::vector<std::pair<std::string, Metadata>> fields_;
+};
+
+class Packages_t {
+ public:
+  void Add(const std::shared_ptr<StateDescriptor> &pkg) {
+    PARTHENON_REQUIRE_THROWS(!packages_.count(pkg->label()), "package " + pkg->label() + " added twice");
+    packages_[pkg->label()] = pkg;
+    order_.push_back(pkg->label());
+  }
+  std::shared_ptr<StateDescriptor> const &Get(const std::string &name) const {
+    auto it = packages_.find(name);
+    PARTHENON_REQUIRE_THROWS(it != packages_.end(), "no package named " + name);
+    return it->second;
+  }
+  const std::map<std::string, std::shared_ptr<StateDescriptor>> &AllPackages() const { return packages_; }
+  // registration order (fields are laid out in it)
+  const std::vector<std::string> &Order() const { return order_; }
+
+ private:
+  std::map<std::string, std::shared_ptr<StateDescriptor>> packages_;
+  std::vector<std::string> order_;
+};
+
+}  // namespace parthenon

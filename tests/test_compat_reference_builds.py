@@ -1,0 +1,26 @@
+"""The reference's own Burgers benchmark application (benchmarks/burgers: package,
+driver, problem generator, main) compiles and links against the package-facing
+compatibility layer and libparthenon_gb300.so without a changed line.
+
+The reference sources are read where they lie when they are available (this is the one
+test that reads them); the test is skipped elsewhere. Nothing is copied into the
+repository and the binary is only built, not run (the GPU runs of the layer use the
+repository's own package, tests/test_gpu_compat_burgers.py).
+"""
+import os
+
+import pytest
+
+from compat_build import compile_objects, link
+
+REFERENCE = os.environ.get("PARTHENON_REFERENCE_DIR", "/root/reference")
+BURGERS = os.path.join(REFERENCE, "benchmarks", "burgers")
+
+
+@pytest.mark.skipif(not os.path.isdir(BURGERS), reason="reference sources not available here")
+def test_reference_burgers_app_builds_unchanged():
+    srcs = [os.path.join(BURGERS, f) for f in
+            ("burgers_package.cpp", "burgers_driver.cpp", "parthenon_app_inputs.cpp", "main.cpp")]
+    objs = compile_objects(srcs, "refburgers", include=(BURGERS,))
+    exe = link(objs, "reference_burgers_app")
+    assert os.path.getsize(exe) > 0
