@@ -69,11 +69,14 @@ PGB_DF float ffma(float a, float b, float c) {
   return std::fmaf(a, b, c);
 #endif
 }
-// single-precision reciprocal seed (about 23 correct bits is plenty: the Newton step in
-// df_recip doubles it)
+// single-precision reciprocal seed: the hardware approximation (within 1 ulp) on the
+// device, the correctly rounded quotient on the host; the Newton step in recip() squares
+// its error either way
 PGB_DF float frcp(float a) {
 #if defined(__CUDA_ARCH__)
-  return __frcp_rn(a);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
 #else
   return 1.0f / a;
 #endif
@@ -155,6 +158,12 @@ PGB_DF df add(df a, float b) {
   s.lo = fadd(s.lo, a.lo);
   return fast_two_sum(s.hi, s.lo);
 }
+// a + b when |a.hi| >= |b| (or a == 0): one fast two-sum instead of a two-sum
+PGB_DF df add_dominant(df a, float b) {
+  df s = fast_two_sum(a.hi, b);
+  s.lo = fadd(s.lo, a.lo);
+  return fast_two_sum(s.hi, s.lo);
+}
 PGB_DF df mul(df a, df b) {
   df p = two_prod(a.hi, b.hi);
   p.lo = ffma(a.hi, b.lo, p.lo);
@@ -172,8 +181,37 @@ PGB_DF df sqr(df a) {
   p.lo = ffma(fadd(a.hi, a.hi), a.lo, p.lo);
   return fast_two_sum(p.hi, p.lo);
 }
+// ---- unnormalised variants ----------------------------------------------------------
+// The same sums and products without the final renormalisation: the pair's value is
+// kept as accurately, but lo may exceed ulp(hi)/2 (after a cancellation hi may even be 0
+// while lo is not). Sums of such pairs stay accurate. A product drops lo*lo, so its
+// factors must be normalised (a larger lo costs it accuracy); sign tests, comparisons,
+// reciprocals and exponent reads also need norm() first.
+PGB_DF df norm(df a) { return fast_two_sum(a.hi, a.lo); }
+PGB_DF df addu(df a, df b) {
+  const df s = two_sum(a.hi, b.hi);
+  return {s.hi, fadd(s.lo, fadd(a.lo, b.lo))};
+}
+PGB_DF df subu(df a, df b) { return addu(a, neg(b)); }
+PGB_DF df addu(df a, float b) {
+  const df s = two_sum(a.hi, b);
+  return {s.hi, fadd(s.lo, a.lo)};
+}
+PGB_DF df mulu(df a, df b) {
+  const df p = two_prod(a.hi, b.hi);
+  return {p.hi, ffma(a.lo, b.hi, ffma(a.hi, b.lo, p.lo))};
+}
+PGB_DF df mulu(df a, float b) {
+  const df p = two_prod(a.hi, b);
+  return {p.hi, ffma(a.lo, b, p.lo)};
+}
+PGB_DF df sqru(df a) {
+  const df p = two_prod(a.hi, a.hi);
+  return {p.hi, ffma(fadd(a.hi, a.hi), a.lo, p.lo)};
+}
+
 // 1/a: single-precision seed r, residual 1 - a r formed exactly from two_prod, one
-// Newton correction (relative error about 2^-46)
+// Newton correction (relative error about 2^-45)
 PGB_DF df recip(df a) {
   const float r = frcp(a.hi);
   const df p = two_prod(a.hi, r);                      // a.hi r exactly

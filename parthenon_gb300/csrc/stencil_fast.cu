@@ -90,6 +90,7 @@ __device__ __forceinline__ void weno5z(double q0, double q1, double q2, double q
 }  // namespace fast
 }  // namespace pgb
 
+#include "advection_df.cuh"
 #include "stencil_impl.cuh"
 #include "burgers_fast.cuh"
 #define PGB_HAVE_BURGERS_FAST 1

@@ -192,31 +192,24 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
   const double area = g.area[D];
   const double *__restrict__ u = a.u_in;
   const double vd = a.ncvel ? a.cvel[v][D] : a.vel[D];
-  [[maybe_unused]] const int pos0 = D == 0 ? m.i0 : (D == 1 ? m.j0 : m.k0);
-  double Lprev = 0.0, AFprev = 0.0;
 #ifndef PGB_EXACT_ARITH
-  // PLM: the window is carried along the line, so each cell costs one load and one
-  // difference (its left difference is the previous cell's right one)
-  double qc = 0.0, dql = 0.0;
+  // fast build, PLM: the line in double-float pairs (advection_df.cuh)
   if (a.recon != 0) {
-    qc = ld<D>(u, c0 - step);
-    dql = qc - ld<D>(u, c0 - 2 * step);
+    plm_line_df<D, MODE>(a, b, v, c0, m.n, cs, step, g, vd);
+    return;
   }
 #endif
+  [[maybe_unused]] const int pos0 = D == 0 ? m.i0 : (D == 1 ? m.j0 : m.k0);
+  double Lprev = 0.0, AFprev = 0.0;
   for (int p = -1; p <= n; ++p) {
     const int64_t e = c0 + (int64_t)p * step;
-    // donor cell or PLM (plm_inline.hpp, uniform van Leer)
-#ifdef PGB_EXACT_ARITH
+    // donor cell, or PLM in the exact build (plm_inline.hpp, uniform van Leer)
     const double q0 = ld<D>(u, e);
-#else
-    const double q0 = a.recon != 0 ? qc : ld<D>(u, e);
-#endif
     double Lc, Rc;
     if (a.recon == 0) {
       Lc = q0;
       Rc = q0;
     } else {
-#ifdef PGB_EXACT_ARITH
       // the face weights from the cell-centre and face coordinates (plm_inline.hpp); x / dx
       // as an exact multiplication when dx is a power of two (div_rn)
       const int pos = pos0 + p;
@@ -231,21 +224,6 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
       if (dq2 <= 0.0) dqm = 0.0;
       Lc = q0 + cp_ * dqm;
       Rc = q0 - cm_ * dqm;
-#else
-      // uniform Cartesian cells: both face weights are 1/2 (the coordinate form rounds
-      // to within an ulp of it), so the face values are q0 +- dq2 / (dql + dqr), half
-      // the van Leer slope, with a refined reciprocal (FP64 divides bound this sweep).
-      // A zero denominator means dq2 <= 0, where the slope is zero.
-      const double qn = ld<D>(u, e + step);
-      const double dqr = qn - q0;
-      const double dq2 = dql * dqr;
-      double r = recip(dql + dqr);
-      if (dq2 <= 0.0) r = 0.0;
-      Lc = fma(dq2, r, q0);
-      Rc = fma(-dq2, r, q0);
-      dql = dqr;
-      qc = qn;
-#endif
     }
     if (p >= 0) {
       const double F = vd > 0.0 ? Lprev * vd : Rc * vd;

@@ -99,15 +99,20 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df e3 = from_double(e3d, w.off);
   const df q4p = from_double(q4, w.off);
   const df e0 = w.e0, e1 = w.e1, e2 = w.e2;
+  // Sums and the products that only feed sums keep their pairs unnormalised
+  // (dfloat.cuh addu/mulu/sqru, from normalised operands); every pair that enters a
+  // product, a sign test, a comparison or a reciprocal is normalised first (an
+  // unnormalised factor's larger lo would cost the product accuracy, and after a
+  // cancellation a pair holds its value in lo).
   // smoothness indicators (recon.hpp:54-64 in first differences)
-  const df t2c = t2_of(sub(e3, e2));
-  const df b0 = sub(mul(e1, 3.0f), e0);
-  const df b1 = add(e1, e2);
-  const df b2 = sub(e3, mul(e2, 3.0f));
-  const df be0 = add(add(sqr(b0), w.t2a), w.eps_b);
-  const df be1 = add(add(sqr(b1), w.t2b), w.eps_b);
-  const df be2 = add(add(sqr(b2), t2c), w.eps_b);
-  const df tau = dabs(sub(be2, be0));
+  const df t2c = t2_of(norm(subu(e3, e2)));
+  const df b0 = norm(subu(mulu(e1, 3.0f), e0));
+  const df b1 = norm(addu(e1, e2));
+  const df b2 = norm(subu(e3, mulu(e2, 3.0f)));
+  const df be0 = addu(addu(sqru(b0), w.t2a), w.eps_b);
+  const df be1 = addu(addu(sqru(b1), w.t2b), w.eps_b);
+  const df be2 = addu(addu(sqru(b2), t2c), w.eps_b);
+  const df tau = dabs(norm(subu(be2, be0)));
   bool fast = true;
   df B0 = make(1.0f), B1 = make(1.0f), B2 = make(1.0f);
   if (tau.hi != 0.0f && !w.eps_only) {
@@ -121,11 +126,12 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
     B1 = add(mul(tau, recip(be1)), 1.0f);
     B2 = add(mul(tau, recip(be2)), 1.0f);
   }
-  // nonlinear weights (unnormalised) and their sums
-  const df l0 = add(mul(B0, kG0), kEpsF), l1 = add(mul(B1, kG1), kEpsF), l2 = add(mul(B2, kG2), kEpsF);
-  const df r0 = add(mul(B2, kG0), kEpsF), r2 = add(mul(B0, kG2), kEpsF);
-  const df SL = add(add(l0, l1), l2);
-  const df SR = add(add(r0, l1), r2);
+  // nonlinear weights (unnormalised) and their sums (g_k B_k >= 0.1 dominates eps)
+  const df l0 = add_dominant(mul(B0, kG0), kEpsF), l1 = add_dominant(mul(B1, kG1), kEpsF),
+           l2 = add_dominant(mul(B2, kG2), kEpsF);
+  const df r0 = add_dominant(mul(B2, kG0), kEpsF), r2 = add_dominant(mul(B0, kG2), kEpsF);
+  const df SL = add(addu(l0, l1), l2);
+  const df SR = add(addu(r0, l1), r2);
   const df isL = recip(SL), isR = recip(SR);
   // blending coefficients alpha_l = 3 E3/(E2 S_L) + eps, alpha_r likewise, and their
   // harmonic mean alpha_lin = 2 al ar / (al + ar)
@@ -135,14 +141,14 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df al = add(mul(F3, isL), kEpsF), ar = add(mul(F3, isR), kEpsF);
   const df alin = scale(mul(mul(al, ar), recip(add(al, ar))), 2.0f);
   // 6 (P_k - q2) for the candidate polynomials of both faces (recon.hpp:45-47,69-85)
-  const df d0 = sub(mul(e1, 5.0f), scale(e0, 2.0f));
-  const df d1 = add(e1, scale(e2, 2.0f));
-  const df d2 = sub(scale(e2, 4.0f), e3);
-  const df d0r = sub(scale(e3, 2.0f), mul(e2, 5.0f));
-  const df d1r = neg(add(scale(e1, 2.0f), e2));
-  const df d2r = sub(e0, scale(e1, 4.0f));
-  const df XL = mul(add(add(mul(l0, d0), mul(l1, d1)), mul(l2, d2)), mul(isL, kSixth));
-  const df XR = mul(add(add(mul(r0, d0r), mul(l1, d1r)), mul(r2, d2r)), mul(isR, kSixth));
+  const df d0 = norm(subu(mulu(e1, 5.0f), scale(e0, 2.0f)));
+  const df d1 = norm(addu(e1, scale(e2, 2.0f)));
+  const df d2 = norm(subu(scale(e2, 4.0f), e3));
+  const df d0r = norm(subu(scale(e3, 2.0f), mulu(e2, 5.0f)));
+  const df d1r = neg(norm(addu(scale(e1, 2.0f), e2)));
+  const df d2r = norm(subu(e0, scale(e1, 4.0f)));
+  const df XL = mul(norm(addu(addu(mulu(l0, d0), mulu(l1, d1)), mulu(l2, d2))), mul(isL, kSixth));
+  const df XR = mul(norm(addu(addu(mulu(r0, d0r), mulu(l1, d1r)), mulu(r2, d2r))), mul(isR, kSixth));
   // MC-limited slope (recon.hpp:27-40, 87-88): dq = sign(s) min(|s|/4, |e1|, |e2|) when
   // e1 and e2 have the same sign (both nonzero), else 0; s = e1 + e2 = b1
   const bool same = (e1.hi > 0.0f && e2.hi > 0.0f) || (e1.hi < 0.0f && e2.hi < 0.0f);
@@ -150,8 +156,8 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   df dq = b1.hi < 0.0f ? neg(mag) : mag;
   if (!same) dq = make(0.0f);
   // blend (recon.hpp:90-92) about q2
-  ql = add(w.q2, add(dq, mul(alin, sub(XL, dq))));
-  qr = add(w.q2, sub(mul(alin, add(XR, dq)), dq));
+  ql = norm(addu(w.q2, addu(dq, mul(alin, norm(subu(XL, dq))))));
+  qr = norm(addu(w.q2, subu(mul(alin, norm(addu(XR, dq))), dq)));
   // advance
   w.q3d = q4;
   w.q2 = w.q3;
