@@ -189,7 +189,10 @@ int pgb_rk2_cycles(pgb_mesh *mesh, const pgb_stage_params *p, double *base, doub
 
 /* Host-buffer entry point: copies host_in (interior+ghosts, the field layout) to the
  * device, exchanges ghosts, runs ncycles RK2 cycles and copies the result back.
- * *dt_inout: in, the current dt (<= 0: estimate the initial dt); out, the next dt. */
+ * *dt_inout: in, the current dt (<= 0: estimate the initial dt); out, the next dt.
+ * The device buffers it needs (two fields, the increment or flux scratch, the coarse
+ * buffers, a stream) belong to the mesh handle and are kept between calls of the same
+ * sizes; pgb_release_host_workspace or pgb_mesh_destroy frees them. */
 int pgb_run_host(pgb_mesh *mesh, const pgb_stage_params *p, const double *host_in, double *host_out, int32_t ncomp,
                  int32_t ncycles, double *dt_inout);
 /* The same, and dt_cycles (host, ncycles doubles; may be NULL) receives the dt of the
@@ -197,6 +200,9 @@ int pgb_run_host(pgb_mesh *mesh, const pgb_stage_params *p, const double *host_i
  * scalar result a driver would log). */
 int pgb_run_host_dt(pgb_mesh *mesh, const pgb_stage_params *p, const double *host_in, double *host_out,
                     int32_t ncomp, int32_t ncycles, double *dt_inout, double *dt_cycles);
+/* Frees the device buffers that pgb_run_host* keep in the mesh handle (waits for their
+ * stream first). The next pgb_run_host* call allocates them again. */
+int pgb_release_host_workspace(pgb_mesh *mesh);
 
 /* ---------------------------------------------------------------- multigrid
  * Geometric multigrid for div(grad u) = rhs on a uniform periodic cube of n^3 cells

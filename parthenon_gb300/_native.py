@@ -74,6 +74,7 @@ _SIGNATURES = {
                        ctypes.c_int32, ctypes.c_int32, VP],
     "pgb_run_host": [VP, ctypes.POINTER(StageParams), VP, VP, ctypes.c_int32, ctypes.c_int32, DP],
     "pgb_run_host_dt": [VP, ctypes.POINTER(StageParams), VP, VP, ctypes.c_int32, ctypes.c_int32, DP, DP],
+    "pgb_release_host_workspace": [VP],
     "pgb_gmg_create": [ctypes.POINTER(GmgParams), ctypes.POINTER(VP)],
     "pgb_gmg_destroy": [VP],
     "pgb_gmg_vcycles": [VP, VP, VP, ctypes.c_int32, VP, VP],

@@ -55,13 +55,37 @@ int launch_div_update(const StageArgs &a, int ncomp, cudaStream_t s);
 
 using namespace pgb;
 
+// Device buffers of the host-buffer entry points (pgb_run_host*), kept between calls so
+// that a driver calling them once per output interval pays for the allocation once. Sized
+// for one field of n values (and nc coarse values on multilevel meshes); a call with other
+// sizes frees and reallocates them.
+struct HostRunWorkspace {
+  size_t n = 0, nc = 0, nd = 0;
+  bool ml = false;
+  double *base = nullptr, *stage = nullptr, *dudt = nullptr, *flux = nullptr, *cb = nullptr, *cs = nullptr,
+         *dt = nullptr, *derived = nullptr;
+  double *dt_pinned = nullptr;  // per-cycle dt read-back (pinned host memory)
+  size_t dt_pinned_cap = 0;
+  cudaStream_t s = nullptr;
+  void release() {
+    double *ps[] = {base, stage, dudt, flux, cb, cs, dt, derived};
+    for (double *q : ps)
+      if (q) cudaFree(q);
+    if (dt_pinned) cudaFreeHost(dt_pinned);
+    if (s) cudaStreamDestroy(s);
+    *this = HostRunWorkspace();
+  }
+};
+
 struct pgb_mesh {
   MeshState st;
   // cached cycle graphs keyed by the bytes of the pointers and parameters they were
   // captured with
   std::map<std::string, cudaGraphExec_t> graphs;
+  HostRunWorkspace host_ws;
   ~pgb_mesh() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    host_ws.release();
   }
 };
 
@@ -467,72 +491,84 @@ int pgb_run_host_dt(pgb_mesh *m, const pgb_stage_params *p, const double *host_i
   const GridTables &t = m->st.leaf;
   const size_t n = (size_t)t.nblocks * ncomp * t.dims.N[0] * t.dims.N[1] * t.dims.N[2];
   const size_t nc = (size_t)t.nblocks * ncomp * t.dims.Nc[0] * t.dims.Nc[1] * t.dims.Nc[2];
+  // Burgers: the package's derived field, filled after every stage (FillDerived)
+  const size_t nd = p->physics == 1 ? (size_t)t.nblocks * t.dims.N[0] * t.dims.N[1] * t.dims.N[2] : 0;
   const bool ml = t.multilevel;
-  double *base = nullptr, *stage = nullptr, *dudt = nullptr, *flux = nullptr, *cb = nullptr, *cs = nullptr,
-         *dt = nullptr, *dt_pinned = nullptr, *derived = nullptr;
-  cudaStream_t s = nullptr;
-  auto cleanup = [&]() {
-    double *ps[] = {base, stage, dudt, flux, cb, cs, dt, derived};
-    for (double *q : ps)
-      if (q) cudaFree(q);
-    if (dt_pinned) cudaFreeHost(dt_pinned);
-    if (s) cudaStreamDestroy(s);
-  };
-  auto guard = [&](cudaError_t e, const char *w) {
+  HostRunWorkspace &w = m->host_ws;
+  // a failure frees the workspace, so that the next call starts from nothing
+  auto guard = [&](cudaError_t e, const char *what) {
     if (e != cudaSuccess) {
-      int r = check_cuda(e, w);
-      cleanup();
+      int r = check_cuda(e, what);
+      w.release();
       return r;
     }
     return 0;
   };
-  if ((rc = guard(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream"))) return rc;
-  if ((rc = guard(cudaMalloc(&base, n * 8), "malloc")) || (rc = guard(cudaMalloc(&stage, n * 8), "malloc")) ||
-      (rc = guard(cudaMalloc(&dt, 3 * sizeof(double)), "malloc")) ||
-      (rc = guard(cudaMemsetAsync(dt, 0, 3 * sizeof(double), s), "memset")))
-    return rc;
-  if (ml) {
-    if ((rc = guard(cudaMalloc(&flux, 3 * n * 8), "malloc")) || (rc = guard(cudaMalloc(&cb, nc * 8), "malloc")) ||
-        (rc = guard(cudaMalloc(&cs, nc * 8), "malloc")))
+  if (w.s && (w.n != n || w.nc != nc || w.nd < nd || w.ml != ml)) w.release();
+  if (!w.s) {
+    if ((rc = guard(cudaStreamCreateWithFlags(&w.s, cudaStreamNonBlocking), "stream"))) return rc;
+    w.n = n;
+    w.nc = nc;
+    w.nd = nd;
+    w.ml = ml;
+    if ((rc = guard(cudaMalloc(&w.base, n * 8), "malloc")) || (rc = guard(cudaMalloc(&w.stage, n * 8), "malloc")) ||
+        (rc = guard(cudaMalloc(&w.dt, 3 * sizeof(double)), "malloc")))
       return rc;
-  } else if ((rc = guard(cudaMalloc(&dudt, n * 8), "malloc"))) {
-    return rc;
-  }
-  // Burgers: the package's derived field, filled after every stage (FillDerived)
-  const size_t nd = (size_t)t.nblocks * t.dims.N[0] * t.dims.N[1] * t.dims.N[2];
-  if (p->physics == 1 && (rc = guard(cudaMalloc(&derived, nd * 8), "malloc"))) return rc;
-  if ((rc = guard(cudaMemcpyAsync(base, host_in, n * 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
-  if ((rc = guard(cudaMemcpyAsync(stage, base, n * 8, cudaMemcpyDeviceToDevice, s), "d2d"))) return rc;
-  // initial fill: Mesh::CommunicateBoundaries prolongates for every package
-  if ((rc = exchange_leaf(m, base, cb, ncomp, PGB_EXCHANGE_PROLONGATE, nullptr, s))) {
-    cleanup();
-    return rc;
-  }
-  if (*dt_inout > 0) {
-    if ((rc = guard(cudaMemcpyAsync(dt, dt_inout, 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
-  } else if ((rc = estimate_dt(m->st, p->physics, base, ncomp, p->vel, p->cfl, dt, 1, s, p->ncomp_vel, p->comp_vel))) {
-    cleanup();
-    return rc;
+    if (ml) {
+      if ((rc = guard(cudaMalloc(&w.flux, 3 * n * 8), "malloc")) || (rc = guard(cudaMalloc(&w.cb, nc * 8), "malloc")) ||
+          (rc = guard(cudaMalloc(&w.cs, nc * 8), "malloc")))
+        return rc;
+    } else if ((rc = guard(cudaMalloc(&w.dudt, n * 8), "malloc"))) {
+      return rc;
+    }
+    if (nd && (rc = guard(cudaMalloc(&w.derived, nd * 8), "malloc"))) return rc;
   }
   // each cycle's dt is read back as the cycle ends (into pinned memory: the copies queue
   // behind the cycles without stalling the host)
-  if (dt_cycles && ncycles > 0 &&
-      (rc = guard(cudaMallocHost(&dt_pinned, (size_t)ncycles * sizeof(double)), "pinned dt")))
+  if (dt_cycles && (size_t)ncycles > w.dt_pinned_cap) {
+    if (w.dt_pinned) cudaFreeHost(w.dt_pinned);
+    w.dt_pinned = nullptr;
+    w.dt_pinned_cap = 0;
+    if ((rc = guard(cudaMallocHost(&w.dt_pinned, (size_t)ncycles * sizeof(double)), "pinned dt"))) return rc;
+    w.dt_pinned_cap = (size_t)ncycles;
+  }
+  cudaStream_t s = w.s;
+  double *derived = nd ? w.derived : nullptr;
+  if ((rc = guard(cudaMemsetAsync(w.dt, 0, 3 * sizeof(double), s), "memset"))) return rc;
+  if ((rc = guard(cudaMemcpyAsync(w.base, host_in, n * 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
+  if ((rc = guard(cudaMemcpyAsync(w.stage, w.base, n * 8, cudaMemcpyDeviceToDevice, s), "d2d"))) return rc;
+  // initial fill: Mesh::CommunicateBoundaries prolongates for every package
+  if ((rc = exchange_leaf(m, w.base, w.cb, ncomp, PGB_EXCHANGE_PROLONGATE, nullptr, s))) {
+    w.release();
     return rc;
+  }
+  if (*dt_inout > 0) {
+    if ((rc = guard(cudaMemcpyAsync(w.dt, dt_inout, 8, cudaMemcpyHostToDevice, s), "h2d"))) return rc;
+  } else if ((rc = estimate_dt(m->st, p->physics, w.base, ncomp, p->vel, p->cfl, w.dt, 1, s, p->ncomp_vel,
+                                p->comp_vel))) {
+    w.release();
+    return rc;
+  }
   for (int c = 0; c < ncycles; ++c) {
-    if ((rc = cycle_impl(m, p, base, stage, dudt, flux, cb, cs, ncomp, dt, s, derived))) {
-      cleanup();
+    if ((rc = cycle_impl(m, p, w.base, w.stage, w.dudt, w.flux, w.cb, w.cs, ncomp, w.dt, s, derived))) {
+      w.release();
       return rc;
     }
-    if (dt_pinned && (rc = guard(cudaMemcpyAsync(dt_pinned + c, dt, 8, cudaMemcpyDeviceToHost, s), "d2h dt")))
+    if (dt_cycles && (rc = guard(cudaMemcpyAsync(w.dt_pinned + c, w.dt, 8, cudaMemcpyDeviceToHost, s), "d2h dt")))
       return rc;
   }
-  if ((rc = guard(cudaMemcpyAsync(host_out, base, n * 8, cudaMemcpyDeviceToHost, s), "d2h"))) return rc;
-  if ((rc = guard(cudaMemcpyAsync(dt_inout, dt, 8, cudaMemcpyDeviceToHost, s), "d2h"))) return rc;
+  if ((rc = guard(cudaMemcpyAsync(host_out, w.base, n * 8, cudaMemcpyDeviceToHost, s), "d2h"))) return rc;
+  if ((rc = guard(cudaMemcpyAsync(dt_inout, w.dt, 8, cudaMemcpyDeviceToHost, s), "d2h"))) return rc;
   if ((rc = guard(cudaStreamSynchronize(s), "sync"))) return rc;
-  if (dt_pinned) std::memcpy(dt_cycles, dt_pinned, (size_t)ncycles * sizeof(double));
-  cleanup();
+  if (dt_cycles && ncycles > 0) std::memcpy(dt_cycles, w.dt_pinned, (size_t)ncycles * sizeof(double));
   return kOk;
+}
+
+int pgb_release_host_workspace(pgb_mesh *m) {
+  if (!m) return fail(kErrInvalid, "null mesh");
+  const cudaError_t e = m->host_ws.s ? cudaStreamSynchronize(m->host_ws.s) : cudaSuccess;
+  m->host_ws.release();
+  return e == cudaSuccess ? kOk : check_cuda(e, "sync");
 }
 
 }  // extern "C"

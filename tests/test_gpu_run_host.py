@@ -65,3 +65,25 @@ def test_run_host_burgers_fast_within_tolerance():
     assert err.max() <= 1e-12, err
     np.testing.assert_allclose(dts[:-1], used[1:], rtol=1e-12)
     np.testing.assert_allclose(dt, o.dt(), rtol=1e-12)
+
+
+def test_run_host_reuses_and_releases_its_workspace():
+    """A second call reuses the mesh's device buffers and gives the same result; a call
+    with another component count reallocates them; after a release the next call
+    allocates them again."""
+    nx, bnx, ng = (32, 32, 32), (8, 8, 8), 2
+    leaves = refined_cube(2, 1, 3)
+    mesh = pg.Mesh(nx, bnx, ng, leaves=leaves).upload()
+    cfg = pg.StageConfig("advection", "plm", 0.3, exact=True)
+    s1 = pg.problems.advection_state(mesh, nscalars=0)
+    s3 = pg.problems.advection_state(mesh, nscalars=2)
+    a1, dta, _ = _run_host(mesh, cfg, s1, 1, 3)
+    b1, dtb, _ = _run_host(mesh, cfg, s1, 1, 3)
+    assert np.array_equal(a1, b1) and dta == dtb
+    c3, _, _ = _run_host(mesh, cfg, s3, 3, 2)
+    nat.check(nat.lib().pgb_release_host_workspace(mesh.handle), "pgb_release_host_workspace")
+    d3, _, _ = _run_host(mesh, cfg, s3, 3, 2)
+    assert np.array_equal(c3, d3)
+    # component 0 of the three-component run is the one-component run
+    e1, _, _ = _run_host(mesh, cfg, s1, 1, 2)
+    assert np.array_equal(e1[:, 0], d3[:, 0])
