@@ -322,6 +322,40 @@ int pgb_mg_solve(pgb_mg *mg, double *u, const double *rhs, double tol, int32_t r
 int pgb_mg_bicgstab(pgb_mg *mg, double *u, const double *rhs, int32_t precondition, double rtol, int32_t relative,
                     int32_t max_iters, int32_t *iters_out, double *rms_out, void *stream);
 
+/* ---- the composite grids for a package-side solver --------------------------------
+ * MGSolver<u, rhs, Eq> with a package's own equation (src/solvers/mg_solver.hpp:59-72:
+ * the Eq supplies Ax and SetDiagonal) runs its V-cycle on fields it holds itself; these
+ * calls give it the grids of a pgb_mg and move one such field between them. A field has
+ * one device array per store, [slot][k][j][i] with ghosts, x fastest; store 0 holds the
+ * full-size blocks (the leaves first in gid order, so its first slots are the leaf
+ * layout of the mesh, then the internal blocks of levels >= 0), store L < 0 the blocks of
+ * level L. A face field has three such arrays back to back (x1, x2, x3 faces; face i is
+ * the low face of cell i).
+ * Replaces the gmg_same / gmg_restrict / gmg_prolongate boundary tasks
+ * (src/bvals/comms/bvals_in_one.hpp:41-93 on the grids of src/mesh/mesh-gmg.cpp:103-201). */
+/* out[5]: coarsest and finest grid level, leaf blocks, stores, exact build (1) or not */
+int pgb_mg_layout(pgb_mg *mg, int32_t *out);
+/* out[8]: slots, nx[3], nghost, N[3] of store `store` (0, or a level below 0); geom
+ * (may be NULL): 6 doubles per slot, the first interior cell's low corner and the cell
+ * widths; levels (may be NULL): the logical level per slot. */
+int pgb_mg_store_info(pgb_mg *mg, int32_t store, int32_t *out, double *geom, int32_t *levels);
+/* out[4]: the grid's store, its fine blocks (level `level`, internal blocks first), its
+ * coarser leaves (level - 1) and internal blocks among the fine ones; fine / coarse (may
+ * be NULL) receive the slots. */
+int pgb_mg_grid_info(pgb_mg *mg, int32_t level, int32_t *out, int32_t *fine, int32_t *coarse);
+/* gmg_same ghost exchange of one field on grid `level` (field: the array of the grid's
+ * store), with ProlongateSharedLinear across its coarse/fine faces. */
+int pgb_mg_field_exchange(pgb_mg *mg, int32_t level, double *field, void *stream);
+/* RestrictAverage of the fine blocks of grid `level` (fine: their store's array) into
+ * their parents' octants on grid level - 1 (coarse: that grid's store array). */
+int pgb_mg_field_restrict(pgb_mg *mg, int32_t level, const double *fine, double *coarse, void *stream);
+/* ProlongateSharedLinear of the parents (coarse: grid level - 1's store array, ghosts
+ * current) written into the interior of every fine block of grid `level`. */
+int pgb_mg_field_prolongate(pgb_mg *mg, int32_t level, const double *coarse, double *fine, void *stream);
+/* RestrictAverage on faces of a face field from the fine blocks of grid `level` into
+ * their parents (the setup step's GMGRestrict of a face field). */
+int pgb_mg_face_restrict(pgb_mg *mg, int32_t level, const double *fine, double *coarse, void *stream);
+
 /* ---- launch-shape autotuner ------------------------------------------------------ */
 
 /* The first pgb_rk2_cycles call on a mesh (before it captures the cycle graph) times a

@@ -94,6 +94,13 @@ _SIGNATURES = {
     "pgb_mg_set_coefficient": [VP, VP, VP],
     "pgb_mg_bicgstab": [VP, VP, VP, ctypes.c_int32, ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
                         ctypes.POINTER(ctypes.c_int32), DP, VP],
+    "pgb_mg_layout": [VP, I32P],
+    "pgb_mg_store_info": [VP, ctypes.c_int32, I32P, DP, I32P],
+    "pgb_mg_grid_info": [VP, ctypes.c_int32, I32P, I32P, I32P],
+    "pgb_mg_field_exchange": [VP, ctypes.c_int32, VP, VP],
+    "pgb_mg_field_restrict": [VP, ctypes.c_int32, VP, VP, VP],
+    "pgb_mg_field_prolongate": [VP, ctypes.c_int32, VP, VP, VP],
+    "pgb_mg_face_restrict": [VP, ctypes.c_int32, VP, VP, VP],
     "pgb_history_mass": [VP, VP, ctypes.c_int32, VP, ctypes.c_int32, ctypes.c_double, VP, VP],
     "pgb_tune_report": [ctypes.c_char_p, ctypes.c_int32],
     "pgb_amr_block_criterion": [VP, VP, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, VP, VP],

@@ -1,0 +1,4 @@
+// Mirrors the reference header of the same path (parthenon-hpc-lab/parthenon src/parameter_input.hpp):
+// the compatibility layer declares everything in one place.
+#pragma once
+#include "pgb_compat/all.hpp"

@@ -14,6 +14,8 @@
 #include "driver.hpp"
 #include "mesh.hpp"
 #include "params.hpp"
+#include "solvers.hpp"
+#include "sparse_pack.hpp"
 #include "state.hpp"
 #include "tasks.hpp"
 #include "update.hpp"
@@ -49,7 +51,13 @@ KOKKOS_INLINE_FUNCTION auto ratio(const A &a, const B &b) {
 }  // namespace robust
 
 namespace prelude {
+using ::parthenon::Globals::my_rank;
+using ::parthenon::Globals::nranks;
 using ::parthenon::Coordinates_t;
+using ::parthenon::MakePackDescriptor;
+using ::parthenon::PDOpt;
+using ::parthenon::SparsePack;
+using ::parthenon::TopologicalElement;
 using ::parthenon::DevExecSpace;
 using ::parthenon::IndexDomain;
 using ::parthenon::IndexRange;
@@ -85,6 +93,12 @@ using ::parthenon::VariablePack;
 namespace driver {
 namespace prelude {
 using namespace ::parthenon::prelude;
+using ::parthenon::AllReduce;
+using ::parthenon::Outputs;
+using ::parthenon::ParameterInput;
+using ::parthenon::ParthenonManager;
+using ::parthenon::TaskQualifier;
+using ::parthenon::TaskStatus;
 using ::parthenon::ApplicationInput;
 using ::parthenon::BlockList_t;
 using ::parthenon::Driver;

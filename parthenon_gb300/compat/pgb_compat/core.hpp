@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <cassert>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <sstream>
@@ -60,7 +61,46 @@ enum class IndexDomain {
   inner_x3,
   outer_x3
 };
-enum class TopologicalElement { CC, F1, F2, F3, E1, E2, E3, NN };
+// numbered as in the reference, so that static_cast<int>(te) % 3 is the face direction
+enum class TopologicalElement : std::size_t { CC = 0, F1 = 3, F2 = 4, F3 = 5, E1 = 6, E2 = 7, E3 = 8, NN = 9 };
+enum class TopologicalType { Cell, Face, Edge, Node };
+KOKKOS_FORCEINLINE_FUNCTION constexpr TopologicalType GetTopologicalType(TopologicalElement el) {
+  const int e = static_cast<int>(el);
+  return e == 0 ? TopologicalType::Cell
+                : (e < 6 ? TopologicalType::Face : (e < 9 ? TopologicalType::Edge : TopologicalType::Node));
+}
+// offsets of an element's index range past the cell range (faces: one more along their
+// normal) -- src/basic_types.hpp TopologicalOffsetI/J/K
+KOKKOS_FORCEINLINE_FUNCTION constexpr int TopologicalOffsetI(TopologicalElement el) {
+  return el == TopologicalElement::F1 || el == TopologicalElement::E2 || el == TopologicalElement::E3 ||
+         el == TopologicalElement::NN;
+}
+KOKKOS_FORCEINLINE_FUNCTION constexpr int TopologicalOffsetJ(TopologicalElement el) {
+  return el == TopologicalElement::F2 || el == TopologicalElement::E3 || el == TopologicalElement::E1 ||
+         el == TopologicalElement::NN;
+}
+KOKKOS_FORCEINLINE_FUNCTION constexpr int TopologicalOffsetK(TopologicalElement el) {
+  return el == TopologicalElement::F3 || el == TopologicalElement::E2 || el == TopologicalElement::E1 ||
+         el == TopologicalElement::NN;
+}
+
+// src/mesh/mesh.hpp / src/interface/mesh_data.hpp: which grid a MeshData covers -- the
+// leaves, or the two-level composite multigrid grid of a logical level
+enum class GridType { none, leaf, two_level_composite };
+struct GridIdentifier {
+  GridType type = GridType::none;
+  int logical_level = 0;
+  static GridIdentifier leaf() { return GridIdentifier{GridType::leaf, 0}; }
+  static GridIdentifier two_level_composite(int level) {
+    return GridIdentifier{GridType::two_level_composite, level};
+  }
+  bool operator==(const GridIdentifier &o) const {
+    return type == o.type && (type != GridType::two_level_composite || logical_level == o.logical_level);
+  }
+  bool operator<(const GridIdentifier &o) const {
+    return type != o.type ? type < o.type : logical_level < o.logical_level;
+  }
+};
 
 struct IndexRange {
   int s = 0;  // first index
@@ -71,6 +111,17 @@ struct IndexRange {
 
 // src/defs.hpp CoordinateDirection
 enum CoordinateDirection { NODIR = -1, X0DIR = 0, X1DIR = 1, X2DIR = 2, X3DIR = 3 };
+// src/defs.hpp: the six faces of a block
+constexpr int BOUNDARY_NFACES = 6;
+enum BoundaryFace { undef = -1, inner_x1 = 0, outer_x1 = 1, inner_x2 = 2, outer_x2 = 3, inner_x3 = 4, outer_x3 = 5 };
+enum class BoundaryFlag { block = -1, undef, periodic, user };
+
+// src/globals.hpp: one process on one GPU
+namespace Globals {
+inline int my_rank = 0;
+inline int nranks = 1;
+inline int nghost = 0;
+}  // namespace Globals
 
 // src/utils/error_checking.hpp
 namespace ErrorChecking {

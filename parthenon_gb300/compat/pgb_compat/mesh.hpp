@@ -1,23 +1,31 @@
 // Package-facing compatibility layer: coordinates, index shapes, the mesh and its
-// blocks, data containers (MeshData / MeshBlockData) and variable packs.
+// blocks, data containers (MeshData / MeshBlockData), variable packs and the multigrid
+// grids.
 //
 // Reference: src/coordinates/uniform_cartesian.hpp:30-251 (UniformCartesian),
 // src/mesh/domain.hpp:83 (IndexShape), src/mesh/mesh.hpp, src/mesh/meshblock.hpp,
 // src/interface/mesh_data.hpp:191-370 (MeshData: PackVariables(AndFluxes), bounds,
-// NumBlocks, SetAllowedDt), src/interface/meshblock_data.hpp,
+// NumBlocks, SetAllowedDt, grid), src/interface/meshblock_data.hpp,
 // src/interface/variable_pack.hpp:433-503 (VariablePack / VariableFluxPack, PackIndexMap),
-// src/interface/data_collection.hpp (GetOrAdd / Add / Get).
+// src/interface/data_collection.hpp (GetOrAdd / Add / AddShallow / Get),
+// src/mesh/mesh-gmg.cpp:103-201 (the multigrid grids, GetGMGMin/MaxLevel).
 //
-// Storage: one device arena per (container, variable), [block][component][k][j][i]
-// with ghosts -- the layout the library's C ABI exchanges -- and, for variables with
-// fluxes, one flux arena per container, [block][direction][component][k][j][i]
-// (cell-aligned faces). Metadata::OneCopy variables have one arena shared by every
-// container. A pack is a device table of per-(block, component) base pointers plus the
-// blocks' coordinates, built once per (container, variable list) and cached, so
+// Storage: one device arena per (container, variable, store), [slot][component][k][j][i]
+// with ghosts -- the layout the library's C ABI exchanges. Store 0 holds the full-size
+// blocks, the leaves first (so its head is the leaf layout), then, on a mesh with
+// multigrid, the internal blocks of the grids at and above the root level; store L < 0
+// the smaller blocks of level L. A face field has three arenas back to back (x1, x2, x3
+// faces; face i is the low face of cell i). Variables with fluxes have one flux arena
+// per container and store, [slot][direction][component][k][j][i] (cell-aligned faces).
+// Metadata::OneCopy variables have one arena per store shared by every container.
+// A VariablePack is a device table of per-(block, component) base pointers plus the
+// blocks' coordinates; a SparsePack the same per topological slot (sparse_pack.hpp);
+// both are built once per (container, grid, variable selection) and cached, so
 // v(b, n, k, j, i) is one table read and one indexed load in a kernel.
 #pragma once
 
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <string>
@@ -26,6 +34,7 @@
 
 #include "dispatch.hpp"
 #include "params.hpp"
+#include "sparse_pack.hpp"
 #include "state.hpp"
 
 namespace parthenon {
@@ -64,6 +73,30 @@ class UniformCartesian {
   KOKKOS_FORCEINLINE_FUNCTION Real Xf(const int idx) const {
     return xmin_[dir - 1] + idx * dx_[dir - 1];
   }
+  template <int dir>
+  KOKKOS_FORCEINLINE_FUNCTION Real Xf(const int k, const int j, const int i) const {
+    return dir == 1 ? Xf<1>(i) : (dir == 2 ? Xf<2>(j) : Xf<3>(k));
+  }
+  // position of element `el` along dir (uniform_cartesian.hpp:166-193): a face, edge or
+  // node offset along dir sits on the cell's low face, else at the cell centre
+  template <int dir, TopologicalElement el>
+  KOKKOS_FORCEINLINE_FUNCTION Real X(const int idx) const {
+    constexpr bool edge = (dir == 1 && TopologicalOffsetI(el)) || (dir == 2 && TopologicalOffsetJ(el)) ||
+                          (dir == 3 && TopologicalOffsetK(el));
+    if constexpr (edge) {
+      return xmin_[dir - 1] + idx * dx_[dir - 1];
+    } else {
+      return xmin_[dir - 1] + (idx + 0.5) * dx_[dir - 1];
+    }
+  }
+  template <int dir, TopologicalElement el>
+  KOKKOS_FORCEINLINE_FUNCTION Real X(const int k, const int j, const int i) const {
+    return dir == 1 ? X<dir, el>(i) : (dir == 2 ? X<dir, el>(j) : X<dir, el>(k));
+  }
+  template <int dir, class... Args>
+  KOKKOS_FORCEINLINE_FUNCTION Real CellWidth(Args...) const {
+    return dx_[dir - 1];
+  }
   template <int dir, class... Args>
   KOKKOS_FORCEINLINE_FUNCTION Real FaceArea(Args...) const {
     return area_[dir - 1];
@@ -83,16 +116,24 @@ class IndexShape {
  public:
   IndexShape() = default;
   IndexShape(int nx1, int nx2, int nx3, int ng) : nx_{nx1, nx2, nx3}, ng_(ng) {}
-  KOKKOS_INLINE_FUNCTION IndexRange GetBoundsI(IndexDomain d) const { return bounds(0, d); }
-  KOKKOS_INLINE_FUNCTION IndexRange GetBoundsJ(IndexDomain d) const { return bounds(1, d); }
-  KOKKOS_INLINE_FUNCTION IndexRange GetBoundsK(IndexDomain d) const { return bounds(2, d); }
+  KOKKOS_INLINE_FUNCTION IndexRange GetBoundsI(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const {
+    return bounds(0, d, TopologicalOffsetI(te));
+  }
+  KOKKOS_INLINE_FUNCTION IndexRange GetBoundsJ(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const {
+    return bounds(1, d, TopologicalOffsetJ(te));
+  }
+  KOKKOS_INLINE_FUNCTION IndexRange GetBoundsK(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const {
+    return bounds(2, d, TopologicalOffsetK(te));
+  }
   KOKKOS_INLINE_FUNCTION int ncellsi(IndexDomain d) const { return bounds(0, d).size(); }
   KOKKOS_INLINE_FUNCTION int ncellsj(IndexDomain d) const { return bounds(1, d).size(); }
   KOKKOS_INLINE_FUNCTION int ncellsk(IndexDomain d) const { return bounds(2, d).size(); }
 
  private:
-  KOKKOS_INLINE_FUNCTION IndexRange bounds(int d, IndexDomain dom) const {
-    return dom == IndexDomain::interior ? IndexRange{ng_, ng_ + nx_[d] - 1} : IndexRange{0, nx_[d] + 2 * ng_ - 1};
+  // interior cells (one more index along an element's offset direction), or the whole
+  // array
+  KOKKOS_INLINE_FUNCTION IndexRange bounds(int d, IndexDomain dom, int off = 0) const {
+    return dom == IndexDomain::interior ? IndexRange{ng_, ng_ + nx_[d] - 1 + off} : IndexRange{0, nx_[d] + 2 * ng_ - 1};
   }
   int nx_[3] = {1, 1, 1};
   int ng_ = 0;
@@ -186,11 +227,17 @@ class MeshData;
 template <typename T>
 class MeshBlockData;
 
-// Device arrays of one named container.
+// Device arrays of one named container: per variable, one array per multigrid store
+// (key 0: the full-size blocks -- the leaves first, so its head is the leaf layout --,
+// key L < 0: the blocks of level L below the root grid; meshes without multigrid have
+// store 0 only, the leaves).
 struct Container {
   std::string name;
-  std::vector<Real *> data;  // per variable (OneCopy variables point at the shared arena)
-  std::vector<Real *> flux;  // per variable, null without fluxes
+  std::vector<Real *> data;  // per variable, store 0 (OneCopy variables point at the shared arena)
+  std::vector<Real *> flux;  // per variable, store 0, null without fluxes
+  std::vector<std::map<int, Real *>> sdata, sflux;  // per variable and store
+  Real *at(int v, int store) const { return store == 0 ? data[v] : sdata[v].at(store); }
+  Real *flux_at(int v, int store) const { return store == 0 ? flux[v] : sflux[v].at(store); }
 };
 
 // One registered variable.
@@ -198,6 +245,32 @@ struct VarInfo {
   std::string name;
   Metadata m;
   int ncomp;
+  bool face() const { return m.IsSet(Metadata::Face); }
+  bool with_fluxes() const { return m.IsSet(Metadata::WithFluxes) && !m.IsSet(Metadata::OneCopy); }
+};
+
+// A multigrid store: slots of equal blocks and their coordinates.
+struct BlockStore {
+  int key = 0, nslots = 0, nx[3] = {1, 1, 1}, ng = 0, N[3] = {1, 1, 1};
+  std::vector<Coordinates_t> coords;  // per slot
+  std::vector<int> level;             // logical level per slot
+  int64_t cells() const { return (int64_t)N[0] * N[1] * N[2]; }
+};
+
+// The blocks a MeshData covers: the leaves, or one two-level composite multigrid grid
+// (its blocks of the grid's level first -- internal blocks, then leaves -- then the
+// leaves of the next coarser level that lend it boundary values).
+struct BlockSet {
+  int store = 0;
+  std::vector<int> slot;       // per block of the MeshData
+  std::vector<char> fine;      // a block of the grid's own level
+  std::vector<char> internal;  // not a leaf (the reference's blocks without neighbours)
+};
+
+// src/mesh/mesh.hpp BlockListPartition: a set of blocks handed to one task list
+struct BlockListPartition {
+  GridIdentifier grid;
+  int partition = 0;
 };
 
 template <typename T>
@@ -228,14 +301,15 @@ using BlockList_t = std::vector<std::shared_ptr<MeshBlock>>;
 template <typename T>
 class MeshData {
  public:
-  MeshData(Mesh *pm, const std::string &container) : pm_(pm), name_(container) {}
+  MeshData(Mesh *pm, const std::string &container, GridIdentifier g = GridIdentifier::leaf());
+  GridIdentifier grid;
   const std::string &StageName() const { return name_; }
   Mesh *GetMeshPointer() const { return pm_; }
   Mesh *GetParentPointer() const { return pm_; }
-  int NumBlocks() const;
-  IndexRange GetBoundsI(IndexDomain d) const;
-  IndexRange GetBoundsJ(IndexDomain d) const;
-  IndexRange GetBoundsK(IndexDomain d) const;
+  int NumBlocks() const { return (int)set_.slot.size(); }
+  IndexRange GetBoundsI(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const { return bounds(0, d, te); }
+  IndexRange GetBoundsJ(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const { return bounds(1, d, te); }
+  IndexRange GetBoundsK(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const { return bounds(2, d, te); }
   void SetAllowedDt(Real dt) { dt_ = dt; }
   Real GetAllowedDt() const { return dt_; }
   std::shared_ptr<MeshBlockData<T>> &GetBlockData(int b);
@@ -271,13 +345,19 @@ class MeshData {
     return pack(n, n, nullptr, true);
   }
 
-  // the layer's own: variable names whose metadata has every flag given
+  // ---- the layer's own
+  // variable names whose metadata has every flag given
   std::vector<std::string> names_with(const std::vector<MetadataFlag> &flags) const;
   // block-level view (MeshBlockData) packs restrict to one block
   const VariableFluxPack<T> &pack(const std::vector<std::string> &names, const std::vector<std::string> &fluxes,
                                   PackIndexMap *imap, bool with_fluxes, int only_block = -1);
+  const BlockSet &blocks() const { return set_; }
+  const BlockStore &store() const;
+  const compat_detail::PackTables &sparse_pack(const compat_detail::PackSpec &spec, const std::vector<bool> &include,
+                                               bool only_fine, int only_block = -1);
 
  private:
+  IndexRange bounds(int d, IndexDomain dom, TopologicalElement te) const;
   struct CachedPack {
     VariableFluxPack<T> view;
     PackIndexMap imap;
@@ -286,10 +366,19 @@ class MeshData {
       if (table) cudaFree(table);
     }
   };
+  struct CachedSparse {
+    compat_detail::PackTables t;
+    void *dev = nullptr;
+    ~CachedSparse() {
+      if (dev) cudaFree(dev);
+    }
+  };
   Mesh *pm_;
   std::string name_;
+  BlockSet set_;
   Real dt_ = std::numeric_limits<Real>::max();
   std::map<std::string, std::unique_ptr<CachedPack>> packs_;
+  std::map<std::string, std::unique_ptr<CachedSparse>> sparse_;
   std::vector<std::shared_ptr<MeshBlockData<T>>> block_data_;
 };
 
@@ -317,8 +406,9 @@ class MeshBlockData {
   std::string name_;
 };
 
-// Named containers (src/interface/data_collection.hpp): of the mesh (MeshData, one
-// partition holding every block) or of a block (MeshBlockData).
+// Named containers (src/interface/data_collection.hpp): of the mesh (MeshData: the
+// leaves, one partition holding every block, or a multigrid grid) or of a block
+// (MeshBlockData).
 template <typename T>
 class DataCollection {};
 
@@ -327,11 +417,22 @@ class DataCollection<MeshData<Real>> {
  public:
   explicit DataCollection(Mesh *pm) : pm_(pm) {}
   std::shared_ptr<MeshData<Real>> &GetOrAdd(const std::string &name, int partition);
+  std::shared_ptr<MeshData<Real>> &GetOrAdd(const std::string &name, const GridIdentifier &grid);
   std::shared_ptr<MeshData<Real>> &Get(const std::string &name = "base") { return GetOrAdd(name, 0); }
+  std::shared_ptr<MeshData<Real>> &Add(const std::string &name, const std::shared_ptr<BlockListPartition> &p) {
+    return GetOrAdd(name, p->grid);
+  }
+  std::shared_ptr<MeshData<Real>> &Add(const std::string &name, int partition) { return GetOrAdd(name, partition); }
+  // a container sharing md's variables (every container holds every variable here, so
+  // the new name aliases md's data)
+  std::shared_ptr<MeshData<Real>> &AddShallow(const std::string &, std::shared_ptr<MeshData<Real>> &md,
+                                              const std::vector<std::string> & = {}) {
+    return md;
+  }
 
  private:
   Mesh *pm_;
-  std::map<std::string, std::shared_ptr<MeshData<Real>>> mds_;
+  std::map<std::pair<std::string, GridIdentifier>, std::shared_ptr<MeshData<Real>>> mds_;
 };
 
 template <>
@@ -353,7 +454,9 @@ class DataCollection<MeshBlockData<Real>> {
 class ApplicationInput;
 
 // The mesh (src/mesh/mesh.hpp): a uniform periodic grid of equal blocks, its library
-// handle, the registered variables and the device arenas of every container.
+// handle, the registered variables and the device arenas of every container; with
+// `multigrid = true` also the multigrid grids below the leaves (mesh-gmg.cpp:103-201),
+// from the library's composite-grid layout (pgb_mg_*).
 class Mesh {
  public:
   Mesh(ParameterInput *pin, ApplicationInput *app_in, Packages_t &packages);
@@ -364,19 +467,33 @@ class Mesh {
   int ndim = 3;
   bool adaptive = false;
   bool multilevel = false;
+  bool multigrid = false;
   int nbtotal = 0;
   Packages_t packages;
+  // the packages merged (the reference resolves them into one descriptor)
+  std::shared_ptr<StateDescriptor> resolved_packages;
   BlockList_t block_list;
   DataCollection<MeshData<Real>> mesh_data;
 
   int DefaultNumPartitions() const { return 1; }
   int64_t GetNumberOfMeshBlockCells() const { return (int64_t)nx_[0] * nx_[1] * nx_[2]; }
+  int64_t GetTotalCells() const { return (int64_t)nbtotal * GetNumberOfMeshBlockCells(); }
+  int GetGMGMaxLevel() const { return gmg_max_; }
+  int GetGMGMinLevel() const { return gmg_min_; }
+  std::vector<std::shared_ptr<BlockListPartition>> GetDefaultBlockPartitions(
+      GridIdentifier g = GridIdentifier::leaf()) const {
+    if (g.type == GridType::two_level_composite &&
+        (!multigrid || g.logical_level < gmg_min_ || g.logical_level > gmg_max_))
+      return {};
+    return {std::make_shared<BlockListPartition>(BlockListPartition{g, 0})};
+  }
   // runs the application's problem generator on every block, fills the ghosts and
   // the derived fields (Mesh::Initialize, src/mesh/mesh.cpp:745-858)
   void Initialize(ApplicationInput *app_in, ParameterInput *pin);
 
   // ---- the layer's own ---------------------------------------------------------------
   pgb_mesh *handle() const { return handle_; }
+  pgb_mg *mg() const { return mg_; }
   Container &container(const std::string &name);
   const std::vector<VarInfo> &variables() const { return vars_; }
   int var_index(const std::string &name) const;
@@ -385,14 +502,38 @@ class Mesh {
   int nghost() const { return ng_; }
   const Coordinates_t *device_coords() const { return d_coords_; }
   int64_t cells_per_comp() const { return (int64_t)N_[0] * N_[1] * N_[2]; }
+  const BlockStore &store(int key) const { return stores_.at(key); }
+  // the block set of a grid (leaf or a multigrid level)
+  BlockSet block_set(const GridIdentifier &g) const;
+  // elements of variable v's array on a store (all components, faces included)
+  int64_t var_elems(int v, int store) const {
+    const BlockStore &s = stores_.at(store);
+    return (int64_t)s.nslots * vars_[v].ncomp * s.cells() * (vars_[v].face() ? 3 : 1);
+  }
+  // allocations of the layer (freed with the mesh)
+  template <class U>
+  U *alloc_table(size_t n) {
+    void *p = nullptr;
+    check_cuda(cudaMalloc(&p, n * sizeof(U)), "table allocation");
+    allocations_.push_back(p);
+    return static_cast<U *>(p);
+  }
 
  private:
   Real *alloc(size_t n);
   pgb_mesh *handle_ = nullptr;
+  pgb_mg *mg_ = nullptr;
   int nx_[3] = {1, 1, 1}, N_[3] = {1, 1, 1}, ng_ = 0;
+  int gmg_min_ = 0, gmg_max_ = 0;
   std::vector<VarInfo> vars_;
   std::map<std::string, Container> containers_;
-  std::vector<Real *> onecopy_;  // per variable (null unless OneCopy)
+  std::vector<std::map<int, Real *>> onecopy_;  // per variable and store (empty unless OneCopy)
+  std::map<int, BlockStore> stores_;
+  struct GridBlocks {
+    int store = 0, nint = 0;
+    std::vector<int> fine, coarse;
+  };
+  std::map<int, GridBlocks> grids_;
   std::vector<void *> allocations_;
   Coordinates_t *d_coords_ = nullptr;
 };
@@ -401,14 +542,15 @@ class Mesh {
 
 inline Real *Mesh::alloc(size_t n) {
   void *p = nullptr;
-  check_cuda(cudaMalloc(&p, n * sizeof(Real)), "container allocation");
-  check_cuda(cudaMemsetAsync(p, 0, n * sizeof(Real), compat_stream()), "container zero fill");
+  check_cuda(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(Real)), "container allocation");
+  check_cuda(cudaMemsetAsync(p, 0, std::max<size_t>(n, 1) * sizeof(Real), compat_stream()), "container zero fill");
   allocations_.push_back(p);
   return static_cast<Real *>(p);
 }
 
 inline Mesh::Mesh(ParameterInput *pin, ApplicationInput *, Packages_t &pkgs)
-    : packages(pkgs), mesh_data(this) {
+    : packages(pkgs), resolved_packages(std::make_shared<StateDescriptor>("parthenon::resolved_state")),
+      mesh_data(this) {
   pgb_mesh_spec spec{};
   const char *ax[3] = {"1", "2", "3"};
   for (int d = 0; d < 3; ++d) {
@@ -425,7 +567,9 @@ inline Mesh::Mesh(ParameterInput *pin, ApplicationInput *, Packages_t &pkgs)
   spec.nghost = pin->GetOrAddInteger("parthenon/mesh", "nghost", 2);
   const std::string refinement = pin->GetOrAddString("parthenon/mesh", "refinement", "none");
   PARTHENON_REQUIRE_THROWS(refinement == "none", "this compatibility mesh is uniform (refinement = none)");
+  multigrid = pin->GetOrAddBoolean("parthenon/mesh", "multigrid", false);
   ng_ = spec.nghost;
+  Globals::nghost = ng_;
   for (int d = 0; d < 3; ++d) N_[d] = nx_[d] + 2 * ng_;
   check_pgb(pgb_mesh_create(&spec, 0, nullptr, &handle_), "pgb_mesh_create");
   check_pgb(pgb_mesh_upload(handle_), "pgb_mesh_upload");
@@ -436,28 +580,84 @@ inline Mesh::Mesh(ParameterInput *pin, ApplicationInput *, Packages_t &pkgs)
   std::vector<int64_t> locs(4 * (size_t)nbtotal);
   std::vector<double> geom(6 * (size_t)nbtotal);
   check_pgb(pgb_mesh_block_info(handle_, locs.data(), geom.data()), "pgb_mesh_block_info");
-  std::vector<Coordinates_t> coords;
+  BlockStore leaf;
+  leaf.nslots = nbtotal;
+  leaf.ng = ng_;
+  for (int d = 0; d < 3; ++d) {
+    leaf.nx[d] = nx_[d];
+    leaf.N[d] = N_[d];
+  }
   for (int b = 0; b < nbtotal; ++b) {
     block_list.push_back(std::make_shared<MeshBlock>(this, b, &geom[6 * b], &geom[6 * b + 3], nx_, ng_));
-    coords.push_back(block_list.back()->coords);
+    leaf.coords.push_back(block_list.back()->coords);
+    leaf.level.push_back((int)locs[4 * b]);
   }
-  check_cuda(cudaMalloc(&d_coords_, sizeof(Coordinates_t) * nbtotal), "coordinates");
+  gmg_min_ = gmg_max_ = nbtotal ? leaf.level[0] : 0;
+  stores_[0] = leaf;
+  if (multigrid) {
+    // every grid down to the coarsest (MGSolver picks its own range from max_coarsenings)
+    pgb_mg_params mp{};
+    mp.stages = 2;
+    mp.weight = 1.0;
+    mp.max_coarsenings = 1000;
+    mp.D = 1.0;
+    mp.exact = pin->GetOrAddBoolean("parthenon/mesh", "multigrid_exact_transfers", true) ? 1 : 0;
+    check_pgb(pgb_mg_create(handle_, &mp, &mg_), "pgb_mg_create");
+    int32_t lay[5];
+    check_pgb(pgb_mg_layout(mg_, lay), "pgb_mg_layout");
+    gmg_min_ = lay[0];
+    gmg_max_ = lay[1];
+    for (int key = 0; key >= std::min(0, gmg_min_); --key) {
+      int32_t si[8];
+      check_pgb(pgb_mg_store_info(mg_, key, si, nullptr, nullptr), "pgb_mg_store_info");
+      BlockStore st;
+      st.key = key;
+      st.nslots = si[0];
+      st.ng = si[4];
+      for (int d = 0; d < 3; ++d) {
+        st.nx[d] = si[1 + d];
+        st.N[d] = si[5 + d];
+      }
+      std::vector<double> g(6 * (size_t)st.nslots);
+      st.level.resize(st.nslots);
+      check_pgb(pgb_mg_store_info(mg_, key, si, g.data(), st.level.data()), "pgb_mg_store_info");
+      for (int b = 0; b < st.nslots; ++b) st.coords.emplace_back(&g[6 * b], &g[6 * b + 3], st.ng);
+      stores_[key] = st;
+    }
+    for (int L = gmg_min_; L <= gmg_max_; ++L) {
+      int32_t gi[4];
+      check_pgb(pgb_mg_grid_info(mg_, L, gi, nullptr, nullptr), "pgb_mg_grid_info");
+      GridBlocks gb;
+      gb.store = gi[0];
+      gb.nint = gi[3];
+      gb.fine.resize(gi[1]);
+      gb.coarse.resize(gi[2]);
+      check_pgb(pgb_mg_grid_info(mg_, L, gi, gb.fine.data(), gb.coarse.data()), "pgb_mg_grid_info");
+      grids_[L] = gb;
+    }
+  }
+  check_cuda(cudaMalloc(&d_coords_, sizeof(Coordinates_t) * std::max(nbtotal, 1)), "coordinates");
   allocations_.push_back(d_coords_);
-  check_cuda(cudaMemcpy(d_coords_, coords.data(), sizeof(Coordinates_t) * nbtotal, cudaMemcpyHostToDevice),
+  check_cuda(cudaMemcpy(d_coords_, leaf.coords.data(), sizeof(Coordinates_t) * nbtotal, cudaMemcpyHostToDevice),
              "coordinates upload");
   // variables in package registration order
   for (const auto &name : packages.Order())
-    for (const auto &f : packages.Get(name)->AllFields()) vars_.push_back(VarInfo{f.first, f.second, f.second.NumComponents()});
-  onecopy_.assign(vars_.size(), nullptr);
-  const size_t cs = (size_t)cells_per_comp() * nbtotal;
+    for (const auto &f : packages.Get(name)->AllFields()) {
+      vars_.push_back(VarInfo{f.first, f.second, f.second.NumComponents()});
+      resolved_packages->AddField(f.first, f.second);
+    }
+  onecopy_.assign(vars_.size(), {});
   for (size_t v = 0; v < vars_.size(); ++v)
-    if (vars_[v].m.IsSet(Metadata::OneCopy)) onecopy_[v] = alloc(cs * vars_[v].ncomp);
+    if (vars_[v].m.IsSet(Metadata::OneCopy))
+      for (auto &kv : stores_) onecopy_[v][kv.first] = alloc((size_t)var_elems((int)v, kv.first));
   container("base");
 }
 
 inline Mesh::~Mesh() {
   cudaStreamSynchronize(compat_stream());
+  mesh_data = DataCollection<MeshData<Real>>(this);  // packs free their tables first
   for (void *p : allocations_) cudaFree(p);
+  if (mg_) pgb_mg_destroy(mg_);
   if (handle_) pgb_mesh_destroy(handle_);
 }
 
@@ -472,14 +672,50 @@ inline Container &Mesh::container(const std::string &name) {
   if (it != containers_.end()) return it->second;
   Container c;
   c.name = name;
-  const size_t cs = (size_t)cells_per_comp() * nbtotal;
+  c.sdata.resize(vars_.size());
+  c.sflux.resize(vars_.size());
   for (size_t v = 0; v < vars_.size(); ++v) {
     const VarInfo &vi = vars_[v];
-    c.data.push_back(vi.m.IsSet(Metadata::OneCopy) ? onecopy_[v] : alloc(cs * vi.ncomp));
-    const bool fl = vi.m.IsSet(Metadata::WithFluxes) && !vi.m.IsSet(Metadata::OneCopy);
-    c.flux.push_back(fl ? alloc(3 * cs * vi.ncomp) : nullptr);
+    for (auto &kv : stores_) {
+      const int key = kv.first;
+      Real *d = vi.m.IsSet(Metadata::OneCopy) ? onecopy_[v].at(key) : alloc((size_t)var_elems((int)v, key));
+      Real *f = vi.with_fluxes() ? alloc(3 * (size_t)var_elems((int)v, key)) : nullptr;
+      c.sdata[v][key] = d;
+      c.sflux[v][key] = f;
+    }
+    c.data.push_back(c.sdata[v].at(0));
+    c.flux.push_back(c.sflux[v].at(0));
   }
   return containers_.emplace(name, std::move(c)).first->second;
+}
+
+inline BlockSet Mesh::block_set(const GridIdentifier &g) const {
+  BlockSet s;
+  if (g.type != GridType::two_level_composite) {
+    s.store = 0;
+    for (int b = 0; b < nbtotal; ++b) {
+      s.slot.push_back(b);
+      s.fine.push_back(1);
+      s.internal.push_back(0);
+    }
+    return s;
+  }
+  PARTHENON_REQUIRE_THROWS(multigrid, "multigrid grids need <parthenon/mesh> multigrid = true");
+  auto it = grids_.find(g.logical_level);
+  PARTHENON_REQUIRE_THROWS(it != grids_.end(), "no multigrid grid at level " + std::to_string(g.logical_level));
+  const GridBlocks &gb = it->second;
+  s.store = gb.store;
+  for (size_t q = 0; q < gb.fine.size(); ++q) {
+    s.slot.push_back(gb.fine[q]);
+    s.fine.push_back(1);
+    s.internal.push_back((int)q < gb.nint);
+  }
+  for (int c : gb.coarse) {
+    s.slot.push_back(c);
+    s.fine.push_back(0);
+    s.internal.push_back(0);
+  }
+  return s;
 }
 
 inline MeshBlock::MeshBlock(Mesh *pm, int g, const double xmin[3], const double dx[3], const int nx[3], int ng)
@@ -499,23 +735,28 @@ inline Real MeshBlock::NewDt() const {
 }
 
 template <typename T>
-int MeshData<T>::NumBlocks() const {
-  return pm_->nbtotal;
-}
+MeshData<T>::MeshData(Mesh *pm, const std::string &container, GridIdentifier g)
+    : grid(g), pm_(pm), name_(container), set_(pm->block_set(g)) {}
+
 template <typename T>
-IndexRange MeshData<T>::GetBoundsI(IndexDomain d) const {
-  return pm_->block_list[0]->cellbounds.GetBoundsI(d);
+const BlockStore &MeshData<T>::store() const {
+  return pm_->store(set_.store);
 }
+
+// index ranges of the MeshData's blocks: interior cells, or the whole array; an element
+// offset along d (faces) adds one index to the interior range
 template <typename T>
-IndexRange MeshData<T>::GetBoundsJ(IndexDomain d) const {
-  return pm_->block_list[0]->cellbounds.GetBoundsJ(d);
+IndexRange MeshData<T>::bounds(int d, IndexDomain dom, TopologicalElement te) const {
+  const BlockStore &s = store();
+  const int off = d == 0 ? TopologicalOffsetI(te) : (d == 1 ? TopologicalOffsetJ(te) : TopologicalOffsetK(te));
+  if (dom == IndexDomain::interior) return IndexRange{s.ng, s.ng + s.nx[d] - 1 + off};
+  return IndexRange{0, s.N[d] - 1};
 }
-template <typename T>
-IndexRange MeshData<T>::GetBoundsK(IndexDomain d) const {
-  return pm_->block_list[0]->cellbounds.GetBoundsK(d);
-}
+
 template <typename T>
 std::shared_ptr<MeshBlockData<T>> &MeshData<T>::GetBlockData(int b) {
+  PARTHENON_REQUIRE_THROWS(grid.type != GridType::two_level_composite,
+                           "block data of multigrid blocks is not on this path");
   return pm_->block_list[b]->meshblock_data.Get(name_);
 }
 template <typename T>
@@ -537,6 +778,8 @@ template <typename T>
 const VariableFluxPack<T> &MeshData<T>::pack(const std::vector<std::string> &names,
                                              const std::vector<std::string> &fluxes, PackIndexMap *imap,
                                              bool with_fluxes, int only_block) {
+  PARTHENON_REQUIRE_THROWS(grid.type != GridType::two_level_composite,
+                           "VariablePack of a multigrid grid: use a SparsePack");
   std::string key = std::to_string(only_block) + (with_fluxes ? "|F|" : "|V|");
   for (const auto &n : names) key += n + ",";
   key += "|";
@@ -554,6 +797,7 @@ const VariableFluxPack<T> &MeshData<T>::pack(const std::vector<std::string> &nam
     for (const auto &n : names) {
       const int v = pm_->var_index(n);
       PARTHENON_REQUIRE_THROWS(v >= 0, "no variable named " + n);
+      PARTHENON_REQUIRE_THROWS(!pm_->variables()[v].face(), "face field " + n + " in a VariablePack");
       cp->imap.insert(n, nvar, nvar + pm_->variables()[v].ncomp - 1);
       vars.push_back({v, pm_->variables()[v].ncomp});
       nvar += pm_->variables()[v].ncomp;
@@ -587,6 +831,104 @@ const VariableFluxPack<T> &MeshData<T>::pack(const std::vector<std::string> &nam
   return it->second->view;
 }
 
+// Resolve a pack descriptor on this MeshData's blocks (sparse_pack_base.cpp: variable
+// groups in order, each the matching variables in registration order, each of those
+// its components; one table entry per block, component and topological slot).
+template <typename T>
+const compat_detail::PackTables &MeshData<T>::sparse_pack(const compat_detail::PackSpec &spec,
+                                                          const std::vector<bool> &include, bool only_fine,
+                                                          int only_block) {
+  std::vector<int> blocks;  // positions in the block set
+  const int nb = NumBlocks();
+  PARTHENON_REQUIRE_THROWS(include.empty() || (int)include.size() == nb, "Passed wrong size block include list.");
+  for (int b = 0; b < nb; ++b) {
+    if (only_block >= 0 && b != only_block) continue;
+    if (!include.empty() && !include[b]) continue;
+    if (only_fine && grid.type == GridType::two_level_composite && !set_.fine[b]) continue;
+    blocks.push_back(b);
+  }
+  std::string key = spec.key() + "#" + std::to_string(only_block) + "#";
+  for (int b : blocks) key += std::to_string(b) + ",";
+  auto it = sparse_.find(key);
+  if (it != sparse_.end()) return it->second->t;
+  // variables of each group
+  const auto &vars = pm_->variables();
+  std::vector<std::vector<int>> groups(spec.names.size());
+  for (size_t g = 0; g < spec.names.size(); ++g) {
+    for (size_t v = 0; v < vars.size(); ++v) {
+      if (!vars[v].m.AllFlagsSet(spec.flags)) continue;
+      const bool match = spec.regex[g] ? std::regex_match(vars[v].name, std::regex(spec.names[g]))
+                                       : vars[v].name == spec.names[g];
+      if (match) groups[g].push_back((int)v);
+    }
+  }
+  auto cs = std::make_unique<CachedSparse>();
+  compat_detail::PackTables &t = cs->t;
+  std::vector<std::pair<int, int>> entries;  // (variable, component) in pack order
+  for (size_t g = 0; g < groups.size(); ++g) {
+    t.lo.push_back((int)entries.size());
+    for (int v : groups[g])
+      for (int q = 0; q < vars[v].ncomp; ++q) entries.push_back({v, q});
+    t.hi.push_back((int)entries.size() - 1);
+  }
+  const BlockStore &st = store();
+  Container &c = pm_->container(name_);
+  t.nblocks = (int)blocks.size();
+  t.nvar = (int)entries.size();
+  t.N0 = st.N[0];
+  t.N01 = st.N[0] * st.N[1];
+  t.with_fluxes = spec.with_fluxes;
+  const int64_t cells = st.cells();
+  std::vector<Real *> ptr((size_t)t.nblocks * t.nvar * 3, nullptr), fptr;
+  if (spec.with_fluxes) fptr.assign(ptr.size(), nullptr);
+  std::vector<Coordinates_t> coords;
+  std::vector<int> gids;
+  for (int pb = 0; pb < t.nblocks; ++pb) {
+    const int slot = set_.slot[blocks[pb]];
+    coords.push_back(st.coords[slot]);
+    gids.push_back(set_.store == 0 && slot < pm_->nbtotal ? slot : -1);
+    for (int e = 0; e < t.nvar; ++e) {
+      const int v = entries[e].first, q = entries[e].second, nc = vars[v].ncomp;
+      Real *base = c.at(v, set_.store);
+      const int64_t off = ((int64_t)slot * nc + q) * cells;
+      const int64_t plane = (int64_t)st.nslots * nc * cells;  // one face direction
+      for (int sl = 0; sl < 3; ++sl)
+        ptr[((size_t)pb * t.nvar + e) * 3 + sl] = base + off + (vars[v].face() ? sl * plane : 0);
+      if (spec.with_fluxes && vars[v].with_fluxes()) {
+        Real *fb = c.flux_at(v, set_.store);
+        for (int d = 0; d < 3; ++d)
+          fptr[((size_t)pb * t.nvar + e) * 3 + d] = fb + (((int64_t)slot * 3 + d) * nc + q) * cells;
+      }
+    }
+  }
+  // one device allocation: pointer tables, coordinates, block ids
+  const size_t np = ptr.size(), nf = fptr.size();
+  const size_t bytes_ptr = (np + nf) * sizeof(Real *);
+  const size_t off_c = (bytes_ptr + 255) & ~size_t(255);
+  const size_t off_g = (off_c + coords.size() * sizeof(Coordinates_t) + 255) & ~size_t(255);
+  const size_t bytes = off_g + gids.size() * sizeof(int) + 16;
+  check_cuda(cudaMalloc(&cs->dev, bytes), "pack table");
+  std::vector<char> h(bytes, 0);
+  if (np) std::memcpy(h.data(), ptr.data(), np * sizeof(Real *));
+  if (nf) std::memcpy(h.data() + np * sizeof(Real *), fptr.data(), nf * sizeof(Real *));
+  if (!coords.empty()) std::memcpy(h.data() + off_c, coords.data(), coords.size() * sizeof(Coordinates_t));
+  if (!gids.empty()) std::memcpy(h.data() + off_g, gids.data(), gids.size() * sizeof(int));
+  check_cuda(cudaMemcpy(cs->dev, h.data(), bytes, cudaMemcpyHostToDevice), "pack table upload");
+  char *d = static_cast<char *>(cs->dev);
+  t.ptr = reinterpret_cast<Real **>(d);
+  t.fptr = nf ? reinterpret_cast<Real **>(d + np * sizeof(Real *)) : nullptr;
+  t.coords = reinterpret_cast<const Coordinates_t *>(d + off_c);
+  t.gid = reinterpret_cast<const int *>(d + off_g);
+  return sparse_.emplace(key, std::move(cs)).first->second->t;
+}
+
+namespace compat_detail {
+inline const PackTables &get_pack_tables(MeshData<Real> *md, const PackSpec &spec, const std::vector<bool> &include,
+                                         bool only_fine) {
+  return md->sparse_pack(spec, include, only_fine);
+}
+}  // namespace compat_detail
+
 template <typename T>
 const VariablePack<T> &MeshBlockData<T>::PackVariables(const std::vector<std::string> &names, PackIndexMap &imap) {
   return pmb_->pmy_mesh->mesh_data.GetOrAdd(name_, 0)->pack(names, {}, &imap, false, pmb_->gid);
@@ -612,13 +954,27 @@ const VariableFluxPack<T> &MeshBlockData<T>::PackVariablesAndFluxes(const std::v
   return pmb_->pmy_mesh->mesh_data.GetOrAdd(name_, 0)->pack(names, fluxes, &imap, true, pmb_->gid);
 }
 
+namespace compat_detail {
+inline const PackTables &get_pack_tables(MeshBlockData<Real> *mbd, const PackSpec &spec) {
+  MeshBlock *pmb = mbd->GetBlockPointer();
+  return pmb->pmy_mesh->mesh_data.GetOrAdd(mbd->StageName(), 0)->sparse_pack(spec, {}, true, pmb->gid);
+}
+}  // namespace compat_detail
+
 inline std::shared_ptr<MeshData<Real>> &DataCollection<MeshData<Real>>::GetOrAdd(const std::string &name,
                                                                                    int partition) {
   PARTHENON_REQUIRE_THROWS(partition == 0, "one partition holds every block");
-  auto it = mds_.find(name);
+  return GetOrAdd(name, GridIdentifier::leaf());
+}
+
+inline std::shared_ptr<MeshData<Real>> &DataCollection<MeshData<Real>>::GetOrAdd(const std::string &name,
+                                                                                   const GridIdentifier &grid) {
+  const GridIdentifier g = grid.type == GridType::none ? GridIdentifier::leaf() : grid;
+  const auto key = std::make_pair(name, g);
+  auto it = mds_.find(key);
   if (it == mds_.end()) {
     pm_->container(name);
-    it = mds_.emplace(name, std::make_shared<MeshData<Real>>(pm_, name)).first;
+    it = mds_.emplace(key, std::make_shared<MeshData<Real>>(pm_, name, g)).first;
   }
   return it->second;
 }

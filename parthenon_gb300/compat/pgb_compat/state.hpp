@@ -8,6 +8,7 @@
 // src/interface/params.hpp (HistoryOutputVar, UserHistoryOperation, hist_param_key).
 #pragma once
 
+#include <array>
 #include <functional>
 #include <map>
 #include <memory>
@@ -77,12 +78,30 @@ class Metadata {
     return n;
   }
   const std::vector<std::string> &getComponentLabels() const { return labels_; }
+  // refinement operators of the variable (metadata.hpp RegisterRefinementOps): the
+  // library's transfers use ProlongateSharedLinear/MinMod and RestrictAverage, chosen by
+  // the caller of the exchange, so the registration is recorded only
+  template <class ProlongationOp, class RestrictionOp, class InternalProlongationOp = ProlongationOp>
+  void RegisterRefinementOps() {
+    has_refinement_ops_ = true;
+  }
+  bool HasRefinementOps() const { return has_refinement_ops_; }
 
  private:
   std::set<MetadataFlag> flags_;
   std::vector<int> shape_;
   std::vector<std::string> labels_;
+  bool has_refinement_ops_ = false;
 };
+
+// src/prolong_restrict/pr_ops.hpp: operator tags for RegisterRefinementOps
+namespace refinement_ops {
+struct ProlongateSharedMinMod {};
+struct ProlongateSharedLinear {};
+struct ProlongatePiecewiseConstant {};
+struct ProlongateInternalAverage {};
+struct RestrictAverage {};
+}  // namespace refinement_ops
 
 // refinement tags (src/amr_criteria/amr_criteria.hpp AmrTag)
 enum class AmrTag : int { derefine = -1, same = 0, refine = 1 };
@@ -99,8 +118,15 @@ struct HistoryOutputVar {
 using HstVar_list = std::vector<HistoryOutputVar>;
 inline const std::string hist_param_key = "HistoryFunctions";
 
+// src/bvals/boundary_conditions.hpp: a user boundary condition of one block face
+using BValFunc = std::function<void(std::shared_ptr<MeshBlockData<Real>> &, bool)>;
+using BValFuncArray_t = std::array<std::vector<BValFunc>, BOUNDARY_NFACES>;
+
 class StateDescriptor {
  public:
+  // boundary functions the package registers per block face (state_descriptor.hpp:397);
+  // every boundary of the meshes on this path is periodic, so they are kept, not called
+  BValFuncArray_t UserBoundaryFunctions;
   explicit StateDescriptor(const std::string &label) : label_(label) {}
   const std::string &label() const { return label_; }
 
@@ -131,8 +157,10 @@ class StateDescriptor {
   bool AddField(const std::string &name, const Metadata &m) {
     for (const auto &f : fields_)
       if (f.first == name) return false;
-    PARTHENON_REQUIRE_THROWS(m.IsSet(Metadata::Cell),
-                             "field " + name + ": only cell-centred fields are on this path");
+    PARTHENON_REQUIRE_THROWS(m.IsSet(Metadata::Cell) || m.IsSet(Metadata::Face),
+                             "field " + name + ": only cell-centred and face fields are on this path");
+    PARTHENON_REQUIRE_THROWS(!m.IsSet(Metadata::Face) || !m.IsSet(Metadata::FillGhost),
+                             "field " + name + ": face fields are not exchanged on this path");
     PARTHENON_REQUIRE_THROWS(!m.IsSet(Metadata::Sparse), "field " + name + ": sparse fields go through the C ABI");
     fields_.emplace_back(name, m);
     return true;

@@ -10,7 +10,10 @@
 // dependencies' kernels without host synchronisation.
 #pragma once
 
+#include <cstdint>
 #include <functional>
+#include <string>
+#include <type_traits>
 #include <memory>
 #include <set>
 #include <tuple>
@@ -18,6 +21,11 @@
 #include <vector>
 
 #include "core.hpp"
+
+// task labels: the function's spelling, then the function (src/tasks/tasks.hpp:39)
+#ifndef TF
+#define TF(...) std::string(#__VA_ARGS__), __VA_ARGS__
+#endif
 
 namespace parthenon {
 
@@ -47,16 +55,66 @@ class TaskID {
   std::set<int> ids_;
 };
 
+// src/tasks/tasks.hpp:52-80: how a task takes part in its region. One partition per
+// region runs here, so local and global synchronisation are the dependency order
+// itself; `completion` tasks decide whether an iterating sublist goes round again.
+class TaskQualifier {
+ public:
+  using qualifier_t = uint64_t;
+  TaskQualifier() = delete;
+  TaskQualifier(const qualifier_t n) : flags(n) {}  // NOLINT(runtime/explicit)
+  static inline constexpr qualifier_t normal{0};
+  static inline constexpr qualifier_t local_sync{1 << 0};
+  static inline constexpr qualifier_t global_sync{1 << 1};
+  static inline constexpr qualifier_t completion{1 << 2};
+  static inline constexpr qualifier_t once_per_region{1 << 3};
+  bool LocalSync() const { return flags & local_sync; }
+  bool GlobalSync() const { return flags & global_sync; }
+  bool Completion() const { return flags & completion; }
+  bool Once() const { return flags & once_per_region; }
+
+ private:
+  qualifier_t flags;
+};
+
+template <class T>
+struct compat_is_tuple : std::false_type {};
+template <class... Ts>
+struct compat_is_tuple<std::tuple<Ts...>> : std::true_type {};
+
 class TaskList {
  public:
-  // fn(args...) must return a TaskStatus; the arguments are stored by value
-  template <class F, class... Args>
-  TaskID AddTask(const TaskID &dep, F &&fn, Args &&...args) {
-    auto call = [f = std::forward<F>(fn), tup = std::make_tuple(std::forward<Args>(args)...)]() mutable {
-      return std::apply([&f](auto &...a) { return static_cast<TaskStatus>(f(a...)); }, tup);
-    };
-    tasks_.push_back(Task{(int)tasks_.size() + 1, dep, std::function<TaskStatus()>(std::move(call)), false});
-    return TaskID(tasks_.back().id);
+  TaskList() = default;
+  TaskList(int min_iters, int max_iters) : min_iters_(min_iters), max_iters_(max_iters) {}
+
+  // AddTask([qualifier,] dep, [label | (label, verbosity, fn) tuple,] fn, args...): fn
+  // (a callable or a member-function pointer followed by its object) must return a
+  // TaskStatus; the arguments are stored by value
+  template <class Arg1, class... Args>
+  TaskID AddTask(const TaskID &dep, Arg1 &&a1, Args &&...args) {
+    return AddTask(TaskQualifier::normal, dep, std::forward<Arg1>(a1), std::forward<Args>(args)...);
+  }
+  template <class Arg1, class... Args>
+  TaskID AddTask(const TaskQualifier tq, const TaskID &dep, Arg1 &&a1, Args &&...args) {
+    if constexpr (std::is_invocable<Arg1, Args...>::value) {
+      return add(tq, dep, std::forward<Arg1>(a1), std::forward<Args>(args)...);
+    } else if constexpr (std::is_convertible<Arg1, std::string>::value) {
+      return add(tq, dep, std::forward<Args>(args)...);  // a label
+    } else if constexpr (compat_is_tuple<std::decay_t<Arg1>>::value) {
+      return add(tq, dep, std::get<2>(a1), std::forward<Args>(args)...);
+    } else {
+      static_assert(std::is_invocable<Arg1, Args...>::value, "AddTask: bad signature");
+      return TaskID();
+    }
+  }
+  // A list that runs after `dep` and, when its tasks are done, runs again while a
+  // completion task asked to iterate (at least min, at most max times); the returned id
+  // completes with it (src/tasks/tasks.hpp:342-347)
+  std::pair<TaskList &, TaskID> AddSublist(const TaskID &dep, std::pair<int, int> minmax_iters) {
+    sublists_.push_back(std::make_unique<TaskList>(minmax_iters.first, minmax_iters.second));
+    TaskList *sub = sublists_.back().get();
+    const TaskID id = add(TaskQualifier::normal, dep, [sub]() { return sub->RunIterations(); });
+    return {*sub, id};
   }
   // one pass over the tasks whose dependencies are done; returns the list's status
   TaskListStatus Step() {
@@ -73,6 +131,7 @@ class TaskList {
         }
         if (st == TaskStatus::complete || st == TaskStatus::iterate) {
           t.done = true;
+          t.status = st;
           ran = true;
         }
       }
@@ -80,6 +139,22 @@ class TaskList {
     for (auto &t : tasks_)
       if (!t.done) return TaskListStatus::running;
     return TaskListStatus::complete;
+  }
+  // the whole list, iterated as a sublist: complete, fail, or incomplete while a task
+  // waits
+  TaskStatus RunIterations() {
+    while (true) {
+      const TaskListStatus st = Step();
+      if (st == TaskListStatus::fail) return TaskStatus::fail;
+      if (st != TaskListStatus::complete) return TaskStatus::incomplete;
+      ++iter_;
+      bool again = false;
+      for (auto &t : tasks_)
+        if (t.completion && t.status == TaskStatus::iterate) again = true;
+      if (iter_ < min_iters_) again = true;
+      if (!again || iter_ >= max_iters_) return TaskStatus::complete;
+      for (auto &t : tasks_) t.done = false;
+    }
   }
   bool Empty() const { return tasks_.empty(); }
 
@@ -89,14 +164,27 @@ class TaskList {
     TaskID dep;
     std::function<TaskStatus()> fn;
     bool done;
+    bool completion;
+    TaskStatus status;
   };
+  template <class F, class... Args>
+  TaskID add(const TaskQualifier tq, const TaskID &dep, F &&fn, Args &&...args) {
+    auto call = [f = std::forward<F>(fn), tup = std::make_tuple(std::forward<Args>(args)...)]() mutable {
+      return std::apply([&f](auto &...a) { return static_cast<TaskStatus>(std::invoke(f, a...)); }, tup);
+    };
+    tasks_.push_back(Task{(int)tasks_.size() + 1, dep, std::function<TaskStatus()>(std::move(call)), false,
+                          tq.Completion(), TaskStatus::incomplete});
+    return TaskID(tasks_.back().id);
+  }
   bool ready(const Task &t) const {
     for (int d : t.dep.ids())
       if (d < 1 || d > (int)tasks_.size() || !tasks_[d - 1].done) return false;
     return true;
   }
   std::vector<Task> tasks_;
+  std::vector<std::unique_ptr<TaskList>> sublists_;
   bool failed_ = false;
+  int min_iters_ = 1, max_iters_ = 1, iter_ = 0;
 };
 
 class TaskRegion {

@@ -71,24 +71,91 @@ KOKKOS_FORCEINLINE_FUNCTION Real div_rn(Real a, Real b) {
 #endif
 }
 
-// the ghost exchange of every FillGhost variable of a container
+// The multigrid grids of the layer's mesh: one field of a grid (its store's array),
+// moved with the library's transfers (pgb_mg_field_*).
+namespace mg {
+inline int store_of(int level) { return level >= 0 ? 0 : level; }
+inline Real *field(Mesh *pm, const std::string &container, int v, int level) {
+  PARTHENON_REQUIRE_THROWS(pm->variables()[v].ncomp == 1, "multigrid fields have one component on this path");
+  return pm->container(container).at(v, store_of(level));
+}
+inline Real *field(Mesh *pm, const std::string &container, const std::string &name, int level) {
+  const int v = pm->var_index(name);
+  PARTHENON_REQUIRE_THROWS(v >= 0, "no variable named " + name);
+  return field(pm, container, v, level);
+}
+inline bool has_flag(Mesh *pm, const std::string &name, const MetadataFlag &f) {
+  const int v = pm->var_index(name);
+  return v >= 0 && pm->variables()[v].m.IsSet(f);
+}
+// gmg_same ghost exchange of one field on grid `level`
+inline void exchange(Mesh *pm, const std::string &container, int v, int level) {
+  check_pgb(pgb_mg_field_exchange(pm->mg(), level, field(pm, container, v, level), compat_stream()),
+            "pgb_mg_field_exchange");
+}
+// gmg_restrict_send + recv: grid level's fine blocks into their parents on level - 1
+// (RestrictAverage; on faces for a face field)
+inline void restrict_field(Mesh *pm, const std::string &container, int v, int level) {
+  Real *fine = pm->container(container).at(v, store_of(level));
+  Real *coarse = pm->container(container).at(v, store_of(level - 1));
+  PARTHENON_REQUIRE_THROWS(pm->variables()[v].ncomp == 1, "multigrid fields have one component on this path");
+  if (pm->variables()[v].face())
+    check_pgb(pgb_mg_face_restrict(pm->mg(), level, fine, coarse, compat_stream()), "pgb_mg_face_restrict");
+  else
+    check_pgb(pgb_mg_field_restrict(pm->mg(), level, fine, coarse, compat_stream()), "pgb_mg_field_restrict");
+}
+// gmg_prolongate_send/recv + ProlongateBounds: the parents on level - 1 into the
+// interiors of grid level's fine blocks (ProlongateSharedLinear)
+inline void prolongate_field(Mesh *pm, const std::string &container, int v, int level) {
+  check_pgb(pgb_mg_field_prolongate(pm->mg(), level, field(pm, container, v, level - 1),
+                                    field(pm, container, v, level), compat_stream()),
+            "pgb_mg_field_prolongate");
+}
+}  // namespace mg
+
+// the ghost exchange of every FillGhost variable of a container: the leaves
+// (pgb_exchange), or a multigrid grid (gmg_same)
 inline TaskStatus exchange(MeshData<Real> *md) {
   Mesh *pm = md->GetMeshPointer();
   Container &c = pm->container(md->StageName());
   const auto &vars = pm->variables();
   for (size_t v = 0; v < vars.size(); ++v) {
     if (!vars[v].m.IsSet(Metadata::FillGhost)) continue;
-    check_pgb(pgb_exchange(pm->handle(), c.data[v], nullptr, vars[v].ncomp, 0, nullptr, compat_stream()),
-              "pgb_exchange");
+    if (md->grid.type == GridType::two_level_composite)
+      mg::exchange(pm, md->StageName(), (int)v, md->grid.logical_level);
+    else
+      check_pgb(pgb_exchange(pm->handle(), c.data[v], nullptr, vars[v].ncomp, 0, nullptr, compat_stream()),
+                "pgb_exchange");
+  }
+  return TaskStatus::complete;
+}
+// the multigrid transfers of a grid's MeshData: every variable with the flag
+inline TaskStatus gmg_transfer(MeshData<Real> *md, BoundaryType bt) {
+  Mesh *pm = md->GetMeshPointer();
+  PARTHENON_REQUIRE_THROWS(md->grid.type == GridType::two_level_composite, "multigrid transfer off a multigrid grid");
+  const int L = md->grid.logical_level;
+  const auto &vars = pm->variables();
+  for (size_t v = 0; v < vars.size(); ++v) {
+    if (bt == BoundaryType::gmg_restrict_send && vars[v].m.IsSet(Metadata::GMGRestrict) && L > pm->GetGMGMinLevel())
+      mg::restrict_field(pm, md->StageName(), (int)v, L);
+    if (bt == BoundaryType::gmg_prolongate_send && vars[v].m.IsSet(Metadata::GMGProlongate) &&
+        L < pm->GetGMGMaxLevel())
+      mg::prolongate_field(pm, md->StageName(), (int)v, L + 1);
   }
   return TaskStatus::complete;
 }
 }  // namespace compat_detail
 
 // ---- boundary exchange (same-rank: Send does the exchange) --------------------------
+// gmg_restrict_send / gmg_prolongate_send move the grid's GMGRestrict / GMGProlongate
+// fields to the next coarser / finer grid (their receiving tasks have nothing left to
+// do); the other kinds exchange ghosts
 template <BoundaryType BT>
 TaskStatus SendBoundBufs(std::shared_ptr<MeshData<Real>> &md) {
   if (BT == BoundaryType::nonlocal) return TaskStatus::complete;  // no other ranks
+  if (BT == BoundaryType::gmg_restrict_send || BT == BoundaryType::gmg_prolongate_send)
+    return compat_detail::gmg_transfer(md.get(), BT);
+  if (BT == BoundaryType::gmg_restrict_recv || BT == BoundaryType::gmg_prolongate_recv) return TaskStatus::complete;
   return compat_detail::exchange(md.get());
 }
 template <BoundaryType BT>
@@ -113,13 +180,13 @@ inline TaskStatus LoadAndSendFluxCorrections(std::shared_ptr<MeshData<Real>> &) 
 inline TaskStatus ReceiveFluxCorrections(std::shared_ptr<MeshData<Real>> &) { return TaskStatus::complete; }
 inline TaskStatus SetFluxCorrections(std::shared_ptr<MeshData<Real>> &) { return TaskStatus::complete; }
 
-inline TaskID AddBoundaryExchangeTasks(TaskID dependency, TaskList &tl, std::shared_ptr<MeshData<Real>> &md,
-                                       bool multilevel) {
-  const auto any = BoundaryType::any;
-  auto send = tl.AddTask(dependency, SendBoundBufs<any>, md);
-  auto recv = tl.AddTask(dependency, ReceiveBoundBufs<any>, md);
-  auto set = tl.AddTask(send | recv, SetBounds<any>, md);
-  if (multilevel) set = tl.AddTask(set, ProlongateBounds<any>, md);
+// bvals_in_one.hpp:83-93
+template <BoundaryType bounds = BoundaryType::any, class TL_t>
+TaskID AddBoundaryExchangeTasks(TaskID dependency, TL_t &tl, std::shared_ptr<MeshData<Real>> &md, bool multilevel) {
+  auto send = tl.AddTask(dependency, SendBoundBufs<bounds>, md);
+  auto recv = tl.AddTask(dependency, ReceiveBoundBufs<bounds>, md);
+  auto set = tl.AddTask(send | recv, SetBounds<bounds>, md);
+  if (multilevel) set = tl.AddTask(set, ProlongateBounds<bounds>, md);
   return set;
 }
 inline TaskID AddFluxCorrectionTasks(TaskID dependency, TaskList &tl, std::shared_ptr<MeshData<Real>> &md,
@@ -252,5 +319,25 @@ TaskStatus FillDerived(T *rc) {
 // the mesh-level initialisation (Mesh::Initialize, mesh.cpp:745-858): problem
 // generator on every block, ghost exchange, derived fields
 class ApplicationInput;
+
+// src/bvals/boundary_conditions_generic.hpp: the generic physical boundary conditions.
+// The meshes of this path are periodic in every direction, so no block face is a
+// physical boundary and these are never applied; a call is an error.
+namespace BoundaryFunction {
+enum class BCSide { Inner, Outer };
+enum class BCType { Outflow, Reflect, ConstantDeriv, Fixed, FixedFace, Periodic };
+template <CoordinateDirection DIR, BCSide SIDE, BCType TYPE, class... var_ts>
+void GenericBC(std::shared_ptr<MeshBlockData<Real>> &, bool, TopologicalElement, Real) {
+  PARTHENON_FAIL("physical boundary conditions: every boundary is periodic on this path");
+}
+template <CoordinateDirection DIR, BCSide SIDE, BCType TYPE, class... var_ts>
+void GenericBC(std::shared_ptr<MeshBlockData<Real>> &rc, bool coarse, Real val = 0.0) {
+  GenericBC<DIR, SIDE, TYPE, var_ts...>(rc, coarse, TopologicalElement::CC, val);
+}
+}  // namespace BoundaryFunction
+
+// host arrays of the reference's Kokkos host views
+template <class T>
+using HostArray1D = std::vector<T>;
 
 }  // namespace parthenon

@@ -318,65 +318,69 @@ __device__ __forceinline__ void fas_cell(const StoreView<T> &s, bool internal, c
   }
 }
 
-// RestrictAverage (pr_ops.hpp:105-164) of the child's interior, u and res_err, into the
-// parent's octant (gmg_restrict_send + gmg_restrict_recv), one parent cell. FP64
-// children: the reference's volume-weighted form; FP32 children (the mixed V-cycle): the
-// mean of the eight cells. TP is the parent's type.
+// RestrictAverage (pr_ops.hpp:105-164) of one field of the child's interior into the
+// parent's octant, one parent cell (f, p: the first fine cell and the parent cell).
+// FP64 children: the reference's volume-weighted form; FP32 children (the mixed
+// V-cycle): the mean of the eight cells. TP is the parent's type.
+template <class TC, class TP>
+__device__ __forceinline__ void restrict_field_cell(const TC *__restrict__ a, TP *__restrict__ out, const Dims &d,
+                                                    double vol, int64_t f, int64_t p) {
+  const int64_t cj = d.N[0], ck = (int64_t)d.N[0] * d.N[1];
+  if constexpr (sizeof(TC) == 8) {
+    const double tv = ((vol + vol) + (vol + vol)) + ((vol + vol) + (vol + vol));
+    // t[ok][oj][oi] = vol * fine(k + ok, j + oj, i + oi)
+    const double t000 = vol * a[f], t001 = vol * a[f + 1];
+    const double t010 = vol * a[f + cj], t011 = vol * a[f + cj + 1];
+    const double t100 = vol * a[f + ck], t101 = vol * a[f + ck + 1];
+    const double t110 = vol * a[f + ck + cj], t111 = vol * a[f + ck + cj + 1];
+    const double num = ((t000 + t010) + (t001 + t011)) + ((t100 + t110) + (t101 + t111));
+    out[p] = (TP)div_rn(num, tv);
+  } else {
+    const TC sum = ((a[f] + a[f + cj]) + (a[f + 1] + a[f + cj + 1])) +
+                   ((a[f + ck] + a[f + ck + cj]) + (a[f + ck + 1] + a[f + ck + cj + 1]));
+    out[p] = (TP)((TC)0.125 * sum);
+  }
+}
+
+// u and res_err of one parent cell (gmg_restrict_send + gmg_restrict_recv)
 template <class TC, class TP>
 __device__ __forceinline__ void restrict_cell(const StoreView<TC> &cs, const StoreView<TP> &ps, const MgXfer &t,
                                               double vol, int ci, int cjj, int ckk) {
   const int ng = cs.d.ng;
-  const int64_t cj = cs.d.N[0], ck = (int64_t)cs.d.N[0] * cs.d.N[1];
   const int64_t f = cell_of(cs.d, t.child, 2 * ckk + ng, 2 * cjj + ng, 2 * ci + ng);
   const int64_t p = cell_of(ps.d, t.parent, t.lo[2] + ckk, t.lo[1] + cjj, t.lo[0] + ci);
-#pragma unroll
-  for (int v = 0; v < 2; ++v) {
-    const TC *__restrict__ a = v == 0 ? cs.u : cs.res;
-    TP out;
-    if constexpr (sizeof(TC) == 8) {
-      const double tv = ((vol + vol) + (vol + vol)) + ((vol + vol) + (vol + vol));
-      // t[ok][oj][oi] = vol * fine(k + ok, j + oj, i + oi)
-      const double t000 = vol * a[f], t001 = vol * a[f + 1];
-      const double t010 = vol * a[f + cj], t011 = vol * a[f + cj + 1];
-      const double t100 = vol * a[f + ck], t101 = vol * a[f + ck + 1];
-      const double t110 = vol * a[f + ck + cj], t111 = vol * a[f + ck + cj + 1];
-      const double num = ((t000 + t010) + (t001 + t011)) + ((t100 + t110) + (t101 + t111));
-      out = (TP)div_rn(num, tv);
-    } else {
-      const TC sum = ((a[f] + a[f + cj]) + (a[f + 1] + a[f + cj + 1])) +
-                     ((a[f + ck] + a[f + ck + cj]) + (a[f + ck + 1] + a[f + ck + cj + 1]));
-      out = (TP)((TC)0.125 * sum);
-    }
-    (v == 0 ? ps.u : ps.res)[p] = out;
-  }
+  restrict_field_cell(cs.u, ps.u, cs.d, vol, f, p);
+  restrict_field_cell(cs.res, ps.res, cs.d, vol, f, p);
 }
 
-// ProlongateSharedLinear (pr_ops.hpp:166-285) of the parent's res_err (its octant with
-// ghosts is the child's coarse buffer) and AddFieldsAndStore<u, res_err, u>, one coarse
-// cell of the child's interior (eight fine cells). The exact build forms the slopes from
-// the cell-centre coordinates as the reference does (g: the child's geometry); the fast
-// build uses the uniform-spacing value dx_fine / 2 / dx_coarse = 1/4 of each difference.
-// TC is the child's type (the arithmetic), TP the parent's.
-template <bool kFast, class TC, class TP>
-__device__ __forceinline__ void prolong_add_cell(const StoreView<TC> &cs, const StoreView<TP> &ps, const MgXfer &t,
-                                                 const DevBlockGeom *__restrict__ g, int c0, int c1, int c2) {
-  const int ng = cs.d.ng;
-  const int64_t pj = ps.d.N[0], pk = (int64_t)ps.d.N[0] * ps.d.N[1];
-  const int64_t N0 = cs.d.N[0], N01 = (int64_t)cs.d.N[0] * cs.d.N[1];
+// ProlongateSharedLinear (pr_ops.hpp:166-285) of a parent field (its octant with ghosts
+// is the child's coarse buffer), one coarse cell of the child's interior: apply(offset,
+// value) receives each of the eight fine values, offset relative to the first fine cell
+// `fine`. The exact build forms the slopes from the cell-centre coordinates as the
+// reference does (g: the child's geometry); the fast build uses the uniform-spacing value
+// dx_fine / 2 / dx_coarse = 1/4 of each difference. TC is the child's type (the
+// arithmetic), TP the parent's.
+template <bool kFast, class TC, class TP, class F>
+__device__ __forceinline__ void prolong_field_cell(const TP *__restrict__ pf, const Dims &pd, const Dims &cd,
+                                                   const MgXfer &t, const DevBlockGeom *__restrict__ g, int c0, int c1,
+                                                   int c2, int64_t &fine, F &&apply) {
+  const int ng = cd.ng;
+  const int64_t pj = pd.N[0], pk = (int64_t)pd.N[0] * pd.N[1];
+  const int64_t N0 = cd.N[0], N01 = (int64_t)cd.N[0] * cd.N[1];
   const int c[3] = {c0 + ng, c1 + ng, c2 + ng};  // coarse-buffer index
   const int f[3] = {2 * c0 + ng, 2 * c1 + ng, 2 * c2 + ng};
   const int p[3] = {t.lo[0] + c0, t.lo[1] + c1, t.lo[2] + c2};
-  const int64_t pe = cell_of(ps.d, t.parent, p[2], p[1], p[0]);
-  const TC fc = (TC)ps.res[pe];
+  const int64_t pe = cell_of(pd, t.parent, p[2], p[1], p[0]);
+  const TC fc = (TC)pf[pe];
   // the parent's cells next to p along d: its ghosts, or on a grid read directly the
   // face neighbour's interior cell
   auto side = [&](int d, int s) -> TC {
     const int64_t st = d == 0 ? 1 : (d == 1 ? pj : pk);
-    const int lo = ps.d.ng, hi = ps.d.ng + ps.d.nx[d] - 1;
-    if (t.pnb[0] < 0 || (s < 0 ? p[d] > lo : p[d] < hi)) return (TC)ps.res[pe + s * st];
+    const int lo = pd.ng, hi = pd.ng + pd.nx[d] - 1;
+    if (t.pnb[0] < 0 || (s < 0 ? p[d] > lo : p[d] < hi)) return (TC)pf[pe + s * st];
     int q[3] = {p[0], p[1], p[2]};
     q[d] = s < 0 ? hi : lo;
-    return (TC)ps.res[cell_of(ps.d, t.pnb[2 * d + (s > 0)], q[2], q[1], q[0])];
+    return (TC)pf[cell_of(pd, t.pnb[2 * d + (s > 0)], q[2], q[1], q[0])];
   };
   TC mq[3], pq[3];
 #pragma unroll
@@ -396,15 +400,26 @@ __device__ __forceinline__ void prolong_add_cell(const StoreView<TC> &cs, const 
     }
   }
   const TC m0 = mq[0], p0 = pq[0], m1 = mq[1], p1 = pq[1], m2 = mq[2], p2 = pq[2];
-  TC *U = cs.u + cell_of(cs.d, t.child, f[2], f[1], f[0]);
-  U[0] = U[0] + (fc - ((m0 + m1) + m2));
-  U[1] = U[1] + (fc + ((p0 - m1) - m2));
-  U[N0] = U[N0] + (fc - ((m0 - p1) + m2));
-  U[N0 + 1] = U[N0 + 1] + (fc + ((p0 + p1) - m2));
-  U[N01] = U[N01] + (fc - ((m0 + m1) - p2));
-  U[N01 + 1] = U[N01 + 1] + (fc + ((p0 - m1) + p2));
-  U[N01 + N0] = U[N01 + N0] + (fc - ((m0 - p1) - p2));
-  U[N01 + N0 + 1] = U[N01 + N0 + 1] + (fc + ((p0 + p1) + p2));
+  fine = cell_of(cd, t.child, f[2], f[1], f[0]);
+  apply((int64_t)0, fc - ((m0 + m1) + m2));
+  apply((int64_t)1, fc + ((p0 - m1) - m2));
+  apply(N0, fc - ((m0 - p1) + m2));
+  apply(N0 + 1, fc + ((p0 + p1) - m2));
+  apply(N01, fc - ((m0 + m1) - p2));
+  apply(N01 + 1, fc + ((p0 - m1) + p2));
+  apply(N01 + N0, fc - ((m0 - p1) - p2));
+  apply(N01 + N0 + 1, fc + ((p0 + p1) + p2));
+}
+
+// The prolongation of the parent's res_err added into the child's u
+// (AddFieldsAndStore<u, res_err, u>), one coarse cell of the child's interior
+template <bool kFast, class TC, class TP>
+__device__ __forceinline__ void prolong_add_cell(const StoreView<TC> &cs, const StoreView<TP> &ps, const MgXfer &t,
+                                                 const DevBlockGeom *__restrict__ g, int c0, int c1, int c2) {
+  int64_t fine = 0;
+  TC *__restrict__ U = cs.u;
+  prolong_field_cell<kFast, TC>(ps.res, ps.d, cs.d, t, g, c0, c1, c2, fine,
+                                [&](int64_t o, TC v) { U[fine + o] = U[fine + o] + v; });
 }
 
 // ---- grid kernels: every interior cell of the listed blocks
@@ -489,6 +504,44 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreV
     const int r = e - q * per;
     const MgXfer t = x[q];
     prolong_add_cell<kFast>(cs, ps, t, cgeom + t.child, r % h0, (r / h0) % h1, r / (h0 * h1));
+  }
+}
+
+// ---- one field of a package-side solver (pgb_mg_field_*): the same transfers on a
+// field held in the store layout by the caller
+
+// RestrictAverage of every fine block of a grid into its parent's octant, one field
+__global__ void __launch_bounds__(256) k_mgf_restrict(const double *__restrict__ cf, Dims cd, double *__restrict__ pf,
+                                                      Dims pd, const MgXfer *__restrict__ x, int n,
+                                                      const DevBlockGeom *__restrict__ cgeom) {
+  const int h0 = max(1, cd.nx[0] / 2), h1 = max(1, cd.nx[1] / 2), h2 = max(1, cd.nx[2] / 2);
+  const int per = h0 * h1 * h2, total = per * n;
+  const int ng = cd.ng;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int q = e / per;
+    const int r = e - q * per;
+    const MgXfer t = x[q];
+    const int ci = r % h0, cj = (r / h0) % h1, ck = r / (h0 * h1);
+    restrict_field_cell(cf, pf, cd, cgeom[t.child].vol, cell_of(cd, t.child, 2 * ck + ng, 2 * cj + ng, 2 * ci + ng),
+                        cell_of(pd, t.parent, t.lo[2] + ck, t.lo[1] + cj, t.lo[0] + ci));
+  }
+}
+
+// ProlongateSharedLinear of the parents' field into the interior of every fine block of
+// a grid (the values written, not added), one thread per coarse cell of a child
+template <bool kFast>
+__global__ void __launch_bounds__(256) k_mgf_prolong(const double *__restrict__ pf, Dims pd, double *__restrict__ cf,
+                                                     Dims cd, const MgXfer *__restrict__ x, int n,
+                                                     const DevBlockGeom *__restrict__ cgeom) {
+  const int h0 = max(1, cd.nx[0] / 2), h1 = max(1, cd.nx[1] / 2), h2 = max(1, cd.nx[2] / 2);
+  const int per = h0 * h1 * h2, total = per * n;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int q = e / per;
+    const int r = e - q * per;
+    const MgXfer t = x[q];
+    int64_t fine = 0;
+    prolong_field_cell<kFast, double>(pf, pd, cd, t, cgeom + t.child, r % h0, (r / h0) % h1, r / (h0 * h1), fine,
+                                      [&](int64_t o, double v) { cf[fine + o] = v; });
   }
 }
 
@@ -2029,6 +2082,125 @@ int pgb_mg_bicgstab(pgb_mg *g, double *u, const double *rhs, int32_t preconditio
   PGB_CUDA(cudaStreamSynchronize(s));
   if (iters_out) *iters_out = it;
   if (rms_out) *rms_out = rms;
+  return kOk;
+}
+
+/* ---- the composite grids for a package-side solver ---------------------------- */
+
+int pgb_mg_layout(pgb_mg *g, int32_t *out) {
+  if (!g || !out) return fail(kErrInvalid, "null argument");
+  int rc;
+  if ((rc = mg_upload(g))) return rc;
+  out[0] = g->lmin;
+  out[1] = g->lmax;
+  out[2] = g->nleaf;
+  out[3] = (int32_t)g->stores.size();
+  out[4] = g->exact ? 1 : 0;
+  return kOk;
+}
+
+int pgb_mg_store_info(pgb_mg *g, int32_t store, int32_t *out, double *geom, int32_t *levels) {
+  if (!g || !out) return fail(kErrInvalid, "null argument");
+  int rc;
+  if ((rc = mg_upload(g))) return rc;
+  auto it = g->stores.find(store);
+  if (it == g->stores.end()) return fail(kErrInvalid, "no multigrid store with that key");
+  const pgb_mg::Store &S = it->second;
+  out[0] = S.nslots;
+  for (int d = 0; d < 3; ++d) {
+    out[1 + d] = S.dims.nx[d];
+    out[5 + d] = S.dims.N[d];
+  }
+  out[4] = S.dims.ng;
+  for (int b = 0; b < S.nslots; ++b) {
+    const BlockInfo &bi = S.blocks[b];
+    if (geom)
+      for (int d = 0; d < 3; ++d) {
+        geom[6 * b + d] = bi.xmin[d];
+        geom[6 * b + 3 + d] = bi.dx[d];
+      }
+    if (levels) levels[b] = bi.loc.level;
+  }
+  return kOk;
+}
+
+int pgb_mg_grid_info(pgb_mg *g, int32_t level, int32_t *out, int32_t *fine, int32_t *coarse) {
+  if (!g || !out) return fail(kErrInvalid, "null argument");
+  int rc;
+  if ((rc = mg_upload(g))) return rc;
+  auto it = g->grids.find(level);
+  if (it == g->grids.end()) return fail(kErrInvalid, "no multigrid grid at that level");
+  const pgb_mg::Grid &G = it->second;
+  out[0] = G.store;
+  out[1] = (int32_t)G.fine_h.size();
+  out[2] = (int32_t)G.coarse_h.size();
+  out[3] = G.nint;
+  if (fine) std::memcpy(fine, G.fine_h.data(), G.fine_h.size() * sizeof(int32_t));
+  if (coarse) std::memcpy(coarse, G.coarse_h.data(), G.coarse_h.size() * sizeof(int32_t));
+  return kOk;
+}
+
+int pgb_mg_field_exchange(pgb_mg *g, int32_t level, double *field, void *stream) {
+  if (!g || !field) return fail(kErrInvalid, "null argument");
+  int rc;
+  if ((rc = mg_upload(g))) return rc;
+  if (!g->grids.count(level)) return fail(kErrInvalid, "no multigrid grid at that level");
+  return exch(g, level, field, (cudaStream_t)stream);
+}
+
+int pgb_mg_field_restrict(pgb_mg *g, int32_t level, const double *fine, double *coarse, void *stream) {
+  if (!g || !fine || !coarse) return fail(kErrInvalid, "null argument");
+  int rc;
+  if ((rc = mg_upload(g))) return rc;
+  if (!g->grids.count(level) || level <= g->lmin) return fail(kErrInvalid, "no coarser grid below that level");
+  const pgb_mg::Grid &G = g->grids.at(level);
+  const pgb_mg::Store &C = g->store_of(level), &P = g->store_of(level - 1);
+  const int nx = (int)G.xfer_h.size();
+  if (nx == 0) return kOk;
+  const int64_t per = (int64_t)std::max(1, C.dims.nx[0] / 2) * std::max(1, C.dims.nx[1] / 2) *
+                      std::max(1, C.dims.nx[2] / 2);
+  k_mgf_restrict<<<grid_for(nx * per), 256, 0, (cudaStream_t)stream>>>(fine, C.dims, coarse, P.dims, G.xfer, nx,
+                                                                        G.tab.geom);
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+int pgb_mg_field_prolongate(pgb_mg *g, int32_t level, const double *coarse, double *fine, void *stream) {
+  if (!g || !fine || !coarse) return fail(kErrInvalid, "null argument");
+  int rc;
+  if ((rc = mg_upload(g))) return rc;
+  if (!g->grids.count(level) || level <= g->lmin) return fail(kErrInvalid, "no coarser grid below that level");
+  const pgb_mg::Grid &G = g->grids.at(level);
+  const pgb_mg::Store &C = g->store_of(level), &P = g->store_of(level - 1);
+  const int nx = (int)G.xfer_h.size();
+  if (nx == 0) return kOk;
+  const int64_t per = (int64_t)std::max(1, C.dims.nx[0] / 2) * std::max(1, C.dims.nx[1] / 2) *
+                      std::max(1, C.dims.nx[2] / 2);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (g->exact)
+    k_mgf_prolong<false><<<grid_for(nx * per), 256, 0, s>>>(coarse, P.dims, fine, C.dims, G.xfer, nx, G.tab.geom);
+  else
+    k_mgf_prolong<true><<<grid_for(nx * per), 256, 0, s>>>(coarse, P.dims, fine, C.dims, G.xfer, nx, G.tab.geom);
+  PGB_CUDA(cudaGetLastError());
+  return kOk;
+}
+
+int pgb_mg_face_restrict(pgb_mg *g, int32_t level, const double *fine, double *coarse, void *stream) {
+  if (!g || !fine || !coarse) return fail(kErrInvalid, "null argument");
+  int rc;
+  if ((rc = mg_upload(g))) return rc;
+  if (!g->grids.count(level) || level <= g->lmin) return fail(kErrInvalid, "no coarser grid below that level");
+  const pgb_mg::Grid &G = g->grids.at(level);
+  const pgb_mg::Store &C = g->store_of(level), &P = g->store_of(level - 1);
+  const int nx = (int)G.xfer_h.size();
+  if (nx == 0) return kOk;
+  const int64_t per = (int64_t)(C.dims.nx[0] / 2 + 1) * (C.dims.nx[1] / 2 + 1) * (C.dims.nx[2] / 2 + 1);
+  const int64_t cc = (int64_t)C.nslots * C.dims.N[0] * C.dims.N[1] * C.dims.N[2];
+  const int64_t pc = (int64_t)P.nslots * P.dims.N[0] * P.dims.N[1] * P.dims.N[2];
+  for (int q = 0; q < 3; ++q)
+    k_mg_restrict_faces<<<grid_for(nx * per), 256, 0, (cudaStream_t)stream>>>(fine + q * cc, C.dims, coarse + q * pc,
+                                                                               P.dims, G.xfer, nx, G.tab.geom, q);
+  PGB_CUDA(cudaGetLastError());
   return kOk;
 }
 

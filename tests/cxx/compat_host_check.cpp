@@ -21,6 +21,18 @@ static int failures = 0;
     }                                                             \
   } while (0)
 
+// variable-name types of a pack (pack_utils.hpp): a 2x3 tensor field and a scalar
+struct vec3 : public variable_names::base_t<false, 2, 3> {
+  template <class... Ts>
+  vec3(Ts &&...args) : variable_names::base_t<false, 2, 3>(std::forward<Ts>(args)...) {}
+  static std::string name() { return "vec3"; }
+};
+struct scal : public variable_names::base_t<false> {
+  template <class... Ts>
+  scal(Ts &&...args) : variable_names::base_t<false>(std::forward<Ts>(args)...) {}
+  static std::string name() { return "scal"; }
+};
+
 int main(int argc, char *argv[]) {
   // ---- tasks: dependencies, polling of incomplete tasks, failure
   {
@@ -101,6 +113,94 @@ int main(int argc, char *argv[]) {
     CHECK(rk2.nstages == 2 && rk2.beta[0] == 1.0 && rk2.beta[1] == 0.5);
     CHECK(rk2.stage_name[0] == "base" && rk2.stage_name[1] == "1" && rk2.stage_name[2] == "base");
     CHECK(rk3.nstages == 3 && rk3.gam0[2] == 2.0 / 3.0 && rk3.stage_name[2] == "2");
+  }
+  // ---- task qualifiers, labels, member-function tasks, iterating sublists
+  {
+    struct Counter {
+      int n = 0;
+      TaskStatus bump(int by) {
+        n += by;
+        return TaskStatus::complete;
+      }
+    } cnt;
+    TaskList tl;
+    const TaskID none(0);
+    auto a = tl.AddTask(none, TF(&Counter::bump), &cnt, 2);                      // labelled member function
+    auto b = tl.AddTask(TaskQualifier::once_per_region, a, "label", [&]() { return cnt.bump(1); });
+    // a sublist that runs at least twice and stops when its completion task says so
+    auto [sub, sid] = tl.AddSublist(b, {2, 10});
+    int rounds = 0;
+    auto s1 = sub.AddTask(none, [&]() {
+      ++rounds;
+      return TaskStatus::complete;
+    });
+    sub.AddTask(TaskQualifier::completion, s1, [&]() { return rounds < 5 ? TaskStatus::iterate : TaskStatus::complete; });
+    int after = 0;
+    tl.AddTask(sid, [&]() {
+      after = rounds;
+      return TaskStatus::complete;
+    });
+    TaskCollection tc;
+    tc.AddRegion(1)[0] = std::move(tl);
+    CHECK(tc.Execute() == TaskListStatus::complete);
+    CHECK(cnt.n == 3 && rounds == 5 && after == 5);
+    // the iteration cap ends a sublist whose completion task keeps asking
+    TaskList tl2;
+    auto [sub2, sid2] = tl2.AddSublist(none, {1, 3});
+    int r2 = 0;
+    sub2.AddTask(TaskQualifier::completion, none, [&]() {
+      ++r2;
+      return TaskStatus::iterate;
+    });
+    TaskCollection tc2;
+    tc2.AddRegion(1)[0] = std::move(tl2);
+    CHECK(tc2.Execute() == TaskListStatus::complete && r2 == 3);
+  }
+  // ---- variable-name types, pack indices, pack descriptors, element bounds
+  {
+    const int i0 = vec3().idx, i4 = vec3(4).idx, i12 = vec3(1, 2).idx;
+    CHECK(i0 == 0 && i4 == 4 && i12 == 5 && vec3::size() == 6 && vec3::ndim() == 2);
+    CHECK(scal::size() == 1 && !scal::regex() && variable_names::any::regex());
+    PackIdx pi(3);
+    CHECK((pi + 2).VariableIdx() == 3 && (2 + pi).Offset() == 2);
+    const auto d = MakePackDescriptor<scal, vec3>(static_cast<StateDescriptor *>(nullptr),
+                                                  std::vector<MetadataFlag>{Metadata::Independent},
+                                                  std::set<PDOpt>{PDOpt::WithFluxes});
+    CHECK(d.spec().names.size() == 2 && d.spec().names[1] == "vec3" && d.spec().with_fluxes);
+    CHECK(d.spec().flags.size() == 1 && d.spec().flags[0] == Metadata::Independent);
+    auto dn = MakePackDescriptor(static_cast<StateDescriptor *>(nullptr), std::vector<std::string>{"a", "b.*"},
+                                 std::vector<bool>{false, true});
+    CHECK(dn.GetMap()["b.*"].VariableIdx() == 1 && dn.spec().regex[1] && !dn.spec().with_fluxes);
+    bool threw = false;
+    try {
+      MakePackDescriptor(static_cast<StateDescriptor *>(nullptr), std::vector<std::string>{"a"}, {}, {PDOpt::Coarse});
+    } catch (std::exception &) {
+      threw = true;
+    }
+    CHECK(threw);
+    IndexShape sh(8, 8, 8, 2);
+    using TE = TopologicalElement;
+    CHECK(sh.GetBoundsI(IndexDomain::interior).e == 9 && sh.GetBoundsI(IndexDomain::interior, TE::F1).e == 10);
+    CHECK(sh.GetBoundsJ(IndexDomain::interior, TE::F1).e == 9 && sh.GetBoundsK(IndexDomain::interior, TE::F3).e == 10);
+    CHECK(sh.GetBoundsI(IndexDomain::entire).e == 11);
+    CHECK(static_cast<int>(TE::F2) % 3 == 1 && static_cast<int>(TE::F3) % 3 == 2 && static_cast<int>(TE::CC) % 3 == 0);
+    // coordinates of cells and faces (uniform_cartesian.hpp:166-193)
+    const double x0[3] = {0.25, 0.5, 0.0}, dx[3] = {0.125, 0.25, 0.5};
+    UniformCartesian c(x0, dx, 2);
+    const double xc1 = c.X<1, TE::CC>(2), xf1 = c.X<1, TE::F1>(2);
+    const double x2 = c.X<2, TE::F1>(3), x3 = c.X<3, TE::F3>(0, 0, 0);
+    CHECK(xc1 == 0.25 + 0.5 * 0.125 && xf1 == 0.25);
+    CHECK(x2 == 0.5 + 1.5 * 0.25 && x3 == -1.0);
+    // a face field registers; a face field that fills ghosts is refused
+    StateDescriptor pkg("faces");
+    CHECK(pkg.AddField("D", Metadata({Metadata::Face, Metadata::OneCopy})));
+    threw = false;
+    try {
+      pkg.AddField("E", Metadata({Metadata::Face, Metadata::FillGhost}));
+    } catch (std::exception &) {
+      threw = true;
+    }
+    CHECK(threw);
   }
   std::printf(failures ? "FAILED\n" : "ok\n");
   return failures ? 1 : 0;

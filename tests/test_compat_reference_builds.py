@@ -1,6 +1,9 @@
-"""The reference's own Burgers benchmark application (benchmarks/burgers: package,
-driver, problem generator, main) compiles and links against the package-facing
-compatibility layer and libparthenon_gb300.so without a changed line.
+"""The reference's own applications compile and link against the package-facing
+compatibility layer and libparthenon_gb300.so without a changed line: the Burgers
+benchmark (benchmarks/burgers: package, driver, problem generator, main) and the
+geometric-multigrid Poisson example (example/poisson_gmg: its PoissonEquation on
+SparsePacks and face fields, MGSolver / BiCGSTABSolver on that equation, the driver's
+task list).
 
 The reference sources are read where they lie when they are available (this is the one
 test that reads them); the test is skipped elsewhere. Nothing is copied into the
@@ -15,6 +18,7 @@ from compat_build import compile_objects, link
 
 REFERENCE = os.environ.get("PARTHENON_REFERENCE_DIR", "/root/reference")
 BURGERS = os.path.join(REFERENCE, "benchmarks", "burgers")
+POISSON = os.path.join(REFERENCE, "example", "poisson_gmg")
 
 
 @pytest.mark.skipif(not os.path.isdir(BURGERS), reason="reference sources not available here")
@@ -23,4 +27,13 @@ def test_reference_burgers_app_builds_unchanged():
             ("burgers_package.cpp", "burgers_driver.cpp", "parthenon_app_inputs.cpp", "main.cpp")]
     objs = compile_objects(srcs, "refburgers", include=(BURGERS,))
     exe = link(objs, "reference_burgers_app")
+    assert os.path.getsize(exe) > 0
+
+
+@pytest.mark.skipif(not os.path.isdir(POISSON), reason="reference sources not available here")
+def test_reference_poisson_gmg_app_builds_unchanged():
+    srcs = [os.path.join(POISSON, f) for f in
+            ("poisson_package.cpp", "poisson_driver.cpp", "parthenon_app_inputs.cpp", "main.cpp")]
+    objs = compile_objects(srcs, "refpoisson", include=(POISSON,))
+    exe = link(objs, "reference_poisson_app")
     assert os.path.getsize(exe) > 0
