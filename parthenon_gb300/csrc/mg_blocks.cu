@@ -103,21 +103,47 @@ __device__ __forceinline__ int64_t cell_of(const Dims &d, int slot, int k, int j
   return ((int64_t)slot * d.N[2] + k) * ((int64_t)d.N[1] * d.N[0]) + (int64_t)j * d.N[0] + i;
 }
 
+// log2 of a power of two, else -1
+__device__ __forceinline__ int pow2_log(int v) { return v > 0 && (v & (v - 1)) == 0 ? __ffs(v) - 1 : -1; }
+
+// Flat index e over boxes of n0 x n1 x n2 cells -> (box, k, j, i), i fastest. Block
+// extents are powers of two on every mesh of this path, and then the split is shifts and
+// masks; the integer divisions it replaces were a third of the instructions of the
+// FP32 grid kernels. The branch is uniform across the launch.
+struct CellSplit {
+  int n0, n1, per, l0, l1, lp;
+  __device__ __forceinline__ CellSplit(int a, int b, int c)
+      : n0(a), n1(b), per(a * b * c), l0(pow2_log(a)), l1(pow2_log(b)), lp(pow2_log(a * b * c)) {}
+  __device__ __forceinline__ void operator()(int e, int &q, int &k, int &j, int &i) const {
+    if ((l0 | l1 | lp) >= 0) {
+      q = e >> lp;
+      const int c = e & (per - 1);
+      i = c & (n0 - 1);
+      const int r = c >> l0;
+      j = r & (n1 - 1);
+      k = r >> l1;
+    } else {
+      q = e / per;
+      const int c = e - q * per;
+      const int r = c / n0;
+      i = c - r * n0;
+      k = r / n1;
+      j = r - k * n1;
+    }
+  }
+};
+
 // Every interior cell of the listed blocks (list == null: slots 0 .. n-1), consecutive
 // threads on consecutive i; f gets (position in the list, slot, k, j, i). The host keeps
 // cells x blocks below 2^31.
 template <class F>
 __device__ __forceinline__ void for_interior(const int *__restrict__ list, int n, const Dims &d, F &&f) {
-  const int n0 = d.nx[0], n1 = d.nx[1], ng = d.ng;
-  const int per = n0 * n1 * d.nx[2];
-  const int total = per * n;
+  const int ng = d.ng;
+  const CellSplit sp(d.nx[0], d.nx[1], d.nx[2]);
+  const int total = sp.per * n;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const int q = e / per;
-    const int c = e - q * per;
-    const int r = c / n0;
-    const int i = c - r * n0;
-    const int k = r / n1;
-    const int j = r - k * n1;
+    int q, k, j, i;
+    sp(e, q, k, j, i);
     f(q, list ? list[q] : q, k + ng, j + ng, i + ng);
   }
 }
@@ -481,13 +507,13 @@ template <class TC, class TP>
 __global__ void __launch_bounds__(256) k_mg_restrict(StoreView<TC> cs, StoreView<TP> ps, const MgXfer *__restrict__ x,
                                                      int n, const DevBlockGeom *__restrict__ cgeom) {
   pdl_enter();
-  const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
-  const int per = h0 * h1 * h2, total = per * n;
+  const CellSplit sp(max(1, cs.d.nx[0] / 2), max(1, cs.d.nx[1] / 2), max(1, cs.d.nx[2] / 2));
+  const int total = sp.per * n;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const int q = e / per;
-    const int r = e - q * per;
+    int q, ck, cj, ci;
+    sp(e, q, ck, cj, ci);
     const MgXfer t = x[q];
-    restrict_cell(cs, ps, t, cgeom[t.child].vol, r % h0, (r / h0) % h1, r / (h0 * h1));
+    restrict_cell(cs, ps, t, cgeom[t.child].vol, ci, cj, ck);
   }
 }
 
@@ -497,13 +523,13 @@ __global__ void __launch_bounds__(256) k_mg_prolong_add(StoreView<TC> cs, StoreV
                                                         const MgXfer *__restrict__ x, int n,
                                                         const DevBlockGeom *__restrict__ cgeom) {
   pdl_enter();
-  const int h0 = max(1, cs.d.nx[0] / 2), h1 = max(1, cs.d.nx[1] / 2), h2 = max(1, cs.d.nx[2] / 2);
-  const int per = h0 * h1 * h2, total = per * n;
+  const CellSplit sp(max(1, cs.d.nx[0] / 2), max(1, cs.d.nx[1] / 2), max(1, cs.d.nx[2] / 2));
+  const int total = sp.per * n;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const int q = e / per;
-    const int r = e - q * per;
+    int q, ck, cj, ci;
+    sp(e, q, ck, cj, ci);
     const MgXfer t = x[q];
-    prolong_add_cell<kFast>(cs, ps, t, cgeom + t.child, r % h0, (r / h0) % h1, r / (h0 * h1));
+    prolong_add_cell<kFast>(cs, ps, t, cgeom + t.child, ci, cj, ck);
   }
 }
 
