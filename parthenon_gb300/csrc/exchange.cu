@@ -634,6 +634,7 @@ __global__ void __launch_bounds__(256) k_flux_correct(const DevFluxCorr *__restr
 __global__ void __launch_bounds__(128) k_copy_f32(const DevPair *__restrict__ pairs,
                                                   const DevWork *__restrict__ work, Dims d,
                                                   float *__restrict__ fine, float *__restrict__ coarse) {
+  pdl_enter();
   const DevWork w = work[blockIdx.x];
   const DevPair p = pairs[w.item];
   for_work_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], [&](int k, int j, int i) {
@@ -650,6 +651,7 @@ __global__ void __launch_bounds__(128) k_copy_f32(const DevPair *__restrict__ pa
 __global__ void __launch_bounds__(256) k_restrict_f32(const DevRegion *__restrict__ regs,
                                                       const DevWork *__restrict__ work, int nwork, Dims d,
                                                       const float *__restrict__ fine, float *__restrict__ coarse) {
+  pdl_enter();
   const int wi = warp_item();
   if (wi >= nwork) return;
   const DevWork w = work[wi];
@@ -668,6 +670,7 @@ __global__ void __launch_bounds__(256) k_restrict_f32(const DevRegion *__restric
 __global__ void __launch_bounds__(256) k_prolong_f32(const DevRegion *__restrict__ regs,
                                                      const DevWork *__restrict__ work, int nwork, Dims d,
                                                      float *__restrict__ fine, const float *__restrict__ coarse) {
+  pdl_enter();
   const int wi = warp_item();
   if (wi >= nwork) return;
   const DevWork w = work[wi];
@@ -740,18 +743,23 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
   return kOk;
 }
 
+// Launched with programmatic dependent launch, as the FP32 V-cycle's own kernels are:
+// each waits for its predecessor before any access (pdl_enter), so the chain restrict ->
+// copy -> restrict -> prolong keeps its order while the launch latencies overlap.
 int exchange_grid_f32(GridTables &t, float *fine, float *coarse, cudaStream_t s) {
   if (!fine || (t.multilevel && !coarse)) return fail(kErrInvalid, "null field pointer");
+  const unsigned iw = 32 * kItemWarps;
   if (t.multilevel && t.nrs_work)
-    k_restrict_f32<<<warp_item_grid(t.nrs_work), 32 * kItemWarps, 0, s>>>(t.rs, t.rs_work, t.nrs_work, t.dims,
-                                                                        fine, coarse);
-  if (t.ncopy_work) k_copy_f32<<<t.ncopy_work, 128, 0, s>>>(t.pairs, t.copy_work, t.dims, fine, coarse);
+    PGB_TRY(launch_pdl(k_restrict_f32, warp_item_grid(t.nrs_work), iw, s, t.rs, t.rs_work, t.nrs_work, t.dims,
+                       fine, coarse));
+  if (t.ncopy_work) PGB_TRY(launch_pdl(k_copy_f32, (unsigned)t.ncopy_work, 128u, s, t.pairs, t.copy_work, t.dims,
+                                       fine, coarse));
   if (t.multilevel && t.nrr_work)
-    k_restrict_f32<<<warp_item_grid(t.nrr_work), 32 * kItemWarps, 0, s>>>(t.rr, t.rr_work, t.nrr_work, t.dims,
-                                                                        fine, coarse);
+    PGB_TRY(launch_pdl(k_restrict_f32, warp_item_grid(t.nrr_work), iw, s, t.rr, t.rr_work, t.nrr_work, t.dims,
+                       fine, coarse));
   if (t.multilevel && t.npro_work)
-    k_prolong_f32<<<warp_item_grid(t.npro_work), 32 * kItemWarps, 0, s>>>(t.pro, t.pro_work, t.npro_work, t.dims,
-                                                                        fine, coarse);
+    PGB_TRY(launch_pdl(k_prolong_f32, warp_item_grid(t.npro_work), iw, s, t.pro, t.pro_work, t.npro_work, t.dims,
+                       fine, coarse));
   PGB_CUDA(cudaGetLastError());
   return kOk;
 }

@@ -481,6 +481,48 @@ __global__ void __launch_bounds__(256) k_mg_fas(StoreView<T> s, const int *__res
   });
 }
 
+// The FAS start of a level fused with the first Jacobi sweep of its pre-smoothing, on a
+// grid that reads its face neighbours directly: u0 = u, rhs = A u + res_err (internal
+// blocks), then temp = the sweep of u against that rhs. The sweep reads u and the cell's
+// own rhs, both final when the cell's thread reaches it, so the values are those of the
+// two separate launches.
+template <bool kFast, class T>
+__global__ void __launch_bounds__(256) k_mg_fas_jacobi(StoreView<T> s, const int *__restrict__ list, int n,
+                                                       int nint, const int *__restrict__ nbr, MgCoef cf, MgOp o,
+                                                       MgSweep sw, FaceD<T> fd) {
+  pdl_enter();
+  for_interior(list, n, s.d, [&](int q, int b, int k, int j, int i) {
+    const int *nb = nbr ? nbr + 6 * q : nullptr;
+    fas_cell<kFast>(s, q < nint, nb, cf, o, fd, b, k, j, i);
+    jacobi_cell<kFast>(s.u, s.rhs, s.temp, s.d, nb, cf, o, sw, fd, b, k, j, i);
+  });
+}
+
+// A level's residual fused with its restriction: one thread per parent cell forms the
+// residual of its eight fine cells (res = rhs - A u) and restricts u and res_err into
+// the parent. MgXfer::pad holds the child's position in the grid's block list (its
+// face-neighbour row on a grid read directly).
+template <bool kFast, class TC, class TP>
+__global__ void __launch_bounds__(256) k_mg_residual_restrict(StoreView<TC> cs, StoreView<TP> ps,
+                                                              const MgXfer *__restrict__ x, int n,
+                                                              const int *__restrict__ nbr, MgCoef cf, MgOp o,
+                                                              FaceD<TC> fd, const DevBlockGeom *__restrict__ cgeom) {
+  pdl_enter();
+  const CellSplit sp(cs.d.nx[0] / 2, cs.d.nx[1] / 2, cs.d.nx[2] / 2);
+  const int total = sp.per * n, ng = cs.d.ng;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    int q, ck, cj, ci;
+    sp(e, q, ck, cj, ci);
+    const MgXfer t = x[q];
+    const int *nb = nbr ? nbr + 6 * t.pad : nullptr;
+#pragma unroll
+    for (int o8 = 0; o8 < 8; ++o8)
+      residual_cell<kFast>(cs, nb, cf, o, fd, t.child, 2 * ck + ng + (o8 >> 2), 2 * cj + ng + ((o8 >> 1) & 1),
+                           2 * ci + ng + (o8 & 1));
+    restrict_cell(cs, ps, t, cgeom[t.child].vol, ci, cj, ck);
+  }
+}
+
 // CopyData on the interiors of the listed blocks
 template <class T>
 __global__ void __launch_bounds__(256) k_mg_copy(T *__restrict__ dst, const T *__restrict__ src,
@@ -1363,7 +1405,11 @@ int mg_build(pgb_mg *g) {
         const size_t q0 = 6 * (size_t)(it - PG.fine_h.begin());
         for (int q = 0; q < 6; ++q) x.pnb[q] = PG.nbr_h[q0 + q];
       }
-      x.pad = 0;
+      {
+        const auto it = std::find(G.fine_h.begin(), G.fine_h.end(), x.child);
+        if (it == G.fine_h.end()) return fail(kErrInvalid, "child outside its grid's block list");
+        x.pad = (int32_t)(it - G.fine_h.begin());  // the child's row in the grid's lists
+      }
       G.xfer_h.push_back(x);
     }
   }
@@ -1511,8 +1557,10 @@ struct VCycle {
     return (int64_t)d.nx[0] * d.nx[1] * d.nx[2];
   }
 
+  // Sweeps first .. stages - 1 of the smoother (first = 1: sweep 0, u into temp, was
+  // fused into the level's FAS launch)
   template <class T>
-  int smooth(int L, int stages) {
+  int smooth(int L, int stages, int first = 0) {
     if (stages == 0) return kOk;
     pgb_mg::Grid &G = g->grids.at(L);
     pgb_mg::Store &S = g->store_of(L);
@@ -1524,8 +1572,8 @@ struct VCycle {
     // exchange of the second sweep then runs on temp, whose coarser leaves must hold
     // their u.
     if (stages >= 2 && nc) PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nc * cl), 256, s, v.temp, v.u, G.coarse, nc, v.d));
-    T *src = v.u, *dst = v.temp;
-    for (int st = 0; st < stages; ++st) {
+    T *src = first % 2 ? v.temp : v.u, *dst = first % 2 ? v.u : v.temp;
+    for (int st = first; st < stages; ++st) {
       int rc = G.halofree ? kOk : exch(g, L, src, s);
       if (rc) return rc;
       MgSweep sw;
@@ -1563,6 +1611,25 @@ struct VCycle {
     return kOk;
   }
 
+  // the level's residual and its restriction into the next coarser grid: one fused
+  // launch when every block has at least two cells along each direction
+  template <class T, class TP>
+  int residual_restrict(int L) {
+    pgb_mg::Grid &G = g->grids.at(L);
+    const StoreView<T> v = g->store_of(L).template view<T>();
+    const int nf = (int)G.fine_h.size(), nx = (int)G.xfer_h.size();
+    if (v.d.nx[0] >= 2 && v.d.nx[1] >= 2 && v.d.nx[2] >= 2 && nx == nf) {
+      PGB_TRY(launch_pdl(k_mg_residual_restrict<kFast, T, TP>, grid_for(nx * cells(L) / 8), 256, s, v,
+                         g->store_of(L - 1).template view<TP>(), G.xfer, nx, G.nb(), G.coef, o,
+                         g->store_of(L).template fd<T>(), G.tab.geom));
+      PGB_CUDA(cudaGetLastError());
+      return kOk;
+    }
+    PGB_TRY(launch_pdl(k_mg_residual<kFast, T>, grid_for(nf * cells(L)), 256, s, v, G.fine, nf, G.nb(), G.coef, o,
+                       g->store_of(L).template fd<T>()));
+    return restrict_down<T, TP>(L);
+  }
+
   template <class T>
   int down(int L) {
     pgb_mg::Grid &G = g->grids.at(L);
@@ -1570,21 +1637,31 @@ struct VCycle {
     const int nf = (int)G.fine_h.size();
     const int64_t cl = cells(L);
     int rc;
+    int first = 0;
     if (L < g->lmax) {
-      // FAS: exchange, u0 = u, rhs = A u + res_err on internal blocks
+      // FAS: exchange, u0 = u, rhs = A u + res_err on internal blocks; on a grid read
+      // directly, fused with the first sweep of the smoother
       if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
-      PGB_TRY(launch_pdl(k_mg_fas<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nint, G.nb(), G.coef, o,
-                         g->store_of(L).template fd<T>()));
+      if (G.halofree && g->cfg.stages > 0 && G.coarse_h.empty()) {
+        MgSweep sw;
+        sw.w = srj_weight(g->cfg, 0);
+        sw.omw = 1.0 - sw.w;
+        sw.wd = sw.w / G.coef.den;
+        PGB_TRY(launch_pdl(k_mg_fas_jacobi<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nint, G.nb(),
+                           G.coef, o, sw, g->store_of(L).template fd<T>()));
+        first = 1;
+      } else {
+        PGB_TRY(launch_pdl(k_mg_fas<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nint, G.nb(), G.coef, o,
+                           g->store_of(L).template fd<T>()));
+      }
     } else {
       PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nf * cl), 256, s, v.u0, v.u, G.fine, nf, v.d));
     }
-    if ((rc = smooth<T>(L, g->cfg.stages))) return rc;
+    if ((rc = smooth<T>(L, g->cfg.stages, first))) return rc;
     if (L > g->lmin) {
       if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
-      PGB_TRY(launch_pdl(k_mg_residual<kFast, T>, grid_for(nf * cl), 256, s, v, G.fine, nf, G.nb(), G.coef, o,
-                         g->store_of(L).template fd<T>()));
-      if constexpr (kFast) rc = dbl(L - 1) ? restrict_down<T, double>(L) : restrict_down<T, float>(L);
-      else rc = restrict_down<T, double>(L);
+      if constexpr (kFast) rc = dbl(L - 1) ? residual_restrict<T, double>(L) : residual_restrict<T, float>(L);
+      else rc = residual_restrict<T, double>(L);
       if (rc) return rc;
     } else {
       for (int c = 0; c < g->cfg.coarse_sweeps; ++c)
