@@ -648,6 +648,51 @@ __global__ void __launch_bounds__(128) k_copy_f32(const DevPair *__restrict__ pa
   });
 }
 
+// The first two steps of the FP32 exchange in one launch: CTAs [0, ncopy) run the copy
+// work items, the rest run the restriction of each fine block's interior into its
+// coarse buffer (the `rs` regions, one warp per item). The copies whose source is a
+// sender's coarse buffer -- a fine block sending to a coarser neighbour, the cells that
+// restriction fills -- restrict the sender's interior themselves (the same mean of the
+// eight fine cells), so the two parts have no order between them.
+constexpr int kCopyRsThreads = 128;
+__global__ void __launch_bounds__(kCopyRsThreads) k_copy_rs_f32(const DevPair *__restrict__ pairs,
+                                                               const DevWork *__restrict__ work, int ncopy,
+                                                               const DevRegion *__restrict__ regs,
+                                                               const DevWork *__restrict__ rwork, int nrwork, Dims d,
+                                                               float *__restrict__ fine, float *__restrict__ coarse) {
+  pdl_enter();
+  const int ng = d.ng;
+  const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
+  auto mean8 = [&](const float *f) {
+    return 0.125f * (((f[0] + f[sj]) + (f[1] + f[sj + 1])) + ((f[sk] + f[sk + sj]) + (f[sk + 1] + f[sk + sj + 1])));
+  };
+  if ((int)blockIdx.x < ncopy) {
+    const DevWork w = work[blockIdx.x];
+    const DevPair p = pairs[w.item];
+    for_work_rows(w.row0, w.nrows, p.src.n[0], p.src.n[1], [&](int k, int j, int i) {
+      const int dk = p.dst.lo[2] + k, dj = p.dst.lo[1] + j, di = p.dst.lo[0] + i;
+      if (!p.full_mask && !mask_active(p.mask, p.dst, dk, dj, di)) return;
+      const int ck = p.src.lo[2] + k, cj = p.src.lo[1] + j, ci = p.src.lo[0] + i;
+      const float v = p.src_coarse ? mean8(fine + fine_index(d, 1, p.src_block, 0, (ck - ng) * 2 + ng,
+                                                              (cj - ng) * 2 + ng, (ci - ng) * 2 + ng))
+                                   : fine[fine_index(d, 1, p.src_block, 0, ck, cj, ci)];
+      if (p.dst_coarse) coarse[coarse_index(d, 1, p.dst_block, 0, dk, dj, di)] = v;
+      else fine[fine_index(d, 1, p.dst_block, 0, dk, dj, di)] = v;
+    });
+    return;
+  }
+  const int wi = (int)(blockIdx.x - ncopy) * (kCopyRsThreads / 32) + (int)(threadIdx.x >> 5);
+  if (wi >= nrwork) return;
+  const DevWork w = rwork[wi];
+  const DevRegion r = regs[w.item];
+  for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
+    const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
+    if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
+    coarse[coarse_index(d, 1, r.block, 0, ck, cj, ci)] =
+        mean8(fine + fine_index(d, 1, r.block, 0, (ck - ng) * 2 + ng, (cj - ng) * 2 + ng, (ci - ng) * 2 + ng));
+  });
+}
+
 __global__ void __launch_bounds__(256) k_restrict_f32(const DevRegion *__restrict__ regs,
                                                       const DevWork *__restrict__ work, int nwork, Dims d,
                                                       const float *__restrict__ fine, float *__restrict__ coarse) {
@@ -744,16 +789,20 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
 }
 
 // Launched with programmatic dependent launch, as the FP32 V-cycle's own kernels are:
-// each waits for its predecessor before any access (pdl_enter), so the chain restrict ->
-// copy -> restrict -> prolong keeps its order while the launch latencies overlap.
+// each waits for its predecessor before any access (pdl_enter), so the chain
+// (restrict + copy) -> restrict -> prolong keeps its order while the launch latencies
+// overlap.
 int exchange_grid_f32(GridTables &t, float *fine, float *coarse, cudaStream_t s) {
   if (!fine || (t.multilevel && !coarse)) return fail(kErrInvalid, "null field pointer");
   const unsigned iw = 32 * kItemWarps;
-  if (t.multilevel && t.nrs_work)
-    PGB_TRY(launch_pdl(k_restrict_f32, warp_item_grid(t.nrs_work), iw, s, t.rs, t.rs_work, t.nrs_work, t.dims,
-                       fine, coarse));
-  if (t.ncopy_work) PGB_TRY(launch_pdl(k_copy_f32, (unsigned)t.ncopy_work, 128u, s, t.pairs, t.copy_work, t.dims,
-                                       fine, coarse));
+  if (t.multilevel && t.nrs_work) {
+    const int per = kCopyRsThreads / 32;
+    const unsigned grid = (unsigned)(t.ncopy_work + (t.nrs_work + per - 1) / per);
+    PGB_TRY(launch_pdl(k_copy_rs_f32, grid, (unsigned)kCopyRsThreads, s, t.pairs, t.copy_work, (int)t.ncopy_work,
+                       t.rs, t.rs_work, (int)t.nrs_work, t.dims, fine, coarse));
+  } else if (t.ncopy_work) {
+    PGB_TRY(launch_pdl(k_copy_f32, (unsigned)t.ncopy_work, 128u, s, t.pairs, t.copy_work, t.dims, fine, coarse));
+  }
   if (t.multilevel && t.nrr_work)
     PGB_TRY(launch_pdl(k_restrict_f32, warp_item_grid(t.nrr_work), iw, s, t.rr, t.rr_work, t.nrr_work, t.dims,
                        fine, coarse));

@@ -658,9 +658,10 @@ __device__ __forceinline__ const FaceD<T> &tfd(const TailGrid &g) {
 // every interior cell of one block, the whole CTA
 template <class F>
 __device__ __forceinline__ void for_block(const Dims &d, F &&f) {
-  const int n0 = d.nx[0], n1 = d.nx[1], per = n0 * n1 * d.nx[2];
-  for (int e = threadIdx.x; e < per; e += blockDim.x) {
-    const int r = e / n0, i = e - r * n0, k = r / n1, j = r - k * n1;
+  const CellSplit sp(d.nx[0], d.nx[1], d.nx[2]);
+  for (int e = threadIdx.x; e < sp.per; e += blockDim.x) {
+    int q, k, j, i;
+    sp(e, q, k, j, i);
     f(k + d.ng, j + d.ng, i + d.ng);
   }
 }
@@ -1698,7 +1699,6 @@ struct VCycle {
   // build), or lmin - 1 when fewer than two qualify.
   int tail_top() const {
     int top = g->lmin - 1;
-    if (mixed) return top;  // the FP32 grids' launches are cheaper than their steps on one SM
     for (int L = g->lmin; L <= g->lmax; ++L) {
       const pgb_mg::Grid &G = g->grids.at(L);
       if (G.fine_h.size() != 1 || !G.coarse_h.empty() || !G.halofree) break;
