@@ -280,15 +280,27 @@ __device__ __forceinline__ void fast_op(const Faces<T> &f, const MgCoef &cf, con
 // Jacobi sweep (mg_solver.hpp:222-297): dst = w ratio(rhs - (A src - dg src), dg) + (1 - w) src
 // ---- per-cell steps, shared by the grid kernels below and the one-CTA coarse end
 
+template <bool kFast, class T>
+__device__ __forceinline__ void jacobi_cell_f(const Faces<T> &f, const T *__restrict__ rhs, T *__restrict__ dst,
+                                              const Dims &d, const MgCoef &cf, const MgOp &o, const MgSweep &sw,
+                                              const FaceD<T> &fd, int b, int k, int j, int i);
+
 // Jacobi sweep (mg_solver.hpp:222-297): dst = w ratio(rhs - (A src - dg src), dg) + (1 - w) src
 template <bool kFast, class T>
 __device__ __forceinline__ void jacobi_cell(const T *__restrict__ src, const T *__restrict__ rhs, T *__restrict__ dst,
                                             const Dims &d, const int *__restrict__ nb, const MgCoef &cf,
                                             const MgOp &o, const MgSweep &sw, const FaceD<T> &fd, int b, int k,
                                             int j, int i) {
+  jacobi_cell_f<kFast>(faces(src, d, nb, b, k, j, i), rhs, dst, d, cf, o, sw, fd, b, k, j, i);
+}
+
+// the sweep of one cell from its stencil values f
+template <bool kFast, class T>
+__device__ __forceinline__ void jacobi_cell_f(const Faces<T> &f, const T *__restrict__ rhs, T *__restrict__ dst,
+                                              const Dims &d, const MgCoef &cf, const MgOp &o, const MgSweep &sw,
+                                              const FaceD<T> &fd, int b, int k, int j, int i) {
   const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
   const int64_t c = cell_of(d, b, k, j, i);
-  const Faces<T> f = faces(src, d, nb, b, k, j, i);
   if constexpr (kFast) {
     T off, dg;
     fast_op(f, cf, o, fd, c, sj, sk, off, dg);
@@ -459,6 +471,24 @@ __global__ void __launch_bounds__(256) k_mg_jacobi(const T *__restrict__ src, co
   for_interior(list, n, d, [&](int q, int b, int k, int j, int i) {
     jacobi_cell<kFast>(src, rhs, dst, d, nbr ? nbr + 6 * q : nullptr, cf, o, sw, fd, b, k, j, i);
   });
+}
+
+// The first sweep from a zero initial guess: every value of the stencil is zero (ghosts
+// included -- the exchange of a zero field writes zeros), so no exchange precedes it and
+// the sweep reads only the right-hand side.
+// The coarser leaves of the grid (clist, nc) get dst = 0, their u, which the next sweep's
+// exchange of dst reads.
+template <bool kFast, class T>
+__global__ void __launch_bounds__(256) k_mg_jacobi_zero(const T *__restrict__ rhs, T *__restrict__ dst,
+                                                        const int *__restrict__ list, int n,
+                                                        const int *__restrict__ clist, int nc, Dims d, MgCoef cf,
+                                                        MgOp o, MgSweep sw, FaceD<T> fd) {
+  pdl_enter();
+  const Faces<T> zero{};
+  for_interior(list, n, d, [&](int, int b, int k, int j, int i) {
+    jacobi_cell_f<kFast>(zero, rhs, dst, d, cf, o, sw, fd, b, k, j, i);
+  });
+  if (nc) for_interior(clist, nc, d, [&](int, int b, int k, int j, int i) { dst[cell_of(d, b, k, j, i)] = (T)0; });
 }
 
 template <bool kFast, class T>
@@ -1552,6 +1582,9 @@ struct VCycle {
   cudaStream_t s;
   bool mixed;
   MgOp o;
+  // the finest grid's u is zero on entry, ghosts and the coarser leaves included
+  // (iterative refinement and the preconditioners solve for a correction from zero)
+  bool zero_guess = false;
   bool dbl(int L) const { return !mixed || (L == g->lmin && g->lmin < 0); }
   int64_t cells(int L) const {
     const Dims &d = g->store_of(L).dims;
@@ -1561,7 +1594,7 @@ struct VCycle {
   // Sweeps first .. stages - 1 of the smoother (first = 1: sweep 0, u into temp, was
   // fused into the level's FAS launch)
   template <class T>
-  int smooth(int L, int stages, int first = 0) {
+  int smooth(int L, int stages, int first = 0, bool zero_first = false) {
     if (stages == 0) return kOk;
     pgb_mg::Grid &G = g->grids.at(L);
     pgb_mg::Store &S = g->store_of(L);
@@ -1572,17 +1605,25 @@ struct VCycle {
     // u into temp on every block first and each sweep's result back into u; the
     // exchange of the second sweep then runs on temp, whose coarser leaves must hold
     // their u.
-    if (stages >= 2 && nc) PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nc * cl), 256, s, v.temp, v.u, G.coarse, nc, v.d));
+    const bool zero = zero_first && first == 0;  // the coarser leaves' temp = u = 0 in the first sweep
+    if (stages >= 2 && nc && !zero)
+      PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nc * cl), 256, s, v.temp, v.u, G.coarse, nc, v.d));
     T *src = first % 2 ? v.temp : v.u, *dst = first % 2 ? v.u : v.temp;
     for (int st = first; st < stages; ++st) {
-      int rc = G.halofree ? kOk : exch(g, L, src, s);
-      if (rc) return rc;
       MgSweep sw;
       sw.w = srj_weight(g->cfg, st);
       sw.omw = 1.0 - sw.w;
       sw.wd = sw.w / G.coef.den;
-      PGB_TRY(launch_pdl(k_mg_jacobi<kFast, T>, grid_for(nf * cl), 256, s, src, v.rhs, dst, G.fine, nf, G.nb(), v.d,
-                         G.coef, o, sw, g->store_of(L).template fd<T>()));
+      if (zero_first && st == 0) {
+        PGB_TRY(launch_pdl(k_mg_jacobi_zero<kFast, T>, grid_for(nf * cl), 256, s, (const T *)v.rhs, dst, G.fine, nf,
+                           (const int *)G.coarse, stages >= 2 ? nc : 0, v.d, G.coef, o, sw,
+                           g->store_of(L).template fd<T>()));
+      } else {
+        int rc = G.halofree ? kOk : exch(g, L, src, s);
+        if (rc) return rc;
+        PGB_TRY(launch_pdl(k_mg_jacobi<kFast, T>, grid_for(nf * cl), 256, s, src, v.rhs, dst, G.fine, nf, G.nb(),
+                           v.d, G.coef, o, sw, g->store_of(L).template fd<T>()));
+      }
       std::swap(src, dst);
     }
     if (src != v.u) PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nf * cl), 256, s, v.u, v.temp, G.fine, nf, v.d));
@@ -1658,7 +1699,7 @@ struct VCycle {
     } else {
       PGB_TRY(launch_pdl(k_mg_copy<T>, grid_for(nf * cl), 256, s, v.u0, v.u, G.fine, nf, v.d));
     }
-    if ((rc = smooth<T>(L, g->cfg.stages, first))) return rc;
+    if ((rc = smooth<T>(L, g->cfg.stages, first, zero_guess && L == g->lmax))) return rc;
     if (L > g->lmin) {
       if (!G.halofree && (rc = exch(g, L, v.u, s))) return rc;
       if constexpr (kFast) rc = dbl(L - 1) ? residual_restrict<T, double>(L) : residual_restrict<T, float>(L);
@@ -1798,6 +1839,7 @@ int leaf_residual(pgb_mg *g, bool mixed, cudaStream_t s) {
 template <bool kFast>
 int enqueue_iteration_t(pgb_mg *g, bool mixed, cudaStream_t s) {
   VCycle<kFast> vc{g, s, mixed, MgOp{g->cfg.D, g->cfg.alpha}};
+  vc.zero_guess = mixed;  // the FP32 correction starts from e = 0 (k_mg_leaf_residual)
   int rc = vc.run();
   if (rc) return rc;
   if (mixed) {
@@ -1838,10 +1880,12 @@ int bicg_precond(pgb_mg *g, int mode, const double *src, cudaStream_t s) {
   if (mode == 1) {
     PGB_TRY(launch_pdl(k_bi_in<double>, grid, 256, s, src, S.rhs, S.u, g->nleaf, S.dims));
     VCycle<true> vc{g, s, false, MgOp{g->cfg.D, g->cfg.alpha}};
+    vc.zero_guess = true;  // k_bi_in zeroed u
     return vc.run();
   }
   PGB_TRY(launch_pdl(k_bi_in<float>, grid, 256, s, src, S.rhs32, S.u32, g->nleaf, S.dims));
   VCycle<true> vc{g, s, true, MgOp{g->cfg.D, g->cfg.alpha}};
+  vc.zero_guess = true;  // k_bi_in zeroed u32
   PGB_TRY(vc.run());
   return launch_pdl(k_bi_out32, grid, 256, s, (const float *)S.u32, S.u, g->nleaf, S.dims);
 }
