@@ -419,6 +419,8 @@ def leg_summary(name, r):
                 "mixed_over_fp64": rnd(r["time_ratio_mixed_over_fp64"], 3),
                 "mixed_vs_fp64_rel_err": rnd(r["mixed_vs_fp64_rel_err"], 2),
                 "bicgstab_mg_fp32_ms": rnd(1e3 * r["bicgstab_mg_fp32"]["seconds"]),
+                "blocks_fp64_ms": rnd(1e3 * r["blocks"]["fp64"]["seconds"]),
+                "blocks_mixed_over_fp64": rnd(r["blocks"]["time_ratio_mixed_over_fp64"], 3),
                 "workload": "poisson3d-128^3-periodic-vcycle-to-8^3-jacobi2/3-2+2"}
     keep = {"fp64_ms": rnd(1e3 * r["seconds"]), "fp64_vcycles": r["vcycles"],
             "mixed_ms": rnd(1e3 * r["mixed"]["seconds"]), "mixed_iterations": r["mixed"]["iterations"],
@@ -479,7 +481,50 @@ def gmg_bench(torch):
                                       "vs_fp64_vcycle_rel_err": float((x - a).abs().max() / a.abs().max())}
     res["config"] = {"n": GMG_N, "levels": GMG_COARSEN + 1, "smoother": "weighted Jacobi 2/3, 2+2",
                      "coarse": "+16 smoother passes, FP64", "rhs": "32 Gaussians sigma 0.03 seed 4, mean removed"}
+    res["blocks"] = gmg_c4_blocks(torch, pg, a)
     return res
+
+
+def gmg_c4_blocks(torch, pg, flat_fp64):
+    """C4 through the block-structured solver (pgb_mg_*, the MGSolver path packages
+    call): the same problem on the 128^3 periodic mesh in 16^3 blocks, grids down to one
+    8^3 block (4 coarsenings), weighted Jacobi 2/3 with 2+2 sweeps and 16 more passes on
+    the coarsest grid. FP64 V-cycles vs the FP32 V-cycle inside FP64 refinement, to a
+    1e-10 relative residual; the FP64 solution against the flat solver's."""
+    mesh = pg.Mesh((GMG_N,) * 3, (16,) * 3, 2)
+    rhs_h = pg.problems.poisson_rhs_blocks(mesh, ngauss=32, sigma=0.03, seed=4)
+    rhs = torch.tensor(rhs_h, device="cuda")
+    mg = pg.CompositeMultigrid(mesh, stages=2, jacobi=True, weight=2.0 / 3.0, coarse_sweeps=16,
+                               max_coarsenings=GMG_COARSEN, alpha=0.0)
+    s = torch.cuda.Stream()
+    out, sols = {}, {}
+    for mixed in (False, True):
+        best = None
+        for rep in range(3):
+            u = torch.zeros_like(rhs)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            cyc, rel = mg.solve(u, rhs, tol=1e-10, relative=True, max_cycles=400, mixed=mixed, stream=s)
+            s.synchronize()
+            dt = time.perf_counter() - t0
+            if rep > 0 and (best is None or dt < best[0]):
+                best = (dt, cyc, rel)
+        sols[mixed] = u
+        out["mixed" if mixed else "fp64"] = {"seconds": best[0], "vcycles": best[1], "rel_residual": best[2]}
+    out["time_ratio_mixed_over_fp64"] = out["mixed"]["seconds"] / out["fp64"]["seconds"]
+    # the block solution on the global grid, against the flat solver's (means removed)
+    locs, geom = mesh.block_info()
+    ng, b = 2, 16
+    glob = torch.zeros((GMG_N,) * 3, dtype=torch.float64)
+    ub = sols[False].cpu()
+    for q in range(locs.shape[0]):
+        lx = [int(x) for x in locs[q, 1:4]]
+        glob[lx[2] * b:(lx[2] + 1) * b, lx[1] * b:(lx[1] + 1) * b, lx[0] * b:(lx[0] + 1) * b] = \
+            ub[q, ng:ng + b, ng:ng + b, ng:ng + b]
+    glob = glob - glob.mean()
+    out["fp64_vs_flat_solver_rel_err"] = float((glob - flat_fp64).abs().max() / flat_fp64.abs().max())
+    out["config"] = {"mesh": "128^3 periodic, 16^3 blocks (512)", "grids": mg.ngrids, "levels": [mg.lmin, mg.lmax]}
+    return out
 
 
 SMR_ROOT, SMR_BLOCK, SMR_NG, SMR_NSCALARS, SMR_CYCLES = 128, 16, 4, 4, 20
