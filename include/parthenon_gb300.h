@@ -141,8 +141,11 @@ int pgb_flux_correct(pgb_mesh *mesh, double *flux, int32_t ncomp, void *stream);
 
 /* One RK stage: fluxes from u_in, flux divergence, u_out = (w_in u_in + w_base u_base)
  * + beta * dt * dudt on the interior. dt is a device scalar (dt[0]). Uniform meshes use the
- * fused path (dudt is scratch of the field's size); multilevel meshes store fluxes in
- * `flux` (3x the field's size), correct them at fine/coarse faces and then update.
+ * fused path (dudt is scratch of the field's size); on multilevel meshes the blocks with a
+ * fine/coarse face store fluxes in `flux` (3x the field's size), which are corrected at
+ * those faces before the update, and the other blocks take the fused path with `dudt`
+ * as scratch (dudt NULL: the flux array serves; on a mesh with sparse variables every
+ * block then stores fluxes).
  * Replaces CalculateFluxes (benchmarks/burgers/burgers_package.cpp:202-404,
  * example/advection/advection_package.cpp:499-647), FluxDivergence
  * (src/interface/update.cpp:62-85), AverageIndependentData and UpdateIndependentData

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     const int t0 = (int)(ln % n_fast);
     const int64_t r = ln / n_fast;
     const int t1 = (int)(r % n_slow);
-    const int b = (int)(r / n_slow);
+    const int b = a.blist ? a.blist[r / n_slow] : (int)(r / n_slow);
     int i0, j0, k0;
     if (D == 0) {
       i0 = ng; j0 = ng + t0; k0 = ng + t1;
@@ -220,7 +220,7 @@ int launch_burgers_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
       if (attr != cudaSuccess) return;
     }
     const int pick = g_tune_force >= 0 ? g_tune_force
-                                       : tuned_choice(burgers_tune_key(NC, n, store_flux, a.nblocks), kBurgersGridDefault);
+                                       : tuned_choice(burgers_tune_key(NC, n, a.tune_ml != 0, a.tune_nblocks), kBurgersGridDefault);
     const int64_t grid = std::min<int64_t>(groups, (int64_t)nsm * kBurgersGridMult[pick]);
     kern<<<(unsigned)grid, 32 * NC, smem, s>>>(a, groups);
   };

@@ -131,6 +131,9 @@ int stage_impl(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const
   a.geom = t.geom;
   a.d = t.dims;
   a.nblocks = t.nblocks;
+  a.blist = nullptr;
+  a.tune_nblocks = t.nblocks;
+  a.tune_ml = t.multilevel ? 1 : 0;
   a.recon = p->recon;
   a.ncomp = ncomp;
   for (int q = 0; q < 3; ++q) a.vel[q] = p->vel[q];
@@ -145,14 +148,37 @@ int stage_impl(pgb_mesh *m, const pgb_stage_params *p, const double *u_in, const
   int rc;
   auto launch = p->exact ? exact::launch_stage : fast::launch_stage;
   auto divup = p->exact ? exact::launch_div_update : fast::launch_div_update;
-  rc = launch(a, ncomp, p->physics, ml, s);
-  if (rc == kErrUnsupported) return fail(rc, "no stencil kernel for this component count");
-  if (rc != kOk) return check_cuda(cudaGetLastError(), "stencil launch");
-  if (ml) {
+  auto checked = [&](int r, const char *what) {
+    if (r == kErrUnsupported) return fail(r, "no kernel for this component count");
+    if (r != kOk) return check_cuda(cudaGetLastError(), what);
+    return kOk;
+  };
+  if (!ml) return checked(launch(a, ncomp, p->physics, false, s), "stencil launch");
+  // Multilevel: the blocks without a fine/coarse face take the uniform path (per-
+  // direction increments in a scratch array, the update fused into the last sweep);
+  // then the blocks on such faces store face fluxes, the fine/coarse faces are corrected
+  // and their divergence updates them. Both paths round the update the same way (exact
+  // build: bitwise the same). The scratch is dudt, or else the flux array: the two parts
+  // run one after the other and the second rewrites every flux it reads. With sparse
+  // variables and no dudt every block stores fluxes, as the zeroed flux slices of
+  // unallocated variables must stay zero.
+  const bool split = t.nplain > 0 && (dudt != nullptr || sp == nullptr);
+  if (split) {
+    StageArgs ap = a;
+    ap.nblocks = t.nplain;
+    ap.blist = t.plain;
+    ap.dudt = dudt ? dudt : flux;
+    if ((rc = checked(launch(ap, ncomp, p->physics, false, s), "stencil launch"))) return rc;
+  }
+  StageArgs af = a;
+  if (split) {
+    af.nblocks = t.nfcb;
+    af.blist = t.fcb;
+  }
+  if (af.nblocks > 0) {
+    if ((rc = checked(launch(af, ncomp, p->physics, true, s), "stencil launch"))) return rc;
     if ((rc = flux_correct_grid(t, flux, ncomp, s, sp))) return rc;
-    rc = divup(a, ncomp, s);
-    if (rc == kErrUnsupported) return fail(rc, "no update kernel for this component count");
-    if (rc != kOk) return check_cuda(cudaGetLastError(), "update launch");
+    if ((rc = checked(divup(af, ncomp, s), "update launch"))) return rc;
   }
   return kOk;
 }
@@ -514,13 +540,10 @@ int pgb_run_host_dt(pgb_mesh *m, const pgb_stage_params *p, const double *host_i
     if ((rc = guard(cudaMalloc(&w.base, n * 8), "malloc")) || (rc = guard(cudaMalloc(&w.stage, n * 8), "malloc")) ||
         (rc = guard(cudaMalloc(&w.dt, 3 * sizeof(double)), "malloc")))
       return rc;
-    if (ml) {
-      if ((rc = guard(cudaMalloc(&w.flux, 3 * n * 8), "malloc")) || (rc = guard(cudaMalloc(&w.cb, nc * 8), "malloc")) ||
-          (rc = guard(cudaMalloc(&w.cs, nc * 8), "malloc")))
-        return rc;
-    } else if ((rc = guard(cudaMalloc(&w.dudt, n * 8), "malloc"))) {
+    if (ml && ((rc = guard(cudaMalloc(&w.flux, 3 * n * 8), "malloc")) ||
+               (rc = guard(cudaMalloc(&w.cb, nc * 8), "malloc")) || (rc = guard(cudaMalloc(&w.cs, nc * 8), "malloc"))))
       return rc;
-    }
+    if ((rc = guard(cudaMalloc(&w.dudt, n * 8), "malloc"))) return rc;  // multilevel: the fused blocks' scratch
     if (nd && (rc = guard(cudaMalloc(&w.derived, nd * 8), "malloc"))) return rc;
   }
   // each cycle's dt is read back as the cycle ends (into pinned memory: the copies queue

@@ -174,6 +174,7 @@ void GridTables::release() {
   rs_work = rr_work = pro_work = nullptr;
   fc = nullptr;
   fc_work = nullptr;
+  fcb = plain = nullptr;
   geom = nullptr;
 }
 
@@ -312,6 +313,16 @@ int lower_grid_impl(const GridTopology &g, const MeshSpec &spec, GridTables &out
   out.nfc_work = (int)fw.size();
   stage.add(&out.fc, fcs);
   stage.add(&out.fc_work, fw);
+  if (g.multilevel) {
+    std::vector<char> in_fc(g.blocks.size(), 0);
+    for (auto &f : g.flux_corr) in_fc[f.fine] = in_fc[f.coarse] = 1;
+    std::vector<int> fcb, plain;
+    for (size_t b = 0; b < g.blocks.size(); ++b) (in_fc[b] ? fcb : plain).push_back((int)b);
+    out.nfcb = (int)fcb.size();
+    out.nplain = (int)plain.size();
+    stage.add(&out.fcb, fcb);
+    stage.add(&out.plain, plain);
+  }
 
   out.geom_h.clear();
   for (auto &b : g.blocks) {

@@ -28,6 +28,10 @@ struct GridTables {
   DevWork *rs_work = nullptr, *rr_work = nullptr, *pro_work = nullptr;
   DevFluxCorr *fc = nullptr;
   DevWork *fc_work = nullptr;
+  // multilevel meshes: the blocks with a fine/coarse face (either side of a flux
+  // correction) and the others, whose stage needs no stored fluxes
+  int nfcb = 0, nplain = 0;
+  int *fcb = nullptr, *plain = nullptr;
   DevBlockGeom *geom = nullptr;
   void *arena = nullptr;        // one device allocation holding every table above
   std::vector<DevBlockGeom> geom_h;

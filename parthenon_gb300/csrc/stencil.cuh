@@ -49,7 +49,10 @@ struct StageArgs {
   double beta;           // Update weight (dt factor)
   const DevBlockGeom *geom;
   Dims d;
-  int nblocks;
+  int nblocks;           // blocks this launch covers
+  const int *blist;      // their indices (null: blocks 0 .. nblocks - 1)
+  int tune_nblocks;      // the mesh's blocks and multilevel flag: the autotuner's key
+  int tune_ml;           // (one choice per mesh for every launch of its stage)
   int recon;             // Burgers: 0 WENO5, 1 linear; advection: 0 donor cell, 1 PLM
   double vel[3];         // advection velocity
   int ncomp;             // components of the fields

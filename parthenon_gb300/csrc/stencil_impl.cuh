@@ -87,6 +87,7 @@ __device__ __forceinline__ bool march_line(const StageArgs &a, MarchLine &m) {
   const int64_t r = line / n_fast;
   const int t1 = (int)(r % n_slow);
   m.b = (int)(r / n_slow);
+  if (a.blist) m.b = a.blist[m.b];
   if (D == 0) {
     m.i0 = ng; m.j0 = ng + t0; m.k0 = ng + t1;
   } else if (D == 1) {
@@ -268,7 +269,7 @@ __global__ void __launch_bounds__(128) k_div_update(StageArgs a) {
   const int j = (int)(r % d.nx[1]) + d.ng;
   r /= d.nx[1];
   const int k = (int)(r % d.nx[2]) + d.ng;
-  const int b = (int)(r / d.nx[2]);
+  const int b = a.blist ? a.blist[r / d.nx[2]] : (int)(r / d.nx[2]);
   const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1];
   const int64_t cs = N01 * d.N[2];
   const DevBlockGeom g = a.geom[b];
