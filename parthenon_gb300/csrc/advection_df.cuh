@@ -21,16 +21,16 @@ namespace fast {
 
 // One line of one component: cells -1 .. n of direction D from c0 (first interior
 // cell), faces 0 .. n. MODE as in the shared kernels; vel the component's velocity
-// along D, area/vol the block's face area and cell volume.
-template <int D, int MODE>
+// along D, area/vol the block's face area and cell volume; ld(p) returns the value of
+// cell p (-2 .. n+1) of the line, from global or shared memory.
+template <int D, int MODE, class Ld>
 __device__ __forceinline__ void plm_line_df(const StageArgs &a, int b, int v, int64_t c0, int n, int64_t cs,
-                                            int64_t step, const DevBlockGeom &g, double vel) {
+                                            int64_t step, const DevBlockGeom &g, double vel, Ld &&ld) {
   using namespace dfl;
-  const double *__restrict__ u = a.u_in;
   const int NC = a.ncomp;
   // scale of the line: the largest exponent among the values read (cells -2 .. n+1)
   int emax = 0;
-  for (int p = -2; p <= n + 1; ++p) emax = max(emax, dexp_field(__ldg(u + c0 + (int64_t)p * step)));
+  for (int p = -2; p <= n + 1; ++p) emax = max(emax, dexp_field(ld(p)));
   const int off = emax == 0 ? 0 : 1023 - emax;
   // the flux factor: the velocity (flux-store mode) or area * velocity, as a scaled pair
   const double fac_d = MODE == kStoreFlux ? vel : g.area[D] * vel;
@@ -39,14 +39,14 @@ __device__ __forceinline__ void plm_line_df(const StageArgs &a, int b, int v, in
   const df fac = from_double(fac_d, ov);
   const int ofl = off + ov;  // units of fluxes and their differences
   const bool upwind_left = vel > 0.0;
-  df q0 = from_double(__ldg(u + c0 - step), off);
-  df dql = sub(q0, from_double(__ldg(u + c0 - 2 * step), off));
+  df q0 = from_double(ld(-1), off);
+  df dql = sub(q0, from_double(ld(-2), off));
   df Lprev = make(0.0f), AFprev = make(0.0f);
-  double qn_d = __ldg(u + c0);
+  double qn_d = ld(0);
   for (int p = -1; p <= n; ++p) {
     const int64_t e = c0 + (int64_t)p * step;
     const df qn = from_double(qn_d, off);
-    if (p < n) qn_d = __ldg(u + e + 2 * step);  // the cell after next
+    if (p < n) qn_d = ld(p + 2);  // the cell after next
     const df dqr = sub(qn, q0);
     const df dq2 = mul(dql, dqr);
     df s = mul(dq2, recip(add(dql, dqr)));
@@ -80,6 +80,52 @@ __device__ __forceinline__ void plm_line_df(const StageArgs &a, int b, int v, in
     }
     Lprev = Lc;
   }
+}
+
+// The x sweep with its lines staged through shared memory. In the sweep along x one
+// thread marches one line and a warp's 32 lines are 32 different rows, so each of its
+// loads touches 32 sectors and waits on the previous one (memory-latency bound). Here
+// each warp first copies its 32 lines (cells -2 .. n+1, n + 4 values each) into shared
+// memory -- consecutive lanes on consecutive values of a row, so the loads coalesce --
+// and each lane then marches its line from there. Rows are kept at an odd stride, so the
+// lanes' 8-byte reads at one position of their rows hit distinct banks.
+constexpr int kXStageMaxN = 32;
+// dynamic shared memory of one 128-thread CTA: 4 warps x 32 rows of (n + 4) | 1 doubles
+inline size_t x_stage_smem(int n) { return (size_t)4 * 32 * ((n + 4) | 1) * sizeof(double); }
+template <int MODE>
+__global__ void __launch_bounds__(128) k_march_adv_x_df(StageArgs a) {
+  extern __shared__ double x_rows[];
+  const Dims d = a.d;
+  const int n = d.nx[0], ng = d.ng, NC = a.ncomp, v = blockIdx.y;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int L = n + 4, R = L | 1;  // values per line, row stride in shared memory
+  const int64_t line = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nlines = (int64_t)a.nblocks * d.nx[1] * d.nx[2];
+  const bool live = line < nlines;
+  const int64_t ln = live ? line : 0;
+  const int j = (int)(ln % d.nx[1]);
+  const int64_t r = ln / d.nx[1];
+  const int k = (int)(r % d.nx[2]);
+  const int b = a.blist ? a.blist[r / d.nx[2]] : (int)(r / d.nx[2]);
+  const int64_t N0 = d.N[0], N01 = (int64_t)d.N[0] * d.N[1], cs = N01 * d.N[2];
+  const int64_t c0 = ((int64_t)b * NC + v) * cs + (int64_t)(k + ng) * N01 + (int64_t)(j + ng) * N0 + ng;
+  const bool active = live && !(a.alloc && !a.alloc[b * NC + v]);
+  // stage the warp's lines: value q of the flattened 32 x L tile is cell (q % L) - 2 of
+  // the line of lane q / L
+  double *my = x_rows + (size_t)w * 32 * R;
+  const double *__restrict__ u = a.u_in;
+  for (int q = lane; q < 32 * L; q += 32) {
+    const int src = q / L, col = q - src * L;
+    const int64_t base = __shfl_sync(0xffffffffu, c0, src);
+    const int act = __shfl_sync(0xffffffffu, active ? 1 : 0, src);
+    my[src * R + col] = act ? __ldg(u + base - 2 + col) : 0.0;
+  }
+  __syncwarp();
+  if (!active) return;
+  const double *row = my + lane * R + 2;  // row[p] = cell p of this lane's line
+  const DevBlockGeom g = a.geom[b];
+  const double vd = a.ncvel ? a.cvel[v][0] : a.vel[0];
+  plm_line_df<0, MODE>(a, b, v, c0, n, cs, 1, g, vd, [&](int p) { return row[p]; });
 }
 
 }  // namespace fast

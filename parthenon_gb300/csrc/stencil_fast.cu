@@ -91,6 +91,7 @@ __device__ __forceinline__ void weno5z(double q0, double q1, double q2, double q
 }  // namespace pgb
 
 #include "advection_df.cuh"
+#define PGB_HAVE_PLM_X_STAGED 1
 #include "stencil_impl.cuh"
 #include "burgers_fast.cuh"
 #define PGB_HAVE_BURGERS_FAST 1

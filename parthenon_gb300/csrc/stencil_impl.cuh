@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(128) k_march_adv(StageArgs a) {
 #ifndef PGB_EXACT_ARITH
   // fast build, PLM: the line in double-float pairs (advection_df.cuh)
   if (a.recon != 0) {
-    plm_line_df<D, MODE>(a, b, v, c0, m.n, cs, step, g, vd);
+    plm_line_df<D, MODE>(a, b, v, c0, m.n, cs, step, g, vd, [&](int p) { return __ldg(u + c0 + (int64_t)p * step); });
     return;
   }
 #endif

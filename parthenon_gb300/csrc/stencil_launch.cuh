@@ -37,12 +37,24 @@ int launch_advection(const StageArgs &a, bool store_flux, cudaStream_t s) {
     const int64_t lines = (int64_t)a.nblocks * nf * ns;
     return dim3((unsigned)((lines + 127) / 128), (unsigned)a.ncomp);
   };
+#ifdef PGB_HAVE_PLM_X_STAGED
+  // fast build, PLM: the x sweep from lines staged in shared memory (advection_df.cuh)
+  const bool staged = a.recon != 0 && d.nx[0] <= kXStageMaxN;
+#else
+  const bool staged = false;
+#endif
   if (store_flux) {
-    k_march_adv<0, kStoreFlux><<<g(0), 128, 0, s>>>(a);
+#ifdef PGB_HAVE_PLM_X_STAGED
+    if (staged) k_march_adv_x_df<kStoreFlux><<<g(0), 128, x_stage_smem(d.nx[0]), s>>>(a);
+#endif
+    if (!staged) k_march_adv<0, kStoreFlux><<<g(0), 128, 0, s>>>(a);
     k_march_adv<1, kStoreFlux><<<g(1), 128, 0, s>>>(a);
     k_march_adv<2, kStoreFlux><<<g(2), 128, 0, s>>>(a);
   } else {
-    k_march_adv<0, kStoreDu><<<g(0), 128, 0, s>>>(a);
+#ifdef PGB_HAVE_PLM_X_STAGED
+    if (staged) k_march_adv_x_df<kStoreDu><<<g(0), 128, x_stage_smem(d.nx[0]), s>>>(a);
+#endif
+    if (!staged) k_march_adv<0, kStoreDu><<<g(0), 128, 0, s>>>(a);
     k_march_adv<1, kAddDu><<<g(1), 128, 0, s>>>(a);
     k_march_adv<2, kFinishUpdate><<<g(2), 128, 0, s>>>(a);
   }
