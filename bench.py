@@ -329,21 +329,26 @@ def run_ours(args, ws, rank):
     nat.check(L.pgb_run_host_dt(mesh.handle, ctypes.byref(p), ctypes.c_void_p(host_in.data_ptr()),
                                 ctypes.c_void_p(host_out.data_ptr()), NCOMP, args.warmup, ctypes.byref(dt_h),
                                 dt_steps), "pgb_run_host_dt")
-    dt_h = ctypes.c_double(0.0)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    nat.check(L.pgb_run_host_dt(mesh.handle, ctypes.byref(p), ctypes.c_void_p(host_in.data_ptr()),
-                                ctypes.c_void_p(host_out.data_ptr()), NCOMP, e2e_steps, ctypes.byref(dt_h),
-                                dt_steps), "pgb_run_host_dt")
-    e2e_s = time.perf_counter() - t0
+    # the median of three timed calls (host-side variation between calls is a few %)
+    e2e_runs = []
+    for _ in range(3):
+        dt_h = ctypes.c_double(0.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nat.check(L.pgb_run_host_dt(mesh.handle, ctypes.byref(p), ctypes.c_void_p(host_in.data_ptr()),
+                                    ctypes.c_void_p(host_out.data_ptr()), NCOMP, e2e_steps, ctypes.byref(dt_h),
+                                    dt_steps), "pgb_run_host_dt")
+        e2e_runs.append(time.perf_counter() - t0)
+    e2e_s = sorted(e2e_runs)[1]
     nat.check(L.pgb_release_host_workspace(mesh.handle), "pgb_release_host_workspace")
     nbytes = state.nbytes
     e2e = {"value": ws * e2e_steps * zones / e2e_s, "unit": METRIC, "h2d_bytes_per_step": nbytes / e2e_steps,
            "d2h_bytes_per_step": nbytes / e2e_steps + 8, "steps": e2e_steps,
+           "calls_s": [round(x, 4) for x in e2e_runs],
            "note": "pgb_run_host_dt with host buffers: H2D of the initial field (2.9 GB, pinned), ghost fill, "
-                   "initial dt, K cycles each followed by a D2H of that step's dt, D2H of the final field; the "
-                   "state stays resident between steps; the mesh's device workspace was allocated by an untimed "
-                   "warm-up call of W cycles"}
+                   "initial dt, K cycles (the mesh's cycle graph) each followed by a D2H of that step's dt, D2H of "
+                   "the final field; the state stays resident between steps; the mesh's device workspace was "
+                   "allocated by an untimed warm-up call of W cycles; the median of three timed calls"}
 
     peak_hbm = peaks["hbm_gbs"]
     out = {

@@ -279,6 +279,46 @@ int autotune(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage
   return rc;
 }
 
+// The CUDA graph of one RK2 cycle on these buffers: found in the mesh's cache (keyed
+// by everything the captured launches were built from: pointers, stage parameters --
+// the velocity table by value -- and whether sparse variables are on), or tuned,
+// captured and instantiated now.
+int cycle_graph(pgb_mesh *m, const pgb_stage_params *p, double *base, double *stage, double *dudt, double *flux,
+                double *cbase, double *cstage, int ncomp, double *dt, cudaStream_t s, double *derived,
+                cudaGraphExec_t *out) {
+  int rc;
+  std::string key;
+  auto put = [&](const void *q, size_t n) { key.append((const char *)q, n); };
+  const void *ptrs[] = {base, stage, dudt, flux, cbase, cstage, dt, derived};
+  put(ptrs, sizeof(ptrs));
+  put(p, offsetof(pgb_stage_params, comp_vel));
+  if (p->physics == 0 && p->ncomp_vel) put(p->comp_vel, 3 * sizeof(double) * p->ncomp_vel);
+  const int extra[2] = {ncomp, m->st.sparse_dev() ? 1 : 0};
+  put(extra, sizeof(extra));
+  auto it = m->graphs.find(key);
+  if (it == m->graphs.end()) {
+    // launch shapes are chosen before the cycle is frozen into a graph
+    if ((rc = autotune(m, p, base, stage, dudt, flux, cbase, ncomp, dt, s))) return rc;
+    cudaGraph_t g;
+    PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s, derived);
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (rc) {
+      // the capture ended with a graph of the launches made before the failure
+      if (ce == cudaSuccess) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ce != cudaSuccess) return check_cuda(ce, "cudaStreamEndCapture");
+    cudaGraphExec_t ge;
+    ce = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return check_cuda(ce, "cudaGraphInstantiate");
+    it = m->graphs.emplace(key, ge).first;
+  }
+  *out = it->second;
+  return kOk;
+}
+
 }  // namespace
 
 extern "C" {
@@ -469,37 +509,9 @@ int pgb_rk2_cycles(pgb_mesh *m, const pgb_stage_params *p, double *base, double 
     return kOk;
   }
   if (!s) return fail(kErrInvalid, "graph replay needs a non-default stream");
-  // everything the captured launches were built from: pointers, stage parameters (the
-  // velocity table by value) and whether sparse variables are on
-  std::string key;
-  auto put = [&](const void *q, size_t n) { key.append((const char *)q, n); };
-  const void *ptrs[] = {base, stage, dudt, flux, cbase, cstage, dt, derived};
-  put(ptrs, sizeof(ptrs));
-  put(p, offsetof(pgb_stage_params, comp_vel));
-  if (p->physics == 0 && p->ncomp_vel) put(p->comp_vel, 3 * sizeof(double) * p->ncomp_vel);
-  const int extra[2] = {ncomp, m->st.sparse_dev() ? 1 : 0};
-  put(extra, sizeof(extra));
-  auto it = m->graphs.find(key);
-  if (it == m->graphs.end()) {
-    // launch shapes are chosen before the cycle is frozen into a graph
-    if ((rc = autotune(m, p, base, stage, dudt, flux, cbase, ncomp, dt, s))) return rc;
-    cudaGraph_t g;
-    PGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    rc = cycle_impl(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s, derived);
-    cudaError_t ce = cudaStreamEndCapture(s, &g);
-    if (rc) {
-      // the capture ended with a graph of the launches made before the failure
-      if (ce == cudaSuccess) cudaGraphDestroy(g);
-      return rc;
-    }
-    if (ce != cudaSuccess) return check_cuda(ce, "cudaStreamEndCapture");
-    cudaGraphExec_t ge;
-    ce = cudaGraphInstantiate(&ge, g, 0);
-    cudaGraphDestroy(g);
-    if (ce != cudaSuccess) return check_cuda(ce, "cudaGraphInstantiate");
-    it = m->graphs.emplace(key, ge).first;
-  }
-  for (int c = 0; c < ncycles; ++c) PGB_CUDA(cudaGraphLaunch(it->second, s));
+  cudaGraphExec_t ge = nullptr;
+  if ((rc = cycle_graph(m, p, base, stage, dudt, flux, cbase, cstage, ncomp, dt, s, derived, &ge))) return rc;
+  for (int c = 0; c < ncycles; ++c) PGB_CUDA(cudaGraphLaunch(ge, s));
   return kOk;
 }
 
@@ -572,11 +584,15 @@ int pgb_run_host_dt(pgb_mesh *m, const pgb_stage_params *p, const double *host_i
     w.release();
     return rc;
   }
+  // the cycles replay the mesh's cycle graph on the workspace (captured on first use)
+  cudaGraphExec_t ge = nullptr;
+  if (ncycles > 0 &&
+      (rc = cycle_graph(m, p, w.base, w.stage, w.dudt, w.flux, w.cb, w.cs, ncomp, w.dt, s, derived, &ge))) {
+    w.release();
+    return rc;
+  }
   for (int c = 0; c < ncycles; ++c) {
-    if ((rc = cycle_impl(m, p, w.base, w.stage, w.dudt, w.flux, w.cb, w.cs, ncomp, w.dt, s, derived))) {
-      w.release();
-      return rc;
-    }
+    if ((rc = guard(cudaGraphLaunch(ge, s), "graph launch"))) return rc;
     if (dt_cycles && (rc = guard(cudaMemcpyAsync(w.dt_pinned + c, w.dt, 8, cudaMemcpyDeviceToHost, s), "d2h dt")))
       return rc;
   }
