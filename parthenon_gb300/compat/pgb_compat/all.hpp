@@ -59,6 +59,7 @@ using ::parthenon::PDOpt;
 using ::parthenon::SparsePack;
 using ::parthenon::TopologicalElement;
 using ::parthenon::DevExecSpace;
+using ::parthenon::HostExecSpace;
 using ::parthenon::IndexDomain;
 using ::parthenon::IndexRange;
 using ::parthenon::IndexShape;

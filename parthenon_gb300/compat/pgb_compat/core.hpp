@@ -18,6 +18,7 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstdlib>
+#include <limits>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -131,6 +132,20 @@ namespace ErrorChecking {
      << "\n  Line number: " << line;
   throw std::runtime_error(os.str());
 }
+// a failed requirement: on the host an exception; in device code (a par_for body) the
+// message is printed and the kernel carries on -- a device trap would end the CUDA
+// context of every stream of the process
+inline void require_fail(const char *cond, const std::string &msg, const char *file, int line) {
+  fail_throws(cond, msg, file, line);
+}
+__host__ __device__ inline void require_fail(const char *cond, const char *msg, const char *file, int line) {
+#ifdef __CUDA_ARCH__
+  printf("### PARTHENON ERROR (device)\n  Condition:   %s\n  Message:     %s\n  File:        %s\n  Line number: %d\n",
+         cond, msg, file, line);
+#else
+  fail_throws(cond, msg, file, line);
+#endif
+}
 inline void warn(const std::string &msg, const char *file, int line) {
   std::fprintf(stderr, "### PARTHENON WARNING\n  Message:     %s\n  File:        %s\n  Line number: %d\n", msg.c_str(),
                file, line);
@@ -142,6 +157,16 @@ inline void warn(const std::string &msg, const char *file, int line) {
 struct DevExecSpace {
   cudaStream_t stream() const;
   void fence() const;
+};
+// the host execution space (Kokkos::DefaultHostExecutionSpace): a tag for reducers that
+// name their space
+struct HostExecSpace {};
+
+// src/basic_types.hpp SimTime: the evolution's clock
+struct SimTime {
+  Real start_time = 0, time = 0, tlim = std::numeric_limits<Real>::max(), dt = std::numeric_limits<Real>::max();
+  int ncycle = 0, nlim = -1, ncycle_out = 1;
+  bool KeepGoing() const { return time < tlim && (nlim < 0 || ncycle < nlim); }
 };
 
 // The layer's stream (created on first use; graph capture and the library's calls use it).
@@ -170,9 +195,9 @@ inline void check_pgb(int rc, const char *what) {
 
 }  // namespace parthenon
 
-#define PARTHENON_REQUIRE(cond, msg)                                                         \
-  do {                                                                                       \
-    if (!(cond)) ::parthenon::ErrorChecking::fail_throws(#cond, msg, __FILE__, __LINE__);    \
+#define PARTHENON_REQUIRE(cond, msg)                                                          \
+  do {                                                                                        \
+    if (!(cond)) ::parthenon::ErrorChecking::require_fail(#cond, msg, __FILE__, __LINE__);    \
   } while (0)
 #define PARTHENON_REQUIRE_THROWS(cond, msg) PARTHENON_REQUIRE(cond, msg)
 #define PARTHENON_FAIL(msg) ::parthenon::ErrorChecking::fail_throws("false", msg, __FILE__, __LINE__)

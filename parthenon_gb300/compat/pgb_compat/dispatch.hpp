@@ -24,8 +24,9 @@
 namespace Kokkos {
 
 // Reducers (Kokkos_Reducers): a reference to the host result plus the identity and the
-// join of the reduction.
-template <class T>
+// join of the reduction. The optional second parameter names the result's memory space
+// (always the host here).
+template <class T, class Space = void>
 struct Min {
   using value_type = T;
   T &result;
@@ -33,7 +34,7 @@ struct Min {
   __host__ __device__ static T identity() { return std::numeric_limits<T>::max(); }
   __host__ __device__ static void join(T &a, const T &b) { a = b < a ? b : a; }
 };
-template <class T>
+template <class T, class Space = void>
 struct Max {
   using value_type = T;
   T &result;
@@ -41,13 +42,31 @@ struct Max {
   __host__ __device__ static T identity() { return std::numeric_limits<T>::lowest(); }
   __host__ __device__ static void join(T &a, const T &b) { a = b > a ? b : a; }
 };
-template <class T>
+template <class T, class Space = void>
 struct Sum {
   using value_type = T;
   T &result;
   explicit Sum(T &r) : result(r) {}
   __host__ __device__ static T identity() { return T(0); }
   __host__ __device__ static void join(T &a, const T &b) { a += b; }
+};
+// the pair of a min and a max reduction (Kokkos::MinMax, value type MinMaxScalar)
+template <class T>
+struct MinMaxScalar {
+  T min_val, max_val;
+};
+template <class T, class Space = void>
+struct MinMax {
+  using value_type = MinMaxScalar<T>;
+  value_type &result;
+  explicit MinMax(value_type &r) : result(r) {}
+  __host__ __device__ static value_type identity() {
+    return value_type{std::numeric_limits<T>::max(), std::numeric_limits<T>::lowest()};
+  }
+  __host__ __device__ static void join(value_type &a, const value_type &b) {
+    a.min_val = b.min_val < a.min_val ? b.min_val : a.min_val;
+    a.max_val = b.max_val > a.max_val ? b.max_val : a.max_val;
+  }
 };
 
 inline void fence() { ::parthenon::DevExecSpace().fence(); }
@@ -380,6 +399,22 @@ __host__ __device__ __forceinline__ void par_for_inner(P, const team_mbr_t &m, c
                                               const int ju, const int il, const int iu, const F &f) {
   const int ni = iu - il + 1, nj = ju - jl + 1, n = (ku - kl + 1) * nj * ni;
   for (int t = m.team_rank(); t < n; t += m.team_size()) f(kl + t / (nj * ni), jl + (t / ni) % nj, il + t % ni);
+}
+
+// par_for_inner(member, bounds..., f): the default inner pattern
+template <class F>
+__host__ __device__ __forceinline__ void par_for_inner(const team_mbr_t &m, const int il, const int iu, const F &f) {
+  par_for_inner(InnerLoopPatternTVR{}, m, il, iu, f);
+}
+template <class F>
+__host__ __device__ __forceinline__ void par_for_inner(const team_mbr_t &m, const int jl, const int ju, const int il,
+                                                       const int iu, const F &f) {
+  par_for_inner(InnerLoopPatternTVR{}, m, jl, ju, il, iu, f);
+}
+template <class F>
+__host__ __device__ __forceinline__ void par_for_inner(const team_mbr_t &m, const int kl, const int ku, const int jl,
+                                                       const int ju, const int il, const int iu, const F &f) {
+  par_for_inner(InnerLoopPatternTVR{}, m, kl, ku, jl, ju, il, iu, f);
 }
 
 }  // namespace parthenon

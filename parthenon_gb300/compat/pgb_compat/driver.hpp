@@ -11,7 +11,9 @@
 #pragma once
 
 #include <algorithm>
+#include <array>
 #include <functional>
+#include <map>
 #include <limits>
 #include <memory>
 #include <string>
@@ -26,33 +28,69 @@ namespace parthenon {
 class ApplicationInput {
  public:
   std::function<Packages_t(std::unique_ptr<ParameterInput> &)> ProcessPackages = nullptr;
-  std::function<void(MeshBlock *, ParameterInput *)> ProblemGenerator = nullptr;
-  std::function<void(Mesh *, ParameterInput *, MeshData<Real> *)> MeshProblemGenerator = nullptr;
+  // mesh hooks
   std::function<void(Mesh *, ParameterInput *)> InitUserMeshData = nullptr;
-  std::function<void(Mesh *, ParameterInput *)> UserWorkAfterLoop = nullptr;
+  std::function<void(Mesh *, ParameterInput *, MeshData<Real> *)> MeshProblemGenerator = nullptr;
+  std::function<void(Mesh *, ParameterInput *, MeshData<Real> *)> MeshPostInitialization = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime &)> PreStepMeshUserWorkInLoop = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime const &)> PostStepMeshUserWorkInLoop = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime const &)> UserMeshWorkBeforeOutput = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime const &)> PreStepDiagnosticsInLoop = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime const &)> PostStepDiagnosticsInLoop = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime &)> UserWorkAfterLoop = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime &)> UserWorkBeforeLoop = nullptr;
+  // block hooks
+  std::function<void(MeshBlock *, ParameterInput *)> InitMeshBlockUserData = nullptr;
+  std::function<void(MeshBlock *, ParameterInput *)> ProblemGenerator = nullptr;
+  std::function<void(MeshBlock *, ParameterInput *)> PostInitialization = nullptr;
+  std::function<void(MeshBlock *, ParameterInput *, const SimTime &)> MeshBlockUserWorkBeforeOutput = nullptr;
+  // physical boundaries (application_input.hpp:79-86): recorded; the meshes of this
+  // layer are periodic, and Mesh refuses any other boundary flag in the input
+  void RegisterBoundaryCondition(BoundaryFace face, const std::string &name, BValFunc condition) {
+    PARTHENON_REQUIRE_THROWS(face >= 0 && face < BOUNDARY_NFACES, "boundary face out of range");
+    boundary_conditions[face][name] = std::move(condition);
+  }
+  void RegisterBoundaryCondition(BoundaryFace face, BValFunc condition) {
+    RegisterBoundaryCondition(face, "user", std::move(condition));
+  }
+  void RegisterDefaultReflectingBoundaryConditions() {
+    for (int f = 0; f < BOUNDARY_NFACES; ++f) boundary_conditions[f]["reflecting"] = nullptr;
+  }
+  std::array<std::map<std::string, BValFunc>, BOUNDARY_NFACES> boundary_conditions;
 };
 
 inline void Mesh::Initialize(ApplicationInput *app_in, ParameterInput *pin) {
   if (app_in && app_in->InitUserMeshData) app_in->InitUserMeshData(this, pin);
   auto &base = mesh_data.GetOrAdd("base", 0);
+  if (app_in && app_in->InitMeshBlockUserData)
+    for (auto &pmb : block_list) app_in->InitMeshBlockUserData(pmb.get(), pin);
   if (app_in && app_in->MeshProblemGenerator) {
     app_in->MeshProblemGenerator(this, pin, base.get());
   } else if (app_in && app_in->ProblemGenerator) {
     for (auto &pmb : block_list) app_in->ProblemGenerator(pmb.get(), pin);
   }
-  Update::PreCommFillDerived(base.get());
+  if (app_in && app_in->MeshPostInitialization) {
+    app_in->MeshPostInitialization(this, pin, base.get());
+  } else if (app_in && app_in->PostInitialization) {
+    for (auto &pmb : block_list) app_in->PostInitialization(pmb.get(), pin);
+  }
+  PreCommFillDerived();
   compat_detail::exchange(base.get());  // Mesh::CommunicateBoundaries
-  Update::FillDerived(base.get());
+  FillDerived();
   DevExecSpace().fence();
 }
 
-enum class DriverStatus { complete, timeout, failed };
+// mesh.cpp:709-738: the block hooks on every block, the mesh hooks on the partitions
+inline void Mesh::PreCommFillDerived() {
+  for (auto &pmb : block_list) Update::PreCommFillDerived(pmb->meshblock_data.Get().get());
+  for (auto &part : GetDefaultBlockPartitions()) Update::PreCommFillDerived(mesh_data.Add("base", part).get());
+}
+inline void Mesh::FillDerived() {
+  for (auto &part : GetDefaultBlockPartitions()) Update::FillDerived(mesh_data.Add("base", part).get());
+  for (auto &pmb : block_list) Update::FillDerived(pmb->meshblock_data.Get().get());
+}
 
-struct SimTime {
-  Real start_time = 0, time = 0, tlim = std::numeric_limits<Real>::max(), dt = std::numeric_limits<Real>::max();
-  int ncycle = 0, nlim = -1, ncycle_out = 1;
-  bool KeepGoing() const { return time < tlim && (nlim < 0 || ncycle < nlim); }
-};
+enum class DriverStatus { complete, timeout, failed };
 
 // src/outputs/outputs.hpp: file outputs are not on this path (the fields stay in
 // device memory for the caller)
@@ -92,35 +130,46 @@ class EvolutionDriver : public Driver {
     tm.nlim = pin->GetOrAddInteger("parthenon/time", "nlim", -1);
     tm.ncycle_out = pin->GetOrAddInteger("parthenon/time", "ncycle_out", 1);
   }
-  // driver.cpp:67-166 (outputs, load balancing and signals are not on this path)
+  // driver.cpp:67-166 with its hooks in the same order (outputs, load balancing and
+  // signals are not on this path)
   DriverStatus Execute() override {
     InitializeBlockTimeSteps();
     SetGlobalTimeStep();
+    if (app_input && app_input->UserWorkBeforeLoop) app_input->UserWorkBeforeLoop(pmesh, pinput, tm);
+    for (auto &np : pmesh->packages.AllPackages()) np.second->UserWorkBeforeLoop(pmesh, pinput, tm);
     zone_cycles = 0;
     while (tm.KeepGoing()) {
+      if (app_input && app_input->PreStepMeshUserWorkInLoop) app_input->PreStepMeshUserWorkInLoop(pmesh, pinput, tm);
+      if (app_input && app_input->PreStepDiagnosticsInLoop) app_input->PreStepDiagnosticsInLoop(pmesh, pinput, tm);
       if (Step() != TaskListStatus::complete) return DriverStatus::failed;
+      if (app_input && app_input->PostStepMeshUserWorkInLoop)
+        app_input->PostStepMeshUserWorkInLoop(pmesh, pinput, tm);
+      if (app_input && app_input->PostStepDiagnosticsInLoop) app_input->PostStepDiagnosticsInLoop(pmesh, pinput, tm);
       tm.ncycle++;
       tm.time += tm.dt;
       zone_cycles += (int64_t)pmesh->nbtotal * pmesh->GetNumberOfMeshBlockCells();
       SetGlobalTimeStep();
     }
+    if (app_input && app_input->UserWorkAfterLoop) app_input->UserWorkAfterLoop(pmesh, pinput, tm);
     DevExecSpace().fence();
-    return DriverStatus::complete;
+    return tm.KeepGoing() ? DriverStatus::timeout : DriverStatus::complete;
   }
   virtual TaskListStatus Step() = 0;
-  // driver.cpp:194-204: every partition votes from the current state
+  // driver.cpp:194-204: the block hooks on every block, then the mesh hooks on every
+  // partition, vote from the current state
   void InitializeBlockTimeSteps() {
-    for (int i = 0; i < pmesh->DefaultNumPartitions(); ++i)
-      Update::EstimateTimestep(pmesh->mesh_data.GetOrAdd("base", i).get());
+    for (auto &pmb : pmesh->block_list) Update::EstimateTimestep(pmb->meshblock_data.Get().get());
+    for (auto &part : pmesh->GetDefaultBlockPartitions())
+      Update::EstimateTimestep(pmesh->mesh_data.Add("base", part).get());
   }
-  // driver.cpp:210-232 with the default controls: growth limited to 2x, then the
-  // smallest vote of the blocks
+  // driver.cpp:210-235 with the default controls: growth limited to 2x, then the
+  // smallest vote of the blocks, whose votes are reset
   void SetGlobalTimeStep() {
     if (tm.dt < 0.1 * std::numeric_limits<Real>::max()) tm.dt *= 2.0;
-    Real mn = std::numeric_limits<Real>::max();
-    for (int i = 0; i < pmesh->DefaultNumPartitions(); ++i)
-      for (const char *name : {"base"}) mn = std::min(mn, pmesh->mesh_data.GetOrAdd(name, i)->GetAllowedDt());
-    tm.dt = std::min(tm.dt, mn);
+    for (auto &pmb : pmesh->block_list) {
+      tm.dt = std::min(tm.dt, pmb->NewDt());
+      pmb->SetAllowedDt(std::numeric_limits<Real>::max());
+    }
     tm.dt = std::max(std::numeric_limits<Real>::min(), std::min(tm.dt, std::numeric_limits<Real>::max()));
   }
   SimTime tm;

@@ -25,6 +25,7 @@
 #pragma once
 
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -146,6 +147,11 @@ class PackIndexMap {
     auto it = m_.find(name);
     return it == m_.end() ? std::pair<int, int>{-1, -2} : it->second;
   }
+  // variable_pack.hpp PackIndexMap::get: by name, or by a sparse pool's base name and id
+  std::pair<int, int> get(const std::string &name) const { return (*this)[name]; }
+  std::pair<int, int> get(const std::string &base, int sparse_id) const {
+    return (*this)[MakeVarLabel(base, sparse_id)];
+  }
   void insert(const std::string &name, int first, int last) { m_[name] = {first, last}; }
   bool count(const std::string &name) const { return m_.count(name) > 0; }
 
@@ -179,6 +185,9 @@ class VariableFluxPack {
   }
   KOKKOS_FORCEINLINE_FUNCTION T &flux(int b, int dir, int n, int k, int j, int i) const {
     return (*this)(b).flux(dir, n, k, j, i);
+  }
+  KOKKOS_FORCEINLINE_FUNCTION T &flux(int dir, int n, int k, int j, int i) const {
+    return (*this)(0).flux(dir, n, k, j, i);
   }
   KOKKOS_FORCEINLINE_FUNCTION const Coordinates_t &GetCoords(int b = 0) const { return coords_[b]; }
   // 5: blocks, 4: variables, 3..1: k, j, i extents (4..1 for a block-level pack)
@@ -273,6 +282,110 @@ struct BlockListPartition {
   int partition = 0;
 };
 
+// One block's array of a variable (src/parthenon_arrays.hpp ParArrayND, with the
+// dimensions of metadata.cpp GetArrayDims): GetDim(1..3) the cells along x, y, z, ghosts
+// included, GetDim(4..6) the variable's shape. Indices are right-aligned, the last
+// fastest: a(k, j, i) is a(0, 0, 0, k, j, i). ParArrayND views device memory;
+// GetHostMirrorAndCopy returns a host copy (HostArrayND) indexed the same way.
+namespace compat_detail {
+struct Dims6 {
+  int d[6] = {1, 1, 1, 1, 1, 1};  // d[0]: the fastest index
+  KOKKOS_FORCEINLINE_FUNCTION int64_t at(int64_t l, int64_t m, int64_t n, int64_t k, int64_t j, int64_t i) const {
+    return ((((l * d[4] + m) * d[3] + n) * d[2] + k) * d[1] + j) * d[0] + i;
+  }
+  KOKKOS_FORCEINLINE_FUNCTION int64_t size() const {
+    return (int64_t)d[0] * d[1] * d[2] * d[3] * d[4] * d[5];
+  }
+};
+}  // namespace compat_detail
+
+template <typename T>
+class HostArrayND {
+ public:
+  HostArrayND() = default;
+  explicit HostArrayND(const compat_detail::Dims6 &dims)
+      : dims_(dims), v_(std::make_shared<std::vector<T>>((size_t)dims.size())) {}
+  T &operator()(int i) const { return (*v_)[i]; }
+  T &operator()(int j, int i) const { return (*v_)[dims_.at(0, 0, 0, 0, j, i)]; }
+  T &operator()(int k, int j, int i) const { return (*v_)[dims_.at(0, 0, 0, k, j, i)]; }
+  T &operator()(int n, int k, int j, int i) const { return (*v_)[dims_.at(0, 0, n, k, j, i)]; }
+  T &operator()(int m, int n, int k, int j, int i) const { return (*v_)[dims_.at(0, m, n, k, j, i)]; }
+  T &operator()(int l, int m, int n, int k, int j, int i) const { return (*v_)[dims_.at(l, m, n, k, j, i)]; }
+  int GetDim(int d) const { return d >= 1 && d <= 6 ? dims_.d[d - 1] : 1; }
+  int64_t size() const { return dims_.size(); }
+  T *data() const { return v_->data(); }
+
+ private:
+  compat_detail::Dims6 dims_;
+  std::shared_ptr<std::vector<T>> v_;
+};
+
+template <typename T>
+class ParArrayND {
+ public:
+  ParArrayND() = default;
+  ParArrayND(T *p, const compat_detail::Dims6 &dims) : p_(p), dims_(dims) {}
+  KOKKOS_FORCEINLINE_FUNCTION T &operator()(int i) const { return p_[i]; }
+  KOKKOS_FORCEINLINE_FUNCTION T &operator()(int j, int i) const { return p_[dims_.at(0, 0, 0, 0, j, i)]; }
+  KOKKOS_FORCEINLINE_FUNCTION T &operator()(int k, int j, int i) const { return p_[dims_.at(0, 0, 0, k, j, i)]; }
+  KOKKOS_FORCEINLINE_FUNCTION T &operator()(int n, int k, int j, int i) const {
+    return p_[dims_.at(0, 0, n, k, j, i)];
+  }
+  KOKKOS_FORCEINLINE_FUNCTION T &operator()(int m, int n, int k, int j, int i) const {
+    return p_[dims_.at(0, m, n, k, j, i)];
+  }
+  KOKKOS_FORCEINLINE_FUNCTION T &operator()(int l, int m, int n, int k, int j, int i) const {
+    return p_[dims_.at(l, m, n, k, j, i)];
+  }
+  KOKKOS_FORCEINLINE_FUNCTION int GetDim(int d) const { return d >= 1 && d <= 6 ? dims_.d[d - 1] : 1; }
+  KOKKOS_FORCEINLINE_FUNCTION int64_t size() const { return dims_.size(); }
+  KOKKOS_FORCEINLINE_FUNCTION T *data() const { return p_; }
+  // an uninitialised host array of the same dimensions
+  HostArrayND<T> GetHostMirror() const { return HostArrayND<T>(dims_); }
+  // a host copy of the array, after the work queued on the layer's stream
+  HostArrayND<T> GetHostMirrorAndCopy() const {
+    HostArrayND<T> h(dims_);
+    check_cuda(cudaMemcpyAsync(h.data(), p_, sizeof(T) * (size_t)size(), cudaMemcpyDeviceToHost, compat_stream()),
+               "host mirror copy");
+    check_cuda(cudaStreamSynchronize(compat_stream()), "host mirror copy");
+    return h;
+  }
+  // copies a host array of the same size into this one (Kokkos::deep_copy)
+  void DeepCopy(const HostArrayND<T> &h) const {
+    PARTHENON_REQUIRE_THROWS(h.size() == size(), "deep copy between arrays of different sizes");
+    check_cuda(cudaMemcpyAsync(p_, h.data(), sizeof(T) * (size_t)size(), cudaMemcpyHostToDevice, compat_stream()),
+               "deep copy");
+    check_cuda(cudaStreamSynchronize(compat_stream()), "deep copy");
+  }
+
+ private:
+  T *p_ = nullptr;
+  compat_detail::Dims6 dims_;
+};
+
+// A block's variable in a container (src/interface/variable.hpp): its array and
+// metadata. Every variable of the layer is allocated.
+template <typename T>
+class Variable {
+ public:
+  Variable(const std::string &label, const Metadata &m, const ParArrayND<T> &d, int sparse_id)
+      : data(d), label_(label), m_(m), sparse_id_(sparse_id) {}
+  ParArrayND<T> data;
+  const std::string &label() const { return label_; }
+  const Metadata &metadata() const { return m_; }
+  bool IsSet(const MetadataFlag &f) const { return m_.IsSet(f); }
+  int GetDim(int d) const { return data.GetDim(d); }
+  int NumComponents() const { return m_.NumComponents(); }
+  bool IsAllocated() const { return true; }
+  bool IsSparse() const { return m_.IsSet(Metadata::Sparse); }
+  int GetSparseID() const { return sparse_id_; }
+
+ private:
+  std::string label_;
+  Metadata m_;
+  int sparse_id_;
+};
+
 template <typename T>
 class DataCollection;
 
@@ -280,6 +393,8 @@ class DataCollection;
 class MeshBlock {
  public:
   MeshBlock(Mesh *pm, int gid, const double xmin[3], const double dx[3], const int nx[3], int ng);
+  MeshBlock(const MeshBlock &) = delete;
+  MeshBlock &operator=(const MeshBlock &) = delete;
   int gid;
   int64_t lid;
   Coordinates_t coords;
@@ -289,12 +404,31 @@ class MeshBlock {
   std::unique_ptr<DataCollection<MeshBlockData<Real>>> meshblock_data_ptr;
   DataCollection<MeshBlockData<Real>> &meshblock_data;
   Mesh *GetParentPointer() const { return pmy_mesh; }
-  // par_for on this block's data (the reference's MeshBlock::par_for)
+  // the mesh's packages (the reference block holds a copy of the same pointers)
+  Packages_t &packages;
+  // par_for / par_reduce on this block's data (the reference's MeshBlock::par_for)
   template <class... Args>
   void par_for(Args &&...args) const {
     ::parthenon::par_for(std::forward<Args>(args)...);
   }
-  Real NewDt() const;
+  template <class... Args>
+  void par_reduce(Args &&...args) const {
+    ::parthenon::par_reduce(std::forward<Args>(args)...);
+  }
+  template <class... Args>
+  void par_for_outer(Args &&...args) const {
+    ::parthenon::par_for_outer(std::forward<Args>(args)...);
+  }
+  // meshblock.hpp AllocSparseID: every id of a pool is allocated from the start, so
+  // this checks that the field exists
+  void AllocSparseID(const std::string &base, int sparse_id);
+  bool IsAllocated(const std::string &name) const;
+  // the block's vote for the next time step (meshblock.hpp:303-304)
+  void SetAllowedDt(const Real dt) { new_block_dt_ = dt; }
+  Real NewDt() const { return new_block_dt_; }
+
+ private:
+  Real new_block_dt_ = std::numeric_limits<Real>::max();
 };
 using BlockList_t = std::vector<std::shared_ptr<MeshBlock>>;
 
@@ -310,8 +444,10 @@ class MeshData {
   IndexRange GetBoundsI(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const { return bounds(0, d, te); }
   IndexRange GetBoundsJ(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const { return bounds(1, d, te); }
   IndexRange GetBoundsK(IndexDomain d, TopologicalElement te = TopologicalElement::CC) const { return bounds(2, d, te); }
-  void SetAllowedDt(Real dt) { dt_ = dt; }
-  Real GetAllowedDt() const { return dt_; }
+  // mesh_data.hpp:210-214: each block's vote becomes at most dt (a multigrid grid keeps
+  // its own value)
+  void SetAllowedDt(Real dt);
+  Real GetAllowedDt() const;
   std::shared_ptr<MeshBlockData<T>> &GetBlockData(int b);
   std::vector<std::shared_ptr<MeshBlockData<T>>> &GetAllBlockData();
 
@@ -399,11 +535,19 @@ class MeshBlockData {
   const VariablePack<T> &PackVariables(const std::vector<MetadataFlag> &flags);
   const VariableFluxPack<T> &PackVariablesAndFluxes(const std::vector<std::string> &names,
                                                     const std::vector<std::string> &fluxes, PackIndexMap &imap);
-  Real dt_allowed = std::numeric_limits<Real>::max();
+  const VariableFluxPack<T> &PackVariablesAndFluxes(const std::vector<MetadataFlag> &flags, PackIndexMap &imap);
+  const VariableFluxPack<T> &PackVariablesAndFluxes(const std::vector<MetadataFlag> &flags);
+  // a cell-centred variable of this block (meshblock_data.hpp Get / GetVarPtr)
+  Variable<T> &Get(const std::string &name);
+  std::shared_ptr<Variable<T>> GetVarPtr(const std::string &name);
+  bool HasVariable(const std::string &name) const;
+  bool IsAllocated(const std::string &name) const { return HasVariable(name); }
+  void SetAllowedDt(const Real dt) const { pmb_->SetAllowedDt(dt); }
 
  private:
   MeshBlock *pmb_;
   std::string name_;
+  std::map<std::string, std::shared_ptr<Variable<T>>> vars_;
 };
 
 // Named containers (src/interface/data_collection.hpp): of the mesh (MeshData: the
@@ -423,6 +567,12 @@ class DataCollection<MeshData<Real>> {
     return GetOrAdd(name, p->grid);
   }
   std::shared_ptr<MeshData<Real>> &Add(const std::string &name, int partition) { return GetOrAdd(name, partition); }
+  // a container over src's blocks (data_collection.hpp Add(label, src, field_names,
+  // shallow)): every container holds every variable here, so the names select nothing
+  std::shared_ptr<MeshData<Real>> &Add(const std::string &name, const std::shared_ptr<MeshData<Real>> &src,
+                                       const std::vector<std::string> & = {}, bool = false) {
+    return GetOrAdd(name, src->grid);
+  }
   // a container sharing md's variables (every container holds every variable here, so
   // the new name aliases md's data)
   std::shared_ptr<MeshData<Real>> &AddShallow(const std::string &, std::shared_ptr<MeshData<Real>> &md,
@@ -451,6 +601,24 @@ class DataCollection<MeshBlockData<Real>> {
   std::map<std::string, std::shared_ptr<MeshBlockData<Real>>> mbds_;
 };
 
+// src/defs.hpp RegionSize: the extent and cell counts of a region, by coordinate
+// direction (X1DIR ... X3DIR)
+struct RegionSize {
+  std::array<Real, 3> xmin_{0, 0, 0}, xmax_{1, 1, 1}, xrat_{1, 1, 1};
+  std::array<int, 3> nx_{1, 1, 1};
+  std::array<bool, 3> symmetry_{false, false, false};
+  Real &xmin(CoordinateDirection d) { return xmin_[d - 1]; }
+  const Real &xmin(CoordinateDirection d) const { return xmin_[d - 1]; }
+  Real &xmax(CoordinateDirection d) { return xmax_[d - 1]; }
+  const Real &xmax(CoordinateDirection d) const { return xmax_[d - 1]; }
+  Real &xrat(CoordinateDirection d) { return xrat_[d - 1]; }
+  const Real &xrat(CoordinateDirection d) const { return xrat_[d - 1]; }
+  int &nx(CoordinateDirection d) { return nx_[d - 1]; }
+  const int &nx(CoordinateDirection d) const { return nx_[d - 1]; }
+  bool &symmetry(CoordinateDirection d) { return symmetry_[d - 1]; }
+  const bool &symmetry(CoordinateDirection d) const { return symmetry_[d - 1]; }
+};
+
 class ApplicationInput;
 
 // The mesh (src/mesh/mesh.hpp): a uniform periodic grid of equal blocks, its library
@@ -465,6 +633,8 @@ class Mesh {
   Mesh &operator=(const Mesh &) = delete;
 
   int ndim = 3;
+  bool is_restart = false;  // restarts are not on this path
+  RegionSize mesh_size;     // the root domain: its extent and cells
   bool adaptive = false;
   bool multilevel = false;
   bool multigrid = false;
@@ -490,6 +660,8 @@ class Mesh {
   // runs the application's problem generator on every block, fills the ghosts and
   // the derived fields (Mesh::Initialize, src/mesh/mesh.cpp:745-858)
   void Initialize(ApplicationInput *app_in, ParameterInput *pin);
+  void PreCommFillDerived();
+  void FillDerived();
 
   // ---- the layer's own ---------------------------------------------------------------
   pgb_mesh *handle() const { return handle_; }
@@ -563,6 +735,10 @@ inline Mesh::Mesh(ParameterInput *pin, ApplicationInput *, Packages_t &pkgs)
     PARTHENON_REQUIRE_THROWS(bc_in == "periodic" && bc_out == "periodic",
                              "this path supports periodic boundaries only");
     nx_[d] = spec.block_nx[d];
+    mesh_size.xmin_[d] = spec.xmin[d];
+    mesh_size.xmax_[d] = spec.xmax[d];
+    mesh_size.nx_[d] = spec.nx[d];
+    mesh_size.symmetry_[d] = spec.nx[d] == 1;
   }
   spec.nghost = pin->GetOrAddInteger("parthenon/mesh", "nghost", 2);
   const std::string refinement = pin->GetOrAddString("parthenon/mesh", "refinement", "none");
@@ -644,7 +820,7 @@ inline Mesh::Mesh(ParameterInput *pin, ApplicationInput *, Packages_t &pkgs)
   for (const auto &name : packages.Order())
     for (const auto &f : packages.Get(name)->AllFields()) {
       vars_.push_back(VarInfo{f.first, f.second, f.second.NumComponents()});
-      resolved_packages->AddField(f.first, f.second);
+      resolved_packages->add_field(f.first, f.second);
     }
   onecopy_.assign(vars_.size(), {});
   for (size_t v = 0; v < vars_.size(); ++v)
@@ -726,17 +902,63 @@ inline MeshBlock::MeshBlock(Mesh *pm, int g, const double xmin[3], const double 
       c_cellbounds(std::max(1, nx[0] / 2), std::max(1, nx[1] / 2), std::max(1, nx[2] / 2), ng),
       pmy_mesh(pm),
       meshblock_data_ptr(new DataCollection<MeshBlockData<Real>>(this)),
-      meshblock_data(*meshblock_data_ptr) {}
+      meshblock_data(*meshblock_data_ptr),
+      packages(pm->packages) {}
 
-inline Real MeshBlock::NewDt() const {
-  Real dt = std::numeric_limits<Real>::max();
-  for (auto *name : {"base"}) dt = std::min(dt, meshblock_data_ptr->Get(name)->dt_allowed);
-  return dt;
+inline void MeshBlock::AllocSparseID(const std::string &base, int sparse_id) {
+  PARTHENON_REQUIRE_THROWS(pmy_mesh->var_index(MakeVarLabel(base, sparse_id)) >= 0,
+                           "no sparse field " + MakeVarLabel(base, sparse_id));
+}
+inline bool MeshBlock::IsAllocated(const std::string &name) const { return pmy_mesh->var_index(name) >= 0; }
+
+template <typename T>
+bool MeshBlockData<T>::HasVariable(const std::string &name) const {
+  return pmb_->pmy_mesh->var_index(name) >= 0;
+}
+template <typename T>
+std::shared_ptr<Variable<T>> MeshBlockData<T>::GetVarPtr(const std::string &name) {
+  auto it = vars_.find(name);
+  if (it != vars_.end()) return it->second;
+  Mesh *pm = pmb_->pmy_mesh;
+  const int v = pm->var_index(name);
+  PARTHENON_REQUIRE_THROWS(v >= 0, "no variable named " + name);
+  const VarInfo &vi = pm->variables()[v];
+  PARTHENON_REQUIRE_THROWS(!vi.face(), "face field " + name + ": read it through a SparsePack");
+  compat_detail::Dims6 dims;
+  for (int d = 0; d < 3; ++d) dims.d[d] = pm->N()[d];
+  const auto &shape = vi.m.Shape();
+  for (size_t q = 0; q < shape.size() && q < 3; ++q) dims.d[3 + q] = shape[q];
+  T *p = pm->container(name_).data[v] + (int64_t)pmb_->gid * vi.ncomp * pm->cells_per_comp();
+  int sparse_id = -1;  // InvalidSparseID for dense variables
+  if (vi.m.IsSet(Metadata::Sparse)) sparse_id = std::stoi(name.substr(name.rfind('_') + 1));
+  auto var = std::make_shared<Variable<T>>(name, vi.m, ParArrayND<T>(p, dims), sparse_id);
+  vars_.emplace(name, var);
+  return var;
+}
+template <typename T>
+Variable<T> &MeshBlockData<T>::Get(const std::string &name) {
+  return *GetVarPtr(name);
 }
 
 template <typename T>
 MeshData<T>::MeshData(Mesh *pm, const std::string &container, GridIdentifier g)
     : grid(g), pm_(pm), name_(container), set_(pm->block_set(g)) {}
+
+template <typename T>
+void MeshData<T>::SetAllowedDt(Real dt) {
+  if (grid.type == GridType::two_level_composite) {
+    dt_ = dt;
+    return;
+  }
+  for (int b : set_.slot) pm_->block_list[b]->SetAllowedDt(std::min(dt, pm_->block_list[b]->NewDt()));
+}
+template <typename T>
+Real MeshData<T>::GetAllowedDt() const {
+  if (grid.type == GridType::two_level_composite) return dt_;
+  Real dt = std::numeric_limits<Real>::max();
+  for (int b : set_.slot) dt = std::min(dt, pm_->block_list[b]->NewDt());
+  return dt;
+}
 
 template <typename T>
 const BlockStore &MeshData<T>::store() const {
@@ -954,6 +1176,20 @@ const VariableFluxPack<T> &MeshBlockData<T>::PackVariablesAndFluxes(const std::v
   return pmb_->pmy_mesh->mesh_data.GetOrAdd(name_, 0)->pack(names, fluxes, &imap, true, pmb_->gid);
 }
 
+template <typename T>
+const VariableFluxPack<T> &MeshBlockData<T>::PackVariablesAndFluxes(const std::vector<MetadataFlag> &flags,
+                                                                    PackIndexMap &imap) {
+  auto &md = pmb_->pmy_mesh->mesh_data.GetOrAdd(name_, 0);
+  const auto n = md->names_with(flags);
+  return md->pack(n, n, &imap, true, pmb_->gid);
+}
+template <typename T>
+const VariableFluxPack<T> &MeshBlockData<T>::PackVariablesAndFluxes(const std::vector<MetadataFlag> &flags) {
+  auto &md = pmb_->pmy_mesh->mesh_data.GetOrAdd(name_, 0);
+  const auto n = md->names_with(flags);
+  return md->pack(n, n, nullptr, true, pmb_->gid);
+}
+
 namespace compat_detail {
 inline const PackTables &get_pack_tables(MeshBlockData<Real> *mbd, const PackSpec &spec) {
   MeshBlock *pmb = mbd->GetBlockPointer();
@@ -991,14 +1227,6 @@ inline std::shared_ptr<MeshBlockData<Real>> &DataCollection<MeshBlockData<Real>>
     const std::string &name, const std::shared_ptr<MeshBlockData<Real>> &) {
   // every container holds every variable: a new one is allocated (zero) on first use
   return Get(name);
-}
-
-inline Real StateDescriptor::EstimateTimestep(MeshData<Real> *rc) const {
-  if (EstimateTimestepMesh) return EstimateTimestepMesh(rc);
-  Real dt = std::numeric_limits<Real>::max();
-  if (EstimateTimestepBlock)
-    for (auto &mbd : rc->GetAllBlockData()) dt = std::min(dt, EstimateTimestepBlock(mbd.get()));
-  return dt;
 }
 
 }  // namespace parthenon

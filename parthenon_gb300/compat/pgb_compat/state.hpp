@@ -10,6 +10,7 @@
 
 #include <array>
 #include <functional>
+#include <limits>
 #include <map>
 #include <memory>
 #include <set>
@@ -28,6 +29,7 @@ template <typename T>
 class MeshBlockData;
 class Mesh;
 class MeshBlock;
+class ParameterInput;
 
 class MetadataFlag {
  public:
@@ -117,6 +119,22 @@ struct HistoryOutputVar {
 };
 using HstVar_list = std::vector<HistoryOutputVar>;
 inline const std::string hist_param_key = "HistoryFunctions";
+// src/outputs/outputs.hpp:108-133: a history function returning one value per component
+using HstVecFun_t = std::function<std::vector<Real>(MeshData<Real> *md)>;
+struct HistoryOutputVec {
+  UserHistoryOperation hst_op;
+  HstVecFun_t hst_vec_fun;
+  std::string label;
+  HistoryOutputVec(const UserHistoryOperation &op, const HstVecFun_t &f, const std::string &l)
+      : hst_op(op), hst_vec_fun(f), label(l) {}
+};
+using HstVec_list = std::vector<HistoryOutputVec>;
+inline const std::string hist_vec_param_key = "HistoryVectorFunctions";
+
+// src/utils/utils.hpp MakeVarLabel: the name of a sparse field, base name and sparse id
+inline std::string MakeVarLabel(const std::string &base, int sparse_id) {
+  return base + "_" + std::to_string(sparse_id);
+}
 
 // src/bvals/boundary_conditions.hpp: a user boundary condition of one block face
 using BValFunc = std::function<void(std::shared_ptr<MeshBlockData<Real>> &, bool)>;
@@ -155,32 +173,75 @@ class StateDescriptor {
 
   // a cell-centred field; returns false when the name is taken
   bool AddField(const std::string &name, const Metadata &m) {
-    for (const auto &f : fields_)
-      if (f.first == name) return false;
-    PARTHENON_REQUIRE_THROWS(m.IsSet(Metadata::Cell) || m.IsSet(Metadata::Face),
-                             "field " + name + ": only cell-centred and face fields are on this path");
-    PARTHENON_REQUIRE_THROWS(!m.IsSet(Metadata::Face) || !m.IsSet(Metadata::FillGhost),
-                             "field " + name + ": face fields are not exchanged on this path");
-    PARTHENON_REQUIRE_THROWS(!m.IsSet(Metadata::Sparse), "field " + name + ": sparse fields go through the C ABI");
-    fields_.emplace_back(name, m);
-    return true;
+    PARTHENON_REQUIRE_THROWS(!m.IsSet(Metadata::Sparse), "field " + name + ": sparse fields come from AddSparsePool");
+    return add_field(name, m);
+  }
+  // a sparse pool (state_descriptor.hpp:183-195, sparse_pool.hpp): one field per sparse
+  // id, named MakeVarLabel(base, id), with the pool's metadata and Metadata::Sparse. The
+  // layer allocates every id of the pool from the start (the reference allocates on
+  // demand), so AllocSparseID only checks the id and a pool field reads as a dense field.
+  bool AddSparsePool(const std::string &base, const Metadata &m_in, const std::vector<int> &sparse_ids) {
+    PARTHENON_REQUIRE_THROWS(!sparse_ids.empty(), "sparse pool " + base + " without ids");
+    Metadata m = m_in;
+    m.Set(Metadata::Sparse);
+    bool ok = true;
+    for (int id : sparse_ids) {
+      ok = add_field(MakeVarLabel(base, id), m) && ok;
+      sparse_ids_[base].push_back(id);
+    }
+    return ok;
+  }
+  // the sparse ids of a pool (empty for an unknown base name)
+  std::vector<int> SparseIds(const std::string &base) const {
+    auto it = sparse_ids_.find(base);
+    return it == sparse_ids_.end() ? std::vector<int>{} : it->second;
   }
   const std::vector<std::pair<std::string, Metadata>> &AllFields() const { return fields_; }
 
-  // hooks (state_descriptor.hpp:297-391)
+  // hooks (state_descriptor.hpp:297-391): the block version calls the block hook, the
+  // mesh version the mesh hook
+  void PreCommFillDerived(MeshBlockData<Real> *rc) const {
+    if (PreCommFillDerivedBlock) PreCommFillDerivedBlock(rc);
+  }
   void PreCommFillDerived(MeshData<Real> *rc) const {
     if (PreCommFillDerivedMesh) PreCommFillDerivedMesh(rc);
+  }
+  void PreFillDerived(MeshBlockData<Real> *rc) const {
+    if (PreFillDerivedBlock) PreFillDerivedBlock(rc);
   }
   void PreFillDerived(MeshData<Real> *rc) const {
     if (PreFillDerivedMesh) PreFillDerivedMesh(rc);
   }
+  void FillDerived(MeshBlockData<Real> *rc) const {
+    if (FillDerivedBlock) FillDerivedBlock(rc);
+  }
   void FillDerived(MeshData<Real> *rc) const {
     if (FillDerivedMesh) FillDerivedMesh(rc);
+  }
+  void PostFillDerived(MeshBlockData<Real> *rc) const {
+    if (PostFillDerivedBlock) PostFillDerivedBlock(rc);
   }
   void PostFillDerived(MeshData<Real> *rc) const {
     if (PostFillDerivedMesh) PostFillDerivedMesh(rc);
   }
-  Real EstimateTimestep(MeshData<Real> *rc) const;  // mesh.hpp: block hooks need the blocks
+  Real EstimateTimestep(MeshBlockData<Real> *rc) const {
+    return EstimateTimestepBlock ? EstimateTimestepBlock(rc) : std::numeric_limits<Real>::max();
+  }
+  Real EstimateTimestep(MeshData<Real> *rc) const {
+    return EstimateTimestepMesh ? EstimateTimestepMesh(rc) : std::numeric_limits<Real>::max();
+  }
+  AmrTag CheckRefinement(MeshBlockData<Real> *rc) const {
+    return CheckRefinementBlock ? CheckRefinementBlock(rc) : AmrTag::derefine;
+  }
+  void UserWorkBeforeLoop(Mesh *pmesh, ParameterInput *pin, SimTime &tm) const {
+    if (UserWorkBeforeLoopMesh) UserWorkBeforeLoopMesh(pmesh, pin, tm);
+  }
+  void PreStepDiagnostics(SimTime const &tm, MeshData<Real> *rc) const {
+    if (PreStepDiagnosticsMesh) PreStepDiagnosticsMesh(tm, rc);
+  }
+  void PostStepDiagnostics(SimTime const &tm, MeshData<Real> *rc) const {
+    if (PostStepDiagnosticsMesh) PostStepDiagnosticsMesh(tm, rc);
+  }
 
   std::function<void(MeshBlockData<Real> *rc)> PreCommFillDerivedBlock = nullptr;
   std::function<void(MeshData<Real> *rc)> PreCommFillDerivedMesh = nullptr;
@@ -193,11 +254,27 @@ class StateDescriptor {
   std::function<Real(MeshBlockData<Real> *rc)> EstimateTimestepBlock = nullptr;
   std::function<Real(MeshData<Real> *rc)> EstimateTimestepMesh = nullptr;
   std::function<AmrTag(MeshBlockData<Real> *rc)> CheckRefinementBlock = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime &)> UserWorkBeforeLoopMesh = nullptr;
+  std::function<void(Mesh *, ParameterInput *, SimTime &)> UserWorkBeforeOutputMesh = nullptr;
+  std::function<void(SimTime const &, MeshData<Real> *)> PreStepDiagnosticsMesh = nullptr;
+  std::function<void(SimTime const &, MeshData<Real> *)> PostStepDiagnosticsMesh = nullptr;
 
  private:
+  friend class Mesh;  // merges the packages' fields, sparse ones included
+  bool add_field(const std::string &name, const Metadata &m) {
+    for (const auto &f : fields_)
+      if (f.first == name) return false;
+    PARTHENON_REQUIRE_THROWS(m.IsSet(Metadata::Cell) || m.IsSet(Metadata::Face),
+                             "field " + name + ": only cell-centred and face fields are on this path");
+    PARTHENON_REQUIRE_THROWS(!m.IsSet(Metadata::Face) || !m.IsSet(Metadata::FillGhost),
+                             "field " + name + ": face fields are not exchanged on this path");
+    fields_.emplace_back(name, m);
+    return true;
+  }
   std::string label_;
   Params params_;
   std::vector<std::pair<std::string, Metadata>> fields_;
+  std::map<std::string, std::vector<int>> sparse_ids_;
 };
 
 class Packages_t {
