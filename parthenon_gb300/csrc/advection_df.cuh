@@ -49,20 +49,22 @@ __device__ __forceinline__ void plm_line_df(const StageArgs &a, int b, int v, in
     if (p < n) qn_d = ld(p + 2);  // the cell after next
     const df dqr = sub(qn, q0);
     const df dq2 = mul(dql, dqr);
-    df s = mul(dq2, recip(add(dql, dqr)));
+    // s, the flux F and its difference feed only sums and to_double (which adds a pair's
+    // halves exactly), so they stay unnormalised (dfloat.cuh mulu/subu)
+    df s = mulu(dq2, recip(add(dql, dqr)));
     if (!(dq2.hi > 0.0f)) s = make(0.0f);
     const df Lc = add(q0, s), Rc = sub(q0, s);
     dql = dqr;
     q0 = qn;
     if (p >= 0) {
-      const df F = mul(upwind_left ? Lprev : Rc, fac);
+      const df F = mulu(upwind_left ? Lprev : Rc, fac);
       if (MODE == kStoreFlux) {
         // face p of direction D, stored at the cell index of the cell on its right
         a.flux[(((int64_t)b * 3 + D) * NC + v) * cs + (e - ((int64_t)b * NC + v) * cs)] = to_double(F, ofl);
       } else {
         if (p >= 1) {
           const int64_t ec = e - step;  // cell p-1
-          double du = to_double(sub(F, AFprev), ofl);
+          double du = to_double(subu(F, AFprev), ofl);
           if (MODE == kStoreDu) {
             a.dudt[ec] = du;
           } else if (MODE == kAddDu) {

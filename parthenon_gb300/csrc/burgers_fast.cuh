@@ -147,10 +147,11 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           ca[fi] = make_float2(A.hi, A.lo);
           cb[fi] = make_float2(B.hi, B.lo);
           ci[fi] = make_float2(is.hi, is.lo);
-          F = dfl::scale(dfl::mul(dfl::add(dfl::mul(A, upl), dfl::mul(B, upr)), is), 0.5f);
+          F = dfl::scale(dfl::mul(dfl::norm(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr))), is), 0.5f);
         } else {
           const float2 A = ca[fi], B = cb[fi], is = ci[fi];
-          F = dfl::mul(dfl::add(dfl::mul(df{A.x, A.y}, lprev), dfl::mul(df{B.x, B.y}, qr)), df{is.x, is.y});
+          F = dfl::mul(dfl::norm(dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr))),
+                       df{is.x, is.y});
           F = dfl::scale(F, fhalf);
         }
         if (MODE == kStoreFlux) {
@@ -163,7 +164,8 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
         if (p >= 1 && live) {
           // dudt holds the scaled increments of the directions done so far (FP64)
           const int64_t e = c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step;
-          const double du = dfl::to_double(dfl::mul(dfl::sub(F, fprev), scale), odu);
+          // to_double adds the pair's two halves exactly, so the product may stay unnormalised
+          const double du = dfl::to_double(dfl::mulu(dfl::sub(F, fprev), scale), odu);
           if (MODE == kStoreDu) {
             a.dudt[e] = du;
           } else if (MODE == kAddDu) {

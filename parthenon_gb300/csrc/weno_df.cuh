@@ -69,7 +69,8 @@ struct Line {
   bool eps_only;  // eps exceeds every scaled indicator by far: B_k = 1 exactly
 };
 
-PGB_DF df t2_of(df d2) { return dfl::mul(dfl::sqr(d2), kThirteenThirds); }
+// (13/3) d2^2, feeding sums only: the product is left unnormalised
+PGB_DF df t2_of(df d2) { return dfl::mulu(dfl::sqr(d2), kThirteenThirds); }
 
 // Prime with q[p-2], q[p-1], q[p], q[p+1] of the first cell p and the line's scale.
 PGB_DF void prime(Line &w, double q0, double q1, double q2, double q3, int off) {
@@ -122,23 +123,23 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
     const int xmin = x0 < x1 ? (x0 < x2 ? x0 : x2) : (x1 < x2 ? x1 : x2);
     const int xmax = x0 > x1 ? (x0 > x2 ? x0 : x2) : (x1 > x2 ? x1 : x2);
     fast = xmax - xmin <= 40;
-    B0 = add(mul(tau, recip(be0)), 1.0f);
-    B1 = add(mul(tau, recip(be1)), 1.0f);
-    B2 = add(mul(tau, recip(be2)), 1.0f);
+    B0 = add(mulu(tau, recip(be0)), 1.0f);
+    B1 = add(mulu(tau, recip(be1)), 1.0f);
+    B2 = add(mulu(tau, recip(be2)), 1.0f);
   }
   // nonlinear weights (unnormalised) and their sums (g_k B_k >= 0.1 dominates eps)
-  const df l0 = add_dominant(mul(B0, kG0), kEpsF), l1 = add_dominant(mul(B1, kG1), kEpsF),
-           l2 = add_dominant(mul(B2, kG2), kEpsF);
-  const df r0 = add_dominant(mul(B2, kG0), kEpsF), r2 = add_dominant(mul(B0, kG2), kEpsF);
+  const df l0 = add_dominant(mulu(B0, kG0), kEpsF), l1 = add_dominant(mulu(B1, kG1), kEpsF),
+           l2 = add_dominant(mulu(B2, kG2), kEpsF);
+  const df r0 = add_dominant(mulu(B2, kG0), kEpsF), r2 = add_dominant(mulu(B0, kG2), kEpsF);
   const df SL = add(addu(l0, l1), l2);
   const df SR = add(addu(r0, l1), r2);
   const df isL = recip(SL), isR = recip(SR);
   // blending coefficients alpha_l = 3 E3/(E2 S_L) + eps, alpha_r likewise, and their
   // harmonic mean alpha_lin = 2 al ar / (al + ar)
   const df B12 = mul(B1, B2);
-  const df E2 = add(mul(B0, add(B1, B2)), B12);
+  const df E2 = add(mulu(B0, add(B1, B2)), B12);
   const df F3 = mul(mul(B0, B12), mul(recip(E2), 3.0f));
-  const df al = add(mul(F3, isL), kEpsF), ar = add(mul(F3, isR), kEpsF);
+  const df al = add(mulu(F3, isL), kEpsF), ar = add(mulu(F3, isR), kEpsF);
   const df alin = scale(mul(mul(al, ar), recip(add(al, ar))), 2.0f);
   // 6 (P_k - q2) for the candidate polynomials of both faces (recon.hpp:45-47,69-85)
   const df d0 = norm(subu(mulu(e1, 5.0f), scale(e0, 2.0f)));
@@ -147,8 +148,8 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df d0r = norm(subu(scale(e3, 2.0f), mulu(e2, 5.0f)));
   const df d1r = neg(norm(addu(scale(e1, 2.0f), e2)));
   const df d2r = norm(subu(e0, scale(e1, 4.0f)));
-  const df XL = mul(norm(addu(addu(mulu(l0, d0), mulu(l1, d1)), mulu(l2, d2))), mul(isL, kSixth));
-  const df XR = mul(norm(addu(addu(mulu(r0, d0r), mulu(l1, d1r)), mulu(r2, d2r))), mul(isR, kSixth));
+  const df XL = mulu(norm(addu(addu(mulu(l0, d0), mulu(l1, d1)), mulu(l2, d2))), mul(isL, kSixth));
+  const df XR = mulu(norm(addu(addu(mulu(r0, d0r), mulu(l1, d1r)), mulu(r2, d2r))), mul(isR, kSixth));
   // MC-limited slope (recon.hpp:27-40, 87-88): dq = sign(s) min(|s|/4, |e1|, |e2|) when
   // e1 and e2 have the same sign (both nonzero), else 0; s = e1 + e2 = b1
   const bool same = (e1.hi > 0.0f && e2.hi > 0.0f) || (e1.hi < 0.0f && e2.hi < 0.0f);
@@ -156,8 +157,8 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   df dq = b1.hi < 0.0f ? neg(mag) : mag;
   if (!same) dq = make(0.0f);
   // blend (recon.hpp:90-92) about q2
-  ql = norm(addu(w.q2, addu(dq, mul(alin, norm(subu(XL, dq))))));
-  qr = norm(addu(w.q2, subu(mul(alin, norm(addu(XR, dq))), dq)));
+  ql = norm(addu(w.q2, addu(dq, mulu(alin, norm(subu(XL, dq))))));
+  qr = norm(addu(w.q2, subu(mulu(alin, norm(addu(XR, dq))), dq)));
   // advance
   w.q3d = q4;
   w.q2 = w.q3;
