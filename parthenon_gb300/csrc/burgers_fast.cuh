@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
   const int nf = n + 1;
   const int nthreads = 32 * NC;
   const double bdt = a.beta * a.dt[0];
-  const float fhalf = comp < 3 ? 0.5f : 1.0f;  // velocity fluxes carry the 1/2 of u^2/2
+  // velocity fluxes carry the 1/2 of u^2/2: one more power of two in their conversion
+  const int fhalf_exp = comp < 3 ? 1 : 0;
 
   int it = 0;
   for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x, ++it) {
@@ -108,9 +109,9 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     const int off = wdf::line_offset(emax);
     if (producer) coef_off[buf][lane] = off;
     // the normal velocity's scale (fluxes are in units 2^(ou + off), increments in
-    // 2^(ou + off + os))
+    // 2^(ou + off + os); a velocity flux's 1/2 is one more power of two)
     const int ou = producer ? off : coef_off[buf][lane];
-    const int of = ou + off, odu = ou + off + os;
+    const int of = ou + off + fhalf_exp, odu = ou + off + os + fhalf_exp;
     wdf::Line wl;
     wdf::prime(wl, __ldg(u - 3 * step), __ldg(u - 2 * step), __ldg(u - step), __ldg(u), off);
     double qn = __ldg(u + step);  // q[p+2] of the first cell p = -1
@@ -141,18 +142,17 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           // velocity line is below 2^-127 and the face's coefficients vanish
           const bool stagnant = sl.hi == 0.0f || sr.hi == 0.0f;
           const float flag = stagnant ? dfl::pow2f(off) : 0.0f;
-          df is = dfl::recip(dfl::add(dfl::sub(sr, sl), flag));
+          df is = dfl::recip(dfl::add(dfl::subu(sr, sl), flag));  // sr >= 0 >= sl: no cancellation
           if (stagnant && off > 126) is = dfl::make(0.0f);
           const df A = dfl::mul(sr, dfl::sub(upl, sl)), B = dfl::mul(sl, dfl::sub(sr, upr));
           ca[fi] = make_float2(A.hi, A.lo);
           cb[fi] = make_float2(B.hi, B.lo);
           ci[fi] = make_float2(is.hi, is.lo);
-          F = dfl::scale(dfl::mul(dfl::norm(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr))), is), 0.5f);
+          F = dfl::mul(dfl::norm(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr))), is);
         } else {
           const float2 A = ca[fi], B = cb[fi], is = ci[fi];
           F = dfl::mul(dfl::norm(dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr))),
                        df{is.x, is.y});
-          F = dfl::scale(F, fhalf);
         }
         if (MODE == kStoreFlux) {
           // face p of direction D at the index of the cell on its right (multilevel path)

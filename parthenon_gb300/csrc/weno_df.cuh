@@ -10,8 +10,9 @@
 //   (g0 B2, g1 B1, g2 B0) + eps;
 //   the reference's D = g2 a0 a1 + g1 a0 a2 + g0 a1 a2 and a0 a1 a2 are, up to the
 //   weights' eps, g0 g1 g2 E2 and g0 g1 g2 E3 with E2 = B0B1 + B0B2 + B1B2 and
-//   E3 = B0B1B2, the same on both sides, so alpha_l = 3 E3 / (E2 S_L) + eps and
-//   alpha_r = 3 E3 / (E2 S_R) + eps;
+//   E3 = B0B1B2, the same on both sides, so alpha_l = 3 E3 / (E2 S_L) + eps,
+//   alpha_r = 3 E3 / (E2 S_R) + eps, and their harmonic mean, without the eps terms,
+//   alpha_lin = 6 E3 / (E2 (S_L + S_R));
 // and forms the face values about the cell value q2 from first differences
 // e_k = q[k+1] - q[k]: ql = q2 + dq + alin (XL - dq), qr = q2 - dq + alin (XR + dq),
 // XL = sum w_k (P_k - q2). Only the new difference e3 = q4 - q3 is an FP64 operation;
@@ -37,7 +38,6 @@ constexpr df kG0 = dfl::constant(0.1);
 constexpr df kG1 = dfl::constant(0.6);
 constexpr df kG2 = dfl::constant(0.3);
 constexpr df kThirteenThirds = dfl::constant(13.0 / 3.0);
-constexpr df kSixth = dfl::constant(1.0 / 6.0);
 // the reference's eps (robust.hpp EPS(): 10 DBL_EPSILON); as a float its relative error
 // (3e-8) changes sums with terms >= eps by less than 1e-22 of the term
 constexpr double kEpsD = 10.0 * 2.220446049250313080847e-16;
@@ -127,20 +127,26 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
     B1 = add(mulu(tau, recip(be1)), 1.0f);
     B2 = add(mulu(tau, recip(be2)), 1.0f);
   }
-  // nonlinear weights (unnormalised) and their sums (g_k B_k >= 0.1 dominates eps)
-  const df l0 = add_dominant(mulu(B0, kG0), kEpsF), l1 = add_dominant(mulu(B1, kG1), kEpsF),
-           l2 = add_dominant(mulu(B2, kG2), kEpsF);
-  const df r0 = add_dominant(mulu(B2, kG0), kEpsF), r2 = add_dominant(mulu(B0, kG2), kEpsF);
+  // nonlinear weights g_k B_k + eps (unnormalised) and their sums: g_k B_k >= 0.1, whose
+  // float ulp (2^-27) is far above eps (2e-15), so eps belongs to the low word alone
+  const auto weight = [](df B, df g) {
+    const df m = mulu(B, g);
+    return df{m.hi, fadd(m.lo, kEpsF)};
+  };
+  const df l0 = weight(B0, kG0), l1 = weight(B1, kG1), l2 = weight(B2, kG2);
+  const df r0 = weight(B2, kG0), r2 = weight(B0, kG2);
   const df SL = add(addu(l0, l1), l2);
   const df SR = add(addu(r0, l1), r2);
   const df isL = recip(SL), isR = recip(SR);
   // blending coefficients alpha_l = 3 E3/(E2 S_L) + eps, alpha_r likewise, and their
-  // harmonic mean alpha_lin = 2 al ar / (al + ar)
+  // harmonic mean alpha_lin = 2 al ar / (al + ar): without the two eps terms this is
+  // 6 E3 / (E2 (S_L + S_R)); leaving them out moves alpha_lin by about eps, i.e. the
+  // face value by about eps times the stencil's differences. a6 = alpha_lin / 6 (the
+  // candidate polynomials below carry the 6)
   const df B12 = mul(B1, B2);
   const df E2 = add(mulu(B0, add(B1, B2)), B12);
-  const df F3 = mul(mul(B0, B12), mul(recip(E2), 3.0f));
-  const df al = add(mulu(F3, isL), kEpsF), ar = add(mulu(F3, isR), kEpsF);
-  const df alin = scale(mul(mul(al, ar), recip(add(al, ar))), 2.0f);
+  const df E3 = mul(B0, B12);
+  const df a6 = mul(E3, recip(mul(E2, add(SL, SR))));
   // 6 (P_k - q2) for the candidate polynomials of both faces (recon.hpp:45-47,69-85)
   const df d0 = norm(subu(mulu(e1, 5.0f), scale(e0, 2.0f)));
   const df d1 = norm(addu(e1, scale(e2, 2.0f)));
@@ -148,17 +154,19 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df d0r = norm(subu(scale(e3, 2.0f), mulu(e2, 5.0f)));
   const df d1r = neg(norm(addu(scale(e1, 2.0f), e2)));
   const df d2r = norm(subu(e0, scale(e1, 4.0f)));
-  const df XL = mulu(norm(addu(addu(mulu(l0, d0), mulu(l1, d1)), mulu(l2, d2))), mul(isL, kSixth));
-  const df XR = mulu(norm(addu(addu(mulu(r0, d0r), mulu(l1, d1r)), mulu(r2, d2r))), mul(isR, kSixth));
+  // 6 XL, 6 XR: the weighted sums of 6 (P_k - q2)
+  const df XL6 = mulu(norm(addu(addu(mulu(l0, d0), mulu(l1, d1)), mulu(l2, d2))), isL);
+  const df XR6 = mulu(norm(addu(addu(mulu(r0, d0r), mulu(l1, d1r)), mulu(r2, d2r))), isR);
   // MC-limited slope (recon.hpp:27-40, 87-88): dq = sign(s) min(|s|/4, |e1|, |e2|) when
   // e1 and e2 have the same sign (both nonzero), else 0; s = e1 + e2 = b1
   const bool same = (e1.hi > 0.0f && e2.hi > 0.0f) || (e1.hi < 0.0f && e2.hi < 0.0f);
   const df mag = dmin(scale(dabs(b1), 0.25f), dmin(dabs(e1), dabs(e2)));
   df dq = b1.hi < 0.0f ? neg(mag) : mag;
   if (!same) dq = make(0.0f);
-  // blend (recon.hpp:90-92) about q2
-  ql = norm(addu(w.q2, addu(dq, mulu(alin, norm(subu(XL, dq))))));
-  qr = norm(addu(w.q2, subu(mulu(alin, norm(addu(XR, dq))), dq)));
+  // blend (recon.hpp:90-92) about q2: alpha_lin (XL - dq) = a6 (6 XL - 6 dq)
+  const df dq6 = mulu(dq, 6.0f);
+  ql = norm(addu(w.q2, addu(dq, mulu(a6, norm(subu(XL6, dq6))))));
+  qr = norm(addu(w.q2, subu(mulu(a6, norm(addu(XR6, dq6))), dq)));
   // advance
   w.q3d = q4;
   w.q2 = w.q3;
