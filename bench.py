@@ -199,12 +199,12 @@ DIVUPD_OPS = 12    # per component: 3 face differences, sum, /V, average, update
 
 
 # From one ncu capture of the three directional launches of a stage on the 128^3 mesh
-# (64 blocks of 32^3, 11 components): warp instructions executed (800.3 + 831.1 +
-# 856.2 M) and DRAM bytes read + written (427.0 + 679.8 + 942.3 MB), and one direct
+# (64 blocks of 32^3, 11 components): warp instructions executed (684.0 + 711.2 +
+# 736.6 M) and DRAM bytes read + written (432.2 + 677.6 + 947.8 MB), and one direct
 # exchange launch (319.6 MB). Instructions and traffic grow in proportion to the
 # blocks processed.
-STAGE_WARP_INSTR_PER_BLOCK = (800.3e6 + 831.1e6 + 856.2e6) / 64
-STAGE_DRAM_BYTES_PER_BLOCK = (427.0e6 + 679.8e6 + 942.3e6) / 64
+STAGE_WARP_INSTR_PER_BLOCK = (684.0e6 + 711.2e6 + 736.6e6) / 64
+STAGE_DRAM_BYTES_PER_BLOCK = (432.2e6 + 677.6e6 + 947.8e6) / 64
 EXCHANGE_DRAM_BYTES_PER_BLOCK = 319.6e6 / 64
 # instruction issue of a GB300: 152 SMs x 4 schedulers x one warp instruction per cycle
 ISSUE_PER_SM_CYCLE = 4
