@@ -210,12 +210,12 @@ PGB_DF df sqru(df a) {
   return {p.hi, ffma(fadd(a.hi, a.hi), a.lo, p.lo)};
 }
 
-// 1/a: single-precision seed r, residual 1 - a r formed exactly from two_prod, one
-// Newton correction (relative error about 2^-45)
+// 1/a: single-precision seed r, one Newton correction r + r (1 - a r) (relative error
+// about 2^-45). The residual 1 - a.hi r is about 2^-23 in size, so the FMA that forms it
+// rounds it with an error near 2^-47; a second FMA takes off a.lo r.
 PGB_DF df recip(df a) {
   const float r = frcp(a.hi);
-  const df p = two_prod(a.hi, r);                      // a.hi r exactly
-  const float res = fsub(fsub(fsub(1.0f, p.hi), p.lo), fmul(a.lo, r));  // 1 - a r
+  const float res = ffma(-a.lo, r, ffma(-a.hi, r, 1.0f));  // 1 - a r
   return fast_two_sum(r, fmul(r, res));
 }
 // a / b

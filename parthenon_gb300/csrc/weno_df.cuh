@@ -21,10 +21,10 @@
 // Each line is scaled by a power of two 2^off that brings its largest magnitude near 1
 // (the caller finds it), so every quantity fits the float exponent range whatever the
 // field's units; values below 2^-80 of the line's largest enter as zero. A cell falls
-// back to the reference expression in FP64 (weno5z_ref, the caller's job) when its
-// smoothness indicators spread over more than 2^40 while tau > 0 (a sub-stencil that
-// is exactly constant next to a jump): B_k would then leave the float range of the
-// products below.
+// back to the reference expression in FP64 (weno5z_ref, the caller's job) when tau > 0
+// and its smallest smoothness indicator lies below 2^-40 tau (a sub-stencil that is
+// exactly constant next to a jump): B_k = 1 + tau / beta_k would then exceed 2^40 and
+// take the products below out of the float range.
 #pragma once
 
 #include "dfloat.cuh"
@@ -51,9 +51,6 @@ PGB_DF double dsub(double a, double b) {
 #endif
 }
 
-// unbiased binary exponent of a float's high word
-PGB_DF int fexp(float f) { return (int)((dfl::f2u(f) >> 23) & 0xff) - 127; }
-
 // Power-of-two scale 2^off that brings the largest magnitude of a line of values into
 // [1, 2): off from the largest biased exponent field among them (0 for an all-zero line).
 PGB_DF int line_offset(int max_exp_field) { return max_exp_field == 0 ? 0 : 1023 - max_exp_field; }
@@ -63,14 +60,15 @@ struct Line {
   double q3d;     // q[p+1] in FP64, unscaled (the next difference is formed in FP64)
   df q2, q3;      // q[p], q[p+1]
   df e0, e1, e2;  // q[p-1]-q[p-2], q[p]-q[p-1], q[p+1]-q[p]
-  df t2a, t2b;    // (13/3) (second difference)^2 of cells p-1 and p
+  df t2a, t2b;    // (13/3) (second difference)^2 + eps of cells p-1 and p
   int off;        // scale exponent of the line
   float eps_b;    // the smoothness indicators' eps in scaled units (eps 2^(2 off))
   bool eps_only;  // eps exceeds every scaled indicator by far: B_k = 1 exactly
 };
 
-// (13/3) d2^2, feeding sums only: the product is left unnormalised
-PGB_DF df t2_of(df d2) { return dfl::mulu(dfl::sqr(d2), kThirteenThirds); }
+// (13/3) d2^2 + eps (the indicators' eps rides with the term each cell's three
+// indicators share along the line), feeding sums only: left unnormalised
+PGB_DF df t2_of(df d2, float eps_b) { return dfl::addu(dfl::mulu(dfl::sqr(d2), kThirteenThirds), eps_b); }
 
 // Prime with q[p-2], q[p-1], q[p], q[p+1] of the first cell p and the line's scale.
 PGB_DF void prime(Line &w, double q0, double q1, double q2, double q3, int off) {
@@ -87,8 +85,8 @@ PGB_DF void prime(Line &w, double q0, double q1, double q2, double q3, int off) 
   w.e0 = dfl::from_double(e0, off);
   w.e1 = dfl::from_double(e1, off);
   w.e2 = dfl::from_double(e2, off);
-  w.t2a = t2_of(dfl::sub(w.e1, w.e0));
-  w.t2b = t2_of(dfl::sub(w.e2, w.e1));
+  w.t2a = t2_of(dfl::sub(w.e1, w.e0), w.eps_b);
+  w.t2b = t2_of(dfl::sub(w.e2, w.e1), w.eps_b);
 }
 
 // Face values of cell p (ql at its right face, qr at its left face, scaled) given
@@ -106,23 +104,20 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   // unnormalised factor's larger lo would cost the product accuracy, and after a
   // cancellation a pair holds its value in lo).
   // smoothness indicators (recon.hpp:54-64 in first differences)
-  const df t2c = t2_of(norm(subu(e3, e2)));
+  const df t2c = t2_of(norm(subu(e3, e2)), w.eps_b);
   const df b0 = norm(subu(mulu(e1, 3.0f), e0));
   const df b1 = norm(addu(e1, e2));
   const df b2 = norm(subu(e3, mulu(e2, 3.0f)));
-  const df be0 = addu(addu(sqru(b0), w.t2a), w.eps_b);
-  const df be1 = addu(addu(sqru(b1), w.t2b), w.eps_b);
-  const df be2 = addu(addu(sqru(b2), t2c), w.eps_b);
+  const df be0 = addu(sqru(b0), w.t2a);
+  const df be1 = addu(sqru(b1), w.t2b);
+  const df be2 = addu(sqru(b2), t2c);
   const df tau = dabs(norm(subu(be2, be0)));
   bool fast = true;
   df B0 = make(1.0f), B1 = make(1.0f), B2 = make(1.0f);
   if (tau.hi != 0.0f && !w.eps_only) {
-    // B_k = 1 + tau / beta_k; a spread above 2^40 (a zero indicator included) would
-    // take the products below out of the float range
-    const int x0 = fexp(be0.hi), x1 = fexp(be1.hi), x2 = fexp(be2.hi);
-    const int xmin = x0 < x1 ? (x0 < x2 ? x0 : x2) : (x1 < x2 ? x1 : x2);
-    const int xmax = x0 > x1 ? (x0 > x2 ? x0 : x2) : (x1 > x2 ? x1 : x2);
-    fast = xmax - xmin <= 40;
+    // B_k = 1 + tau / beta_k; a B_k above 2^40 (a zero indicator included) would take
+    // the products below out of the float range
+    fast = fminf(fminf(be0.hi, be1.hi), be2.hi) >= fmul(tau.hi, 0x1p-40f);
     B0 = add(mulu(tau, recip(be0)), 1.0f);
     B1 = add(mulu(tau, recip(be1)), 1.0f);
     B2 = add(mulu(tau, recip(be2)), 1.0f);
