@@ -202,6 +202,73 @@ int main(int argc, char *argv[]) {
     }
     CHECK(threw);
   }
+  // ---- sparse pools, pack index lookups, regions, reducers, block/mesh hooks
+  {
+    StateDescriptor pkg("sparse");
+    CHECK(MakeVarLabel("rho", 12) == "rho_12");
+    CHECK(pkg.AddSparsePool("rho", Metadata({Metadata::Cell, Metadata::Derived}, {2}), {12, 37}));
+    const auto &f = pkg.AllFields();
+    CHECK(f.size() == 2 && f[0].first == "rho_12" && f[1].first == "rho_37");
+    CHECK(f[1].second.IsSet(Metadata::Sparse) && f[1].second.NumComponents() == 2);
+    CHECK(pkg.SparseIds("rho") == std::vector<int>({12, 37}) && pkg.SparseIds("none").empty());
+    bool threw = false;
+    try {
+      pkg.AddField("s", Metadata({Metadata::Cell, Metadata::Sparse}));  // sparse only through a pool
+    } catch (std::exception &) {
+      threw = true;
+    }
+    CHECK(threw);
+    PackIndexMap im;
+    im.insert("rho_37", 4, 5);
+    const bool by_id = im.get("rho", 37) == std::make_pair(4, 5);
+    const bool by_name = im.get("rho_37") == std::make_pair(4, 5);
+    const bool missing = im.get("rho", 12).first < 0;
+    CHECK(by_id && by_name && missing);
+    RegionSize rs;
+    rs.xmin(X1DIR) = -0.5;
+    rs.xmax(X3DIR) = 2.0;
+    rs.nx(X2DIR) = 64;
+    CHECK(rs.xmin_[0] == -0.5 && rs.xmax_[2] == 2.0 && rs.nx_[1] == 64);
+    // reducers: identities and joins (the space parameter selects nothing)
+    double mn = 0, sm = 0;
+    Kokkos::MinMaxScalar<double> mm{};
+    Kokkos::Min<double, HostExecSpace> rmin(mn);
+    Kokkos::Sum<double, HostExecSpace> rsum(sm);
+    Kokkos::MinMax<double> rmm(mm);
+    double a = rmin.identity();
+    rmin.join(a, 3.0);
+    rmin.join(a, -1.0);
+    double b = rsum.identity();
+    rsum.join(b, 2.5);
+    rsum.join(b, 0.5);
+    auto c = rmm.identity();
+    rmm.join(c, Kokkos::MinMaxScalar<double>{2.0, 2.0});
+    rmm.join(c, Kokkos::MinMaxScalar<double>{-3.0, 1.0});
+    CHECK(a == -1.0 && b == 3.0 && c.min_val == -3.0 && c.max_val == 2.0);
+    // hook dispatch: the block overloads call the block hooks, the mesh ones the mesh hooks
+    StateDescriptor h("hooks");
+    int nb = 0, nm = 0;
+    h.FillDerivedBlock = [&](MeshBlockData<Real> *) { ++nb; };
+    h.FillDerivedMesh = [&](MeshData<Real> *) { ++nm; };
+    h.EstimateTimestepBlock = [](MeshBlockData<Real> *) { return 0.25; };
+    h.FillDerived(static_cast<MeshBlockData<Real> *>(nullptr));
+    h.FillDerived(static_cast<MeshData<Real> *>(nullptr));
+    h.PostFillDerived(static_cast<MeshBlockData<Real> *>(nullptr));
+    CHECK(nb == 1 && nm == 1);
+    CHECK(h.EstimateTimestep(static_cast<MeshBlockData<Real> *>(nullptr)) == 0.25);
+    CHECK(h.EstimateTimestep(static_cast<MeshData<Real> *>(nullptr)) == std::numeric_limits<Real>::max());
+    CHECK(h.CheckRefinement(static_cast<MeshBlockData<Real> *>(nullptr)) == AmrTag::derefine);
+    // application hooks of the reference's ApplicationInput with their signatures
+    ApplicationInput app;
+    SimTime tm;
+    int calls = 0;
+    app.UserWorkAfterLoop = [&](Mesh *, ParameterInput *, SimTime &t) { calls += t.ncycle + 1; };
+    app.UserMeshWorkBeforeOutput = [&](Mesh *, ParameterInput *, SimTime const &) { ++calls; };
+    app.UserWorkAfterLoop(nullptr, nullptr, tm);
+    app.UserMeshWorkBeforeOutput(nullptr, nullptr, tm);
+    app.RegisterDefaultReflectingBoundaryConditions();
+    CHECK(calls == 2 && app.boundary_conditions[inner_x1].count("reflecting") == 1);
+  }
   std::printf(failures ? "FAILED\n" : "ok\n");
   return failures ? 1 : 0;
 }

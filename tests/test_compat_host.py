@@ -1,5 +1,6 @@
 """Host-side logic of the package-facing compatibility layer (task lists, input deck,
-parameters, metadata, integrator tables), built with nvcc and run on the CPU."""
+parameters, metadata, integrator tables, sparse pools, pack index lookups, reducers,
+package and application hooks), built with nvcc and run on the CPU."""
 import os
 import subprocess
 
