@@ -468,8 +468,20 @@ __global__ void __launch_bounds__(128) k_unpack(const DevPair *__restrict__ pair
   });
 }
 
+// The 2^e scaling of RestrictAverage's products: with the fine volume vol = 2^e
+// (-73 <= e <= 0), every product vol * u and every pairing sum of them is the 2^e
+// multiple of the plain pairing sum of the u, exactly, as long as each u is zero or has
+// a biased exponent in [74, 2042]: nonzero sums of such values are then at least
+// 2^-1001 (so their 2^e multiples stay normal) and below 2^1023. The mean then equals
+// the plain pairing sum times 1/8 bit for bit.
+__device__ __forceinline__ bool restrict_scalable(double u) {
+  const unsigned long long m = (unsigned long long)__double_as_longlong(u) & 0x7FFFFFFFFFFFFFFFull;
+  return m == 0 || (m >= (74ull << 52) && m < (2043ull << 52));
+}
+
 // RestrictAverage (pr_ops.hpp:105-164): volume-weighted mean of the 2x2x2 fine cells,
-// summed in the reference's pairing order.
+// summed in the reference's pairing order (on power-of-two volumes through the exact
+// shortcut above, which skips the eight products).
 // One warp per work item, components in turn.
 __global__ void __launch_bounds__(256) k_restrict(const DevRegion *__restrict__ regs,
                                                   const DevWork *__restrict__ work, int nwork,
@@ -482,30 +494,67 @@ __global__ void __launch_bounds__(256) k_restrict(const DevRegion *__restrict__ 
   const DevRegion r = regs[w.item];
   const double vol = geom[r.block].vol;
   const int ng = d.ng;
+  const double tv = __dadd_rn(__dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)),
+                              __dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)));
+  const unsigned long long vb = (unsigned long long)__double_as_longlong(vol);
+  const int vef = (int)((vb >> 52) & 0x7FF);  // biased exponent; sign 0 and e in [-73, 0]
+  const bool vol_pow2 = (vb & 0x800FFFFFFFFFFFFFull) == 0 && vef >= 1023 - 73 && vef <= 1023;
   for (int v = 0; v < ncomp; ++v) {
     if (alloc && !alloc[r.block * ncomp + v]) continue;  // unallocated sparse variable
     for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
       const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
       if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
       const int fi = (ci - ng) * 2 + ng, fj = (cj - ng) * 2 + ng, fk = (ck - ng) * 2 + ng;
-      double t[2][2][2];
+      double u[2][2][2];
+      bool fast = vol_pow2;
   #pragma unroll
       for (int ok = 0; ok < 2; ++ok)
   #pragma unroll
         for (int oj = 0; oj < 2; ++oj)
   #pragma unroll
-          for (int oi = 0; oi < 2; ++oi)
-            t[ok][oj][oi] = __dmul_rn(vol, fine[fine_index(d, ncomp, r.block, v, fk + ok, fj + oj, fi + oi)]);
-      const double tv = __dadd_rn(__dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)),
-                                  __dadd_rn(__dadd_rn(vol, vol), __dadd_rn(vol, vol)));
-      const double num = __dadd_rn(__dadd_rn(__dadd_rn(t[0][0][0], t[0][1][0]), __dadd_rn(t[0][0][1], t[0][1][1])),
-                                   __dadd_rn(__dadd_rn(t[1][0][0], t[1][1][0]), __dadd_rn(t[1][0][1], t[1][1][1])));
-      coarse[coarse_index(d, ncomp, r.block, v, ck, cj, ci)] = div_rn(num, tv);
+          for (int oi = 0; oi < 2; ++oi) {
+            u[ok][oj][oi] = fine[fine_index(d, ncomp, r.block, v, fk + ok, fj + oj, fi + oi)];
+            fast = fast && restrict_scalable(u[ok][oj][oi]);
+          }
+      double out;
+      if (fast) {
+        const double num = __dadd_rn(__dadd_rn(__dadd_rn(u[0][0][0], u[0][1][0]), __dadd_rn(u[0][0][1], u[0][1][1])),
+                                     __dadd_rn(__dadd_rn(u[1][0][0], u[1][1][0]), __dadd_rn(u[1][0][1], u[1][1][1])));
+        out = __dmul_rn(num, 0.125);
+      } else {
+        double t[2][2][2];
+  #pragma unroll
+        for (int ok = 0; ok < 2; ++ok)
+  #pragma unroll
+          for (int oj = 0; oj < 2; ++oj)
+  #pragma unroll
+            for (int oi = 0; oi < 2; ++oi) t[ok][oj][oi] = __dmul_rn(vol, u[ok][oj][oi]);
+        const double num = __dadd_rn(__dadd_rn(__dadd_rn(t[0][0][0], t[0][1][0]), __dadd_rn(t[0][0][1], t[0][1][1])),
+                                     __dadd_rn(__dadd_rn(t[1][0][0], t[1][1][0]), __dadd_rn(t[1][0][1], t[1][1][1])));
+        out = div_rn(num, tv);
+      }
+      coarse[coarse_index(d, ncomp, r.block, v, ck, cj, ci)] = out;
     });
   }
 }
 
 __device__ __forceinline__ double sign1(double x) { return x < 0.0 ? -1.0 : 1.0; }
+
+// The minmod slope 0.5 (sign1(a) + sign1(b)) smin(|a|, |b|) bit for bit, decided on the
+// bit patterns (integer pipe) for finite slopes: +-min(|a|, |b|) when both are negative
+// or neither is (a -0 counts as not negative), +0 otherwise; infinities and NaNs through
+// the FP64 form.
+__device__ __forceinline__ double minmod_slope(double a, double b) {
+  const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+  const unsigned long long ma = ua & 0x7FFFFFFFFFFFFFFFull, mb = ub & 0x7FFFFFFFFFFFFFFFull;
+  if (ma >= 0x7FF0000000000000ull || mb >= 0x7FF0000000000000ull)
+    return __dmul_rn(__dmul_rn(0.5, __dadd_rn(sign1(a), sign1(b))), smin(fabs(a), fabs(b)));
+  const bool na = (ua >> 63) != 0 && ma != 0, nb = (ub >> 63) != 0 && mb != 0;
+  if (na != nb) return 0.0;
+  const unsigned long long m = mb < ma ? mb : ma;  // smin: |b| when smaller, else |a|
+  return __longlong_as_double((long long)(na ? (m | 0x8000000000000000ull) : m));
+}
 
 // ProlongateSharedGeneral (pr_ops.hpp:166-285): op 0 minmod, 1 linear, 2 constant;
 // ops 3 and 4 are the linear and minmod ops in their uniform-spacing form (slopes a
@@ -551,7 +600,7 @@ __global__ void __launch_bounds__(256, 2) k_prolong(const DevRegion *__restrict_
             mq[q] = 0.25 * a;
             pq[q] = 0.25 * b;
           } else {
-            const double mm = (0.5 * (sign1(a) + sign1(b))) * smin(fabs(a), fabs(b));
+            const double mm = minmod_slope(a, b);
             mq[q] = 0.25 * mm;
             pq[q] = 0.25 * mm;
           }
