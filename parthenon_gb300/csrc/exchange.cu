@@ -482,14 +482,16 @@ __device__ __forceinline__ bool restrict_scalable(double u) {
 // RestrictAverage (pr_ops.hpp:105-164): volume-weighted mean of the 2x2x2 fine cells,
 // summed in the reference's pairing order (on power-of-two volumes through the exact
 // shortcut above, which skips the eight products).
-// One warp per work item, components in turn.
+// One warp per (work item, component): the regions are few and each cell is a short
+// dependent FP64 chain, so the warps of every component are needed to hide its latency.
 __global__ void __launch_bounds__(256) k_restrict(const DevRegion *__restrict__ regs,
                                                   const DevWork *__restrict__ work, int nwork,
                                                   const DevBlockGeom *__restrict__ geom, Dims d,
                                                   int ncomp, const double *__restrict__ fine,
                                                   double *__restrict__ coarse, const uint8_t *__restrict__ alloc) {
-  const int wi = warp_item();
-  if (wi >= nwork) return;
+  const int q = warp_item();
+  if (q >= nwork * ncomp) return;
+  const int wi = q / ncomp, v = q - wi * ncomp;
   const DevWork w = work[wi];
   const DevRegion r = regs[w.item];
   const double vol = geom[r.block].vol;
@@ -499,8 +501,8 @@ __global__ void __launch_bounds__(256) k_restrict(const DevRegion *__restrict__ 
   const unsigned long long vb = (unsigned long long)__double_as_longlong(vol);
   const int vef = (int)((vb >> 52) & 0x7FF);  // biased exponent; sign 0 and e in [-73, 0]
   const bool vol_pow2 = (vb & 0x800FFFFFFFFFFFFFull) == 0 && vef >= 1023 - 73 && vef <= 1023;
-  for (int v = 0; v < ncomp; ++v) {
-    if (alloc && !alloc[r.block * ncomp + v]) continue;  // unallocated sparse variable
+  if (alloc && !alloc[r.block * ncomp + v]) return;  // unallocated sparse variable
+  {
     for_item_rows(w.row0, w.nrows, r.box.n[0], r.box.n[1], threadIdx.x & 31, 32, [&](int k, int j, int i) {
       const int ck = r.box.lo[2] + k, cj = r.box.lo[1] + j, ci = r.box.lo[0] + i;
       if (!r.full_mask && !mask_active(r.mask, r.box, ck, cj, ci)) return;
@@ -561,19 +563,20 @@ __device__ __forceinline__ double minmod_slope(double a, double b) {
 // quarter of the differences).
 // Written with explicit round-to-nearest intrinsics so no FMA contraction changes
 // the result relative to the reference's separately rounded host arithmetic.
-// One warp per work item, components in turn.
+// One warp per (work item, component), as in k_restrict.
 __global__ void __launch_bounds__(256, 2) k_prolong(const DevRegion *__restrict__ regs,
                                                  const DevWork *__restrict__ work, int nwork,
                                                  const DevBlockGeom *__restrict__ geom, Dims d,
                                                  int ncomp, double *__restrict__ fine,
                                                  const double *__restrict__ coarse, int op,
                                                  const uint8_t *__restrict__ alloc) {
-  const int wi = warp_item();
-  if (wi >= nwork) return;
+  const int q0 = warp_item();
+  if (q0 >= nwork * ncomp) return;
+  const int wi = q0 / ncomp, v = q0 - wi * ncomp;
   const DevWork w = work[wi];
   const DevRegion r = regs[w.item];
-  for (int v = 0; v < ncomp; ++v) {
-    if (alloc && !alloc[r.block * ncomp + v]) continue;  // unallocated sparse variable
+  if (alloc && !alloc[r.block * ncomp + v]) return;  // unallocated sparse variable
+  {
     // geometry read through the pointer, and each direction's two slope products formed
     // as soon as they exist: keeps the kernel near 64 registers (4 CTAs of 8 warps)
     const DevBlockGeom *__restrict__ g = geom + r.block;
@@ -810,13 +813,16 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
                   int prolong_op, double *buffer, cudaStream_t s, const SparseDev *sp) {
   if (ncomp < 1 || ncomp > 65535) return fail(kErrInvalid, "ncomp out of range");
   if (!fine) return fail(kErrInvalid, "null field pointer");
+  // the transfer kernels index (work item, component) pairs with an int
+  const int64_t most = std::max<int64_t>(std::max<int64_t>(t.nrs_work, t.nrr_work), t.npro_work);
+  if (most * ncomp > 0x7FFFFFFF) return fail(kErrUnsupported, "too many transfer work items for one launch");
   if (t.multilevel && !coarse) return fail(kErrInvalid, "multilevel mesh needs a coarse buffer");
   if (sp && sp->ncomp != ncomp) return fail(kErrInvalid, "field components differ from the mesh's sparse variables");
   if (sp && buffer) return fail(kErrUnsupported, "the packed-buffer exchange does not take sparse variables");
   const uint8_t *alloc = sp ? sp->alloc : nullptr;
   const dim3 blk(128);
   if (t.multilevel && t.nrs_work)
-    k_restrict<<<warp_item_grid(t.nrs_work), 32 * kItemWarps, 0, s>>>(
+    k_restrict<<<warp_item_grid((int64_t)t.nrs_work * ncomp), 32 * kItemWarps, 0, s>>>(
         t.rs, t.rs_work, t.nrs_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
   if (sp) {
     int rc = sparse_exchange_copy(t, *sp, fine, coarse, ncomp, s);
@@ -839,10 +845,10 @@ int exchange_grid(GridTables &t, double *fine, double *coarse, int ncomp, int pr
     }
   }
   if (t.multilevel && t.nrr_work)
-    k_restrict<<<warp_item_grid(t.nrr_work), 32 * kItemWarps, 0, s>>>(
+    k_restrict<<<warp_item_grid((int64_t)t.nrr_work * ncomp), 32 * kItemWarps, 0, s>>>(
         t.rr, t.rr_work, t.nrr_work, t.geom, t.dims, ncomp, fine, coarse, alloc);
   if (t.multilevel && prolongate && t.npro_work)
-    k_prolong<<<warp_item_grid(t.npro_work), 32 * kItemWarps, 0, s>>>(
+    k_prolong<<<warp_item_grid((int64_t)t.npro_work * ncomp), 32 * kItemWarps, 0, s>>>(
         t.pro, t.pro_work, t.npro_work, t.geom, t.dims, ncomp, fine, coarse, prolong_op, alloc);
   PGB_CUDA(cudaGetLastError());
   return kOk;
