@@ -39,6 +39,9 @@ __device__ __forceinline__ void plm_line_df(const StageArgs &a, int b, int v, in
   const df fac = from_double(fac_d, ov);
   const int ofl = off + ov;  // units of fluxes and their differences
   const bool upwind_left = vel > 0.0;
+  // the update's factor -beta dt / vol, once per line (update modes only)
+  const bool stage1 = a.w_in == 1.0 && a.w_base == 0.0;
+  const double nbv = MODE == kStoreDu || MODE == kAddDu || MODE == kStoreFlux ? 0.0 : div_rn(-(a.beta * a.dt[0]), g.vol);
   df q0 = from_double(ld(-1), off);
   df dql = sub(q0, from_double(ld(-2), off));
   df Lprev = make(0.0f), AFprev = make(0.0f);
@@ -71,10 +74,10 @@ __device__ __forceinline__ void plm_line_df(const StageArgs &a, int b, int v, in
             a.dudt[ec] = a.dudt[ec] + du;
           } else {
             if (MODE == kFinishUpdate) du = a.dudt[ec] + du;
-            const double dudt = div_rn(-du, g.vol);
-            const double avg = a.w_in * __ldg(a.u_in + ec) + a.w_base * __ldg(a.u_base + ec);
-            const double bdt = a.beta * a.dt[0];
-            a.u_out[ec] = avg + bdt * dudt;
+            // stage 1 of RK2 averages with weights (1, 0): the average is u_in itself
+            const double avg = stage1 ? __ldg(a.u_in + ec)
+                                      : fma(a.w_in, __ldg(a.u_in + ec), a.w_base * __ldg(a.u_base + ec));
+            a.u_out[ec] = fma(nbv, du, avg);
           }
         }
         AFprev = F;

@@ -277,6 +277,7 @@ __global__ void __launch_bounds__(128) k_div_update(StageArgs a) {
 #ifndef PGB_EXACT_ARITH
   const double nbv = div_rn(-bdt, g.vol);
   const double s0 = nbv * g.area[0], s1 = nbv * g.area[1], s2 = nbv * g.area[2];
+  const bool stage1 = a.w_in == 1.0 && a.w_base == 0.0;
 #endif
 #pragma unroll
   for (int v = 0; v < NC; ++v) {
@@ -296,7 +297,8 @@ __global__ void __launch_bounds__(128) k_div_update(StageArgs a) {
 #else
     // avg + sum_d (-bdt area_d / vol) (F_high - F_low): the update folded into one
     // constant per direction (FP64 issue bounds this kernel)
-    const double avg = fma(a.w_in, a.u_in[e], a.w_base * a.u_base[e]);
+    // stage 1 of RK2 averages with weights (1, 0): the average is u_in itself
+    const double avg = stage1 ? a.u_in[e] : fma(a.w_in, a.u_in[e], a.w_base * a.u_base[e]);
     double out = fma(s0, F0[o + 1] - F0[o], avg);
     out = fma(s1, F1[o + N0] - F1[o], out);
     a.u_out[e] = fma(s2, F2[o + N01] - F2[o], out);
