@@ -294,29 +294,35 @@ __device__ __forceinline__ void jacobi_cell(const T *__restrict__ src, const T *
   jacobi_cell_f<kFast>(faces(src, d, nb, b, k, j, i), rhs, dst, d, cf, o, sw, fd, b, k, j, i);
 }
 
-// the sweep of one cell from its stencil values f
+// the swept value of cell c (global index) from its stencil values f and right-hand side
 template <bool kFast, class T>
-__device__ __forceinline__ void jacobi_cell_f(const Faces<T> &f, const T *__restrict__ rhs, T *__restrict__ dst,
-                                              const Dims &d, const MgCoef &cf, const MgOp &o, const MgSweep &sw,
-                                              const FaceD<T> &fd, int b, int k, int j, int i) {
+__device__ __forceinline__ T jacobi_value(const Faces<T> &f, T rhs_c, const Dims &d, const MgCoef &cf,
+                                          const MgOp &o, const MgSweep &sw, const FaceD<T> &fd, int64_t c) {
   const int64_t sj = d.N[0], sk = (int64_t)d.N[0] * d.N[1];
-  const int64_t c = cell_of(d, b, k, j, i);
   if constexpr (kFast) {
     T off, dg;
     fast_op(f, cf, o, fd, c, sj, sk, off, dg);
     if (fd.d0) {
       const T small = (T)10 * (sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN);
       const T den = dg + (dg >= (T)0 ? (T)1 : (T)-1) * small;
-      dst[c] = fma_t((T)sw.w / den, rhs[c] - off, (T)sw.omw * f.c);
-    } else {
-      dst[c] = fma_t((T)sw.wd, rhs[c] - off, (T)sw.omw * f.c);
+      return fma_t((T)sw.w / den, rhs_c - off, (T)sw.omw * f.c);
     }
+    return fma_t((T)sw.wd, rhs_c - off, (T)sw.omw * f.c);
   } else {
     const ExactOp e = exact_op(f, cf, o, fd, c, sj, sk);
     const double off = e.ax - e.dg * f.c;
-    const double val = rhs[c] - off;
-    dst[c] = sw.w * div_rn(val, e.den) + sw.omw * f.c;
+    const double val = rhs_c - off;
+    return sw.w * div_rn(val, e.den) + sw.omw * f.c;
   }
+}
+
+// the sweep of one cell from its stencil values f
+template <bool kFast, class T>
+__device__ __forceinline__ void jacobi_cell_f(const Faces<T> &f, const T *__restrict__ rhs, T *__restrict__ dst,
+                                              const Dims &d, const MgCoef &cf, const MgOp &o, const MgSweep &sw,
+                                              const FaceD<T> &fd, int b, int k, int j, int i) {
+  const int64_t c = cell_of(d, b, k, j, i);
+  dst[c] = jacobi_value<kFast>(f, rhs[c], d, cf, o, sw, fd, c);
 }
 
 // Ax + AddFieldsAndStoreInteriorSelect<rhs, temp, res_err>(1, -1): res = rhs - A u
@@ -718,6 +724,65 @@ __device__ void tail_smooth(const TailArgs &a, const TailGrid &g, int stages) {
   }
 }
 
+// The coarsest grid's extra sweeps (coarse_sweeps x stages passes) when it is one block
+// that tiles the periodic domain (its own face neighbour on all six sides) of at most
+// kTailSmemCells cells: the block's values and right-hand side sit in shared memory for
+// all the passes, so a pass costs a CTA barrier instead of a round trip to L2. Each
+// cell's value is the same expression (jacobi_value) as in tail_smooth; u ends with the
+// last pass's values, as there.
+constexpr int kTailSmemCells = 512;
+__shared__ double tail_sweep_smem[3 * kTailSmemCells];  // two sweep buffers and the rhs
+template <class T>
+__device__ bool tail_smem_fits(const TailGrid &g) {
+  const Dims &d = tview<T>(g).d;
+  for (int q = 0; q < 6; ++q)
+    if (g.nb[q] != g.slot) return false;
+  return d.nx[0] * d.nx[1] * d.nx[2] <= kTailSmemCells;
+}
+template <class T>
+__device__ void tail_coarse_sweeps_smem(const TailArgs &a, const TailGrid &g, double *smem) {
+  const StoreView<T> &v = tview<T>(g);
+  const Dims &d = v.d;
+  const int n0 = d.nx[0], n1 = d.nx[1], n2 = d.nx[2], per = n0 * n1 * n2, ng = d.ng;
+  T *s0 = reinterpret_cast<T *>(smem), *s1 = s0 + kTailSmemCells, *sr = s1 + kTailSmemCells;
+  for (int e = threadIdx.x; e < per; e += blockDim.x) {
+    const int i = e % n0, j = (e / n0) % n1, k = e / (n0 * n1);
+    const int64_t c = cell_of(d, g.slot, k + ng, j + ng, i + ng);
+    s0[e] = v.u[c];
+    sr[e] = v.rhs[c];
+  }
+  __syncthreads();
+  T *cur = s0, *nxt = s1;
+  for (int c = 0; c < a.coarse_sweeps; ++c)
+    for (int st = 0; st < a.stages; ++st) {
+      for (int e = threadIdx.x; e < per; e += blockDim.x) {
+        const int i = e % n0, j = (e / n0) % n1, k = e / (n0 * n1);
+        const int im = i > 0 ? i - 1 : n0 - 1, ip = i < n0 - 1 ? i + 1 : 0;
+        const int jm = j > 0 ? j - 1 : n1 - 1, jp = j < n1 - 1 ? j + 1 : 0;
+        const int km = k > 0 ? k - 1 : n2 - 1, kp = k < n2 - 1 ? k + 1 : 0;
+        Faces<T> f;
+        f.c = cur[e];
+        f.xm = cur[(k * n1 + j) * n0 + im];
+        f.xp = cur[(k * n1 + j) * n0 + ip];
+        f.ym = cur[(k * n1 + jm) * n0 + i];
+        f.yp = cur[(k * n1 + jp) * n0 + i];
+        f.zm = cur[(km * n1 + j) * n0 + i];
+        f.zp = cur[(kp * n1 + j) * n0 + i];
+        nxt[e] = jacobi_value<true>(f, sr[e], d, g.coef, a.o, g.sw[st], tfd<T>(g),
+                                    cell_of(d, g.slot, k + ng, j + ng, i + ng));
+      }
+      __syncthreads();
+      T *tmp = cur;
+      cur = nxt;
+      nxt = tmp;
+    }
+  for (int e = threadIdx.x; e < per; e += blockDim.x) {
+    const int i = e % n0, j = (e / n0) % n1, k = e / (n0 * n1);
+    v.u[cell_of(d, g.slot, k + ng, j + ng, i + ng)] = cur[e];
+  }
+  __syncthreads();
+}
+
 template <class T>
 __device__ void tail_error(const TailGrid &g) {
   const StoreView<T> &v = tview<T>(g);
@@ -750,7 +815,11 @@ __device__ void tail_down(const TailArgs &a, int t) {
       restrict_cell(v, tview<TP>(a.g[t + 1]), g.up, g.vol, e % h0, (e / h0) % h1, e / (h0 * h1));
     __syncthreads();
   } else {
-    for (int c = 0; c < a.coarse_sweeps; ++c) tail_smooth<T>(a, g, a.stages);
+    if (a.coarse_sweeps > 0 && tail_smem_fits<T>(g)) {
+      tail_coarse_sweeps_smem<T>(a, g, tail_sweep_smem);
+    } else {
+      for (int c = 0; c < a.coarse_sweeps; ++c) tail_smooth<T>(a, g, a.stages);
+    }
     // res = u (the coarsest level's post-smooth copy), then res = u - u0 below the top
     for_block(v.d, [&](int k, int j, int i) {
       const int64_t c = cell_of(v.d, g.slot, k, j, i);
@@ -1737,7 +1806,9 @@ struct VCycle {
   }
 
   // The highest level of the trailing one-block grids that k_mg_tail takes (the fast
-  // build), or lmin - 1 when fewer than two qualify.
+  // build), or lmin - 1 when none qualifies. A single one takes it too: the coarsest
+  // grid's smoothing passes (2 + 2 and the extra coarse sweeps, about 35 launches of a
+  // few microseconds) then run in one launch.
   int tail_top() const {
     int top = g->lmin - 1;
     for (int L = g->lmin; L <= g->lmax; ++L) {
@@ -1747,7 +1818,7 @@ struct VCycle {
       top = L;
     }
     const int n = top - g->lmin + 1;
-    return (n >= 2 && n <= kTailMax) ? top : g->lmin - 1;
+    return (n >= 1 && n <= kTailMax) ? top : g->lmin - 1;
   }
 
   int tail(int top) {
