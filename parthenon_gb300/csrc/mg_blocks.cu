@@ -655,7 +655,7 @@ __global__ void __launch_bounds__(256) k_mgf_prolong(const double *__restrict__ 
 // of about a dozen launches per grid. Fast build only, grids of at most 8^3 cells (the
 // 16^3 grid in the CTA made the mixed iteration slower on the refined 128^3 mesh: 0.85
 // ms against 0.82 ms). Measured there: the FP64 V-cycle 1.19 ms with it, 1.22 ms
-// without. On the uniform 128^3 mesh the one 8^3 grid's 2 + 16 x 2 + 2 sweeps run from
+// without. On the uniform 128^3 mesh the one 8^3 grid's 16 x 2 extra sweeps run from
 // shared memory (tail_coarse_sweeps_smem): FP64 solve 11.9 -> 11.6 ms.
 constexpr int kTailMax = 8;
 constexpr int kTailThreads = 1024;
