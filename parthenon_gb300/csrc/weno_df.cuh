@@ -99,15 +99,18 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df q4p = from_double(q4, w.off);
   const df e0 = w.e0, e1 = w.e1, e2 = w.e2;
   // Sums and the products that only feed sums keep their pairs unnormalised
-  // (dfloat.cuh addu/mulu/sqru, from normalised operands); every pair that enters a
-  // product, a sign test, a comparison or a reciprocal is normalised first (an
-  // unnormalised factor's larger lo would cost the product accuracy, and after a
-  // cancellation a pair holds its value in lo).
+  // (dfloat.cuh addu/mulu/sqru); a pair that enters a sign test, a comparison or a
+  // reciprocal is normalised first (after a cancellation a pair holds its value in lo).
+  // The first-difference combinations b0, b2 and d* enter products unnormalised: a
+  // product drops lo*lo, which is at most 2^-46 of the product when lo is within a few
+  // ulp of hi, and after a cancellation (hi near zero, the value in lo) is below 2^-46 of
+  // the differences that cancelled, so the face values keep their accuracy relative to
+  // the stencil's differences.
   // smoothness indicators (recon.hpp:54-64 in first differences)
   const df t2c = t2_of(norm(subu(e3, e2)), w.eps_b);
-  const df b0 = norm(subu(mulu(e1, 3.0f), e0));
+  const df b0 = subu(mulu(e1, 3.0f), e0);
   const df b1 = norm(addu(e1, e2));
-  const df b2 = norm(subu(e3, mulu(e2, 3.0f)));
+  const df b2 = subu(e3, mulu(e2, 3.0f));
   const df be0 = addu(sqru(b0), w.t2a);
   const df be1 = addu(sqru(b1), w.t2b);
   const df be2 = addu(sqru(b2), t2c);
@@ -143,12 +146,12 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df E3 = mul(B0, B12);
   const df a6 = mul(E3, recip(mul(E2, add(SL, SR))));
   // 6 (P_k - q2) for the candidate polynomials of both faces (recon.hpp:45-47,69-85)
-  const df d0 = norm(subu(mulu(e1, 5.0f), scale(e0, 2.0f)));
-  const df d1 = norm(addu(e1, scale(e2, 2.0f)));
-  const df d2 = norm(subu(scale(e2, 4.0f), e3));
-  const df d0r = norm(subu(scale(e3, 2.0f), mulu(e2, 5.0f)));
-  const df d1r = neg(norm(addu(scale(e1, 2.0f), e2)));
-  const df d2r = norm(subu(e0, scale(e1, 4.0f)));
+  const df d0 = subu(mulu(e1, 5.0f), scale(e0, 2.0f));
+  const df d1 = addu(e1, scale(e2, 2.0f));
+  const df d2 = subu(scale(e2, 4.0f), e3);
+  const df d0r = subu(scale(e3, 2.0f), mulu(e2, 5.0f));
+  const df d1r = neg(addu(scale(e1, 2.0f), e2));
+  const df d2r = subu(e0, scale(e1, 4.0f));
   // 6 XL, 6 XR: the weighted sums of 6 (P_k - q2)
   const df XL6 = mulu(norm(addu(addu(mulu(l0, d0), mulu(l1, d1)), mulu(l2, d2))), isL);
   const df XR6 = mulu(norm(addu(addu(mulu(r0, d0r), mulu(l1, d1r)), mulu(r2, d2r))), isR);
