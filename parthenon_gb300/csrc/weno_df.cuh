@@ -68,7 +68,7 @@ struct Line {
 
 // (13/3) d2^2 + eps (the indicators' eps rides with the term each cell's three
 // indicators share along the line), feeding sums only: left unnormalised
-PGB_DF df t2_of(df d2, float eps_b) { return dfl::addu(dfl::mulu(dfl::sqr(d2), kThirteenThirds), eps_b); }
+PGB_DF df t2_of(df d2, float eps_b) { return dfl::addu(dfl::mulu(dfl::sqru(d2), kThirteenThirds), eps_b); }
 
 // Prime with q[p-2], q[p-1], q[p], q[p+1] of the first cell p and the line's scale.
 PGB_DF void prime(Line &w, double q0, double q1, double q2, double q3, int off) {
@@ -101,13 +101,15 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   // Sums and the products that only feed sums keep their pairs unnormalised
   // (dfloat.cuh addu/mulu/sqru); a pair that enters a sign test, a comparison or a
   // reciprocal is normalised first (after a cancellation a pair holds its value in lo).
-  // The first-difference combinations b0, b2 and d* enter products unnormalised: a
-  // product drops lo*lo, which is at most 2^-46 of the product when lo is within a few
-  // ulp of hi, and after a cancellation (hi near zero, the value in lo) is below 2^-46 of
-  // the differences that cancelled, so the face values keep their accuracy relative to
-  // the stencil's differences.
+  // Several pairs also enter products unnormalised (the first-difference combinations
+  // b0, b2 and d*, the second difference of t2, B_k, the weighted sums and the blend's
+  // differences): a product drops lo*lo, which is at most 2^-46 of the product when lo
+  // is within a few ulp of hi, and after a cancellation (hi near zero, the value in lo)
+  // is below 2^-46 of the differences that cancelled. Face values stay within 2e-14 of
+  // the line's magnitude (the host test's bar is 3e-14); leaving the products of the B_k
+  // (E2, E3) unnormalised as well took that to 2.7e-14, so those stay normalised.
   // smoothness indicators (recon.hpp:54-64 in first differences)
-  const df t2c = t2_of(norm(subu(e3, e2)), w.eps_b);
+  const df t2c = t2_of(subu(e3, e2), w.eps_b);
   const df b0 = subu(mulu(e1, 3.0f), e0);
   const df b1 = norm(addu(e1, e2));
   const df b2 = subu(e3, mulu(e2, 3.0f));
@@ -121,9 +123,9 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
     // B_k = 1 + tau / beta_k; a B_k above 2^40 (a zero indicator included) would take
     // the products below out of the float range
     fast = fminf(fminf(be0.hi, be1.hi), be2.hi) >= fmul(tau.hi, 0x1p-40f);
-    B0 = add(mulu(tau, recip(be0)), 1.0f);
-    B1 = add(mulu(tau, recip(be1)), 1.0f);
-    B2 = add(mulu(tau, recip(be2)), 1.0f);
+    B0 = addu(mulu(tau, recip(be0)), 1.0f);
+    B1 = addu(mulu(tau, recip(be1)), 1.0f);
+    B2 = addu(mulu(tau, recip(be2)), 1.0f);
   }
   // nonlinear weights g_k B_k + eps (unnormalised) and their sums: g_k B_k >= 0.1, whose
   // float ulp (2^-27) is far above eps (2e-15), so eps belongs to the low word alone
@@ -153,8 +155,8 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df d1r = neg(addu(scale(e1, 2.0f), e2));
   const df d2r = subu(e0, scale(e1, 4.0f));
   // 6 XL, 6 XR: the weighted sums of 6 (P_k - q2)
-  const df XL6 = mulu(norm(addu(addu(mulu(l0, d0), mulu(l1, d1)), mulu(l2, d2))), isL);
-  const df XR6 = mulu(norm(addu(addu(mulu(r0, d0r), mulu(l1, d1r)), mulu(r2, d2r))), isR);
+  const df XL6 = mulu(addu(addu(mulu(l0, d0), mulu(l1, d1)), mulu(l2, d2)), isL);
+  const df XR6 = mulu(addu(addu(mulu(r0, d0r), mulu(l1, d1r)), mulu(r2, d2r)), isR);
   // MC-limited slope (recon.hpp:27-40, 87-88): dq = sign(s) min(|s|/4, |e1|, |e2|) when
   // e1 and e2 have the same sign (both nonzero), else 0; s = e1 + e2 = b1
   const bool same = (e1.hi > 0.0f && e2.hi > 0.0f) || (e1.hi < 0.0f && e2.hi < 0.0f);
@@ -163,8 +165,8 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   if (!same) dq = make(0.0f);
   // blend (recon.hpp:90-92) about q2: alpha_lin (XL - dq) = a6 (6 XL - 6 dq)
   const df dq6 = mulu(dq, 6.0f);
-  ql = norm(addu(w.q2, addu(dq, mulu(a6, norm(subu(XL6, dq6))))));
-  qr = norm(addu(w.q2, subu(mulu(a6, norm(addu(XR6, dq6))), dq)));
+  ql = norm(addu(w.q2, addu(dq, mulu(a6, subu(XL6, dq6)))));
+  qr = norm(addu(w.q2, subu(mulu(a6, addu(XR6, dq6)), dq)));
   // advance
   w.q3d = q4;
   w.q2 = w.q3;
