@@ -148,11 +148,12 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           ca[fi] = make_float2(A.hi, A.lo);
           cb[fi] = make_float2(B.hi, B.lo);
           ci[fi] = make_float2(is.hi, is.lo);
-          F = dfl::mul(dfl::norm(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr))), is);
+          F = dfl::mul(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr)), is);
         } else {
           const float2 A = ca[fi], B = cb[fi], is = ci[fi];
-          F = dfl::mul(dfl::norm(dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr))),
-                       df{is.x, is.y});
+          // A L + B R may cancel; the product then drops a lo*lo below 2^-46 of the terms
+          // that cancelled, as does the increment's product below
+          F = dfl::mul(dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr)), df{is.x, is.y});
         }
         if (MODE == kStoreFlux) {
           // face p of direction D at the index of the cell on its right (multilevel path)
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           // dudt holds the scaled increments of the directions done so far (FP64)
           const int64_t e = c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step;
           // to_double adds the pair's two halves exactly, so the product may stay unnormalised
-          const double du = dfl::to_double(dfl::mulu(dfl::sub(F, fprev), scale), odu);
+          const double du = dfl::to_double(dfl::mulu(dfl::subu(F, fprev), scale), odu);
           if (MODE == kStoreDu) {
             a.dudt[e] = du;
           } else if (MODE == kAddDu) {
