@@ -156,8 +156,8 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": float(np.median(sm)), "sm_min_mhz": min(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def measured_peaks():
@@ -199,12 +199,12 @@ DIVUPD_OPS = 12    # per component: 3 face differences, sum, /V, average, update
 
 
 # From one ncu capture of the three directional launches of a stage on the 128^3 mesh
-# (64 blocks of 32^3, 11 components): warp instructions executed (684.0 + 711.2 +
-# 736.6 M) and DRAM bytes read + written (432.2 + 677.6 + 947.8 MB), and one direct
+# (64 blocks of 32^3, 11 components): warp instructions executed (604.4 + 630.8 +
+# 656.2 M) and DRAM bytes read + written (436.3 + 675.6 + 948.7 MB), and one direct
 # exchange launch (319.6 MB). Instructions and traffic grow in proportion to the
 # blocks processed.
-STAGE_WARP_INSTR_PER_BLOCK = (684.0e6 + 711.2e6 + 736.6e6) / 64
-STAGE_DRAM_BYTES_PER_BLOCK = (432.2e6 + 677.6e6 + 947.8e6) / 64
+STAGE_WARP_INSTR_PER_BLOCK = (604.4e6 + 630.8e6 + 656.2e6) / 64
+STAGE_DRAM_BYTES_PER_BLOCK = (436.3e6 + 675.6e6 + 948.7e6) / 64
 EXCHANGE_DRAM_BYTES_PER_BLOCK = 319.6e6 / 64
 # instruction issue of a GB300: 152 SMs x 4 schedulers x one warp instruction per cycle
 ISSUE_PER_SM_CYCLE = 4
@@ -329,22 +329,23 @@ def run_ours(args, ws, rank):
     nat.check(L.pgb_run_host_dt(mesh.handle, ctypes.byref(p), ctypes.c_void_p(host_in.data_ptr()),
                                 ctypes.c_void_p(host_out.data_ptr()), NCOMP, args.warmup, ctypes.byref(dt_h),
                                 dt_steps), "pgb_run_host_dt")
-    # the median of three timed calls (host-side variation between calls is a few %)
+    # the median of three timed calls, with the clocks they ran at
     e2e_runs = []
-    for _ in range(3):
-        dt_h = ctypes.c_double(0.0)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        nat.check(L.pgb_run_host_dt(mesh.handle, ctypes.byref(p), ctypes.c_void_p(host_in.data_ptr()),
-                                    ctypes.c_void_p(host_out.data_ptr()), NCOMP, e2e_steps, ctypes.byref(dt_h),
-                                    dt_steps), "pgb_run_host_dt")
-        e2e_runs.append(time.perf_counter() - t0)
+    with ClockSampler(dev) as e2e_clk:
+        for _ in range(3):
+            dt_h = ctypes.c_double(0.0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            nat.check(L.pgb_run_host_dt(mesh.handle, ctypes.byref(p), ctypes.c_void_p(host_in.data_ptr()),
+                                        ctypes.c_void_p(host_out.data_ptr()), NCOMP, e2e_steps, ctypes.byref(dt_h),
+                                        dt_steps), "pgb_run_host_dt")
+            e2e_runs.append(time.perf_counter() - t0)
     e2e_s = sorted(e2e_runs)[1]
     nat.check(L.pgb_release_host_workspace(mesh.handle), "pgb_release_host_workspace")
     nbytes = state.nbytes
     e2e = {"value": ws * e2e_steps * zones / e2e_s, "unit": METRIC, "h2d_bytes_per_step": nbytes / e2e_steps,
            "d2h_bytes_per_step": nbytes / e2e_steps + 8, "steps": e2e_steps,
-           "calls_s": [round(x, 4) for x in e2e_runs],
+           "calls_s": [round(x, 4) for x in e2e_runs], "clocks": e2e_clk.summary(),
            "note": "pgb_run_host_dt with host buffers: H2D of the initial field (2.9 GB, pinned), ghost fill, "
                    "initial dt, K cycles (the mesh's cycle graph) each followed by a D2H of that step's dt, D2H of "
                    "the final field; the state stays resident between steps; the mesh's device workspace was "
