@@ -123,6 +123,41 @@ def test_line_matches_reference(lib, name):
     assert np.abs(qr[2:-2] - rr).max() <= TOL * scale
 
 
+def _random_lines(count=100, seed=5):
+    """Seeded lines of five kinds (signed noise, sinusoids of random wavenumber and
+    phase, a random walk about 1, sparse spikes on 1, Gaussians of random width), each
+    scaled by a random power of ten in [1e-5, 1e5]."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0, 1, 200)
+    out = []
+    for t in range(count):
+        kind = t % 5
+        if kind == 0:
+            q = rng.standard_normal(200)
+        elif kind == 1:
+            q = np.sin(2 * np.pi * rng.uniform(1, 20) * x + rng.uniform(0, 6))
+        elif kind == 2:
+            q = np.cumsum(rng.standard_normal(200)) * 0.01 + 1.0
+        elif kind == 3:
+            q = np.where(rng.random(200) < 0.05, rng.standard_normal(200) * 5, 0.0) + 1.0
+        else:
+            q = np.exp(-((x - rng.uniform(0.2, 0.8)) / rng.uniform(0.01, 0.2)) ** 2)
+        out.append(q * 10.0 ** rng.uniform(-5, 5))
+    return out
+
+
+def test_random_lines_match_reference(lib):
+    worst = 0.0
+    for q in _random_lines():
+        q = np.ascontiguousarray(q, np.float64)
+        ql, qr = np.zeros(q.size), np.zeros(q.size)
+        lib.pgb_test_weno_line(_p(q), q.size, _p(ql), _p(qr))
+        rl, rr = weno5z_numpy(q)
+        scale = np.abs(q).max()
+        worst = max(worst, np.abs(ql[2:-2] - rl).max() / scale, np.abs(qr[2:-2] - rr).max() / scale)
+    assert worst <= TOL
+
+
 @pytest.mark.parametrize("name", ["uniform-noise", "constant-with-box", "shock-on-slope"])
 def test_fp64_fallback_is_the_reference_expression(lib, name):
     q = np.ascontiguousarray(LINES[name], np.float64)
