@@ -176,7 +176,7 @@ class EvolutionDriver : public Driver {
   int64_t zone_cycles = 0;
 };
 
-// low_storage_integrator.cpp: rk1, rk2, vl2, rk3 (gamma_0, gamma_1, beta, delta, c)
+// low_storage_integrator.cpp: rk1, rk2, vl2, rk3, rk4 (gamma_0, gamma_1, beta, delta, c)
 class LowStorageIntegrator {
  public:
   explicit LowStorageIntegrator(const std::string &name) : name_(name) {
@@ -189,8 +189,16 @@ class LowStorageIntegrator {
     } else if (name == "rk3") {
       set(3, {1.0, 0.0, 0.0}, {1.0, 0.25, 2.0 / 3.0}, {0.0, 0.25, 2.0 / 3.0}, {1.0, 0.75, 1.0 / 3.0},
           {0.0, 1.0, 0.5});
+    } else if (name == "rk4") {
+      // the 5-stage SSPRK(5)4 in 2S* low-storage form, Ketcheson, J. Comput. Phys. 229
+      // (2010) 1763-1773, Table 4 (the published coefficients, as the reference uses)
+      set(5, {1.0, 0.0, 0.0, 0.0, 0.0},
+          {0.357534921136978, 2.364680399061355, 0.016239790859612, 0.498173799587251, 0.433334235669763},
+          {0.0, -3.666545952121251, 0.035802535958088, 4.398279365655791, 0.770411587328417},
+          {1.0, 4.666545952121251, 0.964197464041912, -3.398279365655790, 0.229588412671583},
+          {0.0, 0.357534921136978, 1.0537621812245777, 0.05396714924417825, 0.7355363985311864});
     } else {
-      PARTHENON_THROW("unknown integrator " + name + " (rk1, rk2, vl2, rk3)");
+      PARTHENON_THROW("unknown integrator " + name + " (rk1, rk2, vl2, rk3, rk4)");
     }
     // staged_integrator.cpp MakePeriodicNames_: base, "1", ..., base
     stage_name.resize(nstages + 1);

@@ -3,6 +3,7 @@
 // and its command-line overrides, typed package parameters, Metadata flags, the
 // integrator tables. Prints the failed check and exits non-zero on a mismatch.
 // Test infrastructure.
+#include <cmath>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -113,6 +114,36 @@ int main(int argc, char *argv[]) {
     CHECK(rk2.nstages == 2 && rk2.beta[0] == 1.0 && rk2.beta[1] == 0.5);
     CHECK(rk2.stage_name[0] == "base" && rk2.stage_name[1] == "1" && rk2.stage_name[2] == "base");
     CHECK(rk3.nstages == 3 && rk3.gam0[2] == 2.0 / 3.0 && rk3.stage_name[2] == "2");
+  }
+  // ---- the low-storage tables on the reference's known-answer problem
+  // (tst/unit/test_unit_integrators.cpp:38-228): the harmonic oscillator u'' = -(2 pi)^2 u
+  // from (1, 0) to t = 1.15 with the 2S* stage update S0 = gam0 S0 + gam1 S1 + beta dt
+  // rhs(S0) (S1 the state at the start of the step), within 1e-2 of cos / -2 pi sin
+  {
+    const double K = 2.0 * M_PI, tf = 1.15;
+    const struct {
+      const char *name;
+      double dt;
+    } cases[] = {{"rk1", 1e-5}, {"rk2", 1e-3}, {"vl2", 1e-3}, {"rk3", 1e-2}, {"rk4", 1e-2}};
+    for (const auto &cs : cases) {
+      LowStorageIntegrator in(cs.name);
+      double u[2] = {1.0, 0.0};
+      auto step = [&](double dt) {
+        const double s1[2] = {u[0], u[1]};
+        for (int st = 0; st < in.nstages; ++st) {
+          const double rhs[2] = {u[1], -K * K * u[0]};
+          for (int v = 0; v < 2; ++v) u[v] = in.gam0[st] * u[v] + in.gam1[st] * s1[v] + in.beta[st] * dt * rhs[v];
+        }
+      };
+      const int nt = (int)std::ceil(tf / cs.dt);
+      double t = 0;
+      for (int i = 0; i < nt; ++i, t += cs.dt) step(cs.dt);
+      if (t < tf && std::abs(tf - t) > 1e-12) step(tf - t);
+      const bool ok0 = std::abs(u[0] - std::cos(K * tf)) <= 1e-2, ok1 = std::abs(u[1] + K * std::sin(K * tf)) <= 1e-2;
+      CHECK(ok0 && ok1);
+    }
+    LowStorageIntegrator rk4("rk4");
+    CHECK(rk4.nstages == 5 && rk4.stage_name.size() == 6 && rk4.stage_name[4] == "4");
   }
   // ---- task qualifiers, labels, member-function tasks, iterating sublists
   {
