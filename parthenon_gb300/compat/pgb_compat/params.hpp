@@ -1,7 +1,7 @@
 // Package-facing compatibility layer: Params (typed package parameters) and
 // ParameterInput (the input deck).
 //
-// Reference: src/interface/params.hpp (Params::Add/Get/GetMutable/Update/hasKey),
+// Reference: src/interface/params.hpp (Params::Add/Get/GetMutable/Update/hasKey/reset),
 // src/parameter_input.hpp (ParameterInput: <block> sections of `key = value` lines,
 // `#` comments, `&` continuation lines; Get*/GetOrAdd*/Set*/CheckRequired/CheckDesired;
 // command-line overrides `block/key=value`).
@@ -53,6 +53,8 @@ class Params {
     *GetMutable<T>(key) = std::move(value);
   }
   bool hasKey(const std::string &key) const { return entries_.count(key) > 0; }
+  // removes every parameter (params.hpp Params::reset)
+  void reset() { entries_.clear(); }
 
  private:
   struct Entry {

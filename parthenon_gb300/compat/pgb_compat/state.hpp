@@ -88,6 +88,9 @@ class Metadata {
     has_refinement_ops_ = true;
   }
   bool HasRefinementOps() const { return has_refinement_ops_; }
+  // metadata.hpp operator==: the same flags and the same shape
+  bool operator==(const Metadata &o) const { return flags_ == o.flags_ && shape_ == o.shape_; }
+  bool operator!=(const Metadata &o) const { return !(*this == o); }
 
  private:
   std::set<MetadataFlag> flags_;
@@ -186,8 +189,11 @@ class StateDescriptor {
     m.Set(Metadata::Sparse);
     bool ok = true;
     for (int id : sparse_ids) {
-      ok = add_field(MakeVarLabel(base, id), m) && ok;
-      sparse_ids_[base].push_back(id);
+      if (add_field(MakeVarLabel(base, id), m)) {
+        sparse_ids_[base].push_back(id);
+      } else {
+        ok = false;  // the id is already in the pool
+      }
     }
     return ok;
   }

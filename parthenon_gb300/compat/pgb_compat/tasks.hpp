@@ -49,6 +49,7 @@ class TaskID {
   }
   bool operator==(const TaskID &o) const { return ids_ == o.ids_; }
   const std::set<int> &ids() const { return ids_; }
+  const std::set<int> &GetIDs() const { return ids_; }  // tasks.hpp TaskID::GetIDs
   bool empty() const { return ids_.empty(); }
 
  private:

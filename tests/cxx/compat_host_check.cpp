@@ -5,6 +5,7 @@
 // Test infrastructure.
 #include <cmath>
 #include <cstdio>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -144,6 +145,101 @@ int main(int argc, char *argv[]) {
     }
     LowStorageIntegrator rk4("rk4");
     CHECK(rk4.nstages == 5 && rk4.stage_name.size() == 6 && rk4.stage_name[4] == "4");
+  }
+  // ---- Params (tst/unit/test_unit_params.cpp): the errors of an immutable parameter,
+  // a mutable one through GetMutable and Update, missing keys, reset
+  {
+    auto throws = [](auto &&f) {
+      try {
+        f();
+      } catch (std::runtime_error &) {
+        return true;
+      }
+      return false;
+    };
+    Params p;
+    p.Add<double>("x", 1.5);
+    CHECK(p.Get<double>("x") == 1.5);
+    CHECK(throws([&] { p.Update<double>("x", 2.0); }));  // not mutable
+    CHECK(throws([&] { p.Add("x", 1.5); }));             // the key again
+    CHECK(throws([&] { p.Get<int>("x"); }));             // another type
+    CHECK(throws([&] { p.GetMutable<double>("x"); }));
+    p.Add<double>("m", 1.0, Params::Mutability::Mutable);
+    *p.GetMutable<double>("m") = 3.0;
+    const bool via_pointer = p.Get<double>("m") == 3.0;
+    p.Update<double>("m", 2.0);
+    CHECK(via_pointer && p.Get<double>("m") == 2.0);
+    CHECK(throws([&] { p.Update<int>("m", 2); }));  // wrong type
+    CHECK(throws([&] { p.Get<double>("none"); }) && throws([&] { p.Update<double>("none", 2.0); }));
+    CHECK(p.hasKey("x"));
+    p.reset();
+    CHECK(!p.hasKey("x") && throws([&] { p.Get<double>("x"); }));
+  }
+  // ---- Metadata and packages (tst/unit/test_metadata.cpp:110-160,
+  // test_state_descriptor.cpp:86-106,179-193): a default struct has no flag, Set sets one,
+  // equality by flags and shape, the package registry's errors, duplicates refused
+  {
+    const MetadataFlag all[] = {Metadata::Cell,        Metadata::Face,        Metadata::Independent,
+                                Metadata::Derived,     Metadata::FillGhost,   Metadata::WithFluxes,
+                                Metadata::OneCopy,     Metadata::Sparse,      Metadata::Conserved,
+                                Metadata::Intensive,   Metadata::Restart,     Metadata::GMGProlongate,
+                                Metadata::GMGRestrict, Metadata::ForceRemeshComm};
+    Metadata m0, m1;
+    m1.Set(Metadata::FillGhost);
+    bool none_set = true, only_fill = m1.IsSet(Metadata::FillGhost);
+    for (const auto &f : all) {
+      none_set = none_set && !m0.IsSet(f);
+      if (f != Metadata::FillGhost) only_fill = only_fill && !m1.IsSet(f);
+    }
+    CHECK(none_set && only_fill);
+    Metadata a({Metadata::Cell}), b({Metadata::Face});
+    b.Unset(Metadata::Face);
+    b.Set(Metadata::Cell);
+    Metadata c, d;
+    c.Set(Metadata::Cell);
+    c.Set(Metadata::Derived);
+    d.Set(Metadata::Derived);
+    d.Set(Metadata::Cell);
+    CHECK(a == b && c == d);
+    CHECK(Metadata({Metadata::Cell}) != Metadata({Metadata::Face}));
+    CHECK(Metadata({Metadata::Cell, Metadata::Derived}) != Metadata({Metadata::Face, Metadata::Derived}));
+    CHECK(Metadata({Metadata::Cell, Metadata::Derived}) !=
+          Metadata({Metadata::Cell, Metadata::Derived, Metadata::OneCopy}));
+    Packages_t packages;
+    packages.Add(std::make_shared<StateDescriptor>("package1"));
+    bool missing = false, twice = false;
+    try {
+      packages.Get("package2");
+    } catch (std::exception &) {
+      missing = true;
+    }
+    try {
+      packages.Add(std::make_shared<StateDescriptor>("package1"));
+    } catch (std::exception &) {
+      twice = true;
+    }
+    CHECK(packages.Get("package1")->label() == "package1" && missing && twice);
+    StateDescriptor pkg("p");
+    const Metadata md({Metadata::Cell, Metadata::Independent});
+    CHECK(pkg.AddField("dense", md) && !pkg.AddField("dense", md));
+    CHECK(pkg.AddSparsePool("sp", md, std::vector<int>{1, 2}) && !pkg.AddSparsePool("sp", md, std::vector<int>{2}));
+    CHECK(pkg.SparseIds("sp") == std::vector<int>({1, 2}));
+  }
+  // ---- task ids and task lifetimes (tst/unit/test_taskid.cpp, test_tasklist.cpp): an
+  // empty id, the union of two, and the list's task objects destroyed with the list
+  {
+    TaskID none, a(1), b(2);
+    const TaskID c = a | b;
+    CHECK(none.empty() && c.GetIDs().size() == 2);
+    std::weak_ptr<int> track;
+    {
+      auto obj = std::make_shared<int>(0);
+      track = obj;
+      TaskList tl;
+      tl.AddTask(TaskID{}, [obj] { return TaskStatus::complete; });
+      CHECK(!track.expired());
+    }
+    CHECK(track.expired());
   }
   // ---- task qualifiers, labels, member-function tasks, iterating sublists
   {
