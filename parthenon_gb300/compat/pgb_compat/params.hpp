@@ -8,8 +8,10 @@
 #pragma once
 
 #include <fstream>
+#include <iostream>
 #include <map>
 #include <memory>
+#include <set>
 #include <sstream>
 #include <string>
 #include <typeindex>
@@ -87,11 +89,19 @@ class ParameterInput {
     PARTHENON_REQUIRE_THROWS(f.good(), "cannot open input file " + path);
     LoadFromStream(f);
   }
+  // parameter_input.cpp LoadFromStream: a value continues on the next line after a
+  // trailing '&' (text after the '&' is an error); a line whose comment is the marker
+  // GetOrAdd* writes ("Default value added at run time") holds a code default, which
+  // CheckRequired does not accept
   void LoadFromStream(std::istream &is) {
     std::string line, block, pending;
     while (std::getline(is, line)) {
       const auto hash = line.find('#');
-      if (hash != std::string::npos) line = line.substr(0, hash);
+      bool is_default = false;
+      if (hash != std::string::npos) {
+        is_default = trim(line.substr(hash + 1)) == kDefaultMarker;
+        line = line.substr(0, hash);
+      }
       line = trim(line);
       if (line.empty()) continue;
       if (!pending.empty()) {  // continuation of the previous value
@@ -104,13 +114,16 @@ class ParameterInput {
         block = trim(line.substr(1, close - 1));
         continue;
       }
-      if (line.back() == '&') {
+      const auto amp = line.find('&');
+      if (amp != std::string::npos) {
+        PARTHENON_REQUIRE_THROWS(amp == line.size() - 1, "text after '&' in the input line " + line);
         pending = trim(line.substr(0, line.size() - 1));
         continue;
       }
       const auto eq = line.find('=');
       PARTHENON_REQUIRE_THROWS(eq != std::string::npos && !block.empty(), "malformed input line " + line);
       Set(block, trim(line.substr(0, eq)), trim(line.substr(eq + 1)));
+      if (is_default) defaults_.insert(block + "/" + trim(line.substr(0, eq)));
     }
   }
   // "block/key=value" overrides (ParthenonManager's command line)
@@ -137,30 +150,36 @@ class ParameterInput {
     return v == "true" || v == "1" || v == "yes" || v == "on";
   }
   std::string GetOrAddString(const std::string &b, const std::string &k, const std::string &d) {
-    if (!DoesParameterExist(b, k)) Set(b, k, d);
+    if (!DoesParameterExist(b, k)) SetDefault(b, k, d);
     return GetString(b, k);
   }
   double GetOrAddReal(const std::string &b, const std::string &k, double d) {
-    if (!DoesParameterExist(b, k)) Set(b, k, num(d));
+    if (!DoesParameterExist(b, k)) SetDefault(b, k, num(d));
     return GetReal(b, k);
   }
   int GetOrAddInteger(const std::string &b, const std::string &k, int d) {
-    if (!DoesParameterExist(b, k)) Set(b, k, std::to_string(d));
+    if (!DoesParameterExist(b, k)) SetDefault(b, k, std::to_string(d));
     return GetInteger(b, k);
   }
   bool GetOrAddBoolean(const std::string &b, const std::string &k, bool d) {
-    if (!DoesParameterExist(b, k)) Set(b, k, d ? "true" : "false");
+    if (!DoesParameterExist(b, k)) SetDefault(b, k, d ? "true" : "false");
     return GetBoolean(b, k);
   }
   void SetString(const std::string &b, const std::string &k, const std::string &v) { Set(b, k, v); }
   void SetReal(const std::string &b, const std::string &k, double v) { Set(b, k, num(v)); }
   void SetInteger(const std::string &b, const std::string &k, int v) { Set(b, k, std::to_string(v)); }
   void SetBoolean(const std::string &b, const std::string &k, bool v) { Set(b, k, v ? "true" : "false"); }
+  // parameter_input.cpp CheckRequired / CheckDesired: a code default does not count as
+  // provided; a missing desired field prints a warning on stdout
   void CheckRequired(const std::string &b, const std::string &k) const {
-    PARTHENON_REQUIRE_THROWS(DoesParameterExist(b, k), "Parameter " + b + "/" + k + " is required");
+    PARTHENON_REQUIRE_THROWS(DoesParameterExist(b, k) && !defaults_.count(b + "/" + k),
+                             "Parameter file missing required field <" + b + ">/" + k);
   }
   void CheckDesired(const std::string &b, const std::string &k) const {
-    if (!DoesParameterExist(b, k)) PARTHENON_WARN("Parameter " + b + "/" + k + " is desired but not set");
+    if (!DoesParameterExist(b, k) || defaults_.count(b + "/" + k))
+      std::cout << std::endl
+                << "### WARNING in CheckDesired:" << std::endl
+                << "Parameter file missing desired field <" << b << ">/" << k << std::endl;
   }
 
  private:
@@ -175,7 +194,15 @@ class ParameterInput {
     os << d;
     return os.str();
   }
-  void Set(const std::string &b, const std::string &k, const std::string &v) { blocks_[b][k] = v; }
+  static constexpr const char *kDefaultMarker = "Default value added at run time";
+  void Set(const std::string &b, const std::string &k, const std::string &v) {
+    blocks_[b][k] = v;
+    defaults_.erase(b + "/" + k);
+  }
+  void SetDefault(const std::string &b, const std::string &k, const std::string &v) {
+    Set(b, k, v);
+    defaults_.insert(b + "/" + k);
+  }
   std::string raw(const std::string &b, const std::string &k) const {
     auto it = blocks_.find(b);
     PARTHENON_REQUIRE_THROWS(it != blocks_.end() && it->second.count(k),
@@ -183,6 +210,7 @@ class ParameterInput {
     return it->second.at(k);
   }
   std::map<std::string, std::map<std::string, std::string>> blocks_;
+  std::set<std::string> defaults_;  // "block/key" of the values a code default set
 };
 
 }  // namespace parthenon

@@ -5,7 +5,9 @@
 // Test infrastructure.
 #include <cmath>
 #include <cstdio>
+#include <iostream>
 #include <memory>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -224,6 +226,56 @@ int main(int argc, char *argv[]) {
     CHECK(pkg.AddField("dense", md) && !pkg.AddField("dense", md));
     CHECK(pkg.AddSparsePool("sp", md, std::vector<int>{1, 2}) && !pkg.AddSparsePool("sp", md, std::vector<int>{2}));
     CHECK(pkg.SparseIds("sp") == std::vector<int>({1, 2}));
+  }
+  // ---- input decks (tst/unit/test_parameter_input.cpp:31-103): continuation lines,
+  // required and desired fields, a code default is not a provided field, text after '&'
+  {
+    const std::string deck =
+        "<block1>\nvar1 = 0   # comment\nvar2 = 1,  & # another comment\n       2\n<block2>\nvar3 = 3\n"
+        "# comment\nvar4 = 4\nvar_default = 5 # Default value added at run time\n";
+    ParameterInput in(deck);
+    bool ok = true;
+    try {
+      in.CheckRequired("block1", "var1");
+      in.CheckRequired("block2", "var4");
+      in.CheckRequired("block1", "var2");
+    } catch (std::exception &) {
+      ok = false;
+    }
+    auto required_throws = [&](const char *b, const char *k) {
+      try {
+        in.CheckRequired(b, k);
+      } catch (std::runtime_error &) {
+        return true;
+      }
+      return false;
+    };
+    CHECK(ok && required_throws("block2", "var9") && required_throws("block2", "var_default"));
+    std::ostringstream cap;
+    std::streambuf *old = std::cout.rdbuf(cap.rdbuf());
+    in.CheckDesired("block2", "var2");
+    in.CheckDesired("block3", "var4");
+    std::cout.rdbuf(old);
+    CHECK(cap.str() ==
+          "\n### WARNING in CheckDesired:\nParameter file missing desired field <block2>/var2\n"
+          "\n### WARNING in CheckDesired:\nParameter file missing desired field <block3>/var4\n");
+    bool bad = false;
+    try {
+      ParameterInput broken("<block1>\nvar2 = 1,  & 2.5 # another comment\n       2\n");
+    } catch (std::runtime_error &) {
+      bad = true;
+    }
+    CHECK(bad);
+    ParameterInput pin2;
+    pin2.GetOrAddInteger("b", "k", 3);
+    CHECK(required_throws("block2", "var_default"));
+    bool dflt = false;
+    try {
+      pin2.CheckRequired("b", "k");
+    } catch (std::runtime_error &) {
+      dflt = true;
+    }
+    CHECK(dflt);
   }
   // ---- task ids and task lifetimes (tst/unit/test_taskid.cpp, test_tasklist.cpp): an
   // empty id, the union of two, and the list's task objects destroyed with the list
