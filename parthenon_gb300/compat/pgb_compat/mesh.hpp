@@ -312,8 +312,8 @@ class HostArrayND {
   T &operator()(int m, int n, int k, int j, int i) const { return (*v_)[dims_.at(0, m, n, k, j, i)]; }
   T &operator()(int l, int m, int n, int k, int j, int i) const { return (*v_)[dims_.at(l, m, n, k, j, i)]; }
   int GetDim(int d) const { return d >= 1 && d <= 6 ? dims_.d[d - 1] : 1; }
-  int64_t size() const { return dims_.size(); }
-  T *data() const { return v_->data(); }
+  int64_t size() const { return v_ ? dims_.size() : 0; }
+  T *data() const { return v_ ? v_->data() : nullptr; }
 
  private:
   compat_detail::Dims6 dims_;
