@@ -132,6 +132,8 @@ class AMRDriver:
         if new is None:
             return False
         new.upload()
+        # the old scratch goes first; the stream orders its last uses before the reuse
+        self.rk.release_scratch()
         base = self.mesh.transfer(new, self.base, stream=self.stream)
         self.rk.rebind(new, base)
         self.nremesh += 1

@@ -83,6 +83,12 @@ class RK2Driver:
             self.derived = mesh.new_field(1) if self.cfg.physics == "burgers" else None
         nat.check(nat.lib().pgb_set_derived(self.mesh.handle, _ptr(self.derived)), "pgb_set_derived")
 
+    def release_scratch(self):
+        """Drops every buffer but the base field before a remesh, so that the new mesh's
+        arena is allocated beside the old base alone (the transfer reads only the base)."""
+        nat.check(nat.lib().pgb_set_derived(self.mesh.handle, None), "pgb_set_derived")
+        self.stage = self.dudt = self.flux = self.cbase = self.cstage = self.derived = None
+
     def rebind(self, mesh, base):
         """Continue on a new mesh (after a remesh) with `base` already on it: fresh
         scratch and coarse buffers, ghosts filled with prolongation (the post-remesh
