@@ -320,6 +320,9 @@ class MGSolver {
   int GetCurrentIterations() const { return iter_counter; }
   Real GetFinalResidual() const { return final_residual; }
   int GetFinalIterations() const { return final_iteration; }
+  // true once the V-cycle replays from a captured CUDA graph (no counterpart in the
+  // reference, whose V-cycle is a task list run each time)
+  bool VCycleCaptured() const { return vgraph_->exec != nullptr; }
 
   // ---- the steps (public: they launch kernels, as in the reference)
   void Setup(Mesh *pm) {
@@ -331,7 +334,7 @@ class MGSolver {
     iter_counter = 0;
     for (int it = 0; it < std::max(1, params_.max_iters); ++it) {
       iter_counter++;
-      VCycle(pm);
+      VCycleGraph(pm);
       // the leaf residual (mg_solver.hpp:136-144)
       compat_detail::exchange(md.get());
       mg_detail::run_now([&](TaskList &tl) { eqs_.template Ax<u, res_err>(tl, TaskID(0), md); });
@@ -349,6 +352,42 @@ class MGSolver {
     const int lmin = min_level(pm), lmax = max_level(pm);
     for (int level = lmax; level >= lmin; --level) Down(pm, level, lmin, lmax);
     for (int level = lmin; level <= lmax; ++level) Up(pm, level, lmin, lmax);
+  }
+  // One V-cycle as above, replayed from a CUDA graph: the first call runs it eagerly
+  // (its packs and device tables are built then), the second captures it on the layer's
+  // stream and launches the graph, later calls launch the graph. The V-cycle is kernels
+  // and library calls on that stream only (no host synchronisation), so the graph is the
+  // same work in the same order; if anything in it cannot be captured, the V-cycles stay
+  // eager.
+  void VCycleGraph(Mesh *pm) {
+    VGraph &vg = *vgraph_;
+    if (vg.failed || vg.calls++ == 0) {
+      VCycle(pm);
+      return;
+    }
+    const cudaStream_t st = compat_stream();
+    if (!vg.exec) {
+      cudaGraph_t g = nullptr;
+      bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        try {
+          VCycle(pm);
+        } catch (...) {
+          ok = false;
+        }
+        const cudaError_t e = cudaStreamEndCapture(st, &g);
+        ok = ok && e == cudaSuccess && g != nullptr && cudaGraphInstantiate(&vg.exec, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+      }
+      if (!ok) {
+        cudaGetLastError();  // a refused capture leaves no sticky error
+        vg.exec = nullptr;
+        vg.failed = true;
+        VCycle(pm);  // nothing of the captured attempt ran
+        return;
+      }
+    }
+    check_cuda(cudaGraphLaunch(vg.exec, st), "V-cycle graph");
   }
 
   // mg_solver.hpp:222-297, scalar diagonal: xnew <- w ratio(rhs - (Ax - D xold), D)
@@ -386,6 +425,17 @@ class MGSolver {
   Real final_residual = 0;
   int final_iteration = 0;
   std::string container_;
+
+  // the captured V-cycle, shared by copies of the solver (they work on the same fields)
+  struct VGraph {
+    cudaGraphExec_t exec = nullptr;
+    int calls = 0;
+    bool failed = false;
+    ~VGraph() {
+      if (exec) cudaGraphExecDestroy(exec);
+    }
+  };
+  std::shared_ptr<VGraph> vgraph_ = std::make_shared<VGraph>();
 
   KOKKOS_FORCEINLINE_FUNCTION static Real robust_small() { return 10 * std::numeric_limits<Real>::min(); }
   int max_level(Mesh *pm) const { return pm->GetGMGMaxLevel(); }
@@ -604,7 +654,7 @@ class BiCGSTABSolver {
     if (params_.precondition) {
       utils::CopyData<src_t, rhs>(md);
       utils::SetToZero<u>(md);
-      preconditioner.VCycle(pm);
+      preconditioner.VCycleGraph(pm);
     } else {
       utils::CopyData<src_t, u>(md);
     }

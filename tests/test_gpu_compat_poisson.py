@@ -76,8 +76,11 @@ def _run(app, tmp_path, n, b, ng, solver, alpha, iters, tol, relative, rhs, coef
         cmd += ["--coef", coef_file]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-3000:]
-    it, res, ms = open(prefix + "_info.txt").read().split()
+    it, res, ms, graph = open(prefix + "_info.txt").read().split()
     u = np.fromfile(prefix + "_u.bin").reshape(rhs.shape)
+    print(r.stdout.strip())
+    if solver == "MG":
+        assert graph == "1"  # the V-cycles after the first replay from a captured CUDA graph
     return u, int(it), float(res), float(ms)
 
 
@@ -136,4 +139,4 @@ def test_package_equation_c4_shape_solve(app, tmp_path):
     assert rms_o[-1] <= tol and (it == 1 or rms_o[-2] > tol)
     ref = _interior(om.u(), ng)
     assert np.array_equal(_interior(u, ng), ref)
-    print("compat MGSolver<u, rhs, Eq> C4 solve: %d V-cycles, %.1f ms" % (it, ms))
+    print("compat MGSolver<u, rhs, Eq> C4 solve: %d V-cycles, %.1f ms (warm)" % (it, ms))
