@@ -96,17 +96,19 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     const int os = wdf::line_offset(dfl::dexp_field(scale_d));
     const df scale = dfl::from_double(scale_d, os);
 
+    const double *__restrict__ u = a.u_in + c0 + (int64_t)comp * cs;
+    // scale of this line: the largest exponent among the values the march reads (read
+    // before the barrier wait below, which it does not depend on, so the two overlap)
+    int emax = 0;
+#pragma unroll 8
+    for (int q = -3; q <= n + 2; ++q) emax = max(emax, dfl::dexp_field(__ldg(u + (int64_t)q * step)));
+    const int off = wdf::line_offset(emax);
+
     if (producer) {
       if (it >= 2) bar_sync(3 + buf, nthreads);  // consumers released this buffer
     } else {
       bar_sync(1 + buf, nthreads);  // coefficients of this group are ready
     }
-
-    const double *__restrict__ u = a.u_in + c0 + (int64_t)comp * cs;
-    // scale of this line: the largest exponent among the values the march reads
-    int emax = 0;
-    for (int q = -3; q <= n + 2; ++q) emax = max(emax, dfl::dexp_field(__ldg(u + (int64_t)q * step)));
-    const int off = wdf::line_offset(emax);
     if (producer) coef_off[buf][lane] = off;
     // the normal velocity's scale (fluxes are in units 2^(ou + off), increments in
     // 2^(ou + off + os); a velocity flux's 1/2 is one more power of two)
@@ -119,6 +121,18 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     for (int p = -1; p <= n; ++p) {
       const double q4 = qn;
       if (p < n) qn = __ldg(u + (int64_t)(p + 3) * step);
+      // the update of cell p-1 at the end of this step reads its stored increment and
+      // its RK inputs: the loads are issued here, so the step's arithmetic covers their
+      // latency (one thread owns each cell of its line and component in this launch)
+      double pre_du = 0.0, pre_in = 0.0, pre_base = 0.0;
+      if (MODE != kStoreFlux && MODE != kStoreDu && p >= 1 && live) {
+        const int64_t e = c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step;
+        if (MODE == kAddDu || MODE == kFinishUpdate) pre_du = a.dudt[e];
+        if (MODE != kAddDu) {
+          pre_in = __ldg(a.u_in + e);
+          if (!(a.w_in == 1.0 && a.w_base == 0.0)) pre_base = __ldg(a.u_base + e);
+        }
+      }
       df ql, qr;
       if (!wdf::step(wl, q4, ql, qr)) {
         // outside the pairs' range: the reference expression in FP64 for this cell
@@ -170,13 +184,11 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           if (MODE == kStoreDu) {
             a.dudt[e] = du;
           } else if (MODE == kAddDu) {
-            a.dudt[e] += du;
+            a.dudt[e] = pre_du + du;
           } else {
-            const double tot = MODE == kFinishUpdate ? a.dudt[e] + du : du;
+            const double tot = MODE == kFinishUpdate ? pre_du + du : du;
             // stage 1 of RK2 averages with weights (1, 0): the average is u_in itself
-            const double avg = (a.w_in == 1.0 && a.w_base == 0.0)
-                                   ? __ldg(a.u_in + e)
-                                   : a.w_in * __ldg(a.u_in + e) + a.w_base * __ldg(a.u_base + e);
+            const double avg = (a.w_in == 1.0 && a.w_base == 0.0) ? pre_in : a.w_in * pre_in + a.w_base * pre_base;
             a.u_out[e] = avg + tot;
           }
         }
