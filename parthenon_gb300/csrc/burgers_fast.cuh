@@ -147,7 +147,8 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
         df F;
         const int fi = p * 32 + lane;
         if (producer) {
-          const df upl = lprev, upr = qr;
+          // the wave speeds compare the face values: normalised pairs
+          const df upl = dfl::norm(lprev), upr = dfl::norm(qr);
           df sl = dfl::dmin(upl, upr);
           if (sl.hi > 0.0f) sl = dfl::make(0.0f);
           df sr = dfl::dmax(upl, upr);
@@ -156,18 +157,22 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           // velocity line is below 2^-127 and the face's coefficients vanish
           const bool stagnant = sl.hi == 0.0f || sr.hi == 0.0f;
           const float flag = stagnant ? dfl::pow2f(off) : 0.0f;
-          df is = dfl::recip(dfl::add(dfl::subu(sr, sl), flag));  // sr >= 0 >= sl: no cancellation
+          // sr >= 0 >= sl: no cancellation, and the reciprocal's Newton step takes the
+          // unnormalised sum
+          df is = dfl::recip(dfl::addu(dfl::subu(sr, sl), flag));
           if (stagnant && off > 126) is = dfl::make(0.0f);
-          const df A = dfl::mul(sr, dfl::sub(upl, sl)), B = dfl::mul(sl, dfl::sub(sr, upr));
+          // A and B enter only products (here and in the consumers): unnormalised
+          const df A = dfl::mulu(sr, dfl::subu(upl, sl)), B = dfl::mulu(sl, dfl::subu(sr, upr));
           ca[fi] = make_float2(A.hi, A.lo);
           cb[fi] = make_float2(B.hi, B.lo);
           ci[fi] = make_float2(is.hi, is.lo);
-          F = dfl::mul(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr)), is);
+          F = dfl::mulu(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr)), is);
         } else {
           const float2 A = ca[fi], B = cb[fi], is = ci[fi];
           // A L + B R may cancel; the product then drops a lo*lo below 2^-46 of the terms
-          // that cancelled, as does the increment's product below
-          F = dfl::mul(dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr)), df{is.x, is.y});
+          // that cancelled, as does the increment's product below. F feeds only the
+          // flux difference and the FP64 conversion: it stays unnormalised
+          F = dfl::mulu(dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr)), df{is.x, is.y});
         }
         if (MODE == kStoreFlux) {
           // face p of direction D at the index of the cell on its right (multilevel path)

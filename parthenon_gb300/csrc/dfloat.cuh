@@ -241,6 +241,10 @@ PGB_DF int dexp_field(double x) { return (int)((d2u(x) >> 52) & 0x7ff); }
 // below 2^kMinExp of the scale); above 2^kMaxExp the pair saturates to +-FLT_MAX
 // (callers choose off so that this does not happen). hi takes the leading 24
 // significand bits, lo the next 29 rounded to 23: the pair holds x to a relative 2^-47.
+// NORM false leaves out the final renormalisation: hi then holds the leading 24 bits
+// truncated and lo the rest (|lo| <= ulp(hi), same sign as hi), an unnormalised pair
+// for sums, products and sign tests.
+template <bool NORM = true>
 PGB_DF df from_double(double x, int off = 0) {
   const uint64_t u = d2u(x);
   const uint32_t sign = (uint32_t)(u >> 32) & 0x80000000u;
@@ -257,6 +261,7 @@ PGB_DF df from_double(double x, int off = 0) {
   const float ri = fsub(u2f(0x4b000000u + r), 8388608.0f);
   const float sc = u2f((uint32_t)(e - 46 + 127) << 23);
   const float lo = fmul(ri, sc);
+  if (!NORM) return {hi, sign ? -lo : lo};
   return fast_two_sum(hi, sign ? -lo : lo);
 }
 // f * 2^-off as a double, exactly (zero and results below the double range give 0)

@@ -89,14 +89,15 @@ PGB_DF void prime(Line &w, double q0, double q1, double q2, double q3, int off) 
   w.t2b = t2_of(dfl::sub(w.e2, w.e1), w.eps_b);
 }
 
-// Face values of cell p (ql at its right face, qr at its left face, scaled) given
+// Face values of cell p (ql at its right face, qr at its left face, scaled, as
+// unnormalised pairs) given
 // q[p+2], then advance the window by one cell. Returns false when this cell must be
 // evaluated in FP64 instead (the window still advances).
 PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   using namespace dfl;
   const double e3d = dsub(q4, w.q3d);
-  const df e3 = from_double(e3d, w.off);
-  const df q4p = from_double(q4, w.off);
+  const df e3 = from_double<false>(e3d, w.off);
+  const df q4p = from_double<false>(q4, w.off);
   const df e0 = w.e0, e1 = w.e1, e2 = w.e2;
   // Sums and the products that only feed sums keep their pairs unnormalised
   // (dfloat.cuh addu/mulu/sqru); a pair that enters a sign test, a comparison or a
@@ -164,9 +165,11 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   df dq = b1.hi < 0.0f ? neg(mag) : mag;
   if (!same) dq = make(0.0f);
   // blend (recon.hpp:90-92) about q2: alpha_lin (XL - dq) = a6 (6 XL - 6 dq)
+  // the face values come back unnormalised: they feed flux products and sums (a
+  // caller that compares them normalises first; norm() does not change a pair's value)
   const df dq6 = mulu(dq, 6.0f);
-  ql = norm(addu(w.q2, addu(dq, mulu(a6, subu(XL6, dq6)))));
-  qr = norm(addu(w.q2, subu(mulu(a6, addu(XR6, dq6)), dq)));
+  ql = addu(w.q2, addu(dq, mulu(a6, subu(XL6, dq6))));
+  qr = addu(w.q2, subu(mulu(a6, addu(XR6, dq6)), dq));
   // advance
   w.q3d = q4;
   w.q2 = w.q3;
