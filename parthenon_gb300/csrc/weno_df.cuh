@@ -96,7 +96,9 @@ PGB_DF void prime(Line &w, double q0, double q1, double q2, double q3, int off) 
 PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   using namespace dfl;
   const double e3d = dsub(q4, w.q3d);
-  const df e3 = from_double<false>(e3d, w.off);
+  // e3 is compared (as e1, e2) in the MC limiter against normalised pairs, which needs
+  // it normalised; q4 enters sums only
+  const df e3 = from_double(e3d, w.off);
   const df q4p = from_double<false>(q4, w.off);
   const df e0 = w.e0, e1 = w.e1, e2 = w.e2;
   // Sums and the products that only feed sums keep their pairs unnormalised
@@ -106,9 +108,12 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   // b0, b2 and d*, the second difference of t2, B_k, the weighted sums and the blend's
   // differences): a product drops lo*lo, which is at most 2^-46 of the product when lo
   // is within a few ulp of hi, and after a cancellation (hi near zero, the value in lo)
-  // is below 2^-46 of the differences that cancelled. Face values stay within 2e-14 of
-  // the line's magnitude (the host test's bar is 3e-14); leaving the products of the B_k
-  // (E2, E3) unnormalised as well took that to 2.7e-14, so those stay normalised.
+  // is below 2^-46 of the differences that cancelled. The weight sums S_L, S_R (also
+  // under reciprocals, whose Newton step takes an unnormalised input), E2 and E3 stay
+  // unnormalised too. Face values stay within 1.8e-14 of the line's magnitude over the
+  // host test's random lines (its bar is 3e-14; 99.9% of faces within 1.2e-14); leaving
+  // B1 B2, the blending coefficient's last product and the sum under its reciprocal
+  // unnormalised as well took the worst face to 2.7-3.0e-14, so those stay normalised.
   // smoothness indicators (recon.hpp:54-64 in first differences)
   const df t2c = t2_of(subu(e3, e2), w.eps_b);
   const df b0 = subu(mulu(e1, 3.0f), e0);
@@ -136,8 +141,8 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   };
   const df l0 = weight(B0, kG0), l1 = weight(B1, kG1), l2 = weight(B2, kG2);
   const df r0 = weight(B2, kG0), r2 = weight(B0, kG2);
-  const df SL = add(addu(l0, l1), l2);
-  const df SR = add(addu(r0, l1), r2);
+  const df SL = addu(addu(l0, l1), l2);
+  const df SR = addu(addu(r0, l1), r2);
   const df isL = recip(SL), isR = recip(SR);
   // blending coefficients alpha_l = 3 E3/(E2 S_L) + eps, alpha_r likewise, and their
   // harmonic mean alpha_lin = 2 al ar / (al + ar): without the two eps terms this is
@@ -145,8 +150,8 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   // face value by about eps times the stencil's differences. a6 = alpha_lin / 6 (the
   // candidate polynomials below carry the 6)
   const df B12 = mul(B1, B2);
-  const df E2 = add(mulu(B0, add(B1, B2)), B12);
-  const df E3 = mul(B0, B12);
+  const df E2 = addu(mulu(B0, addu(B1, B2)), B12);
+  const df E3 = mulu(B0, B12);
   const df a6 = mul(E3, recip(mul(E2, add(SL, SR))));
   // 6 (P_k - q2) for the candidate polynomials of both faces (recon.hpp:45-47,69-85)
   const df d0 = subu(mulu(e1, 5.0f), scale(e0, 2.0f));
