@@ -158,8 +158,8 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           const bool stagnant = sl.hi == 0.0f || sr.hi == 0.0f;
           const float flag = stagnant ? dfl::pow2f(off) : 0.0f;
           // sr >= 0 >= sl: no cancellation, and the reciprocal's Newton step takes the
-          // unnormalised sum
-          df is = dfl::recip(dfl::addu(dfl::subu(sr, sl), flag));
+          // unnormalised sum; the reciprocal feeds only products
+          df is = dfl::recipu(dfl::addu(dfl::subu(sr, sl), flag));
           if (stagnant && off > 126) is = dfl::make(0.0f);
           // A and B enter only products (here and in the consumers): unnormalised
           const df A = dfl::mulu(sr, dfl::subu(upl, sl)), B = dfl::mulu(sl, dfl::subu(sr, upr));

@@ -218,6 +218,13 @@ PGB_DF df recip(df a) {
   const float res = ffma(-a.lo, r, ffma(-a.hi, r, 1.0f));  // 1 - a r
   return fast_two_sum(r, fmul(r, res));
 }
+// 1/a as above without the final renormalisation: r + r (1 - a r), whose second word is
+// already within about ulp(r) (for factors of products and terms of sums)
+PGB_DF df recipu(df a) {
+  const float r = frcp(a.hi);
+  const float res = ffma(-a.lo, r, ffma(-a.hi, r, 1.0f));
+  return {r, fmul(r, res)};
+}
 // a / b
 PGB_DF df div(df a, df b) { return mul(a, recip(b)); }
 

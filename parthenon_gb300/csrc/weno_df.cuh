@@ -102,18 +102,18 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df q4p = from_double<false>(q4, w.off);
   const df e0 = w.e0, e1 = w.e1, e2 = w.e2;
   // Sums and the products that only feed sums keep their pairs unnormalised
-  // (dfloat.cuh addu/mulu/sqru); a pair that enters a sign test, a comparison or a
-  // reciprocal is normalised first (after a cancellation a pair holds its value in lo).
-  // Several pairs also enter products unnormalised (the first-difference combinations
-  // b0, b2 and d*, the second difference of t2, B_k, the weighted sums and the blend's
-  // differences): a product drops lo*lo, which is at most 2^-46 of the product when lo
-  // is within a few ulp of hi, and after a cancellation (hi near zero, the value in lo)
-  // is below 2^-46 of the differences that cancelled. The weight sums S_L, S_R (also
-  // under reciprocals, whose Newton step takes an unnormalised input), E2 and E3 stay
-  // unnormalised too. Face values stay within 1.8e-14 of the line's magnitude over the
-  // host test's random lines (its bar is 3e-14; 99.9% of faces within 1.2e-14); leaving
-  // B1 B2, the blending coefficient's last product and the sum under its reciprocal
-  // unnormalised as well took the worst face to 2.7-3.0e-14, so those stay normalised.
+  // (dfloat.cuh addu/mulu/sqru/recipu); a pair that enters a sign test or a comparison
+  // is normalised first (after a cancellation a pair holds its value in lo). Products
+  // also take unnormalised factors (the first-difference combinations b0, b2 and d*,
+  // the second difference of t2, B_k, the weight sums, E2, E3, the reciprocals, the
+  // weighted sums and the blend's differences): a product drops lo*lo, which is at most
+  // 2^-46 of the product when lo is within a few ulp of hi, and after a cancellation
+  // (hi near zero, the value in lo) is below 2^-46 of the differences that cancelled; a
+  // reciprocal's Newton step takes an unnormalised argument the same way. Face values
+  // stay within 1.8e-14 of the line's magnitude over the host test's random lines (its
+  // bar is 3e-14; 99.9% of faces within 1.2e-14); leaving B1 B2, the blending
+  // coefficient's last product and the sum under its reciprocal unnormalised as well
+  // took the worst face to 2.7-3.0e-14, so those stay normalised.
   // smoothness indicators (recon.hpp:54-64 in first differences)
   const df t2c = t2_of(subu(e3, e2), w.eps_b);
   const df b0 = subu(mulu(e1, 3.0f), e0);
@@ -129,9 +129,9 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
     // B_k = 1 + tau / beta_k; a B_k above 2^40 (a zero indicator included) would take
     // the products below out of the float range
     fast = fminf(fminf(be0.hi, be1.hi), be2.hi) >= fmul(tau.hi, 0x1p-40f);
-    B0 = addu(mulu(tau, recip(be0)), 1.0f);
-    B1 = addu(mulu(tau, recip(be1)), 1.0f);
-    B2 = addu(mulu(tau, recip(be2)), 1.0f);
+    B0 = addu(mulu(tau, recipu(be0)), 1.0f);
+    B1 = addu(mulu(tau, recipu(be1)), 1.0f);
+    B2 = addu(mulu(tau, recipu(be2)), 1.0f);
   }
   // nonlinear weights g_k B_k + eps (unnormalised) and their sums: g_k B_k >= 0.1, whose
   // float ulp (2^-27) is far above eps (2e-15), so eps belongs to the low word alone
@@ -143,7 +143,7 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df r0 = weight(B2, kG0), r2 = weight(B0, kG2);
   const df SL = addu(addu(l0, l1), l2);
   const df SR = addu(addu(r0, l1), r2);
-  const df isL = recip(SL), isR = recip(SR);
+  const df isL = recipu(SL), isR = recipu(SR);
   // blending coefficients alpha_l = 3 E3/(E2 S_L) + eps, alpha_r likewise, and their
   // harmonic mean alpha_lin = 2 al ar / (al + ar): without the two eps terms this is
   // 6 E3 / (E2 (S_L + S_R)); leaving them out moves alpha_lin by about eps, i.e. the
@@ -152,7 +152,7 @@ PGB_DF bool step(Line &w, double q4, df &ql, df &qr) {
   const df B12 = mul(B1, B2);
   const df E2 = addu(mulu(B0, addu(B1, B2)), B12);
   const df E3 = mulu(B0, B12);
-  const df a6 = mul(E3, recip(mul(E2, add(SL, SR))));
+  const df a6 = mul(E3, recipu(mul(E2, add(SL, SR))));
   // 6 (P_k - q2) for the candidate polynomials of both faces (recon.hpp:45-47,69-85)
   const df d0 = subu(mulu(e1, 5.0f), scale(e0, 2.0f));
   const df d1 = addu(e1, scale(e2, 2.0f));
