@@ -114,6 +114,10 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     // 2^(ou + off + os); a velocity flux's 1/2 is one more power of two)
     const int ou = producer ? off : coef_off[buf][lane];
     const int of = ou + off + fhalf_exp, odu = ou + off + os + fhalf_exp;
+    // increments convert with the hardware conversions where 2^-odu and the results stay
+    // far inside the double range (every line of ordinary magnitude), else bit by bit
+    const bool hw_du = odu > -800 && odu < 800;
+    const double pow2_du = dfl::pow2d_neg(hw_du ? odu : 0);
     wdf::Line wl;
     wdf::prime(wl, __ldg(u - 3 * step), __ldg(u - 2 * step), __ldg(u - step), __ldg(u), off);
     double qn = __ldg(u + step);  // q[p+2] of the first cell p = -1
@@ -185,7 +189,8 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           // dudt holds the scaled increments of the directions done so far (FP64)
           const int64_t e = c0 + (int64_t)comp * cs + (int64_t)(p - 1) * step;
           // to_double adds the pair's two halves exactly, so the product may stay unnormalised
-          const double du = dfl::to_double(dfl::mulu(dfl::subu(F, fprev), scale), odu);
+          const df dpair = dfl::mulu(dfl::subu(F, fprev), scale);
+          const double du = hw_du ? dfl::to_double_pow2(dpair, pow2_du) : dfl::to_double(dpair, odu);
           if (MODE == kStoreDu) {
             a.dudt[e] = du;
           } else if (MODE == kAddDu) {

@@ -291,6 +291,18 @@ PGB_DF double to_double(df a, int off = 0) {
   return f2d(a.hi, off) + f2d(a.lo, off);
 #endif
 }
+// 2^-off as a double for to_double_pow2 (off in [-1022, 1022]; callers check)
+PGB_DF double pow2d_neg(int off) { return u2d((uint64_t)(1023 - off) << 52); }
+// a * 2^-off as a double with the hardware conversions: the two halves convert
+// exactly, their FP64 sum is exact (about 48 significant bits), and the product with
+// the power of two is exact while the result stays a normal double
+PGB_DF double to_double_pow2(df a, double pow2) {
+#if defined(__CUDA_ARCH__)
+  return __dmul_rn(__dadd_rn((double)a.hi, (double)a.lo), pow2);
+#else
+  return ((double)a.hi + (double)a.lo) * pow2;
+#endif
+}
 // 2^k as a float: 0 below the normal range, +inf above it
 PGB_DF float pow2f(int k) {
   const int ex = k + 127;
