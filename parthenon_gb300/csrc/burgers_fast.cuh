@@ -3,11 +3,11 @@
 // A CTA owns 32 lines of cells along direction D (fixed transverse indices) and all NC
 // components: warp v marches component v, lane l marches line l. The warp of the
 // normal velocity component (v == D) goes first: it reconstructs the normal velocity
-// and turns every face into the three HLL coefficients shared by all components
-//   A = sr (upl - sl), B = sl (sr - upr), is = 1/(sr - sl + [sl*sr == 0])
-// (the reference's sr upl L - sl upr R + sl sr (R - L) regrouped as A L + B R;
+// and turns every face into the two HLL coefficients shared by all components
+//   A' = sr (upl - sl) is, B' = sl (sr - upr) is, is = 1/(sr - sl + [sl*sr == 0])
+// (the reference's (sr upl L - sl upr R + sl sr (R - L)) is regrouped as A' L + B' R;
 // burgers_package.hpp:32-43, burgers_package.cpp:328-333), kept in shared memory; the
-// other warps then march their component, form F = (A L + B R) * is (times 1/2 for
+// other warps then march their component, form F = A' L + B' R (times 1/2 for
 // velocities) and emit flux differences. Per face the wave speeds and their reciprocal
 // are therefore computed once, not once per component.
 //
@@ -47,7 +47,7 @@ __device__ __forceinline__ void bar_arrive(int id, int count) {
 // overlaps the flux work of the previous group.
 template <int NC, int D, int MODE>
 __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t ngroups) {
-  extern __shared__ float2 coef_all[];  // [2][3][n+1][32] pairs: A, B, is
+  extern __shared__ float2 coef_all[];  // [2][2][n+1][32] pairs: A', B'
   __shared__ int coef_off[2][32];        // scale exponent of each line's normal velocity
   const Dims d = a.d;
   const int ng = d.ng;
@@ -71,8 +71,8 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
   int it = 0;
   for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x, ++it) {
     const int buf = it & 1;
-    float2 *ca = coef_all + (size_t)buf * 3 * nf * 32;
-    float2 *cb = ca + nf * 32, *ci = ca + 2 * nf * 32;
+    float2 *ca = coef_all + (size_t)buf * 2 * nf * 32;
+    float2 *cb = ca + nf * 32;
     const int64_t line = grp * 32 + lane;
     const bool live = line < nlines;
     const int64_t ln = live ? line : 0;
@@ -116,8 +116,9 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     const int of = ou + off + fhalf_exp, odu = ou + off + os + fhalf_exp;
     // increments convert with the hardware conversions where 2^-odu and the results stay
     // far inside the double range (every line of ordinary magnitude), else bit by bit
-    const bool hw_du = odu > -800 && odu < 800;
+    const bool hw_du = odu > -800 && odu < 800, hw_f = of > -800 && of < 800;
     const double pow2_du = dfl::pow2d_neg(hw_du ? odu : 0);
+    const double pow2_f = dfl::pow2d_neg(hw_f ? of : 0);
     wdf::Line wl;
     wdf::prime(wl, __ldg(u - 3 * step), __ldg(u - 2 * step), __ldg(u - step), __ldg(u), off);
     double qn = __ldg(u + step);  // q[p+2] of the first cell p = -1
@@ -165,23 +166,24 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           // unnormalised sum; the reciprocal feeds only products
           df is = dfl::recipu(dfl::addu(dfl::subu(sr, sl), flag));
           if (stagnant && off > 126) is = dfl::make(0.0f);
-          // A and B enter only products (here and in the consumers): unnormalised
-          const df A = dfl::mulu(sr, dfl::subu(upl, sl)), B = dfl::mulu(sl, dfl::subu(sr, upr));
+          // A' and B' carry the reciprocal and enter only products (here and in the
+          // consumers): unnormalised
+          const df A = dfl::mulu(dfl::mulu(sr, dfl::subu(upl, sl)), is);
+          const df B = dfl::mulu(dfl::mulu(sl, dfl::subu(sr, upr)), is);
           ca[fi] = make_float2(A.hi, A.lo);
           cb[fi] = make_float2(B.hi, B.lo);
-          ci[fi] = make_float2(is.hi, is.lo);
-          F = dfl::mulu(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr)), is);
+          F = dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr));
         } else {
-          const float2 A = ca[fi], B = cb[fi], is = ci[fi];
-          // A L + B R may cancel; the product then drops a lo*lo below 2^-46 of the terms
-          // that cancelled, as does the increment's product below. F feeds only the
-          // flux difference and the FP64 conversion: it stays unnormalised
-          F = dfl::mulu(dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr)), df{is.x, is.y});
+          const float2 A = ca[fi], B = cb[fi];
+          // A' L + B' R may cancel; the increment's product below then drops a lo*lo
+          // below 2^-46 of the terms that cancelled. F feeds only the flux difference and
+          // the FP64 conversion: it stays unnormalised
+          F = dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr));
         }
         if (MODE == kStoreFlux) {
           // face p of direction D at the index of the cell on its right (multilevel path)
           if (live)
-            a.flux[c0 + ((int64_t)b * 2 + D) * NC * cs + (int64_t)comp * cs + (int64_t)p * step] = dfl::to_double(F, of);
+            a.flux[c0 + ((int64_t)b * 2 + D) * NC * cs + (int64_t)comp * cs + (int64_t)p * step] = hw_f ? dfl::to_double_pow2(F, pow2_f) : dfl::to_double(F, of);
           lprev = ql;
           continue;
         }
@@ -237,8 +239,8 @@ int launch_burgers_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
     const int64_t ns = D == 2 ? d.nx[1] : d.nx[2];
     const int64_t lines = (int64_t)a.nblocks * nf * ns;
     const int64_t groups = (lines + 31) / 32;
-    const size_t smem = 2 * 3 * (size_t)(n + 1) * 32 * sizeof(float2);
-    // more than the default 48 KB of dynamic shared memory (n = 32: 50.7 KB) needs the
+    const size_t smem = 2 * 2 * (size_t)(n + 1) * 32 * sizeof(float2);
+    // more than the default 48 KB of dynamic shared memory (n = 32: 33.8 KB; n >= 48) needs the
     // opt-in attribute; a failure here stops the stage before any launch of it
     if (smem > 48 * 1024) {
       attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

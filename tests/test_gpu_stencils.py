@@ -81,8 +81,10 @@ CASES = {
     "smr-burgers-weno5": ((32,) * 3, (8,) * 3, 4, refined_cube(2, 1, 3), "burgers", "weno5", 5, 0.8, _burgers5),
     "smr-burgers-11": ((32,) * 3, (8,) * 3, 4, refined_cube(2, 0, 2), "burgers", "weno5", 11, 0.8, _burgers),
     # the uniform Burgers benchmark's block shape: 32^3 blocks, 4 ghosts, 11 components
-    # (the fast sweep's shared-memory line buffers exceed 48 KB at n = 32)
     "burgers-weno5-64-32cubed-blocks": ((64,) * 3, (32,) * 3, 4, None, "burgers", "weno5", 11, 0.8, _burgers),
+    # one 64^3 block (its own neighbour): the fast sweep's shared-memory coefficient
+    # buffers exceed the default 48 KB from n = 48 on and take the opt-in launch attribute
+    "single-block-64cubed-burgers": ((64,) * 3, (64,) * 3, 4, None, "burgers", "weno5", 5, 0.8, _burgers5),
     # the reference's own Burgers initial condition: exactly constant scalars with a
     # box of +10 (jumps next to constant stretches) and tanh fronts
     "burgers-reference-ic-32": ((32,) * 3, (8,) * 3, 4, None, "burgers", "weno5", 11, 0.8, _burgers_reference_ic),
