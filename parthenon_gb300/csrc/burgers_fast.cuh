@@ -9,7 +9,8 @@
 // burgers_package.hpp:32-43, burgers_package.cpp:328-333), kept in shared memory; the
 // other warps then march their component, form F = A' L + B' R (times 1/2 for
 // velocities) and emit flux differences. Per face the wave speeds and their reciprocal
-// are therefore computed once, not once per component.
+// are therefore computed once, not once per component. (With fewer than 8 components
+// the producer stores A, B and is unfolded and the consumers form (A L + B R) is.)
 //
 // Arithmetic: GB300 runs one FP64 lane operation per 64 FP32 ones, so the
 // reconstruction, the fluxes and the per-direction increments are evaluated in
@@ -47,7 +48,12 @@ __device__ __forceinline__ void bar_arrive(int id, int count) {
 // overlaps the flux work of the previous group.
 template <int NC, int D, int MODE>
 __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t ngroups) {
-  extern __shared__ float2 coef_all[];  // [2][2][n+1][32] pairs: A', B'
+  // With many components (NC >= 8) the producer folds the reciprocal into A and B and
+  // stores two coefficient arrays, which saves every consumer a product per face; with
+  // few components the producer's extra products outweigh that, and it stores A, B, is.
+  constexpr bool kFold = NC >= 8;
+  constexpr int kCoefArrays = kFold ? 2 : 3;
+  extern __shared__ float2 coef_all[];  // [2][kCoefArrays][n+1][32] pairs: A', B' (or A, B, is)
   __shared__ int coef_off[2][32];        // scale exponent of each line's normal velocity
   const Dims d = a.d;
   const int ng = d.ng;
@@ -71,8 +77,8 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
   int it = 0;
   for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x, ++it) {
     const int buf = it & 1;
-    float2 *ca = coef_all + (size_t)buf * 2 * nf * 32;
-    float2 *cb = ca + nf * 32;
+    float2 *ca = coef_all + (size_t)buf * kCoefArrays * nf * 32;
+    float2 *cb = ca + nf * 32, *ci = ca + 2 * nf * 32;
     const int64_t line = grp * 32 + lane;
     const bool live = line < nlines;
     const int64_t ln = live ? line : 0;
@@ -115,8 +121,12 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
     const int ou = producer ? off : coef_off[buf][lane];
     const int of = ou + off + fhalf_exp, odu = ou + off + os + fhalf_exp;
     // increments convert with the hardware conversions where 2^-odu and the results stay
-    // far inside the double range (every line of ordinary magnitude), else bit by bit
-    const bool hw_du = odu > -800 && odu < 800, hw_f = of > -800 && of < 800;
+    // far inside the double range (every line of ordinary magnitude), else bit by bit.
+    // The conversions run on the FP64 pipe with its latency: they pay where many warps
+    // hide it (NC >= 8 at 80 registers, 22 warps per SM); the few-component instances
+    // (over 100 registers, about 10 warps per SM) convert bit by bit
+    constexpr bool kHwConvert = NC >= 8;
+    const bool hw_du = kHwConvert && odu > -800 && odu < 800, hw_f = kHwConvert && of > -800 && of < 800;
     const double pow2_du = dfl::pow2d_neg(hw_du ? odu : 0);
     const double pow2_f = dfl::pow2d_neg(hw_f ? of : 0);
     wdf::Line wl;
@@ -166,19 +176,31 @@ __global__ void __launch_bounds__(32 * NC, 2) k_burgers_dir(StageArgs a, int64_t
           // unnormalised sum; the reciprocal feeds only products
           df is = dfl::recipu(dfl::addu(dfl::subu(sr, sl), flag));
           if (stagnant && off > 126) is = dfl::make(0.0f);
-          // A' and B' carry the reciprocal and enter only products (here and in the
-          // consumers): unnormalised
-          const df A = dfl::mulu(dfl::mulu(sr, dfl::subu(upl, sl)), is);
-          const df B = dfl::mulu(dfl::mulu(sl, dfl::subu(sr, upr)), is);
-          ca[fi] = make_float2(A.hi, A.lo);
-          cb[fi] = make_float2(B.hi, B.lo);
-          F = dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr));
+          // A' and B' (or A, B and is) enter only products, here and in the consumers:
+          // unnormalised
+          if constexpr (kFold) {
+            const df A = dfl::mulu(dfl::mulu(sr, dfl::subu(upl, sl)), is);
+            const df B = dfl::mulu(dfl::mulu(sl, dfl::subu(sr, upr)), is);
+            ca[fi] = make_float2(A.hi, A.lo);
+            cb[fi] = make_float2(B.hi, B.lo);
+            F = dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr));
+          } else {
+            const df A = dfl::mulu(sr, dfl::subu(upl, sl)), B = dfl::mulu(sl, dfl::subu(sr, upr));
+            ca[fi] = make_float2(A.hi, A.lo);
+            cb[fi] = make_float2(B.hi, B.lo);
+            ci[fi] = make_float2(is.hi, is.lo);
+            F = dfl::mulu(dfl::addu(dfl::mulu(A, upl), dfl::mulu(B, upr)), is);
+          }
         } else {
           const float2 A = ca[fi], B = cb[fi];
           // A' L + B' R may cancel; the increment's product below then drops a lo*lo
           // below 2^-46 of the terms that cancelled. F feeds only the flux difference and
           // the FP64 conversion: it stays unnormalised
           F = dfl::addu(dfl::mulu(df{A.x, A.y}, lprev), dfl::mulu(df{B.x, B.y}, qr));
+          if constexpr (!kFold) {
+            const float2 is = ci[fi];
+            F = dfl::mulu(F, df{is.x, is.y});
+          }
         }
         if (MODE == kStoreFlux) {
           // face p of direction D at the index of the cell on its right (multilevel path)
@@ -239,8 +261,9 @@ int launch_burgers_nc(const StageArgs &a, bool store_flux, cudaStream_t s) {
     const int64_t ns = D == 2 ? d.nx[1] : d.nx[2];
     const int64_t lines = (int64_t)a.nblocks * nf * ns;
     const int64_t groups = (lines + 31) / 32;
-    const size_t smem = 2 * 2 * (size_t)(n + 1) * 32 * sizeof(float2);
-    // more than the default 48 KB of dynamic shared memory (n = 32: 33.8 KB; n >= 48) needs the
+    const size_t smem = 2 * (NC >= 8 ? 2 : 3) * (size_t)(n + 1) * 32 * sizeof(float2);
+    // more than the default 48 KB of dynamic shared memory (11 components at n = 32:
+    // 33.8 KB; from n = 48 with 11 components, n = 32 with 5) needs the
     // opt-in attribute; a failure here stops the stage before any launch of it
     if (smem > 48 * 1024) {
       attr = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
