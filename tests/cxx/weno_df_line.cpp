@@ -40,11 +40,18 @@ void pgb_test_weno_ref(const double *q, int m, double *ql, double *qr) {
   for (int p = 2; p <= m - 3; ++p) wdf::weno5z_ref(q[p - 2], q[p - 1], q[p], q[p + 1], q[p + 2], ql[p], qr[p]);
 }
 
-// double -> pair -> double round trip
+// double -> pair -> double round trip (normalised pair, or the unnormalised conversion
+// when raw != 0)
 double pgb_test_df_roundtrip(double x) { return dfl::to_double(dfl::from_double(x)); }
+double pgb_test_df_roundtrip_raw(double x) { return dfl::to_double(dfl::from_double<false>(x)); }
+// the increment conversion through 2^-off (hardware conversions on the device)
+double pgb_test_df_pow2(double x, int off) {
+  return dfl::to_double_pow2(dfl::from_double(x, off), dfl::pow2d_neg(off));
+}
 
 // pair arithmetic on converted inputs, returned as doubles: op 0 add, 1 sub, 2 mul,
-// 3 div, 4 recip(a), 5 sqr(a)
+// 3 div, 4 recip(a), 5 sqr(a), 6 recipu(a) (unnormalised reciprocal), 7 mulu(a, recipu(b))
+// (a quotient through the unnormalised forms)
 double pgb_test_df_op(int op, double a, double b) {
   const dfl::df x = dfl::from_double(a), y = dfl::from_double(b);
   switch (op) {
@@ -54,6 +61,8 @@ double pgb_test_df_op(int op, double a, double b) {
     case 3: return dfl::to_double(dfl::div(x, y));
     case 4: return dfl::to_double(dfl::recip(x));
     case 5: return dfl::to_double(dfl::sqr(x));
+    case 6: return dfl::to_double(dfl::recipu(x));
+    case 7: return dfl::to_double(dfl::mulu(x, dfl::recipu(y)));
     default: return 0.0;
   }
 }

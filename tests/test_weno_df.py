@@ -36,6 +36,10 @@ def lib():
     L.pgb_test_df_roundtrip.restype = ctypes.c_double
     L.pgb_test_df_op.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
     L.pgb_test_df_op.restype = ctypes.c_double
+    L.pgb_test_df_roundtrip_raw.argtypes = [ctypes.c_double]
+    L.pgb_test_df_roundtrip_raw.restype = ctypes.c_double
+    L.pgb_test_df_pow2.argtypes = [ctypes.c_double, ctypes.c_int]
+    L.pgb_test_df_pow2.restype = ctypes.c_double
     return L
 
 
@@ -183,9 +187,23 @@ def test_pair_arithmetic(lib):
     assert np.max(np.abs(rt - xs) / np.abs(xs)) < 8e-15  # 2^-47
     a, b = rng.uniform(0.1, 10, 500), rng.uniform(0.1, 10, 500)
     for op, ref, tol in [(0, a + b, 3e-14), (2, a * b, 3e-14), (3, a / b, 5e-14), (4, 1 / a, 5e-14),
-                         (5, a * a, 3e-14)]:
+                         (5, a * a, 3e-14), (6, 1 / a, 5e-14), (7, a / b, 5e-14)]:
         got = np.array([lib.pgb_test_df_op(op, x, y) for x, y in zip(a, b)])
         assert np.max(np.abs(got - ref) / np.abs(ref)) < tol, op
     # differences: absolute accuracy relative to the operands
     got = np.array([lib.pgb_test_df_op(1, x, y) for x, y in zip(a, b)])
     assert np.max(np.abs(got - (a - b)) / (np.abs(a) + np.abs(b))) < 3e-14
+
+
+def test_unnormalised_conversions(lib):
+    """from_double<false> keeps the value of the normalised conversion (only the split
+    between the words differs); the increment conversion through 2^-off is exact."""
+    rng = np.random.default_rng(5)
+    xs = rng.standard_normal(2000) * 10.0 ** rng.uniform(-20, 20, 2000)
+    raw = np.array([lib.pgb_test_df_roundtrip_raw(x) for x in xs])
+    norm = np.array([lib.pgb_test_df_roundtrip(x) for x in xs])
+    assert np.array_equal(raw, norm)
+    for off in (-600, -40, 0, 3, 200, 700):
+        x = xs * 2.0 ** -off  # scaled to magnitudes near 2^-off, as a line's increments are
+        got = np.array([lib.pgb_test_df_pow2(v, off) for v in x])
+        assert np.max(np.abs(got - x) / np.abs(x)) < 8e-15, off
